@@ -1,0 +1,170 @@
+"""Python mirror of the reference solver interface, on top of the C ABI.
+
+Function names, argument meaning and error behaviour follow the reference's
+`ipt_cuda*` entry points (IPT_C_GPU/src/ipt_cuda.cu:262-308): a non-zero
+status raises IPTError carrying the status code.  Dense matrices are taken
+as 2-D numpy arrays (copied to column-major doubles); sparse input is CSC.
+Every call goes through libipt_gb300.so; nothing here computes on the CPU.
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+from ._lib import IPTBlockOptions, IPTBlockReport, IPTCudaResult, IPTError
+
+
+def _f64(a):
+    return np.asfortranarray(a, dtype=np.float64)
+
+
+def _i32(a):
+    return np.ascontiguousarray(a, dtype=np.int32)
+
+
+def _ptr(a):
+    return None if a is None else C.c_void_p(a.ctypes.data)
+
+
+def _take_result(res, status, what):
+    lib = _lib.load()
+    if status != _lib.IPT_CUDA_SUCCESS:
+        lib.ipt_cuda_free_result(C.byref(res))
+        raise IPTError(status, what)
+    n, k = res.n, res.k
+    vec = np.ctypeslib.as_array(res.vectors, shape=(n * k,)).reshape((n, k), order="F").copy()
+    val = np.ctypeslib.as_array(res.values, shape=(k,)).copy()
+    info = {
+        "iterations": res.iterations,
+        "basis_cols": res.basis_cols,
+        "matvecs": res.matvecs,
+        "fixed_point_residual": res.fixed_point_residual,
+        "solve_time_sec": res.solve_time_sec,
+        "iteration_time_sec": res.iteration_time_sec,
+        "rayleigh_ritz_time_sec": res.rayleigh_ritz_time_sec,
+        "davidson_time_sec": res.davidson_time_sec,
+        "davidson_residual_after": res.davidson_residual_after,
+    }
+    lib.ipt_cuda_free_result(C.byref(res))
+    return vec, val, info
+
+
+# ---- dense, host buffers --------------------------------------------------
+def ipt_cuda(matrix, k, iterations, initial_vectors=None):
+    """Fixed-iteration plain IPT (ipt_cuda / ipt_cuda_with_initial)."""
+    H = _f64(matrix)
+    n = H.shape[0]
+    X0 = None if initial_vectors is None else _f64(initial_vectors)
+    res = IPTCudaResult()
+    lib = _lib.load()
+    if X0 is None:
+        st = lib.ipt_cuda(_ptr(H), n, k, iterations, C.byref(res))
+    else:
+        st = lib.ipt_cuda_with_initial(_ptr(H), _ptr(X0), n, k, iterations, C.byref(res))
+    return _take_result(res, st, "ipt_cuda")
+
+
+def ipt_cuda_tol(matrix, k, tol, maxiter, initial_vectors=None):
+    """Tolerance-stopped plain IPT (ipt_cuda_tol / ipt_cuda_with_initial_tol)."""
+    H = _f64(matrix)
+    n = H.shape[0]
+    X0 = None if initial_vectors is None else _f64(initial_vectors)
+    res = IPTCudaResult()
+    lib = _lib.load()
+    if X0 is None:
+        st = lib.ipt_cuda_tol(_ptr(H), n, k, tol, maxiter, C.byref(res))
+    else:
+        st = lib.ipt_cuda_with_initial_tol(_ptr(H), _ptr(X0), n, k, tol, maxiter, C.byref(res))
+    return _take_result(res, st, "ipt_cuda_tol")
+
+
+# ---- sparse CSC, host buffers ------------------------------------------------
+def ipt_cuda_sparse_csc(col_ptr, row_ind, values, n, k, iterations, initial_vectors=None):
+    cp, ri, va = _i32(col_ptr), _i32(row_ind), np.ascontiguousarray(values, dtype=np.float64)
+    res = IPTCudaResult()
+    lib = _lib.load()
+    if initial_vectors is None:
+        st = lib.ipt_cuda_sparse_csc(_ptr(cp), _ptr(ri), _ptr(va), n, k, len(ri), iterations,
+                                     C.byref(res))
+    else:
+        X0 = _f64(initial_vectors)
+        st = lib.ipt_cuda_sparse_csc_with_initial(_ptr(cp), _ptr(ri), _ptr(va), _ptr(X0), n, k,
+                                                  len(ri), iterations, C.byref(res))
+    return _take_result(res, st, "ipt_cuda_sparse_csc")
+
+
+def ipt_cuda_sparse_csc_tol(col_ptr, row_ind, values, n, k, tol, maxiter, initial_vectors=None):
+    cp, ri, va = _i32(col_ptr), _i32(row_ind), np.ascontiguousarray(values, dtype=np.float64)
+    res = IPTCudaResult()
+    lib = _lib.load()
+    if initial_vectors is None:
+        st = lib.ipt_cuda_sparse_csc_tol(_ptr(cp), _ptr(ri), _ptr(va), n, k, len(ri), tol,
+                                         maxiter, C.byref(res))
+    else:
+        X0 = _f64(initial_vectors)
+        st = lib.ipt_cuda_sparse_csc_with_initial_tol(_ptr(cp), _ptr(ri), _ptr(va), _ptr(X0), n,
+                                                      k, len(ri), tol, maxiter, C.byref(res))
+    return _take_result(res, st, "ipt_cuda_sparse_csc_tol")
+
+
+# ---- block solver (include/ipt_block.h) ----------------------------------------
+PRECISIONS = {"fp64": _lib.IPT_BLOCK_FP64, "fp16": _lib.IPT_BLOCK_FP16,
+              "bf16": _lib.IPT_BLOCK_BF16, "tf32": _lib.IPT_BLOCK_TF32}
+
+
+def block_options(precision="fp64", stream=None, **kw):
+    opt = IPTBlockOptions()
+    _lib.load().ipt_block_default_options(C.byref(opt))
+    opt.ipt_precision = PRECISIONS[precision] if isinstance(precision, str) else int(precision)
+    if stream is not None:
+        opt.stream = C.c_void_p(int(stream))
+    for key, val in kw.items():
+        if not hasattr(opt, key):
+            raise TypeError("unknown block option %r" % key)
+        if key == "mlp_params":
+            val = C.c_void_p(int(val)) if val is not None else None
+        setattr(opt, key, val)
+    return opt
+
+
+def block_solve_dense(matrix, k, precision="fp64", **kw):
+    """k lowest eigenpairs of a dense symmetric matrix held in host memory."""
+    H = _f64(matrix)
+    n = H.shape[0]
+    opt = block_options(precision, **kw)
+    vec = np.zeros((n, k), dtype=np.float64, order="F")
+    val = np.zeros(k, dtype=np.float64)
+    rep = IPTBlockReport()
+    st = _lib.load().ipt_block_solve_dense(_ptr(H), n, k, C.byref(opt), _ptr(vec), _ptr(val),
+                                           C.byref(rep))
+    if st != _lib.IPT_CUDA_SUCCESS:
+        raise IPTError(st, "ipt_block_solve_dense")
+    return vec, val, rep.as_dict()
+
+
+def block_solve_dense_device(d_matrix_ptr, n, k, d_vectors_ptr, d_values_ptr, precision="fp64",
+                             **kw):
+    """Device-pointer variant; pointers are integers (e.g. torch data_ptr())."""
+    opt = block_options(precision, **kw)
+    rep = IPTBlockReport()
+    st = _lib.load().ipt_block_solve_dense_device(C.c_void_p(d_matrix_ptr), n, k, C.byref(opt),
+                                                  C.c_void_p(d_vectors_ptr),
+                                                  C.c_void_p(d_values_ptr), C.byref(rep))
+    if st != _lib.IPT_CUDA_SUCCESS:
+        raise IPTError(st, "ipt_block_solve_dense_device")
+    return rep.as_dict()
+
+
+def block_solve_csr(row_ptr, col_ind, values, n, k, precision="fp64", **kw):
+    """k lowest eigenpairs of a symmetric CSR matrix held in host memory."""
+    rp, ci = _i32(row_ptr), _i32(col_ind)
+    va = np.ascontiguousarray(values, dtype=np.float64)
+    opt = block_options(precision, **kw)
+    vec = np.zeros((n, k), dtype=np.float64, order="F")
+    val = np.zeros(k, dtype=np.float64)
+    rep = IPTBlockReport()
+    st = _lib.load().ipt_block_solve_csr(_ptr(rp), _ptr(ci), _ptr(va), n, len(ci), k,
+                                         C.byref(opt), _ptr(vec), _ptr(val), C.byref(rep))
+    if st != _lib.IPT_CUDA_SUCCESS:
+        raise IPTError(st, "ipt_block_solve_csr")
+    return vec, val, rep.as_dict()

@@ -1,0 +1,654 @@
+// block_api.cu - FP64 operators/stages and the exported block-solver API
+// (include/ipt_block.h), plus the reference's IPT_BLOCK_CLUSTER sparse path.
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <algorithm>
+#include <chrono>
+#include <climits>
+#include <memory>
+#include <numeric>
+#include <vector>
+
+#include "block_solver.h"
+#include "common.cuh"
+#include "ipt_plain.h"
+#include "prep.h"
+#include "reduce.cuh"
+
+#define IPT_API extern "C" __attribute__((visibility("default")))
+
+namespace iptgb {
+
+// ---------------------------------------------------------------------------
+// FP64 accurate products
+// ---------------------------------------------------------------------------
+struct DenseApply final : Fp64Apply {
+    const double *H = nullptr;
+    int n = 0;
+    int sms = 148;
+    cudaStream_t s = nullptr;
+    DeviceBuffer<double> P;
+    int apply(const double *V, int c, double *AV) override
+    {
+        const int S = dense64_split_for(n, c, sms);
+        const size_t need = (size_t)S * (size_t)n * (size_t)c;
+        if (P.count < need) {
+            IPTGB_CHECK(P.alloc(need, s));
+        }
+        IPTGB_CHECK(launch_dense64_partial(H, n, n, V, n, c, P.ptr, S, s));
+        return launch_sum_partials(P.ptr, S, (size_t)n * c, AV, s);
+    }
+};
+
+struct CsrApply final : Fp64Apply {
+    const int *row_ptr = nullptr;
+    const int *col_ind = nullptr;
+    const double *vals = nullptr;
+    int n = 0;
+    cudaStream_t s = nullptr;
+    int apply(const double *V, int c, double *AV) override
+    {
+        return launch_csr64_spmm(row_ptr, col_ind, vals, n, V, c, AV, s);
+    }
+};
+
+// ---------------------------------------------------------------------------
+// FP64 IPT stage on a plain operator.  Stops at ipt_tol, at maxiter, or when
+// the fixed-point residual stops decreasing (the block is then handed to
+// Rayleigh-Ritz as it is; a non-finite step is rolled back).
+// ---------------------------------------------------------------------------
+struct Fp64Stage final : IptStage {
+    std::unique_ptr<Fp64Operator> op;
+    DenseFp64Operator *dense = nullptr;
+    CsrFp64Operator *csr = nullptr;
+    const double *d = nullptr;
+    int n = 0;
+    int sms = 148;
+    cudaStream_t s = nullptr;
+    DeviceBuffer<double> P, Y, Xb;
+
+    int run(int p, int maxiter, double tol, int check_every, double *X, int *iterations,
+            double *fpres_out, long long *matvecs) override
+    {
+        const size_t elems = (size_t)n * (size_t)p;
+        if (dense != nullptr) {
+            dense->k = p;
+            dense->S = dense64_split_for(n, p, sms);
+            IPTGB_CHECK(P.alloc((size_t)dense->S * elems, s));
+            dense->P = P.ptr;
+        } else {
+            csr->k = p;
+            IPTGB_CHECK(Y.alloc(elems, s));
+            csr->Y = Y.ptr;
+        }
+        IPTGB_CHECK(Xb.alloc(elems, s));
+        SolveScratch scratch;
+        IPTGB_CHECK(scratch.init(elems, s));
+        IPTGB_CHECK(launch_set_identity(X, n, p, s));
+        double *x = X;
+        double *y = Xb.ptr;
+        double best = INFINITY;
+        int worse = 0;
+        int done = 0;
+        double fpres = NAN;
+        int status = IPT_CUDA_SUCCESS;
+        for (int it = 0; it < maxiter; ++it) {
+            const int want = ((it + 1) % check_every == 0) || it + 1 == maxiter;
+            status = op->step(x, y, d, want, &scratch.ns);
+            if (status != IPT_CUDA_SUCCESS) break;
+            done = it + 1;
+            if (want) {
+                if (cudaMemcpyAsync(scratch.host_norms, scratch.ns.norms, 2 * sizeof(double),
+                                    cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+                    cudaStreamSynchronize(s) != cudaSuccess) {
+                    status = IPT_CUDA_CUDA_ERROR;
+                    break;
+                }
+                const double r = scratch.host_norms[0] / scratch.host_norms[1];
+                if (!isfinite(r)) {
+                    break;  // keep x (the last finite block)
+                }
+                fpres = r;
+                std::swap(x, y);
+                if (r <= tol) break;
+                if (r < best) {
+                    best = r;
+                    worse = 0;
+                } else if (++worse >= 3) {
+                    break;
+                }
+            } else {
+                std::swap(x, y);
+            }
+        }
+        scratch.release(s);
+        if (status != IPT_CUDA_SUCCESS) return status;
+        if (x != X) {
+            IPTGB_CUDA(cudaMemcpyAsync(X, x, elems * sizeof(double), cudaMemcpyDeviceToDevice, s));
+        }
+        *iterations = done;
+        *fpres_out = fpres;
+        *matvecs = (long long)done * p;
+        return IPT_CUDA_SUCCESS;
+    }
+};
+
+IptStage *make_fp64_dense_stage(const double *dH, int n, const double *d, cudaStream_t stream)
+{
+    auto *st = new Fp64Stage();
+    auto *op = new DenseFp64Operator();
+    op->H = dH;
+    op->ldh = n;
+    op->n = n;
+    op->stream = stream;
+    st->op.reset(op);
+    st->dense = op;
+    st->d = d;
+    st->n = n;
+    st->sms = device_sm_count();
+    st->s = stream;
+    return st;
+}
+
+IptStage *make_fp64_csr_stage(const int *row_ptr, const int *col_ind, const double *vals, int n,
+                              const double *d, cudaStream_t stream)
+{
+    auto *st = new Fp64Stage();
+    auto *op = new CsrFp64Operator();
+    op->row_ptr = row_ptr;
+    op->col_ind = col_ind;
+    op->vals = vals;
+    op->n = n;
+    op->stream = stream;
+    st->op.reset(op);
+    st->csr = op;
+    st->d = d;
+    st->n = n;
+    st->sms = device_sm_count();
+    st->s = stream;
+    return st;
+}
+
+LearnedCorrection *make_learned_correction(const float *params, cudaStream_t stream);
+
+// ---------------------------------------------------------------------------
+// Row sums of |H| (dense col-major: thread per row, coalesced over columns).
+// ---------------------------------------------------------------------------
+__global__ void dense_row_abs_sum_kernel(const double *__restrict__ H, int n, double *rs)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double s = 0.0;
+    for (int l = 0; l < n; ++l) {
+        s += fabs(H[(size_t)i + (size_t)l * n]);
+    }
+    rs[i] = s;
+}
+
+__global__ void csr_row_abs_sum_kernel(const int *row_ptr, const double *vals, int n, double *rs)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double s = 0.0;
+    for (int p = row_ptr[i]; p < row_ptr[i + 1]; ++p) {
+        s += fabs(vals[p]);
+    }
+    rs[i] = s;
+}
+
+// Dense symmetric permutation: out[i, j] = H[perm[i], perm[j]].
+__global__ void dense_permute_kernel(const double *__restrict__ H, const int *__restrict__ perm,
+                                     int n, double *__restrict__ out)
+{
+    const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= (size_t)n * n) return;
+    const int i = (int)(e % (size_t)n);
+    const int j = (int)(e / (size_t)n);
+    out[e] = H[(size_t)perm[i] + (size_t)perm[j] * n];
+}
+
+// out[perm[i], c] = in[i, c].
+__global__ void unpermute_rows_kernel(const double *__restrict__ in, const int *__restrict__ perm,
+                                      int n, int k, double *__restrict__ out)
+{
+    const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= (size_t)n * k) return;
+    const int i = (int)(e % (size_t)n);
+    const int c = (int)(e / (size_t)n);
+    out[(size_t)perm[i] + (size_t)c * n] = in[e];
+}
+
+namespace {
+
+int max_of_device(const double *v, int n, cudaStream_t s, double *out)
+{
+    std::vector<double> h((size_t)n);
+    IPTGB_CUDA(cudaMemcpyAsync(h.data(), v, (size_t)n * sizeof(double), cudaMemcpyDeviceToHost, s));
+    IPTGB_CUDA(cudaStreamSynchronize(s));
+    double m = 0.0;
+    for (double x : h) m = std::max(m, x);
+    *out = m;
+    return IPT_CUDA_SUCCESS;
+}
+
+bool options_valid(const IPTBlockOptions *o)
+{
+    return o->ipt_precision >= IPT_BLOCK_FP64 && o->ipt_precision <= IPT_BLOCK_TF32 &&
+           o->ipt_maxiter >= 0 && o->davidson_maxsteps >= 0 &&
+           (o->preconditioner == IPT_BLOCK_PRECOND_DIAGONAL ||
+            (o->preconditioner == IPT_BLOCK_PRECOND_MLP && o->mlp_params != nullptr));
+}
+
+}  // namespace
+
+int dense_block_device(const double *dH_in, int n, int k, const IPTBlockOptions *options,
+                       double *d_vectors, double *d_values, IPTBlockReport *report)
+{
+    IPTBlockOptions opt;
+    if (options != nullptr) {
+        opt = *options;
+    } else {
+        fill_default_options(&opt);
+    }
+    IPTBlockReport local;
+    if (report == nullptr) report = &local;
+    memset(report, 0, sizeof(*report));
+    if (dH_in == nullptr || d_vectors == nullptr || d_values == nullptr || n <= 0 || k <= 0 ||
+        k > n || !options_valid(&opt)) {
+        return IPT_CUDA_INVALID_ARGUMENT;
+    }
+    cudaStream_t s = (cudaStream_t)opt.stream;
+    DeviceBuffer<double> d, rs, Hp, Xtmp;
+    DeviceBuffer<int> dperm;
+    IPTGB_CHECK(d.alloc((size_t)n, s));
+    IPTGB_CHECK(launch_extract_diagonal(dH_in, n, n, d.ptr, s));
+    // ascending diagonal order; permute H when it is not already sorted
+    std::vector<double> hd((size_t)n);
+    IPTGB_CUDA(cudaMemcpyAsync(hd.data(), d.ptr, (size_t)n * sizeof(double),
+                               cudaMemcpyDeviceToHost, s));
+    IPTGB_CUDA(cudaStreamSynchronize(s));
+    std::vector<int> perm((size_t)n);
+    std::iota(perm.begin(), perm.end(), 0);
+    std::stable_sort(perm.begin(), perm.end(),
+                     [&hd](int a, int b) { return hd[(size_t)a] < hd[(size_t)b]; });
+    bool permuted = false;
+    for (int i = 0; i < n; ++i) {
+        if (perm[(size_t)i] != i) {
+            permuted = true;
+            break;
+        }
+    }
+    const double *dH = dH_in;
+    if (permuted) {
+        IPTGB_CHECK(Hp.alloc((size_t)n * n, s));
+        IPTGB_CHECK(dperm.alloc((size_t)n, s));
+        IPTGB_CUDA(cudaMemcpyAsync(dperm.ptr, perm.data(), (size_t)n * sizeof(int),
+                                   cudaMemcpyHostToDevice, s));
+        dense_permute_kernel<<<blocks_for((size_t)n * n), kThreads, 0, s>>>(dH_in, dperm.ptr, n,
+                                                                           Hp.ptr);
+        IPTGB_LAUNCH();
+        dH = Hp.ptr;
+        IPTGB_CHECK(launch_extract_diagonal(dH, n, n, d.ptr, s));
+        IPTGB_CHECK(Xtmp.alloc((size_t)n * k, s));
+    }
+    IPTGB_CHECK(rs.alloc((size_t)n, s));
+    dense_row_abs_sum_kernel<<<blocks_for(n), kThreads, 0, s>>>(dH, n, rs.ptr);
+    IPTGB_LAUNCH();
+    double hnorm = 0.0;
+    IPTGB_CHECK(max_of_device(rs.ptr, n, s, &hnorm));
+
+    DenseApply apply;
+    apply.H = dH;
+    apply.n = n;
+    apply.sms = device_sm_count();
+    apply.s = s;
+    std::unique_ptr<IptStage> stage;
+    int st = IPT_CUDA_SUCCESS;
+    if (opt.ipt_precision == IPT_BLOCK_FP64) {
+        stage.reset(make_fp64_dense_stage(dH, n, d.ptr, s));
+    } else {
+        stage.reset(make_lowp_dense_stage(dH, n, d.ptr, opt.ipt_precision, s, &st));
+        if (stage == nullptr) {
+            return st != IPT_CUDA_SUCCESS ? st : IPT_CUDA_INVALID_ARGUMENT;
+        }
+    }
+    std::unique_ptr<LearnedCorrection> learned;
+    if (opt.preconditioner == IPT_BLOCK_PRECOND_MLP) {
+        learned.reset(make_learned_correction(opt.mlp_params, s));
+    }
+    BlockSolveInput in;
+    in.apply = &apply;
+    in.ipt = stage.get();
+    in.learned = learned.get();
+    in.d = d.ptr;
+    in.n = n;
+    in.k = k;
+    in.hnorm = hnorm;
+    in.opt = opt;
+    in.lowp = opt.ipt_precision != IPT_BLOCK_FP64;
+    double *xout = permuted ? Xtmp.ptr : d_vectors;
+    IPTGB_CHECK(block_solve(in, xout, d_values, report, s));
+    if (permuted) {
+        unpermute_rows_kernel<<<blocks_for((size_t)n * k), kThreads, 0, s>>>(Xtmp.ptr, dperm.ptr,
+                                                                              n, k, d_vectors);
+        IPTGB_LAUNCH();
+    }
+    IPTGB_CUDA(cudaStreamSynchronize(s));
+    return IPT_CUDA_SUCCESS;
+}
+
+int csr_block_device(const int *row_ptr, const int *col_ind, const double *vals, int n, int nnz,
+                     int k, const IPTBlockOptions *options, const double *d_diag_sorted,
+                     double *d_vectors, double *d_values, IPTBlockReport *report)
+{
+    IPTBlockOptions opt;
+    if (options != nullptr) {
+        opt = *options;
+    } else {
+        fill_default_options(&opt);
+    }
+    IPTBlockReport local;
+    if (report == nullptr) report = &local;
+    memset(report, 0, sizeof(*report));
+    if (row_ptr == nullptr || (nnz > 0 && (col_ind == nullptr || vals == nullptr)) ||
+        d_vectors == nullptr || d_values == nullptr || n <= 0 || k <= 0 || k > n || nnz < 0 ||
+        !options_valid(&opt) || opt.ipt_precision != IPT_BLOCK_FP64) {
+        return IPT_CUDA_INVALID_ARGUMENT;
+    }
+    cudaStream_t s = (cudaStream_t)opt.stream;
+    DeviceBuffer<double> d, rs;
+    const double *dd = d_diag_sorted;
+    if (dd == nullptr) {
+        IPTGB_CHECK(d.alloc((size_t)n, s));
+        IPTGB_CHECK(launch_csr64_diagonal(row_ptr, col_ind, vals, n, d.ptr, s));
+        dd = d.ptr;
+    }
+    IPTGB_CHECK(rs.alloc((size_t)n, s));
+    csr_row_abs_sum_kernel<<<blocks_for(n), kThreads, 0, s>>>(row_ptr, vals, n, rs.ptr);
+    IPTGB_LAUNCH();
+    double hnorm = 0.0;
+    IPTGB_CHECK(max_of_device(rs.ptr, n, s, &hnorm));
+    CsrApply apply;
+    apply.row_ptr = row_ptr;
+    apply.col_ind = col_ind;
+    apply.vals = vals;
+    apply.n = n;
+    apply.s = s;
+    std::unique_ptr<IptStage> stage(make_fp64_csr_stage(row_ptr, col_ind, vals, n, dd, s));
+    std::unique_ptr<LearnedCorrection> learned;
+    if (opt.preconditioner == IPT_BLOCK_PRECOND_MLP) {
+        learned.reset(make_learned_correction(opt.mlp_params, s));
+    }
+    BlockSolveInput in;
+    in.apply = &apply;
+    in.ipt = stage.get();
+    in.learned = learned.get();
+    in.d = dd;
+    in.n = n;
+    in.k = k;
+    in.hnorm = hnorm;
+    in.opt = opt;
+    IPTGB_CHECK(block_solve(in, d_vectors, d_values, report, s));
+    IPTGB_CUDA(cudaStreamSynchronize(s));
+    return IPT_CUDA_SUCCESS;
+}
+
+}  // namespace iptgb
+
+using namespace iptgb;
+
+IPT_API void ipt_block_default_options(IPTBlockOptions *options)
+{
+    if (options != nullptr) {
+        fill_default_options(options);
+    }
+}
+
+IPT_API int ipt_block_solve_dense_device(const double *d_matrix_col_major, int n, int k,
+                                         const IPTBlockOptions *options, double *d_vectors,
+                                         double *d_values, IPTBlockReport *report)
+{
+    return dense_block_device(d_matrix_col_major, n, k, options, d_vectors, d_values, report);
+}
+
+IPT_API int ipt_block_solve_dense(const double *matrix_col_major, int n, int k,
+                                  const IPTBlockOptions *options, double *vectors, double *values,
+                                  IPTBlockReport *report)
+{
+    if (matrix_col_major == nullptr || vectors == nullptr || values == nullptr || n <= 0 ||
+        k <= 0 || k > n) {
+        return IPT_CUDA_INVALID_ARGUMENT;
+    }
+    IPTBlockOptions opt;
+    if (options != nullptr) {
+        opt = *options;
+    } else {
+        fill_default_options(&opt);
+    }
+    cudaStream_t s = (cudaStream_t)opt.stream;
+    const size_t mat = (size_t)n * n;
+    DeviceBuffer<double> dH, dX, dv;
+    IPTGB_CHECK(dH.alloc(mat, s));
+    IPTGB_CHECK(dX.alloc((size_t)n * k, s));
+    IPTGB_CHECK(dv.alloc((size_t)k, s));
+    IPTGB_CUDA(cudaMemcpyAsync(dH.ptr, matrix_col_major, mat * sizeof(double),
+                               cudaMemcpyHostToDevice, s));
+    IPTGB_CHECK(dense_block_device(dH.ptr, n, k, &opt, dX.ptr, dv.ptr, report));
+    IPTGB_CUDA(cudaMemcpyAsync(vectors, dX.ptr, (size_t)n * k * sizeof(double),
+                               cudaMemcpyDeviceToHost, s));
+    IPTGB_CUDA(cudaMemcpyAsync(values, dv.ptr, (size_t)k * sizeof(double), cudaMemcpyDeviceToHost,
+                               s));
+    IPTGB_CUDA(cudaStreamSynchronize(s));
+    return IPT_CUDA_SUCCESS;
+}
+
+IPT_API int ipt_block_solve_csr_device(const int *d_row_ptr, const int *d_col_ind,
+                                       const double *d_values_csr, int n, int nnz, int k,
+                                       const IPTBlockOptions *options, double *d_vectors,
+                                       double *d_values, IPTBlockReport *report)
+{
+    return csr_block_device(d_row_ptr, d_col_ind, d_values_csr, n, nnz, k, options, nullptr,
+                            d_vectors, d_values, report);
+}
+
+IPT_API int ipt_block_solve_csr(const int *row_ptr, const int *col_ind, const double *values_csr,
+                                int n, int nnz, int k, const IPTBlockOptions *options,
+                                double *vectors, double *values, IPTBlockReport *report)
+{
+    if (row_ptr == nullptr || col_ind == nullptr || values_csr == nullptr || vectors == nullptr ||
+        values == nullptr || n <= 0 || k <= 0 || k > n || nnz < 0) {
+        return IPT_CUDA_INVALID_ARGUMENT;
+    }
+    // For a symmetric H the CSR arrays are the CSC arrays of the same matrix.
+    PreparedCsr prep;
+    IPTGB_CHECK(prepare_csc(row_ptr, col_ind, values_csr, n, nnz, true, &prep));
+    IPTBlockOptions opt;
+    if (options != nullptr) {
+        opt = *options;
+    } else {
+        fill_default_options(&opt);
+    }
+    cudaStream_t s = (cudaStream_t)opt.stream;
+    DeviceBuffer<int> rp, ci;
+    DeviceBuffer<double> cv, dd, dX, dv;
+    IPTGB_CHECK(rp.alloc(prep.row_ptr.size(), s));
+    IPTGB_CHECK(ci.alloc(prep.col_ind.size(), s));
+    IPTGB_CHECK(cv.alloc(prep.vals.size(), s));
+    IPTGB_CHECK(dd.alloc((size_t)n, s));
+    IPTGB_CHECK(dX.alloc((size_t)n * k, s));
+    IPTGB_CHECK(dv.alloc((size_t)k, s));
+    IPTGB_CUDA(cudaMemcpyAsync(rp.ptr, prep.row_ptr.data(), prep.row_ptr.size() * sizeof(int),
+                               cudaMemcpyHostToDevice, s));
+    if (!prep.col_ind.empty()) {
+        IPTGB_CUDA(cudaMemcpyAsync(ci.ptr, prep.col_ind.data(), prep.col_ind.size() * sizeof(int),
+                                   cudaMemcpyHostToDevice, s));
+        IPTGB_CUDA(cudaMemcpyAsync(cv.ptr, prep.vals.data(), prep.vals.size() * sizeof(double),
+                                   cudaMemcpyHostToDevice, s));
+    }
+    IPTGB_CUDA(cudaMemcpyAsync(dd.ptr, prep.diag.data(), (size_t)n * sizeof(double),
+                               cudaMemcpyHostToDevice, s));
+    IPTGB_CHECK(csr_block_device(rp.ptr, ci.ptr, cv.ptr, n, prep.nnz, k, &opt, dd.ptr, dX.ptr,
+                                 dv.ptr, report));
+    IPTGB_CUDA(cudaMemcpyAsync(vectors, dX.ptr, (size_t)n * k * sizeof(double),
+                               cudaMemcpyDeviceToHost, s));
+    IPTGB_CUDA(cudaMemcpyAsync(values, dv.ptr, (size_t)k * sizeof(double), cudaMemcpyDeviceToHost,
+                               s));
+    IPTGB_CUDA(cudaStreamSynchronize(s));
+    unpermute_vectors(prep, vectors, k);
+    return IPT_CUDA_SUCCESS;
+}
+
+// The reference's IPT_BLOCK_CLUSTER path for the sparse host entry points
+// (IPT_C_GPU/src/ipt_cuda.cu:5070-5075 -> 4712-5016): requires a real
+// symmetric matrix; Ritz pairs in ascending order, unit-norm vectors, the
+// Davidson enrichment (IPT_DAVIDSON_ENRICH) run until the residuals reach
+// IPT_DAVIDSON_CONVERGED_TOL.
+int ipt_block_sparse_host_entry(const int *col_ptr, const int *row_ind, const double *vals, int n,
+                                int k, int nnz, int maxiter, double tol, int use_tol,
+                                IPTCudaResult *result)
+{
+    auto t0 = std::chrono::steady_clock::now();
+    memset(result, 0, sizeof(*result));
+    result->fixed_point_residual = NAN;
+    result->davidson_target_index = -1;
+    result->davidson_residual_before = NAN;
+    result->davidson_residual_after = NAN;
+    result->davidson_denom_clip = NAN;
+    result->best_so_far_enabled = 1;
+    result->best_so_far_step = -1;
+    strcpy(result->best_so_far_source, "none");
+    result->best_so_far_max_residual = NAN;
+    result->best_so_far_max_residual_index = -1;
+    if (!validate_csc(col_ptr, row_ind, n, nnz)) {
+        return IPT_CUDA_INVALID_ARGUMENT;
+    }
+    PreparedCsr prep;
+    IPTGB_CHECK(prepare_csc(col_ptr, row_ind, vals, n, nnz, true, &prep));
+    // symmetry check on the transposed arrays, O(nnz)
+    {
+        std::vector<int> rp, ci;
+        std::vector<double> cv;
+        csc_to_csr(prep.row_ptr.data(), prep.col_ind.data(), prep.vals.data(), n, prep.nnz, &rp,
+                   &ci, &cv);
+        for (size_t p = 0; p < cv.size(); ++p) {
+            const double a = cv[p], b = prep.vals[p];
+            if (ci[p] != prep.col_ind[p] ||
+                fabs(a - b) > 1e-12 * std::max(1.0, std::max(fabs(a), fabs(b)))) {
+                ipt_cuda_free_result(result);
+                return IPT_CUDA_INVALID_ARGUMENT;
+            }
+        }
+    }
+    IPTBlockOptions opt;
+    fill_default_options(&opt);
+    opt.ipt_maxiter = env_int("IPT_BLOCK_CLUSTER_MAXITER", maxiter > 0 ? maxiter : 100);
+    opt.ipt_tol = env_double("IPT_BLOCK_CLUSTER_TOL", use_tol ? tol : 1e-12);
+    opt.oversample = env_int("IPT_BLOCK_CLUSTER_OVERSAMPLE", 0);
+    const int enrich = env_flag("IPT_DAVIDSON_ENRICH", 0);
+    const int steps = std::max(0, env_int("IPT_DAVIDSON_STEPS", 1)) +
+                      std::max(0, env_int("IPT_DAVIDSON_EXTRA_STEPS", 0));
+    opt.davidson_maxsteps = enrich ? std::max(1, steps) : 0;
+    opt.residual_tol = env_double("IPT_DAVIDSON_CONVERGED_TOL", 1e-13);
+    result->vectors = (double *)calloc((size_t)n * k, sizeof(double));
+    result->values = (double *)calloc((size_t)k, sizeof(double));
+    if (result->vectors == nullptr || result->values == nullptr) {
+        ipt_cuda_free_result(result);
+        return IPT_CUDA_ALLOCATION_FAILED;
+    }
+    result->preparation_time_sec =
+        std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    IPTBlockReport rep;
+    int status;
+    {
+        cudaStream_t s = nullptr;
+        status = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) == cudaSuccess
+                     ? IPT_CUDA_SUCCESS
+                     : IPT_CUDA_CUDA_ERROR;
+        opt.stream = s;
+        DeviceBuffer<int> rp, ci;
+        DeviceBuffer<double> cv, dd, dX, dv;
+        if (status == IPT_CUDA_SUCCESS) status = rp.alloc(prep.row_ptr.size(), s);
+        if (status == IPT_CUDA_SUCCESS) status = ci.alloc(prep.col_ind.size(), s);
+        if (status == IPT_CUDA_SUCCESS) status = cv.alloc(prep.vals.size(), s);
+        if (status == IPT_CUDA_SUCCESS) status = dd.alloc((size_t)n, s);
+        if (status == IPT_CUDA_SUCCESS) status = dX.alloc((size_t)n * k, s);
+        if (status == IPT_CUDA_SUCCESS) status = dv.alloc((size_t)k, s);
+        if (status == IPT_CUDA_SUCCESS &&
+            (cudaMemcpyAsync(rp.ptr, prep.row_ptr.data(), prep.row_ptr.size() * sizeof(int),
+                             cudaMemcpyHostToDevice, s) != cudaSuccess ||
+             (prep.nnz > 0 &&
+              (cudaMemcpyAsync(ci.ptr, prep.col_ind.data(), prep.col_ind.size() * sizeof(int),
+                               cudaMemcpyHostToDevice, s) != cudaSuccess ||
+               cudaMemcpyAsync(cv.ptr, prep.vals.data(), prep.vals.size() * sizeof(double),
+                               cudaMemcpyHostToDevice, s) != cudaSuccess)) ||
+             cudaMemcpyAsync(dd.ptr, prep.diag.data(), (size_t)n * sizeof(double),
+                             cudaMemcpyHostToDevice, s) != cudaSuccess)) {
+            status = IPT_CUDA_CUDA_ERROR;
+        }
+        if (status == IPT_CUDA_SUCCESS) {
+            status = csr_block_device(rp.ptr, ci.ptr, cv.ptr, n, prep.nnz, k, &opt, dd.ptr, dX.ptr,
+                                      dv.ptr, &rep);
+        }
+        if (status == IPT_CUDA_SUCCESS &&
+            (cudaMemcpyAsync(result->vectors, dX.ptr, (size_t)n * k * sizeof(double),
+                             cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+             cudaMemcpyAsync(result->values, dv.ptr, (size_t)k * sizeof(double),
+                             cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+             cudaStreamSynchronize(s) != cudaSuccess)) {
+            status = IPT_CUDA_CUDA_ERROR;
+        }
+        rp.release();
+        ci.release();
+        cv.release();
+        dd.release();
+        dX.release();
+        dv.release();
+        if (s != nullptr) {
+            cudaStreamSynchronize(s);
+            cudaStreamDestroy(s);
+        }
+    }
+    if (status != IPT_CUDA_SUCCESS) {
+        ipt_cuda_free_result(result);
+        return status;
+    }
+    unpermute_vectors(prep, result->vectors, k);
+    result->n = n;
+    result->k = k;
+    result->iterations = rep.ipt_iterations;
+    result->basis_cols = rep.basis_cols;
+    result->matvecs = rep.fp64_matvecs;
+    result->fixed_point_residual = rep.ipt_fixed_point_residual;
+    result->iteration_time_sec = rep.ipt_ms * 1e-3;
+    result->rayleigh_ritz_time_sec = rep.rayleigh_ritz_ms * 1e-3;
+    result->davidson_time_sec = rep.davidson_ms * 1e-3;
+    result->solve_time_sec = rep.total_ms * 1e-3;
+    result->oversample = opt.oversample;
+    result->rayleigh_ritz_used_qr = 0;
+    result->davidson_attempted = opt.davidson_maxsteps > 0;
+    result->davidson_accepted = rep.davidson_steps > 0;
+    result->davidson_residual_after = rep.max_scaled_residual;
+    result->davidson_restart_count = rep.restarts;
+    result->accepted_steps = rep.davidson_steps;
+    result->best_so_far_max_residual = rep.max_scaled_residual;
+    strcpy(result->best_so_far_source, rep.davidson_steps > 0 ? "davidson" : "rayleigh_ritz");
+    result->final_returned_from_best_so_far = 1;
+    strcpy(result->pair28_lock_state, "inactive");
+    strcpy(result->pair29_lock_state, "inactive");
+    result->gap28_29 = NAN;
+    result->relative_gap28_29 = NAN;
+    result->cluster_residual_fro = NAN;
+    result->cluster_residual_max = NAN;
+    result->pair28_best_residual = NAN;
+    result->pair29_best_residual = NAN;
+    result->adaptive_coupling_tau = NAN;
+    result->adaptive_target_block_start = -1;
+    result->adaptive_target_block_end = -1;
+    result->basis_orthogonality_frobenius_error = NAN;
+    result->basis_orthogonality_max_abs_error = NAN;
+    result->ritz_vectors_orthogonality_frobenius_error = NAN;
+    result->ritz_vectors_orthogonality_max_abs_error = NAN;
+    return IPT_CUDA_SUCCESS;
+}

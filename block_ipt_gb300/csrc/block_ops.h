@@ -1,0 +1,41 @@
+// block_ops.h - FP64 block operations (CholQR, Rayleigh-Ritz, Davidson).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stddef.h>
+
+namespace iptgb {
+
+// Launch wrapper bound to one stream; owns a reusable partial-sum buffer.
+// All matrices are column-major doubles with explicit leading dimensions.
+struct BlockOps {
+    cudaStream_t stream = nullptr;
+    int sms = 148;
+    double *partials = nullptr;
+    size_t partials_capacity = 0;
+
+    // C = alpha * A^T B + beta * C, A: n x ma, B: n x mb, C: ma x mb.
+    int gram(const double *A, long long lda, int ma, const double *B, long long ldb, int mb, int n,
+             double *C, long long ldc, double alpha = 1.0, double beta = 0.0);
+    // C = alpha * A B + beta * C, A: n x m, B: m x p, C: n x p.
+    int tall_gemm(const double *A, long long lda, const double *B, long long ldb, double *C,
+                  long long ldc, int n, int m, int p, double alpha = 1.0, double beta = 0.0);
+    // G = R^T R (one CTA); Rinv = R^{-1}; status_dev[0] = shifts used or -1.
+    int chol_inverse(const double *G, int m, double *Rinv, int *status_dev);
+    // Symmetric eigensolve (one CTA Jacobi): ascending w, eigenvectors Z.
+    int jacobi_eig(const double *T, int m, double *w, double *Z, int *sweeps_dev);
+    // R = AX - X diag(theta); rnorm[j] = ||r_j||; scaled[j] as the reference.
+    int residuals(const double *X, const double *AX, const double *theta, int n, int k,
+                  long long ldx, double hnorm, double *R, double *rnorm, double *scaled);
+    // T[:, c] = R[:, sel[c]] / clip(d - theta[sel[c]]).
+    int diag_correction(const double *R, const double *d, const double *theta, const int *sel,
+                        int nsel, int n, double clip, double *T);
+    int column_norms(const double *A, long long lda, int n, int c, double *out);
+    int gather_columns(const double *src, long long lds, const int *idx, const double *scale,
+                       int n, int c, double *dst, long long ldd);
+
+    int ensure_partials(size_t count);
+    void release();
+};
+
+}  // namespace iptgb

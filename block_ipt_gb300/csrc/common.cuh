@@ -1,0 +1,109 @@
+// common.cuh - shared definitions for the GB300 block-IPT library.
+//
+// Everything here is internal; the exported C ABI lives in abi.cu and is
+// declared in include/ipt_cuda.h and include/ipt_block.h.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stdio.h>
+
+#include <cstddef>
+
+#include "../../include/ipt_cuda.h"
+
+namespace iptgb {
+
+// Launch geometry shared by the element-wise kernels.
+constexpr int kThreads = 256;
+
+inline int blocks_for(size_t count, int threads = kThreads)
+{
+    size_t b = (count + (size_t)threads - 1) / (size_t)threads;
+    if (b == 0) {
+        b = 1;
+    }
+    return (int)b;
+}
+
+// Error propagation: every internal call returns an IPT_CUDA_* status.
+#define IPTGB_CUDA(call)                                                        \
+    do {                                                                        \
+        cudaError_t iptgb_err_ = (call);                                        \
+        if (iptgb_err_ != cudaSuccess) {                                        \
+            fprintf(stderr, "ipt_gb300: CUDA error at %s:%d: %s\n", __FILE__,   \
+                    __LINE__, cudaGetErrorString(iptgb_err_));                  \
+            return IPT_CUDA_CUDA_ERROR;                                         \
+        }                                                                       \
+    } while (0)
+
+#define IPTGB_CHECK(expr)                                                       \
+    do {                                                                        \
+        int iptgb_status_ = (expr);                                             \
+        if (iptgb_status_ != IPT_CUDA_SUCCESS) {                                \
+            return iptgb_status_;                                               \
+        }                                                                       \
+    } while (0)
+
+#define IPTGB_LAUNCH()                                                          \
+    do {                                                                        \
+        cudaError_t iptgb_err_ = cudaGetLastError();                            \
+        if (iptgb_err_ != cudaSuccess) {                                        \
+            fprintf(stderr, "ipt_gb300: launch error at %s:%d: %s\n",           \
+                    __FILE__, __LINE__, cudaGetErrorString(iptgb_err_));        \
+            return IPT_CUDA_CUDA_ERROR;                                         \
+        }                                                                       \
+    } while (0)
+
+// A device buffer released by its destructor (stream-ordered when possible).
+template <typename T>
+struct DeviceBuffer {
+    T *ptr = nullptr;
+    size_t count = 0;
+    cudaStream_t stream = nullptr;
+    DeviceBuffer() = default;
+    DeviceBuffer(const DeviceBuffer &) = delete;
+    DeviceBuffer &operator=(const DeviceBuffer &) = delete;
+    ~DeviceBuffer() { release(); }
+    int alloc(size_t n, cudaStream_t s)
+    {
+        release();
+        stream = s;
+        count = n;
+        if (n == 0) {
+            return IPT_CUDA_SUCCESS;
+        }
+        cudaError_t e = cudaMallocAsync((void **)&ptr, n * sizeof(T), s);
+        if (e != cudaSuccess) {
+            ptr = nullptr;
+            count = 0;
+            fprintf(stderr, "ipt_gb300: cudaMallocAsync(%zu bytes) failed: %s\n",
+                    n * sizeof(T), cudaGetErrorString(e));
+            return IPT_CUDA_CUDA_ERROR;
+        }
+        return IPT_CUDA_SUCCESS;
+    }
+    void release()
+    {
+        if (ptr != nullptr) {
+            cudaFreeAsync(ptr, stream);
+            ptr = nullptr;
+            count = 0;
+        }
+    }
+    T *release_ownership()
+    {
+        T *p = ptr;
+        ptr = nullptr;
+        count = 0;
+        return p;
+    }
+};
+
+// Environment knobs keep the reference's names and parsing rules
+// (IPT_C_GPU/src/ipt_cuda.cu:18-73).
+double env_double(const char *name, double default_value);
+int env_int(const char *name, int default_value);
+int env_flag(const char *name, int default_value);
+
+}  // namespace iptgb

@@ -1,0 +1,62 @@
+// ipt_plain.h - FP64 plain-IPT drivers behind the reference ABI (internal).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "kernels.cuh"
+
+namespace iptgb {
+
+// One application of the IPT map X' = F(X) in FP64, plus (H X)_jj.
+struct Fp64Operator {
+    virtual ~Fp64Operator() = default;
+    // Xn = F(X); with want_norms the step leaves ||Xn - X||_F, ||X||_F in ns->norms.
+    virtual int step(const double *X, double *Xn, const double *d, int want_norms,
+                     NormScratch *ns) = 0;
+    // values[j] = (H X)_jj.
+    virtual int diag_values(const double *X, double *values) = 0;
+};
+
+struct DenseFp64Operator final : Fp64Operator {
+    const double *H = nullptr;
+    long long ldh = 0;
+    int n = 0, k = 0, S = 1;
+    double *P = nullptr;  // S * n * k partial slices
+    cudaStream_t stream = nullptr;
+    int step(const double *X, double *Xn, const double *d, int want_norms,
+             NormScratch *ns) override;
+    int diag_values(const double *X, double *values) override;
+};
+
+struct CsrFp64Operator final : Fp64Operator {
+    const int *row_ptr = nullptr;
+    const int *col_ind = nullptr;
+    const double *vals = nullptr;
+    int n = 0, k = 0;
+    double *Y = nullptr;  // n * k
+    cudaStream_t stream = nullptr;
+    int step(const double *X, double *Xn, const double *d, int want_norms,
+             NormScratch *ns) override;
+    int diag_values(const double *X, double *values) override;
+};
+
+// Scratch owned by a solve: norm reduction slots + pinned readback.
+struct SolveScratch {
+    NormScratch ns;
+    double *host_norms = nullptr;  // pinned, 2 doubles
+    int init(size_t max_elems, cudaStream_t stream);
+    void release(cudaStream_t stream);
+};
+
+// The reference's plain IPT loop (IPT_C_GPU/src/ipt_cuda.cu:1644-1703):
+// X_a holds the start block on entry; on success *X_final points at the
+// buffer (X_a or X_b) holding the returned block.  In tolerance mode the loop
+// stops once ||F(X)-X||_F / ||X||_F <= tol and returns F(X).
+int run_plain_ipt(Fp64Operator &op, int n, int k, const double *d, int maxiter, double tol,
+                  int use_tol, double *X_a, double *X_b, double **X_final,
+                  int *iterations_done, double *fixed_point_residual, SolveScratch *scratch,
+                  cudaStream_t stream);
+
+int device_sm_count();
+
+}  // namespace iptgb

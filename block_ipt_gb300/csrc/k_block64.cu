@@ -1,0 +1,653 @@
+// k_block64.cu - FP64 block kernels for CholQR, Rayleigh-Ritz and Davidson.
+//
+// These are the steps whose stability needs FP64 (Gram matrices, the
+// projected matrix and its eigensolve, residual norms, the correction step).
+// Reference counterparts: Householder QR / Gram + sygvd Rayleigh-Ritz
+// (IPT_C_GPU/src/ipt_cuda.cu:3039-3316), mixed CholQR
+// (IPT_C_GPU/mixed/ipt_rayleigh_mixed_mpqr_cuda.cu:169-386), residual kernels
+// (ipt_cuda.cu:2399-2447,2608-2709) and the Davidson correction
+// (ipt_cuda.cu:2449-2465,2711-2780,3389-3403).
+//
+// GB300 retires ~8 GFLOP/s of FP64 per SM, so every O(n m^2) kernel here is
+// spread over all SMs (row-chunk partials reduced in a fixed order), and the
+// O(m^3) kernels run in one CTA on data held in shared memory.
+#include <math.h>
+
+#include "block_ops.h"
+#include "common.cuh"
+#include "reduce.cuh"
+
+namespace iptgb {
+
+// ---------------------------------------------------------------------------
+// Gram-type products C = A^T B (A: n x ma, B: n x mb, column-major).
+// Grid: (row chunks, output tiles of 32x32).  Partials [chunk][mb][ma].
+// ---------------------------------------------------------------------------
+constexpr int kGramRows = 64;
+constexpr int kGramTile = 32;
+
+__global__ void __launch_bounds__(256)
+gram_partial_kernel(const double *__restrict__ A, long long lda, int ma,
+                    const double *__restrict__ B, long long ldb, int mb, int n, int chunks_per_block,
+                    double *__restrict__ P)
+{
+    __shared__ double as[kGramRows][kGramTile + 1];
+    __shared__ double bs[kGramRows][kGramTile + 1];
+    const int tiles_i = (ma + kGramTile - 1) / kGramTile;
+    const int ti = blockIdx.y % tiles_i;
+    const int tj = blockIdx.y / tiles_i;
+    const int i0 = ti * kGramTile;
+    const int j0 = tj * kGramTile;
+    // thread -> 4 outputs: (li, lj + 8q), q = 0..3
+    const int li = threadIdx.x % kGramTile;
+    const int lj = threadIdx.x / kGramTile;  // 0..7
+    double acc[4] = {0.0, 0.0, 0.0, 0.0};
+    for (int c = 0; c < chunks_per_block; ++c) {
+        const int r0 = (blockIdx.x * chunks_per_block + c) * kGramRows;
+        if (r0 >= n) {
+            break;
+        }
+        __syncthreads();
+        for (int e = threadIdx.x; e < kGramRows * kGramTile; e += blockDim.x) {
+            const int r = e % kGramRows;
+            const int col = e / kGramRows;
+            const int row = r0 + r;
+            as[r][col] = (row < n && i0 + col < ma) ? A[(size_t)row + (size_t)(i0 + col) * lda] : 0.0;
+            bs[r][col] = (row < n && j0 + col < mb) ? B[(size_t)row + (size_t)(j0 + col) * ldb] : 0.0;
+        }
+        __syncthreads();
+#pragma unroll 8
+        for (int r = 0; r < kGramRows; ++r) {
+            const double a = as[r][li];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                acc[q] = fma(a, bs[r][lj + 8 * q], acc[q]);
+            }
+        }
+    }
+    const size_t mm = (size_t)ma * (size_t)mb;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const int i = i0 + li;
+        const int j = j0 + lj + 8 * q;
+        if (i < ma && j < mb) {
+            P[(size_t)blockIdx.x * mm + (size_t)j * ma + i] = acc[q];
+        }
+    }
+}
+
+__global__ void reduce_slices_kernel(const double *__restrict__ P, int slices, size_t elems,
+                                     double *__restrict__ out, long long ldo, int rows,
+                                     double alpha, double beta)
+{
+    const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= elems) {
+        return;
+    }
+    double s = 0.0;
+    for (int b = 0; b < slices; ++b) {
+        s += P[(size_t)b * elems + e];
+    }
+    const size_t i = e % (size_t)rows;
+    const size_t j = e / (size_t)rows;
+    double *o = out + i + j * (size_t)ldo;
+    *o = beta == 0.0 ? alpha * s : alpha * s + beta * *o;
+}
+
+int BlockOps::gram(const double *A, long long lda, int ma, const double *B, long long ldb, int mb,
+                   int n, double *C, long long ldc, double alpha, double beta)
+{
+    if (ma <= 0 || mb <= 0) {
+        return IPT_CUDA_SUCCESS;
+    }
+    const int chunks = (n + kGramRows - 1) / kGramRows;
+    const int tiles = ((ma + kGramTile - 1) / kGramTile) * ((mb + kGramTile - 1) / kGramTile);
+    // ~2 blocks per SM in total, each taking consecutive row chunks
+    int blocks_x = (2 * sms + tiles - 1) / tiles;
+    if (blocks_x > chunks) blocks_x = chunks;
+    if (blocks_x < 1) blocks_x = 1;
+    const int per_block = (chunks + blocks_x - 1) / blocks_x;
+    blocks_x = (chunks + per_block - 1) / per_block;
+    const size_t mm = (size_t)ma * (size_t)mb;
+    IPTGB_CHECK(ensure_partials((size_t)blocks_x * mm));
+    gram_partial_kernel<<<dim3(blocks_x, tiles), 256, 0, stream>>>(A, lda, ma, B, ldb, mb, n,
+                                                                   per_block, partials);
+    IPTGB_LAUNCH();
+    reduce_slices_kernel<<<blocks_for(mm), kThreads, 0, stream>>>(partials, blocks_x, mm, C, ldc,
+                                                                  ma, alpha, beta);
+    IPTGB_LAUNCH();
+    return IPT_CUDA_SUCCESS;
+}
+
+// ---------------------------------------------------------------------------
+// Tall-by-small product C = alpha * A B + beta * C
+// (A: n x m, B: m x p, C: n x p, column-major).  One row per thread, 32
+// output columns per block column; B tile staged in shared memory.
+// ---------------------------------------------------------------------------
+constexpr int kTallCols = 32;
+constexpr int kTallK = 32;
+
+__global__ void __launch_bounds__(256)
+tall_gemm_kernel(const double *__restrict__ A, long long lda, const double *__restrict__ B,
+                 long long ldb, double *__restrict__ C, long long ldc, int n, int m, int p,
+                 double alpha, double beta)
+{
+    __shared__ double bs[kTallK][kTallCols];
+    const int row = blockIdx.x * blockDim.x + threadIdx.x;
+    const int c0 = blockIdx.y * kTallCols;
+    double acc[kTallCols];
+#pragma unroll
+    for (int j = 0; j < kTallCols; ++j) {
+        acc[j] = 0.0;
+    }
+    for (int l0 = 0; l0 < m; l0 += kTallK) {
+        __syncthreads();
+        for (int e = threadIdx.x; e < kTallK * kTallCols; e += blockDim.x) {
+            const int l = e % kTallK;
+            const int j = e / kTallK;
+            bs[l][j] = (l0 + l < m && c0 + j < p) ? B[(size_t)(l0 + l) + (size_t)(c0 + j) * ldb] : 0.0;
+        }
+        __syncthreads();
+        if (row < n) {
+            const int lc = min(kTallK, m - l0);
+            for (int l = 0; l < lc; ++l) {
+                const double a = A[(size_t)row + (size_t)(l0 + l) * lda];
+#pragma unroll
+                for (int j = 0; j < kTallCols; ++j) {
+                    acc[j] = fma(a, bs[l][j], acc[j]);
+                }
+            }
+        }
+    }
+    if (row < n) {
+#pragma unroll
+        for (int j = 0; j < kTallCols; ++j) {
+            if (c0 + j < p) {
+                double *o = C + (size_t)row + (size_t)(c0 + j) * ldc;
+                *o = beta == 0.0 ? alpha * acc[j] : alpha * acc[j] + beta * *o;
+            }
+        }
+    }
+}
+
+int BlockOps::tall_gemm(const double *A, long long lda, const double *B, long long ldb, double *C,
+                        long long ldc, int n, int m, int p, double alpha, double beta)
+{
+    if (p <= 0) {
+        return IPT_CUDA_SUCCESS;
+    }
+    dim3 grid((n + 255) / 256, (p + kTallCols - 1) / kTallCols);
+    tall_gemm_kernel<<<grid, 256, 0, stream>>>(A, lda, B, ldb, C, ldc, n, m, p, alpha, beta);
+    IPTGB_LAUNCH();
+    return IPT_CUDA_SUCCESS;
+}
+
+// ---------------------------------------------------------------------------
+// One-CTA Cholesky of an m x m SPD matrix G (column-major, ld = m) and the
+// inverse of its upper factor: G = R^T R, Rinv = R^{-1} (upper triangular).
+// If G is not numerically positive definite, G + shift*I is factored with a
+// shift grown from 1e-14 * trace(G) until it succeeds; status[0] gets the
+// number of shifts used (0 = plain), or -1 if it never succeeded.
+// Dynamic shared memory: 2 * m * m doubles.
+// ---------------------------------------------------------------------------
+__global__ void chol_inverse_kernel(const double *__restrict__ G, int m, double *__restrict__ Rinv,
+                                    int *status)
+{
+    extern __shared__ double sm[];
+    double *L = sm;          // lower factor, row-major [i*m + j]
+    double *W = sm + m * m;  // inverse of L, row-major
+    __shared__ int fail;
+    __shared__ double shift;
+    __shared__ int attempts;
+    const int tid = threadIdx.x;
+    const int nt = blockDim.x;
+    if (tid == 0) {
+        double tr = 0.0;
+        for (int i = 0; i < m; ++i) {
+            tr += fabs(G[(size_t)i * m + i]);
+        }
+        shift = 0.0;
+        attempts = 0;
+        // remember the trace for shift growth
+        W[0] = tr > 0.0 ? tr : 1.0;
+    }
+    __syncthreads();
+    const double trace = W[0];
+    for (;;) {
+        for (int e = tid; e < m * m; e += nt) {
+            const int i = e / m;
+            const int j = e % m;
+            L[e] = G[(size_t)j * m + i] + (i == j ? shift : 0.0);
+        }
+        if (tid == 0) {
+            fail = 0;
+        }
+        __syncthreads();
+        for (int j = 0; j < m; ++j) {
+            if (tid == 0) {
+                const double a = L[j * m + j];
+                if (!(a > 0.0) || !isfinite(a)) {
+                    fail = 1;
+                } else {
+                    L[j * m + j] = sqrt(a);
+                }
+            }
+            __syncthreads();
+            if (fail) {
+                break;
+            }
+            const double ljj = L[j * m + j];
+            for (int i = j + 1 + tid; i < m; i += nt) {
+                L[i * m + j] /= ljj;
+            }
+            __syncthreads();
+            // trailing update of the lower triangle: L[i][l] -= L[i][j] L[l][j], j < l <= i
+            const int rem = m - j - 1;
+            for (int e = tid; e < rem * rem; e += nt) {
+                const int i = j + 1 + e / rem;
+                const int l = j + 1 + e % rem;
+                if (l <= i) {
+                    L[i * m + l] -= L[i * m + j] * L[l * m + j];
+                }
+            }
+            __syncthreads();
+        }
+        if (!fail) {
+            break;
+        }
+        __syncthreads();
+        if (tid == 0) {
+            attempts += 1;
+            shift = shift == 0.0 ? 1e-14 * trace : shift * 100.0;
+        }
+        __syncthreads();
+        if (attempts > 12) {
+            if (tid == 0) {
+                status[0] = -1;
+            }
+            return;
+        }
+    }
+    // W = L^{-1} by forward substitution, one column per thread.
+    for (int c = tid; c < m; c += nt) {
+        for (int i = 0; i < m; ++i) {
+            double v = (i == c) ? 1.0 : 0.0;
+            for (int l = c; l < i; ++l) {
+                v -= L[i * m + l] * W[l * m + c];
+            }
+            W[i * m + c] = i < c ? 0.0 : v / L[i * m + i];
+        }
+    }
+    __syncthreads();
+    // R = L^T, so R^{-1} = (L^{-1})^T: Rinv[i][j] = W[j][i]; column-major out.
+    for (int e = tid; e < m * m; e += nt) {
+        const int i = e % m;
+        const int j = e / m;
+        Rinv[(size_t)j * m + i] = W[j * m + i];
+    }
+    if (tid == 0) {
+        status[0] = attempts;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// One-CTA cyclic Jacobi eigensolver for a symmetric m x m matrix (column-major
+// in, ld = m).  Parallel round-robin ordering: m/2 disjoint rotations per
+// round, m-1 rounds per sweep.  Output: ascending eigenvalues w[m] and the
+// matching orthonormal eigenvectors Z (column-major, ld = m).
+// Dynamic shared memory: 2 * M * M + 3 * M doubles, M = m rounded up to even.
+// ---------------------------------------------------------------------------
+__global__ void jacobi_eig_kernel(const double *__restrict__ T, int m, double *__restrict__ w,
+                                  double *__restrict__ Z, int max_sweeps, int *sweeps_out)
+{
+    extern __shared__ double sm[];
+    const int M = (m + 1) & ~1;
+    double *A = sm;              // row-major M x M
+    double *V = sm + M * M;      // row-major M x M
+    double *cs = sm + 2 * M * M; // c[M/2], s[M/2]
+    int *pr = (int *)(cs + M);   // pair indices p[M/2], q[M/2]
+    __shared__ double off_norm;
+    __shared__ double tot_norm;
+    const int tid = threadIdx.x;
+    const int nt = blockDim.x;
+    const int half = M / 2;
+    for (int e = tid; e < M * M; e += nt) {
+        const int i = e / M;
+        const int j = e % M;
+        double a = 0.0;
+        if (i < m && j < m) {
+            a = 0.5 * (T[(size_t)j * m + i] + T[(size_t)i * m + j]);
+        }
+        A[e] = a;
+        V[e] = i == j ? 1.0 : 0.0;
+    }
+    __syncthreads();
+    int sweep = 0;
+    for (; sweep < max_sweeps; ++sweep) {
+        // convergence test on the off-diagonal mass
+        double off = 0.0, tot = 0.0;
+        for (int e = tid; e < M * M; e += nt) {
+            const double a = A[e];
+            tot += a * a;
+            if (e / M != e % M) {
+                off += a * a;
+            }
+        }
+        double2 t = block_sum2(off, tot);
+        if (tid == 0) {
+            off_norm = t.x;
+            tot_norm = t.y;
+        }
+        __syncthreads();
+        // relative off-diagonal Frobenius mass <= 1e-13 (the rounding floor of
+        // the rotations sits near m * 1e-16, so a tighter test may never pass)
+        if (off_norm <= 1e-26 * tot_norm || off_norm == 0.0) {
+            break;
+        }
+        for (int r = 0; r < M - 1; ++r) {
+            for (int k = tid; k < half; k += nt) {
+                int p, q;
+                if (k == 0) {
+                    p = M - 1;
+                    q = r;
+                } else {
+                    p = (r + k) % (M - 1);
+                    q = (r - k + M - 1) % (M - 1);
+                }
+                if (p > q) {
+                    const int tmp = p;
+                    p = q;
+                    q = tmp;
+                }
+                double c = 1.0, s = 0.0;
+                const double apq = A[p * M + q];
+                if (q < m && apq != 0.0) {
+                    const double app = A[p * M + p];
+                    const double aqq = A[q * M + q];
+                    if (fabs(apq) > 1e-300) {
+                        const double theta = (aqq - app) / (2.0 * apq);
+                        const double tt = (theta >= 0.0 ? 1.0 : -1.0) /
+                                          (fabs(theta) + sqrt(theta * theta + 1.0));
+                        c = 1.0 / sqrt(tt * tt + 1.0);
+                        s = tt * c;
+                    }
+                }
+                cs[k] = c;
+                cs[half + k] = s;
+                pr[k] = p;
+                pr[half + k] = q;
+            }
+            __syncthreads();
+            // columns: A <- A J, V <- V J
+            for (int e = tid; e < half * M; e += nt) {
+                const int k = e / M;
+                const int l = e % M;
+                const double c = cs[k], s = cs[half + k];
+                if (s != 0.0) {
+                    const int p = pr[k], q = pr[half + k];
+                    const double alp = A[l * M + p], alq = A[l * M + q];
+                    A[l * M + p] = c * alp - s * alq;
+                    A[l * M + q] = s * alp + c * alq;
+                    const double vlp = V[l * M + p], vlq = V[l * M + q];
+                    V[l * M + p] = c * vlp - s * vlq;
+                    V[l * M + q] = s * vlp + c * vlq;
+                }
+            }
+            __syncthreads();
+            // rows: A <- J^T A
+            for (int e = tid; e < half * M; e += nt) {
+                const int k = e / M;
+                const int l = e % M;
+                const double c = cs[k], s = cs[half + k];
+                if (s != 0.0) {
+                    const int p = pr[k], q = pr[half + k];
+                    const double apl = A[p * M + l], aql = A[q * M + l];
+                    A[p * M + l] = c * apl - s * aql;
+                    A[q * M + l] = s * apl + c * aql;
+                }
+            }
+            __syncthreads();
+        }
+    }
+    // sort ascending (selection by rank; m is small)
+    for (int i = tid; i < m; i += nt) {
+        const double ai = A[i * M + i];
+        int rank = 0;
+        for (int j = 0; j < m; ++j) {
+            const double aj = A[j * M + j];
+            rank += (aj < ai) || (aj == ai && j < i);
+        }
+        w[rank] = ai;
+        for (int l = 0; l < m; ++l) {
+            Z[(size_t)rank * m + l] = V[l * M + i];
+        }
+    }
+    if (tid == 0 && sweeps_out != nullptr) {
+        *sweeps_out = sweep;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Residual block R = AX - X diag(theta) and per-column partial sums of
+// ||r_j||^2, ||x_j||^2.  Grid: (row chunks, k).  Partials [chunk][k][2].
+// ---------------------------------------------------------------------------
+__global__ void residual_partial_kernel(const double *__restrict__ X, const double *__restrict__ AX,
+                                        const double *__restrict__ theta, int n, long long ldx,
+                                        double *__restrict__ R, int rows_per_block,
+                                        double2 *__restrict__ P)
+{
+    const int j = blockIdx.y;
+    const int r0 = blockIdx.x * rows_per_block;
+    const int r1 = min(n, r0 + rows_per_block);
+    const double th = theta[j];
+    double rs = 0.0, xs = 0.0;
+    for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
+        const size_t idx = (size_t)i + (size_t)j * ldx;
+        const double x = X[idx];
+        const double r = AX[idx] - x * th;
+        R[(size_t)i + (size_t)j * n] = r;
+        rs = fma(r, r, rs);
+        xs = fma(x, x, xs);
+    }
+    double2 t = block_sum2(rs, xs);
+    if (threadIdx.x == 0) {
+        P[(size_t)blockIdx.x * gridDim.y + j] = t;
+    }
+}
+
+// norms[j] = (||r_j||, ||x_j||), scaled[j] = ||r_j|| / (max(1,hnorm) max(1,||x_j||))
+// (scaling of IPT_C_GPU/src/ipt_cuda.cu:2684-2697).
+__global__ void residual_finish_kernel(const double2 *__restrict__ P, int chunks, int k,
+                                       double hnorm, double *__restrict__ rnorm,
+                                       double *__restrict__ scaled)
+{
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= k) {
+        return;
+    }
+    double rs = 0.0, xs = 0.0;
+    for (int c = 0; c < chunks; ++c) {
+        const double2 p = P[(size_t)c * k + j];
+        rs += p.x;
+        xs += p.y;
+    }
+    const double r = sqrt(rs);
+    const double x = sqrt(xs);
+    rnorm[j] = r;
+    scaled[j] = r / (fmax(1.0, hnorm) * fmax(1.0, x));
+}
+
+int BlockOps::residuals(const double *X, const double *AX, const double *theta, int n, int k,
+                        long long ldx, double hnorm, double *R, double *rnorm, double *scaled)
+{
+    const int rows_per_block = 2048;
+    const int chunks = (n + rows_per_block - 1) / rows_per_block;
+    IPTGB_CHECK(ensure_partials((size_t)chunks * k * 2));
+    residual_partial_kernel<<<dim3(chunks, k), 256, 0, stream>>>(X, AX, theta, n, ldx, R,
+                                                                 rows_per_block,
+                                                                 (double2 *)partials);
+    IPTGB_LAUNCH();
+    residual_finish_kernel<<<blocks_for(k), kThreads, 0, stream>>>((const double2 *)partials,
+                                                                   chunks, k, hnorm, rnorm,
+                                                                   scaled);
+    IPTGB_LAUNCH();
+    return IPT_CUDA_SUCCESS;
+}
+
+// ---------------------------------------------------------------------------
+// Diagonal Davidson correction for the selected Ritz pairs:
+//   T[:, c] = R[:, sel[c]] / clip(d_i - theta_sel[c])
+// with |denominator| clipped below at `clip` keeping its sign
+// (IPT_C_GPU/src/ipt_cuda.cu:2449-2465, clip rule :3389-3403).
+// ---------------------------------------------------------------------------
+__global__ void diag_correction_kernel(const double *__restrict__ R, const double *__restrict__ d,
+                                       const double *__restrict__ theta, const int *__restrict__ sel,
+                                       int nsel, int n, double clip, double *__restrict__ T)
+{
+    const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (size_t)n * (size_t)nsel) {
+        return;
+    }
+    const int i = (int)(idx % (size_t)n);
+    const int c = (int)(idx / (size_t)n);
+    const int j = sel[c];
+    double den = d[i] - theta[j];
+    if (fabs(den) < clip) {
+        den = den < 0.0 ? -clip : clip;
+    }
+    T[idx] = R[(size_t)i + (size_t)j * n] / den;
+}
+
+int BlockOps::diag_correction(const double *R, const double *d, const double *theta,
+                              const int *sel, int nsel, int n, double clip, double *T)
+{
+    diag_correction_kernel<<<blocks_for((size_t)n * nsel), kThreads, 0, stream>>>(
+        R, d, theta, sel, nsel, n, clip, T);
+    IPTGB_LAUNCH();
+    return IPT_CUDA_SUCCESS;
+}
+
+// Column norms of an n x c block (2-pass deterministic).
+__global__ void colnorm_partial_kernel(const double *__restrict__ A, long long lda, int n,
+                                       int rows_per_block, double *__restrict__ P)
+{
+    const int j = blockIdx.y;
+    const int r0 = blockIdx.x * rows_per_block;
+    const int r1 = min(n, r0 + rows_per_block);
+    double s = 0.0;
+    for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
+        const double a = A[(size_t)i + (size_t)j * lda];
+        s = fma(a, a, s);
+    }
+    double2 t = block_sum2(s, 0.0);
+    if (threadIdx.x == 0) {
+        P[(size_t)blockIdx.x * gridDim.y + j] = t.x;
+    }
+}
+
+__global__ void colnorm_finish_kernel(const double *__restrict__ P, int chunks, int c,
+                                      double *__restrict__ out)
+{
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= c) {
+        return;
+    }
+    double s = 0.0;
+    for (int b = 0; b < chunks; ++b) {
+        s += P[(size_t)b * c + j];
+    }
+    out[j] = sqrt(s);
+}
+
+int BlockOps::column_norms(const double *A, long long lda, int n, int c, double *out)
+{
+    const int rows_per_block = 2048;
+    const int chunks = (n + rows_per_block - 1) / rows_per_block;
+    IPTGB_CHECK(ensure_partials((size_t)chunks * c));
+    colnorm_partial_kernel<<<dim3(chunks, c), 256, 0, stream>>>(A, lda, n, rows_per_block,
+                                                                partials);
+    IPTGB_LAUNCH();
+    colnorm_finish_kernel<<<blocks_for(c), kThreads, 0, stream>>>(partials, chunks, c, out);
+    IPTGB_LAUNCH();
+    return IPT_CUDA_SUCCESS;
+}
+
+// Gather/scale columns: dst[:, c] = src[:, idx[c]] * (scale ? scale[c] : 1).
+__global__ void gather_columns_kernel(const double *__restrict__ src, long long lds,
+                                      const int *__restrict__ idx, const double *__restrict__ scale,
+                                      int n, int c, double *__restrict__ dst, long long ldd)
+{
+    const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= (size_t)n * (size_t)c) {
+        return;
+    }
+    const int i = (int)(e % (size_t)n);
+    const int j = (int)(e / (size_t)n);
+    const double s = scale != nullptr ? scale[j] : 1.0;
+    dst[(size_t)i + (size_t)j * ldd] = src[(size_t)i + (size_t)idx[j] * lds] * s;
+}
+
+int BlockOps::gather_columns(const double *src, long long lds, const int *idx, const double *scale,
+                             int n, int c, double *dst, long long ldd)
+{
+    if (c <= 0) {
+        return IPT_CUDA_SUCCESS;
+    }
+    gather_columns_kernel<<<blocks_for((size_t)n * c), kThreads, 0, stream>>>(src, lds, idx, scale,
+                                                                           n, c, dst, ldd);
+    IPTGB_LAUNCH();
+    return IPT_CUDA_SUCCESS;
+}
+
+int BlockOps::chol_inverse(const double *G, int m, double *Rinv, int *status_dev)
+{
+    const size_t smem = 2 * (size_t)m * (size_t)m * sizeof(double);
+    if (smem > 200 * 1024) {
+        return IPT_CUDA_INVALID_ARGUMENT;
+    }
+    IPTGB_CUDA(cudaFuncSetAttribute(chol_inverse_kernel,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    chol_inverse_kernel<<<1, 256, smem, stream>>>(G, m, Rinv, status_dev);
+    IPTGB_LAUNCH();
+    return IPT_CUDA_SUCCESS;
+}
+
+int BlockOps::jacobi_eig(const double *T, int m, double *w, double *Z, int *sweeps_dev)
+{
+    const int M = (m + 1) & ~1;
+    const size_t smem = (2 * (size_t)M * M + 2 * (size_t)M) * sizeof(double);
+    if (smem > 200 * 1024) {
+        return IPT_CUDA_INVALID_ARGUMENT;
+    }
+    IPTGB_CUDA(cudaFuncSetAttribute(jacobi_eig_kernel,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    jacobi_eig_kernel<<<1, 512, smem, stream>>>(T, m, w, Z, 40, sweeps_dev);
+    IPTGB_LAUNCH();
+    return IPT_CUDA_SUCCESS;
+}
+
+int BlockOps::ensure_partials(size_t count)
+{
+    if (count <= partials_capacity) {
+        return IPT_CUDA_SUCCESS;
+    }
+    if (partials != nullptr) {
+        cudaFreeAsync(partials, stream);
+        partials = nullptr;
+    }
+    size_t want = count < (size_t)1 << 16 ? (size_t)1 << 16 : count;
+    IPTGB_CUDA(cudaMallocAsync((void **)&partials, want * sizeof(double), stream));
+    partials_capacity = want;
+    return IPT_CUDA_SUCCESS;
+}
+
+void BlockOps::release()
+{
+    if (partials != nullptr) {
+        cudaFreeAsync(partials, stream);
+        partials = nullptr;
+        partials_capacity = 0;
+    }
+}
+
+}  // namespace iptgb

@@ -1,0 +1,834 @@
+// k_tc.cu - low-precision dense IPT stage on the GB300 tensor cores.
+//
+// Block product Y = Delta X for the IPT map (reference: cublasGemmEx FP16 /
+// TF32 on the off-diagonal copy, IPT_C_GPU/src/mixed_precision/
+// ipt_mixed_precision_cuda.cu:189-216,520-523,713-716), written for sm_103a:
+//
+//  * Delta (diagonal zeroed, power-of-two scaled for FP16) is stored once per
+//    solve row-major ("K-major") in FP16, BF16 or TF32-rounded FP32, with a
+//    leading dimension padded to 64 elements;
+//  * each CTA owns 128 rows and a K-range (split-K so that the grid covers
+//    the 152 SMs); warp 0 streams 128-byte-wide K chunks of Delta and X
+//    through a multi-stage TMA pipeline (cp.async.bulk.tensor, SWIZZLE_128B,
+//    mbarrier complete_tx), warp 1 issues tcgen05.mma (M = 128, N = padded
+//    block width, FP32 accumulators in TMEM), and all four warps drain TMEM
+//    with tcgen05.ld into per-split FP32 partial blocks;
+//  * a second kernel sums the split partials in a fixed order, applies the
+//    IPT update X' = (Y - X c) * G (c_j = Y_jj, G_ij = 1/(d_j - d_i)) in FP32,
+//    writes the FP32 master block and the low-precision operand copy for the
+//    next product, and reduces ||X' - X||_F and ||X||_F.
+//
+// Every mbarrier wait is bounded; a timeout sets an error flag, the CTA
+// drains its own outstanding copies (bounded), frees its TMEM and returns.
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+#include <math.h>
+#include <string.h>
+
+#include <algorithm>
+#include <memory>
+
+#include "block_solver.h"
+#include "common.cuh"
+#include "lowp.h"
+#include "reduce.cuh"
+
+namespace iptgb {
+namespace tc {
+
+constexpr int kBM = 128;         // UMMA M: rows of Delta per CTA
+constexpr int kRowBytes = 128;   // one SWIZZLE_128B row per K chunk
+constexpr int kThreads = 128;
+constexpr long long kSpinLimit = 1LL << 24;
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p)
+{
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity)
+{
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Bounded wait; returns false (and records `code`) after kSpinLimit polls.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int *err, int code,
+                                          bool sleepy)
+{
+    for (long long it = 0; it < kSpinLimit; ++it) {
+        if (mbar_try_wait(bar, parity)) {
+            return true;
+        }
+        if (sleepy) {
+            __nanosleep(128);
+        }
+    }
+    atomicExch(err, code);
+    return false;
+}
+
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap *map, int x, int y,
+                                            uint32_t bar)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes"
+        " [%0], [%1, {%2, %3}], [%4];" ::"r"(dst),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(bar)
+        : "memory");
+}
+
+// Shared-memory matrix descriptor: K-major operand, 128-byte swizzle, rows of
+// 128 bytes, 8-row atoms 1024 bytes apart (SBO), descriptor version 1.
+__device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr)
+{
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr >> 4) & 0x3FFFu);
+    d |= (uint64_t)(16u >> 4) << 16;
+    d |= (uint64_t)(1024u >> 4) << 32;
+    d |= (uint64_t)1 << 46;
+    d |= (uint64_t)2 << 61;
+    return d;
+}
+
+template <int KIND>
+__device__ __forceinline__ void umma(uint32_t dtmem, uint64_t adesc, uint64_t bdesc,
+                                     uint32_t idesc, uint32_t accumulate)
+{
+    if (KIND == kLowpTF32) {
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "setp.ne.b32 p, %4, 0;\n\t"
+            "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(dtmem),
+            "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+            : "memory");
+    } else {
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "setp.ne.b32 p, %4, 0;\n\t"
+            "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(dtmem),
+            "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+            : "memory");
+    }
+}
+
+__device__ __forceinline__ void umma_commit(uint32_t bar)
+{
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                     bar)
+                 : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld_32cols(uint32_t taddr, float (&v)[32])
+{
+    uint32_t r[32];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+        "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
+        "%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+          "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),
+          "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]),
+          "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+          "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]),
+          "=r"(r[31])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 32; ++i) {
+        v[i] = __uint_as_float(r[i]);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Split-K partial product P[split] = Delta[rows, Ksplit] X[Ksplit, :].
+// Grid (row blocks, splits); 128 threads; dynamic smem = stages * stage bytes
+// + 1 KB alignment slack + barriers.  P layout: [split][col][row], ld = n.
+// ---------------------------------------------------------------------------
+template <int KIND>
+__global__ void __launch_bounds__(kThreads, 1)
+tc_partial_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+                  int n, int p, int p_pad, int stages, int tmem_cols, int chunks_total,
+                  int chunks_per_split, int kchunk_elems, uint32_t idesc, float *__restrict__ P,
+                  int *err)
+{
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t *smem =
+        reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    const uint32_t a_bytes = kBM * kRowBytes;
+    const uint32_t b_bytes = (uint32_t)p_pad * kRowBytes;
+    const uint32_t stage_bytes = a_bytes + b_bytes;
+    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + (size_t)stages * stage_bytes);
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 2 * stages + 1);
+    __shared__ int abort_flag;
+    __shared__ int issued_count;
+
+    const int warp = threadIdx.x >> 5;
+    const int lane = threadIdx.x & 31;
+    const int rb = blockIdx.x;
+    const int split = blockIdx.y;
+    const int c0 = split * chunks_per_split;
+    const int c1 = min(chunks_total, c0 + chunks_per_split);
+    const int nchunks = c1 - c0;
+    const uint32_t smem_base = smem_u32(smem);
+    const uint32_t bar_base = smem_u32(bars);
+    auto full_bar = [&](int s) { return bar_base + 8u * (uint32_t)s; };
+    auto empty_bar = [&](int s) { return bar_base + 8u * (uint32_t)(stages + s); };
+    const uint32_t accum_bar = bar_base + 8u * (uint32_t)(2 * stages);
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < stages; ++s) {
+            mbar_init(full_bar(s), 1);
+            mbar_init(empty_bar(s), 1);
+        }
+        mbar_init(accum_bar, 1);
+        abort_flag = 0;
+        issued_count = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                         smem_u32(tmem_slot)),
+                     "r"(tmem_cols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = *tmem_slot;
+
+    if (warp == 0 && lane == 0) {
+        // ---- TMA producer ----
+        int i = 0;
+        for (; i < nchunks; ++i) {
+            const int s = i % stages;
+            const int r = i / stages;
+            if (r > 0 && !mbar_wait(empty_bar(s), (uint32_t)((r - 1) & 1), err, 1, false)) {
+                abort_flag = 1;
+                break;
+            }
+            if (abort_flag) {
+                break;
+            }
+            const uint32_t sa = smem_base + (uint32_t)s * stage_bytes;
+            const uint32_t sb = sa + a_bytes;
+            const int kx = (c0 + i) * kchunk_elems;
+            mbar_expect_tx(full_bar(s), stage_bytes);
+            tma_load_2d(sa, &tmA, kx, rb * kBM, full_bar(s));
+            tma_load_2d(sb, &tmB, kx, 0, full_bar(s));
+        }
+        issued_count = i;
+    } else if (warp == 1 && lane == 0) {
+        // ---- tcgen05.mma issuer ----
+        for (int i = 0; i < nchunks; ++i) {
+            const int s = i % stages;
+            const int r = i / stages;
+            if (!mbar_wait(full_bar(s), (uint32_t)(r & 1), err, 2, false)) {
+                abort_flag = 1;
+                break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const uint32_t sa = smem_base + (uint32_t)s * stage_bytes;
+            const uint32_t sb = sa + a_bytes;
+            const uint64_t ad = sw128_desc(sa);
+            const uint64_t bd = sw128_desc(sb);
+#pragma unroll
+            for (int kk = 0; kk < 4; ++kk) {
+                // advance 32 bytes along K inside the swizzle atom
+                umma<KIND>(tmem, ad + (uint64_t)(2 * kk), bd + (uint64_t)(2 * kk), idesc,
+                           (i > 0 || kk > 0) ? 1u : 0u);
+            }
+            umma_commit(empty_bar(s));
+        }
+        umma_commit(accum_bar);
+    }
+    __syncwarp();
+
+    // ---- epilogue: TMEM -> registers -> partial block ----
+    const bool ok = mbar_wait(accum_bar, 0u, err, 3, true);
+    __syncwarp();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if (ok && !abort_flag) {
+        const int row = rb * kBM + warp * 32 + lane;
+        for (int cb = 0; cb < p_pad; cb += 32) {
+            float v[32];
+            tmem_ld_32cols(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)cb, v);
+            if (row < n) {
+#pragma unroll
+                for (int j = 0; j < 32; ++j) {
+                    if (cb + j < p) {
+                        P[((size_t)split * p + (size_t)(cb + j)) * (size_t)n + row] = v[j];
+                    }
+                }
+            }
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (abort_flag && threadIdx.x == 0) {
+        // drain copies this CTA may still have in flight (bounded)
+        const int issued = issued_count;
+        for (int i = max(0, issued - stages); i < issued; ++i) {
+            mbar_wait(full_bar(i % stages), (uint32_t)((i / stages) & 1), err, 4, true);
+        }
+    }
+    __syncthreads();
+    if (warp == 0) {
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                     "r"(tmem_cols)
+                     : "memory");
+    }
+}
+
+}  // namespace tc
+
+// ---------------------------------------------------------------------------
+// Delta conversion: out[i * ldp + l] = lp(scale * H[i, l]) for l != i, 0 on the
+// diagonal and in the padding columns.  H column-major (ld = n).  32x32 tiles
+// through shared memory so that both the read and the write are coalesced.
+// ---------------------------------------------------------------------------
+template <typename LP>
+__device__ __forceinline__ LP to_lp(float v);
+template <>
+__device__ __forceinline__ __half to_lp<__half>(float v)
+{
+    return __float2half_rn(v);
+}
+template <>
+__device__ __forceinline__ __nv_bfloat16 to_lp<__nv_bfloat16>(float v)
+{
+    return __float2bfloat16_rn(v);
+}
+template <>
+__device__ __forceinline__ float to_lp<float>(float v)
+{
+    // TF32 operand: round to nearest into the 10-bit mantissa kept by the
+    // tensor core (cvt.rna.tf32.f32 returns the rounded value in fp32 bits).
+    uint32_t r;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(v));
+    return __uint_as_float(r);
+}
+
+template <typename LP>
+__global__ void convert_delta_kernel(const double *__restrict__ H, int n, int ldp, double scale,
+                                     LP *__restrict__ out)
+{
+    __shared__ float tile[32][33];
+    const int l0 = blockIdx.x * 32;  // column block of H (= K index)
+    const int i0 = blockIdx.y * 32;  // row block of H
+    const int tx = threadIdx.x;      // 0..31
+    for (int ty = threadIdx.y; ty < 32; ty += blockDim.y) {
+        const int i = i0 + tx;
+        const int l = l0 + ty;
+        float v = 0.0f;
+        if (i < n && l < n && i != l) {
+            v = (float)(scale * H[(size_t)i + (size_t)l * n]);
+        }
+        tile[ty][tx] = v;  // tile[l - l0][i - i0]
+    }
+    __syncthreads();
+    for (int ty = threadIdx.y; ty < 32; ty += blockDim.y) {
+        const int i = i0 + ty;
+        const int l = l0 + tx;
+        if (i < n && l < ldp) {
+            out[(size_t)i * ldp + l] = to_lp<LP>(tile[tx][ty]);
+        }
+    }
+}
+
+__global__ void max_abs_offdiag_kernel(const double *__restrict__ H, int n,
+                                       unsigned long long *out)
+{
+    double m = 0.0;
+    const size_t total = (size_t)n * n;
+    for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+         e += (size_t)gridDim.x * blockDim.x) {
+        const size_t i = e % (size_t)n;
+        const size_t l = e / (size_t)n;
+        if (i != l) {
+            m = fmax(m, fabs(H[e]));
+        }
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+        m = fmax(m, __shfl_xor_sync(0xffffffffu, m, off));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicMax(out, (unsigned long long)__double_as_longlong(m));
+    }
+}
+
+// G_ij = 1 / (d_j - d_i) as FP32 (0 on the target position, NaN for a zero
+// or non-finite gap); computed once per solve in FP64 then rounded.
+__global__ void build_g32_kernel(const double *__restrict__ d, int n, int p, float *__restrict__ G)
+{
+    const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= (size_t)n * p) return;
+    const int i = (int)(e % (size_t)n);
+    const int j = (int)(e / (size_t)n);
+    float g = 0.0f;
+    if (i != j) {
+        const double gap = d[j] - d[i];
+        g = (isfinite(gap) && gap != 0.0) ? (float)(1.0 / gap) : __int_as_float(0x7fc00000);
+    }
+    G[e] = g;
+}
+
+template <typename LP>
+__global__ void lowp_identity_kernel(float *X32, LP *Xlp, int n, int p, int ldx)
+{
+    const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= (size_t)n * p) return;
+    const int i = (int)(e % (size_t)n);
+    const int j = (int)(e / (size_t)n);
+    const float v = i == j ? 1.0f : 0.0f;
+    X32[e] = v;
+    Xlp[(size_t)i + (size_t)j * ldx] = to_lp<LP>(v);
+}
+
+// Low-precision IPT update (see file header); Delta has a zero diagonal so
+// c_j = (Delta X)_jj is read straight from the product.
+template <typename LP>
+__global__ void lowp_update_kernel(const float *__restrict__ P, int S, int n, int p,
+                                   float inv_scale, const float *__restrict__ G,
+                                   const float *__restrict__ X, float *__restrict__ Xn,
+                                   LP *__restrict__ Xlp, int ldx, int want_norms,
+                                   double2 *partials, unsigned int *counter, double *norms)
+{
+    const size_t elems = (size_t)n * (size_t)p;
+    const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    double dsq = 0.0, xsq = 0.0;
+    if (idx < elems) {
+        const int row = (int)(idx % (size_t)n);
+        const int col = (int)(idx / (size_t)n);
+        const float x = X[idx];
+        float out = 1.0f;
+        if (row != col) {
+            float y = 0.0f, c = 0.0f;
+            for (int s = 0; s < S; ++s) {
+                const size_t base = ((size_t)s * p + col) * (size_t)n;
+                y += P[base + row];
+                c += P[base + col];
+            }
+            out = (y * inv_scale - x * (c * inv_scale)) * G[idx];
+        }
+        Xn[idx] = out;
+        Xlp[(size_t)row + (size_t)col * ldx] = to_lp<LP>(out);
+        if (want_norms) {
+            const double df = (double)out - (double)x;
+            dsq = df * df;
+            xsq = (double)x * (double)x;
+        }
+    }
+    if (want_norms) {
+        const double2 t = block_sum2(dsq, xsq);
+        grid_finish_norms2(t, partials, counter, norms);
+    }
+}
+
+__global__ void f32_to_f64_kernel(const float *__restrict__ in, size_t count, double *__restrict__ out)
+{
+    const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e < count) out[e] = (double)in[e];
+}
+
+// ---------------------------------------------------------------------------
+// Host side
+// ---------------------------------------------------------------------------
+namespace {
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
+                                  const cuuint64_t *, const cuuint64_t *, const cuuint32_t *,
+                                  const cuuint32_t *, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                  CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_fn()
+{
+    static EncodeTiledFn fn = nullptr;
+    static bool tried = false;
+    if (!tried) {
+        tried = true;
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                             &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess) {
+            fn = reinterpret_cast<EncodeTiledFn>(p);
+        }
+    }
+    return fn;
+}
+
+// 2-D K-major tensor map: inner dim = K (ld elements, stride ld*esize),
+// outer = rows; box = {128 bytes of K, box_rows}, 128-byte swizzle.
+int make_map(CUtensorMap *map, CUtensorMapDataType dt, int esize, void *base, int ld, int rows,
+             int box_rows)
+{
+    EncodeTiledFn fn = encode_fn();
+    if (fn == nullptr) {
+        return IPT_CUDA_CUDA_ERROR;
+    }
+    cuuint64_t dims[2] = {(cuuint64_t)ld, (cuuint64_t)rows};
+    cuuint64_t strides[1] = {(cuuint64_t)ld * (cuuint64_t)esize};
+    cuuint32_t box[2] = {(cuuint32_t)(128 / esize), (cuuint32_t)box_rows};
+    cuuint32_t estr[2] = {1, 1};
+    CUresult r = fn(map, dt, 2, base, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                    CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) {
+        fprintf(stderr, "ipt_gb300: cuTensorMapEncodeTiled failed (%d)\n", (int)r);
+        return IPT_CUDA_CUDA_ERROR;
+    }
+    return IPT_CUDA_SUCCESS;
+}
+
+int pick_splits(int row_blocks, int chunks, int sms)
+{
+    int best = 1;
+    double best_eff = 0.0;
+    for (int s = 1; s <= 16 && s * 4 <= chunks; ++s) {
+        const int ctas = row_blocks * s;
+        const int waves = (ctas + sms - 1) / sms;
+        const double eff = (double)ctas / (double)(waves * sms);
+        if (eff > best_eff + 0.02) {
+            best_eff = eff;
+            best = s;
+        }
+    }
+    return best;
+}
+
+template <typename LP>
+struct LowpTypes;
+template <>
+struct LowpTypes<__half> {
+    static constexpr CUtensorMapDataType dt = CU_TENSOR_MAP_DATA_TYPE_FLOAT16;
+    static constexpr int kind = kLowpF16;
+};
+template <>
+struct LowpTypes<__nv_bfloat16> {
+    static constexpr CUtensorMapDataType dt = CU_TENSOR_MAP_DATA_TYPE_BFLOAT16;
+    static constexpr int kind = kLowpBF16;
+};
+template <>
+struct LowpTypes<float> {
+    static constexpr CUtensorMapDataType dt = CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
+    static constexpr int kind = kLowpTF32;
+};
+
+}  // namespace
+
+template <typename LP>
+struct LowpDense final : LowpDenseOperator {
+    static constexpr int esize = (int)sizeof(LP);
+    static constexpr int kchunk = 128 / esize;
+
+    int init(const double *dH, int n_, cudaStream_t s_)
+    {
+        n = n_;
+        s = s_;
+        sms = 148;
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        ldp = ((n + 63) / 64) * 64;
+        IPTGB_CHECK(delta.alloc((size_t)n * ldp, s));
+        DeviceBuffer<unsigned long long> mx;
+        IPTGB_CHECK(mx.alloc(1, s));
+        IPTGB_CUDA(cudaMemsetAsync(mx.ptr, 0, sizeof(unsigned long long), s));
+        max_abs_offdiag_kernel<<<std::min(4 * sms, blocks_for((size_t)n * n)), kThreads, 0, s>>>(
+            dH, n, mx.ptr);
+        IPTGB_LAUNCH();
+        unsigned long long bits = 0;
+        IPTGB_CUDA(cudaMemcpyAsync(&bits, mx.ptr, sizeof(bits), cudaMemcpyDeviceToHost, s));
+        IPTGB_CUDA(cudaStreamSynchronize(s));
+        double maxabs;
+        memcpy(&maxabs, &bits, sizeof(maxabs));
+        scale = 1.0;
+        if (LowpTypes<LP>::kind == kLowpF16 && maxabs > 0.0 && isfinite(maxabs)) {
+            // largest power of two with maxabs * scale <= 16384 (FP16 max 65504)
+            scale = ldexp(1.0, (int)floor(log2(16384.0 / maxabs)));
+            scale = std::min(std::max(scale, ldexp(1.0, -40)), ldexp(1.0, 40));
+        }
+        dim3 grid((ldp + 31) / 32, (n + 31) / 32);
+        convert_delta_kernel<LP><<<grid, dim3(32, 8), 0, s>>>(dH, n, ldp, scale, delta.ptr);
+        IPTGB_LAUNCH();
+        IPTGB_CHECK(make_map(&mapA, LowpTypes<LP>::dt, esize, delta.ptr, ldp, n, tc::kBM));
+        IPTGB_CHECK(err.alloc(1, s));
+        IPTGB_CUDA(cudaMemsetAsync(err.ptr, 0, sizeof(int), s));
+        return IPT_CUDA_SUCCESS;
+    }
+
+    int set_width(int p_) override
+    {
+        p = p_;
+        p_pad = ((p + 15) / 16) * 16;
+        if (p_pad > 256) {
+            return IPT_CUDA_INVALID_ARGUMENT;
+        }
+        tmem_cols = 32;
+        while (tmem_cols < p_pad) tmem_cols <<= 1;
+        const int row_blocks = (n + tc::kBM - 1) / tc::kBM;
+        chunks_total = ldp / kchunk;
+        splits = pick_splits(row_blocks, chunks_total, sms);
+        chunks_per_split = (chunks_total + splits - 1) / splits;
+        splits = (chunks_total + chunks_per_split - 1) / chunks_per_split;
+        const size_t stage_bytes = (size_t)(tc::kBM + p_pad) * tc::kRowBytes;
+        stages = (int)std::min<size_t>(8, (200u * 1024u) / stage_bytes);
+        if (stages < 2) return IPT_CUDA_INVALID_ARGUMENT;
+        smem_bytes = 1024 + stages * stage_bytes + (2 * stages + 1) * 8 + 16;
+        const int afmt = LowpTypes<LP>::kind == kLowpF16 ? 0 : (LowpTypes<LP>::kind == kLowpBF16 ? 1 : 2);
+        idesc = (1u << 4) | ((uint32_t)afmt << 7) | ((uint32_t)afmt << 10) |
+                ((uint32_t)(p_pad >> 3) << 17) | ((uint32_t)(tc::kBM >> 4) << 24);
+        IPTGB_CHECK(P.alloc((size_t)splits * p * n, s));
+        for (int b = 0; b < 2; ++b) {
+            IPTGB_CHECK(Xlp[b].alloc((size_t)ldp * p_pad, s));
+            IPTGB_CUDA(cudaMemsetAsync(Xlp[b].ptr, 0, (size_t)ldp * p_pad * sizeof(LP), s));
+            IPTGB_CHECK(make_map(&mapB[b], LowpTypes<LP>::dt, esize, Xlp[b].ptr, ldp, p_pad, p_pad));
+            IPTGB_CHECK(X32[b].alloc((size_t)n * p, s));
+        }
+        IPTGB_CHECK(G.alloc((size_t)n * p, s));
+        auto kfn = tc::tc_partial_kernel<LowpTypes<LP>::kind>;
+        IPTGB_CUDA(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)smem_bytes));
+        cur = 0;
+        return IPT_CUDA_SUCCESS;
+    }
+
+    int reset_identity(const double *d) override
+    {
+        build_g32_kernel<<<blocks_for((size_t)n * p), kThreads, 0, s>>>(d, n, p, G.ptr);
+        IPTGB_LAUNCH();
+        lowp_identity_kernel<LP><<<blocks_for((size_t)n * p), kThreads, 0, s>>>(
+            X32[0].ptr, Xlp[0].ptr, n, p, ldp);
+        IPTGB_LAUNCH();
+        cur = 0;
+        return IPT_CUDA_SUCCESS;
+    }
+
+    int product() override
+    {
+        const int row_blocks = (n + tc::kBM - 1) / tc::kBM;
+        dim3 grid(row_blocks, splits);
+        tc::tc_partial_kernel<LowpTypes<LP>::kind><<<grid, tc::kThreads, smem_bytes, s>>>(
+            mapA, mapB[cur], n, p, p_pad, stages, tmem_cols, chunks_total, chunks_per_split,
+            kchunk, idesc, P.ptr, err.ptr);
+        IPTGB_LAUNCH();
+        return IPT_CUDA_SUCCESS;
+    }
+
+    int step(int want_norms, NormScratch *ns) override
+    {
+        IPTGB_CHECK(product());
+        const size_t elems = (size_t)n * p;
+        const int grid = blocks_for(elems);
+        if (want_norms && grid > ns->capacity) return IPT_CUDA_INVALID_ARGUMENT;
+        const int nxt = cur ^ 1;
+        lowp_update_kernel<LP><<<grid, kThreads, 0, s>>>(
+            P.ptr, splits, n, p, (float)(1.0 / scale), G.ptr, X32[cur].ptr, X32[nxt].ptr,
+            Xlp[nxt].ptr, ldp, want_norms, ns->partials, ns->counter, ns->norms);
+        IPTGB_LAUNCH();
+        cur = nxt;
+        return IPT_CUDA_SUCCESS;
+    }
+
+    int read_error(int *host_err) override
+    {
+        IPTGB_CUDA(cudaMemcpyAsync(host_err, err.ptr, sizeof(int), cudaMemcpyDeviceToHost, s));
+        return IPT_CUDA_SUCCESS;
+    }
+
+    int export_fp64(double *X) override
+    {
+        f32_to_f64_kernel<<<blocks_for((size_t)n * p), kThreads, 0, s>>>(X32[cur].ptr,
+                                                                         (size_t)n * p, X);
+        IPTGB_LAUNCH();
+        return IPT_CUDA_SUCCESS;
+    }
+
+    int export_fp64_prev(double *X) override
+    {
+        f32_to_f64_kernel<<<blocks_for((size_t)n * p), kThreads, 0, s>>>(X32[cur ^ 1].ptr,
+                                                                         (size_t)n * p, X);
+        IPTGB_LAUNCH();
+        return IPT_CUDA_SUCCESS;
+    }
+
+    const float *partials() const override { return P.ptr; }
+    int num_splits() const override { return splits; }
+
+    int sms = 148;
+    int ldp = 0, p = 0, p_pad = 0, tmem_cols = 32, chunks_total = 0, chunks_per_split = 0;
+    int splits = 1, stages = 2, cur = 0;
+    size_t smem_bytes = 0;
+    uint32_t idesc = 0;
+    double scale = 1.0;
+    cudaStream_t s = nullptr;
+    DeviceBuffer<LP> delta;
+    DeviceBuffer<LP> Xlp[2];
+    DeviceBuffer<float> X32[2];
+    DeviceBuffer<float> G, P;
+    DeviceBuffer<int> err;
+    CUtensorMap mapA, mapB[2];
+};
+
+LowpDenseOperator *make_lowp_dense_operator(const double *dH, int n, int kind, cudaStream_t s,
+                                            int *status)
+{
+    int dev = 0, major = 0, minor = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev);
+    cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, dev);
+    if (major != 10 || encode_fn() == nullptr) {
+        fprintf(stderr, "ipt_gb300: tensor-core IPT stage needs an sm_103 (GB300) device\n");
+        *status = IPT_CUDA_CUDA_ERROR;
+        return nullptr;
+    }
+    std::unique_ptr<LowpDenseOperator> op;
+    int st = IPT_CUDA_INVALID_ARGUMENT;
+    if (kind == kLowpF16) {
+        auto *o = new LowpDense<__half>();
+        op.reset(o);
+        st = o->init(dH, n, s);
+    } else if (kind == kLowpBF16) {
+        auto *o = new LowpDense<__nv_bfloat16>();
+        op.reset(o);
+        st = o->init(dH, n, s);
+    } else if (kind == kLowpTF32) {
+        auto *o = new LowpDense<float>();
+        op.reset(o);
+        st = o->init(dH, n, s);
+    }
+    *status = st;
+    if (st != IPT_CUDA_SUCCESS) {
+        return nullptr;
+    }
+    return op.release();
+}
+
+// ---------------------------------------------------------------------------
+// The IPT stage of the block solver on the low-precision operator.
+// ---------------------------------------------------------------------------
+struct LowpStage final : IptStage {
+    std::unique_ptr<LowpDenseOperator> op;
+    const double *d = nullptr;
+    int n = 0;
+    cudaStream_t s = nullptr;
+    int run(int p, int maxiter, double tol, int check_every, double *X, int *iterations,
+            double *fpres_out, long long *matvecs) override
+    {
+        IPTGB_CHECK(op->set_width(p));
+        IPTGB_CHECK(op->reset_identity(d));
+        return run_lowp_ipt(*op, n, p, maxiter, tol, check_every, X, iterations, fpres_out,
+                            matvecs, s, true);
+    }
+};
+
+IptStage *make_lowp_dense_stage(const double *dH, int n, const double *d, int precision,
+                                cudaStream_t stream, int *status)
+{
+    const int kind = precision == IPT_BLOCK_FP16 ? kLowpF16
+                     : precision == IPT_BLOCK_BF16 ? kLowpBF16
+                                                   : kLowpTF32;
+    LowpDenseOperator *op = make_lowp_dense_operator(dH, n, kind, stream, status);
+    if (op == nullptr) {
+        return nullptr;
+    }
+    auto *st = new LowpStage();
+    st->op.reset(op);
+    st->d = d;
+    st->n = n;
+    st->s = stream;
+    return st;
+}
+
+// Shared IPT loop on a low-precision operator: reads the fixed-point residual
+// every `check_every` iterations; with `guard`, stops once the residual stops
+// decreasing and rolls back a non-finite step.  The final block is exported
+// to X (FP64, n x p).
+int run_lowp_ipt(LowpDenseOperator &op, int n, int p, int maxiter, double tol, int check_every,
+                 double *X, int *iterations, double *fpres_out, long long *matvecs,
+                 cudaStream_t s, bool guard)
+{
+    SolveScratch scratch;
+    IPTGB_CHECK(scratch.init((size_t)n * p, s));
+    int done = 0;
+    double fpres = NAN;
+    double best = INFINITY;
+    int worse = 0;
+    int status = IPT_CUDA_SUCCESS;
+    bool rollback = false;
+    int host_err = 0;
+    for (int it = 0; it < maxiter; ++it) {
+        const int want = ((it + 1) % check_every == 0) || it + 1 == maxiter;
+        status = op.step(want, &scratch.ns);
+        if (status != IPT_CUDA_SUCCESS) break;
+        done = it + 1;
+        if (want) {
+            if (op.read_error(&host_err) != IPT_CUDA_SUCCESS ||
+                cudaMemcpyAsync(scratch.host_norms, scratch.ns.norms, 2 * sizeof(double),
+                                cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+                cudaStreamSynchronize(s) != cudaSuccess) {
+                status = IPT_CUDA_CUDA_ERROR;
+                break;
+            }
+            if (host_err != 0) {
+                fprintf(stderr, "ipt_gb300: tensor-core product timed out (code %d)\n", host_err);
+                status = IPT_CUDA_CUDA_ERROR;
+                break;
+            }
+            const double xn = scratch.host_norms[1];
+            const double r = scratch.host_norms[0] / xn;
+            if (!(xn > 0.0) || !isfinite(r)) {
+                rollback = guard;
+                if (!guard) {
+                    status = IPT_CUDA_INVALID_ARGUMENT;
+                }
+                break;
+            }
+            fpres = r;
+            if (r <= tol) break;
+            if (guard) {
+                if (r < best) {
+                    best = r;
+                    worse = 0;
+                } else if (++worse >= 3) {
+                    break;
+                }
+            }
+        }
+    }
+    scratch.release(s);
+    if (status != IPT_CUDA_SUCCESS) return status;
+    if (rollback) {
+        IPTGB_CHECK(op.export_fp64_prev(X));
+    } else {
+        IPTGB_CHECK(op.export_fp64(X));
+    }
+    *iterations = done;
+    *fpres_out = fpres;
+    *matvecs = (long long)done * p;
+    return IPT_CUDA_SUCCESS;
+}
+
+}  // namespace iptgb

@@ -1,0 +1,45 @@
+// kernels.cuh - launchers of the library's CUDA kernels (internal).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stddef.h>
+
+namespace iptgb {
+
+// Scratch for the deterministic grid-wide norm reductions.
+struct NormScratch {
+    double2 *partials = nullptr;  // one slot per block of the reducing grid
+    int capacity = 0;             // number of slots
+    unsigned int *counter = nullptr;  // ticket counter, zero between launches
+    double *norms = nullptr;      // [0] = ||delta||_F, [1] = ||X||_F
+};
+
+// ---- FP64 dense (k_dense64.cu) -------------------------------------------
+int dense64_split_for(int n, int k, int sms);
+int launch_dense64_partial(const double *H, int n, long long ldh, const double *X,
+                           long long ldx, int k, double *P, int S, cudaStream_t stream);
+int launch_sum_partials(const double *P, int S, size_t elems, double *Y, cudaStream_t stream);
+int launch_dense64_update(const double *P, int S, int n, int k, const double *X,
+                          const double *d, double *Xn, int want_norms, NormScratch *ns,
+                          cudaStream_t stream);
+int launch_set_identity(double *x, int n, int k, cudaStream_t stream);
+int launch_extract_diagonal(const double *H, long long ldh, int n, double *d,
+                            cudaStream_t stream);
+int launch_dense64_diag_values(const double *H, long long ldh, int n, const double *X, int k,
+                               double *values, cudaStream_t stream);
+
+// ---- FP64 CSR (k_csr64.cu) ------------------------------------------------
+// Y = H X with H in CSR (rows sorted, 0-based), X/Y column-major n-by-k.
+int launch_csr64_spmm(const int *row_ptr, const int *col_ind, const double *vals, int n,
+                      const double *X, int k, double *Y, cudaStream_t stream);
+// IPT update from a full Y = H X block (Y may alias nothing); same map as
+// launch_dense64_update with S = 1 partial.
+int launch_ipt_update_from_y(const double *Y, int n, int k, const double *X, const double *d,
+                             double *Xn, int want_norms, NormScratch *ns, cudaStream_t stream);
+int launch_csr64_diagonal(const int *row_ptr, const int *col_ind, const double *vals, int n,
+                          double *d, cudaStream_t stream);
+int launch_csr64_diag_values(const int *row_ptr, const int *col_ind, const double *vals,
+                             int n, const double *X, int k, double *values,
+                             cudaStream_t stream);
+
+}  // namespace iptgb

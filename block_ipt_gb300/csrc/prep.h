@@ -1,0 +1,47 @@
+// prep.h - host preparation of sparse input (internal).
+#pragma once
+
+#include <vector>
+
+namespace iptgb {
+
+// A sparse matrix ready for the CSR gather kernels.  When `permuted` is set
+// the rows/columns are in ascending-diagonal order and perm[sorted] gives the
+// original index (the reference's basis_to_original).
+struct PreparedCsr {
+    int n = 0;
+    int nnz = 0;
+    std::vector<int> row_ptr;
+    std::vector<int> col_ind;
+    std::vector<double> vals;
+    std::vector<double> diag;
+    std::vector<int> perm;
+    bool permuted = false;
+};
+
+// CSC validation (IPT_C_GPU/src/ipt_preparation.cu:148-169).
+bool validate_csc(const int *col_ptr, const int *row_ind, int n, int nnz);
+
+// First stored diagonal entry of each CSC column (ipt_preparation.cu:171-188).
+void csc_diagonal(const int *col_ptr, const int *row_ind, const double *vals, int n,
+                  std::vector<double> *diag);
+
+// Reference preparation without degeneracy lifting
+// (IPT_C_GPU/src/ipt_preparation.cu:1375-1431): validate, stable sort of the
+// diagonal, and, when the order changes, a symmetric permutation that merges
+// duplicates and drops explicit zeros (ipt_permute_csc, :210-262).  The
+// result is emitted as CSR of the same matrix (a transpose of the CSC arrays)
+// so that the gather kernels compute H X for any sparsity pattern.
+// Returns IPT_CUDA_SUCCESS or IPT_CUDA_INVALID_ARGUMENT.
+int prepare_csc(const int *col_ptr, const int *row_ind, const double *vals, int n, int nnz,
+                bool sort_diagonal, PreparedCsr *out);
+
+// Scatter sorted-basis rows back to the original order, in place
+// (ipt_apply_prepared_q_to_vectors without rotations, ipt_preparation.cu:1276-1293).
+void unpermute_vectors(const PreparedCsr &prep, double *vectors_col_major, int k);
+
+// CSC -> CSR transpose keeping duplicates and storage order (stable by column).
+void csc_to_csr(const int *col_ptr, const int *row_ind, const double *vals, int n, int nnz,
+                std::vector<int> *row_ptr, std::vector<int> *col_ind, std::vector<double> *out);
+
+}  // namespace iptgb

@@ -1,0 +1,96 @@
+"""Seeded synthetic workloads with the shapes of the benchmark configurations.
+
+Every random number is a pure function of (seed, stream, i, j) through a
+splitmix64 hash, so matrices are identical on any host and any thread count,
+and symmetric entries come from the canonical pair (min(i,j), max(i,j)).
+
+  dense_config0(n=1024, seed)  d_i = i + U(0,0.5) sorted ascending,
+                               h_ij ~ N(0, 0.05^2) * exp(-|d_i - d_j| / 64)
+  dense_config1(n=8192, seed)  d_i = i/8 + U(0,0.1),
+                               h_ij ~ N(0, 0.02^2) * exp(-|i - j| / 256)
+  batch_config2(count, seed)   per instance: n ~ U{64..2048}, k ~ U{4..16},
+                               sigma ~ U(0.01, 0.1), config-0 construction
+"""
+import numpy as np
+
+_M64 = np.uint64(0xFFFFFFFFFFFFFFFF)
+
+
+def _splitmix(x):
+    with np.errstate(over="ignore"):
+        x = (x + np.uint64(0x9E3779B97F4A7C15)) & _M64
+        z = x
+        z = ((z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)) & _M64
+        z = ((z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)) & _M64
+        return z ^ (z >> np.uint64(31))
+
+
+def _key(seed, stream):
+    return _splitmix(np.uint64((seed * 0x10001 + stream) & 0xFFFFFFFFFFFFFFFF))
+
+
+def _hash2(key, a, b):
+    with np.errstate(over="ignore"):
+        h = _splitmix(key ^ a.astype(np.uint64))
+        return _splitmix(h ^ (b.astype(np.uint64) * np.uint64(0xD1B54A32D192ED03) & _M64))
+
+
+def _u01(h):
+    """Uniform in the open interval (0, 1) from the top 53 bits."""
+    return ((h >> np.uint64(11)).astype(np.float64) + 0.5) * (2.0 ** -53)
+
+
+def uniform(seed, stream, a, b=None):
+    a = np.asarray(a)
+    b = np.zeros_like(a) if b is None else np.asarray(b)
+    return _u01(_hash2(_key(seed, stream), a, b))
+
+
+def normal(seed, stream, a, b):
+    """Standard normal via Box-Muller from two independent hashes."""
+    u1 = uniform(seed, stream, a, b)
+    u2 = uniform(seed, stream + 7919, a, b)
+    return np.sqrt(-2.0 * np.log(u1)) * np.cos(2.0 * np.pi * u2)
+
+
+def _symmetric_offdiag(n, seed, sigma, decay, chunk=1024):
+    """sigma * N(0,1)_{min(i,j),max(i,j)} * decay(i, j), zero diagonal."""
+    H = np.empty((n, n), dtype=np.float64)
+    cols = np.arange(n, dtype=np.int64)
+    for r0 in range(0, n, chunk):
+        rows = np.arange(r0, min(n, r0 + chunk), dtype=np.int64)[:, None]
+        lo = np.minimum(rows, cols[None, :])
+        hi = np.maximum(rows, cols[None, :])
+        H[r0:r0 + len(rows), :] = sigma * normal(seed, 2, lo, hi) * decay(rows, cols[None, :])
+    np.fill_diagonal(H, 0.0)
+    return H
+
+
+def dense_config0(n=1024, seed=0, sigma=0.05):
+    """Plain-IPT dense case: sorted d_i = i + U(0,0.5), exp(-|d_i-d_j|/64) decay."""
+    d = np.sort(np.arange(n, dtype=np.float64) + 0.5 * uniform(seed, 1, np.arange(n)))
+    H = _symmetric_offdiag(n, seed, sigma, lambda i, j: np.exp(-np.abs(d[i] - d[j]) / 64.0))
+    H[np.arange(n), np.arange(n)] = d
+    return np.asfortranarray(H), d
+
+
+def dense_config1(n=8192, seed=0, sigma=0.02):
+    """Mixed-precision dense case: d_i = i/8 + U(0,0.1), exp(-|i-j|/256) decay."""
+    d = np.arange(n, dtype=np.float64) / 8.0 + 0.1 * uniform(seed, 1, np.arange(n))
+    H = _symmetric_offdiag(n, seed, sigma, lambda i, j: np.exp(-np.abs(i - j) / 256.0))
+    H[np.arange(n), np.arange(n)] = d
+    return np.asfortranarray(H), d
+
+
+def batch_config2(count=512, seed=0):
+    """Instance list [(n, k, sigma, seed_b)] of the batched dense workload."""
+    idx = np.arange(count)
+    n = 64 + np.floor(uniform(seed, 11, idx) * (2048 - 64 + 1)).astype(np.int64)
+    k = 4 + np.floor(uniform(seed, 12, idx) * 13).astype(np.int64)
+    sig = 0.01 + 0.09 * uniform(seed, 13, idx)
+    seeds = (seed * 1000003 + idx * 7 + 1).astype(np.int64)
+    return [(int(a), int(b), float(c), int(s)) for a, b, c, s in zip(n, k, sig, seeds)]
+
+
+def batch_instance(n, sigma, seed):
+    return dense_config0(n=n, seed=seed, sigma=sigma)

@@ -1,0 +1,112 @@
+/*
+ * ipt_block.h - block IPT + Rayleigh-Ritz + Davidson solver of libipt_gb300.so.
+ *
+ * These entry points extend the reference ABI of ipt_cuda.h.  They compute the
+ * k lowest eigenpairs of a symmetric H = D + Delta to a scaled residual
+ *      ||H x_j - theta_j x_j|| <= residual_tol * max(1, ||H||_inf),  ||x_j|| = 1,
+ * the stopping scale of the reference's block path
+ * (IPT_C_GPU/src/ipt_cuda.cu:2684-2697), with the steps of its block-cluster
+ * + Davidson driver (IPT_C_GPU/src/ipt_cuda.cu:4712-5016): an IPT stage on
+ * the lowest diagonal positions, Rayleigh-Ritz on the IPT block, then
+ * Davidson corrections with thick restart until every pair converges.
+ *
+ * The IPT stage runs in the precision chosen by `ipt_precision`; FP16/BF16/
+ * TF32 stages multiply on the tensor cores and the FP64 stages that follow
+ * (CholQR Gram matrices, projected matrix, eigensolve, residuals and the
+ * Davidson sweep) win the accuracy back.  The result is always FP64.
+ *
+ * Conventions: dense H is column-major with leading dimension n; CSR input
+ * is 0-based int32 row_ptr[n+1] / col_ind[nnz] with double values (for a
+ * symmetric H these are also its CSC arrays).  Device entry points take
+ * device pointers and run on `stream` (NULL = legacy default stream); host
+ * entry points copy in and out around the same solve.  Return values are the
+ * IPT_CUDA_* status codes of ipt_cuda.h.
+ */
+#ifndef IPT_GB300_IPT_BLOCK_H
+#define IPT_GB300_IPT_BLOCK_H
+
+#include "ipt_cuda.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Precision of the IPT stage's block product Delta X. */
+enum {
+    IPT_BLOCK_FP64 = 0, /* FP64 SIMT product (the plain path) */
+    IPT_BLOCK_FP16 = 1, /* FP16 tensor cores (tcgen05), FP32 accumulation */
+    IPT_BLOCK_BF16 = 2, /* BF16 tensor cores (tcgen05), FP32 accumulation */
+    IPT_BLOCK_TF32 = 3  /* TF32 tensor cores (tcgen05), FP32 accumulation */
+};
+
+/* Davidson preconditioner. */
+enum {
+    IPT_BLOCK_PRECOND_DIAGONAL = 0, /* t_i = r_i / (d_i - theta), clipped */
+    IPT_BLOCK_PRECOND_MLP = 1       /* learned per-row correction, diagonal fallback */
+};
+
+typedef struct {
+    int ipt_precision;      /* IPT_BLOCK_FP64 / _FP16 / _BF16 / _TF32 */
+    int oversample;         /* extra IPT columns carried into Rayleigh-Ritz (>= 0) */
+    int ipt_maxiter;        /* IPT iterations before Rayleigh-Ritz */
+    double ipt_tol;         /* stop the IPT stage once ||F(X)-X||_F/||X||_F <= ipt_tol */
+    int ipt_check_every;    /* fixed-point residual read back every this many iterations */
+    double residual_tol;    /* scaled residual target (default 1e-8) */
+    int davidson_maxsteps;  /* Davidson steps after the first Rayleigh-Ritz */
+    int max_basis;          /* restart size; 0 = automatic */
+    int preconditioner;     /* IPT_BLOCK_PRECOND_* */
+    const float *mlp_params;/* device parameters of the learned preconditioner */
+    void *stream;           /* cudaStream_t, NULL = legacy default stream */
+} IPTBlockOptions;
+
+typedef struct {
+    int n;
+    int k;
+    int converged;              /* 1 if every pair met residual_tol */
+    int ipt_iterations;
+    int davidson_steps;
+    int restarts;
+    int basis_cols;             /* final Rayleigh-Ritz basis size */
+    long long fp64_matvecs;     /* FP64 block-product columns */
+    long long lowp_matvecs;     /* low-precision block-product columns */
+    double ipt_fixed_point_residual;
+    double max_scaled_residual;
+    double matrix_norm_inf;
+    double ipt_ms;              /* device time of the IPT stage */
+    double rayleigh_ritz_ms;    /* first CholQR + Rayleigh-Ritz */
+    double davidson_ms;
+    double total_ms;
+    int mlp_steps_accepted;
+    int mlp_steps_rejected;
+} IPTBlockReport;
+
+void ipt_block_default_options(IPTBlockOptions *options);
+
+/* Dense symmetric H on the device; d_vectors (n*k) and d_values (k) are
+ * caller-allocated device buffers. */
+int ipt_block_solve_dense_device(const double *d_matrix_col_major, int n, int k,
+                                 const IPTBlockOptions *options, double *d_vectors,
+                                 double *d_values, IPTBlockReport *report);
+
+/* Dense symmetric H in host memory; vectors (n*k) and values (k) are host
+ * buffers.  Copies H in, solves, copies the pairs out. */
+int ipt_block_solve_dense(const double *matrix_col_major, int n, int k,
+                          const IPTBlockOptions *options, double *vectors, double *values,
+                          IPTBlockReport *report);
+
+/* Symmetric CSR H on the device. */
+int ipt_block_solve_csr_device(const int *d_row_ptr, const int *d_col_ind, const double *d_values_csr,
+                               int n, int nnz, int k, const IPTBlockOptions *options,
+                               double *d_vectors, double *d_values, IPTBlockReport *report);
+
+/* Symmetric CSR H in host memory (sorted by diagonal inside the call; the
+ * returned vectors are in the caller's row order). */
+int ipt_block_solve_csr(const int *row_ptr, const int *col_ind, const double *values_csr, int n,
+                        int nnz, int k, const IPTBlockOptions *options, double *vectors,
+                        double *values, IPTBlockReport *report);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* IPT_GB300_IPT_BLOCK_H */

@@ -1,0 +1,457 @@
+/*
+ * ipt_oracle.c - CPU restatement of the FJennie/BLOCK_IPT IPT path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This file is the checker for the CUDA solver in
+ * block_ipt_gb300/ and the timed CPU baseline of bench.py; the product never
+ * links, loads or calls it.  Every function names the reference lines it
+ * restates.  It is compiled with -ffp-contract=off so that x86-64 and aarch64
+ * hosts produce bit-identical results, and the OpenMP loops split output
+ * elements between threads without changing any element's summation order,
+ * so the thread count never changes a result bit.
+ */
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#define ORACLE_API __attribute__((visibility("default")))
+
+/* Hash used by the reference dense tests: IPT_C_GPU/test_temp/runtests.cu:46-58. */
+ORACLE_API double oracle_deterministic_noise(int row, int col)
+{
+    uint32_t x = (uint32_t)(row + 1) * 747796405u;
+    x ^= (uint32_t)(col + 1) * 2891336453u;
+    x ^= x >> 16;
+    x *= 2246822519u;
+    x ^= x >> 13;
+    x *= 3266489917u;
+    x ^= x >> 16;
+    return ((double)(x & 0x00ffffffu) / 16777216.0) - 0.5;
+}
+
+/* Dense test matrix: IPT_C_GPU/test_temp/runtests.cu:60-80
+ * (eps = 1e-2 hash noise, optionally symmetrised, diagonal += row + 1). */
+ORACLE_API void oracle_fill_perturbative_matrix(double *matrix, int n, int symmetric)
+{
+    const double eps = 1.0e-2;
+    for (int col = 0; col < n; ++col) {
+        for (int row = 0; row < n; ++row) {
+            double noise = oracle_deterministic_noise(row, col);
+            if (symmetric) {
+                noise = 0.5 * (oracle_deterministic_noise(row, col) +
+                               oracle_deterministic_noise(col, row));
+            }
+            matrix[(size_t)row + (size_t)col * (size_t)n] = eps * noise;
+        }
+    }
+    for (int row = 0; row < n; ++row) {
+        matrix[(size_t)row + (size_t)row * (size_t)n] += (double)(row + 1);
+    }
+}
+
+/* Banded CSC test matrix: IPT_C_GPU/test/sparse/runtests_sparse.cu:224-268.
+ * Arrays must hold n+1, 3n-2 and 3n-2 entries.  Returns nnz. */
+ORACLE_API int oracle_build_banded_csc(int n, int *col_ptr, int *row_ind, double *values)
+{
+    int cursor = 0;
+    for (int col = 0; col < n; ++col) {
+        col_ptr[col] = cursor;
+        if (col > 0) {
+            int edge = col - 1;
+            row_ind[cursor] = col - 1;
+            values[cursor] = 1.0e-2 * (0.50 + 0.03 * (double)(edge % 7));
+            ++cursor;
+        }
+        row_ind[cursor] = col;
+        values[cursor] = (double)(col + 1);
+        ++cursor;
+        if (col + 1 < n) {
+            int edge = col;
+            row_ind[cursor] = col + 1;
+            values[cursor] = 1.0e-2 * (0.50 + 0.03 * (double)(edge % 7));
+            ++cursor;
+        }
+    }
+    col_ptr[n] = cursor;
+    return cursor;
+}
+
+/* out = a * x for column-major a (n x n) and x (n x k).  Each output element
+ * sums inner = 0..n-1 in ascending order, exactly as
+ * IPT_C_GPU/test_temp/runtests.cu:82-96; the loop nest is interchanged
+ * (col, inner, row) for cache reuse, which keeps every element's order. */
+static void oracle_dense_matmul(double *out, const double *a, const double *x, int n, int k)
+{
+#pragma omp parallel for schedule(static)
+    for (int col = 0; col < k; ++col) {
+        double *o = out + (size_t)col * (size_t)n;
+        const double *xc = x + (size_t)col * (size_t)n;
+        for (int row = 0; row < n; ++row) {
+            o[row] = 0.0;
+        }
+        for (int inner = 0; inner < n; ++inner) {
+            const double *ac = a + (size_t)inner * (size_t)n;
+            double xv = xc[inner];
+            for (int row = 0; row < n; ++row) {
+                o[row] += ac[row] * xv;
+            }
+        }
+    }
+}
+
+ORACLE_API void oracle_matmul(double *out, const double *a, const double *x, int n, int k)
+{
+    oracle_dense_matmul(out, a, x, n, k);
+}
+
+static double oracle_sum_squares(const double *v, size_t count)
+{
+    double s = 0.0;
+    for (size_t i = 0; i < count; ++i) {
+        s += v[i] * v[i];
+    }
+    return s;
+}
+
+/* Plain IPT on a dense column-major matrix.
+ *  - fixed-iteration mode (use_tol = 0): IPT_C_GPU/test_temp/runtests.cu:98-174;
+ *  - tolerance mode (use_tol = 1): the stopping rule of
+ *    IPT_C_GPU/src/ipt_cuda.cu:1883-1932 (||F(X)-X||_F / ||X||_F <= tol, the
+ *    returned block is F(X) of the last step; unconverged after maxiter still
+ *    returns the last block).
+ * The map is X'_ij = (Y_ij - d_i X_ij - X_ij c_j) / (d_j - d_i) with
+ * Y = H X, c_j = Y_jj - d_j X_jj, and X'_jj = 1 (runtests.cu:130-150).
+ * Eigenvalues are (H X)_jj of the returned block (runtests.cu:160-164).
+ * x0 may be NULL (identity start, runtests.cu:122-124).
+ * Returns 0, or -1 on allocation failure, -2 on a zero/non-finite ||X||. */
+ORACLE_API int oracle_ipt_dense(const double *matrix, int n, int k, int maxiter, double tol,
+                                int use_tol, const double *x0, double *vectors_out,
+                                double *values_out, int *iterations_out,
+                                double *fixed_point_residual_out)
+{
+    size_t elems = (size_t)n * (size_t)k;
+    double *x = (double *)calloc(elems, sizeof(double));
+    double *y = (double *)calloc(elems, sizeof(double));
+    double *diag = (double *)calloc((size_t)n, sizeof(double));
+    double *cdiag = (double *)calloc((size_t)k, sizeof(double));
+    int done = 0;
+    int status = 0;
+    double fpres = NAN;
+
+    if (x == NULL || y == NULL || diag == NULL || cdiag == NULL) {
+        free(x); free(y); free(diag); free(cdiag);
+        return -1;
+    }
+    if (x0 != NULL) {
+        memcpy(x, x0, elems * sizeof(double));
+    } else {
+        for (int col = 0; col < k; ++col) {
+            x[(size_t)col + (size_t)col * (size_t)n] = 1.0;
+        }
+    }
+    for (int row = 0; row < n; ++row) {
+        diag[row] = matrix[(size_t)row + (size_t)row * (size_t)n];
+    }
+
+    for (int iter = 0; iter < maxiter; ++iter) {
+        oracle_dense_matmul(y, matrix, x, n, k);
+        for (int col = 0; col < k; ++col) {
+            size_t di = (size_t)col + (size_t)col * (size_t)n;
+            cdiag[col] = y[di] - diag[col] * x[di];
+        }
+#pragma omp parallel for schedule(static)
+        for (int col = 0; col < k; ++col) {
+            for (int row = 0; row < n; ++row) {
+                size_t idx = (size_t)row + (size_t)col * (size_t)n;
+                if (row == col) {
+                    y[idx] = 1.0;
+                } else {
+                    double g = 1.0 / (diag[col] - diag[row]);
+                    y[idx] = (y[idx] - diag[row] * x[idx] - x[idx] * cdiag[col]) * g;
+                }
+            }
+        }
+        done = iter + 1;
+        if (use_tol) {
+            double dsum = 0.0;
+            double xsum = oracle_sum_squares(x, elems);
+            for (size_t i = 0; i < elems; ++i) {
+                double d = y[i] - x[i];
+                dsum += d * d;
+            }
+            if (!(xsum > 0.0) || !isfinite(xsum)) {
+                status = -2;
+                break;
+            }
+            fpres = sqrt(dsum) / sqrt(xsum);
+            {
+                double *t = x; x = y; y = t;
+            }
+            if (fpres <= tol) {
+                break;
+            }
+        } else {
+            double *t = x; x = y; y = t;
+        }
+    }
+
+    if (status == 0) {
+        oracle_dense_matmul(y, matrix, x, n, k);
+        for (int col = 0; col < k; ++col) {
+            values_out[col] = y[(size_t)col + (size_t)col * (size_t)n];
+        }
+        memcpy(vectors_out, x, elems * sizeof(double));
+        if (iterations_out != NULL) {
+            *iterations_out = done;
+        }
+        if (fixed_point_residual_out != NULL) {
+            *fixed_point_residual_out = fpres;
+        }
+    }
+    free(x); free(y); free(diag); free(cdiag);
+    return status;
+}
+
+/* Dense copy of a CSC matrix, duplicates summed:
+ * IPT_C_GPU/test/sparse/runtests_sparse.cu:60-75. */
+ORACLE_API void oracle_csc_to_dense(double *dense, const int *col_ptr, const int *row_ind,
+                                    const double *values, int n)
+{
+    memset(dense, 0, (size_t)n * (size_t)n * sizeof(double));
+    for (int col = 0; col < n; ++col) {
+        for (int p = col_ptr[col]; p < col_ptr[col + 1]; ++p) {
+            int row = row_ind[p];
+            if (row >= 0 && row < n) {
+                dense[(size_t)row + (size_t)col * (size_t)n] += values[p];
+            }
+        }
+    }
+}
+
+/* Scaled residual max_j ||H x_j - v_j x_j|| / (max(1,|v_j|) max(1,||x_j||)):
+ * IPT_C_GPU/test_temp/runtests.cu:191-229. */
+ORACLE_API double oracle_max_relative_residual(const double *matrix, const double *vectors,
+                                               const double *values, int n, int k)
+{
+    double *mx = (double *)calloc((size_t)n * (size_t)k, sizeof(double));
+    double max_residual = 0.0;
+    if (mx == NULL) {
+        return INFINITY;
+    }
+    oracle_dense_matmul(mx, matrix, vectors, n, k);
+    for (int col = 0; col < k; ++col) {
+        double rs = 0.0, vs = 0.0;
+        for (int row = 0; row < n; ++row) {
+            size_t idx = (size_t)row + (size_t)col * (size_t)n;
+            double r = mx[idx] - vectors[idx] * values[col];
+            rs += r * r;
+            vs += vectors[idx] * vectors[idx];
+        }
+        {
+            double denom = fmax(1.0, fabs(values[col])) * fmax(1.0, sqrt(vs));
+            double rel = sqrt(rs) / denom;
+            if (rel > max_residual) {
+                max_residual = rel;
+            }
+        }
+    }
+    free(mx);
+    return max_residual;
+}
+
+/* CSC validation: IPT_C_GPU/src/ipt_preparation.cu:148-169. */
+ORACLE_API int oracle_validate_csc(const int *col_ptr, const int *row_ind, int n, int nnz)
+{
+    if (col_ptr == NULL || (nnz > 0 && row_ind == NULL) || n <= 0 || nnz < 0 ||
+        col_ptr[0] != 0 || col_ptr[n] != nnz) {
+        return 0;
+    }
+    for (int col = 0; col < n; ++col) {
+        if (col_ptr[col] > col_ptr[col + 1]) {
+            return 0;
+        }
+    }
+    for (int p = 0; p < nnz; ++p) {
+        if (row_ind[p] < 0 || row_ind[p] >= n) {
+            return 0;
+        }
+    }
+    return 1;
+}
+
+/* Diagonal of a CSC matrix, first matching entry per column:
+ * IPT_C_GPU/src/ipt_preparation.cu:171-188. */
+ORACLE_API void oracle_csc_diagonal(const int *col_ptr, const int *row_ind, const double *values,
+                                    int n, double *diag)
+{
+    for (int col = 0; col < n; ++col) {
+        diag[col] = 0.0;
+        for (int p = col_ptr[col]; p < col_ptr[col + 1]; ++p) {
+            if (row_ind[p] == col) {
+                diag[col] = values[p];
+                break;
+            }
+        }
+    }
+}
+
+static const double *g_sort_key;
+static int oracle_cmp_perm(const void *a, const void *b)
+{
+    int ia = *(const int *)a, ib = *(const int *)b;
+    double da = g_sort_key[ia], db = g_sort_key[ib];
+    if (da < db) return -1;
+    if (db < da) return 1;
+    return (ia > ib) - (ia < ib); /* ties keep the original order (stable) */
+}
+
+/* Stable ascending sort of the diagonal: IPT_C_GPU/src/ipt_preparation.cu:190-208.
+ * perm[sorted] = original index. */
+ORACLE_API void oracle_stable_sort_permutation(const double *diag, int n, int *perm)
+{
+    for (int i = 0; i < n; ++i) {
+        perm[i] = i;
+    }
+    g_sort_key = diag;
+    qsort(perm, (size_t)n, sizeof(int), oracle_cmp_perm);
+    g_sort_key = NULL;
+}
+
+/* y = H x for H in CSC (any symmetry), x/y column-major n-by-k; scatter over
+ * the stored entries in storage order.  This is the product the reference
+ * asks cuSPARSE for (CSC passed as CSR with OP_T,
+ * IPT_C_GPU/src/ipt_cuda.cu:1535-1559). */
+ORACLE_API void oracle_csc_matmul(const int *col_ptr, const int *row_ind, const double *values,
+                                  int n, const double *x, int k, double *y)
+{
+#pragma omp parallel for schedule(static)
+    for (int j = 0; j < k; ++j) {
+        double *yj = y + (size_t)j * (size_t)n;
+        const double *xj = x + (size_t)j * (size_t)n;
+        for (int r = 0; r < n; ++r) {
+            yj[r] = 0.0;
+        }
+        for (int col = 0; col < n; ++col) {
+            double xv = xj[col];
+            for (int p = col_ptr[col]; p < col_ptr[col + 1]; ++p) {
+                yj[row_ind[p]] += values[p] * xv;
+            }
+        }
+    }
+}
+
+/* y = H x for H in CSR, each row summed in stored order (the gather the CUDA
+ * SpMM performs); x/y column-major n-by-k.  Rows are split between threads. */
+ORACLE_API void oracle_csr_matmul(const int *row_ptr, const int *col_ind, const double *values,
+                                  int n, const double *x, int k, double *y)
+{
+#pragma omp parallel for schedule(dynamic, 256)
+    for (int r = 0; r < n; ++r) {
+        for (int j = 0; j < k; ++j) {
+            const double *xj = x + (size_t)j * (size_t)n;
+            double s = 0.0;
+            for (int p = row_ptr[r]; p < row_ptr[r + 1]; ++p) {
+                s += values[p] * xj[col_ind[p]];
+            }
+            y[(size_t)r + (size_t)j * (size_t)n] = s;
+        }
+    }
+}
+
+/* Plain IPT on a CSR matrix (rows summed in stored order), same map and stop
+ * rule as oracle_ipt_dense; diag must hold the matrix diagonal. */
+ORACLE_API int oracle_ipt_csr(const int *row_ptr, const int *col_ind, const double *values,
+                              const double *diag, int n, int k, int maxiter, double tol,
+                              int use_tol, const double *x0, double *vectors_out,
+                              double *values_out, int *iterations_out,
+                              double *fixed_point_residual_out)
+{
+    size_t elems = (size_t)n * (size_t)k;
+    double *x = (double *)calloc(elems, sizeof(double));
+    double *y = (double *)calloc(elems, sizeof(double));
+    double *cdiag = (double *)calloc((size_t)k, sizeof(double));
+    int done = 0;
+    int status = 0;
+    double fpres = NAN;
+
+    if (x == NULL || y == NULL || cdiag == NULL) {
+        free(x); free(y); free(cdiag);
+        return -1;
+    }
+    if (x0 != NULL) {
+        memcpy(x, x0, elems * sizeof(double));
+    } else {
+        for (int col = 0; col < k; ++col) {
+            x[(size_t)col + (size_t)col * (size_t)n] = 1.0;
+        }
+    }
+    for (int iter = 0; iter < maxiter; ++iter) {
+        oracle_csr_matmul(row_ptr, col_ind, values, n, x, k, y);
+        for (int col = 0; col < k; ++col) {
+            size_t di = (size_t)col + (size_t)col * (size_t)n;
+            cdiag[col] = y[di] - diag[col] * x[di];
+        }
+#pragma omp parallel for schedule(static)
+        for (int col = 0; col < k; ++col) {
+            for (int row = 0; row < n; ++row) {
+                size_t idx = (size_t)row + (size_t)col * (size_t)n;
+                if (row == col) {
+                    y[idx] = 1.0;
+                } else {
+                    double g = 1.0 / (diag[col] - diag[row]);
+                    y[idx] = (y[idx] - diag[row] * x[idx] - x[idx] * cdiag[col]) * g;
+                }
+            }
+        }
+        done = iter + 1;
+        if (use_tol) {
+            double dsum = 0.0;
+            double xsum = oracle_sum_squares(x, elems);
+            for (size_t i = 0; i < elems; ++i) {
+                double d = y[i] - x[i];
+                dsum += d * d;
+            }
+            if (!(xsum > 0.0) || !isfinite(xsum)) {
+                status = -2;
+                break;
+            }
+            fpres = sqrt(dsum) / sqrt(xsum);
+            {
+                double *t = x; x = y; y = t;
+            }
+            if (fpres <= tol) {
+                break;
+            }
+        } else {
+            double *t = x; x = y; y = t;
+        }
+    }
+    if (status == 0) {
+        oracle_csr_matmul(row_ptr, col_ind, values, n, x, k, y);
+        for (int col = 0; col < k; ++col) {
+            values_out[col] = y[(size_t)col + (size_t)col * (size_t)n];
+        }
+        memcpy(vectors_out, x, elems * sizeof(double));
+        if (iterations_out != NULL) {
+            *iterations_out = done;
+        }
+        if (fixed_point_residual_out != NULL) {
+            *fixed_point_residual_out = fpres;
+        }
+    }
+    free(x); free(y); free(cdiag);
+    return status;
+}
+
+ORACLE_API int oracle_num_threads(void)
+{
+#ifdef _OPENMP
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
+}

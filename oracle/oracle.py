@@ -1,0 +1,238 @@
+"""Python access to the CPU oracle (TEST INFRASTRUCTURE ONLY).
+
+The oracle is the checker of the CUDA solver and the CPU baseline of
+bench.py; the product (block_ipt_gb300) never imports it.  It offers:
+
+  * the C restatement of the reference IPT path (oracle/ipt_oracle.c, built
+    into oracle/_build/liboracle.so), each function citing the reference;
+  * the reference's own CPU test code compiled from its sources into
+    oracle/_ref/ (only where the reference tree exists, see build_ref.py);
+  * FP64 numpy references for the block path: CholQR, Rayleigh-Ritz and the
+    LAPACK (scipy) dsyevd eigenpairs used as the eigen-oracle.
+"""
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "_build", "liboracle.so")
+REF_DENSE = os.path.join(HERE, "_ref", "libref_dense.so")
+REF_SPARSE = os.path.join(HERE, "_ref", "libref_sparse.so")
+
+_lib = None
+_ref = {}
+
+
+def build():
+    """Compile the C oracle (make -C oracle)."""
+    subprocess.run(["make", "-s", "-C", HERE], check=True)
+    return LIB
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB):
+            build()
+        L = C.CDLL(LIB)
+        vp, i, d = C.c_void_p, C.c_int, C.c_double
+        L.oracle_deterministic_noise.restype = d
+        L.oracle_deterministic_noise.argtypes = [i, i]
+        L.oracle_fill_perturbative_matrix.argtypes = [vp, i, i]
+        L.oracle_build_banded_csc.restype = i
+        L.oracle_build_banded_csc.argtypes = [i, vp, vp, vp]
+        L.oracle_ipt_dense.restype = i
+        L.oracle_ipt_dense.argtypes = [vp, i, i, i, d, i, vp, vp, vp, vp, vp]
+        L.oracle_ipt_csr.restype = i
+        L.oracle_ipt_csr.argtypes = [vp, vp, vp, vp, i, i, i, d, i, vp, vp, vp, vp, vp]
+        L.oracle_matmul.argtypes = [vp, vp, vp, i, i]
+        L.oracle_csc_to_dense.argtypes = [vp, vp, vp, vp, i]
+        L.oracle_max_relative_residual.restype = d
+        L.oracle_max_relative_residual.argtypes = [vp, vp, vp, i, i]
+        L.oracle_validate_csc.restype = i
+        L.oracle_validate_csc.argtypes = [vp, vp, i, i]
+        L.oracle_csc_diagonal.argtypes = [vp, vp, vp, i, vp]
+        L.oracle_stable_sort_permutation.argtypes = [vp, i, vp]
+        L.oracle_csc_matmul.argtypes = [vp, vp, vp, i, vp, i, vp]
+        L.oracle_csr_matmul.argtypes = [vp, vp, vp, i, vp, i, vp]
+        L.oracle_num_threads.restype = i
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    return None if a is None else C.c_void_p(a.ctypes.data)
+
+
+# ---- reference test inputs -------------------------------------------------
+def perturbative_matrix(n, symmetric):
+    """IPT_C_GPU/test_temp/runtests.cu:60-80."""
+    H = np.zeros((n, n), dtype=np.float64, order="F")
+    lib().oracle_fill_perturbative_matrix(_p(H), n, int(symmetric))
+    return H
+
+
+def banded_csc(n):
+    """IPT_C_GPU/test/sparse/runtests_sparse.cu:224-268."""
+    nnz = n + 2 * (n - 1)
+    cp = np.zeros(n + 1, dtype=np.int32)
+    ri = np.zeros(nnz, dtype=np.int32)
+    va = np.zeros(nnz, dtype=np.float64)
+    got = lib().oracle_build_banded_csc(n, _p(cp), _p(ri), _p(va))
+    assert got == nnz
+    return cp, ri, va
+
+
+def csc_to_dense(cp, ri, va, n):
+    H = np.zeros((n, n), dtype=np.float64, order="F")
+    lib().oracle_csc_to_dense(_p(H), _p(np.ascontiguousarray(cp, np.int32)),
+                              _p(np.ascontiguousarray(ri, np.int32)),
+                              _p(np.ascontiguousarray(va, np.float64)), n)
+    return H
+
+
+# ---- plain IPT ---------------------------------------------------------------
+def ipt_dense(H, k, maxiter, tol=0.0, use_tol=False, x0=None):
+    """Plain IPT (runtests.cu:98-174; tolerance rule of ipt_cuda.cu:1883-1932).
+    Returns (vectors n x k, values k, iterations, fixed_point_residual)."""
+    H = np.asfortranarray(H, dtype=np.float64)
+    n = H.shape[0]
+    X = np.zeros((n, k), dtype=np.float64, order="F")
+    v = np.zeros(k, dtype=np.float64)
+    it = C.c_int(0)
+    fp = C.c_double(0.0)
+    x0a = None if x0 is None else np.asfortranarray(x0, dtype=np.float64)
+    st = lib().oracle_ipt_dense(_p(H), n, k, maxiter, float(tol), int(use_tol), _p(x0a), _p(X),
+                                _p(v), C.byref(it), C.byref(fp))
+    if st != 0:
+        raise RuntimeError("oracle_ipt_dense failed: %d" % st)
+    return X, v, it.value, fp.value
+
+
+def ipt_csr(row_ptr, col_ind, vals, diag, n, k, maxiter, tol=0.0, use_tol=False, x0=None):
+    rp = np.ascontiguousarray(row_ptr, np.int32)
+    ci = np.ascontiguousarray(col_ind, np.int32)
+    va = np.ascontiguousarray(vals, np.float64)
+    dg = np.ascontiguousarray(diag, np.float64)
+    X = np.zeros((n, k), dtype=np.float64, order="F")
+    v = np.zeros(k, dtype=np.float64)
+    it = C.c_int(0)
+    fp = C.c_double(0.0)
+    x0a = None if x0 is None else np.asfortranarray(x0, dtype=np.float64)
+    st = lib().oracle_ipt_csr(_p(rp), _p(ci), _p(va), _p(dg), n, k, maxiter, float(tol),
+                              int(use_tol), _p(x0a), _p(X), _p(v), C.byref(it), C.byref(fp))
+    if st != 0:
+        raise RuntimeError("oracle_ipt_csr failed: %d" % st)
+    return X, v, it.value, fp.value
+
+
+def max_relative_residual(H, X, v):
+    """IPT_C_GPU/test_temp/runtests.cu:191-229."""
+    H = np.asfortranarray(H, dtype=np.float64)
+    X = np.asfortranarray(X, dtype=np.float64)
+    v = np.ascontiguousarray(v, dtype=np.float64)
+    return lib().oracle_max_relative_residual(_p(H), _p(X), _p(v), H.shape[0], X.shape[1])
+
+
+def prepare_sorted_csc(cp, ri, va, n):
+    """Stable diagonal sort + symmetric permutation with duplicate merge and
+    zero drop (IPT_C_GPU/src/ipt_preparation.cu:190-262, 1375-1431).
+    Returns (row_ptr, col_ind, vals) as CSR of the sorted matrix, the summed
+    sorted diagonal, and perm (perm[sorted] = original)."""
+    cp = np.ascontiguousarray(cp, np.int32)
+    ri = np.ascontiguousarray(ri, np.int32)
+    va = np.ascontiguousarray(va, np.float64)
+    diag = np.zeros(n)
+    lib().oracle_csc_diagonal(_p(cp), _p(ri), _p(va), n, _p(diag))
+    perm = np.zeros(n, dtype=np.int32)
+    lib().oracle_stable_sort_permutation(_p(diag), n, _p(perm))
+    inv = np.empty(n, dtype=np.int64)
+    inv[perm] = np.arange(n)
+    cols = np.repeat(np.arange(n), np.diff(cp))
+    nr = inv[ri]
+    nc = inv[cols]
+    A = {}
+    for r, c, v in zip(nr.tolist(), nc.tolist(), va.tolist()):
+        A[(r, c)] = A.get((r, c), 0.0) + v
+    keys = sorted(k for k, v in A.items() if v != 0.0 or (perm == np.arange(n)).all())
+    rp = np.zeros(n + 1, dtype=np.int32)
+    for r, _ in keys:
+        rp[r + 1] += 1
+    rp = np.cumsum(rp).astype(np.int32)
+    ci = np.array([c for _, c in keys], dtype=np.int32)
+    vv = np.array([A[k] for k in keys], dtype=np.float64)
+    d = np.zeros(n)
+    for (r, c), v in A.items():
+        if r == c:
+            d[r] += v
+    return rp, ci, vv, d, perm
+
+
+# ---- FP64 eigen-oracle and block references ------------------------------------
+def eigh_lowest(H, k):
+    """LAPACK (scipy) symmetric eigensolver: k lowest pairs, ascending."""
+    import scipy.linalg as sl
+    w, V = sl.eigh(np.asarray(H, dtype=np.float64), subset_by_index=[0, k - 1], driver="evr")
+    return w, V
+
+
+def dsyevd_lowest(H, k):
+    """LAPACK dsyevd (divide and conquer), full spectrum, the k lowest."""
+    from scipy.linalg import lapack
+    w, V, info = lapack.dsyevd(np.asarray(H, dtype=np.float64), compute_v=1, lower=1)
+    if info != 0:
+        raise RuntimeError("dsyevd info=%d" % info)
+    return w[:k], V[:, :k]
+
+
+def cholqr(X):
+    """CholQR: X = Q R with R from the FP64 Gram matrix."""
+    G = X.T @ X
+    R = np.linalg.cholesky(G).T
+    return np.linalg.solve(R.T, X.T).T
+
+
+def rayleigh_ritz(H, V, k):
+    """Ritz pairs of H on span(V) (V orthonormal): ascending values."""
+    T = V.T @ (H @ V)
+    T = 0.5 * (T + T.T)
+    w, Z = np.linalg.eigh(T)
+    return w[:k], V @ Z[:, :k]
+
+
+def scaled_residuals(H_apply, X, w, hnorm):
+    """||H x_j - w_j x_j|| / (max(1,||H||_inf) max(1,||x_j||))
+    (IPT_C_GPU/src/ipt_cuda.cu:2684-2697)."""
+    R = H_apply(X) - X * w[None, :]
+    return np.linalg.norm(R, axis=0) / (max(1.0, hnorm) * np.maximum(1.0, np.linalg.norm(X, axis=0)))
+
+
+# ---- the reference's own compiled CPU code (checker only) -------------------------
+def ref_available():
+    return os.path.exists(REF_DENSE) and os.path.exists(REF_SPARSE)
+
+
+def ref_lib(which):
+    if which not in _ref:
+        path = REF_DENSE if which == "dense" else REF_SPARSE
+        L = C.CDLL(path)
+        vp, i = C.c_void_p, C.c_int
+        if which == "dense":
+            L.ref_ipt_cpu_reference.restype = i
+            L.ref_ipt_cpu_reference.argtypes = [vp, i, i, i, vp, vp]
+            L.ref_fill_perturbative_matrix.argtypes = [vp, i, i]
+            L.ref_result_layout.restype = i
+            L.ref_result_layout.argtypes = [vp, i]
+        else:
+            L.ref_sparse_ipt_cpu_reference.restype = i
+            L.ref_sparse_ipt_cpu_reference.argtypes = [vp, i, i, i, vp, vp]
+            L.ref_build_banded_csc.restype = i
+            L.ref_build_banded_csc.argtypes = [i, vp, vp, vp]
+            L.ref_h20_w_csc.restype = i
+            L.ref_h20_w_csc.argtypes = [vp, vp, vp]
+            L.ref_prepare_sparse_csc_sorted.restype = i
+            L.ref_prepare_sparse_csc_sorted.argtypes = [vp, vp, vp, i, i, i, vp, vp, vp, vp, vp]
+        _ref[which] = L
+    return _ref[which]
