@@ -178,6 +178,15 @@ SIGNATURES = [
                                         C.POINTER(_vp)]),
     ("ipt_cuda_sparse_csc_device_tol", _i, [_vp, _vp, _vp, _i, _i, _i, _d, _i, _vp,
                                             C.POINTER(_vp), C.POINTER(_vp), _ip, _dp]),
+    ("ipt_mixed_precision_cuda_device_tol", _i, [_vp, _i, _i, _d, _i, _d, _i, _vp,
+                                                 C.POINTER(_MixedResult)]),
+    ("ipt_mixed_precision_fp32_cuda_device_tol", _i, [_vp, _i, _i, _d, _i, _d, _i, _vp,
+                                                      C.POINTER(_MixedResult)]),
+    ("ipt_mixed_precision_tf32_cuda_device_tol", _i, [_vp, _i, _i, _d, _i, _d, _i, _vp,
+                                                      C.POINTER(_MixedResult)]),
+    ("ipt_mixed_precision_cuda_free_device_result", None, [C.POINTER(_MixedResult)]),
+    ("ipt_mixed_precision_fp32_cuda_free_device_result", None, [C.POINTER(_MixedResult)]),
+    ("ipt_mixed_precision_tf32_cuda_free_device_result", None, [C.POINTER(_MixedResult)]),
     ("ipt_block_default_options", None, [C.POINTER(IPTBlockOptions)]),
     ("ipt_block_solve_dense_device", _i, [_vp, _i, _i, C.POINTER(IPTBlockOptions), _vp, _vp,
                                           C.POINTER(IPTBlockReport)]),

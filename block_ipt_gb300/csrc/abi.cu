@@ -166,6 +166,18 @@ void reset_result_head(IPTCudaResult *result)
 
 }  // namespace
 
+namespace iptgb {
+// FP64 dense IPT loop on device buffers (shared with the mixed entry points).
+int dense_plain_device_entry(const double *dH, int n, int k, const double *dX0, int maxiter,
+                             double tol, int use_tol, double *X_out, double *values_out,
+                             int *iterations_done, double *fixed_point_residual,
+                             cudaStream_t stream)
+{
+    return dense_plain_device(dH, n, k, dX0, maxiter, tol, use_tol, X_out, values_out,
+                              iterations_done, fixed_point_residual, stream);
+}
+}  // namespace iptgb
+
 // ---------------------------------------------------------------------------
 // Utilities (IPT_C_GPU/src/ipt_cuda.cu:375-483)
 // ---------------------------------------------------------------------------

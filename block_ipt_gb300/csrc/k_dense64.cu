@@ -22,25 +22,25 @@ namespace iptgb {
 constexpr int kD64Rows = 256;
 constexpr int kD64Chunk = 32;
 
-template <int BN>
+template <typename T, int BN>
 __global__ void __launch_bounds__(kD64Rows)
-dense64_partial_kernel(const double *__restrict__ H, int n, long long ldh,
-                       const double *__restrict__ X, long long ldx, int k,
-                       double *__restrict__ P, int kslice)
+dense64_partial_kernel(const T *__restrict__ H, int n, long long ldh,
+                       const T *__restrict__ X, long long ldx, int k,
+                       T *__restrict__ P, int kslice)
 {
-    __shared__ double xs[kD64Chunk][BN];
+    __shared__ T xs[kD64Chunk][BN];
     const int row = blockIdx.x * kD64Rows + threadIdx.x;
     const int s = blockIdx.y;
     const int c0 = blockIdx.z * BN;
     const int kbeg = s * kslice;
     const int kend = min(n, kbeg + kslice);
-    double acc[BN];
+    T acc[BN];
 #pragma unroll
     for (int j = 0; j < BN; ++j) {
-        acc[j] = 0.0;
+        acc[j] = T(0);
     }
     const bool active = row < n;
-    const double *hrow = H + (active ? row : 0);
+    const T *hrow = H + (active ? row : 0);
 
     for (int l0 = kbeg; l0 < kend; l0 += kD64Chunk) {
         const int lc = min(kD64Chunk, kend - l0);
@@ -48,7 +48,7 @@ dense64_partial_kernel(const double *__restrict__ H, int n, long long ldh,
         for (int e = threadIdx.x; e < kD64Chunk * BN; e += kD64Rows) {
             const int ll = e % kD64Chunk;
             const int j = e / kD64Chunk;
-            double v = 0.0;
+            T v = T(0);
             if (ll < lc && c0 + j < k) {
                 v = X[(size_t)(l0 + ll) + (size_t)(c0 + j) * (size_t)ldx];
             }
@@ -56,9 +56,9 @@ dense64_partial_kernel(const double *__restrict__ H, int n, long long ldh,
         }
         __syncthreads();
         if (active) {
-            const double *hp = hrow + (size_t)l0 * (size_t)ldh;
+            const T *hp = hrow + (size_t)l0 * (size_t)ldh;
             if (lc == kD64Chunk) {
-                double h[kD64Chunk];
+                T h[kD64Chunk];
 #pragma unroll
                 for (int ll = 0; ll < kD64Chunk; ++ll) {
                     h[ll] = __ldg(hp + (size_t)ll * (size_t)ldh);
@@ -72,7 +72,7 @@ dense64_partial_kernel(const double *__restrict__ H, int n, long long ldh,
                 }
             } else {
                 for (int ll = 0; ll < lc; ++ll) {
-                    const double h = __ldg(hp + (size_t)ll * (size_t)ldh);
+                    const T h = __ldg(hp + (size_t)ll * (size_t)ldh);
 #pragma unroll
                     for (int j = 0; j < BN; ++j) {
                         acc[j] = fma(h, xs[ll][j], acc[j]);
@@ -113,8 +113,9 @@ int dense64_split_for(int n, int k, int sms)
     return want;
 }
 
-int launch_dense64_partial(const double *H, int n, long long ldh, const double *X,
-                           long long ldx, int k, double *P, int S, cudaStream_t stream)
+template <typename T>
+static int launch_partial_t(const T *H, int n, long long ldh, const T *X, long long ldx, int k,
+                            T *P, int S, cudaStream_t stream)
 {
     int kslice = (n + S - 1) / S;
     kslice = ((kslice + kD64Chunk - 1) / kD64Chunk) * kD64Chunk;
@@ -123,20 +124,34 @@ int launch_dense64_partial(const double *H, int n, long long ldh, const double *
     dim3 grid(row_blocks, S, (k + bn - 1) / bn);
     switch (bn) {
     case 4:
-        dense64_partial_kernel<4><<<grid, kD64Rows, 0, stream>>>(H, n, ldh, X, ldx, k, P, kslice);
+        dense64_partial_kernel<T, 4><<<grid, kD64Rows, 0, stream>>>(H, n, ldh, X, ldx, k, P, kslice);
         break;
     case 8:
-        dense64_partial_kernel<8><<<grid, kD64Rows, 0, stream>>>(H, n, ldh, X, ldx, k, P, kslice);
+        dense64_partial_kernel<T, 8><<<grid, kD64Rows, 0, stream>>>(H, n, ldh, X, ldx, k, P, kslice);
         break;
     case 16:
-        dense64_partial_kernel<16><<<grid, kD64Rows, 0, stream>>>(H, n, ldh, X, ldx, k, P, kslice);
+        dense64_partial_kernel<T, 16><<<grid, kD64Rows, 0, stream>>>(H, n, ldh, X, ldx, k, P, kslice);
         break;
     default:
-        dense64_partial_kernel<32><<<grid, kD64Rows, 0, stream>>>(H, n, ldh, X, ldx, k, P, kslice);
+        dense64_partial_kernel<T, 32><<<grid, kD64Rows, 0, stream>>>(H, n, ldh, X, ldx, k, P, kslice);
         break;
     }
     IPTGB_LAUNCH();
     return IPT_CUDA_SUCCESS;
+}
+
+int launch_dense64_partial(const double *H, int n, long long ldh, const double *X,
+                           long long ldx, int k, double *P, int S, cudaStream_t stream)
+{
+    return launch_partial_t<double>(H, n, ldh, X, ldx, k, P, S, stream);
+}
+
+// FP32 SIMT variant of the same split-K product (the reference's FP32
+// "pedantic" GemmEx path, IPT_C_GPU/src/mixed_precision/ipt_mixed_precision_cuda.cu:802-815).
+int launch_dense32_partial(const float *H, int n, long long ldh, const float *X, long long ldx,
+                           int k, float *P, int S, cudaStream_t stream)
+{
+    return launch_partial_t<float>(H, n, ldh, X, ldx, k, P, S, stream);
 }
 
 // ---------------------------------------------------------------------------

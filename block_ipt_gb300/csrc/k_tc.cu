@@ -172,8 +172,8 @@ tc_partial_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
                   int *err)
 {
     extern __shared__ uint8_t smem_raw[];
-    uint8_t *smem =
-        reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    // 1024-byte alignment of the shared-window address (SWIZZLE_128B atoms)
+    uint8_t *smem = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
     const uint32_t a_bytes = kBM * kRowBytes;
     const uint32_t b_bytes = (uint32_t)p_pad * kRowBytes;
     const uint32_t stage_bytes = a_bytes + b_bytes;
@@ -303,6 +303,11 @@ tc_partial_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
 
 }  // namespace tc
 
+// FP32 storage of a TF32 tensor-core operand (values pre-rounded to TF32).
+struct tf32_t {
+    float v;
+};
+
 // ---------------------------------------------------------------------------
 // Delta conversion: out[i * ldp + l] = lp(scale * H[i, l]) for l != i, 0 on the
 // diagonal and in the padding columns.  H column-major (ld = n).  32x32 tiles
@@ -323,11 +328,18 @@ __device__ __forceinline__ __nv_bfloat16 to_lp<__nv_bfloat16>(float v)
 template <>
 __device__ __forceinline__ float to_lp<float>(float v)
 {
+    return v;
+}
+template <>
+__device__ __forceinline__ tf32_t to_lp<tf32_t>(float v)
+{
     // TF32 operand: round to nearest into the 10-bit mantissa kept by the
     // tensor core (cvt.rna.tf32.f32 returns the rounded value in fp32 bits).
     uint32_t r;
     asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(v));
-    return __uint_as_float(r);
+    tf32_t t;
+    t.v = __uint_as_float(r);
+    return t;
 }
 
 template <typename LP>
@@ -531,7 +543,7 @@ struct LowpTypes<__nv_bfloat16> {
     static constexpr int kind = kLowpBF16;
 };
 template <>
-struct LowpTypes<float> {
+struct LowpTypes<tf32_t> {
     static constexpr CUtensorMapDataType dt = CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
     static constexpr int kind = kLowpTF32;
 };
@@ -678,6 +690,7 @@ struct LowpDense final : LowpDenseOperator {
     int num_splits() const override { return splits; }
 
     int sms = 148;
+    int n = 0;
     int ldp = 0, p = 0, p_pad = 0, tmem_cols = 32, chunks_total = 0, chunks_per_split = 0;
     int splits = 1, stages = 2, cur = 0;
     size_t smem_bytes = 0;
@@ -692,6 +705,105 @@ struct LowpDense final : LowpDenseOperator {
     CUtensorMap mapA, mapB[2];
 };
 
+// FP32 SIMT operator (no tensor cores): Delta kept column-major in FP32 and
+// multiplied with the FP32 split-K kernel; the update shares the kernel
+// above with exact FP32 operand copies.
+__global__ void convert_delta_f32_colmajor_kernel(const double *__restrict__ H, int n,
+                                                  float *__restrict__ out)
+{
+    const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= (size_t)n * n) return;
+    const size_t i = e % (size_t)n;
+    const size_t l = e / (size_t)n;
+    out[e] = i == l ? 0.0f : (float)H[e];
+}
+
+struct LowpDenseSimtF32 final : LowpDenseOperator {
+    int init(const double *dH, int n_, cudaStream_t s_)
+    {
+        n = n_;
+        s = s_;
+        sms = 148;
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        IPTGB_CHECK(delta.alloc((size_t)n * n, s));
+        convert_delta_f32_colmajor_kernel<<<blocks_for((size_t)n * n), kThreads, 0, s>>>(dH, n,
+                                                                                      delta.ptr);
+        IPTGB_LAUNCH();
+        IPTGB_CHECK(err.alloc(1, s));
+        IPTGB_CUDA(cudaMemsetAsync(err.ptr, 0, sizeof(int), s));
+        return IPT_CUDA_SUCCESS;
+    }
+    int set_width(int p_) override
+    {
+        p = p_;
+        splits = dense64_split_for(n, p, sms);
+        IPTGB_CHECK(P.alloc((size_t)splits * p * n, s));
+        for (int b = 0; b < 2; ++b) {
+            IPTGB_CHECK(X32[b].alloc((size_t)n * p, s));
+        }
+        IPTGB_CHECK(G.alloc((size_t)n * p, s));
+        cur = 0;
+        return IPT_CUDA_SUCCESS;
+    }
+    int reset_identity(const double *d) override
+    {
+        build_g32_kernel<<<blocks_for((size_t)n * p), kThreads, 0, s>>>(d, n, p, G.ptr);
+        IPTGB_LAUNCH();
+        lowp_identity_kernel<float><<<blocks_for((size_t)n * p), kThreads, 0, s>>>(
+            X32[0].ptr, X32[0].ptr, n, p, n);
+        IPTGB_LAUNCH();
+        cur = 0;
+        return IPT_CUDA_SUCCESS;
+    }
+    int product() override
+    {
+        return launch_dense32_partial(delta.ptr, n, n, X32[cur].ptr, n, p, P.ptr, splits, s);
+    }
+    int step(int want_norms, NormScratch *ns) override
+    {
+        IPTGB_CHECK(product());
+        const size_t elems = (size_t)n * p;
+        const int grid = blocks_for(elems);
+        if (want_norms && grid > ns->capacity) return IPT_CUDA_INVALID_ARGUMENT;
+        const int nxt = cur ^ 1;
+        lowp_update_kernel<float><<<grid, kThreads, 0, s>>>(
+            P.ptr, splits, n, p, 1.0f, G.ptr, X32[cur].ptr, X32[nxt].ptr, X32[nxt].ptr, n,
+            want_norms, ns->partials, ns->counter, ns->norms);
+        IPTGB_LAUNCH();
+        cur = nxt;
+        return IPT_CUDA_SUCCESS;
+    }
+    int read_error(int *host_err) override
+    {
+        IPTGB_CUDA(cudaMemcpyAsync(host_err, err.ptr, sizeof(int), cudaMemcpyDeviceToHost, s));
+        return IPT_CUDA_SUCCESS;
+    }
+    int export_fp64(double *X) override
+    {
+        f32_to_f64_kernel<<<blocks_for((size_t)n * p), kThreads, 0, s>>>(X32[cur].ptr,
+                                                                         (size_t)n * p, X);
+        IPTGB_LAUNCH();
+        return IPT_CUDA_SUCCESS;
+    }
+    int export_fp64_prev(double *X) override
+    {
+        f32_to_f64_kernel<<<blocks_for((size_t)n * p), kThreads, 0, s>>>(X32[cur ^ 1].ptr,
+                                                                         (size_t)n * p, X);
+        IPTGB_LAUNCH();
+        return IPT_CUDA_SUCCESS;
+    }
+    const float *partials() const override { return P.ptr; }
+    int num_splits() const override { return splits; }
+
+    int n = 0, p = 0, sms = 148, splits = 1, cur = 0;
+    cudaStream_t s = nullptr;
+    DeviceBuffer<float> delta, G, P;
+    DeviceBuffer<float> X32[2];
+    DeviceBuffer<int> err;
+};
+
 LowpDenseOperator *make_lowp_dense_operator(const double *dH, int n, int kind, cudaStream_t s,
                                             int *status)
 {
@@ -699,7 +811,7 @@ LowpDenseOperator *make_lowp_dense_operator(const double *dH, int n, int kind, c
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev);
     cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, dev);
-    if (major != 10 || encode_fn() == nullptr) {
+    if (kind != kLowpF32 && (major != 10 || encode_fn() == nullptr)) {
         fprintf(stderr, "ipt_gb300: tensor-core IPT stage needs an sm_103 (GB300) device\n");
         *status = IPT_CUDA_CUDA_ERROR;
         return nullptr;
@@ -715,7 +827,11 @@ LowpDenseOperator *make_lowp_dense_operator(const double *dH, int n, int kind, c
         op.reset(o);
         st = o->init(dH, n, s);
     } else if (kind == kLowpTF32) {
-        auto *o = new LowpDense<float>();
+        auto *o = new LowpDense<tf32_t>();
+        op.reset(o);
+        st = o->init(dH, n, s);
+    } else if (kind == kLowpF32) {
+        auto *o = new LowpDenseSimtF32();
         op.reset(o);
         st = o->init(dH, n, s);
     }

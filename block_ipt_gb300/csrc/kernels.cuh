@@ -18,6 +18,8 @@ struct NormScratch {
 int dense64_split_for(int n, int k, int sms);
 int launch_dense64_partial(const double *H, int n, long long ldh, const double *X,
                            long long ldx, int k, double *P, int S, cudaStream_t stream);
+int launch_dense32_partial(const float *H, int n, long long ldh, const float *X, long long ldx,
+                           int k, float *P, int S, cudaStream_t stream);
 int launch_sum_partials(const double *P, int S, size_t elems, double *Y, cudaStream_t stream);
 int launch_dense64_update(const double *P, int S, int n, int k, const double *X,
                           const double *d, double *Xn, int want_norms, NormScratch *ns,

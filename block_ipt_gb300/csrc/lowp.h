@@ -1,0 +1,38 @@
+// lowp.h - low-precision (tensor-core) dense IPT operator (internal).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "ipt_plain.h"
+#include "kernels.cuh"
+
+namespace iptgb {
+
+// Operand formats of the tensor-core product.
+enum { kLowpF16 = 0, kLowpBF16 = 1, kLowpTF32 = 2, kLowpF32 = 3 };
+
+// The IPT map X' = E + G o (Delta X - X diag(Delta X)) with Delta X on the
+// tensor cores.  The block lives inside the operator as an FP32 master copy
+// plus the low-precision operand copy; set_width() sizes it, reset_identity()
+// starts from the unit vectors of the first p diagonal positions.
+struct LowpDenseOperator {
+    virtual ~LowpDenseOperator() = default;
+    virtual int set_width(int p) = 0;
+    virtual int reset_identity(const double *d) = 0;
+    virtual int product() = 0;                               // partials of Delta X only
+    virtual int step(int want_norms, NormScratch *ns) = 0;   // product + update
+    virtual int read_error(int *host_err) = 0;               // async copy of the error flag
+    virtual int export_fp64(double *X) = 0;                  // current block -> FP64
+    virtual int export_fp64_prev(double *X) = 0;             // previous block -> FP64
+    virtual const float *partials() const = 0;               // [split][col][row] FP32
+    virtual int num_splits() const = 0;
+};
+
+LowpDenseOperator *make_lowp_dense_operator(const double *dH, int n, int kind, cudaStream_t s,
+                                            int *status);
+
+int run_lowp_ipt(LowpDenseOperator &op, int n, int p, int maxiter, double tol, int check_every,
+                 double *X, int *iterations, double *fpres_out, long long *matvecs,
+                 cudaStream_t s, bool guard);
+
+}  // namespace iptgb

@@ -1,0 +1,115 @@
+"""GPU parity of the tensor-core (tcgen05/TMA) low-precision IPT stage and of
+the mixed-precision solvers, through the C ABI.
+
+Tolerances: a low-precision IPT iterate differs from the FP64 iterate by the
+operand rounding (FP16 2^-11, BF16 2^-8, TF32 2^-11 relative per entry), so
+after a few iterations max|X_lp - X_64| <= 5e-3 (FP16/TF32) and 3e-2 (BF16)
+times max|X|.  After FP64 refinement / Davidson the results meet the FP64
+bars: 1e-9 on refined IPT vectors, |dlambda| <= 1e-10 ||H||, scaled residual
+<= 1e-8.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from block_ipt_gb300 import _lib, api, workloads
+from oracle import oracle
+
+pytestmark = pytest.mark.gpu
+
+KINDS = {"fp16": ("ipt_mixed_precision_cuda_device_tol", 5e-3),
+         "fp32": ("ipt_mixed_precision_fp32_cuda_device_tol", 1e-5),
+         "tf32": ("ipt_mixed_precision_tf32_cuda_device_tol", 5e-3)}
+FREE = {"fp16": "ipt_mixed_precision_cuda_free_device_result",
+        "fp32": "ipt_mixed_precision_fp32_cuda_free_device_result",
+        "tf32": "ipt_mixed_precision_tf32_cuda_free_device_result"}
+
+
+def run_mixed(torch, H, k, kind, lp_tol, lp_maxiter, fp64_tol, fp64_maxiter):
+    from tests.conftest import device_to_host
+    lib = _lib.load()
+    n = H.shape[0]
+    dH = torch.from_numpy(np.asfortranarray(H).T.copy()).cuda()
+    res = _lib._MixedResult()
+    fn = getattr(lib, KINDS[kind][0])
+    st = fn(C.c_void_p(dH.data_ptr()), n, k, lp_tol, lp_maxiter, fp64_tol, fp64_maxiter,
+            C.c_void_p(torch.cuda.current_blas_handle()), C.byref(res))
+    assert st == 0, _lib.status_string(st)
+    torch.cuda.synchronize()
+    X = np.zeros((n, k), order="F")
+    v = np.zeros(k)
+    device_to_host(C.c_void_p(res.d_vectors), X)
+    device_to_host(C.c_void_p(res.d_values), v)
+    info = {"lowp_iterations": res.lowp_iterations, "fp64_iterations": res.fp64_iterations,
+            "lowp_fpres": res.lowp_fixed_point_residual, "fp64_fpres": res.fp64_fixed_point_residual,
+            "lowp_time": res.lowp_time_sec, "fp64_time": res.fp64_time_sec}
+    getattr(lib, FREE[kind])(C.byref(res))
+    assert not res.d_vectors
+    return X, v, info
+
+
+@pytest.mark.parametrize("kind", ["fp16", "tf32", "fp32"])
+@pytest.mark.parametrize("n,k", [(256, 8), (1000, 5), (777, 40)])
+def test_lowp_iterates_track_fp64(cuda, kind, n, k):
+    """m low-precision steps + one FP64 step vs m+1 FP64 steps."""
+    H, _ = workloads.dense_config0(n, seed=11, sigma=0.05)
+    m = 4
+    X, v, info = run_mixed(cuda, H, k, kind, 1e-300, m, 1e300, 1)
+    assert info["lowp_iterations"] == m and info["fp64_iterations"] == 1
+    Xo, vo, _, _ = oracle.ipt_dense(H, k, m + 1)
+    tol = KINDS[kind][1]
+    err = np.abs(X - Xo).max() / np.abs(Xo).max()
+    assert err <= tol, err
+
+
+@pytest.mark.parametrize("kind", ["fp16", "tf32", "fp32"])
+def test_mixed_converges_to_fp64_fixed_point(cuda, kind):
+    H = oracle.perturbative_matrix(96, 1)
+    X, v, info = run_mixed(cuda, H, 16, kind, 1e-3, 100, 1e-12, 300)
+    Xo, vo, _, _ = oracle.ipt_dense(H, 16, 300, tol=1e-12, use_tol=True)
+    assert info["fp64_fpres"] <= 1e-12
+    assert np.abs(X - Xo).max() <= 1e-9
+    assert np.abs(v - vo).max() <= 1e-9
+    assert oracle.max_relative_residual(H, X, v) <= 5e-9
+
+
+def test_mixed_invalid_arguments(cuda):
+    torch = cuda
+    lib = _lib.load()
+    res = _lib._MixedResult()
+    h = C.c_void_p(torch.cuda.current_blas_handle())
+    assert lib.ipt_mixed_precision_cuda_device_tol(None, 8, 2, 1e-3, 5, 1e-9, 5, h,
+                                                   C.byref(res)) == 1
+    dH = torch.zeros(8, 8, dtype=torch.float64, device="cuda")
+    p = C.c_void_p(dH.data_ptr())
+    assert lib.ipt_mixed_precision_tf32_cuda_device_tol(p, 8, 9, 1e-3, 5, 1e-9, 5, h,
+                                                        C.byref(res)) == 1
+    assert lib.ipt_mixed_precision_fp32_cuda_device_tol(p, 8, 2, 0.0, 5, 1e-9, 5, h,
+                                                        C.byref(res)) == 1
+    assert not res.d_vectors
+
+
+def check_pairs(H, X, v, k):
+    hn = np.abs(H).sum(axis=1).max()
+    w, _ = oracle.eigh_lowest(H, k)
+    assert np.abs(v - w).max() <= 1e-10 * hn, np.abs(v - w).max() / hn
+    r = np.linalg.norm(H @ X - X * v[None, :], axis=0) / max(1.0, hn)
+    assert r.max() <= 1e-8, r.max()
+
+
+@pytest.mark.parametrize("prec", ["fp16", "bf16", "tf32"])
+def test_block_mixed_config1_shape_small(cuda, prec):
+    H, _ = workloads.dense_config1(2048, seed=4)
+    X, v, rep = api.block_solve_dense(H, 32, prec, ipt_maxiter=60, ipt_check_every=4)
+    assert rep["converged"] == 1
+    assert rep["lowp_matvecs"] > 0
+    check_pairs(H, X, v, 32)
+
+
+def test_block_mixed_config1_full(cuda):
+    """The n = 8192, k = 32 workload: FP16 tensor-core IPT + FP64 recovery."""
+    H, _ = workloads.dense_config1(8192, seed=0)
+    X, v, rep = api.block_solve_dense(H, 32, "fp16", ipt_maxiter=80, ipt_check_every=8)
+    assert rep["converged"] == 1
+    check_pairs(H, X, v, 32)
