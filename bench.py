@@ -1,0 +1,423 @@
+"""Benchmark: time to the k lowest eigenpairs at ||r|| <= 1e-8 ||H||_inf.
+
+Workload (one step = one solve): dense symmetric n = 8192, k = 32 with
+d_i = i/8 + U(0,0.1) and h_ij ~ N(0, 0.02^2) exp(-|i-j|/256) (seeded synthetic
+matrix, block_ipt_gb300.workloads.dense_config1).  Our arm solves it with
+the block solver: FP16 tensor-core IPT (tcgen05/TMA) followed by FP64
+CholQR2 + Rayleigh-Ritz + Davidson; every step is checked in FP64.
+
+  value        device time per solve, H already resident in HBM (ms)
+  e2e          the same solve through the host C-ABI entry point
+               (ipt_block_solve_dense): H copied in from pinned host memory
+               and the pairs copied back inside the timed region (ms)
+  plain_fp64   the same code with an FP64 IPT stage (ms), and the speed-up
+  roofline     dominant kernel of the timed region, from live CUDA-event
+               timings of every launch (ipt_block_profile_*)
+  cpu_baseline the oracle restatement of the reference's CPU IPT, one
+               iteration timed on all host cores and scaled by the block
+               products plain IPT needs on this matrix
+
+`--impl reference` times the reference's CPU path alone (rank 0 only).
+"""
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "time to k eigenpairs at ||r||<=1e-8, mixed+learned vs plain FP64 IPT, 1xGB300"
+WORKLOAD = ("dense symmetric n=8192 k=32, d_i=i/8+U(0,0.1), h_ij~N(0,0.02^2)exp(-|i-j|/256), "
+            "seed 0; FP16 tcgen05 IPT + FP64 CholQR2/Rayleigh-Ritz/Davidson to scaled residual 1e-8")
+PRODUCTS_FILE = os.path.join(ROOT, "oracle", "plain_ipt_products.json")
+MEASURED_PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=8192)
+    ap.add_argument("--k", type=int, default=32)
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--precision", default="fp16", choices=["fp16", "bf16", "tf32"])
+    ap.add_argument("--plain-steps", type=int, default=2)
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--no-lapack", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def plain_products(n, k, seed):
+    try:
+        with open(PRODUCTS_FILE) as f:
+            tab = json.load(f)
+        ent = tab.get("dense_config1_n%d_k%d_seed%d" % (n, k, seed))
+        if ent and ent["products"] > 0:
+            return int(ent["products"])
+    except OSError:
+        pass
+    return None
+
+
+# ---------------------------------------------------------------------------
+# CPU baseline: the reference's CPU IPT (oracle port or oracle/_ref)
+# ---------------------------------------------------------------------------
+def cpu_iteration_seconds(H, k, reps=1):
+    """Seconds per plain-IPT iteration of the reference CPU path on this host.
+    Uses the reference's own compiled code where it was built for this host,
+    else the oracle restatement on all host cores."""
+    from oracle import oracle
+    kind = "port"
+    cores = oracle.num_threads()
+    fn = None
+    if oracle.ref_available():
+        try:
+            L = oracle.ref_lib("dense")
+            n = H.shape[0]
+            X = np.zeros((n, k), order="F")
+            v = np.zeros(k)
+
+            def fn(it):
+                L.ref_ipt_cpu_reference(C.c_void_p(H.ctypes.data), n, k, it,
+                                        C.c_void_p(X.ctypes.data), C.c_void_p(v.ctypes.data))
+            kind = "reference"
+            cores = 1
+        except OSError:
+            fn = None
+    if fn is None:
+        def fn(it):
+            oracle.ipt_dense(H, k, it)
+    times = []
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        fn(1)
+        times.append(time.perf_counter() - t0)
+    return statistics.median(times), kind, cores
+
+
+def run_reference(args):
+    world, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    from block_ipt_gb300 import workloads
+    from oracle import oracle
+    oracle.build()
+    H, _ = workloads.dense_config1(args.n, seed=args.seed)
+    H = np.asfortranarray(H)
+    prods = plain_products(args.n, args.k, args.seed)
+    if prods is None:
+        prods, _ = oracle.products_to_residual(H, args.k, 2000, 1e-8)
+    for _ in range(args.warmup):
+        cpu_iteration_seconds(H, args.k)
+    samples = []
+    kind, cores = "port", 1
+    for _ in range(args.steps):
+        t, kind, cores = cpu_iteration_seconds(H, args.k)
+        samples.append(t * prods * 1e3)
+    value = statistics.mean(samples)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "ms",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": value,
+        "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic",
+        "config": {"workload": WORKLOAD, "n": args.n, "k": args.k, "seed": args.seed,
+                   "path": "reference CPU plain IPT (runtests.cu:98-174 semantics)"},
+        "cpu_baseline": {"value": value, "unit": "ms", "cores": cores, "kind": kind,
+                         "sample": "1 plain-IPT iteration per step (n=%d, k=%d), scaled by the "
+                                   "%d block products plain IPT needs to reach the scaled "
+                                   "residual 1e-8" % (args.n, args.k, prods)},
+        "e2e": {"value": value, "unit": "ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ---------------------------------------------------------------------------
+# clocks sampler
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.QUERY,
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, parts[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# our arm
+# ---------------------------------------------------------------------------
+def fp64_check(torch, dH, dX, dv, hnorm):
+    R = dH @ dX - dX * dv[None, :]
+    r = (torch.linalg.vector_norm(R, dim=0) / max(1.0, hnorm)).max().item()
+    return r
+
+
+def profile_snapshot(lib):
+    out = {}
+    name = C.c_char_p()
+    ms = C.c_double()
+    cnt = C.c_longlong()
+    for kid in range(9):
+        lib.ipt_block_profile_read(kid, C.byref(name), C.byref(ms), C.byref(cnt))
+        out[name.value.decode()] = (ms.value, cnt.value)
+    return out
+
+
+def run_ours(args):
+    import torch
+    import torch.distributed as dist
+
+    from block_ipt_gb300 import _lib, api, workloads
+
+    world, rank, local = dist_env()
+    if world > 1:
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    lib = _lib.load()
+    dev = torch.device("cuda", local)
+    n, k = args.n, args.k
+    # one independent instance per rank ("replicas only": the dense solve is
+    # not sharded), seeded by rank
+    H, _ = workloads.dense_config1(n, seed=args.seed + rank)
+    H = np.asfortranarray(H)
+    hnorm = float(np.abs(H).sum(axis=1).max())
+    H_pinned = torch.from_numpy(H.T.copy()).pin_memory()  # row-major view of H^T = col-major H
+    dH = H_pinned.to(dev)
+    dHsym = dH  # symmetric: the same buffer is H in either order for the check
+    dX = torch.empty((k, n), dtype=torch.float64, device=dev)  # column-major n x k
+    dv = torch.empty(k, dtype=torch.float64, device=dev)
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)  # 256 MB > L2
+    stream = torch.cuda.current_stream(dev)
+    kw = dict(ipt_maxiter=80, ipt_check_every=8, stream=stream.cuda_stream)
+
+    def solve(prec):
+        return api.block_solve_dense_device(dH.data_ptr(), n, k, dX.data_ptr(), dv.data_ptr(),
+                                            prec, **kw)
+
+    for _ in range(args.warmup):
+        solve(args.precision)
+    torch.cuda.synchronize()
+
+    sampler = ClockSampler(local)
+    sampler.start()
+    time.sleep(0.3)
+    lib.ipt_block_profile_reset()
+    lib.ipt_block_profile_enable(1)
+    launches0 = lib.ipt_block_launch_count()
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    times, reports, worst_res = [], [], 0.0
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    for _ in range(args.steps):
+        flush.zero_()
+        e0.record(stream)
+        rep = solve(args.precision)
+        e1.record(stream)
+        e1.synchronize()
+        times.append(e0.elapsed_time(e1))
+        reports.append(rep)
+        worst_res = max(worst_res, fp64_check(torch, dHsym.T, dX.T, dv, hnorm))
+    torch.cuda.synchronize()
+    launches = lib.ipt_block_launch_count() - launches0
+    lib.ipt_block_profile_enable(0)
+    prof = profile_snapshot(lib)
+    clocks = sampler.stop()
+    ms_mine = statistics.mean(times)
+    t = torch.tensor([ms_mine], device=dev)
+    if world > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        dist.barrier()
+    ms = float(t.item())
+
+    # eigenvalues against LAPACK (once, outside the timed region)
+    vals = dv.cpu().numpy()
+    dlambda = None
+    if not args.no_lapack and rank == 0:
+        from oracle import oracle
+        w, _ = oracle.eigh_lowest(H, k)
+        dlambda = float(np.abs(vals - w).max() / hnorm)
+
+    # plain FP64 path of the same code
+    plain_ms, plain_rep = [], None
+    for _ in range(args.plain_steps):
+        flush.zero_()
+        e0.record(stream)
+        plain_rep = solve("fp64")
+        e1.record(stream)
+        e1.synchronize()
+        plain_ms.append(e0.elapsed_time(e1))
+    plain = statistics.mean(plain_ms) if plain_ms else None
+
+    # end to end through the host entry point (pinned H in, pairs out)
+    Xh = np.zeros((n, k), order="F")
+    vh = np.zeros(k)
+    Hptr = C.c_void_p(H_pinned.data_ptr())
+    opt = api.block_options(args.precision, **kw)
+    e2e = []
+    for _ in range(args.e2e_steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        rep = _lib.IPTBlockReport()
+        st = lib.ipt_block_solve_dense(Hptr, n, k, C.byref(opt), C.c_void_p(Xh.ctypes.data),
+                                       C.c_void_p(vh.ctypes.data), C.byref(rep))
+        torch.cuda.synchronize()
+        e2e.append((time.perf_counter() - t0) * 1e3)
+        assert st == 0, _lib.status_string(st)
+        assert rep.converged == 1
+    e2e_ms = statistics.mean(e2e) if e2e else None
+
+    # roofline of the dominant kernel of the timed region
+    dom = max(prof.items(), key=lambda kv: kv[1][0])
+    name, (tot_ms, cnt) = dom
+    steps = args.steps
+    avg_rep = reports[-1]
+    with open(MEASURED_PEAKS) as f:
+        peaks = json.load(f)
+    roofline = None
+    fp64_peak = C.c_double(0.0)
+    lib.ipt_block_measure_fp64_peak(C.byref(fp64_peak))
+    FP64_PEAK_TFLOPS = fp64_peak.value
+    if name == "fp64_product":
+        flops = 2.0 * n * n * (sum(r["fp64_matvecs"] for r in reports) / steps) * steps
+        achieved = flops / (tot_ms * 1e-3) / 1e12
+        roofline = {"kernel": "dense64_partial_kernel (FP64 SIMT split-K)", "bound": "fp64",
+                    "achieved": achieved, "peak": FP64_PEAK_TFLOPS, "unit": "TFLOP/s",
+                    "frac": achieved / FP64_PEAK_TFLOPS, "traffic": None,
+                    "peak_source": "ipt_block_measure_fp64_peak (DFMA throughput kernel, run "
+                                   "live; MEASURED_PEAKS.json has no FP64 entry)",
+                    "launches": cnt, "avg_launch_ms": tot_ms / max(1, cnt)}
+    lp_ms, lp_cnt = prof["lowp_product"]
+    ldp = (n + 63) // 64 * 64
+    esize = 2 if args.precision in ("fp16", "bf16") else 4
+    lp_bytes = n * ldp * esize + ldp * ((k + 8 + 15) // 16 * 16) * esize
+    lp_ach = lp_bytes / (lp_ms / max(1, lp_cnt) * 1e-3) / 1e9 if lp_cnt else None
+    roofline_lowp = {"kernel": "tc_partial_kernel (tcgen05 + TMA, %s)" % args.precision,
+                     "bound": "hbm", "achieved": lp_ach, "peak": peaks["hbm_gbs"],
+                     "unit": "GB/s", "frac": (lp_ach / peaks["hbm_gbs"]) if lp_ach else None,
+                     "traffic": None, "launches": lp_cnt,
+                     "avg_launch_ms": lp_ms / max(1, lp_cnt),
+                     "algorithmic_bytes_per_launch": lp_bytes}
+    if roofline is None:
+        roofline = roofline_lowp
+
+    cpu = None
+    if not args.no_cpu and rank == 0:
+        prods = plain_products(n, k, args.seed)
+        sec, kind, cores = cpu_iteration_seconds(H, k)
+        if prods:
+            cpu = {"value": sec * prods * 1e3, "unit": "ms", "cores": cores, "kind": kind,
+                   "sample": "1 plain-IPT iteration (n=%d, k=%d) timed, scaled by the %d block "
+                             "products plain IPT needs to reach the scaled residual 1e-8"
+                             % (n, k, prods)}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": ms, "unit": "ms", "n_gpus": world, "steps": steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "%s+f64" % args.precision,
+            "data": "synthetic",
+            "config": {"workload": WORKLOAD, "n": n, "k": k, "seed": args.seed,
+                       "precision": args.precision, "learned_preconditioner": False,
+                       "l2": "256 MB buffer written between timed steps (inputs also > L2)",
+                       "parallelism": "replicas only (one instance per GPU)"},
+            "e2e": ({"value": e2e_ms, "unit": "ms", "h2d_bytes_per_step": 8 * n * n,
+                     "d2h_bytes_per_step": 8 * n * k + 8 * k} if e2e_ms is not None else None),
+            "gpu_launches": launches,
+            "roofline": roofline,
+            "roofline_lowp": roofline_lowp,
+            "cpu_baseline": cpu,
+            "clocks": clocks,
+            "plain_fp64_ms": plain,
+            "speedup_vs_plain_fp64": (plain / ms) if plain else None,
+            "check": {"max_scaled_residual": worst_res, "max_abs_dlambda_over_norm_inf": dlambda,
+                      "converged": all(r["converged"] == 1 for r in reports)},
+            "report": {kk: avg_rep[kk] for kk in ("ipt_iterations", "davidson_steps", "restarts",
+                                                  "basis_cols", "fp64_matvecs", "lowp_matvecs",
+                                                  "ipt_ms", "rayleigh_ritz_ms", "davidson_ms",
+                                                  "total_ms")},
+            "plain_report": ({kk: plain_rep[kk] for kk in ("ipt_iterations", "davidson_steps",
+                                                           "fp64_matvecs", "total_ms")}
+                             if plain_rep else None),
+            "kernel_ms": {kk: round(v[0] / steps, 4) for kk, v in prof.items() if v[1]},
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

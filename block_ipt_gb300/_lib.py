@@ -188,6 +188,11 @@ SIGNATURES = [
     ("ipt_mixed_precision_fp32_cuda_free_device_result", None, [C.POINTER(_MixedResult)]),
     ("ipt_mixed_precision_tf32_cuda_free_device_result", None, [C.POINTER(_MixedResult)]),
     ("ipt_block_default_options", None, [C.POINTER(IPTBlockOptions)]),
+    ("ipt_block_launch_count", C.c_longlong, []),
+    ("ipt_block_profile_enable", None, [_i]),
+    ("ipt_block_profile_reset", None, []),
+    ("ipt_block_profile_read", _i, [_i, C.POINTER(C.c_char_p), _dp, C.POINTER(C.c_longlong)]),
+    ("ipt_block_measure_fp64_peak", _i, [_dp]),
     ("ipt_block_solve_dense_device", _i, [_vp, _i, _i, C.POINTER(IPTBlockOptions), _vp, _vp,
                                           C.POINTER(IPTBlockReport)]),
     ("ipt_block_solve_dense", _i, [_vp, _i, _i, C.POINTER(IPTBlockOptions), _vp, _vp,

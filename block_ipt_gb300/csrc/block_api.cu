@@ -37,7 +37,11 @@ struct DenseApply final : Fp64Apply {
         if (P.count < need) {
             IPTGB_CHECK(P.alloc(need, s));
         }
-        IPTGB_CHECK(launch_dense64_partial(H, n, n, V, n, c, P.ptr, S, s));
+        {
+            KernelTimerScope timer(kProfFp64Product, s);
+            IPTGB_CHECK(launch_dense64_partial(H, n, n, V, n, c, P.ptr, S, s));
+        }
+        KernelTimerScope timer(kProfFp64Update, s);
         return launch_sum_partials(P.ptr, S, (size_t)n * c, AV, s);
     }
 };
@@ -50,6 +54,7 @@ struct CsrApply final : Fp64Apply {
     cudaStream_t s = nullptr;
     int apply(const double *V, int c, double *AV) override
     {
+        KernelTimerScope timer(kProfCsrProduct, s);
         return launch_csr64_spmm(row_ptr, col_ind, vals, n, V, c, AV, s);
     }
 };

@@ -45,6 +45,10 @@ inline int blocks_for(size_t count, int threads = kThreads)
         }                                                                       \
     } while (0)
 
+// Every kernel launch of the library is followed by IPTGB_LAUNCH(), which
+// checks the launch and counts it (ipt_block_launch_count()).
+void count_launch();
+
 #define IPTGB_LAUNCH()                                                          \
     do {                                                                        \
         cudaError_t iptgb_err_ = cudaGetLastError();                            \
@@ -53,7 +57,33 @@ inline int blocks_for(size_t count, int threads = kThreads)
                     __FILE__, __LINE__, cudaGetErrorString(iptgb_err_));        \
             return IPT_CUDA_CUDA_ERROR;                                         \
         }                                                                       \
+        ::iptgb::count_launch();                                                \
     } while (0)
+
+// Optional per-kernel timing (ipt_block_profile_*): when enabled, the
+// instrumented launch sites bracket their kernel with CUDA events on the
+// launch stream.  KernelTimerScope records the start in its constructor and
+// the stop in its destructor.
+enum ProfiledKernel {
+    kProfLowpProduct = 0,   // tensor-core / FP32 SIMT block product (low precision)
+    kProfLowpUpdate = 1,    // low-precision IPT update
+    kProfFp64Product = 2,   // FP64 dense split-K block product
+    kProfFp64Update = 3,    // FP64 IPT update / partial sum
+    kProfCsrProduct = 4,    // FP64 CSR block product
+    kProfSmallEig = 5,      // one-CTA Jacobi eigensolver
+    kProfGram = 6,          // FP64 Gram products
+    kProfTallGemm = 7,      // FP64 tall-by-small products
+    kProfMlp = 8,           // learned-preconditioner kernels
+    kProfCount = 9
+};
+bool profile_enabled();
+struct KernelTimerScope {
+    int kernel;
+    cudaStream_t stream;
+    cudaEvent_t start = nullptr;
+    KernelTimerScope(int k, cudaStream_t s);
+    ~KernelTimerScope();
+};
 
 // A device buffer released by its destructor (stream-ordered when possible).
 template <typename T>

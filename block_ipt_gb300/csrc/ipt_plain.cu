@@ -21,7 +21,11 @@ int device_sm_count()
 int DenseFp64Operator::step(const double *X, double *Xn, const double *d, int want_norms,
                             NormScratch *ns)
 {
-    IPTGB_CHECK(launch_dense64_partial(H, n, ldh, X, n, k, P, S, stream));
+    {
+        KernelTimerScope timer(kProfFp64Product, stream);
+        IPTGB_CHECK(launch_dense64_partial(H, n, ldh, X, n, k, P, S, stream));
+    }
+    KernelTimerScope timer(kProfFp64Update, stream);
     return launch_dense64_update(P, S, n, k, X, d, Xn, want_norms, ns, stream);
 }
 
@@ -33,7 +37,11 @@ int DenseFp64Operator::diag_values(const double *X, double *values)
 int CsrFp64Operator::step(const double *X, double *Xn, const double *d, int want_norms,
                           NormScratch *ns)
 {
-    IPTGB_CHECK(launch_csr64_spmm(row_ptr, col_ind, vals, n, X, k, Y, stream));
+    {
+        KernelTimerScope timer(kProfCsrProduct, stream);
+        IPTGB_CHECK(launch_csr64_spmm(row_ptr, col_ind, vals, n, X, k, Y, stream));
+    }
+    KernelTimerScope timer(kProfFp64Update, stream);
     return launch_ipt_update_from_y(Y, n, k, X, d, Xn, want_norms, ns, stream);
 }
 

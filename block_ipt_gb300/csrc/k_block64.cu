@@ -110,6 +110,7 @@ int BlockOps::gram(const double *A, long long lda, int ma, const double *B, long
     blocks_x = (chunks + per_block - 1) / per_block;
     const size_t mm = (size_t)ma * (size_t)mb;
     IPTGB_CHECK(ensure_partials((size_t)blocks_x * mm));
+    KernelTimerScope timer(kProfGram, stream);
     gram_partial_kernel<<<dim3(blocks_x, tiles), 256, 0, stream>>>(A, lda, ma, B, ldb, mb, n,
                                                                    per_block, partials);
     IPTGB_LAUNCH();
@@ -177,6 +178,7 @@ int BlockOps::tall_gemm(const double *A, long long lda, const double *B, long lo
         return IPT_CUDA_SUCCESS;
     }
     dim3 grid((n + 255) / 256, (p + kTallCols - 1) / kTallCols);
+    KernelTimerScope timer(kProfTallGemm, stream);
     tall_gemm_kernel<<<grid, 256, 0, stream>>>(A, lda, B, ldb, C, ldc, n, m, p, alpha, beta);
     IPTGB_LAUNCH();
     return IPT_CUDA_SUCCESS;
@@ -621,6 +623,7 @@ int BlockOps::jacobi_eig(const double *T, int m, double *w, double *Z, int *swee
     }
     IPTGB_CUDA(cudaFuncSetAttribute(jacobi_eig_kernel,
                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    KernelTimerScope timer(kProfSmallEig, stream);
     jacobi_eig_kernel<<<1, 512, smem, stream>>>(T, m, w, Z, 40, sweeps_dev);
     IPTGB_LAUNCH();
     return IPT_CUDA_SUCCESS;

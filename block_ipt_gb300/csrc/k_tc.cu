@@ -642,6 +642,7 @@ struct LowpDense final : LowpDenseOperator {
     {
         const int row_blocks = (n + tc::kBM - 1) / tc::kBM;
         dim3 grid(row_blocks, splits);
+        KernelTimerScope timer(kProfLowpProduct, s);
         tc::tc_partial_kernel<LowpTypes<LP>::kind><<<grid, tc::kThreads, smem_bytes, s>>>(
             mapA, mapB[cur], n, p, p_pad, stages, tmem_cols, chunks_total, chunks_per_split,
             kchunk, idesc, P.ptr, err.ptr);
@@ -656,6 +657,7 @@ struct LowpDense final : LowpDenseOperator {
         const int grid = blocks_for(elems);
         if (want_norms && grid > ns->capacity) return IPT_CUDA_INVALID_ARGUMENT;
         const int nxt = cur ^ 1;
+        KernelTimerScope timer(kProfLowpUpdate, s);
         lowp_update_kernel<LP><<<grid, kThreads, 0, s>>>(
             P.ptr, splits, n, p, (float)(1.0 / scale), G.ptr, X32[cur].ptr, X32[nxt].ptr,
             Xlp[nxt].ptr, ldp, want_norms, ns->partials, ns->counter, ns->norms);
@@ -759,6 +761,7 @@ struct LowpDenseSimtF32 final : LowpDenseOperator {
     }
     int product() override
     {
+        KernelTimerScope timer(kProfLowpProduct, s);
         return launch_dense32_partial(delta.ptr, n, n, X32[cur].ptr, n, p, P.ptr, splits, s);
     }
     int step(int want_norms, NormScratch *ns) override
@@ -768,6 +771,7 @@ struct LowpDenseSimtF32 final : LowpDenseOperator {
         const int grid = blocks_for(elems);
         if (want_norms && grid > ns->capacity) return IPT_CUDA_INVALID_ARGUMENT;
         const int nxt = cur ^ 1;
+        KernelTimerScope timer(kProfLowpUpdate, s);
         lowp_update_kernel<float><<<grid, kThreads, 0, s>>>(
             P.ptr, splits, n, p, 1.0f, G.ptr, X32[cur].ptr, X32[nxt].ptr, X32[nxt].ptr, n,
             want_norms, ns->partials, ns->counter, ns->norms);

@@ -105,6 +105,25 @@ int ipt_block_solve_csr(const int *row_ptr, const int *col_ind, const double *va
                         int nnz, int k, const IPTBlockOptions *options, double *vectors,
                         double *values, IPTBlockReport *report);
 
+/* ---- instrumentation ---------------------------------------------------- */
+
+/* Number of kernels this library has launched in the calling process. */
+long long ipt_block_launch_count(void);
+
+/* Per-kernel CUDA-event timing of the main kernels (off by default).  When
+ * enabled, every launch of an instrumented kernel is bracketed by events on
+ * its own stream.  Kernel ids: 0 low-precision product (tcgen05 / FP32 SIMT),
+ * 1 low-precision update, 2 FP64 dense product, 3 FP64 update / partial sum,
+ * 4 FP64 CSR product, 5 small eigensolver, 6 Gram products, 7 tall-by-small
+ * products, 8 learned-preconditioner kernels. */
+void ipt_block_profile_enable(int on);
+void ipt_block_profile_reset(void);
+int ipt_block_profile_read(int kernel, const char **name, double *total_ms, long long *launches);
+
+/* FP64 FMA throughput of the current device in TFLOP/s (a short DFMA
+ * throughput kernel); the FP64 roofline denominator. */
+int ipt_block_measure_fp64_peak(double *tflops);
+
 #ifdef __cplusplus
 }
 #endif

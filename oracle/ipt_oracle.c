@@ -82,22 +82,31 @@ ORACLE_API int oracle_build_banded_csc(int n, int *col_ptr, int *row_ind, double
 
 /* out = a * x for column-major a (n x n) and x (n x k).  Each output element
  * sums inner = 0..n-1 in ascending order, exactly as
- * IPT_C_GPU/test_temp/runtests.cu:82-96; the loop nest is interchanged
- * (col, inner, row) for cache reuse, which keeps every element's order. */
+ * IPT_C_GPU/test_temp/runtests.cu:82-96; the loop nest is reordered (row
+ * block, inner, col, row) so that every thread streams its slab of `a` once
+ * per product, which keeps every element's summation order. */
 static void oracle_dense_matmul(double *out, const double *a, const double *x, int n, int k)
 {
-#pragma omp parallel for schedule(static)
-    for (int col = 0; col < k; ++col) {
-        double *o = out + (size_t)col * (size_t)n;
-        const double *xc = x + (size_t)col * (size_t)n;
-        for (int row = 0; row < n; ++row) {
-            o[row] = 0.0;
+    const int rb = 256;
+    const int nblocks = (n + rb - 1) / rb;
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int b = 0; b < nblocks; ++b) {
+        const int r0 = b * rb;
+        const int r1 = r0 + rb < n ? r0 + rb : n;
+        for (int col = 0; col < k; ++col) {
+            double *o = out + (size_t)col * (size_t)n;
+            for (int row = r0; row < r1; ++row) {
+                o[row] = 0.0;
+            }
         }
         for (int inner = 0; inner < n; ++inner) {
             const double *ac = a + (size_t)inner * (size_t)n;
-            double xv = xc[inner];
-            for (int row = 0; row < n; ++row) {
-                o[row] += ac[row] * xv;
+            for (int col = 0; col < k; ++col) {
+                const double xv = x[(size_t)inner + (size_t)col * (size_t)n];
+                double *o = out + (size_t)col * (size_t)n;
+                for (int row = r0; row < r1; ++row) {
+                    o[row] += ac[row] * xv;
+                }
             }
         }
     }
@@ -454,4 +463,75 @@ ORACLE_API int oracle_num_threads(void)
 #else
     return 1;
 #endif
+}
+
+/* Plain IPT with the eigen-residual read off every step: for the block X
+ * entering a step, r_j = H x_j - lambda_j x_j with lambda_j = (H X)_jj equals
+ * (d_j - d_i)(F(X) - X)_ij entrywise (zero on the target row).  Returns the
+ * number of block products needed until the block entering a step satisfies
+ * max_j ||r_j|| / (max(1, hnorm) max(1, ||x_j||)) <= res_tol (that step
+ * included: it yields lambda), or -1 if maxiter products do not reach it.
+ * Same map and arithmetic as oracle_ipt_dense. */
+ORACLE_API int oracle_ipt_dense_products_to_residual(const double *matrix, int n, int k,
+                                                     int maxiter, double hnorm, double res_tol,
+                                                     double *final_scaled_residual)
+{
+    size_t elems = (size_t)n * (size_t)k;
+    double *x = (double *)calloc(elems, sizeof(double));
+    double *y = (double *)calloc(elems, sizeof(double));
+    double *diag = (double *)calloc((size_t)n, sizeof(double));
+    double *cdiag = (double *)calloc((size_t)k, sizeof(double));
+    int found = -1;
+    if (x == NULL || y == NULL || diag == NULL || cdiag == NULL) {
+        free(x); free(y); free(diag); free(cdiag);
+        return -2;
+    }
+    for (int col = 0; col < k; ++col) {
+        x[(size_t)col + (size_t)col * (size_t)n] = 1.0;
+    }
+    for (int row = 0; row < n; ++row) {
+        diag[row] = matrix[(size_t)row + (size_t)row * (size_t)n];
+    }
+    for (int iter = 0; iter < maxiter; ++iter) {
+        double worst = 0.0;
+        oracle_dense_matmul(y, matrix, x, n, k);
+        for (int col = 0; col < k; ++col) {
+            size_t di = (size_t)col + (size_t)col * (size_t)n;
+            cdiag[col] = y[di] - diag[col] * x[di];
+        }
+        for (int col = 0; col < k; ++col) {
+            double rs = 0.0, xs = 0.0;
+            for (int row = 0; row < n; ++row) {
+                size_t idx = (size_t)row + (size_t)col * (size_t)n;
+                double xo = x[idx];
+                xs += xo * xo;
+                if (row == col) {
+                    y[idx] = 1.0;
+                } else {
+                    double g = 1.0 / (diag[col] - diag[row]);
+                    y[idx] = (y[idx] - diag[row] * xo - xo * cdiag[col]) * g;
+                    double r = (diag[col] - diag[row]) * (y[idx] - xo);
+                    rs += r * r;
+                }
+            }
+            {
+                double sc = sqrt(rs) / (fmax(1.0, hnorm) * fmax(1.0, sqrt(xs)));
+                if (!(sc <= worst)) {
+                    worst = sc;
+                }
+            }
+        }
+        if (final_scaled_residual != NULL) {
+            *final_scaled_residual = worst;
+        }
+        if (worst <= res_tol) {
+            found = iter + 1;
+            break;
+        }
+        {
+            double *t = x; x = y; y = t;
+        }
+    }
+    free(x); free(y); free(diag); free(cdiag);
+    return found;
 }

@@ -57,6 +57,8 @@ def lib():
         L.oracle_stable_sort_permutation.argtypes = [vp, i, vp]
         L.oracle_csc_matmul.argtypes = [vp, vp, vp, i, vp, i, vp]
         L.oracle_csr_matmul.argtypes = [vp, vp, vp, i, vp, i, vp]
+        L.oracle_ipt_dense_products_to_residual.restype = i
+        L.oracle_ipt_dense_products_to_residual.argtypes = [vp, i, i, i, d, d, vp]
         L.oracle_num_threads.restype = i
         _lib = L
     return _lib
@@ -126,6 +128,21 @@ def ipt_csr(row_ptr, col_ind, vals, diag, n, k, maxiter, tol=0.0, use_tol=False,
     if st != 0:
         raise RuntimeError("oracle_ipt_csr failed: %d" % st)
     return X, v, it.value, fp.value
+
+
+def products_to_residual(H, k, maxiter, res_tol=1e-8):
+    """Block products plain IPT needs until the scaled eigen-residual of its
+    iterate is <= res_tol (-1 if not within maxiter); see ipt_oracle.c."""
+    H = np.asfortranarray(H, dtype=np.float64)
+    hn = float(np.abs(H).sum(axis=1).max())
+    fr = C.c_double(0.0)
+    got = lib().oracle_ipt_dense_products_to_residual(_p(H), H.shape[0], k, maxiter, hn,
+                                                      float(res_tol), C.byref(fr))
+    return got, fr.value
+
+
+def num_threads():
+    return lib().oracle_num_threads()
 
 
 def max_relative_residual(H, X, v):

@@ -21,7 +21,7 @@ def declared_functions():
         text = open(os.path.join(INCLUDE, fn)).read()
         text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
         text = re.sub(r"//[^\n]*", "", text)
-        for m in re.finditer(r"\b(?:int|void|const char \*)\s*\*?\s*([a-z_][a-z0-9_]*)\s*\(", text):
+        for m in re.finditer(r"\b(?:int|void|long long|const char \*)\s*\*?\s*([a-z_][a-z0-9_]*)\s*\(", text):
             names.add(m.group(1))
     return names
 
