@@ -105,6 +105,25 @@ int ipt_block_solve_csr(const int *row_ptr, const int *col_ind, const double *va
                         int nnz, int k, const IPTBlockOptions *options, double *vectors,
                         double *values, IPTBlockReport *report);
 
+/* ---- allocation-free FP64 dense solve ------------------------------------ */
+
+/* No counterpart in the reference.  The tolerance-stopped FP64 dense IPT of
+ * ipt_cuda_device_tol for callers that cannot let the library allocate
+ * device memory (an application-owned memory pool, no allocation after
+ * start-up, or pipelines that cudaFree's device-wide synchronisation would
+ * stall).  The caller passes H and the outputs d_vectors (n*k) and d_values
+ * (k); all scratch lives in one 16 MiB static device array that each GPU
+ * loading the library keeps until exit, so n*k is limited to about 1.0e6
+ * (2*n*k + n + n*k/128 doubles); larger sizes return
+ * IPT_CUDA_INVALID_ARGUMENT with a message on stderr.  Runs on `stream`
+ * (cudaStream_t, NULL = legacy default stream).  The first call on a device
+ * looks up the scratch address and should come before any stream capture.
+ * Calls share the scratch: calls that overlap on the GPU race and must be
+ * serialised by the caller. */
+int ipt_cuda_device_tol_noalloc(const double *d_matrix_col_major, int n, int k, double tol,
+                                int maxiter, void *stream, double *d_vectors, double *d_values,
+                                int *iterations_done_out, double *fixed_point_residual_out);
+
 /* ---- instrumentation ---------------------------------------------------- */
 
 /* Number of kernels this library has launched in the calling process. */
