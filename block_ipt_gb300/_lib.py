@@ -23,6 +23,8 @@ IPT_BLOCK_FP64 = 0
 IPT_BLOCK_FP16 = 1
 IPT_BLOCK_BF16 = 2
 IPT_BLOCK_TF32 = 3
+IPT_BLOCK_STRATEGY_REFINE = 0
+IPT_BLOCK_STRATEGY_DAVIDSON = 1
 IPT_BLOCK_PRECOND_DIAGONAL = 0
 IPT_BLOCK_PRECOND_MLP = 1
 
@@ -135,7 +137,8 @@ class IPTBlockOptions(C.Structure):
         ("ipt_precision", _i), ("oversample", _i), ("ipt_maxiter", _i), ("ipt_tol", _d),
         ("ipt_check_every", _i), ("residual_tol", _d), ("davidson_maxsteps", _i),
         ("max_basis", _i), ("preconditioner", _i), ("mlp_params", C.c_void_p),
-        ("stream", C.c_void_p),
+        ("stream", C.c_void_p), ("strategy", _i), ("refine_maxiter", _i),
+        ("inner_maxiter", _i), ("inner_tol", _d),
     ]
 
 

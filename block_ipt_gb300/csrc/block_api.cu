@@ -14,6 +14,7 @@
 #include "block_solver.h"
 #include "common.cuh"
 #include "ipt_plain.h"
+#include "lowp.h"
 #include "prep.h"
 #include "reduce.cuh"
 
@@ -181,13 +182,32 @@ LearnedCorrection *make_learned_correction(const float *params, cudaStream_t str
 // ---------------------------------------------------------------------------
 // Row sums of |H| (dense col-major: thread per row, coalesced over columns).
 // ---------------------------------------------------------------------------
-__global__ void dense_row_abs_sum_kernel(const double *__restrict__ H, int n, double *rs)
+// Pass 1: per 256-column slab partial row sums (grid: row blocks x slabs, so
+// the whole GPU streams H once); pass 2 sums the slabs in a fixed order.
+constexpr int kRowSumSlab = 256;
+
+__global__ void dense_row_abs_partial_kernel(const double *__restrict__ H, int n,
+                                             double *__restrict__ part)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int l0 = blockIdx.y * kRowSumSlab;
+    if (i >= n) return;
+    const int l1 = min(n, l0 + kRowSumSlab);
+    double s = 0.0;
+    for (int l = l0; l < l1; ++l) {
+        s += fabs(H[(size_t)i + (size_t)l * n]);
+    }
+    part[(size_t)blockIdx.y * n + i] = s;
+}
+
+__global__ void dense_row_abs_finish_kernel(const double *__restrict__ part, int slabs, int n,
+                                            double *__restrict__ rs)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     double s = 0.0;
-    for (int l = 0; l < n; ++l) {
-        s += fabs(H[(size_t)i + (size_t)l * n]);
+    for (int b = 0; b < slabs; ++b) {
+        s += part[(size_t)b * n + i];
     }
     rs[i] = s;
 }
@@ -299,8 +319,16 @@ int dense_block_device(const double *dH_in, int n, int k, const IPTBlockOptions 
         IPTGB_CHECK(Xtmp.alloc((size_t)n * k, s));
     }
     IPTGB_CHECK(rs.alloc((size_t)n, s));
-    dense_row_abs_sum_kernel<<<blocks_for(n), kThreads, 0, s>>>(dH, n, rs.ptr);
-    IPTGB_LAUNCH();
+    {
+        const int slabs = (n + kRowSumSlab - 1) / kRowSumSlab;
+        DeviceBuffer<double> part;
+        IPTGB_CHECK(part.alloc((size_t)slabs * n, s));
+        dense_row_abs_partial_kernel<<<dim3(blocks_for(n), slabs), kThreads, 0, s>>>(dH, n,
+                                                                                   part.ptr);
+        IPTGB_LAUNCH();
+        dense_row_abs_finish_kernel<<<blocks_for(n), kThreads, 0, s>>>(part.ptr, slabs, n, rs.ptr);
+        IPTGB_LAUNCH();
+    }
     double hnorm = 0.0;
     IPTGB_CHECK(max_of_device(rs.ptr, n, s, &hnorm));
 
@@ -310,31 +338,75 @@ int dense_block_device(const double *dH_in, int n, int k, const IPTBlockOptions 
     apply.sms = device_sm_count();
     apply.s = s;
     std::unique_ptr<IptStage> stage;
+    std::unique_ptr<LowpDenseOperator> lowp;
     int st = IPT_CUDA_SUCCESS;
-    if (opt.ipt_precision == IPT_BLOCK_FP64) {
-        stage.reset(make_fp64_dense_stage(dH, n, d.ptr, s));
-    } else {
-        stage.reset(make_lowp_dense_stage(dH, n, d.ptr, opt.ipt_precision, s, &st));
-        if (stage == nullptr) {
+    const bool lowp_mode = opt.ipt_precision != IPT_BLOCK_FP64;
+    if (lowp_mode) {
+        const int kind = opt.ipt_precision == IPT_BLOCK_FP16 ? kLowpF16
+                         : opt.ipt_precision == IPT_BLOCK_BF16 ? kLowpBF16
+                                                               : kLowpTF32;
+        lowp.reset(make_lowp_dense_operator(dH, n, kind, s, &st));
+        if (lowp == nullptr) {
             return st != IPT_CUDA_SUCCESS ? st : IPT_CUDA_INVALID_ARGUMENT;
         }
+        stage.reset(make_lowp_stage_on(lowp.get(), d.ptr, n, s));
+    } else {
+        stage.reset(make_fp64_dense_stage(dH, n, d.ptr, s));
     }
     std::unique_ptr<LearnedCorrection> learned;
     if (opt.preconditioner == IPT_BLOCK_PRECOND_MLP) {
         learned.reset(make_learned_correction(opt.mlp_params, s));
     }
-    BlockSolveInput in;
-    in.apply = &apply;
-    in.ipt = stage.get();
-    in.learned = learned.get();
-    in.d = d.ptr;
-    in.n = n;
-    in.k = k;
-    in.hnorm = hnorm;
-    in.opt = opt;
-    in.lowp = opt.ipt_precision != IPT_BLOCK_FP64;
     double *xout = permuted ? Xtmp.ptr : d_vectors;
-    IPTGB_CHECK(block_solve(in, xout, d_values, report, s));
+    DeviceBuffer<double> Xfb;
+    bool done = false;
+    if (opt.strategy == IPT_BLOCK_STRATEGY_REFINE && k <= 64) {
+        RefineInput rin;
+        rin.apply = &apply;
+        rin.ipt = lowp_mode ? stage.get() : nullptr;
+        rin.lowp = lowp.get();
+        rin.d = d.ptr;
+        rin.n = n;
+        rin.k = k;
+        rin.hnorm = hnorm;
+        rin.opt = opt;
+        rin.max_outer = lowp_mode ? std::min(std::max(1, opt.refine_maxiter), 12)
+                                  : std::max(1, opt.refine_maxiter);
+        rin.inner_maxiter = std::max(1, opt.inner_maxiter);
+        rin.inner_tol = opt.inner_tol > 0.0 ? opt.inner_tol : 1e-3;
+        rin.opt.ipt_maxiter = opt.ipt_maxiter;
+        IPTGB_CHECK(Xfb.alloc((size_t)n * k, s));
+        bool conv = false;
+        IPTGB_CHECK(refine_solve(rin, xout, d_values, report, s, &conv, Xfb.ptr));
+        done = conv;
+    }
+    if (!done) {
+        // Davidson (the requested strategy, or the fallback when the IPT
+        // fixed point stopped improving: restart from the refined block)
+        IPTBlockReport first = *report;
+        BlockSolveInput in;
+        in.apply = &apply;
+        in.ipt = stage.get();
+        in.learned = learned.get();
+        in.d = d.ptr;
+        in.n = n;
+        in.k = k;
+        in.hnorm = hnorm;
+        in.opt = opt;
+        in.lowp = lowp_mode;
+        if (Xfb.ptr != nullptr) {
+            in.initial = Xfb.ptr;
+            in.initial_cols = k;
+        }
+        IPTGB_CHECK(block_solve(in, xout, d_values, report, s));
+        if (Xfb.ptr != nullptr) {
+            report->ipt_iterations += first.ipt_iterations;
+            report->lowp_matvecs += first.lowp_matvecs;
+            report->fp64_matvecs += first.fp64_matvecs;
+            report->total_ms += first.total_ms;
+            report->ipt_ms += first.ipt_ms;
+        }
+    }
     if (permuted) {
         unpermute_rows_kernel<<<blocks_for((size_t)n * k), kThreads, 0, s>>>(Xtmp.ptr, dperm.ptr,
                                                                               n, k, d_vectors);
@@ -386,16 +458,43 @@ int csr_block_device(const int *row_ptr, const int *col_ind, const double *vals,
     if (opt.preconditioner == IPT_BLOCK_PRECOND_MLP) {
         learned.reset(make_learned_correction(opt.mlp_params, s));
     }
-    BlockSolveInput in;
-    in.apply = &apply;
-    in.ipt = stage.get();
-    in.learned = learned.get();
-    in.d = dd;
-    in.n = n;
-    in.k = k;
-    in.hnorm = hnorm;
-    in.opt = opt;
-    IPTGB_CHECK(block_solve(in, d_vectors, d_values, report, s));
+    DeviceBuffer<double> Xfb;
+    bool done = false;
+    if (opt.strategy == IPT_BLOCK_STRATEGY_REFINE && k <= 64) {
+        RefineInput rin;
+        rin.apply = &apply;
+        rin.d = dd;
+        rin.n = n;
+        rin.k = k;
+        rin.hnorm = hnorm;
+        rin.opt = opt;
+        rin.max_outer = std::max(1, opt.refine_maxiter);
+        IPTGB_CHECK(Xfb.alloc((size_t)n * k, s));
+        bool conv = false;
+        IPTGB_CHECK(refine_solve(rin, d_vectors, d_values, report, s, &conv, Xfb.ptr));
+        done = conv;
+    }
+    if (!done) {
+        IPTBlockReport first = *report;
+        BlockSolveInput in;
+        in.apply = &apply;
+        in.ipt = stage.get();
+        in.learned = learned.get();
+        in.d = dd;
+        in.n = n;
+        in.k = k;
+        in.hnorm = hnorm;
+        in.opt = opt;
+        if (Xfb.ptr != nullptr) {
+            in.initial = Xfb.ptr;
+            in.initial_cols = k;
+        }
+        IPTGB_CHECK(block_solve(in, d_vectors, d_values, report, s));
+        if (Xfb.ptr != nullptr) {
+            report->fp64_matvecs += first.fp64_matvecs;
+            report->total_ms += first.total_ms;
+        }
+    }
     IPTGB_CUDA(cudaStreamSynchronize(s));
     return IPT_CUDA_SUCCESS;
 }

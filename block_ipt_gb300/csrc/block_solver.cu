@@ -37,6 +37,10 @@ void fill_default_options(IPTBlockOptions *opt)
     opt->preconditioner = IPT_BLOCK_PRECOND_DIAGONAL;
     opt->mlp_params = nullptr;
     opt->stream = nullptr;
+    opt->strategy = IPT_BLOCK_STRATEGY_REFINE;
+    opt->refine_maxiter = 300;
+    opt->inner_maxiter = 64;
+    opt->inner_tol = 1e-3;
 }
 
 namespace {
@@ -153,8 +157,17 @@ int block_solve(const BlockSolveInput &in, double *X_out, double *values_out,
     int ipt_iters = 0;
     double ipt_res = NAN;
     long long lowp_mv = 0;
-    IPTGB_CHECK(in.ipt->run(p, opt.ipt_maxiter, opt.ipt_tol, std::max(1, opt.ipt_check_every),
-                            Vt.ptr, &ipt_iters, &ipt_res, &lowp_mv));
+    if (in.initial != nullptr) {
+        // start block given (e.g. from the refinement driver): its columns,
+        // then unit vectors of the next diagonal positions up to p
+        IPTGB_CHECK(launch_set_identity(Vt.ptr, n, p, s));
+        IPTGB_CUDA(cudaMemcpyAsync(Vt.ptr, in.initial,
+                                   (size_t)n * std::min(p, in.initial_cols) * sizeof(double),
+                                   cudaMemcpyDeviceToDevice, s));
+    } else {
+        IPTGB_CHECK(in.ipt->run(p, opt.ipt_maxiter, opt.ipt_tol, std::max(1, opt.ipt_check_every),
+                                Vt.ptr, &ipt_iters, &ipt_res, &lowp_mv));
+    }
     rep->ipt_iterations = ipt_iters;
     rep->ipt_fixed_point_residual = ipt_res;
     if (in.lowp) {

@@ -31,7 +31,11 @@ struct LearnedCorrection {
                         int nsel, int n, double clip, double *T) = 0;
 };
 
+struct LowpDenseOperator;
+
 struct BlockSolveInput {
+    const double *initial = nullptr;  // optional start block (n x initial_cols), skips the IPT stage
+    int initial_cols = 0;
     Fp64Apply *apply = nullptr;
     IptStage *ipt = nullptr;
     LearnedCorrection *learned = nullptr;
@@ -45,6 +49,29 @@ struct BlockSolveInput {
 
 int block_solve(const BlockSolveInput &in, double *X_out, double *values_out,
                 IPTBlockReport *report, cudaStream_t stream);
+
+struct RefineInput {
+    Fp64Apply *apply = nullptr;
+    IptStage *ipt = nullptr;            // low-precision IPT start, or nullptr (identity start)
+    LowpDenseOperator *lowp = nullptr;  // correction solver, or nullptr (plain FP64 IPT steps)
+    const double *d = nullptr;
+    int n = 0;
+    int k = 0;
+    double hnorm = 1.0;
+    int max_outer = 8;
+    int inner_maxiter = 64;
+    double inner_tol = 1e-3;
+    IPTBlockOptions opt{};
+};
+
+// Refinement driver (refine.cu).  On return *converged tells whether the
+// Ritz pairs in X_out / values_out met the tolerance; if not, X_fallback
+// (n x k) holds the best block for a Davidson restart.
+int refine_solve(const RefineInput &in, double *X_out, double *values_out, IPTBlockReport *report,
+                 cudaStream_t stream, bool *converged, double *X_fallback);
+
+// IPT stage running on an existing low-precision operator (not owned).
+IptStage *make_lowp_stage_on(LowpDenseOperator *op, const double *d, int n, cudaStream_t stream);
 
 void fill_default_options(IPTBlockOptions *opt);
 

@@ -465,6 +465,86 @@ __global__ void f32_to_f64_kernel(const float *__restrict__ in, size_t count, do
 }
 
 // ---------------------------------------------------------------------------
+// Mixed refinement: low-precision correction solve (see lowp.h).
+// ---------------------------------------------------------------------------
+template <typename LP>
+__global__ void refine_begin_kernel(const double *__restrict__ R0, const double *__restrict__ X,
+                                    const double *__restrict__ c, const float *__restrict__ sigma_in,
+                                    int use_sigma, int n, int p, int ldx, float *__restrict__ d32,
+                                    LP *__restrict__ dlp, float *__restrict__ R32,
+                                    float *__restrict__ X32, float *__restrict__ c32,
+                                    float *__restrict__ sig, float *__restrict__ sig_inv)
+{
+    const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e < (size_t)p) {
+        const float sg = use_sigma ? sigma_in[e] : 1.0f;
+        sig[e] = sg;
+        sig_inv[e] = 1.0f / sg;
+        c32[e] = (float)c[e];
+    }
+    if (e >= (size_t)n * p) return;
+    const int row = (int)(e % (size_t)n);
+    const int col = (int)(e / (size_t)n);
+    const float sg = use_sigma ? sigma_in[col] : 1.0f;
+    const float r = (float)R0[e];
+    d32[e] = r;
+    R32[e] = r;
+    X32[e] = (float)X[e];
+    dlp[(size_t)row + (size_t)col * ldx] = to_lp<LP>(r * sg);
+}
+
+template <typename LP>
+__global__ void refine_update_kernel(const float *__restrict__ P, int S, int n, int p,
+                                     float inv_scale, const float *__restrict__ sig,
+                                     const float *__restrict__ sig_inv, const float *__restrict__ G,
+                                     const float *__restrict__ R32, const float *__restrict__ X32,
+                                     const float *__restrict__ c32, const float *__restrict__ dcur,
+                                     float *__restrict__ dnext, LP *__restrict__ dlp, int ldx,
+                                     int want_norms, double2 *partials, unsigned int *counter,
+                                     double *norms)
+{
+    const size_t elems = (size_t)n * (size_t)p;
+    const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    double dsq = 0.0, xsq = 0.0;
+    if (idx < elems) {
+        const int row = (int)(idx % (size_t)n);
+        const int col = (int)(idx / (size_t)n);
+        const float cur = dcur[idx];
+        float out = 0.0f;
+        if (row != col) {
+            float y = 0.0f, b = 0.0f;
+            for (int s = 0; s < S; ++s) {
+                const size_t base = ((size_t)s * p + col) * (size_t)n;
+                y += P[base + row];
+                b += P[base + col];
+            }
+            const float sc = inv_scale * sig_inv[col];
+            y *= sc;
+            b *= sc;
+            out = R32[idx] + (y - X32[idx] * b - cur * (c32[col] + b)) * G[idx];
+        }
+        dnext[idx] = out;
+        dlp[(size_t)row + (size_t)col * ldx] = to_lp<LP>(out * sig[col]);
+        if (want_norms) {
+            const double df = (double)out - (double)cur;
+            dsq = df * df;
+            xsq = (double)cur * (double)cur;
+        }
+    }
+    if (want_norms) {
+        const double2 t = block_sum2(dsq, xsq);
+        grid_finish_norms2(t, partials, counter, norms);
+    }
+}
+
+__global__ void refine_apply_kernel(double *__restrict__ X, const float *__restrict__ d,
+                                    size_t count)
+{
+    const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e < count) X[e] += (double)d[e];
+}
+
+// ---------------------------------------------------------------------------
 // Host side
 // ---------------------------------------------------------------------------
 namespace {
@@ -602,11 +682,30 @@ struct LowpDense final : LowpDenseOperator {
         while (tmem_cols < p_pad) tmem_cols <<= 1;
         const int row_blocks = (n + tc::kBM - 1) / tc::kBM;
         chunks_total = ldp / kchunk;
-        splits = pick_splits(row_blocks, chunks_total, sms);
+        const size_t stage_bytes0 = (size_t)(tc::kBM + p_pad) * tc::kRowBytes;
+        // Two CTAs per SM with a 4-stage pipeline when it fits in shared
+        // memory (measured faster than one 8-stage CTA per SM), and enough
+        // K splits to fill one wave of CTA slots.
+        const bool two_per_sm = 4 * stage_bytes0 + 2048 <= 113u * 1024u;
+        const int slots = sms * (two_per_sm ? 2 : 1);
+        splits = std::max(1, std::min(slots / std::max(1, row_blocks), chunks_total / 4));
+        if (splits < 1) splits = pick_splits(row_blocks, chunks_total, sms);
+        // tuning knob: IPT_GB300_TC_SPLITS overrides the split-K factor
+        const int forced = env_int("IPT_GB300_TC_SPLITS", 0);
+        if (forced > 0) {
+            splits = std::min(forced, chunks_total);
+        }
+        const int forced_stages = env_int("IPT_GB300_TC_STAGES", 0);
         chunks_per_split = (chunks_total + splits - 1) / splits;
         splits = (chunks_total + chunks_per_split - 1) / chunks_per_split;
         const size_t stage_bytes = (size_t)(tc::kBM + p_pad) * tc::kRowBytes;
         stages = (int)std::min<size_t>(8, (200u * 1024u) / stage_bytes);
+        if (two_per_sm) {
+            stages = 4;
+        }
+        if (forced_stages >= 2) {
+            stages = std::min(stages, forced_stages);
+        }
         if (stages < 2) return IPT_CUDA_INVALID_ARGUMENT;
         smem_bytes = 1024 + stages * stage_bytes + (2 * stages + 1) * 8 + 16;
         const int afmt = LowpTypes<LP>::kind == kLowpF16 ? 0 : (LowpTypes<LP>::kind == kLowpBF16 ? 1 : 2);
@@ -690,6 +789,50 @@ struct LowpDense final : LowpDenseOperator {
 
     const float *partials() const override { return P.ptr; }
     int num_splits() const override { return splits; }
+
+    int refine_begin(const double *R0, const double *X, const double *c,
+                     const float *sigma) override
+    {
+        const size_t elems = (size_t)n * p;
+        if (R32.count < elems) {
+            IPTGB_CHECK(R32.alloc(elems, s));
+            IPTGB_CHECK(Xref32.alloc(elems, s));
+            IPTGB_CHECK(small.alloc(4 * (size_t)p, s));
+        }
+        refine_begin_kernel<LP><<<blocks_for(elems), kThreads, 0, s>>>(
+            R0, X, c, sigma, 1, n, p, ldp, X32[0].ptr, Xlp[0].ptr, R32.ptr, Xref32.ptr,
+            small.ptr, small.ptr + p, small.ptr + 2 * p);
+        IPTGB_LAUNCH();
+        cur = 0;
+        return IPT_CUDA_SUCCESS;
+    }
+
+    int refine_step(int want_norms, NormScratch *ns) override
+    {
+        IPTGB_CHECK(product());
+        const size_t elems = (size_t)n * p;
+        const int grid = blocks_for(elems);
+        if (want_norms && grid > ns->capacity) return IPT_CUDA_INVALID_ARGUMENT;
+        const int nxt = cur ^ 1;
+        KernelTimerScope timer(kProfLowpUpdate, s);
+        refine_update_kernel<LP><<<grid, kThreads, 0, s>>>(
+            P.ptr, splits, n, p, (float)(1.0 / scale), small.ptr + p, small.ptr + 2 * p, G.ptr,
+            R32.ptr, Xref32.ptr, small.ptr, X32[cur].ptr, X32[nxt].ptr, Xlp[nxt].ptr, ldp,
+            want_norms, ns->partials, ns->counter, ns->norms);
+        IPTGB_LAUNCH();
+        cur = nxt;
+        return IPT_CUDA_SUCCESS;
+    }
+
+    int refine_apply(double *X) override
+    {
+        refine_apply_kernel<<<blocks_for((size_t)n * p), kThreads, 0, s>>>(X, X32[cur].ptr,
+                                                                          (size_t)n * p);
+        IPTGB_LAUNCH();
+        return IPT_CUDA_SUCCESS;
+    }
+
+    DeviceBuffer<float> R32, Xref32, small;  // small: c32 | sigma | 1/sigma
 
     int sms = 148;
     int n = 0;
@@ -801,6 +944,51 @@ struct LowpDenseSimtF32 final : LowpDenseOperator {
     const float *partials() const override { return P.ptr; }
     int num_splits() const override { return splits; }
 
+    int refine_begin(const double *R0, const double *X, const double *c,
+                     const float *sigma) override
+    {
+        const size_t elems = (size_t)n * p;
+        if (R32.count < elems) {
+            IPTGB_CHECK(R32.alloc(elems, s));
+            IPTGB_CHECK(Xref32.alloc(elems, s));
+            IPTGB_CHECK(small.alloc(4 * (size_t)p, s));
+        }
+        // FP32 operands need no column scaling
+        refine_begin_kernel<float><<<blocks_for(elems), kThreads, 0, s>>>(
+            R0, X, c, sigma, 0, n, p, n, X32[0].ptr, X32[0].ptr, R32.ptr, Xref32.ptr, small.ptr,
+            small.ptr + p, small.ptr + 2 * p);
+        IPTGB_LAUNCH();
+        cur = 0;
+        return IPT_CUDA_SUCCESS;
+    }
+
+    int refine_step(int want_norms, NormScratch *ns) override
+    {
+        IPTGB_CHECK(product());
+        const size_t elems = (size_t)n * p;
+        const int grid = blocks_for(elems);
+        if (want_norms && grid > ns->capacity) return IPT_CUDA_INVALID_ARGUMENT;
+        const int nxt = cur ^ 1;
+        KernelTimerScope timer(kProfLowpUpdate, s);
+        refine_update_kernel<float><<<grid, kThreads, 0, s>>>(
+            P.ptr, splits, n, p, 1.0f, small.ptr + p, small.ptr + 2 * p, G.ptr, R32.ptr,
+            Xref32.ptr, small.ptr, X32[cur].ptr, X32[nxt].ptr, X32[nxt].ptr, n, want_norms,
+            ns->partials, ns->counter, ns->norms);
+        IPTGB_LAUNCH();
+        cur = nxt;
+        return IPT_CUDA_SUCCESS;
+    }
+
+    int refine_apply(double *X) override
+    {
+        refine_apply_kernel<<<blocks_for((size_t)n * p), kThreads, 0, s>>>(X, X32[cur].ptr,
+                                                                          (size_t)n * p);
+        IPTGB_LAUNCH();
+        return IPT_CUDA_SUCCESS;
+    }
+
+    DeviceBuffer<float> R32, Xref32, small;
+
     int n = 0, p = 0, sms = 148, splits = 1, cur = 0;
     cudaStream_t s = nullptr;
     DeviceBuffer<float> delta, G, P;
@@ -850,7 +1038,8 @@ LowpDenseOperator *make_lowp_dense_operator(const double *dH, int n, int kind, c
 // The IPT stage of the block solver on the low-precision operator.
 // ---------------------------------------------------------------------------
 struct LowpStage final : IptStage {
-    std::unique_ptr<LowpDenseOperator> op;
+    std::unique_ptr<LowpDenseOperator> owned;
+    LowpDenseOperator *op = nullptr;
     const double *d = nullptr;
     int n = 0;
     cudaStream_t s = nullptr;
@@ -875,7 +1064,18 @@ IptStage *make_lowp_dense_stage(const double *dH, int n, const double *d, int pr
         return nullptr;
     }
     auto *st = new LowpStage();
-    st->op.reset(op);
+    st->owned.reset(op);
+    st->op = op;
+    st->d = d;
+    st->n = n;
+    st->s = stream;
+    return st;
+}
+
+IptStage *make_lowp_stage_on(LowpDenseOperator *op, const double *d, int n, cudaStream_t stream)
+{
+    auto *st = new LowpStage();
+    st->op = op;
     st->d = d;
     st->n = n;
     st->s = stream;

@@ -26,6 +26,18 @@ struct LowpDenseOperator {
     virtual int export_fp64_prev(double *X) = 0;             // previous block -> FP64
     virtual const float *partials() const = 0;               // [split][col][row] FP32
     virtual int num_splits() const = 0;
+
+    // Correction solve of the mixed refinement (after set_width/reset_identity
+    // sized the block).  With the FP64 defect R0 = F(X) - X of the current
+    // FP64 block X and c_j = (Delta X)_jj, iterate in low precision
+    //   delta <- R0 + G o (B - X diag(b) - delta diag(c + b)),  B = Delta delta,
+    // b_j = B_jj, which converges to the exact correction X* - X of the IPT
+    // fixed point.  The operand copy of column j is scaled by sigma_j (a
+    // power of two chosen from max |R0_j|) to use the FP16 range.
+    virtual int refine_begin(const double *R0, const double *X, const double *c,
+                             const float *sigma) = 0;
+    virtual int refine_step(int want_norms, NormScratch *ns) = 0;
+    virtual int refine_apply(double *X) = 0;  // X += delta (FP64)
 };
 
 LowpDenseOperator *make_lowp_dense_operator(const double *dH, int n, int kind, cudaStream_t s,

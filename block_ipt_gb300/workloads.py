@@ -94,3 +94,98 @@ def batch_config2(count=512, seed=0):
 
 def batch_instance(n, sigma, seed):
     return dense_config0(n=n, seed=seed, sigma=sigma)
+
+
+# ---------------------------------------------------------------------------
+# FCI-like sparse Hamiltonians
+# ---------------------------------------------------------------------------
+def _strings(norb, nel):
+    """Occupation bitstrings of nel electrons in norb orbitals, lexicographic."""
+    from itertools import combinations
+    return [sum(1 << o for o in occ) for occ in combinations(range(norb), nel)]
+
+
+def _links(strings, norb, eps):
+    """Single and double excitation links of every string:
+    (targets, delta_eps) arrays of shape (ns, n_singles) and (ns, n_doubles),
+    delta_eps = sum(eps[particles]) - sum(eps[holes])."""
+    index = {s: i for i, s in enumerate(strings)}
+    st, sd, dt, dd = [], [], [], []
+    for s in strings:
+        occ = [o for o in range(norb) if s >> o & 1]
+        vir = [o for o in range(norb) if not s >> o & 1]
+        t1, e1, t2, e2 = [], [], [], []
+        for h in occ:
+            for p in vir:
+                t1.append(index[s ^ (1 << h) ^ (1 << p)])
+                e1.append(eps[p] - eps[h])
+        for ia in range(len(occ)):
+            for ib in range(ia + 1, len(occ)):
+                for pa in range(len(vir)):
+                    for pb in range(pa + 1, len(vir)):
+                        h1, h2, p1, p2 = occ[ia], occ[ib], vir[pa], vir[pb]
+                        t2.append(index[s ^ (1 << h1) ^ (1 << h2) ^ (1 << p1) ^ (1 << p2)])
+                        e2.append(eps[p1] + eps[p2] - eps[h1] - eps[h2])
+        st.append(t1)
+        sd.append(e1)
+        dt.append(t2)
+        dd.append(e2)
+    return (np.array(st, np.int64), np.array(sd), np.array(dt, np.int64), np.array(dd))
+
+
+def fci_like_csr(norb=10, nalpha=5, nbeta=5, seed=0, sigma=0.05):
+    """FCI-like symmetric CSR matrix over all (alpha, beta) string pairs.
+
+    Determinant I = ia * n_beta_strings + ib.  Orbital energies
+    eps_p = 0.5 p + N(0, 0.05); H_II = sum of occupied eps (both spins) +
+    N(0, 0.01).  H_IJ != 0 only for single and double excitations (alpha,
+    beta, alpha-alpha, beta-beta, alpha-beta); its value is
+    sigma * N(0,1)[seed, min(I,J), max(I,J)] * exp(-|d eps|), with d eps the
+    particle-minus-hole orbital energy of the excitation, so H is exactly
+    symmetric.  Returns (row_ptr, col_ind, values, diag) with rows sorted by
+    column (int32 indices, float64 values); the diagonal is stored in the rows.
+    """
+    eps = 0.5 * np.arange(norb) + 0.05 * normal(seed, 31, np.arange(norb), np.zeros(norb, np.int64))
+    sa = _strings(norb, nalpha)
+    sb = _strings(norb, nbeta)
+    na, nb = len(sa), len(sb)
+    a_st, a_sd, a_dt, a_dd = _links(sa, norb, eps)
+    if nbeta == nalpha:
+        b_st, b_sd, b_dt, b_dd = a_st, a_sd, a_dt, a_dd
+    else:
+        b_st, b_sd, b_dt, b_dd = _links(sb, norb, eps)
+    occ_a = np.array([sum(eps[o] for o in range(norb) if s >> o & 1) for s in sa])
+    occ_b = np.array([sum(eps[o] for o in range(norb) if s >> o & 1) for s in sb])
+    N = na * nb
+    I = np.arange(N, dtype=np.int64)
+    ia = I // nb
+    ib = I % nb
+    diag = occ_a[ia] + occ_b[ib] + 0.01 * normal(seed, 32, I, np.zeros(N, np.int64))
+    # connected columns and d eps, grouped by excitation class
+    cols = [a_st[ia] * nb + ib[:, None],                      # alpha singles
+            ia[:, None] * nb + b_st[ib],                      # beta singles
+            a_dt[ia] * nb + ib[:, None],                      # alpha-alpha doubles
+            ia[:, None] * nb + b_dt[ib],                      # beta-beta doubles
+            (a_st[ia][:, :, None] * nb + b_st[ib][:, None, :]).reshape(N, -1)]  # alpha-beta
+    des = [a_sd[ia], b_sd[ib], a_dd[ia], b_dd[ib],
+           (a_sd[ia][:, :, None] + b_sd[ib][:, None, :]).reshape(N, -1)]
+    C = np.concatenate(cols, axis=1)
+    DE = np.concatenate(des, axis=1)
+    del cols, des
+    lo = np.minimum(I[:, None], C)
+    hi = np.maximum(I[:, None], C)
+    V = sigma * normal(seed, 33, lo, hi) * np.exp(-np.abs(DE))
+    del lo, hi, DE
+    C = np.concatenate([C, I[:, None]], axis=1)
+    V = np.concatenate([V, diag[:, None]], axis=1)
+    order = np.argsort(C, axis=1, kind="stable")
+    C = np.take_along_axis(C, order, axis=1)
+    V = np.take_along_axis(V, order, axis=1)
+    per = C.shape[1]
+    row_ptr = (np.arange(N + 1, dtype=np.int64) * per).astype(np.int32)
+    return row_ptr, C.reshape(-1).astype(np.int32), V.reshape(-1), diag
+
+
+def fci_like_dims(norb, nalpha, nbeta):
+    from math import comb
+    return comb(norb, nalpha) * comb(norb, nbeta)

@@ -39,6 +39,15 @@ enum {
     IPT_BLOCK_TF32 = 3  /* TF32 tensor cores (tcgen05), FP32 accumulation */
 };
 
+/* Solver strategy.  REFINE (default): IPT fixed point refined to the FP64
+ * eigen-residual (low-precision correction solves against FP64 defects),
+ * then one Rayleigh-Ritz; falls back to DAVIDSON when the IPT map does not
+ * contract.  DAVIDSON: IPT stage, Rayleigh-Ritz, residual-driven Davidson. */
+enum {
+    IPT_BLOCK_STRATEGY_REFINE = 0,
+    IPT_BLOCK_STRATEGY_DAVIDSON = 1
+};
+
 /* Davidson preconditioner. */
 enum {
     IPT_BLOCK_PRECOND_DIAGONAL = 0, /* t_i = r_i / (d_i - theta), clipped */
@@ -57,6 +66,10 @@ typedef struct {
     int preconditioner;     /* IPT_BLOCK_PRECOND_* */
     const float *mlp_params;/* device parameters of the learned preconditioner */
     void *stream;           /* cudaStream_t, NULL = legacy default stream */
+    int strategy;           /* IPT_BLOCK_STRATEGY_* */
+    int refine_maxiter;     /* FP64 defect products of the refinement (plain FP64: IPT steps) */
+    int inner_maxiter;      /* low-precision correction iterations per refinement step */
+    double inner_tol;       /* stop the correction solve at this relative change */
 } IPTBlockOptions;
 
 typedef struct {

@@ -29,18 +29,24 @@ def check_pairs(H, X, v, k, w=None):
     assert r.max() <= RES_TOL, r.max()
 
 
-def test_block_fp64_config0(cuda):
+STRATEGIES = {"refine": 0, "davidson": 1}
+
+
+@pytest.mark.parametrize("strategy", ["refine", "davidson"])
+def test_block_fp64_config0(cuda, strategy):
     H, _ = workloads.dense_config0(1024, seed=1)
-    X, v, rep = api.block_solve_dense(H, 8, "fp64")
+    X, v, rep = api.block_solve_dense(H, 8, "fp64", strategy=STRATEGIES[strategy])
     assert rep["converged"] == 1
     w, _ = oracle.dsyevd_lowest(H, 8)
     check_pairs(H, X, v, 8, w)
 
 
-def test_block_fp64_config1_shape_small(cuda):
+@pytest.mark.parametrize("strategy", ["refine", "davidson"])
+def test_block_fp64_config1_shape_small(cuda, strategy):
     """The n=8192 construction at n=2048 (same spacing/decay), k=32."""
     H, _ = workloads.dense_config1(2048, seed=2)
-    X, v, rep = api.block_solve_dense(H, 32, "fp64", ipt_maxiter=40)
+    X, v, rep = api.block_solve_dense(H, 32, "fp64", ipt_maxiter=40,
+                                      strategy=STRATEGIES[strategy])
     assert rep["converged"] == 1
     check_pairs(H, X, v, 32)
 
@@ -66,6 +72,20 @@ def test_block_csr_banded(cuda):
     X, v, rep = api.block_solve_csr(cp, ri, va, 64, 5, "fp64")
     Hd = oracle.csc_to_dense(cp, ri, va, 64)
     check_pairs(Hd, X, v, 5)
+
+
+def test_refine_falls_back_to_davidson_on_near_degenerate_targets(cuda):
+    """Targets 1 and 2 nearly degenerate and strongly coupled: the IPT map
+    does not contract there, so the refinement hands over to Davidson, which
+    still returns the FP64-accurate pairs."""
+    H, _ = workloads.dense_config0(400, seed=7)
+    H = np.array(H)
+    H[1, 1] = H[2, 2] = 1.5
+    H[1, 2] = H[2, 1] = 0.3
+    H = np.asfortranarray(H)
+    X, v, rep = api.block_solve_dense(H, 6, "fp64")
+    assert rep["converged"] == 1
+    check_pairs(H, X, v, 6)
 
 
 def test_block_csr_random_sparse(cuda):

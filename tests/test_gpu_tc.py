@@ -98,10 +98,12 @@ def check_pairs(H, X, v, k):
     assert r.max() <= 1e-8, r.max()
 
 
+@pytest.mark.parametrize("strategy", [0, 1])
 @pytest.mark.parametrize("prec", ["fp16", "bf16", "tf32"])
-def test_block_mixed_config1_shape_small(cuda, prec):
+def test_block_mixed_config1_shape_small(cuda, prec, strategy):
     H, _ = workloads.dense_config1(2048, seed=4)
-    X, v, rep = api.block_solve_dense(H, 32, prec, ipt_maxiter=60, ipt_check_every=4)
+    X, v, rep = api.block_solve_dense(H, 32, prec, ipt_maxiter=60, ipt_check_every=4,
+                                      strategy=strategy)
     assert rep["converged"] == 1
     assert rep["lowp_matvecs"] > 0
     check_pairs(H, X, v, 32)
@@ -113,3 +115,13 @@ def test_block_mixed_config1_full(cuda):
     X, v, rep = api.block_solve_dense(H, 32, "fp16", ipt_maxiter=80, ipt_check_every=8)
     assert rep["converged"] == 1
     check_pairs(H, X, v, 32)
+    # the refinement needs only a few FP64 block products
+    assert rep["fp64_matvecs"] <= 4 * 32
+
+
+def test_mixed_refine_uses_fewer_fp64_products_than_plain(cuda):
+    H, _ = workloads.dense_config1(2048, seed=9)
+    _, _, rep_mixed = api.block_solve_dense(H, 16, "fp16", ipt_maxiter=60, ipt_check_every=4)
+    _, _, rep_plain = api.block_solve_dense(H, 16, "fp64")
+    assert rep_mixed["converged"] == 1 and rep_plain["converged"] == 1
+    assert rep_mixed["fp64_matvecs"] * 3 <= rep_plain["fp64_matvecs"]
