@@ -55,6 +55,8 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-lapack", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-fci", action="store_true")
+    ap.add_argument("--fci-steps", type=int, default=2)
     return ap.parse_args()
 
 
@@ -226,6 +228,73 @@ def profile_snapshot(lib):
     return out
 
 
+def fci_section(args, torch, lib, stream, flush, dev):
+    """The FCI-like sparse workload (10 orbitals, 5+5 electrons, n = 63,504,
+    nnz = 55.6M, k = 16): FP64 CSR block solve, device-resident input."""
+    from scipy.sparse import csr_matrix
+
+    from block_ipt_gb300 import _lib, api, workloads
+    rp, ci, v, d = workloads.fci_like_csr(10, 5, 5, seed=0)
+    n, k = len(rp) - 1, 16
+    perm = np.argsort(d, kind="stable")
+    Hs = csr_matrix((v, ci, rp), shape=(n, n))[perm][:, perm].tocsr()
+    Hs.sort_indices()
+    drp = torch.from_numpy(Hs.indptr.astype(np.int32)).to(dev)
+    dci = torch.from_numpy(Hs.indices.astype(np.int32)).to(dev)
+    dvv = torch.from_numpy(Hs.data).to(dev)
+    dX = torch.empty((k, n), dtype=torch.float64, device=dev)
+    dw = torch.empty(k, dtype=torch.float64, device=dev)
+    opt = api.block_options("fp64", stream=stream.cuda_stream)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+
+    def solve():
+        rep = _lib.IPTBlockReport()
+        st = lib.ipt_block_solve_csr_device(C.c_void_p(drp.data_ptr()), C.c_void_p(dci.data_ptr()),
+                                            C.c_void_p(dvv.data_ptr()), n, int(Hs.nnz), k,
+                                            C.byref(opt), C.c_void_p(dX.data_ptr()),
+                                            C.c_void_p(dw.data_ptr()), C.byref(rep))
+        assert st == 0, _lib.status_string(st)
+        return rep.as_dict()
+
+    solve()
+    lib.ipt_block_profile_reset()
+    lib.ipt_block_profile_enable(1)
+    times, rep = [], None
+    for _ in range(max(1, args.fci_steps)):
+        flush.zero_()
+        e0.record(stream)
+        rep = solve()
+        e1.record(stream)
+        e1.synchronize()
+        times.append(e0.elapsed_time(e1))
+    lib.ipt_block_profile_enable(0)
+    prof = profile_snapshot(lib)
+    X = dX.T.cpu().numpy()
+    w = dw.cpu().numpy()
+    hn = float(abs(Hs).sum(axis=1).max())
+    res = float((np.linalg.norm(Hs @ X - X * w[None, :], axis=0) / max(1.0, hn)).max())
+    dl = None
+    try:
+        with open(os.path.join(ROOT, "tests", "golden", "fci_eigs.json")) as f:
+            ref = np.array(json.load(f)["fci_10o_5a5b_seed0"]["eigenvalues"])
+        dl = float(np.abs(w - ref).max() / hn)
+    except (OSError, KeyError):
+        pass
+    cp_ms, cp_cnt = prof["csr_product"]
+    flops = 2.0 * Hs.nnz * sum(1 for _ in range(1))  # per column
+    cols = rep["fp64_matvecs"]
+    achieved = (2.0 * Hs.nnz * cols * len(times)) / (cp_ms * 1e-3) / 1e12 if cp_ms else None
+    return {"workload": "FCI-like CSR, 10 orbitals 5a/5b, n=%d nnz=%d, k=%d, seed 0" % (n, Hs.nnz, k),
+            "ms": statistics.mean(times), "report": {kk: rep[kk] for kk in (
+                "converged", "ipt_iterations", "davidson_steps", "restarts", "basis_cols",
+                "fp64_matvecs", "total_ms")},
+            "check": {"max_scaled_residual": res, "max_abs_dlambda_over_norm_inf": dl},
+            "csr_product": {"launches": cp_cnt, "ms_per_solve": cp_ms / len(times),
+                            "achieved_fp64_tflops": achieved},
+            "kernel_ms": {kk: round(val[0] / len(times), 4) for kk, val in prof.items() if val[1]}}
+
+
 def run_ours(args):
     import torch
     import torch.distributed as dist
@@ -373,6 +442,10 @@ def run_ours(args):
     if roofline is None:
         roofline = roofline_lowp
 
+    fci = None
+    if not args.no_fci and rank == 0:
+        fci = fci_section(args, torch, lib, stream, flush, dev)
+
     cpu = None
     if not args.no_cpu and rank == 0:
         prods = plain_products(n, k, args.seed)
@@ -417,6 +490,7 @@ def run_ours(args):
                 "ipt_iterations", "davidson_steps", "fp64_matvecs", "total_ms", "converged")}
                 if fp64_dav_rep else None),
             "kernel_ms": {kk: round(v[0] / steps, 4) for kk, v in prof.items() if v[1]},
+            "fci_config3": fci,
         }
         print(json.dumps(line), flush=True)
     if world > 1:

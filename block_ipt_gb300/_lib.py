@@ -191,6 +191,7 @@ SIGNATURES = [
     ("ipt_mixed_precision_fp32_cuda_free_device_result", None, [C.POINTER(_MixedResult)]),
     ("ipt_mixed_precision_tf32_cuda_free_device_result", None, [C.POINTER(_MixedResult)]),
     ("ipt_block_default_options", None, [C.POINTER(IPTBlockOptions)]),
+    ("ipt_block_symmetric_eig", _i, [_vp, _i, _vp, _vp, _vp]),
     ("ipt_cuda_device_tol_noalloc", _i, [_vp, _i, _i, _d, _i, _vp, _vp, _vp, _ip, _dp]),
     ("ipt_block_launch_count", C.c_longlong, []),
     ("ipt_block_profile_enable", None, [_i]),

@@ -441,6 +441,59 @@ int csr_block_device(const int *row_ptr, const int *col_ind, const double *vals,
         IPTGB_CHECK(d.alloc((size_t)n, s));
         IPTGB_CHECK(launch_csr64_diagonal(row_ptr, col_ind, vals, n, d.ptr, s));
         dd = d.ptr;
+        // The targets are the k lowest diagonal positions in ascending order,
+        // i.e. the first k rows of a diagonal-sorted matrix.  An unsorted
+        // matrix goes through the host preparation (sort + symmetric
+        // permutation, ipt_preparation.cu:1375-1431) and the rows of the
+        // result are scattered back to the caller's order.
+        std::vector<double> hd((size_t)n);
+        IPTGB_CUDA(cudaMemcpyAsync(hd.data(), d.ptr, (size_t)n * sizeof(double),
+                                   cudaMemcpyDeviceToHost, s));
+        IPTGB_CUDA(cudaStreamSynchronize(s));
+        if (!std::is_sorted(hd.begin(), hd.end())) {
+            std::vector<int> rp((size_t)n + 1U), ci((size_t)nnz);
+            std::vector<double> cv((size_t)nnz);
+            IPTGB_CUDA(cudaMemcpyAsync(rp.data(), row_ptr, rp.size() * sizeof(int),
+                                       cudaMemcpyDeviceToHost, s));
+            if (nnz > 0) {
+                IPTGB_CUDA(cudaMemcpyAsync(ci.data(), col_ind, ci.size() * sizeof(int),
+                                           cudaMemcpyDeviceToHost, s));
+                IPTGB_CUDA(cudaMemcpyAsync(cv.data(), vals, cv.size() * sizeof(double),
+                                           cudaMemcpyDeviceToHost, s));
+            }
+            IPTGB_CUDA(cudaStreamSynchronize(s));
+            PreparedCsr prep;
+            IPTGB_CHECK(prepare_csc(rp.data(), ci.data(), cv.data(), n, nnz, true, &prep));
+            DeviceBuffer<int> prp, pci, dperm;
+            DeviceBuffer<double> pcv, pd, Xs;
+            IPTGB_CHECK(prp.alloc(prep.row_ptr.size(), s));
+            IPTGB_CHECK(pci.alloc(prep.col_ind.size(), s));
+            IPTGB_CHECK(pcv.alloc(prep.vals.size(), s));
+            IPTGB_CHECK(pd.alloc((size_t)n, s));
+            IPTGB_CHECK(Xs.alloc((size_t)n * k, s));
+            IPTGB_CHECK(dperm.alloc((size_t)n, s));
+            IPTGB_CUDA(cudaMemcpyAsync(prp.ptr, prep.row_ptr.data(),
+                                       prep.row_ptr.size() * sizeof(int), cudaMemcpyHostToDevice, s));
+            if (prep.nnz > 0) {
+                IPTGB_CUDA(cudaMemcpyAsync(pci.ptr, prep.col_ind.data(),
+                                           prep.col_ind.size() * sizeof(int),
+                                           cudaMemcpyHostToDevice, s));
+                IPTGB_CUDA(cudaMemcpyAsync(pcv.ptr, prep.vals.data(),
+                                           prep.vals.size() * sizeof(double),
+                                           cudaMemcpyHostToDevice, s));
+            }
+            IPTGB_CUDA(cudaMemcpyAsync(pd.ptr, prep.diag.data(), (size_t)n * sizeof(double),
+                                       cudaMemcpyHostToDevice, s));
+            IPTGB_CUDA(cudaMemcpyAsync(dperm.ptr, prep.perm.data(), (size_t)n * sizeof(int),
+                                       cudaMemcpyHostToDevice, s));
+            IPTGB_CHECK(csr_block_device(prp.ptr, pci.ptr, pcv.ptr, n, prep.nnz, k, &opt, pd.ptr,
+                                         Xs.ptr, d_values, report));
+            unpermute_rows_kernel<<<blocks_for((size_t)n * k), kThreads, 0, s>>>(
+                Xs.ptr, dperm.ptr, n, k, d_vectors);
+            IPTGB_LAUNCH();
+            IPTGB_CUDA(cudaStreamSynchronize(s));
+            return IPT_CUDA_SUCCESS;
+        }
     }
     IPTGB_CHECK(rs.alloc((size_t)n, s));
     csr_row_abs_sum_kernel<<<blocks_for(n), kThreads, 0, s>>>(row_ptr, vals, n, rs.ptr);
@@ -502,6 +555,23 @@ int csr_block_device(const int *row_ptr, const int *col_ind, const double *vals,
 }  // namespace iptgb
 
 using namespace iptgb;
+
+IPT_API int ipt_block_symmetric_eig(const double *d_T, int m, double *d_w, double *d_Z,
+                                    void *stream)
+{
+    if (d_T == nullptr || d_w == nullptr || d_Z == nullptr || m <= 0 || m > 112) {
+        return IPT_CUDA_INVALID_ARGUMENT;
+    }
+    BlockOps ops;
+    ops.stream = (cudaStream_t)stream;
+    ops.sms = device_sm_count();
+    int st = ops.symmetric_eig(d_T, m, d_w, d_Z, nullptr);
+    ops.release();
+    if (st == IPT_CUDA_SUCCESS && cudaStreamSynchronize(ops.stream) != cudaSuccess) {
+        st = IPT_CUDA_CUDA_ERROR;
+    }
+    return st;
+}
 
 IPT_API void ipt_block_default_options(IPTBlockOptions *options)
 {

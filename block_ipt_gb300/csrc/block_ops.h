@@ -13,6 +13,8 @@ struct BlockOps {
     int sms = 148;
     double *partials = nullptr;
     size_t partials_capacity = 0;
+    double *eig_scratch = nullptr;
+    size_t eig_capacity = 0;
 
     // C = alpha * A^T B + beta * C, A: n x ma, B: n x mb, C: ma x mb.
     int gram(const double *A, long long lda, int ma, const double *B, long long ldb, int mb, int n,
@@ -22,8 +24,9 @@ struct BlockOps {
                   long long ldc, int n, int m, int p, double alpha = 1.0, double beta = 0.0);
     // G = R^T R (one CTA); Rinv = R^{-1}; status_dev[0] = shifts used or -1.
     int chol_inverse(const double *G, int m, double *Rinv, int *status_dev);
-    // Symmetric eigensolve (one CTA Jacobi): ascending w, eigenvectors Z.
-    int jacobi_eig(const double *T, int m, double *w, double *Z, int *sweeps_dev);
+    // Symmetric eigensolve for m <= 112: FP32 Jacobi + FP64 refinement +
+    // FP64 cluster polish (k_eig.cu).  Ascending w, eigenvectors Z.
+    int symmetric_eig(const double *T, int m, double *w, double *Z, int *sweeps_dev);
     // R = AX - X diag(theta); rnorm[j] = ||r_j||; scaled[j] as the reference.
     int residuals(const double *X, const double *AX, const double *theta, int n, int k,
                   long long ldx, double hnorm, double *R, double *rnorm, double *scaled);

@@ -293,143 +293,6 @@ __global__ void chol_inverse_kernel(const double *__restrict__ G, int m, double 
 }
 
 // ---------------------------------------------------------------------------
-// One-CTA cyclic Jacobi eigensolver for a symmetric m x m matrix (column-major
-// in, ld = m).  Parallel round-robin ordering: m/2 disjoint rotations per
-// round, m-1 rounds per sweep.  Output: ascending eigenvalues w[m] and the
-// matching orthonormal eigenvectors Z (column-major, ld = m).
-// Dynamic shared memory: 2 * M * M + 3 * M doubles, M = m rounded up to even.
-// ---------------------------------------------------------------------------
-__global__ void jacobi_eig_kernel(const double *__restrict__ T, int m, double *__restrict__ w,
-                                  double *__restrict__ Z, int max_sweeps, int *sweeps_out)
-{
-    extern __shared__ double sm[];
-    const int M = (m + 1) & ~1;
-    double *A = sm;              // row-major M x M
-    double *V = sm + M * M;      // row-major M x M
-    double *cs = sm + 2 * M * M; // c[M/2], s[M/2]
-    int *pr = (int *)(cs + M);   // pair indices p[M/2], q[M/2]
-    __shared__ double off_norm;
-    __shared__ double tot_norm;
-    const int tid = threadIdx.x;
-    const int nt = blockDim.x;
-    const int half = M / 2;
-    for (int e = tid; e < M * M; e += nt) {
-        const int i = e / M;
-        const int j = e % M;
-        double a = 0.0;
-        if (i < m && j < m) {
-            a = 0.5 * (T[(size_t)j * m + i] + T[(size_t)i * m + j]);
-        }
-        A[e] = a;
-        V[e] = i == j ? 1.0 : 0.0;
-    }
-    __syncthreads();
-    int sweep = 0;
-    for (; sweep < max_sweeps; ++sweep) {
-        // convergence test on the off-diagonal mass
-        double off = 0.0, tot = 0.0;
-        for (int e = tid; e < M * M; e += nt) {
-            const double a = A[e];
-            tot += a * a;
-            if (e / M != e % M) {
-                off += a * a;
-            }
-        }
-        double2 t = block_sum2(off, tot);
-        if (tid == 0) {
-            off_norm = t.x;
-            tot_norm = t.y;
-        }
-        __syncthreads();
-        // relative off-diagonal Frobenius mass <= 1e-13 (the rounding floor of
-        // the rotations sits near m * 1e-16, so a tighter test may never pass)
-        if (off_norm <= 1e-26 * tot_norm || off_norm == 0.0) {
-            break;
-        }
-        for (int r = 0; r < M - 1; ++r) {
-            for (int k = tid; k < half; k += nt) {
-                int p, q;
-                if (k == 0) {
-                    p = M - 1;
-                    q = r;
-                } else {
-                    p = (r + k) % (M - 1);
-                    q = (r - k + M - 1) % (M - 1);
-                }
-                if (p > q) {
-                    const int tmp = p;
-                    p = q;
-                    q = tmp;
-                }
-                double c = 1.0, s = 0.0;
-                const double apq = A[p * M + q];
-                if (q < m && apq != 0.0) {
-                    const double app = A[p * M + p];
-                    const double aqq = A[q * M + q];
-                    if (fabs(apq) > 1e-300) {
-                        const double theta = (aqq - app) / (2.0 * apq);
-                        const double tt = (theta >= 0.0 ? 1.0 : -1.0) /
-                                          (fabs(theta) + sqrt(theta * theta + 1.0));
-                        c = 1.0 / sqrt(tt * tt + 1.0);
-                        s = tt * c;
-                    }
-                }
-                cs[k] = c;
-                cs[half + k] = s;
-                pr[k] = p;
-                pr[half + k] = q;
-            }
-            __syncthreads();
-            // columns: A <- A J, V <- V J
-            for (int e = tid; e < half * M; e += nt) {
-                const int k = e / M;
-                const int l = e % M;
-                const double c = cs[k], s = cs[half + k];
-                if (s != 0.0) {
-                    const int p = pr[k], q = pr[half + k];
-                    const double alp = A[l * M + p], alq = A[l * M + q];
-                    A[l * M + p] = c * alp - s * alq;
-                    A[l * M + q] = s * alp + c * alq;
-                    const double vlp = V[l * M + p], vlq = V[l * M + q];
-                    V[l * M + p] = c * vlp - s * vlq;
-                    V[l * M + q] = s * vlp + c * vlq;
-                }
-            }
-            __syncthreads();
-            // rows: A <- J^T A
-            for (int e = tid; e < half * M; e += nt) {
-                const int k = e / M;
-                const int l = e % M;
-                const double c = cs[k], s = cs[half + k];
-                if (s != 0.0) {
-                    const int p = pr[k], q = pr[half + k];
-                    const double apl = A[p * M + l], aql = A[q * M + l];
-                    A[p * M + l] = c * apl - s * aql;
-                    A[q * M + l] = s * apl + c * aql;
-                }
-            }
-            __syncthreads();
-        }
-    }
-    // sort ascending (selection by rank; m is small)
-    for (int i = tid; i < m; i += nt) {
-        const double ai = A[i * M + i];
-        int rank = 0;
-        for (int j = 0; j < m; ++j) {
-            const double aj = A[j * M + j];
-            rank += (aj < ai) || (aj == ai && j < i);
-        }
-        w[rank] = ai;
-        for (int l = 0; l < m; ++l) {
-            Z[(size_t)rank * m + l] = V[l * M + i];
-        }
-    }
-    if (tid == 0 && sweeps_out != nullptr) {
-        *sweeps_out = sweep;
-    }
-}
-
-// ---------------------------------------------------------------------------
 // Residual block R = AX - X diag(theta) and per-column partial sums of
 // ||r_j||^2, ||x_j||^2.  Grid: (row chunks, k).  Partials [chunk][k][2].
 // ---------------------------------------------------------------------------
@@ -614,21 +477,6 @@ int BlockOps::chol_inverse(const double *G, int m, double *Rinv, int *status_dev
     return IPT_CUDA_SUCCESS;
 }
 
-int BlockOps::jacobi_eig(const double *T, int m, double *w, double *Z, int *sweeps_dev)
-{
-    const int M = (m + 1) & ~1;
-    const size_t smem = (2 * (size_t)M * M + 2 * (size_t)M) * sizeof(double);
-    if (smem > 200 * 1024) {
-        return IPT_CUDA_INVALID_ARGUMENT;
-    }
-    IPTGB_CUDA(cudaFuncSetAttribute(jacobi_eig_kernel,
-                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    KernelTimerScope timer(kProfSmallEig, stream);
-    jacobi_eig_kernel<<<1, 512, smem, stream>>>(T, m, w, Z, 40, sweeps_dev);
-    IPTGB_LAUNCH();
-    return IPT_CUDA_SUCCESS;
-}
-
 int BlockOps::ensure_partials(size_t count)
 {
     if (count <= partials_capacity) {
@@ -650,6 +498,11 @@ void BlockOps::release()
         cudaFreeAsync(partials, stream);
         partials = nullptr;
         partials_capacity = 0;
+    }
+    if (eig_scratch != nullptr) {
+        cudaFreeAsync(eig_scratch, stream);
+        eig_scratch = nullptr;
+        eig_capacity = 0;
     }
 }
 

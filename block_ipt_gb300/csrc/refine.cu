@@ -235,6 +235,9 @@ int refine_solve(const RefineInput &in, double *X_out, double *values_out, IPTBl
         // contraction factor of the map, which can be close to one.
         const double gain = in.lowp != nullptr ? 0.5 : 0.999;
         stalls = mx > gain * prev ? stalls + 1 : 0;
+        if (mx > 2.0 * prev || mx > 1e3 * best) {
+            break;  // diverging: the map does not contract at these targets
+        }
         prev = mx;
         if (stalls >= (in.lowp != nullptr ? 2 : 4)) {
             break;
@@ -296,7 +299,7 @@ int refine_solve(const RefineInput &in, double *X_out, double *values_out, IPTBl
     IPTGB_CHECK(cholqr_pair(X.ptr, HX.ptr, Q.ptr, HQ.ptr));
     IPTGB_CHECK(cholqr_pair(Q.ptr, HQ.ptr, X.ptr, HX.ptr));  // CholQR2: basis back in X / HX
     IPTGB_CHECK(ops.gram(X.ptr, n, k, HX.ptr, n, k, n, T, k));
-    IPTGB_CHECK(ops.jacobi_eig(T, k, theta, Z, st_dev));
+    IPTGB_CHECK(ops.symmetric_eig(T, k, theta, Z, st_dev));
     IPTGB_CHECK(ops.tall_gemm(X.ptr, n, Z, k, Q.ptr, n, n, k, k));
     IPTGB_CHECK(ops.tall_gemm(HX.ptr, n, Z, k, HQ.ptr, n, n, k, k));
     IPTGB_CHECK(ops.residuals(Q.ptr, HQ.ptr, theta, n, k, n, in.hnorm, R0.ptr, rnorm, scaled));

@@ -141,7 +141,8 @@ def fci_like_csr(norb=10, nalpha=5, nbeta=5, seed=0, sigma=0.05):
     N(0, 0.01).  H_IJ != 0 only for single and double excitations (alpha,
     beta, alpha-alpha, beta-beta, alpha-beta); its value is
     sigma * N(0,1)[seed, min(I,J), max(I,J)] * exp(-|d eps|), with d eps the
-    particle-minus-hole orbital energy of the excitation, so H is exactly
+    particle-minus-hole orbital energy of the excitation (the difference of
+    the two determinants' occupied-orbital energies), so H is exactly
     symmetric.  Returns (row_ptr, col_ind, values, diag) with rows sorted by
     column (int32 indices, float64 values); the diagonal is stored in the rows.
     """
@@ -167,11 +168,13 @@ def fci_like_csr(norb=10, nalpha=5, nbeta=5, seed=0, sigma=0.05):
             a_dt[ia] * nb + ib[:, None],                      # alpha-alpha doubles
             ia[:, None] * nb + b_dt[ib],                      # beta-beta doubles
             (a_st[ia][:, :, None] * nb + b_st[ib][:, None, :]).reshape(N, -1)]  # alpha-beta
-    des = [a_sd[ia], b_sd[ib], a_dd[ia], b_dd[ib],
-           (a_sd[ia][:, :, None] + b_sd[ib][:, None, :]).reshape(N, -1)]
     C = np.concatenate(cols, axis=1)
-    DE = np.concatenate(des, axis=1)
-    del cols, des
+    del cols
+    # |d eps| of the excitation = |E_occ(J) - E_occ(I)|, written as a
+    # difference of the two determinants' occupied-orbital energies so that
+    # it is bit-identical for (I, J) and (J, I)
+    eocc = occ_a[ia] + occ_b[ib]
+    DE = eocc[C] - eocc[:, None]
     lo = np.minimum(I[:, None], C)
     hi = np.maximum(I[:, None], C)
     V = sigma * normal(seed, 33, lo, hi) * np.exp(-np.abs(DE))
