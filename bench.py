@@ -39,6 +39,11 @@ WORKLOAD = ("dense symmetric n=8192 k=32, d_i=i/8+U(0,0.1), h_ij~N(0,0.02^2)exp(
             "seed 0; FP16 tcgen05 IPT + FP64 CholQR2/Rayleigh-Ritz/Davidson to scaled residual 1e-8")
 PRODUCTS_FILE = os.path.join(ROOT, "oracle", "plain_ipt_products.json")
 MEASURED_PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
+# DRAM bytes (read + write) per launch from one ncu capture of each kernel on
+# this workload (profiles/dense64_partial_fp64_n8192_k32.md,
+# profiles/tc_partial_fp16_n8192_k32.md); keyed by (kernel, n, k, precision).
+NCU_TRAFFIC = {("dense64_partial", 8192, 32, "fp16"): 567.5e6,
+               ("tc_partial", 8192, 32, "fp16"): 137.9e6}
 
 
 def parse():
@@ -424,7 +429,9 @@ def run_ours(args):
         achieved = flops / (tot_ms * 1e-3) / 1e12
         roofline = {"kernel": "dense64_partial_kernel (FP64 SIMT split-K)", "bound": "fp64",
                     "achieved": achieved, "peak": FP64_PEAK_TFLOPS, "unit": "TFLOP/s",
-                    "frac": achieved / FP64_PEAK_TFLOPS, "traffic": None,
+                    "frac": achieved / FP64_PEAK_TFLOPS,
+                    "traffic": NCU_TRAFFIC.get(("dense64_partial", n, k, args.precision)),
+                    "traffic_unit": "bytes per launch (ncu dram__bytes_read.sum + write.sum)",
                     "peak_source": "ipt_block_measure_fp64_peak (DFMA throughput kernel, run "
                                    "live; MEASURED_PEAKS.json has no FP64 entry)",
                     "launches": cnt, "avg_launch_ms": tot_ms / max(1, cnt)}
@@ -436,7 +443,9 @@ def run_ours(args):
     roofline_lowp = {"kernel": "tc_partial_kernel (tcgen05 + TMA, %s)" % args.precision,
                      "bound": "hbm", "achieved": lp_ach, "peak": peaks["hbm_gbs"],
                      "unit": "GB/s", "frac": (lp_ach / peaks["hbm_gbs"]) if lp_ach else None,
-                     "traffic": None, "launches": lp_cnt,
+                     "traffic": NCU_TRAFFIC.get(("tc_partial", n, k, args.precision)),
+                     "traffic_unit": "bytes per launch (ncu dram__bytes_read.sum + write.sum)",
+                     "launches": lp_cnt,
                      "avg_launch_ms": lp_ms / max(1, lp_cnt),
                      "algorithmic_bytes_per_launch": lp_bytes}
     if roofline is None:

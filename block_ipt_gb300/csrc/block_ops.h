@@ -36,6 +36,12 @@ struct BlockOps {
     int column_norms(const double *A, long long lda, int n, int c, double *out);
     int gather_columns(const double *src, long long lds, const int *idx, const double *scale,
                        int n, int c, double *dst, long long ldd);
+    // Incremental projection T = V^T H V held in Tf (ld): insert the border
+    // B = V[:, :m0+c]^T (HV)[:, m0:m0+c]; copy the leading m x m block out;
+    // reset the leading m x m block to diag(theta) after a restart.
+    int proj_insert(const double *B, int m0, int c, double *Tf, int ld);
+    int proj_compact(const double *Tf, int ld, int m, double *Tm);
+    int proj_diag(const double *theta, int m, double *Tf, int ld);
 
     int ensure_partials(size_t count);
     void release();

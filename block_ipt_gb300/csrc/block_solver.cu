@@ -135,7 +135,9 @@ int block_solve(const BlockSolveInput &in, double *X_out, double *values_out,
     IPTGB_CHECK(R.alloc((size_t)n * k, s));
     IPTGB_CHECK(Xbest.alloc((size_t)n * k, s));
     const size_t mm = (size_t)maxb * maxb;
-    IPTGB_CHECK(small.alloc(4 * mm + 4 * (size_t)maxb + 4 * (size_t)k + 64, s));
+    const size_t small_head = 4 * mm + 4 * (size_t)maxb + 4 * (size_t)k + 64;
+    IPTGB_CHECK(small.alloc(small_head + mm, s));
+    double *Tf = small.ptr + small_head;  // V^T H V of the current basis, ld maxb
     double *Tm = small.ptr;
     double *Zm = Tm + mm;
     double *Gm = Zm + mm;
@@ -197,10 +199,17 @@ int block_solve(const BlockSolveInput &in, double *X_out, double *values_out,
     }
 
     // ---- 3. Rayleigh-Ritz ---------------------------------------------------
+    // The projection is kept incrementally: appending c columns at m0 costs
+    // one (m0+c) x c Gram block instead of the full m x m one.
+    auto project_new = [&](int m0, int c) -> int {
+        IPTGB_CHECK(ops.gram(V.ptr, n, m0 + c, AV.ptr + (size_t)m0 * n, n, c, n, Gm, m0 + c));
+        return ops.proj_insert(Gm, m0, c, Tf, maxb);
+    };
     IPTGB_CHECK(in.apply->apply(V.ptr, m, AV.ptr));
     rep->fp64_matvecs += m;
+    IPTGB_CHECK(project_new(0, m));
     auto rayleigh_ritz = [&]() -> int {
-        IPTGB_CHECK(ops.gram(V.ptr, n, m, AV.ptr, n, m, n, Tm, m));
+        IPTGB_CHECK(ops.proj_compact(Tf, maxb, m, Tm));
         IPTGB_CHECK(ops.symmetric_eig(Tm, m, theta, Zm, st_dev));
         IPTGB_CHECK(ops.tall_gemm(V.ptr, n, Zm, m, Xr.ptr, n, n, m, k));
         IPTGB_CHECK(ops.tall_gemm(AV.ptr, n, Zm, m, AXr.ptr, n, n, m, k));
@@ -261,6 +270,7 @@ int block_solve(const BlockSolveInput &in, double *X_out, double *values_out,
             std::swap(V.ptr, Vt.ptr);
             std::swap(AV.ptr, AVt.ptr);
             m = kr;
+            IPTGB_CHECK(ops.proj_diag(theta, m, Tf, maxb));
             ++restarts;
             if (m + nsel > maxb) {
                 nsel = maxb - m;
@@ -330,6 +340,7 @@ int block_solve(const BlockSolveInput &in, double *X_out, double *values_out,
         }
         IPTGB_CHECK(in.apply->apply(Vnew, c, AV.ptr + (size_t)m * n));
         rep->fp64_matvecs += c;
+        IPTGB_CHECK(project_new(m, c));
         const double before = max_res();
         m += c;
         IPTGB_CHECK(rayleigh_ritz());

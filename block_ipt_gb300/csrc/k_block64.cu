@@ -464,6 +464,73 @@ int BlockOps::gather_columns(const double *src, long long lds, const int *idx, c
     return IPT_CUDA_SUCCESS;
 }
 
+// ---------------------------------------------------------------------------
+// Incremental Rayleigh-Ritz projection.  Tf (ld) holds T = V^T (H V) of the
+// current basis.  After c columns are appended at m0, B = V[:, :m0+c]^T
+// (H V)[:, m0:m0+c] (ld m0+c) fills the new border of T: rows i < m0 are
+// mirrored into the new rows, the new c x c block is symmetrised.
+// ---------------------------------------------------------------------------
+__global__ void proj_insert_kernel(const double *__restrict__ B, int m0, int c,
+                                   double *__restrict__ Tf, int ld)
+{
+    const int mt = m0 + c;
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= mt * c) return;
+    const int j = e / mt;  // new column
+    const int i = e - j * mt;
+    const double b = B[e];
+    if (i < m0) {
+        Tf[(size_t)(m0 + j) * ld + i] = b;
+        Tf[(size_t)i * ld + m0 + j] = b;
+    } else {
+        const int ii = i - m0;
+        Tf[(size_t)(m0 + j) * ld + i] = 0.5 * (b + B[(size_t)ii * mt + m0 + j]);
+    }
+}
+
+// Tm (ld m) = Tf[:m, :m]
+__global__ void proj_compact_kernel(const double *__restrict__ Tf, int ld, int m,
+                                    double *__restrict__ Tm)
+{
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= m * m) return;
+    const int j = e / m;
+    const int i = e - j * m;
+    Tm[e] = Tf[(size_t)j * ld + i];
+}
+
+// Tf[:m, :m] = diag(theta[:m]): the projection onto V Z of the Ritz vectors
+__global__ void proj_diag_kernel(const double *__restrict__ theta, int m, double *__restrict__ Tf,
+                                 int ld)
+{
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= m * m) return;
+    const int j = e / m;
+    const int i = e - j * m;
+    Tf[(size_t)j * ld + i] = i == j ? theta[i] : 0.0;
+}
+
+int BlockOps::proj_insert(const double *B, int m0, int c, double *Tf, int ld)
+{
+    proj_insert_kernel<<<blocks_for((size_t)(m0 + c) * c), kThreads, 0, stream>>>(B, m0, c, Tf, ld);
+    IPTGB_LAUNCH();
+    return IPT_CUDA_SUCCESS;
+}
+
+int BlockOps::proj_compact(const double *Tf, int ld, int m, double *Tm)
+{
+    proj_compact_kernel<<<blocks_for((size_t)m * m), kThreads, 0, stream>>>(Tf, ld, m, Tm);
+    IPTGB_LAUNCH();
+    return IPT_CUDA_SUCCESS;
+}
+
+int BlockOps::proj_diag(const double *theta, int m, double *Tf, int ld)
+{
+    proj_diag_kernel<<<blocks_for((size_t)m * m), kThreads, 0, stream>>>(theta, m, Tf, ld);
+    IPTGB_LAUNCH();
+    return IPT_CUDA_SUCCESS;
+}
+
 int BlockOps::chol_inverse(const double *G, int m, double *Rinv, int *status_dev)
 {
     const size_t smem = 2 * (size_t)m * (size_t)m * sizeof(double);

@@ -3,10 +3,14 @@
 // The reference multiplies through cuSPARSE SpMM with the CSC arrays passed
 // as CSR and OP_T (IPT_C_GPU/src/ipt_cuda.cu:1535-1559).  Here the host
 // preparation produces a true CSR of the (sorted) matrix, so the product is a
-// gather: one warp per row, lanes stride over the row's nonzeros, every lane
-// keeps BN column accumulators in registers and the warp reduces them with
-// shuffles.  Works for any sparsity pattern; rows are independent, so no
-// atomics and deterministic results.
+// gather, one warp per row.  X is first copied to a row-major block Xr
+// (row c holds the k entries X[c, :], padded), so that the BN values a
+// nonzero multiplies sit in one cache line: with column-major X every
+// nonzero would touch BN different lines.  Within the warp, BN/4 lanes share
+// a nonzero (each owns 4 columns, loaded as two 16-byte vectors) and 32/(BN/4)
+// nonzeros are in flight; the partial sums are reduced over the nonzero
+// streams with shuffles.  Works for any sparsity pattern; rows are
+// independent, so no atomics and deterministic results.
 #include "common.cuh"
 #include "kernels.cuh"
 #include "reduce.cuh"
@@ -15,61 +19,98 @@ namespace iptgb {
 
 constexpr int kCsrWarpsPerBlock = 8;
 
+// Xr[c * ldr + j] = X[c + j * n] (j < k), 0 for k <= j < ldr; 32 x 32 tiles.
+__global__ void rowmajor_copy_kernel(const double *__restrict__ X, int n, int k,
+                                     double *__restrict__ Xr, int ldr)
+{
+    __shared__ double t[32][33];
+    const int r0 = blockIdx.x * 32;
+    const int c0 = blockIdx.y * 32;
+    for (int y = threadIdx.y; y < 32; y += blockDim.y) {
+        const int j = c0 + y;
+        const int r = r0 + threadIdx.x;
+        t[y][threadIdx.x] = (j < k && r < n) ? X[(size_t)r + (size_t)j * n] : 0.0;
+    }
+    __syncthreads();
+    for (int y = threadIdx.y; y < 32; y += blockDim.y) {
+        const int r = r0 + y;
+        const int j = c0 + threadIdx.x;
+        if (r < n && j < ldr) Xr[(size_t)r * ldr + j] = t[threadIdx.x][y];
+    }
+}
+
 template <int BN>
 __global__ void __launch_bounds__(kCsrWarpsPerBlock * 32)
 csr64_spmm_kernel(const int *__restrict__ row_ptr, const int *__restrict__ col_ind,
-                  const double *__restrict__ vals, int n, const double *__restrict__ X,
-                  int k, double *__restrict__ Y)
+                  const double *__restrict__ vals, int n, const double *__restrict__ Xr,
+                  int ldr, int k, double *__restrict__ Y)
 {
+    constexpr int LPN = BN / 4;          // lanes per nonzero
+    constexpr int STREAMS = 32 / LPN;    // nonzeros in flight per warp
     const int lane = threadIdx.x & 31;
     const int row = blockIdx.x * kCsrWarpsPerBlock + (threadIdx.x >> 5);
-    const int c0 = blockIdx.y * BN;
     if (row >= n) {
         return;
     }
-    double acc[BN];
-#pragma unroll
-    for (int j = 0; j < BN; ++j) {
-        acc[j] = 0.0;
-    }
+    const int sub = lane % LPN;
+    const int q = lane / LPN;
+    const int col0 = blockIdx.y * BN + 4 * sub;
+    double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
     const int pbeg = row_ptr[row];
     const int pend = row_ptr[row + 1];
-    for (int p = pbeg + lane; p < pend; p += 32) {
+    const double *xb = Xr + col0;
+    for (int p = pbeg + q; p < pend; p += STREAMS) {
         const double v = __ldg(vals + p);
         const int c = __ldg(col_ind + p);
-        const double *xc = X + c;
-#pragma unroll
-        for (int j = 0; j < BN; ++j) {
-            if (c0 + j < k) {
-                acc[j] = fma(v, __ldg(xc + (size_t)(c0 + j) * (size_t)n), acc[j]);
-            }
-        }
+        const double2 *x = reinterpret_cast<const double2 *>(xb + (size_t)c * ldr);
+        const double2 x01 = __ldg(x);
+        const double2 x23 = __ldg(x + 1);
+        a0 = fma(v, x01.x, a0);
+        a1 = fma(v, x01.y, a1);
+        a2 = fma(v, x23.x, a2);
+        a3 = fma(v, x23.y, a3);
     }
 #pragma unroll
-    for (int j = 0; j < BN; ++j) {
-        acc[j] = warp_sum(acc[j]);
+    for (int off = 16; off >= LPN; off >>= 1) {
+        a0 += __shfl_xor_sync(0xffffffffu, a0, off);
+        a1 += __shfl_xor_sync(0xffffffffu, a1, off);
+        a2 += __shfl_xor_sync(0xffffffffu, a2, off);
+        a3 += __shfl_xor_sync(0xffffffffu, a3, off);
     }
-    // lane j writes column c0 + j (BN <= 32)
-#pragma unroll
-    for (int j = 0; j < BN; ++j) {
-        if (lane == j && c0 + j < k) {
-            Y[(size_t)row + (size_t)(c0 + j) * (size_t)n] = acc[j];
-        }
+    if (q == 0) {
+        double *y = Y + row;
+        if (col0 + 0 < k) y[(size_t)(col0 + 0) * n] = a0;
+        if (col0 + 1 < k) y[(size_t)(col0 + 1) * n] = a1;
+        if (col0 + 2 < k) y[(size_t)(col0 + 2) * n] = a2;
+        if (col0 + 3 < k) y[(size_t)(col0 + 3) * n] = a3;
     }
 }
 
 int launch_csr64_spmm(const int *row_ptr, const int *col_ind, const double *vals, int n,
                       const double *X, int k, double *Y, cudaStream_t stream)
 {
+    if (n <= 0 || k <= 0) {
+        return IPT_CUDA_SUCCESS;
+    }
     const int bn = k <= 4 ? 4 : (k <= 8 ? 8 : 16);
-    dim3 grid((n + kCsrWarpsPerBlock - 1) / kCsrWarpsPerBlock, (k + bn - 1) / bn);
+    const int nblk = (k + bn - 1) / bn;
+    const int ldr = nblk * bn;
+    DeviceBuffer<double> Xr;
+    IPTGB_CHECK(Xr.alloc((size_t)n * ldr, stream));
+    rowmajor_copy_kernel<<<dim3((n + 31) / 32, (ldr + 31) / 32), dim3(32, 8), 0, stream>>>(
+        X, n, k, Xr.ptr, ldr);
+    IPTGB_LAUNCH();
+    dim3 grid((n + kCsrWarpsPerBlock - 1) / kCsrWarpsPerBlock, nblk);
     const int threads = kCsrWarpsPerBlock * 32;
     if (bn == 4) {
-        csr64_spmm_kernel<4><<<grid, threads, 0, stream>>>(row_ptr, col_ind, vals, n, X, k, Y);
+        csr64_spmm_kernel<4><<<grid, threads, 0, stream>>>(row_ptr, col_ind, vals, n, Xr.ptr, ldr,
+                                                            k, Y);
     } else if (bn == 8) {
-        csr64_spmm_kernel<8><<<grid, threads, 0, stream>>>(row_ptr, col_ind, vals, n, X, k, Y);
+        csr64_spmm_kernel<8><<<grid, threads, 0, stream>>>(row_ptr, col_ind, vals, n, Xr.ptr, ldr,
+                                                            k, Y);
     } else {
-        csr64_spmm_kernel<16><<<grid, threads, 0, stream>>>(row_ptr, col_ind, vals, n, X, k, Y);
+        csr64_spmm_kernel<16><<<grid, threads, 0, stream>>>(row_ptr, col_ind, vals, n, Xr.ptr,
+                                                             ldr, k, Y);
     }
     IPTGB_LAUNCH();
     return IPT_CUDA_SUCCESS;
