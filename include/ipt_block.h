@@ -119,9 +119,11 @@ int ipt_block_solve_csr(const int *row_ptr, const int *col_ind, const double *va
                         double *values, IPTBlockReport *report);
 
 /* Eigenpairs of a small symmetric matrix (m <= 112, column-major, device):
- * the solver of the projected Rayleigh-Ritz matrices (FP32 Jacobi, FP64
- * iterative refinement, FP64 polish of near-degenerate clusters).  Writes
- * ascending d_w (m) and orthonormal eigenvectors d_Z (m*m, column-major). */
+ * the solver of the projected Rayleigh-Ritz matrices, replacing the
+ * reference's cusolverDnDsyevd call (IPT_C_GPU/src/ipt_cuda.cu:3143-3218):
+ * FP32 tridiagonal stage, FP64 iterative refinement, FP64 polish of
+ * near-degenerate clusters.  Writes ascending d_w (m) and orthonormal
+ * eigenvectors d_Z (m*m, column-major); synchronises `stream`. */
 int ipt_block_symmetric_eig(const double *d_T, int m, double *d_w, double *d_Z, void *stream);
 
 /* ---- allocation-free FP64 dense solve ------------------------------------ */
