@@ -192,6 +192,15 @@ SIGNATURES = [
     ("ipt_mixed_precision_tf32_cuda_free_device_result", None, [C.POINTER(_MixedResult)]),
     ("ipt_block_default_options", None, [C.POINTER(IPTBlockOptions)]),
     ("ipt_block_symmetric_eig", _i, [_vp, _i, _vp, _vp, _vp]),
+    ("ipt_block_mlp_param_count", _i, []),
+    ("ipt_block_mlp_init", _i, [_vp, C.c_ulonglong, _vp]),
+    ("ipt_block_mlp_forward", _i, [_vp, _vp, C.c_longlong, _i, _vp, _vp]),
+    ("ipt_block_mlp_loss_grad", _i, [_vp, _vp, C.c_longlong, _vp, _vp]),
+    ("ipt_block_mlp_train", _i, [_vp, _vp, C.c_longlong, _i, _i, C.c_float, C.c_ulonglong, _vp,
+                                 _vp]),
+    ("ipt_block_mlp_collect_csr", _i, [_vp, _vp, _vp, _i, _i, _i, C.POINTER(IPTBlockOptions), _vp,
+                                       _i, _vp, C.c_longlong, C.POINTER(C.c_longlong),
+                                       C.POINTER(IPTBlockReport)]),
     ("ipt_cuda_device_tol_noalloc", _i, [_vp, _i, _i, _d, _i, _vp, _vp, _vp, _ip, _dp]),
     ("ipt_block_launch_count", C.c_longlong, []),
     ("ipt_block_profile_enable", None, [_i]),

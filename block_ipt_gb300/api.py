@@ -168,3 +168,76 @@ def block_solve_csr(row_ptr, col_ind, values, n, k, precision="fp64", **kw):
     if st != _lib.IPT_CUDA_SUCCESS:
         raise IPTError(st, "ipt_block_solve_csr")
     return vec, val, rep.as_dict()
+
+
+def block_solve_csr_device(d_row_ptr, d_col_ind, d_vals, n, nnz, k, d_vectors_ptr, d_values_ptr,
+                           precision="fp64", **kw):
+    """Device-pointer CSR variant (diagonal need not be sorted)."""
+    opt = block_options(precision, **kw)
+    rep = IPTBlockReport()
+    st = _lib.load().ipt_block_solve_csr_device(C.c_void_p(d_row_ptr), C.c_void_p(d_col_ind),
+                                                C.c_void_p(d_vals), n, nnz, k, C.byref(opt),
+                                                C.c_void_p(d_vectors_ptr),
+                                                C.c_void_p(d_values_ptr), C.byref(rep))
+    if st != _lib.IPT_CUDA_SUCCESS:
+        raise IPTError(st, "ipt_block_solve_csr_device")
+    return rep.as_dict()
+
+
+# ---------------------------------------------------------------------------
+# learned preconditioner
+# ---------------------------------------------------------------------------
+def _check(status, what="ipt_block_mlp"):
+    if status != _lib.IPT_CUDA_SUCCESS:
+        raise IPTError(status, what)
+
+
+def _stream_ptr(stream):
+    return C.c_void_p(stream) if stream else None
+
+
+def mlp_param_count():
+    return _lib.load().ipt_block_mlp_param_count()
+
+
+def mlp_init(d_params_ptr, seed=0, stream=None):
+    st = _lib.load().ipt_block_mlp_init(C.c_void_p(d_params_ptr), seed, _stream_ptr(stream))
+    _check(st)
+
+
+def mlp_loss_grad(d_params_ptr, d_rows_ptr, rows, d_grad_ptr, stream=None):
+    st = _lib.load().ipt_block_mlp_loss_grad(C.c_void_p(d_params_ptr), C.c_void_p(d_rows_ptr),
+                                             rows, C.c_void_p(d_grad_ptr), _stream_ptr(stream))
+    _check(st)
+
+
+def mlp_forward(d_params_ptr, d_rows_ptr, rows, row_stride, d_out_ptr, stream=None):
+    st = _lib.load().ipt_block_mlp_forward(C.c_void_p(d_params_ptr), C.c_void_p(d_rows_ptr), rows,
+                                           row_stride, C.c_void_p(d_out_ptr), _stream_ptr(stream))
+    _check(st)
+
+
+def mlp_train(d_params_ptr, d_rows_ptr, rows, steps, batch, lr, seed=0, d_loss_ptr=None,
+              stream=None):
+    st = _lib.load().ipt_block_mlp_train(C.c_void_p(d_params_ptr), C.c_void_p(d_rows_ptr), rows,
+                                         steps, batch, lr, seed,
+                                         C.c_void_p(d_loss_ptr) if d_loss_ptr else None,
+                                         _stream_ptr(stream))
+    _check(st)
+
+
+def mlp_collect_csr(d_row_ptr, d_col_ind, d_vals, n, nnz, k, d_exact_ptr, exact_cols,
+                    d_rows_ptr, capacity, **opts):
+    """Run the diagonal-preconditioned Davidson solver on device CSR arrays and
+    record (features, exact-correction target) rows; returns (rows, report)."""
+    lib = _lib.load()
+    opts.setdefault("strategy", 1)
+    opt = block_options("fp64", **opts)
+    rep = _lib.IPTBlockReport()
+    written = C.c_longlong(0)
+    st = lib.ipt_block_mlp_collect_csr(C.c_void_p(d_row_ptr), C.c_void_p(d_col_ind),
+                                       C.c_void_p(d_vals), n, nnz, k, C.byref(opt),
+                                       C.c_void_p(d_exact_ptr), exact_cols, C.c_void_p(d_rows_ptr),
+                                       capacity, C.byref(written), C.byref(rep))
+    _check(st)
+    return written.value, rep.as_dict()

@@ -177,8 +177,6 @@ IptStage *make_fp64_csr_stage(const int *row_ptr, const int *col_ind, const doub
     return st;
 }
 
-LearnedCorrection *make_learned_correction(const float *params, cudaStream_t stream);
-
 // ---------------------------------------------------------------------------
 // Row sums of |H| (dense col-major: thread per row, coalesced over columns).
 // ---------------------------------------------------------------------------
@@ -354,8 +352,12 @@ int dense_block_device(const double *dH_in, int n, int k, const IPTBlockOptions 
         stage.reset(make_fp64_dense_stage(dH, n, d.ptr, s));
     }
     std::unique_ptr<LearnedCorrection> learned;
+    DeviceBuffer<double> coupling;
     if (opt.preconditioner == IPT_BLOCK_PRECOND_MLP) {
         learned.reset(make_learned_correction(opt.mlp_params, s));
+        IPTGB_CHECK(coupling.alloc((size_t)n, s));
+        IPTGB_CHECK(launch_dense_row_coupling(dH, n, coupling.ptr, s));
+        learned->bind(coupling.ptr, hnorm);
     }
     double *xout = permuted ? Xtmp.ptr : d_vectors;
     DeviceBuffer<double> Xfb;
@@ -418,7 +420,8 @@ int dense_block_device(const double *dH_in, int n, int k, const IPTBlockOptions 
 
 int csr_block_device(const int *row_ptr, const int *col_ind, const double *vals, int n, int nnz,
                      int k, const IPTBlockOptions *options, const double *d_diag_sorted,
-                     double *d_vectors, double *d_values, IPTBlockReport *report)
+                     double *d_vectors, double *d_values, IPTBlockReport *report,
+                     LearnedCorrection *hook = nullptr)
 {
     IPTBlockOptions opt;
     if (options != nullptr) {
@@ -486,6 +489,10 @@ int csr_block_device(const int *row_ptr, const int *col_ind, const double *vals,
                                        cudaMemcpyHostToDevice, s));
             IPTGB_CUDA(cudaMemcpyAsync(dperm.ptr, prep.perm.data(), (size_t)n * sizeof(int),
                                        cudaMemcpyHostToDevice, s));
+            if (hook != nullptr) {
+                // the collector's reference vectors are in the caller's order
+                return IPT_CUDA_INVALID_ARGUMENT;
+            }
             IPTGB_CHECK(csr_block_device(prp.ptr, pci.ptr, pcv.ptr, n, prep.nnz, k, &opt, pd.ptr,
                                          Xs.ptr, d_values, report));
             unpermute_rows_kernel<<<blocks_for((size_t)n * k), kThreads, 0, s>>>(
@@ -508,8 +515,16 @@ int csr_block_device(const int *row_ptr, const int *col_ind, const double *vals,
     apply.s = s;
     std::unique_ptr<IptStage> stage(make_fp64_csr_stage(row_ptr, col_ind, vals, n, dd, s));
     std::unique_ptr<LearnedCorrection> learned;
-    if (opt.preconditioner == IPT_BLOCK_PRECOND_MLP) {
+    LearnedCorrection *corr = hook;
+    DeviceBuffer<double> coupling;
+    if (corr == nullptr && opt.preconditioner == IPT_BLOCK_PRECOND_MLP) {
         learned.reset(make_learned_correction(opt.mlp_params, s));
+        corr = learned.get();
+    }
+    if (corr != nullptr) {
+        IPTGB_CHECK(coupling.alloc((size_t)n, s));
+        IPTGB_CHECK(launch_csr_row_coupling(row_ptr, col_ind, vals, n, coupling.ptr, s));
+        corr->bind(coupling.ptr, hnorm);
     }
     DeviceBuffer<double> Xfb;
     bool done = false;
@@ -532,7 +547,7 @@ int csr_block_device(const int *row_ptr, const int *col_ind, const double *vals,
         BlockSolveInput in;
         in.apply = &apply;
         in.ipt = stage.get();
-        in.learned = learned.get();
+        in.learned = corr;
         in.d = dd;
         in.n = n;
         in.k = k;
@@ -625,6 +640,41 @@ IPT_API int ipt_block_solve_csr_device(const int *d_row_ptr, const int *d_col_in
 {
     return csr_block_device(d_row_ptr, d_col_ind, d_values_csr, n, nnz, k, options, nullptr,
                             d_vectors, d_values, report);
+}
+
+IPT_API int ipt_block_mlp_collect_csr(const int *d_row_ptr, const int *d_col_ind,
+                                      const double *d_values_csr, int n, int nnz, int k,
+                                      const IPTBlockOptions *options,
+                                      const double *d_exact_vectors, int exact_cols,
+                                      float *d_rows, long long capacity, long long *rows_written,
+                                      IPTBlockReport *report)
+{
+    if (d_exact_vectors == nullptr || exact_cols <= 0 || exact_cols > n || d_rows == nullptr ||
+        capacity < 0 || rows_written == nullptr || n <= 0 || k <= 0 || k > n) {
+        return IPT_CUDA_INVALID_ARGUMENT;
+    }
+    IPTBlockOptions opt;
+    if (options != nullptr) {
+        opt = *options;
+    } else {
+        fill_default_options(&opt);
+    }
+    opt.strategy = IPT_BLOCK_STRATEGY_DAVIDSON;
+    // with MLP parameters the rows are recorded along the learned trajectory
+    const float *params =
+        opt.preconditioner == IPT_BLOCK_PRECOND_MLP ? (const float *)opt.mlp_params : nullptr;
+    opt.preconditioner = IPT_BLOCK_PRECOND_DIAGONAL;
+    cudaStream_t s = (cudaStream_t)opt.stream;
+    std::unique_ptr<LearnedCorrection> col(
+        make_mlp_collector(d_exact_vectors, exact_cols, d_rows, capacity, params, s));
+    DeviceBuffer<double> dX, dv;
+    IPTGB_CHECK(dX.alloc((size_t)n * k, s));
+    IPTGB_CHECK(dv.alloc((size_t)k, s));
+    const int st = csr_block_device(d_row_ptr, d_col_ind, d_values_csr, n, nnz, k, &opt, nullptr,
+                                    dX.ptr, dv.ptr, report, col.get());
+    *rows_written = mlp_collector_count(col.get());
+    IPTGB_CUDA(cudaStreamSynchronize(s));
+    return st;
 }
 
 IPT_API int ipt_block_solve_csr(const int *row_ptr, const int *col_ind, const double *values_csr,

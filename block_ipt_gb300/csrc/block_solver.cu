@@ -23,6 +23,10 @@
 
 namespace iptgb {
 
+// Required relative drop of the largest scaled residual for a learned
+// Davidson step to be kept.
+constexpr double kLearnedDrop = 0.75;
+
 void fill_default_options(IPTBlockOptions *opt)
 {
     memset(opt, 0, sizeof(*opt));
@@ -250,6 +254,8 @@ int block_solve(const BlockSolveInput &in, double *X_out, double *values_out,
     // ---- 4. Davidson ----------------------------------------------------------
     int steps = 0;
     int restarts = 0;
+    bool learned_on = true;
+    int learned_rejects = 0;
     while (best > tol && steps < opt.davidson_maxsteps) {
         // pairs that still need a correction (ipt_cuda.cu:774-797)
         int nsel = 0;
@@ -287,72 +293,117 @@ int block_solve(const BlockSolveInput &in, double *X_out, double *values_out,
         const double clip = pow(2.220446049250313e-16, 2.0 / 3.0) * scale;
         IPTGB_CUDA(cudaMemcpyAsync(sel, h_sel.data(), (size_t)nsel * sizeof(int),
                                    cudaMemcpyHostToDevice, s));
-        double *T = Vt.ptr;  // n x nsel scratch
-        bool used_learned = false;
-        if (in.learned != nullptr && opt.preconditioner == IPT_BLOCK_PRECOND_MLP) {
-            IPTGB_CHECK(in.learned->correct(R.ptr, in.d, theta, sel, nsel, n, clip, T));
-            used_learned = true;
-        } else {
-            IPTGB_CHECK(ops.diag_correction(R.ptr, in.d, theta, sel, nsel, n, clip, T));
-        }
-        // CGS2 against the basis, then drop numerically dependent directions
-        IPTGB_CHECK(ops.column_norms(T, n, n, nsel, cnorm0));
-        for (int pass = 0; pass < 2; ++pass) {
-            IPTGB_CHECK(ops.gram(V.ptr, n, m, T, n, nsel, n, Gm, m));
-            IPTGB_CHECK(ops.tall_gemm(V.ptr, n, Gm, m, T, n, n, m, nsel, -1.0, 1.0));
-        }
-        IPTGB_CHECK(ops.column_norms(T, n, n, nsel, cnorm1));
-        IPTGB_CUDA(cudaMemcpyAsync(h_c0.data(), cnorm0, (size_t)nsel * sizeof(double),
-                                   cudaMemcpyDeviceToHost, s));
-        IPTGB_CUDA(cudaMemcpyAsync(h_c1.data(), cnorm1, (size_t)nsel * sizeof(double),
-                                   cudaMemcpyDeviceToHost, s));
-        IPTGB_CUDA(cudaStreamSynchronize(s));
-        std::vector<int> keep;
-        std::vector<double> inv;
-        for (int c = 0; c < nsel; ++c) {
-            const double a = h_c0[(size_t)c], b = h_c1[(size_t)c];
-            if (isfinite(a) && isfinite(b) && b > 1e-10 * a && b > 1e-300) {
-                keep.push_back(c);
-                inv.push_back(1.0 / b);
-            }
-        }
-        ++steps;
-        if (keep.empty()) {
-            break;
-        }
-        const int c = (int)keep.size();
-        // normalised kept columns -> V[:, m:m+c] (via the sel/norm scratch)
-        IPTGB_CUDA(cudaMemcpyAsync(sel, keep.data(), (size_t)c * sizeof(int),
-                                   cudaMemcpyHostToDevice, s));
-        IPTGB_CUDA(cudaMemcpyAsync(cnorm1, inv.data(), (size_t)c * sizeof(double),
-                                   cudaMemcpyHostToDevice, s));
-        double *Vnew = V.ptr + (size_t)m * n;
-        IPTGB_CHECK(ops.gather_columns(T, n, sel, cnorm1, n, c, Vnew, n));
-        // CholQR of the new block, one more projection pass, CholQR again
-        int st = cholqr(ops, Vnew, n, c, T, Gm, Rinv, st_dev, &h_status, s);
-        if (st == IPT_CUDA_SUCCESS) {
-            IPTGB_CHECK(ops.gram(V.ptr, n, m, T, n, c, n, Gm, m));
-            IPTGB_CHECK(ops.tall_gemm(V.ptr, n, Gm, m, T, n, n, m, c, -1.0, 1.0));
-            st = cholqr(ops, T, n, c, Vnew, Gm, Rinv, st_dev, &h_status, s);
-        }
-        if (st != IPT_CUDA_SUCCESS) {
-            break;
-        }
-        IPTGB_CHECK(in.apply->apply(Vnew, c, AV.ptr + (size_t)m * n));
-        rep->fp64_matvecs += c;
-        IPTGB_CHECK(project_new(m, c));
-        const double before = max_res();
-        m += c;
-        IPTGB_CHECK(rayleigh_ritz());
-        const double after = max_res();
-        if (used_learned) {
-            if (after < before) {
-                ++rep->mlp_steps_accepted;
+        // A learned step is judged by the FP64 residual: unless the largest
+        // scaled residual drops by at least kLearnedDrop, the appended
+        // directions are discarded, the previous Rayleigh-Ritz state is
+        // restored and the step is redone with the plain diagonal
+        // correction.  Two rejections in a row switch the learned correction
+        // off for the rest of the solve.
+        bool stop = false;
+        for (int attempt = 0; attempt < 2; ++attempt) {
+            const bool use_learned = attempt == 0 && in.learned != nullptr && learned_on;
+            double *T = Vt.ptr;  // n x nsel scratch
+            if (in.learned != nullptr && (use_learned || !in.learned->learned())) {
+                CorrectionArgs ca;
+                ca.V = V.ptr;
+                ca.m = m;
+                ca.R = R.ptr;
+                ca.X = Xr.ptr;
+                ca.d = in.d;
+                ca.theta = theta;
+                ca.rnorm = rnorm;
+                ca.sel = sel;
+                ca.nsel = nsel;
+                ca.n = n;
+                ca.clip = clip;
+                IPTGB_CHECK(in.learned->correct(ca, T));
             } else {
-                ++rep->mlp_steps_rejected;
+                IPTGB_CHECK(ops.diag_correction(R.ptr, in.d, theta, sel, nsel, n, clip, T));
             }
+            const bool judged = use_learned && in.learned->learned();
+            // CGS2 against the basis, then drop numerically dependent directions
+            IPTGB_CHECK(ops.column_norms(T, n, n, nsel, cnorm0));
+            for (int pass = 0; pass < 2; ++pass) {
+                IPTGB_CHECK(ops.gram(V.ptr, n, m, T, n, nsel, n, Gm, m));
+                IPTGB_CHECK(ops.tall_gemm(V.ptr, n, Gm, m, T, n, n, m, nsel, -1.0, 1.0));
+            }
+            IPTGB_CHECK(ops.column_norms(T, n, n, nsel, cnorm1));
+            IPTGB_CUDA(cudaMemcpyAsync(h_c0.data(), cnorm0, (size_t)nsel * sizeof(double),
+                                       cudaMemcpyDeviceToHost, s));
+            IPTGB_CUDA(cudaMemcpyAsync(h_c1.data(), cnorm1, (size_t)nsel * sizeof(double),
+                                       cudaMemcpyDeviceToHost, s));
+            IPTGB_CUDA(cudaStreamSynchronize(s));
+            std::vector<int> keep;
+            std::vector<double> inv;
+            for (int c = 0; c < nsel; ++c) {
+                const double a = h_c0[(size_t)c], b = h_c1[(size_t)c];
+                if (isfinite(a) && isfinite(b) && b > 1e-10 * a && b > 1e-300) {
+                    keep.push_back(c);
+                    inv.push_back(1.0 / b);
+                }
+            }
+            ++steps;
+            auto reject_learned = [&]() {
+                ++rep->mlp_steps_rejected;
+                if (++learned_rejects >= 2) learned_on = false;
+            };
+            if (keep.empty()) {
+                if (judged) {
+                    reject_learned();
+                    continue;
+                }
+                stop = true;
+                break;
+            }
+            const int c = (int)keep.size();
+            // normalised kept columns -> V[:, m:m+c] (via the sel/norm scratch);
+            // sel is re-uploaded for a retry below
+            IPTGB_CUDA(cudaMemcpyAsync(cnorm1, inv.data(), (size_t)c * sizeof(double),
+                                       cudaMemcpyHostToDevice, s));
+            int *keep_dev = st_dev + 4;
+            IPTGB_CUDA(cudaMemcpyAsync(keep_dev, keep.data(), (size_t)c * sizeof(int),
+                                       cudaMemcpyHostToDevice, s));
+            double *Vnew = V.ptr + (size_t)m * n;
+            IPTGB_CHECK(ops.gather_columns(T, n, keep_dev, cnorm1, n, c, Vnew, n));
+            // CholQR of the new block, one more projection pass, CholQR again
+            int st = cholqr(ops, Vnew, n, c, T, Gm, Rinv, st_dev, &h_status, s);
+            if (st == IPT_CUDA_SUCCESS) {
+                IPTGB_CHECK(ops.gram(V.ptr, n, m, T, n, c, n, Gm, m));
+                IPTGB_CHECK(ops.tall_gemm(V.ptr, n, Gm, m, T, n, n, m, c, -1.0, 1.0));
+                st = cholqr(ops, T, n, c, Vnew, Gm, Rinv, st_dev, &h_status, s);
+            }
+            if (st != IPT_CUDA_SUCCESS) {
+                if (judged) {
+                    reject_learned();
+                    continue;
+                }
+                stop = true;
+                break;
+            }
+            IPTGB_CHECK(in.apply->apply(Vnew, c, AV.ptr + (size_t)m * n));
+            rep->fp64_matvecs += c;
+            IPTGB_CHECK(project_new(m, c));
+            const double before = max_res();
+            m += c;
+            IPTGB_CHECK(rayleigh_ritz());
+            const double after = max_res();
+            if (judged) {
+                if (!(after < kLearnedDrop * before)) {
+                    // reject: restore the basis and the previous Ritz state
+                    reject_learned();
+                    m -= c;
+                    IPTGB_CHECK(rayleigh_ritz());
+                    continue;
+                }
+                ++rep->mlp_steps_accepted;
+                learned_rejects = 0;
+            }
+            IPTGB_CHECK(note_best());
+            break;
         }
-        IPTGB_CHECK(note_best());
+        if (stop) {
+            break;
+        }
     }
     IPTGB_CUDA(cudaEventRecord(ev.e[3], s));
 

@@ -25,11 +25,46 @@ struct IptStage {
 
 // Learned Davidson correction (k_mlp.cu): T[:, c] from features of the
 // residual rows; returns IPT_CUDA_SUCCESS or an error.
+// Inputs of a Davidson correction for the selected Ritz pairs sel[0..nsel):
+// residuals R and Ritz vectors X (n x k), diagonal d, Ritz values theta,
+// residual norms rnorm (k), the clip of the diagonal correction, and the
+// current orthonormal search space V (n x m).
+struct CorrectionArgs {
+    const double *V = nullptr;
+    int m = 0;
+    const double *R = nullptr;
+    const double *X = nullptr;
+    const double *d = nullptr;
+    const double *theta = nullptr;
+    const double *rnorm = nullptr;
+    const int *sel = nullptr;
+    int nsel = 0;
+    int n = 0;
+    double clip = 0.0;
+};
+
+// A replacement for the plain diagonal correction (k_mlp.cu).  bind() gives
+// the per-row off-diagonal coupling ||H[i, j != i]||_2 (device) and
+// ||H||_inf before the solve; learned() says whether the driver should judge
+// the step (accept, or reject and redo it with the plain correction).
 struct LearnedCorrection {
     virtual ~LearnedCorrection() = default;
-    virtual int correct(const double *R, const double *d, const double *theta, const int *sel,
-                        int nsel, int n, double clip, double *T) = 0;
+    virtual void bind(const double *row_coupling, double hnorm) = 0;
+    virtual bool learned() const = 0;
+    virtual int correct(const CorrectionArgs &a, double *T) = 0;
 };
+
+LearnedCorrection *make_learned_correction(const float *params, cudaStream_t stream);
+// Training-data collector: records rows (6 features, target, weight) against
+// the converged vectors Xstar and returns the plain correction, or the
+// learned one when params is not null.
+LearnedCorrection *make_mlp_collector(const double *Xstar, int kstar, float *out,
+                                      long long capacity, const float *params,
+                                      cudaStream_t stream);
+long long mlp_collector_count(const LearnedCorrection *collector);
+int launch_csr_row_coupling(const int *row_ptr, const int *col_ind, const double *vals, int n,
+                            double *sigma, cudaStream_t s);
+int launch_dense_row_coupling(const double *H, int n, double *sigma, cudaStream_t s);
 
 struct LowpDenseOperator;
 

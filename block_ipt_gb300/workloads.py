@@ -192,3 +192,16 @@ def fci_like_csr(norb=10, nalpha=5, nbeta=5, seed=0, sigma=0.05):
 def fci_like_dims(norb, nalpha, nbeta):
     from math import comb
     return comb(norb, nalpha) * comb(norb, nbeta)
+
+
+def sort_by_diagonal(row_ptr, col_ind, values, diag):
+    """Symmetric permutation of a CSR matrix that makes its diagonal ascending
+    (stable order), column indices sorted within rows.  Returns
+    (row_ptr, col_ind, values, diag, perm) with new row r = old row perm[r]."""
+    from scipy.sparse import csr_matrix
+    n = len(row_ptr) - 1
+    perm = np.argsort(diag, kind="stable")
+    H = csr_matrix((values, col_ind, row_ptr), shape=(n, n))[perm][:, perm].tocsr()
+    H.sort_indices()
+    return (H.indptr.astype(np.int32), H.indices.astype(np.int32), H.data.copy(),
+            np.asarray(diag)[perm], perm)

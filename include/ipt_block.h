@@ -145,6 +145,56 @@ int ipt_cuda_device_tol_noalloc(const double *d_matrix_col_major, int n, int k, 
                                 int maxiter, void *stream, double *d_vectors, double *d_values,
                                 int *iterations_done_out, double *fixed_point_residual_out);
 
+/* ---- learned Davidson preconditioner -------------------------------------- */
+
+/* No counterpart in the reference, whose Davidson step uses the diagonal
+ * correction t_i = r_i / (d_i - theta) (IPT_C_GPU/src/ipt_cuda.cu:2449-2465).
+ * A per-row MLP (IPT_BLOCK_MLP_FEATURES -> 64 -> 64 -> 1, ReLU, FP32
+ * parameters on the device) maps six row features of a selected Ritz pair to
+ * a per-row scale of the diagonal correction (clamped to [-2, 3]; 1 is the
+ * plain preconditioner); IPTBlockOptions.preconditioner = IPT_BLOCK_PRECOND_MLP
+ * with mlp_params = the trained parameters enables it.  Every learned step is
+ * judged by the FP64 residual and redone with the diagonal correction when
+ * the largest scaled residual does not drop (IPTBlockReport counts accepted
+ * and rejected learned steps).
+ *
+ * Training rows are 8 floats: the 6 features, the target scale and its weight;
+ * the loss is the mean of weight * (MLP(features) - target)^2. */
+#define IPT_BLOCK_MLP_FEATURES 6
+#define IPT_BLOCK_MLP_ROW 8
+
+/* Number of FP32 parameters (4673). */
+int ipt_block_mlp_param_count(void);
+/* Seeded initialisation (uniform, fan-in scaled; output bias 1, i.e. the
+ * plain correction). */
+int ipt_block_mlp_init(float *d_params, unsigned long long seed, void *stream);
+/* d_out[r] = MLP(d_rows[r*row_stride .. +6]) for r < rows. */
+int ipt_block_mlp_forward(const float *d_params, const float *d_rows, long long rows,
+                          int row_stride, float *d_out, void *stream);
+/* Gradient of the weighted squared error over all `rows` training rows:
+ * d_grad[0..param_count) = dL/dparams, d_grad[param_count] = L. */
+int ipt_block_mlp_loss_grad(const float *d_params, const float *d_rows, long long rows,
+                            float *d_grad, void *stream);
+/* `steps` Adam steps (lr, betas 0.9/0.999, eps 1e-8) on batches of `batch`
+ * rows drawn by a seeded hash; d_loss_history (steps floats, may be NULL)
+ * receives each batch's loss before its update. */
+int ipt_block_mlp_train(float *d_params, const float *d_rows, long long rows, int steps,
+                        int batch, float lr, unsigned long long seed, float *d_loss_history,
+                        void *stream);
+/* Training data from the plain solver: runs the diagonal-preconditioned
+ * Davidson solver on a CSR matrix (diagonal ascending) and, at every
+ * correction, appends per row the features and the exact-correction target
+ * computed against the caller's converged eigenvectors d_exact_vectors
+ * (n x exact_cols, column-major).  At most `capacity` rows are written;
+ * *rows_written reports how many.  With options->preconditioner =
+ * IPT_BLOCK_PRECOND_MLP the solver follows the learned corrections of
+ * options->mlp_params instead (rows along the learned trajectory). */
+int ipt_block_mlp_collect_csr(const int *d_row_ptr, const int *d_col_ind,
+                              const double *d_values_csr, int n, int nnz, int k,
+                              const IPTBlockOptions *options, const double *d_exact_vectors,
+                              int exact_cols, float *d_rows, long long capacity,
+                              long long *rows_written, IPTBlockReport *report);
+
 /* ---- instrumentation ---------------------------------------------------- */
 
 /* Number of kernels this library has launched in the calling process. */
