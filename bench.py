@@ -62,6 +62,10 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fci", action="store_true")
     ap.add_argument("--fci-steps", type=int, default=2)
+    ap.add_argument("--no-learned", action="store_true")
+    ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--batch", type=int, default=512)
+    ap.add_argument("--batch-steps", type=int, default=3)
     return ap.parse_args()
 
 
@@ -287,8 +291,11 @@ def fci_section(args, torch, lib, stream, flush, dev):
     except (OSError, KeyError):
         pass
     cp_ms, cp_cnt = prof["csr_product"]
-    flops = 2.0 * Hs.nnz * sum(1 for _ in range(1))  # per column
     cols = rep["fp64_matvecs"]
+    learned_part = None
+    if not args.no_learned:
+        learned_part = learned_section(args, torch, dev, stream, flush, solve, opt, e0, e1,
+                                       times, rep)
     achieved = (2.0 * Hs.nnz * cols * len(times)) / (cp_ms * 1e-3) / 1e12 if cp_ms else None
     return {"workload": "FCI-like CSR, 10 orbitals 5a/5b, n=%d nnz=%d, k=%d, seed 0" % (n, Hs.nnz, k),
             "ms": statistics.mean(times), "report": {kk: rep[kk] for kk in (
@@ -297,7 +304,108 @@ def fci_section(args, torch, lib, stream, flush, dev):
             "check": {"max_scaled_residual": res, "max_abs_dlambda_over_norm_inf": dl},
             "csr_product": {"launches": cp_cnt, "ms_per_solve": cp_ms / len(times),
                             "achieved_fp64_tflops": achieved},
-            "kernel_ms": {kk: round(val[0] / len(times), 4) for kk, val in prof.items() if val[1]}}
+            "kernel_ms": {kk: round(val[0] / len(times), 4) for kk, val in prof.items() if val[1]},
+            "learned": learned_part}
+
+
+def learned_section(args, torch, dev, stream, flush, solve, opt, e0, e1, plain_times, plain_rep):
+    """Learned Davidson preconditioner on the FCI-like workload: trained (outside
+    any timed region) on 6- and 8-orbital instances of the family by the
+    library's own kernels, then the same solve timed with it."""
+    from block_ipt_gb300 import learned
+    t0 = time.perf_counter()
+    params, info = learned.build(torch, device=dev)
+    torch.cuda.synchronize()
+    train_s = time.perf_counter() - t0
+    # what the network gains on a held-out instance of the training family
+    held = learned.device_csr(torch, 8, 4, 4, 9, device=dev)
+    rows = torch.empty((1_500_000, learned.ROW), dtype=torch.float32, device=dev)
+    got = learned.collect(torch, held, 16, rows, 0)
+    loss_plain, loss_mlp = learned.correction_losses(torch, params, rows, got)
+    del rows
+    opt.preconditioner = 1
+    opt.mlp_params = C.c_void_p(params.data_ptr())
+    solve()
+    times, rep = [], None
+    for _ in range(max(1, args.fci_steps)):
+        flush.zero_()
+        e0.record(stream)
+        rep = solve()
+        e1.record(stream)
+        e1.synchronize()
+        times.append(e0.elapsed_time(e1))
+    opt.preconditioner = 0
+    opt.mlp_params = None
+    return {"ms": statistics.mean(times), "plain_ms": statistics.mean(plain_times),
+            "steps": rep["davidson_steps"], "plain_steps": plain_rep["davidson_steps"],
+            "fp64_matvecs": rep["fp64_matvecs"], "plain_fp64_matvecs": plain_rep["fp64_matvecs"],
+            "converged": rep["converged"], "max_scaled_residual": rep["max_scaled_residual"],
+            "mlp_steps_accepted": rep["mlp_steps_accepted"],
+            "mlp_steps_rejected": rep["mlp_steps_rejected"],
+            "train_s": train_s, "train_rows": info["rows_total"],
+            "heldout_correction_error": {"plain": loss_plain, "learned": loss_mlp,
+                                         "instance": "8 orbitals 4a/4b seed 9"}}
+
+
+def batch_section(args, torch, dev):
+    """The batched dense workload: 512 independent instances, n ~ U{64..2048},
+    k ~ U{4..16}, sigma ~ U(0.01, 0.1), configs[0] construction per instance
+    (generated on the device, same hashes as block_ipt_gb300.workloads), solved
+    by the persistent batched kernel replayed as one CUDA graph, FP64 and
+    mixed (FP32 sweeps then FP64 certification), launch shape autotuned."""
+    from block_ipt_gb300 import api, workloads
+    specs = workloads.batch_config2(args.batch, seed=args.seed)
+    bufs, inst = [], []
+    for n, k, sig, seed in specs:
+        H, _ = workloads.batch_instance_torch(torch, n, sig, seed, device=dev)
+        dX = torch.empty((k, n), dtype=torch.float64, device=dev)
+        dv = torch.empty(k, dtype=torch.float64, device=dev)
+        bufs.append((H, dX, dv))
+        inst.append((H.data_ptr(), n, k, dX.data_ptr(), dv.data_ptr()))
+    torch.cuda.synchronize()
+    out = {"workload": "%d dense instances, n~U{64..2048}, k~U{4..16}, sigma~U(0.01,0.1), "
+                       "seed %d" % (len(specs), args.seed),
+           "fp64_bytes_of_H": int(sum(8 * n * n for n, _, _, _ in specs))}
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    stream = torch.cuda.current_stream(dev)
+    for prec in ("fp64", "fp32"):
+        plan = api.BatchPlan(inst, prec)
+        threads, chunk, _ = plan.autotune(stream.cuda_stream)
+        plan.run(stream.cuda_stream)
+        times = []
+        for _ in range(max(1, args.batch_steps)):
+            e0.record(stream)
+            plan.run(stream.cuda_stream)
+            e1.record(stream)
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1))
+        reps = plan.reports()
+        plan.close()
+        lat = np.array([r["latency_ms"] for r in reps])
+        ms = statistics.median(times)
+        out["fp64" if prec == "fp64" else "mixed"] = {
+            "ms_per_batch": ms, "instances_per_s": len(specs) / (ms * 1e-3),
+            "p50_latency_ms": float(np.percentile(lat, 50)),
+            "p99_latency_ms": float(np.percentile(lat, 99)),
+            "converged": int(sum(r["converged"] for r in reps)),
+            "max_scaled_residual": float(max(r["max_scaled_residual"] for r in reps)),
+            "mean_sweeps": float(np.mean([r["iterations"] for r in reps])),
+            "mean_fp64_sweeps": float(np.mean([r["fp64_iterations"] for r in reps])),
+            "autotuned": {"threads": threads, "chunk": chunk}, "graph_launches": len(times) + 1}
+    # eigenvalue check of a few instances against LAPACK
+    worst = 0.0
+    for b in range(0, len(specs), max(1, len(specs) // 4)):
+        H, _, dv = bufs[b]
+        Hn = H.cpu().numpy()
+        k = specs[b][1]
+        w = np.linalg.eigvalsh(Hn)[:k]
+        worst = max(worst, float(np.abs(np.sort(dv.cpu().numpy()) - w).max()
+                                 / np.abs(Hn).sum(axis=1).max()))
+    out["check"] = {"max_abs_dlambda_over_norm_inf_sampled": worst}
+    del bufs
+    torch.cuda.empty_cache()
+    return out
 
 
 def run_ours(args):
@@ -454,6 +562,9 @@ def run_ours(args):
     fci = None
     if not args.no_fci and rank == 0:
         fci = fci_section(args, torch, lib, stream, flush, dev)
+    batched = None
+    if not args.no_batch and rank == 0:
+        batched = batch_section(args, torch, dev)
 
     cpu = None
     if not args.no_cpu and rank == 0:
@@ -472,7 +583,8 @@ def run_ours(args):
             "scaling": "weak", "vs_baseline": None, "dtype": "%s+f64" % args.precision,
             "data": "synthetic",
             "config": {"workload": WORKLOAD, "n": n, "k": k, "seed": args.seed,
-                       "precision": args.precision, "learned_preconditioner": False,
+                       "precision": args.precision,
+                       "learned_preconditioner": "acts on Davidson steps; this workload converges in the mixed refinement, so it is timed on the FCI-like workload (fci_config3.learned)",
                        "l2": "256 MB buffer written between timed steps (inputs also > L2)",
                        "parallelism": "replicas only (one instance per GPU)"},
             "e2e": ({"value": e2e_ms, "unit": "ms", "h2d_bytes_per_step": 8 * n * n,
@@ -500,6 +612,7 @@ def run_ours(args):
                 if fp64_dav_rep else None),
             "kernel_ms": {kk: round(v[0] / steps, 4) for kk, v in prof.items() if v[1]},
             "fci_config3": fci,
+            "batched_config2": batched,
         }
         print(json.dumps(line), flush=True)
     if world > 1:

@@ -23,6 +23,7 @@ IPT_BLOCK_FP64 = 0
 IPT_BLOCK_FP16 = 1
 IPT_BLOCK_BF16 = 2
 IPT_BLOCK_TF32 = 3
+IPT_BLOCK_FP32 = 4
 IPT_BLOCK_STRATEGY_REFINE = 0
 IPT_BLOCK_STRATEGY_DAVIDSON = 1
 IPT_BLOCK_PRECOND_DIAGONAL = 0
@@ -157,6 +158,23 @@ class IPTBlockReport(C.Structure):
         return {name: getattr(self, name) for name, _ in self._fields_}
 
 
+class IPTBatchInstance(C.Structure):
+    _fields_ = [("H", C.c_void_p), ("n", C.c_int), ("k", C.c_int), ("vectors", C.c_void_p),
+                ("values", C.c_void_p)]
+
+
+class IPTBatchOptions(C.Structure):
+    _fields_ = [("precision", C.c_int), ("residual_tol", C.c_double), ("maxiter", C.c_int),
+                ("lowp_maxiter", C.c_int), ("lowp_tol", C.c_double), ("threads", C.c_int),
+                ("chunk", C.c_int)]
+
+
+class IPTBatchReport(C.Structure):
+    _fields_ = [("converged", C.c_int), ("status", C.c_int), ("iterations", C.c_int),
+                ("fp64_iterations", C.c_int), ("max_scaled_residual", C.c_double),
+                ("latency_ms", C.c_double), ("completion_ms", C.c_double)]
+
+
 # (name, restype, argtypes) of every exported entry point
 _vp = C.c_void_p
 SIGNATURES = [
@@ -193,6 +211,14 @@ SIGNATURES = [
     ("ipt_block_default_options", None, [C.POINTER(IPTBlockOptions)]),
     ("ipt_block_symmetric_eig", _i, [_vp, _i, _vp, _vp, _vp]),
     ("ipt_block_mlp_param_count", _i, []),
+    ("ipt_block_batch_default_options", None, [C.POINTER(IPTBatchOptions)]),
+    ("ipt_block_batch_plan_create", _i, [C.POINTER(IPTBatchInstance), _i,
+                                         C.POINTER(IPTBatchOptions), C.POINTER(C.c_void_p)]),
+    ("ipt_block_batch_plan_run", _i, [_vp, _vp]),
+    ("ipt_block_batch_plan_autotune", _i, [_vp, _vp, C.POINTER(_i), C.POINTER(_i),
+                                           C.POINTER(_d)]),
+    ("ipt_block_batch_plan_reports", _i, [_vp, C.POINTER(IPTBatchReport)]),
+    ("ipt_block_batch_plan_destroy", _i, [_vp]),
     ("ipt_block_mlp_init", _i, [_vp, C.c_ulonglong, _vp]),
     ("ipt_block_mlp_forward", _i, [_vp, _vp, C.c_longlong, _i, _vp, _vp]),
     ("ipt_block_mlp_loss_grad", _i, [_vp, _vp, C.c_longlong, _vp, _vp]),

@@ -241,3 +241,60 @@ def mlp_collect_csr(d_row_ptr, d_col_ind, d_vals, n, nnz, k, d_exact_ptr, exact_
                                        capacity, C.byref(written), C.byref(rep))
     _check(st)
     return written.value, rep.as_dict()
+
+
+# ---------------------------------------------------------------------------
+# batched dense solver
+# ---------------------------------------------------------------------------
+class BatchPlan:
+    """Many independent dense instances solved by one persistent kernel under a
+    captured CUDA graph (include/ipt_block.h, ipt_block_batch_*).
+
+    instances: sequence of (d_H, n, k, d_vectors, d_values) device pointers
+    (integers); they must stay valid while the plan lives."""
+
+    def __init__(self, instances, precision="fp64", **opts):
+        lib = _lib.load()
+        self._lib = lib
+        self.count = len(instances)
+        arr = (_lib.IPTBatchInstance * self.count)()
+        for b, (h, n, k, vec, val) in enumerate(instances):
+            arr[b] = _lib.IPTBatchInstance(C.c_void_p(h), n, k, C.c_void_p(vec), C.c_void_p(val))
+        opt = _lib.IPTBatchOptions()
+        lib.ipt_block_batch_default_options(C.byref(opt))
+        opt.precision = _lib.IPT_BLOCK_FP32 if precision == "fp32" else _lib.IPT_BLOCK_FP64
+        for key, val in opts.items():
+            if not hasattr(opt, key):
+                raise TypeError("unknown batch option %r" % key)
+            setattr(opt, key, val)
+        self._plan = C.c_void_p()
+        _check(lib.ipt_block_batch_plan_create(arr, self.count, C.byref(opt),
+                                               C.byref(self._plan)), "ipt_block_batch_plan_create")
+
+    def run(self, stream=None):
+        _check(self._lib.ipt_block_batch_plan_run(self._plan, _stream_ptr(stream)),
+               "ipt_block_batch_plan_run")
+
+    def autotune(self, stream=None):
+        t, c, ms = C.c_int(0), C.c_int(0), C.c_double(0.0)
+        _check(self._lib.ipt_block_batch_plan_autotune(self._plan, _stream_ptr(stream), C.byref(t),
+                                                       C.byref(c), C.byref(ms)),
+               "ipt_block_batch_plan_autotune")
+        return t.value, c.value, ms.value
+
+    def reports(self):
+        arr = (_lib.IPTBatchReport * self.count)()
+        _check(self._lib.ipt_block_batch_plan_reports(self._plan, arr),
+               "ipt_block_batch_plan_reports")
+        return [{f: getattr(r, f) for f, _ in _lib.IPTBatchReport._fields_} for r in arr]
+
+    def close(self):
+        if self._plan:
+            self._lib.ipt_block_batch_plan_destroy(self._plan)
+            self._plan = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

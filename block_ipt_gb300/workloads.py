@@ -205,3 +205,57 @@ def sort_by_diagonal(row_ptr, col_ind, values, diag):
     H.sort_indices()
     return (H.indptr.astype(np.int32), H.indices.astype(np.int32), H.data.copy(),
             np.asarray(diag)[perm], perm)
+
+
+# ---------------------------------------------------------------------------
+# The same constructions generated on the GPU with torch integer arithmetic
+# (for benchmark-sized batches; numpy generation of the 6 GB batch takes
+# tens of seconds).  Hashes and uniforms are bit-identical to the numpy
+# versions; log/cos/exp round as the device's libm does (~1 ulp).
+# ---------------------------------------------------------------------------
+def _t_signed(v):
+    """The int64 with the bits of the uint64 v."""
+    v &= 0xFFFFFFFFFFFFFFFF
+    return v - (1 << 64) if v >= (1 << 63) else v
+
+
+_T_GOLD = _t_signed(0x9E3779B97F4A7C15)
+_T_M1 = _t_signed(0xBF58476D1CE4E5B9)
+_T_M2 = _t_signed(0x94D049BB133111EB)
+_T_M3 = _t_signed(0xD1B54A32D192ED03)
+
+
+def _t_srl(x, s):
+    """Logical right shift of int64 tensors."""
+    return (x >> s) & ((1 << (64 - s)) - 1)
+
+
+def _t_splitmix(x):
+    x = x + _T_GOLD
+    z = (x ^ _t_srl(x, 30)) * _T_M1
+    z = (z ^ _t_srl(z, 27)) * _T_M2
+    return z ^ _t_srl(z, 31)
+
+
+def _t_uniform(torch, seed, stream, a, b):
+    key = int(_key(seed, stream))
+    h = _t_splitmix(torch.bitwise_xor(a, _t_signed(key)))
+    h = _t_splitmix(h ^ (b * _T_M3))
+    return (_t_srl(h, 11).to(torch.float64) + 0.5) * (2.0 ** -53)
+
+
+def batch_instance_torch(torch, n, sigma, seed, device="cuda"):
+    """dense_config0(n, seed, sigma) built on the device: (H column-major as an
+    n x n tensor whose storage is H^T = H, d)."""
+    i = torch.arange(n, dtype=torch.int64, device=device)
+    d = i.to(torch.float64) + 0.5 * _t_uniform(torch, seed, 1, i, torch.zeros_like(i))
+    # d is increasing by construction (i + U(0, 0.5)), so the sort is the identity
+    lo = torch.minimum(i[:, None], i[None, :])
+    hi = torch.maximum(i[:, None], i[None, :])
+    u1 = _t_uniform(torch, seed, 2, lo, hi)
+    u2 = _t_uniform(torch, seed, 2 + 7919, lo, hi)
+    H = sigma * torch.sqrt(-2.0 * torch.log(u1)) * torch.cos(2.0 * torch.pi * u2)
+    H *= torch.exp(-torch.abs(d[:, None] - d[None, :]) / 64.0)
+    H.fill_diagonal_(0.0)
+    H += torch.diag(d)
+    return H, d

@@ -36,7 +36,8 @@ enum {
     IPT_BLOCK_FP64 = 0, /* FP64 SIMT product (the plain path) */
     IPT_BLOCK_FP16 = 1, /* FP16 tensor cores (tcgen05), FP32 accumulation */
     IPT_BLOCK_BF16 = 2, /* BF16 tensor cores (tcgen05), FP32 accumulation */
-    IPT_BLOCK_TF32 = 3  /* TF32 tensor cores (tcgen05), FP32 accumulation */
+    IPT_BLOCK_TF32 = 3, /* TF32 tensor cores (tcgen05), FP32 accumulation */
+    IPT_BLOCK_FP32 = 4  /* FP32 SIMT sweeps, then FP64 (batched solver only) */
 };
 
 /* Solver strategy.  REFINE (default): IPT fixed point refined to the FP64
@@ -194,6 +195,58 @@ int ipt_block_mlp_collect_csr(const int *d_row_ptr, const int *d_col_ind,
                               const IPTBlockOptions *options, const double *d_exact_vectors,
                               int exact_cols, float *d_rows, long long capacity,
                               long long *rows_written, IPTBlockReport *report);
+
+/* ---- batched dense solver ----------------------------------------------- */
+
+/* No counterpart in the reference, which solves one matrix per call.  Many
+ * independent dense symmetric instances (column-major FP64 on the device,
+ * n >= 1, 1 <= k <= min(16, n)) are solved by one persistent kernel with the
+ * reference's plain IPT map (targets = the first k diagonal positions,
+ * X_jj = 1, IPT_C_GPU/src/ipt_cuda.cu:1644-1703), stopping each instance at
+ * the scaled eigen-residual residual_tol (residuals r_j = H x_j - (HX)_jj x_j,
+ * the IPT map's own) and returning the certified block and its Rayleigh
+ * quotients x_j^T H x_j / x_j^T x_j.  precision IPT_BLOCK_FP32 runs FP32
+ * sweeps to lowp_tol first, then the FP64 sweeps.  The plan owns all
+ * scratch and a captured CUDA graph of the whole batch; run() launches the
+ * graph, autotune() times the launch shapes on the real batch and
+ * re-captures the fastest.  Instance pointers must stay valid for the
+ * plan's lifetime. */
+typedef struct {
+    const double *H;  /* n x n, column-major, device */
+    int n;
+    int k;
+    double *vectors;  /* n x k, column-major, device (output) */
+    double *values;   /* k, device (output) */
+} IPTBatchInstance;
+
+typedef struct {
+    int precision;        /* IPT_BLOCK_FP64 or IPT_BLOCK_FP32 */
+    double residual_tol;  /* scaled eigen-residual target (1e-8) */
+    int maxiter;          /* FP64 sweeps per instance */
+    int lowp_maxiter;     /* FP32 sweeps per instance */
+    double lowp_tol;      /* FP32 fixed-point residual at which to switch */
+    int threads;          /* 0 = default (512) or 128 / 256 / 512 */
+    int chunk;            /* 0 = default (128) or 64 / 128 rows of H per stage */
+} IPTBatchOptions;
+
+typedef struct {
+    int converged;
+    int status;               /* 0, or 1 for a non-finite sweep */
+    int iterations;           /* all sweeps */
+    int fp64_iterations;
+    double max_scaled_residual;
+    double latency_ms;        /* device time from the instance's start to its end */
+    double completion_ms;     /* from the first instance's start to this one's end */
+} IPTBatchReport;
+
+void ipt_block_batch_default_options(IPTBatchOptions *options);
+int ipt_block_batch_plan_create(const IPTBatchInstance *instances, int count,
+                                const IPTBatchOptions *options, void **plan);
+int ipt_block_batch_plan_run(void *plan, void *stream);
+int ipt_block_batch_plan_autotune(void *plan, void *stream, int *threads, int *chunk,
+                                  double *best_ms);
+int ipt_block_batch_plan_reports(void *plan, IPTBatchReport *reports);
+int ipt_block_batch_plan_destroy(void *plan);
 
 /* ---- instrumentation ---------------------------------------------------- */
 

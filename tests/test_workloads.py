@@ -1,5 +1,6 @@
 """Seeded workload generators (no GPU)."""
 import numpy as np
+import pytest
 
 from block_ipt_gb300 import workloads
 
@@ -51,3 +52,12 @@ def test_fci_config3_row_count():
     assert workloads.fci_like_dims(10, 5, 5) == 63504
     # 25 + 25 single, 100 + 100 same-spin double, 625 alpha-beta double = 875 per row
     assert 25 + 25 + 100 + 100 + 625 == 875
+
+
+def test_torch_generator_matches_numpy():
+    torch = pytest.importorskip("torch")
+    for n, sig, seed in [(64, 0.05, 3), (333, 0.1, 17)]:
+        H, d = workloads.batch_instance(n, sig, seed)
+        Ht, dt = workloads.batch_instance_torch(torch, n, sig, seed, device="cpu")
+        assert np.array_equal(d, dt.numpy())
+        assert np.abs(H - Ht.numpy()).max() <= 1e-15
