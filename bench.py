@@ -64,6 +64,8 @@ def parse():
     ap.add_argument("--fci-steps", type=int, default=2)
     ap.add_argument("--no-learned", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--no-fci-free", action="store_true")
+    ap.add_argument("--fci-free-orbitals", type=int, default=14)
     ap.add_argument("--batch", type=int, default=512)
     ap.add_argument("--batch-steps", type=int, default=3)
     return ap.parse_args()
@@ -344,7 +346,8 @@ def learned_section(args, torch, dev, stream, flush, solve, opt, e0, e1, plain_t
             "mlp_steps_rejected": rep["mlp_steps_rejected"],
             "train_s": train_s, "train_rows": info["rows_total"],
             "heldout_correction_error": {"plain": loss_plain, "learned": loss_mlp,
-                                         "instance": "8 orbitals 4a/4b seed 9"}}
+                                         "instance": "8 orbitals 4a/4b seed 9"},
+            "_params": params}
 
 
 def batch_section(args, torch, dev):
@@ -405,6 +408,66 @@ def batch_section(args, torch, dev):
     out["check"] = {"max_abs_dlambda_over_norm_inf_sampled": worst}
     del bufs
     torch.cuda.empty_cache()
+    return out
+
+
+def fci_free_section(args, torch, dev, mlp_params=None):
+    """The matrix-free FCI-like workload: norb orbitals with norb/2 alpha and
+    norb/2 beta electrons (14 -> 11,778,624 determinants, 3,381 couplings per
+    row), k = 8, H regenerated from hashes inside every sigma build.  Plain
+    FP64-accurate Davidson vs a BF16-sigma phase followed by the FP64 one
+    (and the learned preconditioner when trained), each to the scaled
+    residual 1e-8; sigma timed alone per precision."""
+    from block_ipt_gb300 import api
+    norb = args.fci_free_orbitals
+    spec = api.fci_spec(norb, norb // 2, norb // 2, seed=args.seed)
+    n = api.fci_dimension(spec)
+    k = 8
+    couplings = 2 * (norb // 2) ** 2 + 2 * ((norb // 2) * (norb // 2 - 1) // 2) ** 2 \
+        + (norb // 2) ** 4
+    out = {"workload": "matrix-free FCI-like, %d orbitals %d+%d electrons, n=%d, %d couplings "
+                       "per row, k=%d, seed %d" % (norb, norb // 2, norb // 2, n, couplings, k,
+                                                   args.seed)}
+    X = torch.randn((k, n), dtype=torch.float64, device=dev)
+    Y = torch.empty_like(X)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    sig = {}
+    for prec in ("fp64", "fp32", "bf16"):
+        api.fci_sigma(spec, X.data_ptr(), k, Y.data_ptr(), prec)
+        torch.cuda.synchronize()
+        e0.record()
+        api.fci_sigma(spec, X.data_ptr(), k, Y.data_ptr(), prec)
+        e1.record()
+        e1.synchronize()
+        ms = e0.elapsed_time(e1)
+        esize = {"fp64": 8, "fp32": 4, "bf16": 2}[prec]
+        # minimal bytes: X once (k values per determinant), Y once (FP64), diagonal
+        minimal = n * k * esize + n * k * 8 + n * 8
+        sig[prec] = {"ms_incl_setup": ms, "couplings_per_s": n * couplings / (ms * 1e-3),
+                     "achieved_gflops": 2.0 * n * couplings * k / (ms * 1e-3) / 1e9,
+                     "minimal_bytes": minimal,
+                     "gbs_of_minimal_bytes": minimal / (ms * 1e-3) / 1e9}
+    out["sigma_k8"] = sig
+    del X, Y
+    dX = torch.empty((k, n), dtype=torch.float64, device=dev)
+    dv = torch.empty(k, dtype=torch.float64, device=dev)
+    runs = [("fp64", {}), ("bf16", {})]
+    if mlp_params is not None:
+        runs.append(("bf16_learned", {"preconditioner": 1, "mlp_params": mlp_params.data_ptr()}))
+    for name, extra in runs:
+        prec = "bf16" if name.startswith("bf16") else "fp64"
+        t0 = time.perf_counter()
+        rep = api.block_solve_fci(spec, k, dX.data_ptr(), dv.data_ptr(), prec, strategy=1,
+                                  davidson_maxsteps=60, **extra)
+        torch.cuda.synchronize()
+        out[name] = {"s": time.perf_counter() - t0, "converged": rep["converged"],
+                     "davidson_steps": rep["davidson_steps"], "fp64_matvecs": rep["fp64_matvecs"],
+                     "lowp_matvecs": rep["lowp_matvecs"],
+                     "max_scaled_residual": rep["max_scaled_residual"],
+                     "mlp_steps_accepted": rep["mlp_steps_accepted"],
+                     "mlp_steps_rejected": rep["mlp_steps_rejected"],
+                     "lowest": dv.cpu().numpy()[:3].tolist()}
     return out
 
 
@@ -560,11 +623,17 @@ def run_ours(args):
         roofline = roofline_lowp
 
     fci = None
+    mlp_params = None
     if not args.no_fci and rank == 0:
         fci = fci_section(args, torch, lib, stream, flush, dev)
+        if fci.get("learned"):
+            mlp_params = fci["learned"].pop("_params", None)
     batched = None
     if not args.no_batch and rank == 0:
         batched = batch_section(args, torch, dev)
+    fci_free = None
+    if not args.no_fci_free and rank == 0:
+        fci_free = fci_free_section(args, torch, dev, mlp_params)
 
     cpu = None
     if not args.no_cpu and rank == 0:
@@ -613,6 +682,7 @@ def run_ours(args):
             "kernel_ms": {kk: round(v[0] / steps, 4) for kk, v in prof.items() if v[1]},
             "fci_config3": fci,
             "batched_config2": batched,
+            "matrix_free_config4": fci_free,
         }
         print(json.dumps(line), flush=True)
     if world > 1:

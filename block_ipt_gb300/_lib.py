@@ -158,6 +158,11 @@ class IPTBlockReport(C.Structure):
         return {name: getattr(self, name) for name, _ in self._fields_}
 
 
+class IPTFciSpec(C.Structure):
+    _fields_ = [("norb", C.c_int), ("nalpha", C.c_int), ("nbeta", C.c_int),
+                ("seed", C.c_ulonglong), ("offdiag_sigma", C.c_double)]
+
+
 class IPTBatchInstance(C.Structure):
     _fields_ = [("H", C.c_void_p), ("n", C.c_int), ("k", C.c_int), ("vectors", C.c_void_p),
                 ("values", C.c_void_p)]
@@ -212,6 +217,11 @@ SIGNATURES = [
     ("ipt_block_symmetric_eig", _i, [_vp, _i, _vp, _vp, _vp]),
     ("ipt_block_mlp_param_count", _i, []),
     ("ipt_block_batch_default_options", None, [C.POINTER(IPTBatchOptions)]),
+    ("ipt_fci_dimension", _i, [C.POINTER(IPTFciSpec), C.POINTER(C.c_longlong)]),
+    ("ipt_fci_diagonal", _i, [C.POINTER(IPTFciSpec), _vp, _vp]),
+    ("ipt_fci_sigma", _i, [C.POINTER(IPTFciSpec), _vp, _i, _vp, _i, _vp]),
+    ("ipt_block_solve_fci", _i, [C.POINTER(IPTFciSpec), _i, C.POINTER(IPTBlockOptions), _vp, _vp,
+                                 C.POINTER(IPTBlockReport)]),
     ("ipt_block_batch_plan_create", _i, [C.POINTER(IPTBatchInstance), _i,
                                          C.POINTER(IPTBatchOptions), C.POINTER(C.c_void_p)]),
     ("ipt_block_batch_plan_run", _i, [_vp, _vp]),

@@ -298,3 +298,44 @@ class BatchPlan:
             self.close()
         except Exception:
             pass
+
+
+# ---------------------------------------------------------------------------
+# matrix-free FCI-like Hamiltonians
+# ---------------------------------------------------------------------------
+PRECISION_CODES = {"fp64": _lib.IPT_BLOCK_FP64, "fp32": _lib.IPT_BLOCK_FP32,
+                   "bf16": _lib.IPT_BLOCK_BF16}
+
+
+def fci_spec(norb, nalpha, nbeta, seed=0, sigma=0.05):
+    return _lib.IPTFciSpec(norb, nalpha, nbeta, seed, sigma)
+
+
+def fci_dimension(spec):
+    n = C.c_longlong(0)
+    _check(_lib.load().ipt_fci_dimension(C.byref(spec), C.byref(n)), "ipt_fci_dimension")
+    return n.value
+
+
+def fci_diagonal(spec, d_diag_ptr, stream=None):
+    _check(_lib.load().ipt_fci_diagonal(C.byref(spec), C.c_void_p(d_diag_ptr),
+                                        _stream_ptr(stream)), "ipt_fci_diagonal")
+
+
+def fci_sigma(spec, d_x_ptr, k, d_y_ptr, precision="fp64", stream=None):
+    _check(_lib.load().ipt_fci_sigma(C.byref(spec), C.c_void_p(d_x_ptr), k, C.c_void_p(d_y_ptr),
+                                     PRECISION_CODES[precision], _stream_ptr(stream)),
+           "ipt_fci_sigma")
+
+
+def block_solve_fci(spec, k, d_vectors_ptr, d_values_ptr, precision="fp64", **kw):
+    """k lowest eigenpairs of the matrix-free FCI-like H by Davidson; precision
+    "bf16"/"fp32" runs a low-precision sigma phase before the FP64 one."""
+    opt = block_options("fp64", **kw)
+    opt.ipt_precision = PRECISION_CODES[precision]
+    rep = IPTBlockReport()
+    st = _lib.load().ipt_block_solve_fci(C.byref(spec), k, C.byref(opt), C.c_void_p(d_vectors_ptr),
+                                         C.c_void_p(d_values_ptr), C.byref(rep))
+    if st != _lib.IPT_CUDA_SUCCESS:
+        raise IPTError(st, "ipt_block_solve_fci")
+    return rep.as_dict()

@@ -33,12 +33,14 @@ def sources():
 
 
 def _compile(nvcc, src, obj, verbose):
+    # host code without contraction: host-side FP arithmetic (workload tables)
+    # must match the CPU oracle bit for bit
     cmd = [nvcc, "-O3", "-std=c++17", "-lineinfo", *ARCH, "-Xcompiler",
-           "-fPIC,-fvisibility=hidden", "-Xptxas", "-warn-spills",
+           "-fPIC,-fvisibility=hidden,-ffp-contract=off", "-Xptxas", "-warn-spills",
            "-c", src, "-o", obj]
     if src.endswith(".cpp"):
-        cmd = [nvcc, "-O3", "-std=c++17", "-Xcompiler", "-fPIC,-fvisibility=hidden",
-               "-c", src, "-o", obj]
+        cmd = [nvcc, "-O3", "-std=c++17", "-Xcompiler",
+               "-fPIC,-fvisibility=hidden,-ffp-contract=off", "-c", src, "-o", obj]
     proc = subprocess.run(cmd, capture_output=True, text=True)
     if verbose or proc.returncode != 0:
         sys.stderr.write(" ".join(cmd) + "\n" + proc.stdout + proc.stderr)

@@ -248,6 +248,40 @@ int ipt_block_batch_plan_autotune(void *plan, void *stream, int *threads, int *c
 int ipt_block_batch_plan_reports(void *plan, IPTBatchReport *reports);
 int ipt_block_batch_plan_destroy(void *plan);
 
+/* ---- matrix-free FCI-like Hamiltonians ------------------------------------ */
+
+/* No counterpart in the reference (its FCI matrices are assembled into CSC
+ * from PySCF integrals, IPT_C_GPU/test/sparse/H2O/
+ * benchmark_h2o_631g_cas10e10o_primme_vs_ipt.cu:390-766).  H over all
+ * (alpha, beta) occupation-string pairs of norb orbitals, never stored:
+ * eps_p = 0.5 p + 0.05 g(31, p), H_II = E(I) + 0.01 g(32, I),
+ * H_IJ = offdiag_sigma g(33, min(I,J), max(I,J)) exp(-|E(J) - E(I)|) for
+ * single and double excitations (E = summed occupied eps; g a seeded
+ * Box-Muller normal evaluated in FP32 by the library's own deterministic
+ * log/cos/exp).  Determinant I = ia * (number of beta strings) + ib. */
+typedef struct {
+    int norb;
+    int nalpha;
+    int nbeta;
+    unsigned long long seed;
+    double offdiag_sigma;   /* 0.05 for the FCI-like workloads */
+} IPTFciSpec;
+
+int ipt_fci_dimension(const IPTFciSpec *spec, long long *n);
+int ipt_fci_diagonal(const IPTFciSpec *spec, double *d_diag, void *stream);
+/* d_Y (n x k, column-major) = H d_X; precision IPT_BLOCK_FP64 (FP64
+ * accumulation), IPT_BLOCK_FP32 or IPT_BLOCK_BF16 (X rounded to that type,
+ * FP32 accumulation). */
+int ipt_fci_sigma(const IPTFciSpec *spec, const double *d_X, int k, double *d_Y, int precision,
+                  void *stream);
+/* k lowest eigenpairs by Davidson on the matrix-free sigma, starting from the
+ * unit vectors of the lowest diagonal entries.  ipt_precision IPT_BLOCK_BF16
+ * or IPT_BLOCK_FP32 runs a low-precision-sigma phase first (to a scaled
+ * residual of 1e-2 / 1e-5) and finishes with FP64 sigma to residual_tol;
+ * IPT_BLOCK_FP64 uses FP64 sigma throughout. */
+int ipt_block_solve_fci(const IPTFciSpec *spec, int k, const IPTBlockOptions *options,
+                        double *d_vectors, double *d_values, IPTBlockReport *report);
+
 /* ---- instrumentation ---------------------------------------------------- */
 
 /* Number of kernels this library has launched in the calling process. */

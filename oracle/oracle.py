@@ -253,3 +253,47 @@ def ref_lib(which):
             L.ref_prepare_sparse_csc_sorted.argtypes = [vp, vp, vp, i, i, i, vp, vp, vp, vp, vp]
         _ref[which] = L
     return _ref[which]
+
+
+# ---- matrix-free FCI-like construction (fci_oracle.c) -------------------------
+def _fci_lib():
+    L = lib()
+    if not hasattr(L, "_fci_ready"):
+        L.oracle_fci_dimension.restype = C.c_longlong
+        L.oracle_fci_dimension.argtypes = [C.c_int, C.c_int, C.c_int]
+        L.oracle_fci_row_length.restype = C.c_int
+        L.oracle_fci_row_length.argtypes = [C.c_int, C.c_int, C.c_int]
+        L.oracle_fci_matrix.restype = C.c_int
+        L.oracle_fci_matrix.argtypes = [C.c_int, C.c_int, C.c_int, C.c_ulonglong, C.c_double,
+                                        C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+        L.oracle_fci_sigma.restype = C.c_int
+        L.oracle_fci_sigma.argtypes = [C.c_int, C.c_int, C.c_int, C.c_ulonglong, C.c_double,
+                                       C.c_void_p, C.c_int, C.c_void_p]
+        L._fci_ready = True
+    return L
+
+
+def fci_matrix(norb, na, nb, seed=0, sigma=0.05, csr=True):
+    """Diagonal and (optionally) the CSR of the matrix-free FCI-like H."""
+    L = _fci_lib()
+    n = L.oracle_fci_dimension(norb, na, nb)
+    diag = np.zeros(n)
+    if not csr:
+        L.oracle_fci_matrix(norb, na, nb, seed, sigma, _p(diag), None, None, None)
+        return diag
+    per = L.oracle_fci_row_length(norb, na, nb) + 1
+    rp = np.zeros(n + 1, np.int32)
+    ci = np.zeros(n * per, np.int32)
+    va = np.zeros(n * per)
+    st = L.oracle_fci_matrix(norb, na, nb, seed, sigma, _p(diag), _p(rp), _p(ci), _p(va))
+    if st != 0:
+        raise RuntimeError("oracle_fci_matrix failed")
+    return rp, ci, va, diag
+
+
+def fci_sigma(norb, na, nb, X, seed=0, sigma=0.05):
+    L = _fci_lib()
+    X = np.asfortranarray(X, dtype=np.float64)
+    Y = np.zeros_like(X, order="F")
+    L.oracle_fci_sigma(norb, na, nb, seed, sigma, _p(X), X.shape[1], _p(Y))
+    return Y
