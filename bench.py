@@ -3,8 +3,10 @@
 Workload (one step = one solve): dense symmetric n = 8192, k = 32 with
 d_i = i/8 + U(0,0.1) and h_ij ~ N(0, 0.02^2) exp(-|i-j|/256) (seeded synthetic
 matrix, block_ipt_gb300.workloads.dense_config1).  Our arm solves it with
-the block solver: FP16 tensor-core IPT (tcgen05/TMA) followed by FP64
-CholQR2 + Rayleigh-Ritz + Davidson; every step is checked in FP64.
+the block solver: FP16 tensor-core IPT (tcgen05/TMA), refinement of the IPT
+fixed point by FP16 tensor-core correction solves against FP64-accurate
+(double-FP32) defects, and a final FP64 CholQR2 + Rayleigh-Ritz; each result
+is checked in FP64 (torch DGEMM residual, LAPACK eigenvalues).
 
   value        device time per solve, H already resident in HBM (ms)
   e2e          the same solve through the host C-ABI entry point
@@ -16,6 +18,9 @@ CholQR2 + Rayleigh-Ritz + Davidson; every step is checked in FP64.
   cpu_baseline the oracle restatement of the reference's CPU IPT, one
                iteration timed on all host cores and scaled by the block
                products plain IPT needs on this matrix
+  fci_config3  FCI-like CSR (n = 63,504, k = 16), plain and learned Davidson
+  batched_config2      512 dense instances, persistent kernel under a graph
+  matrix_free_config4  matrix-free FCI-like sigma, 14 orbitals (n = 11.8M)
 
 `--impl reference` times the reference's CPU path alone (rank 0 only).
 """
@@ -36,7 +41,8 @@ sys.path.insert(0, ROOT)
 
 METRIC = "time to k eigenpairs at ||r||<=1e-8, mixed+learned vs plain FP64 IPT, 1xGB300"
 WORKLOAD = ("dense symmetric n=8192 k=32, d_i=i/8+U(0,0.1), h_ij~N(0,0.02^2)exp(-|i-j|/256), "
-            "seed 0; FP16 tcgen05 IPT + FP64 CholQR2/Rayleigh-Ritz/Davidson to scaled residual 1e-8")
+            "seed 0; FP16 tcgen05 IPT + refinement against FP64-accurate (double-FP32) defects, "
+            "FP64 CholQR2/Rayleigh-Ritz, to scaled residual 1e-8")
 PRODUCTS_FILE = os.path.join(ROOT, "oracle", "plain_ipt_products.json")
 MEASURED_PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
 # DRAM bytes (read + write) per launch from one ncu capture of each kernel on
@@ -596,15 +602,22 @@ def run_ours(args):
     lib.ipt_block_measure_fp64_peak(C.byref(fp64_peak))
     FP64_PEAK_TFLOPS = fp64_peak.value
     if name == "fp64_product":
-        flops = 2.0 * n * n * (sum(r["fp64_matvecs"] for r in reports) / steps) * steps
-        achieved = flops / (tot_ms * 1e-3) / 1e12
-        roofline = {"kernel": "dense64_partial_kernel (FP64 SIMT split-K)", "bound": "fp64",
-                    "achieved": achieved, "peak": FP64_PEAK_TFLOPS, "unit": "TFLOP/s",
-                    "frac": achieved / FP64_PEAK_TFLOPS,
-                    "traffic": NCU_TRAFFIC.get(("dense64_partial", n, k, args.precision)),
+        terms = n * n * (sum(r["fp64_matvecs"] for r in reports) / steps) * steps
+        fp32_peak = C.c_double(0.0)
+        lib.ipt_block_measure_fp32_peak(C.byref(fp32_peak))
+        FP32_PEAK_TFLOPS = fp32_peak.value
+        # the mixed solve forms its FP64-accurate products in double-FP32
+        # arithmetic: 12 FP32-pipe instructions per term (k_df64.cu)
+        achieved = 12.0 * terms / (tot_ms * 1e-3) / 1e12
+        peak_ops = FP32_PEAK_TFLOPS / 2.0
+        roofline = {"kernel": "df64_partial_kernel (double-FP32 FP64-accurate product, split-K)",
+                    "bound": "fp32_pipe", "achieved": achieved, "peak": peak_ops,
+                    "unit": "T FP32-pipe instructions/s", "frac": achieved / peak_ops,
+                    "fp64_equivalent_tflops": 2.0 * terms / (tot_ms * 1e-3) / 1e12,
+                    "traffic": NCU_TRAFFIC.get(("df64_partial", n, k, args.precision)),
                     "traffic_unit": "bytes per launch (ncu dram__bytes_read.sum + write.sum)",
-                    "peak_source": "ipt_block_measure_fp64_peak (DFMA throughput kernel, run "
-                                   "live; MEASURED_PEAKS.json has no FP64 entry)",
+                    "peak_source": "ipt_block_measure_fp32_peak (FFMA throughput kernel, run "
+                                   "live; MEASURED_PEAKS.json has no FP32 entry), as instructions/s",
                     "launches": cnt, "avg_launch_ms": tot_ms / max(1, cnt)}
     lp_ms, lp_cnt = prof["lowp_product"]
     ldp = (n + 63) // 64 * 64

@@ -243,6 +243,7 @@ SIGNATURES = [
     ("ipt_block_profile_reset", None, []),
     ("ipt_block_profile_read", _i, [_i, C.POINTER(C.c_char_p), _dp, C.POINTER(C.c_longlong)]),
     ("ipt_block_measure_fp64_peak", _i, [_dp]),
+    ("ipt_block_measure_fp32_peak", _i, [_dp]),
     ("ipt_block_solve_dense_device", _i, [_vp, _i, _i, C.POINTER(IPTBlockOptions), _vp, _vp,
                                           C.POINTER(IPTBlockReport)]),
     ("ipt_block_solve_dense", _i, [_vp, _i, _i, C.POINTER(IPTBlockOptions), _vp, _vp,

@@ -27,10 +27,15 @@ namespace iptgb {
 // ---------------------------------------------------------------------------
 struct DenseApply final : Fp64Apply {
     const double *H = nullptr;
+    // optional double-FP32 copy of H: products in double-float arithmetic on
+    // the FP32 pipe (k_df64.cu) instead of FP64 FMAs
+    const float *Hh = nullptr;
+    const float *Hl = nullptr;
     int n = 0;
     int sms = 148;
     cudaStream_t s = nullptr;
     DeviceBuffer<double> P;
+    DeviceBuffer<float> Xs;
     int apply(const double *V, int c, double *AV) override
     {
         const int S = dense64_split_for(n, c, sms);
@@ -40,7 +45,15 @@ struct DenseApply final : Fp64Apply {
         }
         {
             KernelTimerScope timer(kProfFp64Product, s);
-            IPTGB_CHECK(launch_dense64_partial(H, n, n, V, n, c, P.ptr, S, s));
+            if (Hh != nullptr) {
+                const size_t nc = (size_t)n * c;
+                if (Xs.count < 2 * nc) IPTGB_CHECK(Xs.alloc(2 * nc, s));
+                IPTGB_CHECK(launch_df_split(V, nc, Xs.ptr, Xs.ptr + nc, s));
+                IPTGB_CHECK(launch_df64_partial(Hh, Hl, n, n, Xs.ptr, Xs.ptr + nc, n, c, P.ptr, S,
+                                                s));
+            } else {
+                IPTGB_CHECK(launch_dense64_partial(H, n, n, V, n, c, P.ptr, S, s));
+            }
         }
         KernelTimerScope timer(kProfFp64Update, s);
         return launch_sum_partials(P.ptr, S, (size_t)n * c, AV, s);
@@ -339,6 +352,17 @@ int dense_block_device(const double *dH_in, int n, int k, const IPTBlockOptions 
     std::unique_ptr<LowpDenseOperator> lowp;
     int st = IPT_CUDA_SUCCESS;
     const bool lowp_mode = opt.ipt_precision != IPT_BLOCK_FP64;
+    // The mixed-precision solve forms its FP64-accurate products in
+    // double-FP32 arithmetic (one split of H per solve); the plain FP64
+    // path keeps FP64 FMAs throughout.
+    DeviceBuffer<float> Hsplit;
+    if (lowp_mode && !env_flag("IPT_GB300_FP64_DFMA", 0)) {
+        const size_t mat = (size_t)n * n;
+        IPTGB_CHECK(Hsplit.alloc(2 * mat, s));
+        IPTGB_CHECK(launch_df_split(dH, mat, Hsplit.ptr, Hsplit.ptr + mat, s));
+        apply.Hh = Hsplit.ptr;
+        apply.Hl = Hsplit.ptr + mat;
+    }
     if (lowp_mode) {
         const int kind = opt.ipt_precision == IPT_BLOCK_FP16 ? kLowpF16
                          : opt.ipt_precision == IPT_BLOCK_BF16 ? kLowpBF16

@@ -86,6 +86,11 @@ struct KernelTimerScope {
 };
 
 // A device buffer released by its destructor (stream-ordered when possible).
+// Keep memory freed to the current device's stream-ordered pool instead of
+// returning it to the driver at every synchronisation (the pool's default),
+// so repeated solves reuse their scratch; once per device and process.
+void retain_pool_memory();
+
 template <typename T>
 struct DeviceBuffer {
     T *ptr = nullptr;
@@ -97,6 +102,7 @@ struct DeviceBuffer {
     ~DeviceBuffer() { release(); }
     int alloc(size_t n, cudaStream_t s)
     {
+        retain_pool_memory();
         release();
         stream = s;
         count = n;

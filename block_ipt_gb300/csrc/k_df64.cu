@@ -1,0 +1,144 @@
+// k_df64.cu - FP64-accurate dense block product on the FP32 pipe.
+//
+// GB300 retires FP32 FMAs at 64x its FP64 rate, so the accurate products of
+// the mixed-precision solve (the FP64 defect HX of the refinement and the
+// final certification; the reference forms these with cublasDgemm,
+// IPT_C_GPU/src/ipt_cuda.cu:1649,1888) are computed in double-FP32
+// ("double-float") arithmetic: H and X are held as unevaluated sums of two
+// floats, hi + lo (H split once per solve, X per product), and every term
+//   h x = hh xh + (hh xl + hl xh) + O(2^-48 |h x|)
+// is formed with an exact two-product (p = hh xh, e = fma(hh, xh, -p)) and
+// added to a double-float accumulator (S, s) with an exact two-sum
+// (Knuth), ~12 FP32 operations per term.  The result carries ~48 bits, far
+// below the 1e-8 eigen-residual the products certify; the split-K layout
+// and the FP64 partial sums are those of the FP64 kernel (k_dense64.cu).
+#include "common.cuh"
+#include "kernels.cuh"
+
+namespace iptgb {
+
+constexpr int kDfRows = 256;
+constexpr int kDfChunk = 32;
+
+// hi = float(a), lo = float(a - hi)
+__global__ void df_split_kernel(const double *__restrict__ A, size_t count,
+                                float *__restrict__ hi, float *__restrict__ lo)
+{
+    const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= count) return;
+    const double a = A[e];
+    const float h = __double2float_rn(a);
+    hi[e] = h;
+    lo[e] = __double2float_rn(a - (double)h);
+}
+
+__device__ __forceinline__ void df_term(float &S, float &s, float hh, float hl, float xh, float xl)
+{
+    const float p = __fmul_rn(hh, xh);
+    const float pe = __fmaf_rn(hh, xh, -p);
+    const float t = __fmaf_rn(hh, xl, __fmaf_rn(hl, xh, pe));
+    const float u = __fadd_rn(S, p);
+    const float bp = __fsub_rn(u, S);
+    const float err = __fadd_rn(__fsub_rn(S, __fsub_rn(u, bp)), __fsub_rn(p, bp));
+    S = u;
+    s = __fadd_rn(s, __fadd_rn(err, t));
+}
+
+// Split-K partial product, one output row per thread, BN columns in
+// double-float registers; X chunk (hi, lo) staged in shared memory.
+// P[slice][column][row] (FP64) = the slice's partial sums.
+template <int BN>
+__global__ void __launch_bounds__(kDfRows, 1)
+df64_partial_kernel(const float *__restrict__ Hh, const float *__restrict__ Hl, int n,
+                    long long ldh, const float *__restrict__ Xh, const float *__restrict__ Xl,
+                    long long ldx, int k, double *__restrict__ P, int kslice)
+{
+    __shared__ float xsh[kDfChunk][BN];
+    __shared__ float xsl[kDfChunk][BN];
+    const int row = blockIdx.x * kDfRows + threadIdx.x;
+    const int sl = blockIdx.y;
+    const int c0 = blockIdx.z * BN;
+    const int kbeg = sl * kslice;
+    const int kend = min(n, kbeg + kslice);
+    float S[BN], s[BN];
+#pragma unroll
+    for (int j = 0; j < BN; ++j) {
+        S[j] = 0.f;
+        s[j] = 0.f;
+    }
+    const bool active = row < n;
+    const size_t rofs = active ? (size_t)row : 0;
+    for (int l0 = kbeg; l0 < kend; l0 += kDfChunk) {
+        const int lc = min(kDfChunk, kend - l0);
+        __syncthreads();
+        for (int e = threadIdx.x; e < kDfChunk * BN; e += kDfRows) {
+            const int ll = e % kDfChunk;
+            const int j = e / kDfChunk;
+            float vh = 0.f, vl = 0.f;
+            if (ll < lc && c0 + j < k) {
+                const size_t o = (size_t)(l0 + ll) + (size_t)(c0 + j) * (size_t)ldx;
+                vh = Xh[o];
+                vl = Xl[o];
+            }
+            xsh[ll][j] = vh;
+            xsl[ll][j] = vl;
+        }
+        __syncthreads();
+        if (active) {
+#pragma unroll 4
+            for (int ll = 0; ll < lc; ++ll) {
+                const size_t o = rofs + (size_t)(l0 + ll) * (size_t)ldh;
+                const float hh = __ldg(Hh + o);
+                const float hl = __ldg(Hl + o);
+#pragma unroll
+                for (int j = 0; j < BN; ++j) df_term(S[j], s[j], hh, hl, xsh[ll][j], xsl[ll][j]);
+            }
+        }
+    }
+    if (active) {
+#pragma unroll
+        for (int j = 0; j < BN; ++j) {
+            if (c0 + j < k) {
+                P[((size_t)sl * (size_t)k + (size_t)(c0 + j)) * (size_t)n + row] =
+                    (double)S[j] + (double)s[j];
+            }
+        }
+    }
+}
+
+int launch_df_split(const double *A, size_t count, float *hi, float *lo, cudaStream_t stream)
+{
+    df_split_kernel<<<blocks_for(count), kThreads, 0, stream>>>(A, count, hi, lo);
+    IPTGB_LAUNCH();
+    return IPT_CUDA_SUCCESS;
+}
+
+int launch_df64_partial(const float *Hh, const float *Hl, int n, long long ldh, const float *Xh,
+                        const float *Xl, long long ldx, int k, double *P, int S,
+                        cudaStream_t stream)
+{
+    int kslice = (n + S - 1) / S;
+    kslice = ((kslice + kDfChunk - 1) / kDfChunk) * kDfChunk;
+    const int row_blocks = (n + kDfRows - 1) / kDfRows;
+    // 16-column tiles also for wider blocks: H is re-read per tile (from L2 /
+    // HBM, cheap next to the FP32 work) but 80 instead of 148 registers let
+    // three CTAs share an SM (measured faster at n = 8192, k = 32)
+    int bn = k <= 8 ? 8 : 16;
+    const int over = env_int("IPT_GB300_DF_BN", 0);  // tuning override: 8, 16 or 32
+    if (over == 8 || over == 16 || over == 32) bn = over;
+    dim3 grid(row_blocks, S, (k + bn - 1) / bn);
+    if (bn == 8) {
+        df64_partial_kernel<8><<<grid, kDfRows, 0, stream>>>(Hh, Hl, n, ldh, Xh, Xl, ldx, k, P,
+                                                             kslice);
+    } else if (bn == 16) {
+        df64_partial_kernel<16><<<grid, kDfRows, 0, stream>>>(Hh, Hl, n, ldh, Xh, Xl, ldx, k, P,
+                                                              kslice);
+    } else {
+        df64_partial_kernel<32><<<grid, kDfRows, 0, stream>>>(Hh, Hl, n, ldh, Xh, Xl, ldx, k, P,
+                                                              kslice);
+    }
+    IPTGB_LAUNCH();
+    return IPT_CUDA_SUCCESS;
+}
+
+}  // namespace iptgb

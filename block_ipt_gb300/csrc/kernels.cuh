@@ -21,6 +21,11 @@ int launch_dense64_partial(const double *H, int n, long long ldh, const double *
 int launch_dense32_partial(const float *H, int n, long long ldh, const float *X, long long ldx,
                            int k, float *P, int S, cudaStream_t stream);
 int launch_sum_partials(const double *P, int S, size_t elems, double *Y, cudaStream_t stream);
+// Double-FP32 (hi + lo) FP64-accurate products (k_df64.cu).
+int launch_df_split(const double *A, size_t count, float *hi, float *lo, cudaStream_t stream);
+int launch_df64_partial(const float *Hh, const float *Hl, int n, long long ldh, const float *Xh,
+                        const float *Xl, long long ldx, int k, double *P, int S,
+                        cudaStream_t stream);
 int launch_dense64_update(const double *P, int S, int n, int k, const double *X,
                           const double *d, double *Xn, int want_norms, NormScratch *ns,
                           cudaStream_t stream);

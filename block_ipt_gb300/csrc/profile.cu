@@ -116,6 +116,70 @@ IPT_API int ipt_block_profile_read(int kernel, const char **name, double *total_
     return IPT_CUDA_SUCCESS;
 }
 
+namespace iptgb {
+void retain_pool_memory()
+{
+    static std::atomic<unsigned long long> done_mask{0};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return;
+    const unsigned long long bit = 1ULL << dev;
+    if (done_mask.load(std::memory_order_acquire) & bit) return;
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+        unsigned long long threshold = ~0ULL;
+        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &threshold);
+    }
+    done_mask.fetch_or(bit, std::memory_order_acq_rel);
+}
+}  // namespace iptgb
+
+// FP32 FMA throughput of this GPU (same shape as the FP64 probe below); the
+// denominator of kernels bound by the FP32 pipe.
+__global__ void ffma_probe_kernel(float *out, int iters, float a, float b)
+{
+    float acc[16];
+#pragma unroll
+    for (int c = 0; c < 16; ++c) acc[c] = (float)(threadIdx.x + c);
+    for (int it = 0; it < iters; ++it) {
+#pragma unroll
+        for (int c = 0; c < 16; ++c) acc[c] = fmaf(acc[c], a, b);
+    }
+    float s = 0.0f;
+#pragma unroll
+    for (int c = 0; c < 16; ++c) s += acc[c];
+    out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
+IPT_API int ipt_block_measure_fp32_peak(double *tflops)
+{
+    if (tflops == nullptr) return IPT_CUDA_INVALID_ARGUMENT;
+    int dev = 0, sms = 0;
+    IPTGB_CUDA(cudaGetDevice(&dev));
+    IPTGB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    const int blocks = 8 * sms, threads = 256, iters = 65536;
+    float *out = nullptr;
+    IPTGB_CUDA(cudaMalloc((void **)&out, sizeof(float) * blocks * threads));
+    cudaEvent_t a, b;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    ffma_probe_kernel<<<blocks, threads>>>(out, iters, 0.9999999f, 1e-7f);
+    cudaEventRecord(a);
+    ffma_probe_kernel<<<blocks, threads>>>(out, iters, 0.9999999f, 1e-7f);
+    cudaEventRecord(b);
+    cudaEventSynchronize(b);
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, a, b);
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    const cudaError_t e = cudaGetLastError();
+    cudaFree(out);
+    if (e != cudaSuccess || ms <= 0.0f) return IPT_CUDA_CUDA_ERROR;
+    count_launch();
+    count_launch();
+    *tflops = 2.0 * 16.0 * iters * (double)blocks * threads / (ms * 1e-3) / 1e12;
+    return IPT_CUDA_SUCCESS;
+}
+
 // FP64 FMA throughput of this GPU: 16 independent DFMA chains per thread,
 // 4 blocks of 256 threads per SM.  Used as the FP64 roofline denominator.
 __global__ void dfma_probe_kernel(double *out, int iters, double a, double b)

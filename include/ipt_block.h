@@ -300,6 +300,9 @@ int ipt_block_profile_read(int kernel, const char **name, double *total_ms, long
 /* FP64 FMA throughput of the current device in TFLOP/s (a short DFMA
  * throughput kernel); the FP64 roofline denominator. */
 int ipt_block_measure_fp64_peak(double *tflops);
+/* FP32 FMA throughput in TFLOP/s; the denominator of the double-FP32
+ * (FP64-accurate) products. */
+int ipt_block_measure_fp32_peak(double *tflops);
 
 #ifdef __cplusplus
 }
