@@ -47,8 +47,10 @@ PRODUCTS_FILE = os.path.join(ROOT, "oracle", "plain_ipt_products.json")
 MEASURED_PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
 # DRAM bytes (read + write) per launch from one ncu capture of each kernel on
 # this workload (profiles/dense64_partial_fp64_n8192_k32.md,
-# profiles/tc_partial_fp16_n8192_k32.md); keyed by (kernel, n, k, precision).
+# profiles/df64_partial_n8192_k32.md, profiles/tc_partial_fp16_n8192_k32.md);
+# keyed by (kernel, n, k, precision).
 NCU_TRAFFIC = {("dense64_partial", 8192, 32, "fp16"): 567.5e6,
+               ("df64_partial", 8192, 32, "fp16"): 1111.3e6,
                ("tc_partial", 8192, 32, "fp16"): 137.9e6}
 
 
