@@ -214,6 +214,7 @@ SIGNATURES = [
     ("ipt_mixed_precision_fp32_cuda_free_device_result", None, [C.POINTER(_MixedResult)]),
     ("ipt_mixed_precision_tf32_cuda_free_device_result", None, [C.POINTER(_MixedResult)]),
     ("ipt_block_default_options", None, [C.POINTER(IPTBlockOptions)]),
+    ("ipt_block_cholesky_inverse", _i, [_vp, _i, _vp, C.POINTER(C.c_int), _vp]),
     ("ipt_block_symmetric_eig", _i, [_vp, _i, _vp, _vp, _vp]),
     ("ipt_block_mlp_param_count", _i, []),
     ("ipt_block_batch_default_options", None, [C.POINTER(IPTBatchOptions)]),
@@ -242,6 +243,10 @@ SIGNATURES = [
     ("ipt_block_profile_enable", None, [_i]),
     ("ipt_block_profile_reset", None, []),
     ("ipt_block_profile_read", _i, [_i, C.POINTER(C.c_char_p), _dp, C.POINTER(C.c_longlong)]),
+    ("ipt_block_trace_enable", _i, [_i]),
+    ("ipt_block_trace_count", _i, []),
+    ("ipt_block_trace_read", _i, [_i, C.POINTER(C.c_char_p), C.POINTER(C.c_longlong),
+                                  C.POINTER(C.c_longlong)]),
     ("ipt_block_measure_fp64_peak", _i, [_dp]),
     ("ipt_block_measure_fp32_peak", _i, [_dp]),
     ("ipt_block_solve_dense_device", _i, [_vp, _i, _i, C.POINTER(IPTBlockOptions), _vp, _vp,

@@ -339,3 +339,19 @@ def block_solve_fci(spec, k, d_vectors_ptr, d_values_ptr, precision="fp64", **kw
     if st != _lib.IPT_CUDA_SUCCESS:
         raise IPTError(st, "ipt_block_solve_fci")
     return rep.as_dict()
+
+
+def trace_enable(on=True):
+    """Start (clearing earlier marks) or stop the solvers' phase marks."""
+    _check(_lib.load().ipt_block_trace_enable(1 if on else 0), "ipt_block_trace_enable")
+
+
+def trace_read():
+    """[(label, host_ns, gpu_ns)] of the marks recorded since trace_enable()."""
+    lib = _lib.load()
+    m = lib.ipt_block_trace_count()
+    labels = (C.c_char_p * max(1, m))()
+    host = (C.c_longlong * max(1, m))()
+    gpu = (C.c_longlong * max(1, m))()
+    _check(lib.ipt_block_trace_read(m, labels, host, gpu), "ipt_block_trace_read")
+    return [(labels[i].decode(), host[i], gpu[i]) for i in range(m)]

@@ -191,36 +191,84 @@ IptStage *make_fp64_csr_stage(const int *row_ptr, const int *col_ind, const doub
 }
 
 // ---------------------------------------------------------------------------
-// Row sums of |H| (dense col-major: thread per row, coalesced over columns).
+// Statistics of a dense symmetric H from one streaming pass: the diagonal,
+// the largest row sum of |H| (hnorm; a column sum, H being symmetric), the
+// largest off-diagonal |H_il| (the low-precision copy's scale) and the number
+// of descents d_{i+1} < d_i (zero: the diagonal is already ascending and no
+// permutation is needed).  One warp per column reads the contiguous column;
+// one 24-byte read brings the results to the host.
 // ---------------------------------------------------------------------------
-// Pass 1: per 256-column slab partial row sums (grid: row blocks x slabs, so
-// the whole GPU streams H once); pass 2 sums the slabs in a fixed order.
-constexpr int kRowSumSlab = 256;
+struct DenseStats {
+    unsigned long long hnorm_bits;   // non-negative doubles order like their bit patterns
+    unsigned long long maxabs_bits;
+    unsigned long long descents;
+};
 
-__global__ void dense_row_abs_partial_kernel(const double *__restrict__ H, int n,
-                                             double *__restrict__ part)
+constexpr int kStatsWarps = 8;
+
+__global__ void __launch_bounds__(32 * kStatsWarps)
+    dense_stats_kernel(const double *__restrict__ H, int n, bool vec, double *__restrict__ d,
+                       DenseStats *__restrict__ stats)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const int l0 = blockIdx.y * kRowSumSlab;
-    if (i >= n) return;
-    const int l1 = min(n, l0 + kRowSumSlab);
-    double s = 0.0;
-    for (int l = l0; l < l1; ++l) {
-        s += fabs(H[(size_t)i + (size_t)l * n]);
+    const int lane = threadIdx.x & 31;
+    const int c = blockIdx.x * kStatsWarps + (threadIdx.x >> 5);
+    if (c >= n) return;  // whole warps leave together
+    const double *col = H + (size_t)c * n;
+    double s = 0.0, m = 0.0;
+    if (vec) {  // n even and H 16-byte aligned: every column starts 16-byte aligned
+        const double2 *col2 = reinterpret_cast<const double2 *>(col);
+        const int half = n / 2;
+#pragma unroll 4
+        for (int q = lane; q < half; q += 32) {
+            const double2 v = col2[q];
+            const int l = 2 * q;
+            const double a0 = fabs(v.x), a1 = fabs(v.y);
+            s += a0 + a1;
+            m = fmax(m, l == c ? 0.0 : a0);
+            m = fmax(m, l + 1 == c ? 0.0 : a1);
+        }
+    } else {
+#pragma unroll 4
+        for (int l = lane; l < n; l += 32) {
+            const double a = fabs(col[l]);
+            s += a;
+            m = fmax(m, l == c ? 0.0 : a);
+        }
     }
-    part[(size_t)blockIdx.y * n + i] = s;
+    for (int off = 16; off > 0; off >>= 1) {
+        s += __shfl_xor_sync(0xffffffffu, s, off);
+        m = fmax(m, __shfl_xor_sync(0xffffffffu, m, off));
+    }
+    if (lane == 0) {
+        const size_t dstride = (size_t)n + 1;
+        const double dc = H[(size_t)c * dstride];
+        d[c] = dc;
+        if (c + 1 < n && H[(size_t)(c + 1) * dstride] < dc) {
+            atomicAdd(&stats->descents, 1ULL);
+        }
+        if (s > 0.0) atomicMax(&stats->hnorm_bits, (unsigned long long)__double_as_longlong(s));
+        if (m > 0.0) atomicMax(&stats->maxabs_bits, (unsigned long long)__double_as_longlong(m));
+    }
 }
 
-__global__ void dense_row_abs_finish_kernel(const double *__restrict__ part, int slabs, int n,
-                                            double *__restrict__ rs)
+// Diagonal and statistics of H on the stream; returns after the host has them.
+int dense_stats(const double *dH, int n, double *d, cudaStream_t s, double *hnorm,
+                double *maxabs_off, unsigned long long *descents)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    double s = 0.0;
-    for (int b = 0; b < slabs; ++b) {
-        s += part[(size_t)b * n + i];
-    }
-    rs[i] = s;
+    DeviceBuffer<DenseStats> st;
+    IPTGB_CHECK(st.alloc(1, s));
+    IPTGB_CUDA(cudaMemsetAsync(st.ptr, 0, sizeof(DenseStats), s));
+    const bool vec = (n % 2 == 0) && ((reinterpret_cast<uintptr_t>(dH) & 15) == 0);
+    dense_stats_kernel<<<(n + kStatsWarps - 1) / kStatsWarps, 32 * kStatsWarps, 0, s>>>(
+        dH, n, vec, d, st.ptr);
+    IPTGB_LAUNCH();
+    DenseStats h;
+    IPTGB_CUDA(cudaMemcpyAsync(&h, st.ptr, sizeof(h), cudaMemcpyDeviceToHost, s));
+    IPTGB_CUDA(cudaStreamSynchronize(s));
+    memcpy(hnorm, &h.hnorm_bits, sizeof(double));
+    memcpy(maxabs_off, &h.maxabs_bits, sizeof(double));
+    *descents = h.descents;
+    return IPT_CUDA_SUCCESS;
 }
 
 __global__ void csr_row_abs_sum_kernel(const int *row_ptr, const double *vals, int n, double *rs)
@@ -296,28 +344,29 @@ int dense_block_device(const double *dH_in, int n, int k, const IPTBlockOptions 
         return IPT_CUDA_INVALID_ARGUMENT;
     }
     cudaStream_t s = (cudaStream_t)opt.stream;
-    DeviceBuffer<double> d, rs, Hp, Xtmp;
+    DeviceBuffer<double> d, Hp, Xtmp;
     DeviceBuffer<int> dperm;
+    trace_mark("dense:start", s);
     IPTGB_CHECK(d.alloc((size_t)n, s));
-    IPTGB_CHECK(launch_extract_diagonal(dH_in, n, n, d.ptr, s));
-    // ascending diagonal order; permute H when it is not already sorted
-    std::vector<double> hd((size_t)n);
-    IPTGB_CUDA(cudaMemcpyAsync(hd.data(), d.ptr, (size_t)n * sizeof(double),
-                               cudaMemcpyDeviceToHost, s));
-    IPTGB_CUDA(cudaStreamSynchronize(s));
-    std::vector<int> perm((size_t)n);
-    std::iota(perm.begin(), perm.end(), 0);
-    std::stable_sort(perm.begin(), perm.end(),
-                     [&hd](int a, int b) { return hd[(size_t)a] < hd[(size_t)b]; });
-    bool permuted = false;
-    for (int i = 0; i < n; ++i) {
-        if (perm[(size_t)i] != i) {
-            permuted = true;
-            break;
-        }
-    }
+    // one pass: diagonal, hnorm, max off-diagonal, sortedness of the diagonal
+    double hnorm = 0.0, maxabs_off = 0.0;
+    unsigned long long descents = 0;
+    IPTGB_CHECK(dense_stats(dH_in, n, d.ptr, s, &hnorm, &maxabs_off, &descents));
+    trace_mark("dense:stats_done", s);
     const double *dH = dH_in;
+    const bool permuted = descents > 0;
     if (permuted) {
+        // ascending diagonal order (stable, as the reference's host
+        // preparation sorts): permute H symmetrically; the statistics are
+        // invariant under the permutation
+        std::vector<double> hd((size_t)n);
+        IPTGB_CUDA(cudaMemcpyAsync(hd.data(), d.ptr, (size_t)n * sizeof(double),
+                                   cudaMemcpyDeviceToHost, s));
+        IPTGB_CUDA(cudaStreamSynchronize(s));
+        std::vector<int> perm((size_t)n);
+        std::iota(perm.begin(), perm.end(), 0);
+        std::stable_sort(perm.begin(), perm.end(),
+                         [&hd](int a, int b) { return hd[(size_t)a] < hd[(size_t)b]; });
         IPTGB_CHECK(Hp.alloc((size_t)n * n, s));
         IPTGB_CHECK(dperm.alloc((size_t)n, s));
         IPTGB_CUDA(cudaMemcpyAsync(dperm.ptr, perm.data(), (size_t)n * sizeof(int),
@@ -329,19 +378,6 @@ int dense_block_device(const double *dH_in, int n, int k, const IPTBlockOptions 
         IPTGB_CHECK(launch_extract_diagonal(dH, n, n, d.ptr, s));
         IPTGB_CHECK(Xtmp.alloc((size_t)n * k, s));
     }
-    IPTGB_CHECK(rs.alloc((size_t)n, s));
-    {
-        const int slabs = (n + kRowSumSlab - 1) / kRowSumSlab;
-        DeviceBuffer<double> part;
-        IPTGB_CHECK(part.alloc((size_t)slabs * n, s));
-        dense_row_abs_partial_kernel<<<dim3(blocks_for(n), slabs), kThreads, 0, s>>>(dH, n,
-                                                                                   part.ptr);
-        IPTGB_LAUNCH();
-        dense_row_abs_finish_kernel<<<blocks_for(n), kThreads, 0, s>>>(part.ptr, slabs, n, rs.ptr);
-        IPTGB_LAUNCH();
-    }
-    double hnorm = 0.0;
-    IPTGB_CHECK(max_of_device(rs.ptr, n, s, &hnorm));
 
     DenseApply apply;
     apply.H = dH;
@@ -356,10 +392,9 @@ int dense_block_device(const double *dH_in, int n, int k, const IPTBlockOptions 
     // double-FP32 arithmetic (one split of H per solve); the plain FP64
     // path keeps FP64 FMAs throughout.
     DeviceBuffer<float> Hsplit;
+    const size_t mat = (size_t)n * n;
     if (lowp_mode && !env_flag("IPT_GB300_FP64_DFMA", 0)) {
-        const size_t mat = (size_t)n * n;
         IPTGB_CHECK(Hsplit.alloc(2 * mat, s));
-        IPTGB_CHECK(launch_df_split(dH, mat, Hsplit.ptr, Hsplit.ptr + mat, s));
         apply.Hh = Hsplit.ptr;
         apply.Hl = Hsplit.ptr + mat;
     }
@@ -367,10 +402,18 @@ int dense_block_device(const double *dH_in, int n, int k, const IPTBlockOptions 
         const int kind = opt.ipt_precision == IPT_BLOCK_FP16 ? kLowpF16
                          : opt.ipt_precision == IPT_BLOCK_BF16 ? kLowpBF16
                                                                : kLowpTF32;
-        lowp.reset(make_lowp_dense_operator(dH, n, kind, s, &st));
+        // one pass over H writes the low-precision Delta and the double-FP32 split
+        bool split_done = false;
+        lowp.reset(make_lowp_dense_operator(dH, n, kind, s, &st, maxabs_off,
+                                            Hsplit.ptr, Hsplit.ptr ? Hsplit.ptr + mat : nullptr,
+                                            &split_done, true));
         if (lowp == nullptr) {
             return st != IPT_CUDA_SUCCESS ? st : IPT_CUDA_INVALID_ARGUMENT;
         }
+        if (Hsplit.ptr != nullptr && !split_done) {
+            IPTGB_CHECK(launch_df_split(dH, mat, Hsplit.ptr, Hsplit.ptr + mat, s));
+        }
+        trace_mark("dense:operator_done", s);
         stage.reset(make_lowp_stage_on(lowp.get(), d.ptr, n, s));
     } else {
         stage.reset(make_fp64_dense_stage(dH, n, d.ptr, s));
@@ -438,6 +481,7 @@ int dense_block_device(const double *dH_in, int n, int k, const IPTBlockOptions 
                                                                               n, k, d_vectors);
         IPTGB_LAUNCH();
     }
+    trace_mark("dense:end", s);
     IPTGB_CUDA(cudaStreamSynchronize(s));
     return IPT_CUDA_SUCCESS;
 }
@@ -610,6 +654,31 @@ IPT_API int ipt_block_symmetric_eig(const double *d_T, int m, double *d_w, doubl
         st = IPT_CUDA_CUDA_ERROR;
     }
     return st;
+}
+
+IPT_API int ipt_block_cholesky_inverse(const double *d_G, int m, double *d_Rinv, int *shifts,
+                                       void *stream)
+{
+    if (d_G == nullptr || d_Rinv == nullptr || m <= 0 || m > 112) {
+        return IPT_CUDA_INVALID_ARGUMENT;
+    }
+    BlockOps ops;
+    ops.stream = (cudaStream_t)stream;
+    ops.sms = device_sm_count();
+    DeviceBuffer<int> st_dev;
+    IPTGB_CHECK(st_dev.alloc(1, ops.stream));
+    int st = ops.chol_inverse(d_G, m, d_Rinv, st_dev.ptr);
+    int h = -1;
+    if (st == IPT_CUDA_SUCCESS &&
+        (cudaMemcpyAsync(&h, st_dev.ptr, sizeof(int), cudaMemcpyDeviceToHost, ops.stream) !=
+             cudaSuccess ||
+         cudaStreamSynchronize(ops.stream) != cudaSuccess)) {
+        st = IPT_CUDA_CUDA_ERROR;
+    }
+    ops.release();
+    if (st != IPT_CUDA_SUCCESS) return st;
+    if (shifts != nullptr) *shifts = h;
+    return h < 0 ? IPT_CUDA_INVALID_ARGUMENT : IPT_CUDA_SUCCESS;
 }
 
 IPT_API void ipt_block_default_options(IPTBlockOptions *options)

@@ -23,7 +23,12 @@ struct BlockOps {
     int tall_gemm(const double *A, long long lda, const double *B, long long ldb, double *C,
                   long long ldc, int n, int m, int p, double alpha = 1.0, double beta = 0.0);
     // G = R^T R (one CTA); Rinv = R^{-1}; status_dev[0] = shifts used or -1.
-    int chol_inverse(const double *G, int m, double *Rinv, int *status_dev);
+    // cond_bound (device, optional): (1 + e) / (1 - e) with e the Frobenius
+    // distance of the unit-diagonal scaled G from I (infinite for e >= 1), a
+    // bound of that matrix's condition number; m <= 32 and no shift only,
+    // NaN otherwise.
+    int chol_inverse(const double *G, int m, double *Rinv, int *status_dev,
+                     double *cond_bound = nullptr);
     // Symmetric eigensolve for m <= 112: FP32 Jacobi + FP64 refinement +
     // FP64 cluster polish (k_eig.cu).  Ascending w, eigenvectors Z.
     int symmetric_eig(const double *T, int m, double *w, double *Z, int *sweeps_dev);

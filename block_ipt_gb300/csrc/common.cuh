@@ -77,6 +77,11 @@ enum ProfiledKernel {
     kProfCount = 9
 };
 bool profile_enabled();
+// Phase marks (ipt_block_trace_*): when enabled, a one-thread kernel writes
+// the GPU's global timer into the next slot in stream order and the host
+// clock at the call is kept beside it, so the gaps where the GPU waits for
+// the host show up.  label must be a string literal.
+void trace_mark(const char *label, cudaStream_t s);
 struct KernelTimerScope {
     int kernel;
     cudaStream_t stream;

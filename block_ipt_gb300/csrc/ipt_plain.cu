@@ -59,7 +59,6 @@ int SolveScratch::init(size_t max_elems, cudaStream_t stream)
     ns.norms = (double *)((char *)ns.counter + 8);
     ns.capacity = slots;
     IPTGB_CUDA(cudaMemsetAsync(ns.counter, 0, sizeof(unsigned int), stream));
-    IPTGB_CUDA(cudaMallocHost((void **)&host_norms, 2 * sizeof(double)));
     return IPT_CUDA_SUCCESS;
 }
 
@@ -71,11 +70,7 @@ void SolveScratch::release(cudaStream_t stream)
     if (ns.counter != nullptr) {
         cudaFreeAsync(ns.counter, stream);
     }
-    if (host_norms != nullptr) {
-        cudaFreeHost(host_norms);
-    }
     ns = NormScratch();
-    host_norms = nullptr;
 }
 
 int run_plain_ipt(Fp64Operator &op, int n, int k, const double *d, int maxiter, double tol,

@@ -43,7 +43,11 @@ struct CsrFp64Operator final : Fp64Operator {
 // Scratch owned by a solve: norm reduction slots + pinned readback.
 struct SolveScratch {
     NormScratch ns;
-    double *host_norms = nullptr;  // pinned, 2 doubles
+    // the 16-byte norm read-back lands in pageable memory: each read is
+    // followed by a stream synchronisation anyway, and a pinned allocation
+    // (with the device-wide synchronisation of its release) per solve cost
+    // more than it saved
+    double host_norms[2] = {0.0, 0.0};
     int init(size_t max_elems, cudaStream_t stream);
     void release(cudaStream_t stream);
 };

@@ -125,25 +125,28 @@ int BlockOps::gram(const double *A, long long lda, int ma, const double *B, long
 // (A: n x m, B: m x p, C: n x p, column-major).  One row per thread, 32
 // output columns per block column; B tile staged in shared memory.
 // ---------------------------------------------------------------------------
-constexpr int kTallCols = 32;
 constexpr int kTallK = 32;
+constexpr int kTallThreads = 128;
 
-__global__ void __launch_bounds__(256)
-tall_gemm_kernel(const double *__restrict__ A, long long lda, const double *__restrict__ B,
-                 long long ldb, double *__restrict__ C, long long ldc, int n, int m, int p,
-                 double alpha, double beta)
+// TC output columns per thread: fewer columns give more CTAs, so that the
+// FP64 pipes of every SM take part when n is only a few thousand rows.
+template <int TC>
+__global__ void __launch_bounds__(kTallThreads)
+    tall_gemm_kernel(const double *__restrict__ A, long long lda, const double *__restrict__ B,
+                     long long ldb, double *__restrict__ C, long long ldc, int n, int m, int p,
+                     double alpha, double beta)
 {
-    __shared__ double bs[kTallK][kTallCols];
+    __shared__ double bs[kTallK][TC];
     const int row = blockIdx.x * blockDim.x + threadIdx.x;
-    const int c0 = blockIdx.y * kTallCols;
-    double acc[kTallCols];
+    const int c0 = blockIdx.y * TC;
+    double acc[TC];
 #pragma unroll
-    for (int j = 0; j < kTallCols; ++j) {
+    for (int j = 0; j < TC; ++j) {
         acc[j] = 0.0;
     }
     for (int l0 = 0; l0 < m; l0 += kTallK) {
         __syncthreads();
-        for (int e = threadIdx.x; e < kTallK * kTallCols; e += blockDim.x) {
+        for (int e = threadIdx.x; e < kTallK * TC; e += blockDim.x) {
             const int l = e % kTallK;
             const int j = e / kTallK;
             bs[l][j] = (l0 + l < m && c0 + j < p) ? B[(size_t)(l0 + l) + (size_t)(c0 + j) * ldb] : 0.0;
@@ -154,7 +157,7 @@ tall_gemm_kernel(const double *__restrict__ A, long long lda, const double *__re
             for (int l = 0; l < lc; ++l) {
                 const double a = A[(size_t)row + (size_t)(l0 + l) * lda];
 #pragma unroll
-                for (int j = 0; j < kTallCols; ++j) {
+                for (int j = 0; j < TC; ++j) {
                     acc[j] = fma(a, bs[l][j], acc[j]);
                 }
             }
@@ -162,7 +165,7 @@ tall_gemm_kernel(const double *__restrict__ A, long long lda, const double *__re
     }
     if (row < n) {
 #pragma unroll
-        for (int j = 0; j < kTallCols; ++j) {
+        for (int j = 0; j < TC; ++j) {
             if (c0 + j < p) {
                 double *o = C + (size_t)row + (size_t)(c0 + j) * ldc;
                 *o = beta == 0.0 ? alpha * acc[j] : alpha * acc[j] + beta * *o;
@@ -177,9 +180,19 @@ int BlockOps::tall_gemm(const double *A, long long lda, const double *B, long lo
     if (p <= 0) {
         return IPT_CUDA_SUCCESS;
     }
-    dim3 grid((n + 255) / 256, (p + kTallCols - 1) / kTallCols);
+    const int row_blocks = (n + kTallThreads - 1) / kTallThreads;
+    const int want = 2 * std::max(1, sms);
     KernelTimerScope timer(kProfTallGemm, stream);
-    tall_gemm_kernel<<<grid, 256, 0, stream>>>(A, lda, B, ldb, C, ldc, n, m, p, alpha, beta);
+    if ((long long)row_blocks * ((p + 31) / 32) >= want) {
+        tall_gemm_kernel<32><<<dim3(row_blocks, (p + 31) / 32), kTallThreads, 0, stream>>>(
+            A, lda, B, ldb, C, ldc, n, m, p, alpha, beta);
+    } else if ((long long)row_blocks * ((p + 15) / 16) >= want) {
+        tall_gemm_kernel<16><<<dim3(row_blocks, (p + 15) / 16), kTallThreads, 0, stream>>>(
+            A, lda, B, ldb, C, ldc, n, m, p, alpha, beta);
+    } else {
+        tall_gemm_kernel<8><<<dim3(row_blocks, (p + 7) / 8), kTallThreads, 0, stream>>>(
+            A, lda, B, ldb, C, ldc, n, m, p, alpha, beta);
+    }
     IPTGB_LAUNCH();
     return IPT_CUDA_SUCCESS;
 }
@@ -192,10 +205,9 @@ int BlockOps::tall_gemm(const double *A, long long lda, const double *B, long lo
 // number of shifts used (0 = plain), or -1 if it never succeeded.
 // Dynamic shared memory: 2 * m * m doubles.
 // ---------------------------------------------------------------------------
-__global__ void chol_inverse_kernel(const double *__restrict__ G, int m, double *__restrict__ Rinv,
-                                    int *status)
+__device__ void chol_inverse_block(const double *__restrict__ G, int m, double *__restrict__ Rinv,
+                                   int *status, double *sm)
 {
-    extern __shared__ double sm[];
     double *L = sm;          // lower factor, row-major [i*m + j]
     double *W = sm + m * m;  // inverse of L, row-major
     __shared__ int fail;
@@ -290,6 +302,98 @@ __global__ void chol_inverse_kernel(const double *__restrict__ G, int m, double 
     if (tid == 0) {
         status[0] = attempts;
     }
+}
+
+__global__ void chol_inverse_kernel(const double *__restrict__ G, int m, double *__restrict__ Rinv,
+                                    int *status, double *cond_bound)
+{
+    extern __shared__ double sm[];
+    chol_inverse_block(G, m, Rinv, status, sm);
+    if (cond_bound != nullptr && threadIdx.x == 0) *cond_bound = NAN;  // not estimated here
+}
+
+// ---------------------------------------------------------------------------
+// One-warp Cholesky + inverse for m <= 32, in registers: lane i holds row i
+// of the lower factor (padded to the identity beyond m).  The same
+// right-looking factorisation as chol_inverse_block; a matrix that needs a
+// diagonal shift goes through chol_inverse_block (its shift retries and
+// status) instead.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(32)
+    chol_inverse32_kernel(const double *__restrict__ G, int m, double *__restrict__ Rinv,
+                          int *status, double *cond_bound)
+{
+    const int lane = threadIdx.x;
+    double a[32];
+#pragma unroll
+    for (int l = 0; l < 32; ++l) {
+        // G is symmetric: row `lane` of its lower triangle
+        a[l] = (lane < m && l < m) ? G[(size_t)l * m + lane] : (l == lane ? 1.0 : 0.0);
+    }
+    if (cond_bound != nullptr) {
+        // e = ||D^{-1/2} G D^{-1/2} - I||_F (D = diag G): the eigenvalues of
+        // the unit-diagonal G lie in [1 - e, 1 + e], so its condition number
+        // (which governs the orthogonality CholQR leaves) is at most
+        // (1 + e) / (1 - e)
+        double e2 = 0.0;
+        double dii = 1.0;
+#pragma unroll
+        for (int l = 0; l < 32; ++l) {
+            if (l == lane) dii = a[l];
+        }
+#pragma unroll
+        for (int l = 0; l < 32; ++l) {
+            const double dll = __shfl_sync(0xffffffffu, dii, l);
+            if (l != lane) e2 += a[l] * a[l] / (dii * dll);
+        }
+        for (int off = 16; off > 0; off >>= 1) e2 += __shfl_xor_sync(0xffffffffu, e2, off);
+        const bool bad = __any_sync(0xffffffffu, !(dii > 0.0));
+        if (lane == 0) {
+            const double e = sqrt(e2);
+            *cond_bound = (!bad && e < 1.0) ? (1.0 + e) / (1.0 - e) : INFINITY;
+        }
+    }
+    bool fail = false;
+#pragma unroll
+    for (int j = 0; j < 32; ++j) {
+        const double ajj = __shfl_sync(0xffffffffu, a[j], j);
+        fail = fail || !(ajj > 0.0) || !isfinite(ajj);  // warp-uniform
+        const double ljj = fail ? 1.0 : sqrt(ajj);
+        if (lane > j) {
+            a[j] = a[j] / ljj;
+        } else if (lane == j) {
+            a[j] = ljj;
+        }
+#pragma unroll
+        for (int l = j + 1; l < 32; ++l) {
+            const double alj = __shfl_sync(0xffffffffu, a[j], l);
+            if (lane >= l) a[l] -= a[j] * alj;
+        }
+    }
+    if (fail) {
+        __shared__ double sm[2 * 32 * 32];
+        chol_inverse_block(G, m, Rinv, status, sm);
+        if (cond_bound != nullptr && lane == 0) *cond_bound = NAN;  // shifted: not estimated
+        return;
+    }
+    // lane c: column c of W = L^{-1} (column-oriented forward substitution)
+    // = row c of R^{-1}
+    double w[32];
+#pragma unroll
+    for (int i = 0; i < 32; ++i) w[i] = lane == i ? 1.0 : 0.0;
+#pragma unroll
+    for (int l = 0; l < 32; ++l) {
+        w[l] = w[l] / __shfl_sync(0xffffffffu, a[l], l);
+#pragma unroll
+        for (int i = l + 1; i < 32; ++i) {
+            w[i] -= __shfl_sync(0xffffffffu, a[l], i) * w[l];
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < 32; ++i) {
+        if (lane < m && i < m) Rinv[(size_t)i * m + lane] = i < lane ? 0.0 : w[i];
+    }
+    if (lane == 0) status[0] = 0;
 }
 
 // ---------------------------------------------------------------------------
@@ -531,15 +635,20 @@ int BlockOps::proj_diag(const double *theta, int m, double *Tf, int ld)
     return IPT_CUDA_SUCCESS;
 }
 
-int BlockOps::chol_inverse(const double *G, int m, double *Rinv, int *status_dev)
+int BlockOps::chol_inverse(const double *G, int m, double *Rinv, int *status_dev, double *cond_bound)
 {
+    if (m <= 32) {
+        chol_inverse32_kernel<<<1, 32, 0, stream>>>(G, m, Rinv, status_dev, cond_bound);
+        IPTGB_LAUNCH();
+        return IPT_CUDA_SUCCESS;
+    }
     const size_t smem = 2 * (size_t)m * (size_t)m * sizeof(double);
     if (smem > 200 * 1024) {
         return IPT_CUDA_INVALID_ARGUMENT;
     }
     IPTGB_CUDA(cudaFuncSetAttribute(chol_inverse_kernel,
                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    chol_inverse_kernel<<<1, 256, smem, stream>>>(G, m, Rinv, status_dev);
+    chol_inverse_kernel<<<1, 256, smem, stream>>>(G, m, Rinv, status_dev, cond_bound);
     IPTGB_LAUNCH();
     return IPT_CUDA_SUCCESS;
 }

@@ -342,9 +342,12 @@ __device__ __forceinline__ tf32_t to_lp<tf32_t>(float v)
     return t;
 }
 
+// Delta (row-major, diagonal zeroed, scaled) in LP; with hi/lo also the
+// double-FP32 split of the full H in the same pass over H.
 template <typename LP>
 __global__ void convert_delta_kernel(const double *__restrict__ H, int n, int ldp, double scale,
-                                     LP *__restrict__ out)
+                                     LP *__restrict__ out, float *__restrict__ hi,
+                                     float *__restrict__ lo)
 {
     __shared__ float tile[32][33];
     const int l0 = blockIdx.x * 32;  // column block of H (= K index)
@@ -354,8 +357,15 @@ __global__ void convert_delta_kernel(const double *__restrict__ H, int n, int ld
         const int i = i0 + tx;
         const int l = l0 + ty;
         float v = 0.0f;
-        if (i < n && l < n && i != l) {
-            v = (float)(scale * H[(size_t)i + (size_t)l * n]);
+        if (i < n && l < n) {
+            const size_t o = (size_t)i + (size_t)l * n;
+            const double h = H[o];
+            if (i != l) v = (float)(scale * h);
+            if (hi != nullptr) {
+                const float hh = __double2float_rn(h);
+                hi[o] = hh;
+                lo[o] = __double2float_rn(h - (double)hh);
+            }
         }
         tile[ty][tx] = v;  // tile[l - l0][i - i0]
     }
@@ -365,6 +375,62 @@ __global__ void convert_delta_kernel(const double *__restrict__ H, int n, int ld
         const int l = l0 + tx;
         if (i < n && l < ldp) {
             out[(size_t)i * ldp + l] = to_lp<LP>(tile[tx][ty]);
+        }
+    }
+}
+
+// The same conversion for a symmetric H without the transpose: row i of
+// Delta is column i of H, so the pass streams H column by column, writes
+// Delta rows and (with hi/lo) the split in H's own layout.  One CTA covers
+// 2048 entries of one column; each thread two adjacent entries per step
+// (double2 loads when vec: n even and H 16-byte aligned).
+constexpr int kSymChunk = 2048;
+template <typename LP>
+struct alignas(2 * sizeof(LP)) LpPair {  // two adjacent Delta entries, one store
+    LP x, y;
+};
+template <typename LP>
+__global__ void __launch_bounds__(256)
+    convert_delta_sym_kernel(const double *__restrict__ H, int n, int ldp, double scale, bool vec,
+                             LP *__restrict__ out, float *__restrict__ hi,
+                             float *__restrict__ lo)
+{
+    const int c = blockIdx.x;  // column of H = row of Delta
+    const size_t col = (size_t)c * n;
+    LP *orow = out + (size_t)c * ldp;
+#pragma unroll
+    for (int u = 0; u < kSymChunk / 512; ++u) {
+        const int l = blockIdx.y * kSymChunk + u * 512 + 2 * threadIdx.x;  // even
+        if (l >= ldp) break;  // ldp is a multiple of 64: l + 1 < ldp as well
+        double h0 = 0.0, h1 = 0.0;
+        if (vec && l + 1 < n) {
+            const double2 v = *reinterpret_cast<const double2 *>(H + col + l);
+            h0 = v.x;
+            h1 = v.y;
+        } else {
+            if (l < n) h0 = H[col + l];
+            if (l + 1 < n) h1 = H[col + l + 1];
+        }
+        const float v0 = (l < n && l != c) ? (float)(scale * h0) : 0.0f;
+        const float v1 = (l + 1 < n && l + 1 != c) ? (float)(scale * h1) : 0.0f;
+        *reinterpret_cast<LpPair<LP> *>(orow + l) = LpPair<LP>{to_lp<LP>(v0), to_lp<LP>(v1)};
+        if (hi != nullptr) {
+            const float a0 = __double2float_rn(h0), a1 = __double2float_rn(h1);
+            const float b0 = __double2float_rn(h0 - (double)a0);
+            const float b1 = __double2float_rn(h1 - (double)a1);
+            if (vec && l + 1 < n) {
+                *reinterpret_cast<float2 *>(hi + col + l) = make_float2(a0, a1);
+                *reinterpret_cast<float2 *>(lo + col + l) = make_float2(b0, b1);
+            } else {
+                if (l < n) {
+                    hi[col + l] = a0;
+                    lo[col + l] = b0;
+                }
+                if (l + 1 < n) {
+                    hi[col + l + 1] = a1;
+                    lo[col + l + 1] = b1;
+                }
+            }
         }
     }
 }
@@ -635,7 +701,8 @@ struct LowpDense final : LowpDenseOperator {
     static constexpr int esize = (int)sizeof(LP);
     static constexpr int kchunk = 128 / esize;
 
-    int init(const double *dH, int n_, cudaStream_t s_)
+    int init(const double *dH, int n_, cudaStream_t s_, double maxabs_hint = -1.0,
+             float *split_hi = nullptr, float *split_lo = nullptr, bool symmetric = false)
     {
         n = n_;
         s = s_;
@@ -645,25 +712,38 @@ struct LowpDense final : LowpDenseOperator {
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         ldp = ((n + 63) / 64) * 64;
         IPTGB_CHECK(delta.alloc((size_t)n * ldp, s));
-        DeviceBuffer<unsigned long long> mx;
-        IPTGB_CHECK(mx.alloc(1, s));
-        IPTGB_CUDA(cudaMemsetAsync(mx.ptr, 0, sizeof(unsigned long long), s));
-        max_abs_offdiag_kernel<<<std::min(4 * sms, blocks_for((size_t)n * n)), kThreads, 0, s>>>(
-            dH, n, mx.ptr);
-        IPTGB_LAUNCH();
-        unsigned long long bits = 0;
-        IPTGB_CUDA(cudaMemcpyAsync(&bits, mx.ptr, sizeof(bits), cudaMemcpyDeviceToHost, s));
-        IPTGB_CUDA(cudaStreamSynchronize(s));
-        double maxabs;
-        memcpy(&maxabs, &bits, sizeof(maxabs));
+        double maxabs = maxabs_hint;
+        if (!(maxabs >= 0.0)) {
+            DeviceBuffer<unsigned long long> mx;
+            IPTGB_CHECK(mx.alloc(1, s));
+            IPTGB_CUDA(cudaMemsetAsync(mx.ptr, 0, sizeof(unsigned long long), s));
+            max_abs_offdiag_kernel<<<std::min(4 * sms, blocks_for((size_t)n * n)), kThreads, 0,
+                                     s>>>(dH, n, mx.ptr);
+            IPTGB_LAUNCH();
+            unsigned long long bits = 0;
+            IPTGB_CUDA(cudaMemcpyAsync(&bits, mx.ptr, sizeof(bits), cudaMemcpyDeviceToHost, s));
+            IPTGB_CUDA(cudaStreamSynchronize(s));
+            memcpy(&maxabs, &bits, sizeof(maxabs));
+        }
         scale = 1.0;
         if (LowpTypes<LP>::kind == kLowpF16 && maxabs > 0.0 && isfinite(maxabs)) {
             // largest power of two with maxabs * scale <= 16384 (FP16 max 65504)
             scale = ldexp(1.0, (int)floor(log2(16384.0 / maxabs)));
             scale = std::min(std::max(scale, ldexp(1.0, -40)), ldexp(1.0, 40));
         }
-        dim3 grid((ldp + 31) / 32, (n + 31) / 32);
-        convert_delta_kernel<LP><<<grid, dim3(32, 8), 0, s>>>(dH, n, ldp, scale, delta.ptr);
+        if (symmetric) {
+            // vec also needs hi/lo 8-byte aligned at even offsets (pool allocations are)
+            const bool vec = (n % 2 == 0) && ((reinterpret_cast<uintptr_t>(dH) & 15) == 0) &&
+                             ((reinterpret_cast<uintptr_t>(split_hi) & 7) == 0) &&
+                             ((reinterpret_cast<uintptr_t>(split_lo) & 7) == 0);
+            dim3 grid(n, (ldp + kSymChunk - 1) / kSymChunk);
+            convert_delta_sym_kernel<LP><<<grid, 256, 0, s>>>(dH, n, ldp, scale, vec, delta.ptr,
+                                                              split_hi, split_lo);
+        } else {
+            dim3 grid((ldp + 31) / 32, (n + 31) / 32);
+            convert_delta_kernel<LP><<<grid, dim3(32, 8), 0, s>>>(dH, n, ldp, scale, delta.ptr,
+                                                                  split_hi, split_lo);
+        }
         IPTGB_LAUNCH();
         IPTGB_CHECK(make_map(&mapA, LowpTypes<LP>::dt, esize, delta.ptr, ldp, n, tc::kBM));
         IPTGB_CHECK(err.alloc(1, s));
@@ -997,8 +1077,10 @@ struct LowpDenseSimtF32 final : LowpDenseOperator {
 };
 
 LowpDenseOperator *make_lowp_dense_operator(const double *dH, int n, int kind, cudaStream_t s,
-                                            int *status)
+                                            int *status, double maxabs_hint, float *split_hi,
+                                            float *split_lo, bool *split_done, bool symmetric)
 {
+    if (split_done != nullptr) *split_done = false;
     int dev = 0, major = 0, minor = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev);
@@ -1013,15 +1095,18 @@ LowpDenseOperator *make_lowp_dense_operator(const double *dH, int n, int kind, c
     if (kind == kLowpF16) {
         auto *o = new LowpDense<__half>();
         op.reset(o);
-        st = o->init(dH, n, s);
+        st = o->init(dH, n, s, maxabs_hint, split_hi, split_lo, symmetric);
+        if (split_done != nullptr) *split_done = split_hi != nullptr && split_lo != nullptr;
     } else if (kind == kLowpBF16) {
         auto *o = new LowpDense<__nv_bfloat16>();
         op.reset(o);
-        st = o->init(dH, n, s);
+        st = o->init(dH, n, s, maxabs_hint, split_hi, split_lo, symmetric);
+        if (split_done != nullptr) *split_done = split_hi != nullptr && split_lo != nullptr;
     } else if (kind == kLowpTF32) {
         auto *o = new LowpDense<tf32_t>();
         op.reset(o);
-        st = o->init(dH, n, s);
+        st = o->init(dH, n, s, maxabs_hint, split_hi, split_lo, symmetric);
+        if (split_done != nullptr) *split_done = split_hi != nullptr && split_lo != nullptr;
     } else if (kind == kLowpF32) {
         auto *o = new LowpDenseSimtF32();
         op.reset(o);
@@ -1048,6 +1133,7 @@ struct LowpStage final : IptStage {
     {
         IPTGB_CHECK(op->set_width(p));
         IPTGB_CHECK(op->reset_identity(d));
+        trace_mark("ipt:start", s);
         return run_lowp_ipt(*op, n, p, maxiter, tol, check_every, X, iterations, fpres_out,
                             matvecs, s, true);
     }
@@ -1105,6 +1191,7 @@ int run_lowp_ipt(LowpDenseOperator &op, int n, int p, int maxiter, double tol, i
         if (status != IPT_CUDA_SUCCESS) break;
         done = it + 1;
         if (want) {
+            trace_mark("ipt:check", s);
             if (op.read_error(&host_err) != IPT_CUDA_SUCCESS ||
                 cudaMemcpyAsync(scratch.host_norms, scratch.ns.norms, 2 * sizeof(double),
                                 cudaMemcpyDeviceToHost, s) != cudaSuccess ||

@@ -40,8 +40,15 @@ struct LowpDenseOperator {
     virtual int refine_apply(double *X) = 0;  // X += delta (FP64)
 };
 
+// maxabs_hint >= 0: max |H_il| (l != i) is already known (skips a pass over
+// H); split_hi/lo non-null: the conversion pass also writes the double-FP32
+// split of H (hi = float(h), lo = float(h - hi), column-major) and sets
+// *split_done; symmetric: H is exactly symmetric, so the conversion streams
+// columns of H as rows of Delta without a transpose.
 LowpDenseOperator *make_lowp_dense_operator(const double *dH, int n, int kind, cudaStream_t s,
-                                            int *status);
+                                            int *status, double maxabs_hint = -1.0,
+                                            float *split_hi = nullptr, float *split_lo = nullptr,
+                                            bool *split_done = nullptr, bool symmetric = false);
 
 int run_lowp_ipt(LowpDenseOperator &op, int n, int p, int maxiter, double tol, int check_every,
                  double *X, int *iterations, double *fpres_out, long long *matvecs,

@@ -1,5 +1,6 @@
 // profile.cu - launch counter and optional per-kernel event timing.
 #include <atomic>
+#include <chrono>
 #include <mutex>
 #include <vector>
 
@@ -76,9 +77,84 @@ KernelTimerScope::~KernelTimerScope()
     }
 }
 
+// ---- phase marks -----------------------------------------------------------
+namespace {
+constexpr int kTraceSlots = 4096;
+std::atomic<bool> g_trace{false};
+unsigned long long *g_trace_dev = nullptr;  // kTraceSlots GPU timestamps (ns)
+struct TraceMark {
+    const char *label;
+    long long host_ns;
+};
+std::vector<TraceMark> g_marks;
+
+long long host_now_ns()
+{
+    return std::chrono::duration_cast<std::chrono::nanoseconds>(
+               std::chrono::steady_clock::now().time_since_epoch())
+        .count();
+}
+
+__global__ void trace_mark_kernel(unsigned long long *slot)
+{
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    *slot = t;
+}
+}  // namespace
+
+void trace_mark(const char *label, cudaStream_t s)
+{
+    if (!g_trace.load(std::memory_order_relaxed)) return;
+    std::lock_guard<std::mutex> lock(g_mu);
+    if (g_trace_dev == nullptr || g_marks.size() >= (size_t)kTraceSlots) return;
+    g_marks.push_back({label, host_now_ns()});
+    trace_mark_kernel<<<1, 1, 0, s>>>(g_trace_dev + (g_marks.size() - 1));
+}
+
 }  // namespace iptgb
 
 using namespace iptgb;
+
+IPT_API int ipt_block_trace_enable(int on)
+{
+    std::lock_guard<std::mutex> lock(g_mu);
+    g_marks.clear();
+    if (on != 0 && g_trace_dev == nullptr) {
+        if (cudaMalloc(&g_trace_dev, kTraceSlots * sizeof(unsigned long long)) != cudaSuccess) {
+            g_trace_dev = nullptr;
+            return IPT_CUDA_ALLOCATION_FAILED;
+        }
+    }
+    g_trace.store(on != 0);
+    return IPT_CUDA_SUCCESS;
+}
+
+IPT_API int ipt_block_trace_count(void)
+{
+    std::lock_guard<std::mutex> lock(g_mu);
+    return (int)g_marks.size();
+}
+
+IPT_API int ipt_block_trace_read(int count, const char **labels, long long *host_ns,
+                                 long long *gpu_ns)
+{
+    std::lock_guard<std::mutex> lock(g_mu);
+    if (count < 0 || count > (int)g_marks.size() || (count > 0 && g_trace_dev == nullptr)) {
+        return IPT_CUDA_INVALID_ARGUMENT;
+    }
+    std::vector<unsigned long long> t((size_t)count);
+    if (count > 0 && cudaMemcpy(t.data(), g_trace_dev, (size_t)count * sizeof(t[0]),
+                                cudaMemcpyDeviceToHost) != cudaSuccess) {
+        return IPT_CUDA_CUDA_ERROR;
+    }
+    for (int i = 0; i < count; ++i) {
+        if (labels != nullptr) labels[i] = g_marks[(size_t)i].label;
+        if (host_ns != nullptr) host_ns[i] = g_marks[(size_t)i].host_ns;
+        if (gpu_ns != nullptr) gpu_ns[i] = (long long)t[(size_t)i];
+    }
+    return IPT_CUDA_SUCCESS;
+}
 
 IPT_API long long ipt_block_launch_count(void)
 {

@@ -176,6 +176,7 @@ int refine_solve(const RefineInput &in, double *X_out, double *values_out, IPTBl
         }
     } guard{ev};
     IPTGB_CUDA(cudaEventRecord(ev[0], s));
+    trace_mark("refine:start", s);
 
     // ---- initial block ---------------------------------------------------------
     if (in.ipt != nullptr) {
@@ -191,6 +192,7 @@ int refine_solve(const RefineInput &in, double *X_out, double *values_out, IPTBl
         IPTGB_CHECK(launch_set_identity(X.ptr, n, k, s));
     }
     IPTGB_CUDA(cudaEventRecord(ev[1], s));
+    trace_mark("refine:ipt_done", s);
 
     // ---- outer refinement ---------------------------------------------------------
     const int max_outer = std::max(1, in.max_outer);
@@ -201,7 +203,9 @@ int refine_solve(const RefineInput &in, double *X_out, double *values_out, IPTBl
     SolveScratch scratch;
     IPTGB_CHECK(scratch.init(elems, s));
     for (; outer < max_outer; ++outer) {
+        trace_mark("refine:defect", s);
         IPTGB_CHECK(in.apply->apply(X.ptr, k, HX.ptr));
+        trace_mark("refine:defect_product_done", s);
         rep->fp64_matvecs += k;
         defect_partial_kernel<<<dim3(chunks, k), 256, 0, s>>>(X.ptr, HX.ptr, in.d, n, k, R0.ptr, c,
                                                               P);
@@ -251,6 +255,7 @@ int refine_solve(const RefineInput &in, double *X_out, double *values_out, IPTBl
             }
             IPTGB_CUDA(cudaMemcpyAsync(sigma, h_sigma.data(), (size_t)k * sizeof(float),
                                        cudaMemcpyHostToDevice, s));
+            trace_mark("refine:correction", s);
             IPTGB_CHECK(in.lowp->refine_begin(R0.ptr, X.ptr, c, sigma));
             const int check = 8;
             for (int i = 0; i < in.inner_maxiter; ++i) {
@@ -258,6 +263,7 @@ int refine_solve(const RefineInput &in, double *X_out, double *values_out, IPTBl
                 IPTGB_CHECK(in.lowp->refine_step(want, &scratch.ns));
                 rep->lowp_matvecs += k;
                 if (want) {
+                    trace_mark("refine:correction_check", s);
                     IPTGB_CUDA(cudaMemcpyAsync(scratch.host_norms, scratch.ns.norms,
                                                2 * sizeof(double), cudaMemcpyDeviceToHost, s));
                     IPTGB_CUDA(cudaStreamSynchronize(s));
@@ -277,6 +283,7 @@ int refine_solve(const RefineInput &in, double *X_out, double *values_out, IPTBl
     scratch.release(s);
     rep->restarts = outer;
     IPTGB_CUDA(cudaEventRecord(ev[2], s));
+    trace_mark("refine:rayleigh_ritz", s);
     if (!conv) {
         rep->max_scaled_residual = best;
         IPTGB_CUDA(cudaMemcpyAsync(X_fallback, X.ptr, elems * sizeof(double),
@@ -287,28 +294,53 @@ int refine_solve(const RefineInput &in, double *X_out, double *values_out, IPTBl
     }
 
     // ---- Rayleigh-Ritz on span(X) with the FP64 HX of the last product ----------
-    auto cholqr_pair = [&](double *A, double *HA, double *A2, double *HA2) -> int {
+    // CholQR2 (the reference orthonormalises with an FP32 QR and one
+    // Cholesky repair pass, IPT_C_GPU/mixed/ipt_rayleigh_mixed_mpqr_cuda.cu:
+    // 319-360).  The second pass only repairs the orthogonality the first
+    // leaves, about cond(G) * eps for the column-scaled Gram matrix G: with
+    // the bound of that condition number at most kCholQr1Cond the first pass
+    // is kept (an IPT block near convergence is close to orthogonal).
+    constexpr double kCholQr1Cond = 100.0;
+    double *cond_dev = P + (size_t)chunks * k * 3;  // spare tail of `small`
+    auto cholqr_pair = [&](double *A, double *HA, double *A2, double *HA2, double *cond_out,
+                           double *h_cond) -> int {
         IPTGB_CHECK(ops.gram(A, n, k, A, n, k, n, G, k));
-        IPTGB_CHECK(ops.chol_inverse(G, k, Rinv, st_dev));
+        IPTGB_CHECK(ops.chol_inverse(G, k, Rinv, st_dev, cond_out));
         IPTGB_CHECK(ops.tall_gemm(A, n, Rinv, k, A2, n, n, k, k));
         IPTGB_CHECK(ops.tall_gemm(HA, n, Rinv, k, HA2, n, n, k, k));
         IPTGB_CUDA(cudaMemcpyAsync(&h_status, st_dev, sizeof(int), cudaMemcpyDeviceToHost, s));
+        if (cond_out != nullptr) {
+            IPTGB_CUDA(cudaMemcpyAsync(h_cond, cond_out, sizeof(double), cudaMemcpyDeviceToHost,
+                                       s));
+        }
         IPTGB_CUDA(cudaStreamSynchronize(s));
         return h_status < 0 ? IPT_CUDA_INVALID_ARGUMENT : IPT_CUDA_SUCCESS;
     };
-    IPTGB_CHECK(cholqr_pair(X.ptr, HX.ptr, Q.ptr, HQ.ptr));
-    IPTGB_CHECK(cholqr_pair(Q.ptr, HQ.ptr, X.ptr, HX.ptr));  // CholQR2: basis back in X / HX
-    IPTGB_CHECK(ops.gram(X.ptr, n, k, HX.ptr, n, k, n, T, k));
+    double h_cond = INFINITY;
+    IPTGB_CHECK(cholqr_pair(X.ptr, HX.ptr, Q.ptr, HQ.ptr, k <= 32 ? cond_dev : nullptr, &h_cond));
+    // basis B / HB, output O / HO
+    double *B = Q.ptr, *HB = HQ.ptr, *O = X.ptr, *HO = HX.ptr;
+    if (!(h_cond <= kCholQr1Cond)) {
+        IPTGB_CHECK(cholqr_pair(Q.ptr, HQ.ptr, X.ptr, HX.ptr, nullptr, nullptr));
+        B = X.ptr;
+        HB = HX.ptr;
+        O = Q.ptr;
+        HO = HQ.ptr;
+    }
+    IPTGB_CHECK(ops.gram(B, n, k, HB, n, k, n, T, k));
+    trace_mark("refine:projected_eig", s);
     IPTGB_CHECK(ops.symmetric_eig(T, k, theta, Z, st_dev));
-    IPTGB_CHECK(ops.tall_gemm(X.ptr, n, Z, k, Q.ptr, n, n, k, k));
-    IPTGB_CHECK(ops.tall_gemm(HX.ptr, n, Z, k, HQ.ptr, n, n, k, k));
-    IPTGB_CHECK(ops.residuals(Q.ptr, HQ.ptr, theta, n, k, n, in.hnorm, R0.ptr, rnorm, scaled));
+    trace_mark("refine:projected_eig_done", s);
+    IPTGB_CHECK(ops.tall_gemm(B, n, Z, k, O, n, n, k, k));
+    IPTGB_CHECK(ops.tall_gemm(HB, n, Z, k, HO, n, n, k, k));
+    IPTGB_CHECK(ops.residuals(O, HO, theta, n, k, n, in.hnorm, R0.ptr, rnorm, scaled));
     IPTGB_CUDA(cudaMemcpyAsync(h_scaled.data(), scaled, (size_t)k * sizeof(double),
                                cudaMemcpyDeviceToHost, s));
-    IPTGB_CUDA(cudaMemcpyAsync(X_out, Q.ptr, elems * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    IPTGB_CUDA(cudaMemcpyAsync(X_out, O, elems * sizeof(double), cudaMemcpyDeviceToDevice, s));
     IPTGB_CUDA(cudaMemcpyAsync(values_out, theta, (size_t)k * sizeof(double),
                                cudaMemcpyDeviceToDevice, s));
     IPTGB_CUDA(cudaEventRecord(ev[3], s));
+    trace_mark("refine:end", s);
     IPTGB_CUDA(cudaStreamSynchronize(s));
     double mx = 0.0;
     for (int j = 0; j < k; ++j) {
@@ -325,7 +357,7 @@ int refine_solve(const RefineInput &in, double *X_out, double *values_out, IPTBl
     rep->total_ms = ev_ms(ev[0], ev[3]);
     *converged_out = rep->converged == 1;
     if (!*converged_out) {
-        IPTGB_CUDA(cudaMemcpyAsync(X_fallback, Q.ptr, elems * sizeof(double),
+        IPTGB_CUDA(cudaMemcpyAsync(X_fallback, O, elems * sizeof(double),
                                    cudaMemcpyDeviceToDevice, s));
         IPTGB_CUDA(cudaStreamSynchronize(s));
     }

@@ -127,6 +127,16 @@ int ipt_block_solve_csr(const int *row_ptr, const int *col_ind, const double *va
  * eigenvectors d_Z (m*m, column-major); synchronises `stream`. */
 int ipt_block_symmetric_eig(const double *d_T, int m, double *d_w, double *d_Z, void *stream);
 
+/* Cholesky factor inverse of a small SPD Gram matrix (m <= 112, column-major,
+ * device): G = R^T R, d_Rinv = R^{-1} (upper triangular, column-major), the
+ * step of CholQR that replaces the reference's cusolverDnDpotrf + cublasDtrsm
+ * pair (IPT_C_GPU/mixed/ipt_rayleigh_mixed_mpqr_cuda.cu:335-360).  A matrix
+ * that is not numerically positive definite is factored as G + shift*I with
+ * the shift grown from 1e-14 trace(G) by 100x per retry; *shifts gets the
+ * number of retries (0 = plain).  Returns IPT_CUDA_INVALID_ARGUMENT with
+ * *shifts = -1 when 12 retries do not suffice.  Synchronises `stream`. */
+int ipt_block_cholesky_inverse(const double *d_G, int m, double *d_Rinv, int *shifts, void *stream);
+
 /* ---- allocation-free FP64 dense solve ------------------------------------ */
 
 /* No counterpart in the reference.  The tolerance-stopped FP64 dense IPT of
@@ -296,6 +306,17 @@ long long ipt_block_launch_count(void);
 void ipt_block_profile_enable(int on);
 void ipt_block_profile_reset(void);
 int ipt_block_profile_read(int kernel, const char **name, double *total_ms, long long *launches);
+
+/* Phase marks of the solvers (off by default).  Enabling clears the list.
+ * While enabled, each mark point of a solve (setup passes, IPT checks,
+ * refinement steps, Rayleigh-Ritz, end) launches a one-thread kernel that
+ * stores the GPU global timer (ns) in stream order, and keeps the host's
+ * steady clock (ns) at the call: gpu - host offsets that grow between two
+ * marks show the GPU waiting for the host.  read copies the first count
+ * marks (labels are static strings); at most 4096 marks are kept. */
+int ipt_block_trace_enable(int on);
+int ipt_block_trace_count(void);
+int ipt_block_trace_read(int count, const char **labels, long long *host_ns, long long *gpu_ns);
 
 /* FP64 FMA throughput of the current device in TFLOP/s (a short DFMA
  * throughput kernel); the FP64 roofline denominator. */

@@ -116,3 +116,49 @@ def test_block_cluster_env_path(cuda, monkeypatch):
     np.testing.assert_allclose(v, w, atol=1e-9)
     np.testing.assert_allclose(np.linalg.norm(X, axis=0), 1.0, atol=1e-10)
     assert info["basis_cols"] >= 5
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp16"])
+def test_block_dense_diagonal_order_cases(cuda, prec):
+    """The one-pass statistics decide whether H is permuted: a permuted
+    (descending somewhere) diagonal, and ties (a stable sort keeps them)."""
+    H, _ = workloads.dense_config0(512, seed=4)
+    P = np.random.default_rng(1).permutation(512)
+    Hp = np.asfortranarray(H[np.ix_(P, P)])
+    X, v, rep = api.block_solve_dense(Hp, 6, prec)
+    assert rep["converged"] == 1
+    check_pairs(Hp, X, v, 6)
+    Ht = np.array(H)
+    Ht[np.arange(200, 210), np.arange(200, 210)] = H[200, 200]  # a run of equal entries
+    X, v, rep = api.block_solve_dense(np.asfortranarray(Ht), 6, prec)
+    assert rep["converged"] == 1
+    check_pairs(Ht, X, v, 6)
+
+
+def test_trace_marks(cuda):
+    """Phase marks of a dense mixed solve: every phase present, the GPU
+    timestamps in stream order, no marks once tracing is off."""
+    import torch
+    H, _ = workloads.dense_config1(1024, seed=5)
+    dev = torch.device("cuda", 0)
+    dH = torch.from_numpy(np.asfortranarray(H).T.copy()).to(dev)
+    dX = torch.empty((16, 1024), dtype=torch.float64, device=dev)
+    dv = torch.empty(16, dtype=torch.float64, device=dev)
+    api.trace_enable(True)
+    rep = api.block_solve_dense_device(dH.data_ptr(), 1024, 16, dX.data_ptr(), dv.data_ptr(),
+                                       "fp16")
+    torch.cuda.synchronize()
+    marks = api.trace_read()
+    api.trace_enable(False)
+    assert rep["converged"] == 1
+    labels = [m[0] for m in marks]
+    for want in ("dense:start", "dense:stats_done", "dense:operator_done", "ipt:start",
+                 "refine:start", "refine:defect", "refine:rayleigh_ritz", "refine:end",
+                 "dense:end"):
+        assert want in labels, (want, labels)
+    assert labels[0] == "dense:start" and labels[-1] == "dense:end"
+    gpu = np.array([m[2] for m in marks], dtype=np.int64)
+    host = np.array([m[1] for m in marks], dtype=np.int64)
+    assert np.all(np.diff(gpu) >= 0) and np.all(np.diff(host) >= 0)
+    api.block_solve_dense_device(dH.data_ptr(), 1024, 16, dX.data_ptr(), dv.data_ptr(), "fp16")
+    assert api.trace_read() == []
