@@ -13,6 +13,7 @@
 
 #include "block_solver.h"
 #include "common.cuh"
+#include "fpconv.cuh"
 #include "ipt_plain.h"
 #include "lowp.h"
 #include "prep.h"
@@ -192,7 +193,8 @@ IptStage *make_fp64_csr_stage(const int *row_ptr, const int *col_ind, const doub
 
 // ---------------------------------------------------------------------------
 // Statistics of a dense symmetric H from one streaming pass: the diagonal,
-// the largest row sum of |H| (hnorm; a column sum, H being symmetric), the
+// the largest row sum of |H| (hnorm; a column sum, H being symmetric, in
+// double-float arithmetic on the FP32 pipe, about 1e-14 relative), the
 // largest off-diagonal |H_il| (the low-precision copy's scale) and the number
 // of descents d_{i+1} < d_i (zero: the diagonal is already ascending and no
 // permutation is needed).  One warp per column reads the contiguous column;
@@ -206,6 +208,37 @@ struct DenseStats {
 
 constexpr int kStatsWarps = 8;
 
+// One entry of the statistics: |h| added to the double-float column sum
+// (S, C) on the FP32 pipe (|h| = |hi| + sgn(hi) lo exactly, hi/lo from the
+// integer-pipe split), |h| bits into the off-diagonal maximum (non-negative
+// doubles order like their bit patterns).
+__device__ __forceinline__ void stats_entry(double h, bool offdiag, float &S, float &C,
+                                            unsigned long long &mbits)
+{
+    const unsigned long long b = (unsigned long long)__double_as_longlong(h);
+    uint32_t hb, lb;
+    float hi, lo;
+    if (split_double_bits(b, &hb, &lb)) {
+        hi = __uint_as_float(hb);
+        lo = __uint_as_float(lb);
+    } else {
+        hi = __double2float_rn(h);
+        lo = __double2float_rn(h - (double)hi);
+    }
+    const float a = fabsf(hi);
+    const float bl = hi < 0.0f ? -lo : lo;
+    const float t = __fadd_rn(S, a);
+    const float bp = __fsub_rn(t, S);
+    const float err = __fadd_rn(__fsub_rn(S, __fsub_rn(t, bp)), __fsub_rn(a, bp));
+    S = t;
+    C = __fadd_rn(C, __fadd_rn(err, bl));
+    const unsigned long long ab = b & 0x7FFFFFFFFFFFFFFFULL;
+    if (offdiag && ab > mbits) mbits = ab;
+}
+
+// kSums false: no column sums (the low-precision operator's conversion pass
+// forms them), only integer work per entry, so the pass runs at HBM speed.
+template <bool kSums>
 __global__ void __launch_bounds__(32 * kStatsWarps)
     dense_stats_kernel(const double *__restrict__ H, int n, bool vec, double *__restrict__ d,
                        DenseStats *__restrict__ stats)
@@ -214,7 +247,8 @@ __global__ void __launch_bounds__(32 * kStatsWarps)
     const int c = blockIdx.x * kStatsWarps + (threadIdx.x >> 5);
     if (c >= n) return;  // whole warps leave together
     const double *col = H + (size_t)c * n;
-    double s = 0.0, m = 0.0;
+    float S = 0.0f, C = 0.0f;
+    unsigned long long mbits = 0;
     if (vec) {  // n even and H 16-byte aligned: every column starts 16-byte aligned
         const double2 *col2 = reinterpret_cast<const double2 *>(col);
         const int half = n / 2;
@@ -222,22 +256,40 @@ __global__ void __launch_bounds__(32 * kStatsWarps)
         for (int q = lane; q < half; q += 32) {
             const double2 v = col2[q];
             const int l = 2 * q;
-            const double a0 = fabs(v.x), a1 = fabs(v.y);
-            s += a0 + a1;
-            m = fmax(m, l == c ? 0.0 : a0);
-            m = fmax(m, l + 1 == c ? 0.0 : a1);
+            if (kSums) {
+                stats_entry(v.x, l != c, S, C, mbits);
+                stats_entry(v.y, l + 1 != c, S, C, mbits);
+            } else {
+                const unsigned long long a0 =
+                    (unsigned long long)__double_as_longlong(v.x) & 0x7FFFFFFFFFFFFFFFULL;
+                const unsigned long long a1 =
+                    (unsigned long long)__double_as_longlong(v.y) & 0x7FFFFFFFFFFFFFFFULL;
+                if (l != c && a0 > mbits) mbits = a0;
+                if (l + 1 != c && a1 > mbits) mbits = a1;
+            }
         }
     } else {
 #pragma unroll 4
         for (int l = lane; l < n; l += 32) {
-            const double a = fabs(col[l]);
-            s += a;
-            m = fmax(m, l == c ? 0.0 : a);
+            if (kSums) {
+                stats_entry(col[l], l != c, S, C, mbits);
+            } else {
+                const unsigned long long a =
+                    (unsigned long long)__double_as_longlong(col[l]) & 0x7FFFFFFFFFFFFFFFULL;
+                if (l != c && a > mbits) mbits = a;
+            }
         }
     }
     for (int off = 16; off > 0; off >>= 1) {
-        s += __shfl_xor_sync(0xffffffffu, s, off);
-        m = fmax(m, __shfl_xor_sync(0xffffffffu, m, off));
+        const float So = __shfl_xor_sync(0xffffffffu, S, off);
+        const float Co = __shfl_xor_sync(0xffffffffu, C, off);
+        const float t = __fadd_rn(S, So);
+        const float bp = __fsub_rn(t, S);
+        const float err = __fadd_rn(__fsub_rn(S, __fsub_rn(t, bp)), __fsub_rn(So, bp));
+        S = t;
+        C = __fadd_rn(__fadd_rn(C, Co), err);
+        const unsigned long long mo = __shfl_xor_sync(0xffffffffu, mbits, off);
+        if (mo > mbits) mbits = mo;
     }
     if (lane == 0) {
         const size_t dstride = (size_t)n + 1;
@@ -246,21 +298,59 @@ __global__ void __launch_bounds__(32 * kStatsWarps)
         if (c + 1 < n && H[(size_t)(c + 1) * dstride] < dc) {
             atomicAdd(&stats->descents, 1ULL);
         }
-        if (s > 0.0) atomicMax(&stats->hnorm_bits, (unsigned long long)__double_as_longlong(s));
-        if (m > 0.0) atomicMax(&stats->maxabs_bits, (unsigned long long)__double_as_longlong(m));
+        const double sum = (double)S + (double)C;
+        if (kSums && sum > 0.0) {
+            atomicMax(&stats->hnorm_bits, (unsigned long long)__double_as_longlong(sum));
+        }
+        if (mbits > 0) atomicMax(&stats->maxabs_bits, mbits);
     }
 }
 
+// hnorm from the conversion pass's partial column sums [chunk][column]:
+// chunks summed in a fixed order, the maximum over columns.
+__global__ void colsum_finish_kernel(const double *__restrict__ part, int chunks, int n,
+                                     unsigned long long *__restrict__ hnorm_bits)
+{
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    double sum = 0.0;
+    if (c < n) {
+        for (int q = 0; q < chunks; ++q) sum += part[(size_t)q * n + c];
+    }
+    for (int off = 16; off > 0; off >>= 1) sum = fmax(sum, __shfl_xor_sync(0xffffffffu, sum, off));
+    if ((threadIdx.x & 31) == 0 && sum > 0.0) {
+        atomicMax(hnorm_bits, (unsigned long long)__double_as_longlong(sum));
+    }
+}
+
+int dense_hnorm_from_colsums(const double *part, int chunks, int n, cudaStream_t s, double *hnorm)
+{
+    DeviceBuffer<unsigned long long> bits;
+    IPTGB_CHECK(bits.alloc(1, s));
+    IPTGB_CUDA(cudaMemsetAsync(bits.ptr, 0, sizeof(unsigned long long), s));
+    colsum_finish_kernel<<<blocks_for(n), kThreads, 0, s>>>(part, chunks, n, bits.ptr);
+    IPTGB_LAUNCH();
+    unsigned long long h = 0;
+    IPTGB_CUDA(cudaMemcpyAsync(&h, bits.ptr, sizeof(h), cudaMemcpyDeviceToHost, s));
+    IPTGB_CUDA(cudaStreamSynchronize(s));
+    memcpy(hnorm, &h, sizeof(double));
+    return IPT_CUDA_SUCCESS;
+}
+
 // Diagonal and statistics of H on the stream; returns after the host has them.
+// with_sums false leaves *hnorm at 0.
 int dense_stats(const double *dH, int n, double *d, cudaStream_t s, double *hnorm,
-                double *maxabs_off, unsigned long long *descents)
+                double *maxabs_off, unsigned long long *descents, bool with_sums = true)
 {
     DeviceBuffer<DenseStats> st;
     IPTGB_CHECK(st.alloc(1, s));
     IPTGB_CUDA(cudaMemsetAsync(st.ptr, 0, sizeof(DenseStats), s));
     const bool vec = (n % 2 == 0) && ((reinterpret_cast<uintptr_t>(dH) & 15) == 0);
-    dense_stats_kernel<<<(n + kStatsWarps - 1) / kStatsWarps, 32 * kStatsWarps, 0, s>>>(
-        dH, n, vec, d, st.ptr);
+    const int grid = (n + kStatsWarps - 1) / kStatsWarps;
+    if (with_sums) {
+        dense_stats_kernel<true><<<grid, 32 * kStatsWarps, 0, s>>>(dH, n, vec, d, st.ptr);
+    } else {
+        dense_stats_kernel<false><<<grid, 32 * kStatsWarps, 0, s>>>(dH, n, vec, d, st.ptr);
+    }
     IPTGB_LAUNCH();
     DenseStats h;
     IPTGB_CUDA(cudaMemcpyAsync(&h, st.ptr, sizeof(h), cudaMemcpyDeviceToHost, s));
@@ -348,10 +438,13 @@ int dense_block_device(const double *dH_in, int n, int k, const IPTBlockOptions 
     DeviceBuffer<int> dperm;
     trace_mark("dense:start", s);
     IPTGB_CHECK(d.alloc((size_t)n, s));
-    // one pass: diagonal, hnorm, max off-diagonal, sortedness of the diagonal
+    // one pass: diagonal, max off-diagonal, sortedness of the diagonal, and
+    // (plain FP64 solve) hnorm; the mixed solve's conversion pass forms the
+    // column sums for hnorm itself
+    const bool lowp_mode = opt.ipt_precision != IPT_BLOCK_FP64;
     double hnorm = 0.0, maxabs_off = 0.0;
     unsigned long long descents = 0;
-    IPTGB_CHECK(dense_stats(dH_in, n, d.ptr, s, &hnorm, &maxabs_off, &descents));
+    IPTGB_CHECK(dense_stats(dH_in, n, d.ptr, s, &hnorm, &maxabs_off, &descents, !lowp_mode));
     trace_mark("dense:stats_done", s);
     const double *dH = dH_in;
     const bool permuted = descents > 0;
@@ -387,7 +480,6 @@ int dense_block_device(const double *dH_in, int n, int k, const IPTBlockOptions 
     std::unique_ptr<IptStage> stage;
     std::unique_ptr<LowpDenseOperator> lowp;
     int st = IPT_CUDA_SUCCESS;
-    const bool lowp_mode = opt.ipt_precision != IPT_BLOCK_FP64;
     // The mixed-precision solve forms its FP64-accurate products in
     // double-FP32 arithmetic (one split of H per solve); the plain FP64
     // path keeps FP64 FMAs throughout.
@@ -402,16 +494,30 @@ int dense_block_device(const double *dH_in, int n, int k, const IPTBlockOptions 
         const int kind = opt.ipt_precision == IPT_BLOCK_FP16 ? kLowpF16
                          : opt.ipt_precision == IPT_BLOCK_BF16 ? kLowpBF16
                                                                : kLowpTF32;
-        // one pass over H writes the low-precision Delta and the double-FP32 split
-        bool split_done = false;
-        lowp.reset(make_lowp_dense_operator(dH, n, kind, s, &st, maxabs_off,
-                                            Hsplit.ptr, Hsplit.ptr ? Hsplit.ptr + mat : nullptr,
-                                            &split_done, true));
+        // one pass over H writes the low-precision Delta, the double-FP32
+        // split and the partial column sums of |H|
+        DeviceBuffer<double> colpart;
+        const int chunks = (n + kLowpColsumChunk - 1) / kLowpColsumChunk + 1;
+        IPTGB_CHECK(colpart.alloc((size_t)chunks * n, s));
+        LowpDenseSetup su;
+        su.maxabs = maxabs_off;
+        su.symmetric = true;
+        su.split_hi = Hsplit.ptr;
+        su.split_lo = Hsplit.ptr ? Hsplit.ptr + mat : nullptr;
+        su.colsum_part = colpart.ptr;
+        lowp.reset(make_lowp_dense_operator(dH, n, kind, s, &st, &su));
         if (lowp == nullptr) {
             return st != IPT_CUDA_SUCCESS ? st : IPT_CUDA_INVALID_ARGUMENT;
         }
-        if (Hsplit.ptr != nullptr && !split_done) {
+        if (Hsplit.ptr != nullptr && !su.split_done) {
             IPTGB_CHECK(launch_df_split(dH, mat, Hsplit.ptr, Hsplit.ptr + mat, s));
+        }
+        if (su.colsum_chunks > 0 && su.colsum_chunks <= chunks) {
+            IPTGB_CHECK(dense_hnorm_from_colsums(colpart.ptr, su.colsum_chunks, n, s, &hnorm));
+        } else {
+            double m2 = 0.0;
+            unsigned long long d2 = 0;
+            IPTGB_CHECK(dense_stats(dH, n, d.ptr, s, &hnorm, &m2, &d2, true));
         }
         trace_mark("dense:operator_done", s);
         stage.reset(make_lowp_stage_on(lowp.get(), d.ptr, n, s));

@@ -12,7 +12,10 @@
 // (Knuth), ~12 FP32 operations per term.  The result carries ~48 bits, far
 // below the 1e-8 eigen-residual the products certify; the split-K layout
 // and the FP64 partial sums are those of the FP64 kernel (k_dense64.cu).
+#include <string.h>
+
 #include "common.cuh"
+#include "fpconv.cuh"
 #include "kernels.cuh"
 
 namespace iptgb {
@@ -27,9 +30,15 @@ __global__ void df_split_kernel(const double *__restrict__ A, size_t count,
     const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= count) return;
     const double a = A[e];
-    const float h = __double2float_rn(a);
-    hi[e] = h;
-    lo[e] = __double2float_rn(a - (double)h);
+    uint32_t hb, lb;
+    if (split_double_bits((unsigned long long)__double_as_longlong(a), &hb, &lb)) {
+        hi[e] = __uint_as_float(hb);
+        lo[e] = __uint_as_float(lb);
+    } else {
+        const float h = __double2float_rn(a);
+        hi[e] = h;
+        lo[e] = __double2float_rn(a - (double)h);
+    }
 }
 
 __device__ __forceinline__ void df_term(float &S, float &s, float hh, float hl, float xh, float xl)
@@ -142,3 +151,40 @@ int launch_df64_partial(const float *Hh, const float *Hl, int n, long long ldh, 
 }
 
 }  // namespace iptgb
+
+#define IPT_API extern "C" __attribute__((visibility("default")))
+
+// hi = RN_float(a), lo = RN_float(a - hi) for `count` doubles on the device
+// (the double-FP32 operands of the FP64-accurate products).
+IPT_API int ipt_block_split_double(const double *d_in, long long count, float *d_hi, float *d_lo,
+                                   void *stream)
+{
+    if (count < 0 || (count > 0 && (d_in == nullptr || d_hi == nullptr || d_lo == nullptr))) {
+        return IPT_CUDA_INVALID_ARGUMENT;
+    }
+    if (count == 0) return IPT_CUDA_SUCCESS;
+    return iptgb::launch_df_split(d_in, (size_t)count, d_hi, d_lo, (cudaStream_t)stream);
+}
+
+// The same split on the host, through the same integer-pipe helper (the
+// device kernels' conversion restated for checking on machines without a GPU).
+IPT_API int ipt_block_split_double_host(const double *in, long long count, float *hi, float *lo)
+{
+    if (count < 0 || (count > 0 && (in == nullptr || hi == nullptr || lo == nullptr))) {
+        return IPT_CUDA_INVALID_ARGUMENT;
+    }
+    for (long long e = 0; e < count; ++e) {
+        uint64_t b;
+        memcpy(&b, &in[e], sizeof(b));
+        uint32_t hb, lb;
+        if (iptgb::split_double_bits(b, &hb, &lb)) {
+            memcpy(&hi[e], &hb, sizeof(float));
+            memcpy(&lo[e], &lb, sizeof(float));
+        } else {
+            const float h = (float)in[e];
+            hi[e] = h;
+            lo[e] = (float)(in[e] - (double)h);
+        }
+    }
+    return IPT_CUDA_SUCCESS;
+}

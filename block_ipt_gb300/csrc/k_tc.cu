@@ -31,6 +31,7 @@
 
 #include "block_solver.h"
 #include "common.cuh"
+#include "fpconv.cuh"
 #include "lowp.h"
 #include "reduce.cuh"
 
@@ -95,6 +96,29 @@ __device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap *map
         " [%0], [%1, {%2, %3}], [%4];" ::"r"(dst),
         "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(bar)
         : "memory");
+}
+
+// The same load with an L2 cache policy (createpolicy) attached.
+__device__ __forceinline__ void tma_load_2d_hint(uint32_t dst, const CUtensorMap *map, int x,
+                                                 int y, uint32_t bar, uint64_t policy)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes"
+        ".L2::cache_hint [%0], [%1, {%2, %3}], [%4], %5;" ::"r"(dst),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(bar), "l"(policy)
+        : "memory");
+}
+
+// A fraction of the addresses an access touches gets L2 priority evict_last,
+// the rest evict_first: repeated passes over a matrix somewhat larger than L2
+// keep that fraction resident instead of thrashing the whole cache.
+__device__ __forceinline__ uint64_t l2_keep_policy(float fraction)
+{
+    uint64_t pol;
+    asm volatile("createpolicy.fractional.L2::evict_last.L2::evict_first.b64 %0, %1;"
+                 : "=l"(pol)
+                 : "f"(fraction));
+    return pol;
 }
 
 // Shared-memory matrix descriptor: K-major operand, 128-byte swizzle, rows of
@@ -169,7 +193,7 @@ __global__ void __launch_bounds__(kThreads, 1)
 tc_partial_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                   int n, int p, int p_pad, int stages, int tmem_cols, int chunks_total,
                   int chunks_per_split, int kchunk_elems, uint32_t idesc, float *__restrict__ P,
-                  int *err)
+                  int *err, float a_keep)
 {
     extern __shared__ uint8_t smem_raw[];
     // 1024-byte alignment of the shared-window address (SWIZZLE_128B atoms)
@@ -219,6 +243,7 @@ tc_partial_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
     const uint32_t tmem = *tmem_slot;
 
     if (warp == 0 && lane == 0) {
+        const uint64_t a_pol = a_keep > 0.0f ? l2_keep_policy(fminf(a_keep, 1.0f)) : 0ull;
         // ---- TMA producer ----
         int i = 0;
         for (; i < nchunks; ++i) {
@@ -235,7 +260,11 @@ tc_partial_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
             const uint32_t sb = sa + a_bytes;
             const int kx = (c0 + i) * kchunk_elems;
             mbar_expect_tx(full_bar(s), stage_bytes);
-            tma_load_2d(sa, &tmA, kx, rb * kBM, full_bar(s));
+            if (a_keep > 0.0f) {
+                tma_load_2d_hint(sa, &tmA, kx, rb * kBM, full_bar(s), a_pol);
+            } else {
+                tma_load_2d(sa, &tmA, kx, rb * kBM, full_bar(s));
+            }
             tma_load_2d(sb, &tmB, kx, 0, full_bar(s));
         }
         issued_count = i;
@@ -384,20 +413,63 @@ __global__ void convert_delta_kernel(const double *__restrict__ H, int n, int ld
 // Delta rows and (with hi/lo) the split in H's own layout.  One CTA covers
 // 2048 entries of one column; each thread two adjacent entries per step
 // (double2 loads when vec: n even and H 16-byte aligned).
-constexpr int kSymChunk = 2048;
+constexpr int kSymChunk = kLowpColsumChunk;
 template <typename LP>
 struct alignas(2 * sizeof(LP)) LpPair {  // two adjacent Delta entries, one store
     LP x, y;
 };
+// One entry: (hi, lo) from the integer-pipe split, and the Delta value
+// RN_float(2^s2 h) = 2^s2 hi when both are normal floats (s2 is the exponent
+// of the power-of-two scale).
+__device__ __forceinline__ float sym_entry(double h, int s2, double scale, float &hi, float &lo)
+{
+    uint32_t hb, lb;
+    if (split_double_bits((unsigned long long)__double_as_longlong(h), &hb, &lb)) {
+        hi = __uint_as_float(hb);
+        lo = __uint_as_float(lb);
+        const int ex = (int)((hb >> 23) & 0xFFu) + s2;
+        if (ex >= 1 && ex <= 254) {
+            return __uint_as_float(hb + ((uint32_t)s2 << 23));
+        }
+    } else {
+        hi = __double2float_rn(h);
+        lo = __double2float_rn(h - (double)hi);
+    }
+    return (float)(scale * h);
+}
+
+// |h| = |hi| + sgn(hi) lo added to a double-float sum (S, C) on the FP32 pipe
+__device__ __forceinline__ void df_abs_add(float &S, float &C, float hi, float lo)
+{
+    const float a = fabsf(hi);
+    const float bl = hi < 0.0f ? -lo : lo;
+    const float t = __fadd_rn(S, a);
+    const float bp = __fsub_rn(t, S);
+    const float err = __fadd_rn(__fsub_rn(S, __fsub_rn(t, bp)), __fsub_rn(a, bp));
+    S = t;
+    C = __fadd_rn(C, __fadd_rn(err, bl));
+}
+
+// (S, C) += (So, Co) for double-float pairs
+__device__ __forceinline__ void df_pair_add(float &S, float &C, float So, float Co)
+{
+    const float t = __fadd_rn(S, So);
+    const float bp = __fsub_rn(t, S);
+    const float err = __fadd_rn(__fsub_rn(S, __fsub_rn(t, bp)), __fsub_rn(So, bp));
+    S = t;
+    C = __fadd_rn(__fadd_rn(C, Co), err);
+}
+
 template <typename LP>
 __global__ void __launch_bounds__(256)
-    convert_delta_sym_kernel(const double *__restrict__ H, int n, int ldp, double scale, bool vec,
-                             LP *__restrict__ out, float *__restrict__ hi,
-                             float *__restrict__ lo)
+    convert_delta_sym_kernel(const double *__restrict__ H, int n, int ldp, double scale, int s2,
+                             bool vec, LP *__restrict__ out, float *__restrict__ hi,
+                             float *__restrict__ lo, double *__restrict__ colpart)
 {
     const int c = blockIdx.x;  // column of H = row of Delta
     const size_t col = (size_t)c * n;
     LP *orow = out + (size_t)c * ldp;
+    float S = 0.0f, C = 0.0f;  // this thread's share of the column sum of |H|
 #pragma unroll
     for (int u = 0; u < kSymChunk / 512; ++u) {
         const int l = blockIdx.y * kSymChunk + u * 512 + 2 * threadIdx.x;  // even
@@ -411,13 +483,17 @@ __global__ void __launch_bounds__(256)
             if (l < n) h0 = H[col + l];
             if (l + 1 < n) h1 = H[col + l + 1];
         }
-        const float v0 = (l < n && l != c) ? (float)(scale * h0) : 0.0f;
-        const float v1 = (l + 1 < n && l + 1 != c) ? (float)(scale * h1) : 0.0f;
+        float a0, a1, b0, b1;
+        float v0 = sym_entry(h0, s2, scale, a0, b0);
+        float v1 = sym_entry(h1, s2, scale, a1, b1);
+        if (!(l < n && l != c)) v0 = 0.0f;
+        if (!(l + 1 < n && l + 1 != c)) v1 = 0.0f;
+        if (colpart != nullptr) {
+            df_abs_add(S, C, a0, b0);  // entries beyond n are zero
+            df_abs_add(S, C, a1, b1);
+        }
         *reinterpret_cast<LpPair<LP> *>(orow + l) = LpPair<LP>{to_lp<LP>(v0), to_lp<LP>(v1)};
         if (hi != nullptr) {
-            const float a0 = __double2float_rn(h0), a1 = __double2float_rn(h1);
-            const float b0 = __double2float_rn(h0 - (double)a0);
-            const float b1 = __double2float_rn(h1 - (double)a1);
             if (vec && l + 1 < n) {
                 *reinterpret_cast<float2 *>(hi + col + l) = make_float2(a0, a1);
                 *reinterpret_cast<float2 *>(lo + col + l) = make_float2(b0, b1);
@@ -431,6 +507,25 @@ __global__ void __launch_bounds__(256)
                     lo[col + l + 1] = b1;
                 }
             }
+        }
+    }
+    if (colpart != nullptr) {
+        // fixed-order reduction: lanes, then the 8 warps
+        for (int off = 16; off > 0; off >>= 1) {
+            df_pair_add(S, C, __shfl_xor_sync(0xffffffffu, S, off),
+                        __shfl_xor_sync(0xffffffffu, C, off));
+        }
+        __shared__ float red[2][8];
+        const int w = threadIdx.x >> 5;
+        if ((threadIdx.x & 31) == 0) {
+            red[0][w] = S;
+            red[1][w] = C;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            float St = red[0][0], Ct = red[1][0];
+            for (int q = 1; q < 8; ++q) df_pair_add(St, Ct, red[0][q], red[1][q]);
+            colpart[(size_t)blockIdx.y * n + c] = (double)St + (double)Ct;
         }
     }
 }
@@ -701,9 +796,14 @@ struct LowpDense final : LowpDenseOperator {
     static constexpr int esize = (int)sizeof(LP);
     static constexpr int kchunk = 128 / esize;
 
-    int init(const double *dH, int n_, cudaStream_t s_, double maxabs_hint = -1.0,
-             float *split_hi = nullptr, float *split_lo = nullptr, bool symmetric = false)
+    int init(const double *dH, int n_, cudaStream_t s_, LowpDenseSetup *setup = nullptr)
     {
+        LowpDenseSetup none;
+        LowpDenseSetup &su = setup != nullptr ? *setup : none;
+        const bool symmetric = su.symmetric;
+        float *split_hi = symmetric ? su.split_hi : nullptr;
+        float *split_lo = symmetric ? su.split_lo : nullptr;
+        if (split_hi == nullptr || split_lo == nullptr) split_hi = split_lo = nullptr;
         n = n_;
         s = s_;
         sms = 148;
@@ -712,7 +812,7 @@ struct LowpDense final : LowpDenseOperator {
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         ldp = ((n + 63) / 64) * 64;
         IPTGB_CHECK(delta.alloc((size_t)n * ldp, s));
-        double maxabs = maxabs_hint;
+        double maxabs = su.maxabs;
         if (!(maxabs >= 0.0)) {
             DeviceBuffer<unsigned long long> mx;
             IPTGB_CHECK(mx.alloc(1, s));
@@ -726,10 +826,12 @@ struct LowpDense final : LowpDenseOperator {
             memcpy(&maxabs, &bits, sizeof(maxabs));
         }
         scale = 1.0;
+        int s2 = 0;
         if (LowpTypes<LP>::kind == kLowpF16 && maxabs > 0.0 && isfinite(maxabs)) {
             // largest power of two with maxabs * scale <= 16384 (FP16 max 65504)
-            scale = ldexp(1.0, (int)floor(log2(16384.0 / maxabs)));
-            scale = std::min(std::max(scale, ldexp(1.0, -40)), ldexp(1.0, 40));
+            s2 = (int)floor(log2(16384.0 / maxabs));
+            s2 = std::min(std::max(s2, -40), 40);
+            scale = ldexp(1.0, s2);
         }
         if (symmetric) {
             // vec also needs hi/lo 8-byte aligned at even offsets (pool allocations are)
@@ -737,15 +839,33 @@ struct LowpDense final : LowpDenseOperator {
                              ((reinterpret_cast<uintptr_t>(split_hi) & 7) == 0) &&
                              ((reinterpret_cast<uintptr_t>(split_lo) & 7) == 0);
             dim3 grid(n, (ldp + kSymChunk - 1) / kSymChunk);
-            convert_delta_sym_kernel<LP><<<grid, 256, 0, s>>>(dH, n, ldp, scale, vec, delta.ptr,
-                                                              split_hi, split_lo);
+            convert_delta_sym_kernel<LP><<<grid, 256, 0, s>>>(dH, n, ldp, scale, s2, vec,
+                                                              delta.ptr, split_hi, split_lo,
+                                                              su.colsum_part);
+            su.split_done = split_hi != nullptr;
+            su.colsum_chunks = su.colsum_part != nullptr ? (int)grid.y : 0;
         } else {
             dim3 grid((ldp + 31) / 32, (n + 31) / 32);
             convert_delta_kernel<LP><<<grid, dim3(32, 8), 0, s>>>(dH, n, ldp, scale, delta.ptr,
-                                                                  split_hi, split_lo);
+                                                                  nullptr, nullptr);
         }
         IPTGB_LAUNCH();
         IPTGB_CHECK(make_map(&mapA, LowpTypes<LP>::dt, esize, delta.ptr, ldp, n, tc::kBM));
+        // Delta is streamed once per product; when it is larger than about
+        // half of L2, that share of it is marked evict_last so that it stays
+        // resident across the products (the rest evict_first).  Measured at
+        // n = 8192 (FP16 Delta 134 MB): keeping 40-55% of Delta gives the
+        // fastest solve; more than 60% thrashes again.
+        {
+            int l2 = 0;
+            cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, dev);
+            const double bytes = (double)n * (double)ldp * esize;
+            const double keep_bytes = 0.45 * (double)l2;
+            a_keep = bytes > keep_bytes && l2 > 0 ? (float)(keep_bytes / bytes) : 0.0f;
+            // tuning knob: IPT_GB300_L2_KEEP_PCT overrides the fraction (0 = no hint)
+            const int pct = env_int("IPT_GB300_L2_KEEP_PCT", -1);
+            if (pct >= 0) a_keep = std::min(pct, 100) / 100.0f;
+        }
         IPTGB_CHECK(err.alloc(1, s));
         IPTGB_CUDA(cudaMemsetAsync(err.ptr, 0, sizeof(int), s));
         return IPT_CUDA_SUCCESS;
@@ -824,7 +944,7 @@ struct LowpDense final : LowpDenseOperator {
         KernelTimerScope timer(kProfLowpProduct, s);
         tc::tc_partial_kernel<LowpTypes<LP>::kind><<<grid, tc::kThreads, smem_bytes, s>>>(
             mapA, mapB[cur], n, p, p_pad, stages, tmem_cols, chunks_total, chunks_per_split,
-            kchunk, idesc, P.ptr, err.ptr);
+            kchunk, idesc, P.ptr, err.ptr, a_keep);
         IPTGB_LAUNCH();
         return IPT_CUDA_SUCCESS;
     }
@@ -921,6 +1041,7 @@ struct LowpDense final : LowpDenseOperator {
     size_t smem_bytes = 0;
     uint32_t idesc = 0;
     double scale = 1.0;
+    float a_keep = 0.0f;  // fraction of Delta kept in L2 (evict_last) across products
     cudaStream_t s = nullptr;
     DeviceBuffer<LP> delta;
     DeviceBuffer<LP> Xlp[2];
@@ -1077,10 +1198,12 @@ struct LowpDenseSimtF32 final : LowpDenseOperator {
 };
 
 LowpDenseOperator *make_lowp_dense_operator(const double *dH, int n, int kind, cudaStream_t s,
-                                            int *status, double maxabs_hint, float *split_hi,
-                                            float *split_lo, bool *split_done, bool symmetric)
+                                            int *status, LowpDenseSetup *setup)
 {
-    if (split_done != nullptr) *split_done = false;
+    if (setup != nullptr) {
+        setup->split_done = false;
+        setup->colsum_chunks = 0;
+    }
     int dev = 0, major = 0, minor = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev);
@@ -1095,18 +1218,15 @@ LowpDenseOperator *make_lowp_dense_operator(const double *dH, int n, int kind, c
     if (kind == kLowpF16) {
         auto *o = new LowpDense<__half>();
         op.reset(o);
-        st = o->init(dH, n, s, maxabs_hint, split_hi, split_lo, symmetric);
-        if (split_done != nullptr) *split_done = split_hi != nullptr && split_lo != nullptr;
+        st = o->init(dH, n, s, setup);
     } else if (kind == kLowpBF16) {
         auto *o = new LowpDense<__nv_bfloat16>();
         op.reset(o);
-        st = o->init(dH, n, s, maxabs_hint, split_hi, split_lo, symmetric);
-        if (split_done != nullptr) *split_done = split_hi != nullptr && split_lo != nullptr;
+        st = o->init(dH, n, s, setup);
     } else if (kind == kLowpTF32) {
         auto *o = new LowpDense<tf32_t>();
         op.reset(o);
-        st = o->init(dH, n, s, maxabs_hint, split_hi, split_lo, symmetric);
-        if (split_done != nullptr) *split_done = split_hi != nullptr && split_lo != nullptr;
+        st = o->init(dH, n, s, setup);
     } else if (kind == kLowpF32) {
         auto *o = new LowpDenseSimtF32();
         op.reset(o);

@@ -40,15 +40,20 @@ struct LowpDenseOperator {
     virtual int refine_apply(double *X) = 0;  // X += delta (FP64)
 };
 
-// maxabs_hint >= 0: max |H_il| (l != i) is already known (skips a pass over
-// H); split_hi/lo non-null: the conversion pass also writes the double-FP32
-// split of H (hi = float(h), lo = float(h - hi), column-major) and sets
-// *split_done; symmetric: H is exactly symmetric, so the conversion streams
-// columns of H as rows of Delta without a transpose.
+// Optional inputs and outputs of the operator's one pass over H.
+struct LowpDenseSetup {
+    double maxabs = -1.0;           // >= 0: max |H_il| (l != i) is known (no extra pass)
+    bool symmetric = false;         // H exactly symmetric: columns of H stream as rows of Delta
+    float *split_hi = nullptr;      // symmetric only: the pass also writes the double-FP32
+    float *split_lo = nullptr;      //   split of H (column-major)
+    double *colsum_part = nullptr;  // symmetric only: partial column sums of |H|,
+                                    //   [chunk][column], chunk = 2048 rows
+    int colsum_chunks = 0;          // out: chunks written to colsum_part
+    bool split_done = false;        // out: split_hi/lo written
+};
+constexpr int kLowpColsumChunk = 2048;
 LowpDenseOperator *make_lowp_dense_operator(const double *dH, int n, int kind, cudaStream_t s,
-                                            int *status, double maxabs_hint = -1.0,
-                                            float *split_hi = nullptr, float *split_lo = nullptr,
-                                            bool *split_done = nullptr, bool symmetric = false);
+                                            int *status, LowpDenseSetup *setup = nullptr);
 
 int run_lowp_ipt(LowpDenseOperator &op, int n, int p, int maxiter, double tol, int check_every,
                  double *X, int *iterations, double *fpres_out, long long *matvecs,

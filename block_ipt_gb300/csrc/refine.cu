@@ -320,7 +320,9 @@ int refine_solve(const RefineInput &in, double *X_out, double *values_out, IPTBl
     IPTGB_CHECK(cholqr_pair(X.ptr, HX.ptr, Q.ptr, HQ.ptr, k <= 32 ? cond_dev : nullptr, &h_cond));
     // basis B / HB, output O / HO
     double *B = Q.ptr, *HB = HQ.ptr, *O = X.ptr, *HO = HX.ptr;
+    trace_mark("refine:cholqr1_done", s);
     if (!(h_cond <= kCholQr1Cond)) {
+        trace_mark("refine:cholqr2", s);
         IPTGB_CHECK(cholqr_pair(Q.ptr, HQ.ptr, X.ptr, HX.ptr, nullptr, nullptr));
         B = X.ptr;
         HB = HX.ptr;

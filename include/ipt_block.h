@@ -292,6 +292,18 @@ int ipt_fci_sigma(const IPTFciSpec *spec, const double *d_X, int k, double *d_Y,
 int ipt_block_solve_fci(const IPTFciSpec *spec, int k, const IPTBlockOptions *options,
                         double *d_vectors, double *d_values, IPTBlockReport *report);
 
+/* ---- double-FP32 operands ------------------------------------------------- */
+
+/* hi = RN_float(a), lo = RN_float(a - hi) elementwise (a = hi + lo to about
+ * 2^-48 relative): the operands of the FP64-accurate products that run on the
+ * FP32 pipe.  The device version converts on the integer pipe (GB300's FP64
+ * pipe, which also executes double<->float conversions, is too slow for a
+ * pass over a large matrix); results are bit-identical to the FP64
+ * conversions.  The host version runs the same conversion on the CPU. */
+int ipt_block_split_double(const double *d_in, long long count, float *d_hi, float *d_lo,
+                           void *stream);
+int ipt_block_split_double_host(const double *in, long long count, float *hi, float *lo);
+
 /* ---- instrumentation ---------------------------------------------------- */
 
 /* Number of kernels this library has launched in the calling process. */
