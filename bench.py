@@ -277,8 +277,6 @@ def fci_section(args, torch, lib, stream, flush, dev):
         return rep.as_dict()
 
     solve()
-    lib.ipt_block_profile_reset()
-    lib.ipt_block_profile_enable(1)
     times, rep = [], None
     for _ in range(max(1, args.fci_steps)):
         flush.zero_()
@@ -287,6 +285,13 @@ def fci_section(args, torch, lib, stream, flush, dev):
         e1.record(stream)
         e1.synchronize()
         times.append(e0.elapsed_time(e1))
+    # per-kernel event timings over a second, instrumented pass
+    lib.ipt_block_profile_reset()
+    lib.ipt_block_profile_enable(1)
+    for _ in range(len(times)):
+        flush.zero_()
+        solve()
+    torch.cuda.synchronize()
     lib.ipt_block_profile_enable(0)
     prof = profile_snapshot(lib)
     X = dX.T.cpu().numpy()
@@ -519,8 +524,7 @@ def run_ours(args):
     sampler = ClockSampler(local)
     sampler.start()
     time.sleep(0.3)
-    lib.ipt_block_profile_reset()
-    lib.ipt_block_profile_enable(1)
+    lib.ipt_block_profile_enable(0)
     launches0 = lib.ipt_block_launch_count()
     if world > 1:
         dist.barrier()
@@ -539,9 +543,19 @@ def run_ours(args):
         worst_res = max(worst_res, fp64_check(torch, dHsym.T, dX.T, dv, hnorm))
     torch.cuda.synchronize()
     launches = lib.ipt_block_launch_count() - launches0
+    clocks = sampler.stop()
+    # per-kernel CUDA-event timings over a second pass of the same K solves:
+    # the events around every instrumented launch cost ~0.4 ms of host time per
+    # solve, so the headline pass above runs without them
+    lib.ipt_block_profile_reset()
+    lib.ipt_block_profile_enable(1)
+    prof_reports = []
+    for _ in range(args.steps):
+        flush.zero_()
+        prof_reports.append(solve(args.precision))
+    torch.cuda.synchronize()
     lib.ipt_block_profile_enable(0)
     prof = profile_snapshot(lib)
-    clocks = sampler.stop()
     ms_mine = statistics.mean(times)
     t = torch.tensor([ms_mine], device=dev)
     if world > 1:
@@ -604,7 +618,7 @@ def run_ours(args):
     lib.ipt_block_measure_fp64_peak(C.byref(fp64_peak))
     FP64_PEAK_TFLOPS = fp64_peak.value
     if name == "fp64_product":
-        terms = n * n * (sum(r["fp64_matvecs"] for r in reports) / steps) * steps
+        terms = n * n * sum(r["fp64_matvecs"] for r in prof_reports)
         fp32_peak = C.c_double(0.0)
         lib.ipt_block_measure_fp32_peak(C.byref(fp32_peak))
         FP32_PEAK_TFLOPS = fp32_peak.value

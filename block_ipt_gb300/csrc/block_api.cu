@@ -548,8 +548,15 @@ int dense_block_device(const double *dH_in, int n, int k, const IPTBlockOptions 
         rin.max_outer = lowp_mode ? std::min(std::max(1, opt.refine_maxiter), 12)
                                   : std::max(1, opt.refine_maxiter);
         rin.inner_maxiter = std::max(1, opt.inner_maxiter);
-        rin.inner_tol = opt.inner_tol > 0.0 ? opt.inner_tol : 1e-3;
+        rin.inner_tol = opt.inner_tol > 0.0 ? opt.inner_tol : 3e-3;
         rin.opt.ipt_maxiter = opt.ipt_maxiter;
+        if (lowp_mode) {
+            // the low-precision IPT stage cannot go below about twice its
+            // unit roundoff (FP16 / TF32 2^-11, BF16 2^-8): stop there
+            // instead of iterating into stagnation
+            const double u = opt.ipt_precision == IPT_BLOCK_BF16 ? 0x1p-8 : 0x1p-11;
+            rin.opt.ipt_tol = std::max(opt.ipt_tol, 2.0 * u);
+        }
         IPTGB_CHECK(Xfb.alloc((size_t)n * k, s));
         bool conv = false;
         IPTGB_CHECK(refine_solve(rin, xout, d_values, report, s, &conv, Xfb.ptr));

@@ -44,7 +44,7 @@ void fill_default_options(IPTBlockOptions *opt)
     opt->strategy = IPT_BLOCK_STRATEGY_REFINE;
     opt->refine_maxiter = 300;
     opt->inner_maxiter = 64;
-    opt->inner_tol = 1e-3;
+    opt->inner_tol = 3e-3;
 }
 
 namespace {

@@ -54,11 +54,48 @@ int SolveScratch::init(size_t max_elems, cudaStream_t stream)
 {
     const int slots = blocks_for(max_elems);
     IPTGB_CUDA(cudaMallocAsync((void **)&ns.partials, (size_t)slots * sizeof(double2), stream));
-    IPTGB_CUDA(cudaMallocAsync((void **)&ns.counter, sizeof(unsigned int) + 2 * sizeof(double) + 8,
-                               stream));
-    ns.norms = (double *)((char *)ns.counter + 8);
+    // [counter u32 | pad][norms double x2]
+    IPTGB_CUDA(cudaMallocAsync((void **)&ns.counter, 32, stream));
+    ns.norms = (double *)((char *)ns.counter + 16);
     ns.capacity = slots;
-    IPTGB_CUDA(cudaMemsetAsync(ns.counter, 0, sizeof(unsigned int), stream));
+    IPTGB_CUDA(cudaMemsetAsync(ns.counter, 0, 16, stream));
+    return IPT_CUDA_SUCCESS;
+}
+
+int SolveScratch::arm_history(int steps, double tol, cudaStream_t stream)
+{
+    if (steps > ns.hist_cap) {
+        if (ns.hist != nullptr) cudaFreeAsync(ns.hist, stream);
+        ns.hist = nullptr;
+        ns.hist_cap = 0;
+        IPTGB_CUDA(cudaMallocAsync((void **)&ns.hist, 2 * (size_t)steps * sizeof(double), stream));
+        ns.hist_cap = steps;
+    }
+    IPTGB_CUDA(cudaMemsetAsync(ns.hist, 0, 2 * (size_t)steps * sizeof(double), stream));
+    ns.step = 0;
+    ns.stop_tol = tol;
+    return IPT_CUDA_SUCCESS;
+}
+
+int SolveScratch::read_history(int count, int *stopped_at, double *rel, cudaStream_t stream)
+{
+    host_hist.resize(2 * (size_t)count);
+    if (count > 0) {
+        IPTGB_CUDA(cudaMemcpyAsync(host_hist.data(), ns.hist, 2 * (size_t)count * sizeof(double),
+                                   cudaMemcpyDeviceToHost, stream));
+    }
+    IPTGB_CUDA(cudaStreamSynchronize(stream));
+    *stopped_at = -1;
+    *rel = NAN;
+    const double t2 = ns.stop_tol * ns.stop_tol;
+    for (int i = 0; i < count; ++i) {
+        const double d2 = host_hist[2 * (size_t)i], x2 = host_hist[2 * (size_t)i + 1];
+        *rel = sqrt(d2) / sqrt(x2);
+        if (x2 > 0.0 && d2 <= t2 * x2) {
+            *stopped_at = i;
+            break;
+        }
+    }
     return IPT_CUDA_SUCCESS;
 }
 
@@ -69,6 +106,9 @@ void SolveScratch::release(cudaStream_t stream)
     }
     if (ns.counter != nullptr) {
         cudaFreeAsync(ns.counter, stream);
+    }
+    if (ns.hist != nullptr) {
+        cudaFreeAsync(ns.hist, stream);
     }
     ns = NormScratch();
 }

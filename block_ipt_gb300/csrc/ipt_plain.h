@@ -3,6 +3,8 @@
 
 #include <cuda_runtime.h>
 
+#include <vector>
+
 #include "kernels.cuh"
 
 namespace iptgb {
@@ -40,16 +42,22 @@ struct CsrFp64Operator final : Fp64Operator {
     int diag_values(const double *X, double *values) override;
 };
 
-// Scratch owned by a solve: norm reduction slots + pinned readback.
+// Scratch owned by a solve: norm reduction slots + readback.
 struct SolveScratch {
     NormScratch ns;
-    // the 16-byte norm read-back lands in pageable memory: each read is
-    // followed by a stream synchronisation anyway, and a pinned allocation
-    // (with the device-wide synchronisation of its release) per solve cost
-    // more than it saved
+    // the read-backs land in pageable memory: each is followed by a stream
+    // synchronisation anyway, and a pinned allocation (with the device-wide
+    // synchronisation of its release) per solve cost more than it saved
     double host_norms[2] = {0.0, 0.0};
+    std::vector<double> host_hist;
     int init(size_t max_elems, cudaStream_t stream);
     void release(cudaStream_t stream);
+    // zeroed history for up to `steps` steps with the device-side stop at tol
+    int arm_history(int steps, double tol, cudaStream_t stream);
+    // the first `count` history entries: *stopped_at = first step that met
+    // the tolerance (-1: none), *rel = its ||delta||/||X|| (else the last
+    // entry's); synchronises the stream
+    int read_history(int count, int *stopped_at, double *rel, cudaStream_t stream);
 };
 
 // The reference's plain IPT loop (IPT_C_GPU/src/ipt_cuda.cu:1644-1703):

@@ -193,8 +193,10 @@ __global__ void __launch_bounds__(kThreads, 1)
 tc_partial_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                   int n, int p, int p_pad, int stages, int tmem_cols, int chunks_total,
                   int chunks_per_split, int kchunk_elems, uint32_t idesc, float *__restrict__ P,
-                  int *err, float a_keep)
+                  int *err, float a_keep, const double *hist, int step, double stop_tol)
 {
+    // the iteration already met its tolerance on the device: nothing to do
+    if (hist_stopped(hist, step, stop_tol)) return;
     extern __shared__ uint8_t smem_raw[];
     // 1024-byte alignment of the shared-window address (SWIZZLE_128B atoms)
     uint8_t *smem = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
@@ -579,6 +581,24 @@ __global__ void lowp_identity_kernel(float *X32, LP *Xlp, int n, int p, int ldx)
     Xlp[(size_t)i + (size_t)j * ldx] = to_lp<LP>(v);
 }
 
+// History of the device-side stop (NormScratch): a stopped step copies the
+// previous entry forward; a running step adds its block's sums.
+__device__ __forceinline__ void hist_carry(double *hist, int step)
+{
+    if (blockIdx.x == 0 && threadIdx.x == 0 && step > 0) {
+        hist[2 * step] = __ldcg(hist + 2 * (step - 1));
+        hist[2 * step + 1] = __ldcg(hist + 2 * (step - 1) + 1);
+    }
+}
+
+__device__ __forceinline__ void hist_add(double *hist, int step, double2 t)
+{
+    if (threadIdx.x == 0) {
+        atomicAdd(hist + 2 * step, t.x);
+        atomicAdd(hist + 2 * step + 1, t.y);
+    }
+}
+
 // Low-precision IPT update (see file header); Delta has a zero diagonal so
 // c_j = (Delta X)_jj is read straight from the product.
 template <typename LP>
@@ -586,12 +606,26 @@ __global__ void lowp_update_kernel(const float *__restrict__ P, int S, int n, in
                                    float inv_scale, const float *__restrict__ G,
                                    const float *__restrict__ X, float *__restrict__ Xn,
                                    LP *__restrict__ Xlp, int ldx, int want_norms,
-                                   double2 *partials, unsigned int *counter, double *norms)
+                                   double2 *partials, unsigned int *counter, double *norms,
+                                   double *hist, int step, double stop_tol)
 {
+    // grid-stride over the block (a few CTAs per SM)
     const size_t elems = (size_t)n * (size_t)p;
-    const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    if (hist_stopped(hist, step, stop_tol)) {
+        // stopped: pass the block through to the next buffer pair
+        for (size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x; idx < elems;
+             idx += stride) {
+            const float x = X[idx];
+            Xn[idx] = x;
+            Xlp[(idx % (size_t)n) + (idx / (size_t)n) * (size_t)ldx] = to_lp<LP>(x);
+        }
+        hist_carry(hist, step);
+        return;
+    }
+    want_norms = want_norms || hist != nullptr;
     double dsq = 0.0, xsq = 0.0;
-    if (idx < elems) {
+    for (size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x; idx < elems; idx += stride) {
         const int row = (int)(idx % (size_t)n);
         const int col = (int)(idx / (size_t)n);
         const float x = X[idx];
@@ -609,11 +643,13 @@ __global__ void lowp_update_kernel(const float *__restrict__ P, int S, int n, in
         Xlp[(size_t)row + (size_t)col * ldx] = to_lp<LP>(out);
         if (want_norms) {
             const double df = (double)out - (double)x;
-            dsq = df * df;
-            xsq = (double)x * (double)x;
+            dsq = fma(df, df, dsq);
+            xsq = fma((double)x, (double)x, xsq);
         }
     }
-    if (want_norms) {
+    if (hist != nullptr) {
+        hist_add(hist, step, block_sum2(dsq, xsq));
+    } else if (want_norms) {
         const double2 t = block_sum2(dsq, xsq);
         grid_finish_norms2(t, partials, counter, norms);
     }
@@ -662,12 +698,25 @@ __global__ void refine_update_kernel(const float *__restrict__ P, int S, int n, 
                                      const float *__restrict__ c32, const float *__restrict__ dcur,
                                      float *__restrict__ dnext, LP *__restrict__ dlp, int ldx,
                                      int want_norms, double2 *partials, unsigned int *counter,
-                                     double *norms)
+                                     double *norms, double *hist, int step, double stop_tol)
 {
     const size_t elems = (size_t)n * (size_t)p;
-    const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    if (hist_stopped(hist, step, stop_tol)) {
+        // stopped: pass the correction through to the next buffer pair
+        for (size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x; idx < elems;
+             idx += stride) {
+            const float cur = dcur[idx];
+            const int col = (int)(idx / (size_t)n);
+            dnext[idx] = cur;
+            dlp[(idx % (size_t)n) + (size_t)col * (size_t)ldx] = to_lp<LP>(cur * sig[col]);
+        }
+        hist_carry(hist, step);
+        return;
+    }
+    want_norms = want_norms || hist != nullptr;
     double dsq = 0.0, xsq = 0.0;
-    if (idx < elems) {
+    for (size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x; idx < elems; idx += stride) {
         const int row = (int)(idx % (size_t)n);
         const int col = (int)(idx / (size_t)n);
         const float cur = dcur[idx];
@@ -688,11 +737,13 @@ __global__ void refine_update_kernel(const float *__restrict__ P, int S, int n, 
         dlp[(size_t)row + (size_t)col * ldx] = to_lp<LP>(out * sig[col]);
         if (want_norms) {
             const double df = (double)out - (double)cur;
-            dsq = df * df;
-            xsq = (double)cur * (double)cur;
+            dsq = fma(df, df, dsq);
+            xsq = fma((double)cur, (double)cur, xsq);
         }
     }
-    if (want_norms) {
+    if (hist != nullptr) {
+        hist_add(hist, step, block_sum2(dsq, xsq));
+    } else if (want_norms) {
         const double2 t = block_sum2(dsq, xsq);
         grid_finish_norms2(t, partials, counter, norms);
     }
@@ -937,30 +988,40 @@ struct LowpDense final : LowpDenseOperator {
         return IPT_CUDA_SUCCESS;
     }
 
-    int product() override
+    int product() override { return product_until(nullptr, 0, 0.0); }
+
+    // hist/step/tol: the device-side stop of the running iteration (or null)
+    int product_until(const double *hist, int step, double tol)
     {
         const int row_blocks = (n + tc::kBM - 1) / tc::kBM;
         dim3 grid(row_blocks, splits);
         KernelTimerScope timer(kProfLowpProduct, s);
         tc::tc_partial_kernel<LowpTypes<LP>::kind><<<grid, tc::kThreads, smem_bytes, s>>>(
             mapA, mapB[cur], n, p, p_pad, stages, tmem_cols, chunks_total, chunks_per_split,
-            kchunk, idesc, P.ptr, err.ptr, a_keep);
+            kchunk, idesc, P.ptr, err.ptr, a_keep, hist, step, tol);
         IPTGB_LAUNCH();
         return IPT_CUDA_SUCCESS;
     }
 
     int step(int want_norms, NormScratch *ns) override
     {
-        IPTGB_CHECK(product());
+        const bool hm = ns->hist != nullptr && ns->step < ns->hist_cap;
+        double *hist = hm ? ns->hist : nullptr;
+        const int hstep = ns->step;
+        IPTGB_CHECK(product_until(hist, hstep, ns->stop_tol));
         const size_t elems = (size_t)n * p;
-        const int grid = blocks_for(elems);
+        // a few CTAs per SM, grid-stride (tuning knob: IPT_GB300_UPDATE_CTAS_PER_SM)
+        const int per_sm = env_int("IPT_GB300_UPDATE_CTAS_PER_SM", 4);
+        const int grid = per_sm > 0 ? std::min(blocks_for(elems), per_sm * sms) : blocks_for(elems);
         if (want_norms && grid > ns->capacity) return IPT_CUDA_INVALID_ARGUMENT;
         const int nxt = cur ^ 1;
         KernelTimerScope timer(kProfLowpUpdate, s);
         lowp_update_kernel<LP><<<grid, kThreads, 0, s>>>(
             P.ptr, splits, n, p, (float)(1.0 / scale), G.ptr, X32[cur].ptr, X32[nxt].ptr,
-            Xlp[nxt].ptr, ldp, want_norms, ns->partials, ns->counter, ns->norms);
+            Xlp[nxt].ptr, ldp, want_norms, ns->partials, ns->counter, ns->norms, hist, hstep,
+            ns->stop_tol);
         IPTGB_LAUNCH();
+        if (hm) ++ns->step;
         cur = nxt;
         return IPT_CUDA_SUCCESS;
     }
@@ -989,6 +1050,7 @@ struct LowpDense final : LowpDenseOperator {
 
     const float *partials() const override { return P.ptr; }
     int num_splits() const override { return splits; }
+    double streamed_bytes() const override { return (double)n * (double)ldp * esize; }
 
     int refine_begin(const double *R0, const double *X, const double *c,
                      const float *sigma) override
@@ -1009,17 +1071,23 @@ struct LowpDense final : LowpDenseOperator {
 
     int refine_step(int want_norms, NormScratch *ns) override
     {
-        IPTGB_CHECK(product());
+        const bool hm = ns->hist != nullptr && ns->step < ns->hist_cap;
+        double *hist = hm ? ns->hist : nullptr;
+        const int hstep = ns->step;
+        IPTGB_CHECK(product_until(hist, hstep, ns->stop_tol));
         const size_t elems = (size_t)n * p;
-        const int grid = blocks_for(elems);
+        // a few CTAs per SM, grid-stride (tuning knob: IPT_GB300_UPDATE_CTAS_PER_SM)
+        const int per_sm = env_int("IPT_GB300_UPDATE_CTAS_PER_SM", 4);
+        const int grid = per_sm > 0 ? std::min(blocks_for(elems), per_sm * sms) : blocks_for(elems);
         if (want_norms && grid > ns->capacity) return IPT_CUDA_INVALID_ARGUMENT;
         const int nxt = cur ^ 1;
         KernelTimerScope timer(kProfLowpUpdate, s);
         refine_update_kernel<LP><<<grid, kThreads, 0, s>>>(
             P.ptr, splits, n, p, (float)(1.0 / scale), small.ptr + p, small.ptr + 2 * p, G.ptr,
             R32.ptr, Xref32.ptr, small.ptr, X32[cur].ptr, X32[nxt].ptr, Xlp[nxt].ptr, ldp,
-            want_norms, ns->partials, ns->counter, ns->norms);
+            want_norms, ns->partials, ns->counter, ns->norms, hist, hstep, ns->stop_tol);
         IPTGB_LAUNCH();
+        if (hm) ++ns->step;
         cur = nxt;
         return IPT_CUDA_SUCCESS;
     }
@@ -1110,6 +1178,7 @@ struct LowpDenseSimtF32 final : LowpDenseOperator {
     }
     int step(int want_norms, NormScratch *ns) override
     {
+        const bool hm = ns->hist != nullptr && ns->step < ns->hist_cap;
         IPTGB_CHECK(product());
         const size_t elems = (size_t)n * p;
         const int grid = blocks_for(elems);
@@ -1118,8 +1187,10 @@ struct LowpDenseSimtF32 final : LowpDenseOperator {
         KernelTimerScope timer(kProfLowpUpdate, s);
         lowp_update_kernel<float><<<grid, kThreads, 0, s>>>(
             P.ptr, splits, n, p, 1.0f, G.ptr, X32[cur].ptr, X32[nxt].ptr, X32[nxt].ptr, n,
-            want_norms, ns->partials, ns->counter, ns->norms);
+            want_norms, ns->partials, ns->counter, ns->norms, hm ? ns->hist : nullptr, ns->step,
+            ns->stop_tol);
         IPTGB_LAUNCH();
+        if (hm) ++ns->step;
         cur = nxt;
         return IPT_CUDA_SUCCESS;
     }
@@ -1165,6 +1236,7 @@ struct LowpDenseSimtF32 final : LowpDenseOperator {
 
     int refine_step(int want_norms, NormScratch *ns) override
     {
+        const bool hm = ns->hist != nullptr && ns->step < ns->hist_cap;
         IPTGB_CHECK(product());
         const size_t elems = (size_t)n * p;
         const int grid = blocks_for(elems);
@@ -1174,8 +1246,10 @@ struct LowpDenseSimtF32 final : LowpDenseOperator {
         refine_update_kernel<float><<<grid, kThreads, 0, s>>>(
             P.ptr, splits, n, p, 1.0f, small.ptr + p, small.ptr + 2 * p, G.ptr, R32.ptr,
             Xref32.ptr, small.ptr, X32[cur].ptr, X32[nxt].ptr, X32[nxt].ptr, n, want_norms,
-            ns->partials, ns->counter, ns->norms);
+            ns->partials, ns->counter, ns->norms, hm ? ns->hist : nullptr, ns->step,
+            ns->stop_tol);
         IPTGB_LAUNCH();
+        if (hm) ++ns->step;
         cur = nxt;
         return IPT_CUDA_SUCCESS;
     }
@@ -1288,6 +1362,17 @@ IptStage *make_lowp_stage_on(LowpDenseOperator *op, const double *d, int n, cuda
     return st;
 }
 
+bool lowp_device_stop(const LowpDenseOperator &op)
+{
+    const int ds = env_int("IPT_GB300_DEVICE_STOP", -1);
+    if (ds >= 0) return ds != 0;
+    int dev = 0, l2 = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, dev);
+    // measured at n = 8192 FP16 (Delta 1.07 x L2): break-even, so off there
+    return l2 > 0 && op.streamed_bytes() > 2.0 * (double)l2;
+}
+
 // Shared IPT loop on a low-precision operator: reads the fixed-point residual
 // every `check_every` iterations; with `guard`, stops once the residual stops
 // decreasing and rolls back a non-finite step.  The final block is exported
@@ -1298,7 +1383,12 @@ int run_lowp_ipt(LowpDenseOperator &op, int n, int p, int maxiter, double tol, i
 {
     SolveScratch scratch;
     IPTGB_CHECK(scratch.init((size_t)n * p, s));
-    int done = 0;
+    // every step adds its norms to the device history; the step after the
+    // one that meets tol passes the block through, so the host reads the
+    // history only every check_every steps
+    const bool device_stop = lowp_device_stop(op);
+    if (device_stop) IPTGB_CHECK(scratch.arm_history(std::max(1, maxiter), tol, s));
+    int launched = 0, done = 0;
     double fpres = NAN;
     double best = INFINITY;
     int worse = 0;
@@ -1307,15 +1397,26 @@ int run_lowp_ipt(LowpDenseOperator &op, int n, int p, int maxiter, double tol, i
     int host_err = 0;
     for (int it = 0; it < maxiter; ++it) {
         const int want = ((it + 1) % check_every == 0) || it + 1 == maxiter;
-        status = op.step(want, &scratch.ns);
+        status = op.step(device_stop ? 0 : want, &scratch.ns);
         if (status != IPT_CUDA_SUCCESS) break;
-        done = it + 1;
+        launched = it + 1;
+        done = launched;
         if (want) {
             trace_mark("ipt:check", s);
-            if (op.read_error(&host_err) != IPT_CUDA_SUCCESS ||
-                cudaMemcpyAsync(scratch.host_norms, scratch.ns.norms, 2 * sizeof(double),
-                                cudaMemcpyDeviceToHost, s) != cudaSuccess ||
-                cudaStreamSynchronize(s) != cudaSuccess) {
+            int stopped_at = -1;
+            double r = NAN;
+            int rs = IPT_CUDA_SUCCESS;
+            if (device_stop) {
+                rs = scratch.read_history(launched, &stopped_at, &r, s);
+            } else if (cudaMemcpyAsync(scratch.host_norms, scratch.ns.norms, 2 * sizeof(double),
+                                       cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+                       cudaStreamSynchronize(s) != cudaSuccess) {
+                rs = IPT_CUDA_CUDA_ERROR;
+            } else {
+                r = scratch.host_norms[0] / scratch.host_norms[1];
+                if (r <= tol) stopped_at = launched - 1;
+            }
+            if (op.read_error(&host_err) != IPT_CUDA_SUCCESS || rs != IPT_CUDA_SUCCESS) {
                 status = IPT_CUDA_CUDA_ERROR;
                 break;
             }
@@ -1324,9 +1425,12 @@ int run_lowp_ipt(LowpDenseOperator &op, int n, int p, int maxiter, double tol, i
                 status = IPT_CUDA_CUDA_ERROR;
                 break;
             }
-            const double xn = scratch.host_norms[1];
-            const double r = scratch.host_norms[0] / xn;
-            if (!(xn > 0.0) || !isfinite(r)) {
+            if (stopped_at >= 0) {
+                done = stopped_at + 1;
+                fpres = r;
+                break;
+            }
+            if (!isfinite(r)) {
                 rollback = guard;
                 if (!guard) {
                     status = IPT_CUDA_INVALID_ARGUMENT;
@@ -1334,7 +1438,6 @@ int run_lowp_ipt(LowpDenseOperator &op, int n, int p, int maxiter, double tol, i
                 break;
             }
             fpres = r;
-            if (r <= tol) break;
             if (guard) {
                 if (r < best) {
                     best = r;

@@ -12,7 +12,25 @@ struct NormScratch {
     int capacity = 0;             // number of slots
     unsigned int *counter = nullptr;  // ticket counter, zero between launches
     double *norms = nullptr;      // [0] = ||delta||_F, [1] = ||X||_F
+    // Optional per-step history with a device-side stop (tensor-core
+    // operator): step t adds its (||delta||^2, ||X||^2) into hist[2t..2t+1]
+    // with atomics; once a step meets ||delta|| <= stop_tol ||X||, the later
+    // steps' kernels pass the block through unchanged (and copy the
+    // history entry forward), so the host reads the history only now and then.
+    double *hist = nullptr;
+    int hist_cap = 0;    // steps the history holds
+    int step = 0;        // index of the next step
+    double stop_tol = 0.0;
 };
+
+// Did the history entry before `step` meet the stop tolerance?
+__device__ __forceinline__ bool hist_stopped(const double *hist, int step, double tol)
+{
+    if (hist == nullptr || step <= 0) return false;
+    const double d2 = __ldcg(hist + 2 * (step - 1));
+    const double x2 = __ldcg(hist + 2 * (step - 1) + 1);
+    return x2 > 0.0 && d2 <= tol * tol * x2;  // NaN never stops
+}
 
 // ---- FP64 dense (k_dense64.cu) -------------------------------------------
 int dense64_split_for(int n, int k, int sms);

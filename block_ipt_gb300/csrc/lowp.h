@@ -26,6 +26,7 @@ struct LowpDenseOperator {
     virtual int export_fp64_prev(double *X) = 0;             // previous block -> FP64
     virtual const float *partials() const = 0;               // [split][col][row] FP32
     virtual int num_splits() const = 0;
+    virtual double streamed_bytes() const { return 0.0; }    // operator bytes per product
 
     // Correction solve of the mixed refinement (after set_width/reset_identity
     // sized the block).  With the FP64 defect R0 = F(X) - X of the current
@@ -54,6 +55,13 @@ struct LowpDenseSetup {
 constexpr int kLowpColsumChunk = 2048;
 LowpDenseOperator *make_lowp_dense_operator(const double *dH, int n, int kind, cudaStream_t s,
                                             int *status, LowpDenseSetup *setup = nullptr);
+
+// Whether an iteration on `op` should use the device-side stop (NormScratch
+// history): the per-step norm reduction costs a few microseconds, the
+// pass-through steps after convergence save about one check interval of
+// products; worth it once a product streams clearly more than L2 holds.
+// Tuning knob IPT_GB300_DEVICE_STOP (0 = off, 1 = on).
+bool lowp_device_stop(const LowpDenseOperator &op);
 
 int run_lowp_ipt(LowpDenseOperator &op, int n, int p, int maxiter, double tol, int check_every,
                  double *X, int *iterations, double *fpres_out, long long *matvecs,

@@ -257,22 +257,37 @@ int refine_solve(const RefineInput &in, double *X_out, double *values_out, IPTBl
                                        cudaMemcpyHostToDevice, s));
             trace_mark("refine:correction", s);
             IPTGB_CHECK(in.lowp->refine_begin(R0.ptr, X.ptr, c, sigma));
-            const int check = 8;
+            // device-side stop at inner_tol; the history is read every `check` steps
+            const bool device_stop = lowp_device_stop(*in.lowp);
+            if (device_stop) {
+                IPTGB_CHECK(scratch.arm_history(std::max(1, in.inner_maxiter), in.inner_tol, s));
+            }
+            const int check = std::max(1, in.opt.ipt_check_every);
+            int ran = 0;
             for (int i = 0; i < in.inner_maxiter; ++i) {
-                const int want = ((i + 1) % check == 0);
-                IPTGB_CHECK(in.lowp->refine_step(want, &scratch.ns));
-                rep->lowp_matvecs += k;
+                const int want = ((i + 1) % check == 0) || i + 1 == in.inner_maxiter;
+                IPTGB_CHECK(in.lowp->refine_step(device_stop ? 0 : want, &scratch.ns));
+                ran = i + 1;
                 if (want) {
                     trace_mark("refine:correction_check", s);
-                    IPTGB_CUDA(cudaMemcpyAsync(scratch.host_norms, scratch.ns.norms,
-                                               2 * sizeof(double), cudaMemcpyDeviceToHost, s));
-                    IPTGB_CUDA(cudaStreamSynchronize(s));
-                    const double rel = scratch.host_norms[0] / scratch.host_norms[1];
-                    if (!(rel > in.inner_tol)) {  // converged (or non-finite: stop)
+                    int stopped_at = -1;
+                    double rel = NAN;
+                    if (device_stop) {
+                        IPTGB_CHECK(scratch.read_history(i + 1, &stopped_at, &rel, s));
+                    } else {
+                        IPTGB_CUDA(cudaMemcpyAsync(scratch.host_norms, scratch.ns.norms,
+                                                   2 * sizeof(double), cudaMemcpyDeviceToHost, s));
+                        IPTGB_CUDA(cudaStreamSynchronize(s));
+                        rel = scratch.host_norms[0] / scratch.host_norms[1];
+                    }
+                    if (stopped_at >= 0) {
+                        ran = stopped_at + 1;
                         break;
                     }
+                    if (!(rel > in.inner_tol)) break;  // non-finite: stop
                 }
             }
+            rep->lowp_matvecs += (long long)ran * k;
             IPTGB_CHECK(in.lowp->refine_apply(X.ptr));
         } else {
             add_kernel<<<blocks_for(elems), kThreads, 0, s>>>(X.ptr, R0.ptr, elems);

@@ -125,3 +125,21 @@ def test_mixed_refine_uses_fewer_fp64_products_than_plain(cuda):
     _, _, rep_plain = api.block_solve_dense(H, 16, "fp64")
     assert rep_mixed["converged"] == 1 and rep_plain["converged"] == 1
     assert rep_mixed["fp64_matvecs"] * 3 <= rep_plain["fp64_matvecs"]
+
+
+@pytest.mark.parametrize("prec", ["fp16", "bf16"])
+def test_device_stop_matches_host_checks(cuda, monkeypatch, prec):
+    """The device-side stop (per-step norm history; the steps after the one
+    that meets the tolerance pass the block through) gives the same pairs as
+    host checks every few steps, and its IPT stage stops no later.  (Stopping
+    exactly at the tolerance can cost the refinement an extra step, so the
+    total count of low-precision products is not compared.)"""
+    H, _ = workloads.dense_config1(2048, seed=12)
+    runs = {}
+    for mode in ("0", "1"):
+        monkeypatch.setenv("IPT_GB300_DEVICE_STOP", mode)
+        X, v, rep = api.block_solve_dense(H, 16, prec, ipt_maxiter=60, ipt_check_every=8)
+        assert rep["converged"] == 1
+        check_pairs(H, X, v, 16)
+        runs[mode] = rep
+    assert runs["1"]["ipt_iterations"] <= runs["0"]["ipt_iterations"]
