@@ -214,7 +214,7 @@ SIGNATURES = [
     ("ipt_mixed_precision_fp32_cuda_free_device_result", None, [C.POINTER(_MixedResult)]),
     ("ipt_mixed_precision_tf32_cuda_free_device_result", None, [C.POINTER(_MixedResult)]),
     ("ipt_block_default_options", None, [C.POINTER(IPTBlockOptions)]),
-    ("ipt_block_cholesky_inverse", _i, [_vp, _i, _vp, C.POINTER(C.c_int), _vp]),
+    ("ipt_block_cholesky_inverse", _i, [_vp, _i, _vp, C.POINTER(C.c_int), _i, _vp]),
     ("ipt_block_split_double", _i, [_vp, C.c_longlong, _vp, _vp, _vp]),
     ("ipt_block_split_double_host", _i, [_vp, C.c_longlong, _vp, _vp]),
     ("ipt_block_symmetric_eig", _i, [_vp, _i, _vp, _vp, _vp]),

@@ -770,9 +770,10 @@ IPT_API int ipt_block_symmetric_eig(const double *d_T, int m, double *d_w, doubl
 }
 
 IPT_API int ipt_block_cholesky_inverse(const double *d_G, int m, double *d_Rinv, int *shifts,
-                                       void *stream)
+                                       int precision, void *stream)
 {
-    if (d_G == nullptr || d_Rinv == nullptr || m <= 0 || m > 112) {
+    if (d_G == nullptr || d_Rinv == nullptr || m <= 0 || m > 112 || precision < 0 ||
+        precision > 1) {
         return IPT_CUDA_INVALID_ARGUMENT;
     }
     BlockOps ops;
@@ -780,7 +781,7 @@ IPT_API int ipt_block_cholesky_inverse(const double *d_G, int m, double *d_Rinv,
     ops.sms = device_sm_count();
     DeviceBuffer<int> st_dev;
     IPTGB_CHECK(st_dev.alloc(1, ops.stream));
-    int st = ops.chol_inverse(d_G, m, d_Rinv, st_dev.ptr);
+    int st = ops.chol_inverse(d_G, m, d_Rinv, st_dev.ptr, nullptr, precision == 1);
     int h = -1;
     if (st == IPT_CUDA_SUCCESS &&
         (cudaMemcpyAsync(&h, st_dev.ptr, sizeof(int), cudaMemcpyDeviceToHost, ops.stream) !=

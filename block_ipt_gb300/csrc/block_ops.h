@@ -27,8 +27,10 @@ struct BlockOps {
     // distance of the unit-diagonal scaled G from I (infinite for e >= 1), a
     // bound of that matrix's condition number; m <= 32 and no shift only,
     // NaN otherwise.
+    // df: for m <= 32, factor in double-float arithmetic (about 48 bits, several
+    // times faster on GB300 than the FP64 one-warp kernel); FP64 otherwise.
     int chol_inverse(const double *G, int m, double *Rinv, int *status_dev,
-                     double *cond_bound = nullptr);
+                     double *cond_bound = nullptr, bool df = false);
     // Symmetric eigensolve for m <= 112: FP32 Jacobi + FP64 refinement +
     // FP64 cluster polish (k_eig.cu).  Ascending w, eigenvectors Z.
     int symmetric_eig(const double *T, int m, double *w, double *Z, int *sweeps_dev);

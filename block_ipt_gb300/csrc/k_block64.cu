@@ -15,6 +15,7 @@
 
 #include "block_ops.h"
 #include "common.cuh"
+#include "dfloat.cuh"
 #include "reduce.cuh"
 
 namespace iptgb {
@@ -312,88 +313,129 @@ __global__ void chol_inverse_kernel(const double *__restrict__ G, int m, double 
     if (cond_bound != nullptr && threadIdx.x == 0) *cond_bound = NAN;  // not estimated here
 }
 
+
 // ---------------------------------------------------------------------------
-// One-warp Cholesky + inverse for m <= 32, in registers: lane i holds row i
-// of the lower factor (padded to the identity beyond m).  The same
-// right-looking factorisation as chol_inverse_block; a matrix that needs a
-// diagonal shift goes through chol_inverse_block (its shift retries and
-// status) instead.
+// Cholesky + inverse for m <= 32 with one thread per matrix entry (1024
+// threads, 32 x 32 padded to the identity beyond m): the same right-looking
+// factorisation as chol_inverse_block, then the column-oriented forward
+// substitution W = L^{-1}; two barriers per column.  GB300's FP64 pipe
+// holds its partition for 64 cycles per warp instruction, so spreading the
+// trailing updates over all 32 warps (all four partitions) instead of one
+// warp is what makes the kernel fast.  Arithmetic T: double (FP64, the
+// divisions of chol_inverse_block) or dfloat (double-float on the FP32 pipe,
+// about 48 bits, with the pivot reciprocal formed once).  A matrix that
+// needs a diagonal shift goes through chol_inverse_block (FP64, its shift
+// retries and status) instead.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(32)
-    chol_inverse32_kernel(const double *__restrict__ G, int m, double *__restrict__ Rinv,
-                          int *status, double *cond_bound)
+struct CholF64 {
+    typedef double T;
+    static __device__ __forceinline__ T load(double v) { return v; }
+    static __device__ __forceinline__ T value(float v) { return (double)v; }
+    static __device__ __forceinline__ bool positive(T v) { return v > 0.0 && isfinite(v); }
+    static __device__ __forceinline__ T sqrt_(T v) { return sqrt(v); }
+    static __device__ __forceinline__ T scale(T a, T piv, T) { return a / piv; }
+    static __device__ __forceinline__ T fms(T a, T x, T y) { return a - x * y; }
+    static __device__ __forceinline__ T recip(T) { return 0.0; }  // unused: divides
+    static __device__ __forceinline__ double store(T v) { return v; }
+    static __device__ __forceinline__ float lead(T v) { return (float)v; }
+};
+
+struct CholDF {
+    typedef dfloat T;
+    static __device__ __forceinline__ T load(double v) { return df_from_double(v); }
+    static __device__ __forceinline__ T value(float v) { return {v, 0.0f}; }
+    static __device__ __forceinline__ bool positive(T v) { return v.hi > 0.0f && isfinite(v.hi); }
+    static __device__ __forceinline__ T sqrt_(T v) { return df_sqrt(v); }
+    static __device__ __forceinline__ T scale(T a, T, T inv) { return df_mul(a, inv); }
+    static __device__ __forceinline__ T fms(T a, T x, T y) { return df_sub(a, df_mul(x, y)); }
+    static __device__ __forceinline__ T recip(T v) { return df_recip(v); }
+    static __device__ __forceinline__ double store(T v) { return df_to_double(v); }
+    static __device__ __forceinline__ float lead(T v) { return v.hi; }
+};
+
+template <typename Ops>
+__global__ void __launch_bounds__(1024)
+    chol_inverse32x32_kernel(const double *__restrict__ G, int m, double *__restrict__ Rinv,
+                             int *status, double *cond_bound)
 {
-    const int lane = threadIdx.x;
-    double a[32];
-#pragma unroll
-    for (int l = 0; l < 32; ++l) {
-        // G is symmetric: row `lane` of its lower triangle
-        a[l] = (lane < m && l < m) ? G[(size_t)l * m + lane] : (l == lane ? 1.0 : 0.0);
-    }
+    typedef typename Ops::T T;
+    __shared__ T col[32];      // the current column of L
+    __shared__ T piv[2];       // pivot and its reciprocal
+    __shared__ T Ls[32][33];   // L after the factorisation
+    __shared__ T Wrow[32];     // the current row of W
+    __shared__ float red[32];
+    __shared__ int fail;
+    const int tid = threadIdx.x;
+    const int r = tid >> 5;  // row
+    const int c = tid & 31;  // column
+    T a = (r < m && c < m) ? Ops::load(G[(size_t)c * m + r]) : Ops::value(r == c ? 1.0f : 0.0f);
+    if (tid == 0) fail = 0;
     if (cond_bound != nullptr) {
         // e = ||D^{-1/2} G D^{-1/2} - I||_F (D = diag G): the eigenvalues of
         // the unit-diagonal G lie in [1 - e, 1 + e], so its condition number
         // (which governs the orthogonality CholQR leaves) is at most
-        // (1 + e) / (1 - e)
-        double e2 = 0.0;
-        double dii = 1.0;
-#pragma unroll
-        for (int l = 0; l < 32; ++l) {
-            if (l == lane) dii = a[l];
-        }
-#pragma unroll
-        for (int l = 0; l < 32; ++l) {
-            const double dll = __shfl_sync(0xffffffffu, dii, l);
-            if (l != lane) e2 += a[l] * a[l] / (dii * dll);
-        }
-        for (int off = 16; off > 0; off >>= 1) e2 += __shfl_xor_sync(0xffffffffu, e2, off);
-        const bool bad = __any_sync(0xffffffffu, !(dii > 0.0));
-        if (lane == 0) {
-            const double e = sqrt(e2);
-            *cond_bound = (!bad && e < 1.0) ? (1.0 + e) / (1.0 - e) : INFINITY;
+        // (1 + e) / (1 - e); a few digits suffice, so FP32
+        const float grr = (float)G[(size_t)min(r, m - 1) * (m + 1)];
+        const float gcc = (float)G[(size_t)min(c, m - 1) * (m + 1)];
+        const float g = Ops::lead(a);
+        float t = (r != c && r < m && c < m) ? g * g / (grr * gcc) : 0.0f;
+        const bool bad = r == c && r < m && !(grr > 0.0f);
+        for (int off = 16; off > 0; off >>= 1) t += __shfl_xor_sync(0xffffffffu, t, off);
+        const bool wbad = __any_sync(0xffffffffu, bad);
+        if (c == 0) red[r] = wbad ? INFINITY : t;
+        __syncthreads();
+        if (r == 0) {
+            float v = red[c];
+            for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+            if (c == 0) {
+                const double e = sqrt((double)v);
+                *cond_bound = e < 1.0 ? (1.0 + e) / (1.0 - e) : INFINITY;  // NaN/inf: INFINITY
+            }
         }
     }
-    bool fail = false;
-#pragma unroll
+    __syncthreads();
     for (int j = 0; j < 32; ++j) {
-        const double ajj = __shfl_sync(0xffffffffu, a[j], j);
-        fail = fail || !(ajj > 0.0) || !isfinite(ajj);  // warp-uniform
-        const double ljj = fail ? 1.0 : sqrt(ajj);
-        if (lane > j) {
-            a[j] = a[j] / ljj;
-        } else if (lane == j) {
-            a[j] = ljj;
+        if (r == j && c == j) {
+            if (!Ops::positive(a)) {
+                fail = 1;
+                a = Ops::value(1.0f);
+            }
+            a = Ops::sqrt_(a);
+            piv[0] = a;
+            piv[1] = Ops::recip(a);
         }
-#pragma unroll
-        for (int l = j + 1; l < 32; ++l) {
-            const double alj = __shfl_sync(0xffffffffu, a[j], l);
-            if (lane >= l) a[l] -= a[j] * alj;
+        __syncthreads();
+        if (fail) break;  // uniform: read after the barrier
+        if (c == j && r > j) {
+            a = Ops::scale(a, piv[0], piv[1]);
+            col[r] = a;
         }
+        __syncthreads();
+        if (c > j && r >= c) a = Ops::fms(a, col[r], col[c]);
     }
     if (fail) {
         __shared__ double sm[2 * 32 * 32];
+        __syncthreads();
         chol_inverse_block(G, m, Rinv, status, sm);
-        if (cond_bound != nullptr && lane == 0) *cond_bound = NAN;  // shifted: not estimated
+        if (cond_bound != nullptr && tid == 0) *cond_bound = NAN;  // shifted: not estimated
         return;
     }
-    // lane c: column c of W = L^{-1} (column-oriented forward substitution)
-    // = row c of R^{-1}
-    double w[32];
-#pragma unroll
-    for (int i = 0; i < 32; ++i) w[i] = lane == i ? 1.0 : 0.0;
-#pragma unroll
+    Ls[r][c] = a;
+    // W = L^{-1}, thread (r, c) holds W[r][c]; column-oriented substitution
+    T w = Ops::value(r == c ? 1.0f : 0.0f);
+    __syncthreads();
     for (int l = 0; l < 32; ++l) {
-        w[l] = w[l] / __shfl_sync(0xffffffffu, a[l], l);
-#pragma unroll
-        for (int i = l + 1; i < 32; ++i) {
-            w[i] -= __shfl_sync(0xffffffffu, a[l], i) * w[l];
+        if (r == l) {
+            w = Ops::scale(w, Ls[l][l], Ops::recip(Ls[l][l]));
+            Wrow[c] = w;
         }
+        __syncthreads();
+        if (r > l) w = Ops::fms(w, Ls[r][l], Wrow[c]);
+        __syncthreads();
     }
-#pragma unroll
-    for (int i = 0; i < 32; ++i) {
-        if (lane < m && i < m) Rinv[(size_t)i * m + lane] = i < lane ? 0.0 : w[i];
-    }
-    if (lane == 0) status[0] = 0;
+    // R^{-1} = W^T (upper triangular), column-major: Rinv[c + r m] = W[r][c]
+    if (r < m && c < m) Rinv[(size_t)r * m + c] = r < c ? 0.0 : Ops::store(w);
+    if (tid == 0) status[0] = 0;
 }
 
 // ---------------------------------------------------------------------------
@@ -635,10 +677,17 @@ int BlockOps::proj_diag(const double *theta, int m, double *Tf, int ld)
     return IPT_CUDA_SUCCESS;
 }
 
-int BlockOps::chol_inverse(const double *G, int m, double *Rinv, int *status_dev, double *cond_bound)
+int BlockOps::chol_inverse(const double *G, int m, double *Rinv, int *status_dev, double *cond_bound,
+                           bool df)
 {
     if (m <= 32) {
-        chol_inverse32_kernel<<<1, 32, 0, stream>>>(G, m, Rinv, status_dev, cond_bound);
+        if (df) {
+            chol_inverse32x32_kernel<CholDF><<<1, 1024, 0, stream>>>(G, m, Rinv, status_dev,
+                                                                     cond_bound);
+        } else {
+            chol_inverse32x32_kernel<CholF64><<<1, 1024, 0, stream>>>(G, m, Rinv, status_dev,
+                                                                      cond_bound);
+        }
         IPTGB_LAUNCH();
         return IPT_CUDA_SUCCESS;
     }

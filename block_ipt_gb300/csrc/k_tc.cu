@@ -655,6 +655,86 @@ __global__ void lowp_update_kernel(const float *__restrict__ P, int S, int n, in
     }
 }
 
+// Four consecutive rows per thread (n % 4 == 0): the same update as
+// lowp_update_kernel with 16-byte loads and stores and 32-bit index math;
+// the update is latency-bound, so fewer and wider accesses shorten it.
+template <typename LP>
+struct alignas(4 * sizeof(LP)) LpQuad {
+    LP a, b, c, d;
+};
+
+__device__ __forceinline__ float4 f4_add(float4 a, float4 b)
+{
+    return make_float4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w);
+}
+
+__device__ __forceinline__ float &f4_at(float4 &v, int i)
+{
+    return i == 0 ? v.x : (i == 1 ? v.y : (i == 2 ? v.z : v.w));
+}
+
+template <typename LP>
+__global__ void lowp_update4_kernel(const float *__restrict__ P, int S, int n, int p,
+                                    float inv_scale, const float *__restrict__ G,
+                                    const float *__restrict__ X, float *__restrict__ Xn,
+                                    LP *__restrict__ Xlp, int ldx, int want_norms,
+                                    double2 *partials, unsigned int *counter, double *norms,
+                                    double *hist, int step, double stop_tol)
+{
+    const int nq = n >> 2;
+    const int total = nq * p;
+    const int stride = gridDim.x * blockDim.x;
+    if (hist_stopped(hist, step, stop_tol)) {
+        for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < total; q += stride) {
+            const int col = q / nq;
+            const int row0 = (q - col * nq) << 2;
+            const size_t e = (size_t)col * n + row0;
+            const float4 x = *reinterpret_cast<const float4 *>(X + e);
+            *reinterpret_cast<float4 *>(Xn + e) = x;
+            *reinterpret_cast<LpQuad<LP> *>(Xlp + (size_t)col * ldx + row0) =
+                LpQuad<LP>{to_lp<LP>(x.x), to_lp<LP>(x.y), to_lp<LP>(x.z), to_lp<LP>(x.w)};
+        }
+        hist_carry(hist, step);
+        return;
+    }
+    want_norms = want_norms || hist != nullptr;
+    float dsq = 0.0f, xsq = 0.0f;
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < total; q += stride) {
+        const int col = q / nq;
+        const int row0 = (q - col * nq) << 2;
+        const size_t e = (size_t)col * n + row0;
+        float4 y = make_float4(0.f, 0.f, 0.f, 0.f);
+        float c = 0.0f;
+        for (int s = 0; s < S; ++s) {
+            const float *base = P + ((size_t)s * p + col) * (size_t)n;
+            y = f4_add(y, *reinterpret_cast<const float4 *>(base + row0));
+            c += base[col];
+        }
+        const float4 x = *reinterpret_cast<const float4 *>(X + e);
+        const float4 g = *reinterpret_cast<const float4 *>(G + e);
+        const float ci = c * inv_scale;
+        float4 o;
+        o.x = (y.x * inv_scale - x.x * ci) * g.x;
+        o.y = (y.y * inv_scale - x.y * ci) * g.y;
+        o.z = (y.z * inv_scale - x.z * ci) * g.z;
+        o.w = (y.w * inv_scale - x.w * ci) * g.w;
+        if (col >= row0 && col < row0 + 4) f4_at(o, col - row0) = 1.0f;  // X_jj = 1
+        *reinterpret_cast<float4 *>(Xn + e) = o;
+        *reinterpret_cast<LpQuad<LP> *>(Xlp + (size_t)col * ldx + row0) =
+            LpQuad<LP>{to_lp<LP>(o.x), to_lp<LP>(o.y), to_lp<LP>(o.z), to_lp<LP>(o.w)};
+        if (want_norms) {
+            const float d0 = o.x - x.x, d1 = o.y - x.y, d2 = o.z - x.z, d3 = o.w - x.w;
+            dsq += d0 * d0 + d1 * d1 + d2 * d2 + d3 * d3;
+            xsq += x.x * x.x + x.y * x.y + x.z * x.z + x.w * x.w;
+        }
+    }
+    if (hist != nullptr) {
+        hist_add(hist, step, block_sum2((double)dsq, (double)xsq));
+    } else if (want_norms) {
+        grid_finish_norms2(block_sum2((double)dsq, (double)xsq), partials, counter, norms);
+    }
+}
+
 __global__ void f32_to_f64_kernel(const float *__restrict__ in, size_t count, double *__restrict__ out)
 {
     const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -746,6 +826,81 @@ __global__ void refine_update_kernel(const float *__restrict__ P, int S, int n, 
     } else if (want_norms) {
         const double2 t = block_sum2(dsq, xsq);
         grid_finish_norms2(t, partials, counter, norms);
+    }
+}
+
+// refine_update_kernel with four consecutive rows per thread (n % 4 == 0).
+template <typename LP>
+__global__ void refine_update4_kernel(const float *__restrict__ P, int S, int n, int p,
+                                      float inv_scale, const float *__restrict__ sig,
+                                      const float *__restrict__ sig_inv,
+                                      const float *__restrict__ G, const float *__restrict__ R32,
+                                      const float *__restrict__ X32, const float *__restrict__ c32,
+                                      const float *__restrict__ dcur, float *__restrict__ dnext,
+                                      LP *__restrict__ dlp, int ldx, int want_norms,
+                                      double2 *partials, unsigned int *counter, double *norms,
+                                      double *hist, int step, double stop_tol)
+{
+    const int nq = n >> 2;
+    const int total = nq * p;
+    const int stride = gridDim.x * blockDim.x;
+    if (hist_stopped(hist, step, stop_tol)) {
+        for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < total; q += stride) {
+            const int col = q / nq;
+            const int row0 = (q - col * nq) << 2;
+            const size_t e = (size_t)col * n + row0;
+            const float4 cur = *reinterpret_cast<const float4 *>(dcur + e);
+            const float sg = sig[col];
+            *reinterpret_cast<float4 *>(dnext + e) = cur;
+            *reinterpret_cast<LpQuad<LP> *>(dlp + (size_t)col * ldx + row0) =
+                LpQuad<LP>{to_lp<LP>(cur.x * sg), to_lp<LP>(cur.y * sg), to_lp<LP>(cur.z * sg),
+                           to_lp<LP>(cur.w * sg)};
+        }
+        hist_carry(hist, step);
+        return;
+    }
+    want_norms = want_norms || hist != nullptr;
+    float dsq = 0.0f, xsq = 0.0f;
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < total; q += stride) {
+        const int col = q / nq;
+        const int row0 = (q - col * nq) << 2;
+        const size_t e = (size_t)col * n + row0;
+        float4 y = make_float4(0.f, 0.f, 0.f, 0.f);
+        float b = 0.0f;
+        for (int s = 0; s < S; ++s) {
+            const float *base = P + ((size_t)s * p + col) * (size_t)n;
+            y = f4_add(y, *reinterpret_cast<const float4 *>(base + row0));
+            b += base[col];
+        }
+        const float sc = inv_scale * sig_inv[col];
+        y = make_float4(y.x * sc, y.y * sc, y.z * sc, y.w * sc);
+        b *= sc;
+        const float cb = c32[col] + b;
+        const float4 cur = *reinterpret_cast<const float4 *>(dcur + e);
+        const float4 r = *reinterpret_cast<const float4 *>(R32 + e);
+        const float4 x = *reinterpret_cast<const float4 *>(X32 + e);
+        const float4 g = *reinterpret_cast<const float4 *>(G + e);
+        float4 o;
+        o.x = r.x + (y.x - x.x * b - cur.x * cb) * g.x;
+        o.y = r.y + (y.y - x.y * b - cur.y * cb) * g.y;
+        o.z = r.z + (y.z - x.z * b - cur.z * cb) * g.z;
+        o.w = r.w + (y.w - x.w * b - cur.w * cb) * g.w;
+        if (col >= row0 && col < row0 + 4) f4_at(o, col - row0) = 0.0f;  // X_jj stays 1
+        *reinterpret_cast<float4 *>(dnext + e) = o;
+        const float sg = sig[col];
+        *reinterpret_cast<LpQuad<LP> *>(dlp + (size_t)col * ldx + row0) =
+            LpQuad<LP>{to_lp<LP>(o.x * sg), to_lp<LP>(o.y * sg), to_lp<LP>(o.z * sg),
+                       to_lp<LP>(o.w * sg)};
+        if (want_norms) {
+            const float d0 = o.x - cur.x, d1 = o.y - cur.y, d2 = o.z - cur.z, d3 = o.w - cur.w;
+            dsq += d0 * d0 + d1 * d1 + d2 * d2 + d3 * d3;
+            xsq += cur.x * cur.x + cur.y * cur.y + cur.z * cur.z + cur.w * cur.w;
+        }
+    }
+    if (hist != nullptr) {
+        hist_add(hist, step, block_sum2((double)dsq, (double)xsq));
+    } else if (want_norms) {
+        grid_finish_norms2(block_sum2((double)dsq, (double)xsq), partials, counter, norms);
     }
 }
 
@@ -990,6 +1145,16 @@ struct LowpDense final : LowpDenseOperator {
 
     int product() override { return product_until(nullptr, 0, 0.0); }
 
+    // update grid: grid-stride over the block with a few CTAs per SM (four
+    // rows per thread when n % 4 == 0); tuning knob IPT_GB300_UPDATE_CTAS_PER_SM
+    int update_grid() const
+    {
+        const size_t items = n % 4 == 0 ? (size_t)n * p / 4 : (size_t)n * p;
+        const int per_sm = env_int("IPT_GB300_UPDATE_CTAS_PER_SM", 4);
+        const int all = blocks_for(items);
+        return per_sm > 0 ? std::min(all, per_sm * sms) : all;
+    }
+
     // hist/step/tol: the device-side stop of the running iteration (or null)
     int product_until(const double *hist, int step, double tol)
     {
@@ -1009,17 +1174,21 @@ struct LowpDense final : LowpDenseOperator {
         double *hist = hm ? ns->hist : nullptr;
         const int hstep = ns->step;
         IPTGB_CHECK(product_until(hist, hstep, ns->stop_tol));
-        const size_t elems = (size_t)n * p;
-        // a few CTAs per SM, grid-stride (tuning knob: IPT_GB300_UPDATE_CTAS_PER_SM)
-        const int per_sm = env_int("IPT_GB300_UPDATE_CTAS_PER_SM", 4);
-        const int grid = per_sm > 0 ? std::min(blocks_for(elems), per_sm * sms) : blocks_for(elems);
+        const int grid = update_grid();
         if (want_norms && grid > ns->capacity) return IPT_CUDA_INVALID_ARGUMENT;
         const int nxt = cur ^ 1;
         KernelTimerScope timer(kProfLowpUpdate, s);
-        lowp_update_kernel<LP><<<grid, kThreads, 0, s>>>(
-            P.ptr, splits, n, p, (float)(1.0 / scale), G.ptr, X32[cur].ptr, X32[nxt].ptr,
-            Xlp[nxt].ptr, ldp, want_norms, ns->partials, ns->counter, ns->norms, hist, hstep,
-            ns->stop_tol);
+        if (n % 4 == 0) {
+            lowp_update4_kernel<LP><<<grid, kThreads, 0, s>>>(
+                P.ptr, splits, n, p, (float)(1.0 / scale), G.ptr, X32[cur].ptr, X32[nxt].ptr,
+                Xlp[nxt].ptr, ldp, want_norms, ns->partials, ns->counter, ns->norms, hist, hstep,
+                ns->stop_tol);
+        } else {
+            lowp_update_kernel<LP><<<grid, kThreads, 0, s>>>(
+                P.ptr, splits, n, p, (float)(1.0 / scale), G.ptr, X32[cur].ptr, X32[nxt].ptr,
+                Xlp[nxt].ptr, ldp, want_norms, ns->partials, ns->counter, ns->norms, hist, hstep,
+                ns->stop_tol);
+        }
         IPTGB_LAUNCH();
         if (hm) ++ns->step;
         cur = nxt;
@@ -1075,17 +1244,23 @@ struct LowpDense final : LowpDenseOperator {
         double *hist = hm ? ns->hist : nullptr;
         const int hstep = ns->step;
         IPTGB_CHECK(product_until(hist, hstep, ns->stop_tol));
-        const size_t elems = (size_t)n * p;
-        // a few CTAs per SM, grid-stride (tuning knob: IPT_GB300_UPDATE_CTAS_PER_SM)
-        const int per_sm = env_int("IPT_GB300_UPDATE_CTAS_PER_SM", 4);
-        const int grid = per_sm > 0 ? std::min(blocks_for(elems), per_sm * sms) : blocks_for(elems);
+        const int grid = update_grid();
         if (want_norms && grid > ns->capacity) return IPT_CUDA_INVALID_ARGUMENT;
         const int nxt = cur ^ 1;
         KernelTimerScope timer(kProfLowpUpdate, s);
-        refine_update_kernel<LP><<<grid, kThreads, 0, s>>>(
-            P.ptr, splits, n, p, (float)(1.0 / scale), small.ptr + p, small.ptr + 2 * p, G.ptr,
-            R32.ptr, Xref32.ptr, small.ptr, X32[cur].ptr, X32[nxt].ptr, Xlp[nxt].ptr, ldp,
-            want_norms, ns->partials, ns->counter, ns->norms, hist, hstep, ns->stop_tol);
+        if (n % 4 == 0) {
+            refine_update4_kernel<LP><<<grid, kThreads, 0, s>>>(
+                P.ptr, splits, n, p, (float)(1.0 / scale), small.ptr + p, small.ptr + 2 * p,
+                G.ptr, R32.ptr, Xref32.ptr, small.ptr, X32[cur].ptr, X32[nxt].ptr, Xlp[nxt].ptr,
+                ldp, want_norms, ns->partials, ns->counter, ns->norms, hist, hstep,
+                ns->stop_tol);
+        } else {
+            refine_update_kernel<LP><<<grid, kThreads, 0, s>>>(
+                P.ptr, splits, n, p, (float)(1.0 / scale), small.ptr + p, small.ptr + 2 * p,
+                G.ptr, R32.ptr, Xref32.ptr, small.ptr, X32[cur].ptr, X32[nxt].ptr, Xlp[nxt].ptr,
+                ldp, want_norms, ns->partials, ns->counter, ns->norms, hist, hstep,
+                ns->stop_tol);
+        }
         IPTGB_LAUNCH();
         if (hm) ++ns->step;
         cur = nxt;

@@ -320,7 +320,9 @@ int refine_solve(const RefineInput &in, double *X_out, double *values_out, IPTBl
     auto cholqr_pair = [&](double *A, double *HA, double *A2, double *HA2, double *cond_out,
                            double *h_cond) -> int {
         IPTGB_CHECK(ops.gram(A, n, k, A, n, k, n, G, k));
-        IPTGB_CHECK(ops.chol_inverse(G, k, Rinv, st_dev, cond_out));
+        // double-float factor: the Rayleigh-Ritz basis is well conditioned
+        // here (the second pass runs otherwise)
+        IPTGB_CHECK(ops.chol_inverse(G, k, Rinv, st_dev, cond_out, true));
         IPTGB_CHECK(ops.tall_gemm(A, n, Rinv, k, A2, n, n, k, k));
         IPTGB_CHECK(ops.tall_gemm(HA, n, Rinv, k, HA2, n, n, k, k));
         IPTGB_CUDA(cudaMemcpyAsync(&h_status, st_dev, sizeof(int), cudaMemcpyDeviceToHost, s));

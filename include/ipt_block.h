@@ -134,8 +134,11 @@ int ipt_block_symmetric_eig(const double *d_T, int m, double *d_w, double *d_Z, 
  * that is not numerically positive definite is factored as G + shift*I with
  * the shift grown from 1e-14 trace(G) by 100x per retry; *shifts gets the
  * number of retries (0 = plain).  Returns IPT_CUDA_INVALID_ARGUMENT with
- * *shifts = -1 when 12 retries do not suffice.  Synchronises `stream`. */
-int ipt_block_cholesky_inverse(const double *d_G, int m, double *d_Rinv, int *shifts, void *stream);
+ * *shifts = -1 when 12 retries do not suffice.  precision 0: FP64; 1:
+ * double-float (hi + lo FP32 pairs, about 48 bits) for m <= 32 and no shift,
+ * FP64 otherwise.  Synchronises `stream`. */
+int ipt_block_cholesky_inverse(const double *d_G, int m, double *d_Rinv, int *shifts,
+                               int precision, void *stream);
 
 /* ---- allocation-free FP64 dense solve ------------------------------------ */
 

@@ -99,38 +99,42 @@ def test_invalid_sizes(cuda):
     assert lib.ipt_block_symmetric_eig(None, 2, p, p, None) == 1
 
 
-def chol_inv(torch, G):
+def chol_inv(torch, G, precision=0):
     """(status, Rinv, shifts) of ipt_block_cholesky_inverse on the GPU."""
     m = G.shape[0]
     dG = torch.from_numpy(np.asfortranarray(G).T.copy()).cuda()
     dR = torch.zeros((m, m), dtype=torch.float64, device="cuda")
     shifts = C.c_int(-7)
     st = _lib.load().ipt_block_cholesky_inverse(
-        C.c_void_p(dG.data_ptr()), m, C.c_void_p(dR.data_ptr()), C.byref(shifts),
+        C.c_void_p(dG.data_ptr()), m, C.c_void_p(dR.data_ptr()), C.byref(shifts), precision,
         C.c_void_p(torch.cuda.current_stream().cuda_stream))
     torch.cuda.synchronize()
     return st, dR.T.cpu().numpy(), shifts.value
 
 
+@pytest.mark.parametrize("precision", [0, 1])
 @pytest.mark.parametrize("m", [1, 5, 31, 32, 33, 64, 112])
-def test_cholesky_inverse_spd(cuda, m):
-    """One-warp register kernel (m <= 32) and the shared-memory kernel
-    (m > 32) against LAPACK's Cholesky: R^{-1} upper triangular with
-    R^{-T} G R^{-1} = I."""
+def test_cholesky_inverse_spd(cuda, m, precision):
+    """One-warp register kernels (m <= 32: FP64, or double-float ~48 bits) and
+    the FP64 shared-memory kernel (m > 32) against LAPACK's Cholesky: R^{-1}
+    upper triangular with R^{-T} G R^{-1} = I.  Tolerances: FP64 as LAPACK;
+    double-float 64x looser (its unit roundoff 2^-47)."""
     rng = np.random.default_rng(100 + m)
     X = rng.standard_normal((4 * m + 8, m)) * (1.0 + np.arange(m))  # columns of mixed scale
     G = X.T @ X
-    st, Rinv, shifts = chol_inv(cuda, G)
+    st, Rinv, shifts = chol_inv(cuda, G, precision)
     assert st == 0 and shifts == 0
     assert np.all(np.tril(Rinv, -1) == 0.0)
     R_ref = np.linalg.cholesky(G).T
-    np.testing.assert_allclose(Rinv, np.linalg.inv(R_ref), rtol=1e-10,
-                               atol=1e-12 * np.abs(np.linalg.inv(R_ref)).max())
-    assert np.abs(Rinv.T @ G @ Rinv - np.eye(m)).max() <= 1e-12
+    loose = 64.0 if (precision == 1 and m <= 32) else 1.0
+    np.testing.assert_allclose(Rinv, np.linalg.inv(R_ref), rtol=1e-10 * loose,
+                               atol=1e-12 * loose * np.abs(np.linalg.inv(R_ref)).max())
+    assert np.abs(Rinv.T @ G @ Rinv - np.eye(m)).max() <= 1e-12 * loose
 
 
+@pytest.mark.parametrize("precision", [0, 1])
 @pytest.mark.parametrize("m", [8, 40])
-def test_cholesky_inverse_shift_retries(cuda, m):
+def test_cholesky_inverse_shift_retries(cuda, m, precision):
     """An indefinite Gram-like matrix (two eigenvalues at -1e-9 trace) is
     factored with the first shift of the sequence 1e-14 trace * 100^j that
     works (both kernels)."""
@@ -139,7 +143,7 @@ def test_cholesky_inverse_shift_retries(cuda, m):
     X = np.hstack([X, X[:, :2]])  # two repeated columns
     G = X.T @ X
     G -= 1e-9 * np.trace(G) * np.eye(m)
-    st, Rinv, shifts = chol_inv(cuda, G)
+    st, Rinv, shifts = chol_inv(cuda, G, precision)
     assert st == 0 and shifts >= 3
     shift = 1e-14 * np.trace(np.abs(G)) * 100.0 ** (shifts - 1)
     Gs = G + shift * np.eye(m)
@@ -151,7 +155,10 @@ def test_cholesky_inverse_shift_retries(cuda, m):
 def test_cholesky_inverse_invalid(cuda):
     G = np.eye(4)
     G[1, 1] = np.nan
-    st, _, shifts = chol_inv(cuda, G)
-    assert st == _lib.IPT_CUDA_INVALID_ARGUMENT and shifts == -1  # no shift worked
+    for precision in (0, 1):
+        st, _, shifts = chol_inv(cuda, G, precision)
+        assert st == _lib.IPT_CUDA_INVALID_ARGUMENT and shifts == -1  # no shift worked
     st, _, _ = chol_inv(cuda, np.eye(113))
+    assert st == _lib.IPT_CUDA_INVALID_ARGUMENT
+    st, _, _ = chol_inv(cuda, np.eye(4), precision=2)
     assert st == _lib.IPT_CUDA_INVALID_ARGUMENT
