@@ -57,6 +57,7 @@ struct DenseApply final : Fp64Apply {
             }
         }
         KernelTimerScope timer(kProfFp64Update, s);
+        if (Hh != nullptr) return launch_df_sum_partials(P.ptr, S, (size_t)n * c, AV, s);
         return launch_sum_partials(P.ptr, S, (size_t)n * c, AV, s);
     }
 };
@@ -825,17 +826,21 @@ IPT_API int ipt_block_solve_dense(const double *matrix_col_major, int n, int k,
     }
     cudaStream_t s = (cudaStream_t)opt.stream;
     const size_t mat = (size_t)n * n;
+    trace_mark("host_dense:start", s);
     DeviceBuffer<double> dH, dX, dv;
     IPTGB_CHECK(dH.alloc(mat, s));
     IPTGB_CHECK(dX.alloc((size_t)n * k, s));
     IPTGB_CHECK(dv.alloc((size_t)k, s));
+    trace_mark("host_dense:allocated", s);
     IPTGB_CUDA(cudaMemcpyAsync(dH.ptr, matrix_col_major, mat * sizeof(double),
                                cudaMemcpyHostToDevice, s));
+    trace_mark("host_dense:h2d_done", s);
     IPTGB_CHECK(dense_block_device(dH.ptr, n, k, &opt, dX.ptr, dv.ptr, report));
     IPTGB_CUDA(cudaMemcpyAsync(vectors, dX.ptr, (size_t)n * k * sizeof(double),
                                cudaMemcpyDeviceToHost, s));
     IPTGB_CUDA(cudaMemcpyAsync(values, dv.ptr, (size_t)k * sizeof(double), cudaMemcpyDeviceToHost,
                                s));
+    trace_mark("host_dense:d2h_done", s);
     IPTGB_CUDA(cudaStreamSynchronize(s));
     return IPT_CUDA_SUCCESS;
 }

@@ -90,6 +90,22 @@ __device__ __forceinline__ dfloat df_recip(dfloat a)
     return df_fast_two_sum(y, __fmul_rn(y, e.hi));
 }
 
+// (S, s) += (ah + al)(bh + bl), dropping al bl: the exact two-product of the
+// leading parts (p, fma(ah, bh, -p)), the cross terms folded into its error,
+// p added to S with an exact two-sum whose error joins s: 12 FP32 operations,
+// the accumulation step of the double-float dot products.
+__device__ __forceinline__ void df_acc(float &S, float &s, float ah, float al, float bh, float bl)
+{
+    const float p = __fmul_rn(ah, bh);
+    const float pe = __fmaf_rn(ah, bh, -p);
+    const float t = __fmaf_rn(ah, bl, __fmaf_rn(al, bh, pe));
+    const float u = __fadd_rn(S, p);
+    const float bp = __fsub_rn(u, S);
+    const float err = __fadd_rn(__fsub_rn(S, __fsub_rn(u, bp)), __fsub_rn(p, bp));
+    S = u;
+    s = __fadd_rn(s, __fadd_rn(err, t));
+}
+
 // exact conversions
 __device__ __forceinline__ dfloat df_from_double(double v)
 {

@@ -95,6 +95,97 @@ __global__ void reduce_slices_kernel(const double *__restrict__ P, int slices, s
     *o = beta == 0.0 ? alpha * s : alpha * s + beta * *o;
 }
 
+// The same partial Gram products in double-float arithmetic on the FP32
+// pipe (BlockOps::df_products): tiles split into (hi, lo) floats when staged,
+// df_acc per term; GB300's FP32 pipe runs ~5x more of these terms per second
+// than its FP64 pipe runs FMAs.
+__global__ void __launch_bounds__(256)
+gram_partial_df_kernel(const double *__restrict__ A, long long lda, int ma,
+                       const double *__restrict__ B, long long ldb, int mb, int n,
+                       int chunks_per_block, double *__restrict__ P)
+{
+    __shared__ float ash[kGramRows][kGramTile + 1], asl[kGramRows][kGramTile + 1];
+    __shared__ float bsh[kGramRows][kGramTile + 1], bsl[kGramRows][kGramTile + 1];
+    const int tiles_i = (ma + kGramTile - 1) / kGramTile;
+    const int ti = blockIdx.y % tiles_i;
+    const int tj = blockIdx.y / tiles_i;
+    const int i0 = ti * kGramTile;
+    const int j0 = tj * kGramTile;
+    const int li = threadIdx.x % kGramTile;
+    const int lj = threadIdx.x / kGramTile;  // 0..7
+    float S[4] = {0.f, 0.f, 0.f, 0.f}, sl[4] = {0.f, 0.f, 0.f, 0.f};
+    for (int c = 0; c < chunks_per_block; ++c) {
+        const int r0 = (blockIdx.x * chunks_per_block + c) * kGramRows;
+        if (r0 >= n) {
+            break;
+        }
+        __syncthreads();
+        // loads first (all in flight), then the splits into shared memory
+        constexpr int kPer = kGramRows * kGramTile / 256;
+        double av[kPer], bv[kPer];
+#pragma unroll
+        for (int q = 0; q < kPer; ++q) {
+            const int e = threadIdx.x + q * 256;
+            const int r = e % kGramRows;
+            const int col = e / kGramRows;
+            const int row = r0 + r;
+            av[q] = (row < n && i0 + col < ma) ? A[(size_t)row + (size_t)(i0 + col) * lda] : 0.0;
+            bv[q] = (row < n && j0 + col < mb) ? B[(size_t)row + (size_t)(j0 + col) * ldb] : 0.0;
+        }
+#pragma unroll
+        for (int q = 0; q < kPer; ++q) {
+            const int e = threadIdx.x + q * 256;
+            const int r = e % kGramRows;
+            const int col = e / kGramRows;
+            const dfloat a = df_from_double(av[q]);
+            const dfloat b = df_from_double(bv[q]);
+            ash[r][col] = a.hi;
+            asl[r][col] = a.lo;
+            bsh[r][col] = b.hi;
+            bsl[r][col] = b.lo;
+        }
+        __syncthreads();
+#pragma unroll 4
+        for (int r = 0; r < kGramRows; ++r) {
+            const float ah = ash[r][li], al = asl[r][li];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                df_acc(S[q], sl[q], ah, al, bsh[r][lj + 8 * q], bsl[r][lj + 8 * q]);
+            }
+        }
+    }
+    const size_t mm = (size_t)ma * (size_t)mb;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const int i = i0 + li;
+        const int j = j0 + lj + 8 * q;
+        if (i < ma && j < mb) {
+            P[(size_t)blockIdx.x * mm + (size_t)j * ma + i] = (double)S[q] + (double)sl[q];
+        }
+    }
+}
+
+// Slice sums with one warp per output: lanes take every 32nd slice, then a
+// fixed shuffle tree (deterministic; many slices reduce in parallel instead
+// of one thread's FP64 chain).
+__global__ void reduce_slices_warp_kernel(const double *__restrict__ P, int slices, size_t elems,
+                                          double *__restrict__ out, long long ldo, int rows,
+                                          double alpha, double beta)
+{
+    const size_t e = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (e >= elems) return;  // whole warps leave together
+    double s = 0.0;
+    for (int b = lane; b < slices; b += 32) s += P[(size_t)b * elems + e];
+    for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
+    if (lane == 0) {
+        const size_t i = e % (size_t)rows;
+        const size_t j = e / (size_t)rows;
+        double *o = out + i + j * (size_t)ldo;
+        *o = beta == 0.0 ? alpha * s : alpha * s + beta * *o;
+    }
+}
+
 int BlockOps::gram(const double *A, long long lda, int ma, const double *B, long long ldb, int mb,
                    int n, double *C, long long ldc, double alpha, double beta)
 {
@@ -112,6 +203,15 @@ int BlockOps::gram(const double *A, long long lda, int ma, const double *B, long
     const size_t mm = (size_t)ma * (size_t)mb;
     IPTGB_CHECK(ensure_partials((size_t)blocks_x * mm));
     KernelTimerScope timer(kProfGram, stream);
+    if (df_products) {
+        gram_partial_df_kernel<<<dim3(blocks_x, tiles), 256, 0, stream>>>(A, lda, ma, B, ldb, mb,
+                                                                          n, per_block, partials);
+        IPTGB_LAUNCH();
+        reduce_slices_warp_kernel<<<blocks_for(mm * 32), kThreads, 0, stream>>>(
+            partials, blocks_x, mm, C, ldc, ma, alpha, beta);
+        IPTGB_LAUNCH();
+        return IPT_CUDA_SUCCESS;
+    }
     gram_partial_kernel<<<dim3(blocks_x, tiles), 256, 0, stream>>>(A, lda, ma, B, ldb, mb, n,
                                                                    per_block, partials);
     IPTGB_LAUNCH();
@@ -155,6 +255,8 @@ __global__ void __launch_bounds__(kTallThreads)
         __syncthreads();
         if (row < n) {
             const int lc = min(kTallK, m - l0);
+            // unrolled so that several A loads are in flight per thread
+#pragma unroll 8
             for (int l = 0; l < lc; ++l) {
                 const double a = A[(size_t)row + (size_t)(l0 + l) * lda];
 #pragma unroll
@@ -175,6 +277,68 @@ __global__ void __launch_bounds__(kTallThreads)
     }
 }
 
+// tall_gemm_kernel in double-float arithmetic (BlockOps::df_products): the
+// B tile split into (hi, lo) floats in shared memory, each A entry split once
+// per row and used for TC columns.
+template <int TC>
+__global__ void __launch_bounds__(kTallThreads)
+    tall_gemm_df_kernel(const double *__restrict__ A, long long lda, const double *__restrict__ B,
+                        long long ldb, double *__restrict__ C, long long ldc, int n, int m, int p,
+                        double alpha, double beta)
+{
+    __shared__ float bsh[kTallK][TC], bsl[kTallK][TC];
+    const int row = blockIdx.x * blockDim.x + threadIdx.x;
+    const int c0 = blockIdx.y * TC;
+    float S[TC], sl[TC];
+#pragma unroll
+    for (int j = 0; j < TC; ++j) {
+        S[j] = 0.f;
+        sl[j] = 0.f;
+    }
+    for (int l0 = 0; l0 < m; l0 += kTallK) {
+        __syncthreads();
+        for (int e = threadIdx.x; e < kTallK * TC; e += blockDim.x) {
+            const int l = e % kTallK;
+            const int j = e / kTallK;
+            const dfloat b = df_from_double(
+                (l0 + l < m && c0 + j < p) ? B[(size_t)(l0 + l) + (size_t)(c0 + j) * ldb] : 0.0);
+            bsh[l][j] = b.hi;
+            bsl[l][j] = b.lo;
+        }
+        __syncthreads();
+        if (row < n) {
+            const int lc = min(kTallK, m - l0);
+            // all of the row's A values in flight at once (the kernel is
+            // latency-bound at a few warps per SM otherwise)
+            double av[kTallK];
+#pragma unroll
+            for (int l = 0; l < kTallK; ++l) {
+                av[l] = l < lc ? A[(size_t)row + (size_t)(l0 + l) * lda] : 0.0;
+            }
+#pragma unroll
+            for (int l = 0; l < kTallK; ++l) {
+                if (l < lc) {
+                    const dfloat a = df_from_double(av[l]);
+#pragma unroll
+                    for (int j = 0; j < TC; ++j) {
+                        df_acc(S[j], sl[j], a.hi, a.lo, bsh[l][j], bsl[l][j]);
+                    }
+                }
+            }
+        }
+    }
+    if (row < n) {
+#pragma unroll
+        for (int j = 0; j < TC; ++j) {
+            if (c0 + j < p) {
+                double *o = C + (size_t)row + (size_t)(c0 + j) * ldc;
+                const double v = (double)S[j] + (double)sl[j];
+                *o = beta == 0.0 ? alpha * v : alpha * v + beta * *o;
+            }
+        }
+    }
+}
+
 int BlockOps::tall_gemm(const double *A, long long lda, const double *B, long long ldb, double *C,
                         long long ldc, int n, int m, int p, double alpha, double beta)
 {
@@ -184,6 +348,22 @@ int BlockOps::tall_gemm(const double *A, long long lda, const double *B, long lo
     const int row_blocks = (n + kTallThreads - 1) / kTallThreads;
     const int want = 2 * std::max(1, sms);
     KernelTimerScope timer(kProfTallGemm, stream);
+    if (df_products) {
+        // several CTAs per SM hide the latency of the double-float chains:
+        // narrower column groups until the grid has about four per SM
+        if ((long long)row_blocks * ((p + 15) / 16) >= 2 * want) {
+            tall_gemm_df_kernel<16><<<dim3(row_blocks, (p + 15) / 16), kTallThreads, 0, stream>>>(
+                A, lda, B, ldb, C, ldc, n, m, p, alpha, beta);
+        } else if ((long long)row_blocks * ((p + 7) / 8) >= 2 * want) {
+            tall_gemm_df_kernel<8><<<dim3(row_blocks, (p + 7) / 8), kTallThreads, 0, stream>>>(
+                A, lda, B, ldb, C, ldc, n, m, p, alpha, beta);
+        } else {
+            tall_gemm_df_kernel<4><<<dim3(row_blocks, (p + 3) / 4), kTallThreads, 0, stream>>>(
+                A, lda, B, ldb, C, ldc, n, m, p, alpha, beta);
+        }
+        IPTGB_LAUNCH();
+        return IPT_CUDA_SUCCESS;
+    }
     if ((long long)row_blocks * ((p + 31) / 32) >= want) {
         tall_gemm_kernel<32><<<dim3(row_blocks, (p + 31) / 32), kTallThreads, 0, stream>>>(
             A, lda, B, ldb, C, ldc, n, m, p, alpha, beta);

@@ -15,6 +15,7 @@
 #include <string.h>
 
 #include "common.cuh"
+#include "dfloat.cuh"
 #include "fpconv.cuh"
 #include "kernels.cuh"
 
@@ -43,24 +44,18 @@ __global__ void df_split_kernel(const double *__restrict__ A, size_t count,
 
 __device__ __forceinline__ void df_term(float &S, float &s, float hh, float hl, float xh, float xl)
 {
-    const float p = __fmul_rn(hh, xh);
-    const float pe = __fmaf_rn(hh, xh, -p);
-    const float t = __fmaf_rn(hh, xl, __fmaf_rn(hl, xh, pe));
-    const float u = __fadd_rn(S, p);
-    const float bp = __fsub_rn(u, S);
-    const float err = __fadd_rn(__fsub_rn(S, __fsub_rn(u, bp)), __fsub_rn(p, bp));
-    S = u;
-    s = __fadd_rn(s, __fadd_rn(err, t));
+    df_acc(S, s, hh, hl, xh, xl);
 }
 
 // Split-K partial product, one output row per thread, BN columns in
 // double-float registers; X chunk (hi, lo) staged in shared memory.
-// P[slice][column][row] (FP64) = the slice's partial sums.
+// P[slice][column][row] = the slice's partial sum as a double-float pair
+// (float2 hi, lo; summed by df_sum_partials_kernel).
 template <int BN>
 __global__ void __launch_bounds__(kDfRows, 1)
 df64_partial_kernel(const float *__restrict__ Hh, const float *__restrict__ Hl, int n,
                     long long ldh, const float *__restrict__ Xh, const float *__restrict__ Xl,
-                    long long ldx, int k, double *__restrict__ P, int kslice)
+                    long long ldx, int k, float2 *__restrict__ P, int kslice)
 {
     __shared__ float xsh[kDfChunk][BN];
     __shared__ float xsl[kDfChunk][BN];
@@ -109,10 +104,35 @@ df64_partial_kernel(const float *__restrict__ Hh, const float *__restrict__ Hl, 
         for (int j = 0; j < BN; ++j) {
             if (c0 + j < k) {
                 P[((size_t)sl * (size_t)k + (size_t)(c0 + j)) * (size_t)n + row] =
-                    (double)S[j] + (double)s[j];
+                    make_float2(S[j], s[j]);
             }
         }
     }
+}
+
+// Y = sum over the S double-float slices (fixed order, accurate double-float
+// additions on the FP32 pipe), then one conversion to FP64 per entry.
+__global__ void df_sum_partials_kernel(const float2 *__restrict__ P, int S, size_t elems,
+                                       double *__restrict__ Y)
+{
+    const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= elems) return;
+    const float2 p0 = P[idx];
+    dfloat y = {p0.x, p0.y};
+    for (int sl = 1; sl < S; ++sl) {
+        const float2 p = P[(size_t)sl * elems + idx];
+        y = df_add(y, dfloat{p.x, p.y});
+    }
+    Y[idx] = df_to_double(y);
+}
+
+int launch_df_sum_partials(const double *P, int S, size_t elems, double *Y, cudaStream_t stream)
+{
+    if (S <= 0 || elems == 0) return IPT_CUDA_SUCCESS;
+    df_sum_partials_kernel<<<blocks_for(elems), kThreads, 0, stream>>>(
+        reinterpret_cast<const float2 *>(P), S, elems, Y);
+    IPTGB_LAUNCH();
+    return IPT_CUDA_SUCCESS;
 }
 
 int launch_df_split(const double *A, size_t count, float *hi, float *lo, cudaStream_t stream)
@@ -136,14 +156,16 @@ int launch_df64_partial(const float *Hh, const float *Hl, int n, long long ldh, 
     const int over = env_int("IPT_GB300_DF_BN", 0);  // tuning override: 8, 16 or 32
     if (over == 8 || over == 16 || over == 32) bn = over;
     dim3 grid(row_blocks, S, (k + bn - 1) / bn);
+    // the double-float partials (float2) fill the same bytes as FP64 ones
+    float2 *P2 = reinterpret_cast<float2 *>(P);
     if (bn == 8) {
-        df64_partial_kernel<8><<<grid, kDfRows, 0, stream>>>(Hh, Hl, n, ldh, Xh, Xl, ldx, k, P,
+        df64_partial_kernel<8><<<grid, kDfRows, 0, stream>>>(Hh, Hl, n, ldh, Xh, Xl, ldx, k, P2,
                                                              kslice);
     } else if (bn == 16) {
-        df64_partial_kernel<16><<<grid, kDfRows, 0, stream>>>(Hh, Hl, n, ldh, Xh, Xl, ldx, k, P,
+        df64_partial_kernel<16><<<grid, kDfRows, 0, stream>>>(Hh, Hl, n, ldh, Xh, Xl, ldx, k, P2,
                                                               kslice);
     } else {
-        df64_partial_kernel<32><<<grid, kDfRows, 0, stream>>>(Hh, Hl, n, ldh, Xh, Xl, ldx, k, P,
+        df64_partial_kernel<32><<<grid, kDfRows, 0, stream>>>(Hh, Hl, n, ldh, Xh, Xl, ldx, k, P2,
                                                               kslice);
     }
     IPTGB_LAUNCH();

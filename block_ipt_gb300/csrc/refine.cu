@@ -46,10 +46,15 @@ constexpr int kDefectRows = 2048;
 
 // Per (row chunk, column): R0 = F(X) - X and partial sums of ||r||^2,
 // ||x||^2 and max |R0| (see file header).  Partials [chunk][col][3].
+// lowp_rhs: R0 only feeds the low-precision correction solve (converted to
+// FP32 there), so 1/gap is taken in FP32 instead of an FP64 division, which
+// GB300 runs as a long sequence on its slow FP64 pipe; the residual norms
+// stay exact FP64 (r = gap * R0 needs no division).  The plain FP64 path adds
+// R0 to X and keeps the exact quotient.
 __global__ void defect_partial_kernel(const double *__restrict__ X, const double *__restrict__ HX,
                                       const double *__restrict__ d, int n, int k,
                                       double *__restrict__ R0, double *__restrict__ c_out,
-                                      double *__restrict__ P)
+                                      double *__restrict__ P, int lowp_rhs)
 {
     __shared__ double smax[32];
     const int j = blockIdx.y;
@@ -67,10 +72,18 @@ __global__ void defect_partial_kernel(const double *__restrict__ X, const double
         double rdef = 0.0;
         if (i != j) {
             const double gap = d[j] - d[i];
-            const double g = (isfinite(gap) && gap != 0.0) ? 1.0 / gap : NAN;
             const double a = HX[idx] - d[i] * x;
-            rdef = (a - x * c) * g - x;
-            const double r = gap * rdef;
+            double r;
+            if (lowp_rhs) {
+                r = (a - x * c) - gap * x;
+                const double g =
+                    (isfinite(gap) && gap != 0.0) ? (double)__frcp_rn((float)gap) : NAN;
+                rdef = r * g;
+            } else {
+                const double g = (isfinite(gap) && gap != 0.0) ? 1.0 / gap : NAN;
+                rdef = (a - x * c) * g - x;
+                r = gap * rdef;
+            }
             rs = fma(r, r, rs);
             mx = fmax(mx, fabs(rdef));
         }
@@ -141,6 +154,10 @@ int refine_solve(const RefineInput &in, double *X_out, double *values_out, IPTBl
     BlockOps ops;
     ops.stream = s;
     ops.sms = device_sm_count();
+    // the Rayleigh-Ritz products of the converged block in double-float
+    // (about 48 bits: far below the 1e-8 residual and the 1e-10 ||H||
+    // eigenvalue accuracy they serve)
+    ops.df_products = true;
     const int chunks = (n + kDefectRows - 1) / kDefectRows;
     DeviceBuffer<double> X, HX, R0, Q, HQ, small;
     IPTGB_CHECK(X.alloc(elems, s));
@@ -208,7 +225,7 @@ int refine_solve(const RefineInput &in, double *X_out, double *values_out, IPTBl
         trace_mark("refine:defect_product_done", s);
         rep->fp64_matvecs += k;
         defect_partial_kernel<<<dim3(chunks, k), 256, 0, s>>>(X.ptr, HX.ptr, in.d, n, k, R0.ptr, c,
-                                                              P);
+                                                              P, in.lowp != nullptr ? 1 : 0);
         IPTGB_LAUNCH();
         defect_finish_kernel<<<blocks_for(k), kThreads, 0, s>>>(P, chunks, k, in.hnorm, scaled,
                                                                colmax);
