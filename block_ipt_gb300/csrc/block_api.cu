@@ -39,7 +39,7 @@ struct DenseApply final : Fp64Apply {
     DeviceBuffer<float> Xs;
     int apply(const double *V, int c, double *AV) override
     {
-        const int S = dense64_split_for(n, c, sms);
+        const int S = Hh != nullptr ? df64_split_for(n, c, sms) : dense64_split_for(n, c, sms);
         const size_t need = (size_t)S * (size_t)n * (size_t)c;
         if (P.count < need) {
             IPTGB_CHECK(P.alloc(need, s));

@@ -14,6 +14,8 @@
 // and the FP64 partial sums are those of the FP64 kernel (k_dense64.cu).
 #include <string.h>
 
+#include <algorithm>
+
 #include "common.cuh"
 #include "dfloat.cuh"
 #include "fpconv.cuh"
@@ -51,8 +53,11 @@ __device__ __forceinline__ void df_term(float &S, float &s, float hh, float hl, 
 // double-float registers; X chunk (hi, lo) staged in shared memory.
 // P[slice][column][row] = the slice's partial sum as a double-float pair
 // (float2 hi, lo; summed by df_sum_partials_kernel).
+// Three CTAs per SM for BN <= 16 (80 registers, no spills): six warps per
+// scheduler hide the latency of the H loads and of the staging barrier
+// better than four.
 template <int BN>
-__global__ void __launch_bounds__(kDfRows, 1)
+__global__ void __launch_bounds__(kDfRows, BN <= 16 ? 3 : 1)
 df64_partial_kernel(const float *__restrict__ Hh, const float *__restrict__ Hl, int n,
                     long long ldh, const float *__restrict__ Xh, const float *__restrict__ Xl,
                     long long ldx, int k, float2 *__restrict__ P, int kslice)
@@ -142,6 +147,29 @@ int launch_df_split(const double *A, size_t count, float *hi, float *lo, cudaStr
     return IPT_CUDA_SUCCESS;
 }
 
+static int df64_tile_width(int k)
+{
+    int bn = k <= 8 ? 8 : 16;
+    const int over = env_int("IPT_GB300_DF_BN", 0);  // tuning override: 8, 16 or 32
+    if (over == 8 || over == 16 || over == 32) bn = over;
+    return bn;
+}
+
+int df64_split_for(int n, int k, int sms)
+{
+    // K slices so that the grid is a whole number of waves of the resident
+    // CTAs (3 per SM at BN <= 16): two waves by default (tuning knob
+    // IPT_GB300_DF_WAVES), slices at least 64 deep
+    const int bn = df64_tile_width(k);
+    const int row_blocks = (n + kDfRows - 1) / kDfRows;
+    const int tiles = row_blocks * ((k + bn - 1) / bn);
+    const int per_sm = bn <= 16 ? 3 : 1;
+    const int waves = std::max(1, env_int("IPT_GB300_DF_WAVES", 2));
+    int S = (waves * per_sm * std::max(1, sms)) / std::max(1, tiles);
+    S = std::min(S, std::max(1, n / 64));
+    return std::max(1, S);
+}
+
 int launch_df64_partial(const float *Hh, const float *Hl, int n, long long ldh, const float *Xh,
                         const float *Xl, long long ldx, int k, double *P, int S,
                         cudaStream_t stream)
@@ -152,9 +180,7 @@ int launch_df64_partial(const float *Hh, const float *Hl, int n, long long ldh, 
     // 16-column tiles also for wider blocks: H is re-read per tile (from L2 /
     // HBM, cheap next to the FP32 work) but 80 instead of 148 registers let
     // three CTAs share an SM (measured faster at n = 8192, k = 32)
-    int bn = k <= 8 ? 8 : 16;
-    const int over = env_int("IPT_GB300_DF_BN", 0);  // tuning override: 8, 16 or 32
-    if (over == 8 || over == 16 || over == 32) bn = over;
+    const int bn = df64_tile_width(k);
     dim3 grid(row_blocks, S, (k + bn - 1) / bn);
     // the double-float partials (float2) fill the same bytes as FP64 ones
     float2 *P2 = reinterpret_cast<float2 *>(P);

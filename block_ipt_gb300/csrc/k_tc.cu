@@ -28,6 +28,7 @@
 
 #include <algorithm>
 #include <memory>
+#include <utility>
 
 #include "block_solver.h"
 #include "common.cuh"
@@ -36,6 +37,20 @@
 #include "reduce.cuh"
 
 namespace iptgb {
+
+// Programmatic dependent launch: wait for the grids this one depends on
+// (a no-op when it was launched without the attribute), and let the next
+// grid in the stream be scheduled early.
+__device__ __forceinline__ void grid_dependency_wait()
+{
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+}
+
+__device__ __forceinline__ void grid_launch_dependents()
+{
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
 namespace tc {
 
 constexpr int kBM = 128;         // UMMA M: rows of Delta per CTA
@@ -196,7 +211,11 @@ tc_partial_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
                   int *err, float a_keep, const double *hist, int step, double stop_tol)
 {
     // the iteration already met its tolerance on the device: nothing to do
-    if (hist_stopped(hist, step, stop_tol)) return;
+    // (the history is written by the previous update: wait for it first)
+    if (hist != nullptr) {
+        grid_dependency_wait();
+        if (hist_stopped(hist, step, stop_tol)) return;
+    }
     extern __shared__ uint8_t smem_raw[];
     // 1024-byte alignment of the shared-window address (SWIZZLE_128B atoms)
     uint8_t *smem = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
@@ -247,7 +266,26 @@ tc_partial_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
     if (warp == 0 && lane == 0) {
         const uint64_t a_pol = a_keep > 0.0f ? l2_keep_policy(fminf(a_keep, 1.0f)) : 0ull;
         // ---- TMA producer ----
-        int i = 0;
+        // Delta does not depend on the previous kernel: the first stages' Delta
+        // tiles are requested before waiting for the grid that wrote X (with a
+        // programmatic dependent launch that grid may still be running)
+        const int pre = min(stages, nchunks);
+        for (int q = 0; q < pre; ++q) {
+            const uint32_t sa = smem_base + (uint32_t)q * stage_bytes;
+            const int kx = (c0 + q) * kchunk_elems;
+            mbar_expect_tx(full_bar(q), stage_bytes);
+            if (a_keep > 0.0f) {
+                tma_load_2d_hint(sa, &tmA, kx, rb * kBM, full_bar(q), a_pol);
+            } else {
+                tma_load_2d(sa, &tmA, kx, rb * kBM, full_bar(q));
+            }
+        }
+        grid_dependency_wait();
+        for (int q = 0; q < pre; ++q) {
+            const uint32_t sb = smem_base + (uint32_t)q * stage_bytes + a_bytes;
+            tma_load_2d(sb, &tmB, (c0 + q) * kchunk_elems, 0, full_bar(q));
+        }
+        int i = pre;
         for (; i < nchunks; ++i) {
             const int s = i % stages;
             const int r = i / stages;
@@ -270,6 +308,7 @@ tc_partial_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
             tma_load_2d(sb, &tmB, kx, 0, full_bar(s));
         }
         issued_count = i;
+        grid_launch_dependents();
     } else if (warp == 1 && lane == 0) {
         // ---- tcgen05.mma issuer ----
         for (int i = 0; i < nchunks; ++i) {
@@ -609,6 +648,8 @@ __global__ void lowp_update_kernel(const float *__restrict__ P, int S, int n, in
                                    double2 *partials, unsigned int *counter, double *norms,
                                    double *hist, int step, double stop_tol)
 {
+    grid_dependency_wait();  // P and X come from the previous grids
+    grid_launch_dependents();
     // grid-stride over the block (a few CTAs per SM)
     const size_t elems = (size_t)n * (size_t)p;
     const size_t stride = (size_t)gridDim.x * blockDim.x;
@@ -681,6 +722,8 @@ __global__ void lowp_update4_kernel(const float *__restrict__ P, int S, int n, i
                                     double2 *partials, unsigned int *counter, double *norms,
                                     double *hist, int step, double stop_tol)
 {
+    grid_dependency_wait();  // P and X come from the previous grids
+    grid_launch_dependents();
     const int nq = n >> 2;
     const int total = nq * p;
     const int stride = gridDim.x * blockDim.x;
@@ -780,6 +823,8 @@ __global__ void refine_update_kernel(const float *__restrict__ P, int S, int n, 
                                      int want_norms, double2 *partials, unsigned int *counter,
                                      double *norms, double *hist, int step, double stop_tol)
 {
+    grid_dependency_wait();  // P and X come from the previous grids
+    grid_launch_dependents();
     const size_t elems = (size_t)n * (size_t)p;
     const size_t stride = (size_t)gridDim.x * blockDim.x;
     if (hist_stopped(hist, step, stop_tol)) {
@@ -841,6 +886,8 @@ __global__ void refine_update4_kernel(const float *__restrict__ P, int S, int n,
                                       double2 *partials, unsigned int *counter, double *norms,
                                       double *hist, int step, double stop_tol)
 {
+    grid_dependency_wait();  // P and X come from the previous grids
+    grid_launch_dependents();
     const int nq = n >> 2;
     const int total = nq * p;
     const int stride = gridDim.x * blockDim.x;
@@ -915,6 +962,30 @@ __global__ void refine_apply_kernel(double *__restrict__ X, const float *__restr
 // Host side
 // ---------------------------------------------------------------------------
 namespace {
+
+// Launch with programmatic stream serialisation: the kernel may start while
+// its predecessor in the stream finishes; it calls grid_dependency_wait()
+// before reading the predecessor's results.  Tuning knob IPT_GB300_PDL=0
+// launches in plain stream order.
+template <typename... KArgs, typename... Args>
+int launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
+               Args &&...args)
+{
+    static const bool on = env_int("IPT_GB300_PDL", 1) != 0;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = on ? 1 : 0;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    IPTGB_CUDA(cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...));
+    count_launch();
+    return IPT_CUDA_SUCCESS;
+}
 
 typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
                                   const cuuint64_t *, const cuuint64_t *, const cuuint32_t *,
@@ -1161,11 +1232,10 @@ struct LowpDense final : LowpDenseOperator {
         const int row_blocks = (n + tc::kBM - 1) / tc::kBM;
         dim3 grid(row_blocks, splits);
         KernelTimerScope timer(kProfLowpProduct, s);
-        tc::tc_partial_kernel<LowpTypes<LP>::kind><<<grid, tc::kThreads, smem_bytes, s>>>(
-            mapA, mapB[cur], n, p, p_pad, stages, tmem_cols, chunks_total, chunks_per_split,
-            kchunk, idesc, P.ptr, err.ptr, a_keep, hist, step, tol);
-        IPTGB_LAUNCH();
-        return IPT_CUDA_SUCCESS;
+        return launch_pdl(tc::tc_partial_kernel<LowpTypes<LP>::kind>, grid, dim3(tc::kThreads),
+                          smem_bytes, s, mapA, mapB[cur], n, p, p_pad, stages, tmem_cols,
+                          chunks_total, chunks_per_split, (int)kchunk, idesc, P.ptr, err.ptr,
+                          a_keep, hist, step, tol);
     }
 
     int step(int want_norms, NormScratch *ns) override
@@ -1178,18 +1248,12 @@ struct LowpDense final : LowpDenseOperator {
         if (want_norms && grid > ns->capacity) return IPT_CUDA_INVALID_ARGUMENT;
         const int nxt = cur ^ 1;
         KernelTimerScope timer(kProfLowpUpdate, s);
-        if (n % 4 == 0) {
-            lowp_update4_kernel<LP><<<grid, kThreads, 0, s>>>(
-                P.ptr, splits, n, p, (float)(1.0 / scale), G.ptr, X32[cur].ptr, X32[nxt].ptr,
-                Xlp[nxt].ptr, ldp, want_norms, ns->partials, ns->counter, ns->norms, hist, hstep,
-                ns->stop_tol);
-        } else {
-            lowp_update_kernel<LP><<<grid, kThreads, 0, s>>>(
-                P.ptr, splits, n, p, (float)(1.0 / scale), G.ptr, X32[cur].ptr, X32[nxt].ptr,
-                Xlp[nxt].ptr, ldp, want_norms, ns->partials, ns->counter, ns->norms, hist, hstep,
-                ns->stop_tol);
-        }
-        IPTGB_LAUNCH();
+        IPTGB_CHECK(launch_pdl(n % 4 == 0 ? lowp_update4_kernel<LP> : lowp_update_kernel<LP>,
+                               dim3(grid), dim3(kThreads), 0, s, (const float *)P.ptr, splits, n,
+                               p, (float)(1.0 / scale), (const float *)G.ptr,
+                               (const float *)X32[cur].ptr, X32[nxt].ptr, Xlp[nxt].ptr, ldp,
+                               want_norms, ns->partials, ns->counter, ns->norms, hist, hstep,
+                               ns->stop_tol));
         if (hm) ++ns->step;
         cur = nxt;
         return IPT_CUDA_SUCCESS;
@@ -1248,20 +1312,14 @@ struct LowpDense final : LowpDenseOperator {
         if (want_norms && grid > ns->capacity) return IPT_CUDA_INVALID_ARGUMENT;
         const int nxt = cur ^ 1;
         KernelTimerScope timer(kProfLowpUpdate, s);
-        if (n % 4 == 0) {
-            refine_update4_kernel<LP><<<grid, kThreads, 0, s>>>(
-                P.ptr, splits, n, p, (float)(1.0 / scale), small.ptr + p, small.ptr + 2 * p,
-                G.ptr, R32.ptr, Xref32.ptr, small.ptr, X32[cur].ptr, X32[nxt].ptr, Xlp[nxt].ptr,
-                ldp, want_norms, ns->partials, ns->counter, ns->norms, hist, hstep,
-                ns->stop_tol);
-        } else {
-            refine_update_kernel<LP><<<grid, kThreads, 0, s>>>(
-                P.ptr, splits, n, p, (float)(1.0 / scale), small.ptr + p, small.ptr + 2 * p,
-                G.ptr, R32.ptr, Xref32.ptr, small.ptr, X32[cur].ptr, X32[nxt].ptr, Xlp[nxt].ptr,
-                ldp, want_norms, ns->partials, ns->counter, ns->norms, hist, hstep,
-                ns->stop_tol);
-        }
-        IPTGB_LAUNCH();
+        IPTGB_CHECK(launch_pdl(n % 4 == 0 ? refine_update4_kernel<LP> : refine_update_kernel<LP>,
+                               dim3(grid), dim3(kThreads), 0, s, (const float *)P.ptr, splits, n,
+                               p, (float)(1.0 / scale), (const float *)(small.ptr + p),
+                               (const float *)(small.ptr + 2 * p), (const float *)G.ptr,
+                               (const float *)R32.ptr, (const float *)Xref32.ptr,
+                               (const float *)small.ptr, (const float *)X32[cur].ptr,
+                               X32[nxt].ptr, Xlp[nxt].ptr, ldp, want_norms, ns->partials,
+                               ns->counter, ns->norms, hist, hstep, ns->stop_tol));
         if (hm) ++ns->step;
         cur = nxt;
         return IPT_CUDA_SUCCESS;
