@@ -60,6 +60,48 @@ void count_launch();
         ::iptgb::count_launch();                                                \
     } while (0)
 
+int env_int(const char *name, int default_value);
+
+// Programmatic dependent launch.  A kernel launched by launch_pdl() may start
+// while its predecessor in the stream is still running; it calls pdl_wait()
+// before it reads anything the predecessor wrote (or writes anything the
+// predecessor reads), and pdl_trigger() to let its own successor start early.
+// Under a plain launch pdl_wait() returns at once (stream order already
+// holds).  Tuning knob IPT_GB300_PDL=0 launches everything in plain order.
+__device__ __forceinline__ void pdl_wait()
+{
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+}
+
+__device__ __forceinline__ void pdl_trigger()
+{
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
+template <typename... KArgs, typename... Args>
+int launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
+               Args &&...args)
+{
+    static const bool on = env_int("IPT_GB300_PDL", 1) != 0;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = on ? 1 : 0;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    const cudaError_t e = cudaLaunchKernelEx(&cfg, kernel, static_cast<Args &&>(args)...);
+    if (e != cudaSuccess) {
+        fprintf(stderr, "ipt_gb300: launch error: %s\n", cudaGetErrorString(e));
+        return IPT_CUDA_CUDA_ERROR;
+    }
+    count_launch();
+    return IPT_CUDA_SUCCESS;
+}
+
 // Optional per-kernel timing (ipt_block_profile_*): when enabled, the
 // instrumented launch sites bracket their kernel with CUDA events on the
 // launch stream.  KernelTimerScope records the start in its constructor and

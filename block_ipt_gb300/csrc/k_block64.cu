@@ -32,6 +32,8 @@ gram_partial_kernel(const double *__restrict__ A, long long lda, int ma,
                     const double *__restrict__ B, long long ldb, int mb, int n, int chunks_per_block,
                     double *__restrict__ P)
 {
+    pdl_wait();  // programmatic dependent launch: predecessor done
+    pdl_trigger();
     __shared__ double as[kGramRows][kGramTile + 1];
     __shared__ double bs[kGramRows][kGramTile + 1];
     const int tiles_i = (ma + kGramTile - 1) / kGramTile;
@@ -81,6 +83,8 @@ __global__ void reduce_slices_kernel(const double *__restrict__ P, int slices, s
                                      double *__restrict__ out, long long ldo, int rows,
                                      double alpha, double beta)
 {
+    pdl_wait();  // programmatic dependent launch: predecessor done
+    pdl_trigger();
     const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= elems) {
         return;
@@ -104,6 +108,8 @@ gram_partial_df_kernel(const double *__restrict__ A, long long lda, int ma,
                        const double *__restrict__ B, long long ldb, int mb, int n,
                        int chunks_per_block, double *__restrict__ P)
 {
+    pdl_wait();  // programmatic dependent launch: predecessor done
+    pdl_trigger();
     __shared__ float ash[kGramRows][kGramTile + 1], asl[kGramRows][kGramTile + 1];
     __shared__ float bsh[kGramRows][kGramTile + 1], bsl[kGramRows][kGramTile + 1];
     const int tiles_i = (ma + kGramTile - 1) / kGramTile;
@@ -172,6 +178,8 @@ __global__ void reduce_slices_warp_kernel(const double *__restrict__ P, int slic
                                           double *__restrict__ out, long long ldo, int rows,
                                           double alpha, double beta)
 {
+    pdl_wait();  // programmatic dependent launch: predecessor done
+    pdl_trigger();
     const size_t e = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (e >= elems) return;  // whole warps leave together
@@ -204,20 +212,17 @@ int BlockOps::gram(const double *A, long long lda, int ma, const double *B, long
     IPTGB_CHECK(ensure_partials((size_t)blocks_x * mm));
     KernelTimerScope timer(kProfGram, stream);
     if (df_products) {
-        gram_partial_df_kernel<<<dim3(blocks_x, tiles), 256, 0, stream>>>(A, lda, ma, B, ldb, mb,
-                                                                          n, per_block, partials);
-        IPTGB_LAUNCH();
-        reduce_slices_warp_kernel<<<blocks_for(mm * 32), kThreads, 0, stream>>>(
-            partials, blocks_x, mm, C, ldc, ma, alpha, beta);
-        IPTGB_LAUNCH();
+        IPTGB_CHECK(launch_pdl(gram_partial_df_kernel, dim3(blocks_x, tiles), dim3(256), 0, stream,
+                               A, lda, ma, B, ldb, mb, n, per_block, partials));
+        IPTGB_CHECK(launch_pdl(reduce_slices_warp_kernel, dim3(blocks_for(mm * 32)),
+                               dim3(kThreads), 0, stream, (const double *)partials, blocks_x, mm, C,
+                               ldc, ma, alpha, beta));
         return IPT_CUDA_SUCCESS;
     }
-    gram_partial_kernel<<<dim3(blocks_x, tiles), 256, 0, stream>>>(A, lda, ma, B, ldb, mb, n,
-                                                                   per_block, partials);
-    IPTGB_LAUNCH();
-    reduce_slices_kernel<<<blocks_for(mm), kThreads, 0, stream>>>(partials, blocks_x, mm, C, ldc,
-                                                                  ma, alpha, beta);
-    IPTGB_LAUNCH();
+    IPTGB_CHECK(launch_pdl(gram_partial_kernel, dim3(blocks_x, tiles), dim3(256), 0, stream, A,
+                           lda, ma, B, ldb, mb, n, per_block, partials));
+    IPTGB_CHECK(launch_pdl(reduce_slices_kernel, dim3(blocks_for(mm)), dim3(kThreads), 0, stream,
+                           (const double *)partials, blocks_x, mm, C, ldc, ma, alpha, beta));
     return IPT_CUDA_SUCCESS;
 }
 
@@ -237,6 +242,8 @@ __global__ void __launch_bounds__(kTallThreads)
                      long long ldb, double *__restrict__ C, long long ldc, int n, int m, int p,
                      double alpha, double beta)
 {
+    pdl_wait();  // programmatic dependent launch: predecessor done
+    pdl_trigger();
     __shared__ double bs[kTallK][TC];
     const int row = blockIdx.x * blockDim.x + threadIdx.x;
     const int c0 = blockIdx.y * TC;
@@ -286,6 +293,8 @@ __global__ void __launch_bounds__(kTallThreads)
                         long long ldb, double *__restrict__ C, long long ldc, int n, int m, int p,
                         double alpha, double beta)
 {
+    pdl_wait();  // programmatic dependent launch: predecessor done
+    pdl_trigger();
     __shared__ float bsh[kTallK][TC], bsl[kTallK][TC];
     const int row = blockIdx.x * blockDim.x + threadIdx.x;
     const int c0 = blockIdx.y * TC;
@@ -348,34 +357,35 @@ int BlockOps::tall_gemm(const double *A, long long lda, const double *B, long lo
     const int row_blocks = (n + kTallThreads - 1) / kTallThreads;
     const int want = 2 * std::max(1, sms);
     KernelTimerScope timer(kProfTallGemm, stream);
+    // column group: the widest that still gives the grid enough CTAs
+    int tc = 0;
+    void (*kernel)(const double *, long long, const double *, long long, double *, long long, int,
+                   int, int, double, double) = nullptr;
     if (df_products) {
         // several CTAs per SM hide the latency of the double-float chains:
         // narrower column groups until the grid has about four per SM
         if ((long long)row_blocks * ((p + 15) / 16) >= 2 * want) {
-            tall_gemm_df_kernel<16><<<dim3(row_blocks, (p + 15) / 16), kTallThreads, 0, stream>>>(
-                A, lda, B, ldb, C, ldc, n, m, p, alpha, beta);
+            tc = 16;
+            kernel = tall_gemm_df_kernel<16>;
         } else if ((long long)row_blocks * ((p + 7) / 8) >= 2 * want) {
-            tall_gemm_df_kernel<8><<<dim3(row_blocks, (p + 7) / 8), kTallThreads, 0, stream>>>(
-                A, lda, B, ldb, C, ldc, n, m, p, alpha, beta);
+            tc = 8;
+            kernel = tall_gemm_df_kernel<8>;
         } else {
-            tall_gemm_df_kernel<4><<<dim3(row_blocks, (p + 3) / 4), kTallThreads, 0, stream>>>(
-                A, lda, B, ldb, C, ldc, n, m, p, alpha, beta);
+            tc = 4;
+            kernel = tall_gemm_df_kernel<4>;
         }
-        IPTGB_LAUNCH();
-        return IPT_CUDA_SUCCESS;
-    }
-    if ((long long)row_blocks * ((p + 31) / 32) >= want) {
-        tall_gemm_kernel<32><<<dim3(row_blocks, (p + 31) / 32), kTallThreads, 0, stream>>>(
-            A, lda, B, ldb, C, ldc, n, m, p, alpha, beta);
+    } else if ((long long)row_blocks * ((p + 31) / 32) >= want) {
+        tc = 32;
+        kernel = tall_gemm_kernel<32>;
     } else if ((long long)row_blocks * ((p + 15) / 16) >= want) {
-        tall_gemm_kernel<16><<<dim3(row_blocks, (p + 15) / 16), kTallThreads, 0, stream>>>(
-            A, lda, B, ldb, C, ldc, n, m, p, alpha, beta);
+        tc = 16;
+        kernel = tall_gemm_kernel<16>;
     } else {
-        tall_gemm_kernel<8><<<dim3(row_blocks, (p + 7) / 8), kTallThreads, 0, stream>>>(
-            A, lda, B, ldb, C, ldc, n, m, p, alpha, beta);
+        tc = 8;
+        kernel = tall_gemm_kernel<8>;
     }
-    IPTGB_LAUNCH();
-    return IPT_CUDA_SUCCESS;
+    return launch_pdl(kernel, dim3(row_blocks, (p + tc - 1) / tc), dim3(kTallThreads), 0, stream,
+                      A, lda, B, ldb, C, ldc, n, m, p, alpha, beta);
 }
 
 // ---------------------------------------------------------------------------
@@ -488,6 +498,8 @@ __device__ void chol_inverse_block(const double *__restrict__ G, int m, double *
 __global__ void chol_inverse_kernel(const double *__restrict__ G, int m, double *__restrict__ Rinv,
                                     int *status, double *cond_bound)
 {
+    pdl_wait();  // programmatic dependent launch: predecessor done
+    pdl_trigger();
     extern __shared__ double sm[];
     chol_inverse_block(G, m, Rinv, status, sm);
     if (cond_bound != nullptr && threadIdx.x == 0) *cond_bound = NAN;  // not estimated here
@@ -538,6 +550,8 @@ __global__ void __launch_bounds__(1024)
     chol_inverse32x32_kernel(const double *__restrict__ G, int m, double *__restrict__ Rinv,
                              int *status, double *cond_bound)
 {
+    pdl_wait();  // programmatic dependent launch: predecessor done
+    pdl_trigger();
     typedef typename Ops::T T;
     __shared__ T col[32];      // the current column of L
     __shared__ T piv[2];       // pivot and its reciprocal
@@ -627,6 +641,8 @@ __global__ void residual_partial_kernel(const double *__restrict__ X, const doub
                                         double *__restrict__ R, int rows_per_block,
                                         double2 *__restrict__ P)
 {
+    pdl_wait();  // programmatic dependent launch: predecessor done
+    pdl_trigger();
     const int j = blockIdx.y;
     const int r0 = blockIdx.x * rows_per_block;
     const int r1 = min(n, r0 + rows_per_block);
@@ -652,6 +668,8 @@ __global__ void residual_finish_kernel(const double2 *__restrict__ P, int chunks
                                        double hnorm, double *__restrict__ rnorm,
                                        double *__restrict__ scaled)
 {
+    pdl_wait();  // programmatic dependent launch: predecessor done
+    pdl_trigger();
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= k) {
         return;
@@ -674,14 +692,10 @@ int BlockOps::residuals(const double *X, const double *AX, const double *theta, 
     const int rows_per_block = 2048;
     const int chunks = (n + rows_per_block - 1) / rows_per_block;
     IPTGB_CHECK(ensure_partials((size_t)chunks * k * 2));
-    residual_partial_kernel<<<dim3(chunks, k), 256, 0, stream>>>(X, AX, theta, n, ldx, R,
-                                                                 rows_per_block,
-                                                                 (double2 *)partials);
-    IPTGB_LAUNCH();
-    residual_finish_kernel<<<blocks_for(k), kThreads, 0, stream>>>((const double2 *)partials,
-                                                                   chunks, k, hnorm, rnorm,
-                                                                   scaled);
-    IPTGB_LAUNCH();
+    IPTGB_CHECK(launch_pdl(residual_partial_kernel, dim3(chunks, k), dim3(256), 0, stream, X, AX,
+                           theta, n, ldx, R, rows_per_block, (double2 *)partials));
+    IPTGB_CHECK(launch_pdl(residual_finish_kernel, dim3(blocks_for(k)), dim3(kThreads), 0, stream,
+                           (const double2 *)partials, chunks, k, hnorm, rnorm, scaled));
     return IPT_CUDA_SUCCESS;
 }
 
@@ -861,15 +875,8 @@ int BlockOps::chol_inverse(const double *G, int m, double *Rinv, int *status_dev
                            bool df)
 {
     if (m <= 32) {
-        if (df) {
-            chol_inverse32x32_kernel<CholDF><<<1, 1024, 0, stream>>>(G, m, Rinv, status_dev,
-                                                                     cond_bound);
-        } else {
-            chol_inverse32x32_kernel<CholF64><<<1, 1024, 0, stream>>>(G, m, Rinv, status_dev,
-                                                                      cond_bound);
-        }
-        IPTGB_LAUNCH();
-        return IPT_CUDA_SUCCESS;
+        return launch_pdl(df ? chol_inverse32x32_kernel<CholDF> : chol_inverse32x32_kernel<CholF64>,
+                          dim3(1), dim3(1024), 0, stream, G, m, Rinv, status_dev, cond_bound);
     }
     const size_t smem = 2 * (size_t)m * (size_t)m * sizeof(double);
     if (smem > 200 * 1024) {
@@ -877,9 +884,8 @@ int BlockOps::chol_inverse(const double *G, int m, double *Rinv, int *status_dev
     }
     IPTGB_CUDA(cudaFuncSetAttribute(chol_inverse_kernel,
                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    chol_inverse_kernel<<<1, 256, smem, stream>>>(G, m, Rinv, status_dev, cond_bound);
-    IPTGB_LAUNCH();
-    return IPT_CUDA_SUCCESS;
+    return launch_pdl(chol_inverse_kernel, dim3(1), dim3(256), smem, stream, G, m, Rinv,
+                      status_dev, cond_bound);
 }
 
 int BlockOps::ensure_partials(size_t count)

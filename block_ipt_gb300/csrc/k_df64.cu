@@ -30,6 +30,8 @@ constexpr int kDfChunk = 32;
 __global__ void df_split_kernel(const double *__restrict__ A, size_t count,
                                 float *__restrict__ hi, float *__restrict__ lo)
 {
+    pdl_wait();  // programmatic dependent launch: predecessor done
+    pdl_trigger();
     const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= count) return;
     const double a = A[e];
@@ -62,6 +64,8 @@ df64_partial_kernel(const float *__restrict__ Hh, const float *__restrict__ Hl, 
                     long long ldh, const float *__restrict__ Xh, const float *__restrict__ Xl,
                     long long ldx, int k, float2 *__restrict__ P, int kslice)
 {
+    pdl_wait();  // programmatic dependent launch: predecessor done
+    pdl_trigger();
     __shared__ float xsh[kDfChunk][BN];
     __shared__ float xsl[kDfChunk][BN];
     const int row = blockIdx.x * kDfRows + threadIdx.x;
@@ -120,6 +124,8 @@ df64_partial_kernel(const float *__restrict__ Hh, const float *__restrict__ Hl, 
 __global__ void df_sum_partials_kernel(const float2 *__restrict__ P, int S, size_t elems,
                                        double *__restrict__ Y)
 {
+    pdl_wait();  // programmatic dependent launch: predecessor done
+    pdl_trigger();
     const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= elems) return;
     const float2 p0 = P[idx];
@@ -134,16 +140,15 @@ __global__ void df_sum_partials_kernel(const float2 *__restrict__ P, int S, size
 int launch_df_sum_partials(const double *P, int S, size_t elems, double *Y, cudaStream_t stream)
 {
     if (S <= 0 || elems == 0) return IPT_CUDA_SUCCESS;
-    df_sum_partials_kernel<<<blocks_for(elems), kThreads, 0, stream>>>(
-        reinterpret_cast<const float2 *>(P), S, elems, Y);
-    IPTGB_LAUNCH();
+    IPTGB_CHECK(launch_pdl(df_sum_partials_kernel, dim3(blocks_for(elems)), dim3(kThreads), 0,
+                           stream, reinterpret_cast<const float2 *>(P), S, elems, Y));
     return IPT_CUDA_SUCCESS;
 }
 
 int launch_df_split(const double *A, size_t count, float *hi, float *lo, cudaStream_t stream)
 {
-    df_split_kernel<<<blocks_for(count), kThreads, 0, stream>>>(A, count, hi, lo);
-    IPTGB_LAUNCH();
+    IPTGB_CHECK(launch_pdl(df_split_kernel, dim3(blocks_for(count)), dim3(kThreads), 0, stream, A,
+                           count, hi, lo));
     return IPT_CUDA_SUCCESS;
 }
 
@@ -184,18 +189,11 @@ int launch_df64_partial(const float *Hh, const float *Hl, int n, long long ldh, 
     dim3 grid(row_blocks, S, (k + bn - 1) / bn);
     // the double-float partials (float2) fill the same bytes as FP64 ones
     float2 *P2 = reinterpret_cast<float2 *>(P);
-    if (bn == 8) {
-        df64_partial_kernel<8><<<grid, kDfRows, 0, stream>>>(Hh, Hl, n, ldh, Xh, Xl, ldx, k, P2,
-                                                             kslice);
-    } else if (bn == 16) {
-        df64_partial_kernel<16><<<grid, kDfRows, 0, stream>>>(Hh, Hl, n, ldh, Xh, Xl, ldx, k, P2,
-                                                              kslice);
-    } else {
-        df64_partial_kernel<32><<<grid, kDfRows, 0, stream>>>(Hh, Hl, n, ldh, Xh, Xl, ldx, k, P2,
-                                                              kslice);
-    }
-    IPTGB_LAUNCH();
-    return IPT_CUDA_SUCCESS;
+    auto kernel = bn == 8 ? df64_partial_kernel<8>
+                  : bn == 16 ? df64_partial_kernel<16>
+                             : df64_partial_kernel<32>;
+    return launch_pdl(kernel, grid, dim3(kDfRows), 0, stream, Hh, Hl, n, ldh, Xh, Xl, ldx, k, P2,
+                      kslice);
 }
 
 }  // namespace iptgb

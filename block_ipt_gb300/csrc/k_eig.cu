@@ -76,6 +76,8 @@ __global__ void eig_convert_kernel(const double *__restrict__ T, int m, double *
                                    float *__restrict__ Af, double *__restrict__ fro_part,
                                    double *__restrict__ mu_out)
 {
+    pdl_wait();  // programmatic dependent launch: predecessor done
+    pdl_trigger();
     __shared__ double mu_sh;
     const int tid = threadIdx.x;
     if (tid < 32) {
@@ -115,6 +117,8 @@ __global__ void __launch_bounds__(512)
 eig_tridiag_kernel(const float *__restrict__ Af, int m, float *__restrict__ vh,
                    float *__restrict__ tau, float *__restrict__ d, float *__restrict__ e)
 {
+    pdl_wait();  // programmatic dependent launch: predecessor done
+    pdl_trigger();
     extern __shared__ float A[];  // row-major, ld kEigPad
     __shared__ float vs[kEigMax];
     __shared__ float pp[4][kEigMax];
@@ -245,6 +249,8 @@ __global__ void __launch_bounds__(128)
 eig_tri_vectors_kernel(const float *__restrict__ dg, const float *__restrict__ eg, int m,
                        float *__restrict__ Y, int *info)
 {
+    pdl_wait();  // programmatic dependent launch: predecessor done
+    pdl_trigger();
     // Ys: the vectors, column-major with ld kEigPad (thread i's right-hand
     // side and solution live in column i); U0..U2: the U rows of every
     // thread's factorisation, element l of thread i at [l * m + i]
@@ -442,6 +448,8 @@ __global__ void __launch_bounds__(256)
 eig_backtransform_kernel(const float *__restrict__ Y, const float *__restrict__ vh,
                          const float *__restrict__ tau, int m, double *__restrict__ Z)
 {
+    pdl_wait();  // programmatic dependent launch: predecessor done
+    pdl_trigger();
     extern __shared__ float vs_all[];
     float *ts = vs_all + (size_t)m * m;
     for (int x = threadIdx.x; x < m * m; x += blockDim.x) vs_all[x] = vh[x];
@@ -501,6 +509,8 @@ struct SmallGemmJob {
 __global__ void __launch_bounds__(64)
 small_gemm64_kernel(SmallGemmJob j0, SmallGemmJob j1, int m)
 {
+    pdl_wait();  // programmatic dependent launch: predecessor done
+    pdl_trigger();
     __shared__ double As[8][kEigPad];
     __shared__ double Bs[kEigMax][9];
     __shared__ double red[2];
@@ -570,6 +580,8 @@ __global__ void oa_e_kernel(const double *__restrict__ G, const double *__restri
                             int ntiles, int m, double ebound, double *__restrict__ E,
                             double *__restrict__ lam)
 {
+    pdl_wait();  // programmatic dependent launch: predecessor done
+    pdl_trigger();
     __shared__ double delta_sh;
     const int tid = threadIdx.x;
     if (tid < 32) {
@@ -634,6 +646,8 @@ __global__ void __launch_bounds__(512)
 jacobi_polish_kernel(const double *__restrict__ T, int m, double *__restrict__ W,
                      int max_sweeps, int *applied)
 {
+    pdl_wait();  // programmatic dependent launch: predecessor done
+    pdl_trigger();
     extern __shared__ unsigned char sm_raw[];
     const int Mfull = (m + 1) & ~1;
     double *B = reinterpret_cast<double *>(sm_raw);  // row-major, ld C+1
@@ -790,6 +804,8 @@ __global__ void eig_sort_kernel(const double *__restrict__ lam, const double *__
                                 const double *__restrict__ Zin, int m, double *__restrict__ w,
                                 double *__restrict__ Zout)
 {
+    pdl_wait();  // programmatic dependent launch: predecessor done
+    pdl_trigger();
     __shared__ long long keys[kEigMax];
     __shared__ int rank_sh[kEigMax];
     const int tid = threadIdx.x;
@@ -854,42 +870,39 @@ int BlockOps::symmetric_eig(const double *T, int m, double *w, double *Z, int *i
 
     // 1. FP32 eigenvectors of T'
     const int cgrid = blocks_for(mm);
-    eig_convert_kernel<<<cgrid, kThreads, 0, stream>>>(T, m, Tp, Af, fro_part, mu_dev);
-    IPTGB_LAUNCH();
+    IPTGB_CHECK(launch_pdl(eig_convert_kernel, dim3(cgrid), dim3(kThreads), 0, stream, T, m, Tp, Af,
+                           fro_part, mu_dev));
     const size_t tri_smem = (size_t)m * kEigPad * sizeof(float);
     IPTGB_CUDA(cudaFuncSetAttribute(eig_tridiag_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     (int)tri_smem));
-    eig_tridiag_kernel<<<1, 512, tri_smem, stream>>>(Af, m, vh, tau, dg, eg);
-    IPTGB_LAUNCH();
+    IPTGB_CHECK(launch_pdl(eig_tridiag_kernel, dim3(1), dim3(512), tri_smem, stream, Af, m, vh,
+                           tau, dg, eg));
     const size_t vec_smem = tri_vectors_smem_bytes(m);
     IPTGB_CUDA(cudaFuncSetAttribute(eig_tri_vectors_kernel,
                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)vec_smem));
-    eig_tri_vectors_kernel<<<1, 128, vec_smem, stream>>>(dg, eg, m, Yf, info_dev);
-    IPTGB_LAUNCH();
+    IPTGB_CHECK(launch_pdl(eig_tri_vectors_kernel, dim3(1), dim3(128), vec_smem, stream, dg, eg, m,
+                           Yf, info_dev));
     const size_t bt_smem = ((size_t)m * m + m) * sizeof(float);
     IPTGB_CUDA(cudaFuncSetAttribute(eig_backtransform_kernel,
                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bt_smem));
-    eig_backtransform_kernel<<<(m + 7) / 8, 256, bt_smem, stream>>>(Yf, vh, tau, m, Z0);
-    IPTGB_LAUNCH();
+    IPTGB_CHECK(launch_pdl(eig_backtransform_kernel, dim3((m + 7) / 8), dim3(256), bt_smem, stream,
+                           Yf, vh, tau, m, Z0));
 
     // 2. FP64 refinement on T'
     const int tiles = (m + 7) / 8;
     const int ntiles = tiles * tiles;
     const int egrid = blocks_for(mm);
-    auto gemm = [&](SmallGemmJob a, SmallGemmJob b, int count) {
-        small_gemm64_kernel<<<dim3(tiles, tiles, count), 64, 0, stream>>>(a, b, m);
+    auto gemm = [&](SmallGemmJob a, SmallGemmJob b, int count) -> int {
+        return launch_pdl(small_gemm64_kernel, dim3(tiles, tiles, count), dim3(64), 0, stream, a,
+                          b, m);
     };
     auto refine_step = [&](double *cur, double *nxt, double ebound) -> int {
-        gemm({cur, cur, nullptr, G, 1, 1, nullptr, r_part},      // G = Z^T Z, ||R||
-             {Tp, cur, nullptr, TZ, 0, 0, nullptr, nullptr}, 2);  // TZ = T' Z
-        IPTGB_LAUNCH();
-        gemm({cur, TZ, nullptr, S, 1, 2, G, s_part}, {}, 1);      // S = Z^T T' Z
-        IPTGB_LAUNCH();
-        oa_e_kernel<<<egrid, kThreads, 0, stream>>>(G, S, fro_part, cgrid, r_part, s_part, ntiles,
-                                                    m, ebound, E, lam);
-        IPTGB_LAUNCH();
-        gemm({cur, E, cur, nxt, 0, 0, nullptr, nullptr}, {}, 1);  // Z <- Z + Z E
-        IPTGB_LAUNCH();
+        IPTGB_CHECK((gemm({cur, cur, nullptr, G, 1, 1, nullptr, r_part},      // G = Z^T Z, ||R||
+                          {Tp, cur, nullptr, TZ, 0, 0, nullptr, nullptr}, 2)));  // TZ = T' Z
+        IPTGB_CHECK((gemm({cur, TZ, nullptr, S, 1, 2, G, s_part}, {}, 1)));  // S = Z^T T' Z
+        IPTGB_CHECK(launch_pdl(oa_e_kernel, dim3(egrid), dim3(kThreads), 0, stream, G, S,
+                               fro_part, cgrid, r_part, s_part, ntiles, m, ebound, E, lam));
+        IPTGB_CHECK((gemm({cur, E, cur, nxt, 0, 0, nullptr, nullptr}, {}, 1)));  // Z <- Z + Z E
         return IPT_CUDA_SUCCESS;
     };
     // a rotation bound of a few 1e-3 keeps every applied update small; pairs
@@ -904,22 +917,19 @@ int BlockOps::symmetric_eig(const double *T, int m, double *w, double *Z, int *i
         nxt = t;
     }
     // 3. FP64 Jacobi polish of Z^T T' Z, folded into Z
-    gemm({Tp, cur, nullptr, TZ, 0, 0, nullptr, nullptr}, {}, 1);
-    IPTGB_LAUNCH();
-    gemm({cur, TZ, nullptr, S, 1, 0, nullptr, nullptr}, {}, 1);
-    IPTGB_LAUNCH();
+    IPTGB_CHECK((gemm({Tp, cur, nullptr, TZ, 0, 0, nullptr, nullptr}, {}, 1)));
+    IPTGB_CHECK((gemm({cur, TZ, nullptr, S, 1, 0, nullptr, nullptr}, {}, 1)));
     const size_t pol_smem = polish_smem_bytes(m);
     IPTGB_CUDA(cudaFuncSetAttribute(jacobi_polish_kernel,
                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pol_smem));
-    jacobi_polish_kernel<<<1, 512, pol_smem, stream>>>(S, m, W, 30, nullptr);
-    IPTGB_LAUNCH();
-    gemm({cur, W, nullptr, nxt, 0, 0, nullptr, nullptr}, {}, 1);
-    IPTGB_LAUNCH();
+    IPTGB_CHECK(launch_pdl(jacobi_polish_kernel, dim3(1), dim3(512), pol_smem, stream, S, m, W,
+                           30, nullptr));
+    IPTGB_CHECK((gemm({cur, W, nullptr, nxt, 0, 0, nullptr, nullptr}, {}, 1)));
     // 4. Rayleigh quotients of the polished vectors and one symmetric
     // re-orthogonalisation, then the sort
     IPTGB_CHECK(refine_step(nxt, cur, 0.0));
-    eig_sort_kernel<<<1, 256, 0, stream>>>(lam, mu_dev, cur, m, w, Z);
-    IPTGB_LAUNCH();
+    IPTGB_CHECK(launch_pdl(eig_sort_kernel, dim3(1), dim3(256), 0, stream, lam, mu_dev, cur, m, w,
+                           Z));
     return IPT_CUDA_SUCCESS;
 }
 

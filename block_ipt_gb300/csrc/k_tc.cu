@@ -38,19 +38,6 @@
 
 namespace iptgb {
 
-// Programmatic dependent launch: wait for the grids this one depends on
-// (a no-op when it was launched without the attribute), and let the next
-// grid in the stream be scheduled early.
-__device__ __forceinline__ void grid_dependency_wait()
-{
-    asm volatile("griddepcontrol.wait;" ::: "memory");
-}
-
-__device__ __forceinline__ void grid_launch_dependents()
-{
-    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
-}
-
 namespace tc {
 
 constexpr int kBM = 128;         // UMMA M: rows of Delta per CTA
@@ -213,7 +200,7 @@ tc_partial_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
     // the iteration already met its tolerance on the device: nothing to do
     // (the history is written by the previous update: wait for it first)
     if (hist != nullptr) {
-        grid_dependency_wait();
+        pdl_wait();
         if (hist_stopped(hist, step, stop_tol)) return;
     }
     extern __shared__ uint8_t smem_raw[];
@@ -280,7 +267,7 @@ tc_partial_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
                 tma_load_2d(sa, &tmA, kx, rb * kBM, full_bar(q));
             }
         }
-        grid_dependency_wait();
+        pdl_wait();
         for (int q = 0; q < pre; ++q) {
             const uint32_t sb = smem_base + (uint32_t)q * stage_bytes + a_bytes;
             tma_load_2d(sb, &tmB, (c0 + q) * kchunk_elems, 0, full_bar(q));
@@ -308,7 +295,7 @@ tc_partial_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
             tma_load_2d(sb, &tmB, kx, 0, full_bar(s));
         }
         issued_count = i;
-        grid_launch_dependents();
+        pdl_trigger();
     } else if (warp == 1 && lane == 0) {
         // ---- tcgen05.mma issuer ----
         for (int i = 0; i < nchunks; ++i) {
@@ -648,8 +635,8 @@ __global__ void lowp_update_kernel(const float *__restrict__ P, int S, int n, in
                                    double2 *partials, unsigned int *counter, double *norms,
                                    double *hist, int step, double stop_tol)
 {
-    grid_dependency_wait();  // P and X come from the previous grids
-    grid_launch_dependents();
+    pdl_wait();  // P and X come from the previous grids
+    pdl_trigger();
     // grid-stride over the block (a few CTAs per SM)
     const size_t elems = (size_t)n * (size_t)p;
     const size_t stride = (size_t)gridDim.x * blockDim.x;
@@ -722,8 +709,8 @@ __global__ void lowp_update4_kernel(const float *__restrict__ P, int S, int n, i
                                     double2 *partials, unsigned int *counter, double *norms,
                                     double *hist, int step, double stop_tol)
 {
-    grid_dependency_wait();  // P and X come from the previous grids
-    grid_launch_dependents();
+    pdl_wait();  // P and X come from the previous grids
+    pdl_trigger();
     const int nq = n >> 2;
     const int total = nq * p;
     const int stride = gridDim.x * blockDim.x;
@@ -823,8 +810,8 @@ __global__ void refine_update_kernel(const float *__restrict__ P, int S, int n, 
                                      int want_norms, double2 *partials, unsigned int *counter,
                                      double *norms, double *hist, int step, double stop_tol)
 {
-    grid_dependency_wait();  // P and X come from the previous grids
-    grid_launch_dependents();
+    pdl_wait();  // P and X come from the previous grids
+    pdl_trigger();
     const size_t elems = (size_t)n * (size_t)p;
     const size_t stride = (size_t)gridDim.x * blockDim.x;
     if (hist_stopped(hist, step, stop_tol)) {
@@ -886,8 +873,8 @@ __global__ void refine_update4_kernel(const float *__restrict__ P, int S, int n,
                                       double2 *partials, unsigned int *counter, double *norms,
                                       double *hist, int step, double stop_tol)
 {
-    grid_dependency_wait();  // P and X come from the previous grids
-    grid_launch_dependents();
+    pdl_wait();  // P and X come from the previous grids
+    pdl_trigger();
     const int nq = n >> 2;
     const int total = nq * p;
     const int stride = gridDim.x * blockDim.x;
@@ -963,29 +950,6 @@ __global__ void refine_apply_kernel(double *__restrict__ X, const float *__restr
 // ---------------------------------------------------------------------------
 namespace {
 
-// Launch with programmatic stream serialisation: the kernel may start while
-// its predecessor in the stream finishes; it calls grid_dependency_wait()
-// before reading the predecessor's results.  Tuning knob IPT_GB300_PDL=0
-// launches in plain stream order.
-template <typename... KArgs, typename... Args>
-int launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
-               Args &&...args)
-{
-    static const bool on = env_int("IPT_GB300_PDL", 1) != 0;
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = grid;
-    cfg.blockDim = block;
-    cfg.dynamicSmemBytes = smem;
-    cfg.stream = s;
-    cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-    attr[0].val.programmaticStreamSerializationAllowed = on ? 1 : 0;
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
-    IPTGB_CUDA(cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...));
-    count_launch();
-    return IPT_CUDA_SUCCESS;
-}
 
 typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
                                   const cuuint64_t *, const cuuint64_t *, const cuuint32_t *,

@@ -56,6 +56,8 @@ __global__ void defect_partial_kernel(const double *__restrict__ X, const double
                                       double *__restrict__ R0, double *__restrict__ c_out,
                                       double *__restrict__ P, int lowp_rhs)
 {
+    pdl_wait();  // programmatic dependent launch: predecessor done
+    pdl_trigger();
     __shared__ double smax[32];
     const int j = blockIdx.y;
     const size_t dj = (size_t)j + (size_t)j * n;
@@ -108,6 +110,8 @@ __global__ void defect_partial_kernel(const double *__restrict__ X, const double
 __global__ void defect_finish_kernel(const double *__restrict__ P, int chunks, int k, double hnorm,
                                      double *__restrict__ scaled, double *__restrict__ colmax)
 {
+    pdl_wait();  // programmatic dependent launch: predecessor done
+    pdl_trigger();
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= k) return;
     double rs = 0.0, xs = 0.0, mx = 0.0;
@@ -224,12 +228,11 @@ int refine_solve(const RefineInput &in, double *X_out, double *values_out, IPTBl
         IPTGB_CHECK(in.apply->apply(X.ptr, k, HX.ptr));
         trace_mark("refine:defect_product_done", s);
         rep->fp64_matvecs += k;
-        defect_partial_kernel<<<dim3(chunks, k), 256, 0, s>>>(X.ptr, HX.ptr, in.d, n, k, R0.ptr, c,
-                                                              P, in.lowp != nullptr ? 1 : 0);
-        IPTGB_LAUNCH();
-        defect_finish_kernel<<<blocks_for(k), kThreads, 0, s>>>(P, chunks, k, in.hnorm, scaled,
-                                                               colmax);
-        IPTGB_LAUNCH();
+        IPTGB_CHECK(launch_pdl(defect_partial_kernel, dim3(chunks, k), dim3(256), 0, s,
+                               (const double *)X.ptr, (const double *)HX.ptr, in.d, n, k, R0.ptr,
+                               c, P, in.lowp != nullptr ? 1 : 0));
+        IPTGB_CHECK(launch_pdl(defect_finish_kernel, dim3(blocks_for(k)), dim3(kThreads), 0, s,
+                               (const double *)P, chunks, k, in.hnorm, scaled, colmax));
         IPTGB_CUDA(cudaMemcpyAsync(h_scaled.data(), scaled, (size_t)k * sizeof(double),
                                    cudaMemcpyDeviceToHost, s));
         IPTGB_CUDA(cudaMemcpyAsync(h_colmax.data(), colmax, (size_t)k * sizeof(double),
