@@ -201,12 +201,6 @@ IptStage *make_fp64_csr_stage(const int *row_ptr, const int *col_ind, const doub
 // permutation is needed).  One warp per column reads the contiguous column;
 // one 24-byte read brings the results to the host.
 // ---------------------------------------------------------------------------
-struct DenseStats {
-    unsigned long long hnorm_bits;   // non-negative doubles order like their bit patterns
-    unsigned long long maxabs_bits;
-    unsigned long long descents;
-};
-
 constexpr int kStatsWarps = 8;
 
 // One entry of the statistics: |h| added to the double-float column sum
@@ -418,8 +412,13 @@ bool options_valid(const IPTBlockOptions *o)
 
 }  // namespace
 
+// host_src (optional): a device-accessible pointer to H in pinned host
+// memory; dH_in is then an uninitialised device buffer that the solve fills
+// (the fused setup pass reads the host copy once, at the host link's speed,
+// and writes everything it derives from H in the same pass).
 int dense_block_device(const double *dH_in, int n, int k, const IPTBlockOptions *options,
-                       double *d_vectors, double *d_values, IPTBlockReport *report)
+                       double *d_vectors, double *d_values, IPTBlockReport *report,
+                       const double *host_src = nullptr)
 {
     IPTBlockOptions opt;
     if (options != nullptr) {
@@ -439,13 +438,65 @@ int dense_block_device(const double *dH_in, int n, int k, const IPTBlockOptions 
     DeviceBuffer<int> dperm;
     trace_mark("dense:start", s);
     IPTGB_CHECK(d.alloc((size_t)n, s));
-    // one pass: diagonal, max off-diagonal, sortedness of the diagonal, and
-    // (plain FP64 solve) hnorm; the mixed solve's conversion pass forms the
-    // column sums for hnorm itself
     const bool lowp_mode = opt.ipt_precision != IPT_BLOCK_FP64;
+    const int kind = opt.ipt_precision == IPT_BLOCK_FP16 ? kLowpF16
+                     : opt.ipt_precision == IPT_BLOCK_BF16 ? kLowpBF16
+                                                           : kLowpTF32;
     double hnorm = 0.0, maxabs_off = 0.0;
     unsigned long long descents = 0;
-    IPTGB_CHECK(dense_stats(dH_in, n, d.ptr, s, &hnorm, &maxabs_off, &descents, !lowp_mode));
+    // The mixed-precision solve forms its FP64-accurate products in
+    // double-FP32 arithmetic (one split of H per solve); the plain FP64
+    // path keeps FP64 FMAs throughout.
+    DeviceBuffer<float> Hsplit;
+    const size_t mat = (size_t)n * n;
+    if (lowp_mode && !env_flag("IPT_GB300_FP64_DFMA", 0)) {
+        IPTGB_CHECK(Hsplit.alloc(2 * mat, s));
+    }
+    std::unique_ptr<LowpDenseOperator> lowp;
+    int st = IPT_CUDA_SUCCESS;
+    // Mixed solve, n <= kFusedSetupMaxN: one fused pass builds Delta (row
+    // scales of its own), the split, the diagonal and the statistics straight
+    // from H (or from the host copy); an unsorted diagonal falls back to the
+    // permuted path below.  Tuning knob IPT_GB300_FUSED_SETUP=0 disables it.
+    bool fused = false, have_device_copy = host_src == nullptr;
+    if (lowp_mode && n <= kFusedSetupMaxN && env_int("IPT_GB300_FUSED_SETUP", 1) != 0) {
+        DeviceBuffer<DenseStats> stats;
+        IPTGB_CHECK(stats.alloc(1, s));
+        IPTGB_CUDA(cudaMemsetAsync(stats.ptr, 0, sizeof(DenseStats), s));
+        LowpDenseSetup su;
+        su.symmetric = true;
+        su.split_hi = Hsplit.ptr;
+        su.split_lo = Hsplit.ptr ? Hsplit.ptr + mat : nullptr;
+        su.fused_src = host_src != nullptr ? host_src : dH_in;
+        su.fused_copy = host_src != nullptr ? const_cast<double *>(dH_in) : nullptr;
+        su.diag = d.ptr;
+        su.stats = stats.ptr;
+        lowp.reset(make_lowp_dense_operator(dH_in, n, kind, s, &st, &su));
+        if (lowp == nullptr) {
+            return st != IPT_CUDA_SUCCESS ? st : IPT_CUDA_INVALID_ARGUMENT;
+        }
+        if (su.fused_done) {
+            have_device_copy = true;
+            DenseStats h;
+            IPTGB_CUDA(cudaMemcpyAsync(&h, stats.ptr, sizeof(h), cudaMemcpyDeviceToHost, s));
+            IPTGB_CUDA(cudaStreamSynchronize(s));
+            memcpy(&hnorm, &h.hnorm_bits, sizeof(double));
+            memcpy(&maxabs_off, &h.maxabs_bits, sizeof(double));
+            descents = h.descents;
+            fused = descents == 0;
+        }
+        if (!fused) lowp.reset();
+    }
+    if (!have_device_copy) {
+        IPTGB_CUDA(cudaMemcpyAsync(const_cast<double *>(dH_in), host_src, mat * sizeof(double),
+                                   cudaMemcpyDefault, s));
+    }
+    if (!fused) {
+        // one pass: diagonal, max off-diagonal, sortedness of the diagonal, and
+        // (plain FP64 solve) hnorm; the mixed solve's conversion pass forms the
+        // column sums for hnorm itself
+        IPTGB_CHECK(dense_stats(dH_in, n, d.ptr, s, &hnorm, &maxabs_off, &descents, !lowp_mode));
+    }
     trace_mark("dense:stats_done", s);
     const double *dH = dH_in;
     const bool permuted = descents > 0;
@@ -479,22 +530,14 @@ int dense_block_device(const double *dH_in, int n, int k, const IPTBlockOptions 
     apply.sms = device_sm_count();
     apply.s = s;
     std::unique_ptr<IptStage> stage;
-    std::unique_ptr<LowpDenseOperator> lowp;
-    int st = IPT_CUDA_SUCCESS;
-    // The mixed-precision solve forms its FP64-accurate products in
-    // double-FP32 arithmetic (one split of H per solve); the plain FP64
-    // path keeps FP64 FMAs throughout.
-    DeviceBuffer<float> Hsplit;
-    const size_t mat = (size_t)n * n;
-    if (lowp_mode && !env_flag("IPT_GB300_FP64_DFMA", 0)) {
-        IPTGB_CHECK(Hsplit.alloc(2 * mat, s));
+    if (Hsplit.ptr != nullptr) {
         apply.Hh = Hsplit.ptr;
         apply.Hl = Hsplit.ptr + mat;
     }
-    if (lowp_mode) {
-        const int kind = opt.ipt_precision == IPT_BLOCK_FP16 ? kLowpF16
-                         : opt.ipt_precision == IPT_BLOCK_BF16 ? kLowpBF16
-                                                               : kLowpTF32;
+    if (lowp_mode && fused) {
+        trace_mark("dense:operator_done", s);
+        stage.reset(make_lowp_stage_on(lowp.get(), d.ptr, n, s));
+    } else if (lowp_mode) {
         // one pass over H writes the low-precision Delta, the double-FP32
         // split and the partial column sums of |H|
         DeviceBuffer<double> colpart;
@@ -832,10 +875,22 @@ IPT_API int ipt_block_solve_dense(const double *matrix_col_major, int n, int k,
     IPTGB_CHECK(dX.alloc((size_t)n * k, s));
     IPTGB_CHECK(dv.alloc((size_t)k, s));
     trace_mark("host_dense:allocated", s);
-    IPTGB_CUDA(cudaMemcpyAsync(dH.ptr, matrix_col_major, mat * sizeof(double),
-                               cudaMemcpyHostToDevice, s));
+    // Pinned (page-locked) host memory is readable by the GPU: the solve's
+    // first pass then reads H over the host link itself and derives everything
+    // it needs on the way (no separate copy, then pass).  Pageable memory is
+    // copied first.
+    cudaPointerAttributes attr;
+    const double *host_src = nullptr;
+    if (cudaPointerGetAttributes(&attr, matrix_col_major) == cudaSuccess &&
+        attr.type == cudaMemoryTypeHost && attr.devicePointer != nullptr) {
+        host_src = static_cast<const double *>(attr.devicePointer);
+    } else {
+        cudaGetLastError();  // clear a pageable-pointer query error, if any
+        IPTGB_CUDA(cudaMemcpyAsync(dH.ptr, matrix_col_major, mat * sizeof(double),
+                                   cudaMemcpyHostToDevice, s));
+    }
     trace_mark("host_dense:h2d_done", s);
-    IPTGB_CHECK(dense_block_device(dH.ptr, n, k, &opt, dX.ptr, dv.ptr, report));
+    IPTGB_CHECK(dense_block_device(dH.ptr, n, k, &opt, dX.ptr, dv.ptr, report, host_src));
     IPTGB_CUDA(cudaMemcpyAsync(vectors, dX.ptr, (size_t)n * k * sizeof(double),
                                cudaMemcpyDeviceToHost, s));
     IPTGB_CUDA(cudaMemcpyAsync(values, dv.ptr, (size_t)k * sizeof(double), cudaMemcpyDeviceToHost,

@@ -558,6 +558,137 @@ __global__ void __launch_bounds__(256)
     }
 }
 
+// Fused setup of a symmetric H: one CTA per column c (= row c of Delta).
+// Pass 0 stages the column in shared memory and finds its largest
+// off-diagonal |h| (integer max of the bit patterns); the row's FP16 scale is
+// the largest power of two 2^s2 with 2^s2 max <= 16384 (BF16/TF32: 1).
+// Pass 1 writes row c of Delta, the double-FP32 split of column c, optionally
+// the FP64 column (when the source is host memory), and forms the exact
+// double-float column sum.  The CTA's thread 0 then stores 2^-s2, the
+// diagonal entry, the column sum (atomic max: hnorm), its maximum and whether
+// d_{c+1} < d_c.  No FP64 arithmetic per entry (the conversions run on the
+// integer pipe), so the pass streams at memory (or host link) speed.
+template <typename LP>
+__global__ void __launch_bounds__(256)
+    fused_setup_kernel(const double *__restrict__ src, int n, int ldp, int fp16_scale,
+                       double *__restrict__ copy, LP *__restrict__ delta, float *__restrict__ hi,
+                       float *__restrict__ lo, float *__restrict__ inv_row,
+                       double *__restrict__ diag, DenseStats *__restrict__ stats, int vec)
+{
+    extern __shared__ __align__(16) double colbuf[];  // n doubles
+    __shared__ unsigned long long wmax[8];
+    __shared__ float wS[8], wC[8];
+    __shared__ int s2_sh;
+    const int c = blockIdx.x;
+    const int tid = threadIdx.x;
+    const double *scol = src + (size_t)c * n;
+    unsigned long long m = 0;
+    if (vec) {  // n even, src 16-byte aligned
+        const double2 *s2v = reinterpret_cast<const double2 *>(scol);
+        for (int q = tid; q < n / 2; q += 256) {
+            const double2 v = s2v[q];
+            reinterpret_cast<double2 *>(colbuf)[q] = v;
+            const int l = 2 * q;
+            const unsigned long long a0 =
+                (unsigned long long)__double_as_longlong(v.x) & 0x7FFFFFFFFFFFFFFFULL;
+            const unsigned long long a1 =
+                (unsigned long long)__double_as_longlong(v.y) & 0x7FFFFFFFFFFFFFFFULL;
+            if (l != c && a0 > m) m = a0;
+            if (l + 1 != c && a1 > m) m = a1;
+        }
+    } else {
+        for (int l = tid; l < n; l += 256) {
+            const double v = scol[l];
+            colbuf[l] = v;
+            const unsigned long long a =
+                (unsigned long long)__double_as_longlong(v) & 0x7FFFFFFFFFFFFFFFULL;
+            if (l != c && a > m) m = a;
+        }
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+        const unsigned long long o = __shfl_xor_sync(0xffffffffu, m, off);
+        if (o > m) m = o;
+    }
+    if ((tid & 31) == 0) wmax[tid >> 5] = m;
+    __syncthreads();
+    if (tid == 0) {
+        unsigned long long mx = 0;
+        for (int w = 0; w < 8; ++w) mx = wmax[w] > mx ? wmax[w] : mx;
+        wmax[0] = mx;
+        int s2 = 0;
+        const double mv = __longlong_as_double((long long)mx);
+        if (fp16_scale && mv > 0.0 && isfinite(mv)) {
+            s2 = (int)floor(log2(16384.0 / mv));
+            s2 = min(max(s2, -40), 40);
+        }
+        s2_sh = s2;
+    }
+    __syncthreads();
+    const int s2 = s2_sh;
+    const double scale = ldexp(1.0, s2);
+    LP *orow = delta + (size_t)c * ldp;
+    float S = 0.0f, C = 0.0f;
+    for (int l = 2 * tid; l < ldp; l += 512) {  // ldp is a multiple of 64: l + 1 < ldp
+        const double h0 = l < n ? colbuf[l] : 0.0;
+        const double h1 = l + 1 < n ? colbuf[l + 1] : 0.0;
+        float a0, a1, b0, b1;
+        float v0 = sym_entry(h0, s2, scale, a0, b0);
+        float v1 = sym_entry(h1, s2, scale, a1, b1);
+        if (!(l < n && l != c)) v0 = 0.0f;
+        if (!(l + 1 < n && l + 1 != c)) v1 = 0.0f;
+        *reinterpret_cast<LpPair<LP> *>(orow + l) = LpPair<LP>{to_lp<LP>(v0), to_lp<LP>(v1)};
+        df_abs_add(S, C, a0, b0);  // entries beyond n are zero
+        df_abs_add(S, C, a1, b1);
+        const size_t o = (size_t)c * n + l;
+        if (vec && l + 1 < n) {
+            if (hi != nullptr) {
+                *reinterpret_cast<float2 *>(hi + o) = make_float2(a0, a1);
+                *reinterpret_cast<float2 *>(lo + o) = make_float2(b0, b1);
+            }
+            if (copy != nullptr) *reinterpret_cast<double2 *>(copy + o) = make_double2(h0, h1);
+        } else {
+            if (l < n) {
+                if (hi != nullptr) {
+                    hi[o] = a0;
+                    lo[o] = b0;
+                }
+                if (copy != nullptr) copy[o] = h0;
+            }
+            if (l + 1 < n) {
+                if (hi != nullptr) {
+                    hi[o + 1] = a1;
+                    lo[o + 1] = b1;
+                }
+                if (copy != nullptr) copy[o + 1] = h1;
+            }
+        }
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+        df_pair_add(S, C, __shfl_xor_sync(0xffffffffu, S, off),
+                    __shfl_xor_sync(0xffffffffu, C, off));
+    }
+    if ((tid & 31) == 0) {
+        wS[tid >> 5] = S;
+        wC[tid >> 5] = C;
+    }
+    __syncthreads();
+    if (tid == 0) {
+        float St = wS[0], Ct = wC[0];
+        for (int w = 1; w < 8; ++w) df_pair_add(St, Ct, wS[w], wC[w]);
+        const double colsum = (double)St + (double)Ct;
+        if (colsum > 0.0) {
+            atomicMax(&stats->hnorm_bits, (unsigned long long)__double_as_longlong(colsum));
+        }
+        if (wmax[0] > 0) atomicMax(&stats->maxabs_bits, wmax[0]);
+        const double dc = colbuf[c];
+        diag[c] = dc;
+        if (c + 1 < n && src[(size_t)(c + 1) * ((size_t)n + 1)] < dc) {
+            atomicAdd(&stats->descents, 1ULL);
+        }
+        inv_row[c] = (float)ldexp(1.0, -s2);
+    }
+}
+
 __global__ void max_abs_offdiag_kernel(const double *__restrict__ H, int n,
                                        unsigned long long *out)
 {
@@ -629,7 +760,8 @@ __device__ __forceinline__ void hist_add(double *hist, int step, double2 t)
 // c_j = (Delta X)_jj is read straight from the product.
 template <typename LP>
 __global__ void lowp_update_kernel(const float *__restrict__ P, int S, int n, int p,
-                                   float inv_scale, const float *__restrict__ G,
+                                   float inv_scale, const float *__restrict__ inv_row,
+                                   const float *__restrict__ G,
                                    const float *__restrict__ X, float *__restrict__ Xn,
                                    LP *__restrict__ Xlp, int ldx, int want_norms,
                                    double2 *partials, unsigned int *counter, double *norms,
@@ -665,7 +797,9 @@ __global__ void lowp_update_kernel(const float *__restrict__ P, int S, int n, in
                 y += P[base + row];
                 c += P[base + col];
             }
-            out = (y * inv_scale - x * (c * inv_scale)) * G[idx];
+            const float ir = inv_row != nullptr ? inv_row[row] : inv_scale;
+            const float ic = inv_row != nullptr ? inv_row[col] : inv_scale;
+            out = (y * ir - x * (c * ic)) * G[idx];
         }
         Xn[idx] = out;
         Xlp[(size_t)row + (size_t)col * ldx] = to_lp<LP>(out);
@@ -703,7 +837,8 @@ __device__ __forceinline__ float &f4_at(float4 &v, int i)
 
 template <typename LP>
 __global__ void lowp_update4_kernel(const float *__restrict__ P, int S, int n, int p,
-                                    float inv_scale, const float *__restrict__ G,
+                                    float inv_scale, const float *__restrict__ inv_row,
+                                    const float *__restrict__ G,
                                     const float *__restrict__ X, float *__restrict__ Xn,
                                     LP *__restrict__ Xlp, int ldx, int want_norms,
                                     double2 *partials, unsigned int *counter, double *norms,
@@ -742,12 +877,15 @@ __global__ void lowp_update4_kernel(const float *__restrict__ P, int S, int n, i
         }
         const float4 x = *reinterpret_cast<const float4 *>(X + e);
         const float4 g = *reinterpret_cast<const float4 *>(G + e);
-        const float ci = c * inv_scale;
+        const float4 ir = inv_row != nullptr
+                              ? *reinterpret_cast<const float4 *>(inv_row + row0)
+                              : make_float4(inv_scale, inv_scale, inv_scale, inv_scale);
+        const float ci = c * (inv_row != nullptr ? inv_row[col] : inv_scale);
         float4 o;
-        o.x = (y.x * inv_scale - x.x * ci) * g.x;
-        o.y = (y.y * inv_scale - x.y * ci) * g.y;
-        o.z = (y.z * inv_scale - x.z * ci) * g.z;
-        o.w = (y.w * inv_scale - x.w * ci) * g.w;
+        o.x = (y.x * ir.x - x.x * ci) * g.x;
+        o.y = (y.y * ir.y - x.y * ci) * g.y;
+        o.z = (y.z * ir.z - x.z * ci) * g.z;
+        o.w = (y.w * ir.w - x.w * ci) * g.w;
         if (col >= row0 && col < row0 + 4) f4_at(o, col - row0) = 1.0f;  // X_jj = 1
         *reinterpret_cast<float4 *>(Xn + e) = o;
         *reinterpret_cast<LpQuad<LP> *>(Xlp + (size_t)col * ldx + row0) =
@@ -802,7 +940,8 @@ __global__ void refine_begin_kernel(const double *__restrict__ R0, const double 
 
 template <typename LP>
 __global__ void refine_update_kernel(const float *__restrict__ P, int S, int n, int p,
-                                     float inv_scale, const float *__restrict__ sig,
+                                     float inv_scale, const float *__restrict__ inv_row,
+                                     const float *__restrict__ sig,
                                      const float *__restrict__ sig_inv, const float *__restrict__ G,
                                      const float *__restrict__ R32, const float *__restrict__ X32,
                                      const float *__restrict__ c32, const float *__restrict__ dcur,
@@ -840,9 +979,10 @@ __global__ void refine_update_kernel(const float *__restrict__ P, int S, int n, 
                 y += P[base + row];
                 b += P[base + col];
             }
-            const float sc = inv_scale * sig_inv[col];
-            y *= sc;
-            b *= sc;
+            const float ir = inv_row != nullptr ? inv_row[row] : inv_scale;
+            const float ic = inv_row != nullptr ? inv_row[col] : inv_scale;
+            y *= ir * sig_inv[col];
+            b *= ic * sig_inv[col];
             out = R32[idx] + (y - X32[idx] * b - cur * (c32[col] + b)) * G[idx];
         }
         dnext[idx] = out;
@@ -864,7 +1004,8 @@ __global__ void refine_update_kernel(const float *__restrict__ P, int S, int n, 
 // refine_update_kernel with four consecutive rows per thread (n % 4 == 0).
 template <typename LP>
 __global__ void refine_update4_kernel(const float *__restrict__ P, int S, int n, int p,
-                                      float inv_scale, const float *__restrict__ sig,
+                                      float inv_scale, const float *__restrict__ inv_row,
+                                      const float *__restrict__ sig,
                                       const float *__restrict__ sig_inv,
                                       const float *__restrict__ G, const float *__restrict__ R32,
                                       const float *__restrict__ X32, const float *__restrict__ c32,
@@ -906,9 +1047,12 @@ __global__ void refine_update4_kernel(const float *__restrict__ P, int S, int n,
             y = f4_add(y, *reinterpret_cast<const float4 *>(base + row0));
             b += base[col];
         }
-        const float sc = inv_scale * sig_inv[col];
-        y = make_float4(y.x * sc, y.y * sc, y.z * sc, y.w * sc);
-        b *= sc;
+        const float4 ir = inv_row != nullptr
+                              ? *reinterpret_cast<const float4 *>(inv_row + row0)
+                              : make_float4(inv_scale, inv_scale, inv_scale, inv_scale);
+        const float si = sig_inv[col];
+        y = make_float4(y.x * (ir.x * si), y.y * (ir.y * si), y.z * (ir.z * si), y.w * (ir.w * si));
+        b *= (inv_row != nullptr ? inv_row[col] : inv_scale) * si;
         const float cb = c32[col] + b;
         const float4 cur = *reinterpret_cast<const float4 *>(dcur + e);
         const float4 r = *reinterpret_cast<const float4 *>(R32 + e);
@@ -1053,6 +1197,32 @@ struct LowpDense final : LowpDenseOperator {
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         ldp = ((n + 63) / 64) * 64;
         IPTGB_CHECK(delta.alloc((size_t)n * ldp, s));
+        if (su.fused_src != nullptr && symmetric && n <= kFusedSetupMaxN && su.diag != nullptr &&
+            su.stats != nullptr) {
+            IPTGB_CHECK(inv_rows.alloc((size_t)n, s));
+            const size_t smem = (size_t)n * sizeof(double);
+            auto kfn = fused_setup_kernel<LP>;
+            IPTGB_CUDA(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            (int)smem));
+            const int vec = (n % 2 == 0) &&
+                            ((reinterpret_cast<uintptr_t>(su.fused_src) & 15) == 0) &&
+                            ((reinterpret_cast<uintptr_t>(split_hi) & 7) == 0) &&
+                            ((reinterpret_cast<uintptr_t>(split_lo) & 7) == 0) &&
+                            ((reinterpret_cast<uintptr_t>(su.fused_copy) & 15) == 0);
+            kfn<<<n, 256, smem, s>>>(su.fused_src, n, ldp,
+                                     LowpTypes<LP>::kind == kLowpF16 ? 1 : 0, su.fused_copy,
+                                     delta.ptr, split_hi, split_lo, inv_rows.ptr, su.diag,
+                                     su.stats, vec);
+            IPTGB_LAUNCH();
+            scale = 1.0;  // per-row scales in inv_rows
+            su.fused_done = true;
+            su.split_done = split_hi != nullptr;
+            IPTGB_CHECK(make_map(&mapA, LowpTypes<LP>::dt, esize, delta.ptr, ldp, n, tc::kBM));
+            IPTGB_CHECK(err.alloc(1, s));
+            IPTGB_CUDA(cudaMemsetAsync(err.ptr, 0, sizeof(int), s));
+            set_l2_keep(dev);
+            return IPT_CUDA_SUCCESS;
+        }
         double maxabs = su.maxabs;
         if (!(maxabs >= 0.0)) {
             DeviceBuffer<unsigned long long> mx;
@@ -1092,24 +1262,27 @@ struct LowpDense final : LowpDenseOperator {
         }
         IPTGB_LAUNCH();
         IPTGB_CHECK(make_map(&mapA, LowpTypes<LP>::dt, esize, delta.ptr, ldp, n, tc::kBM));
-        // Delta is streamed once per product; when it is larger than about
-        // half of L2, that share of it is marked evict_last so that it stays
-        // resident across the products (the rest evict_first).  Measured at
-        // n = 8192 (FP16 Delta 134 MB): keeping 40-55% of Delta gives the
-        // fastest solve; more than 60% thrashes again.
-        {
-            int l2 = 0;
-            cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, dev);
-            const double bytes = (double)n * (double)ldp * esize;
-            const double keep_bytes = 0.45 * (double)l2;
-            a_keep = bytes > keep_bytes && l2 > 0 ? (float)(keep_bytes / bytes) : 0.0f;
-            // tuning knob: IPT_GB300_L2_KEEP_PCT overrides the fraction (0 = no hint)
-            const int pct = env_int("IPT_GB300_L2_KEEP_PCT", -1);
-            if (pct >= 0) a_keep = std::min(pct, 100) / 100.0f;
-        }
+        set_l2_keep(dev);
         IPTGB_CHECK(err.alloc(1, s));
         IPTGB_CUDA(cudaMemsetAsync(err.ptr, 0, sizeof(int), s));
         return IPT_CUDA_SUCCESS;
+    }
+
+    // Delta is streamed once per product; when it is larger than about
+    // half of L2, that share of it is marked evict_last so that it stays
+    // resident across the products (the rest evict_first).  Measured at
+    // n = 8192 (FP16 Delta 134 MB): keeping 40-55% of Delta gives the
+    // fastest solve; more than 60% thrashes again.
+    void set_l2_keep(int dev)
+    {
+        int l2 = 0;
+        cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, dev);
+        const double bytes = (double)n * (double)ldp * esize;
+        const double keep_bytes = 0.45 * (double)l2;
+        a_keep = bytes > keep_bytes && l2 > 0 ? (float)(keep_bytes / bytes) : 0.0f;
+        // tuning knob: IPT_GB300_L2_KEEP_PCT overrides the fraction (0 = no hint)
+        const int pct = env_int("IPT_GB300_L2_KEEP_PCT", -1);
+        if (pct >= 0) a_keep = std::min(pct, 100) / 100.0f;
     }
 
     int set_width(int p_) override
@@ -1214,7 +1387,8 @@ struct LowpDense final : LowpDenseOperator {
         KernelTimerScope timer(kProfLowpUpdate, s);
         IPTGB_CHECK(launch_pdl(n % 4 == 0 ? lowp_update4_kernel<LP> : lowp_update_kernel<LP>,
                                dim3(grid), dim3(kThreads), 0, s, (const float *)P.ptr, splits, n,
-                               p, (float)(1.0 / scale), (const float *)G.ptr,
+                               p, (float)(1.0 / scale), (const float *)inv_rows.ptr,
+                               (const float *)G.ptr,
                                (const float *)X32[cur].ptr, X32[nxt].ptr, Xlp[nxt].ptr, ldp,
                                want_norms, ns->partials, ns->counter, ns->norms, hist, hstep,
                                ns->stop_tol));
@@ -1278,7 +1452,8 @@ struct LowpDense final : LowpDenseOperator {
         KernelTimerScope timer(kProfLowpUpdate, s);
         IPTGB_CHECK(launch_pdl(n % 4 == 0 ? refine_update4_kernel<LP> : refine_update_kernel<LP>,
                                dim3(grid), dim3(kThreads), 0, s, (const float *)P.ptr, splits, n,
-                               p, (float)(1.0 / scale), (const float *)(small.ptr + p),
+                               p, (float)(1.0 / scale), (const float *)inv_rows.ptr,
+                               (const float *)(small.ptr + p),
                                (const float *)(small.ptr + 2 * p), (const float *)G.ptr,
                                (const float *)R32.ptr, (const float *)Xref32.ptr,
                                (const float *)small.ptr, (const float *)X32[cur].ptr,
@@ -1307,6 +1482,9 @@ struct LowpDense final : LowpDenseOperator {
     uint32_t idesc = 0;
     double scale = 1.0;
     float a_keep = 0.0f;  // fraction of Delta kept in L2 (evict_last) across products
+    // per-row 1/scale of Delta (row i scaled by its own power of two) when the
+    // fused setup pass built Delta; empty: one scale for the whole matrix
+    DeviceBuffer<float> inv_rows;
     cudaStream_t s = nullptr;
     DeviceBuffer<LP> delta;
     DeviceBuffer<LP> Xlp[2];
@@ -1383,7 +1561,7 @@ struct LowpDenseSimtF32 final : LowpDenseOperator {
         const int nxt = cur ^ 1;
         KernelTimerScope timer(kProfLowpUpdate, s);
         lowp_update_kernel<float><<<grid, kThreads, 0, s>>>(
-            P.ptr, splits, n, p, 1.0f, G.ptr, X32[cur].ptr, X32[nxt].ptr, X32[nxt].ptr, n,
+            P.ptr, splits, n, p, 1.0f, nullptr, G.ptr, X32[cur].ptr, X32[nxt].ptr, X32[nxt].ptr, n,
             want_norms, ns->partials, ns->counter, ns->norms, hm ? ns->hist : nullptr, ns->step,
             ns->stop_tol);
         IPTGB_LAUNCH();
@@ -1441,7 +1619,7 @@ struct LowpDenseSimtF32 final : LowpDenseOperator {
         const int nxt = cur ^ 1;
         KernelTimerScope timer(kProfLowpUpdate, s);
         refine_update_kernel<float><<<grid, kThreads, 0, s>>>(
-            P.ptr, splits, n, p, 1.0f, small.ptr + p, small.ptr + 2 * p, G.ptr, R32.ptr,
+            P.ptr, splits, n, p, 1.0f, nullptr, small.ptr + p, small.ptr + 2 * p, G.ptr, R32.ptr,
             Xref32.ptr, small.ptr, X32[cur].ptr, X32[nxt].ptr, X32[nxt].ptr, n, want_norms,
             ns->partials, ns->counter, ns->norms, hm ? ns->hist : nullptr, ns->step,
             ns->stop_tol);

@@ -41,6 +41,19 @@ struct LowpDenseOperator {
     virtual int refine_apply(double *X) = 0;  // X += delta (FP64)
 };
 
+// Statistics of a dense symmetric H (device, zero-initialised before use):
+// the largest column sum of |H|, the largest off-diagonal |H_il| (non-negative
+// doubles order like their bit patterns) and the count of descents
+// d_{i+1} < d_i of the diagonal.
+struct DenseStats {
+    unsigned long long hnorm_bits;
+    unsigned long long maxabs_bits;
+    unsigned long long descents;
+};
+
+// Largest n the fused setup pass handles (one column of H in shared memory).
+constexpr int kFusedSetupMaxN = 16384;
+
 // Optional inputs and outputs of the operator's one pass over H.
 struct LowpDenseSetup {
     double maxabs = -1.0;           // >= 0: max |H_il| (l != i) is known (no extra pass)
@@ -51,6 +64,16 @@ struct LowpDenseSetup {
                                     //   [chunk][column], chunk = 2048 rows
     int colsum_chunks = 0;          // out: chunks written to colsum_part
     bool split_done = false;        // out: split_hi/lo written
+    // Fused setup (symmetric, n <= kFusedSetupMaxN): one CTA per column of
+    // fused_src (device memory or mapped pinned host memory) writes row c of
+    // Delta with its own power-of-two scale (no global maximum needed, so no
+    // pass before it), the split, the diagonal and the statistics; with
+    // fused_copy also the FP64 matrix itself (when fused_src is host memory).
+    const double *fused_src = nullptr;
+    double *fused_copy = nullptr;
+    double *diag = nullptr;         // n entries
+    DenseStats *stats = nullptr;    // device, zeroed by the caller
+    bool fused_done = false;        // out
 };
 constexpr int kLowpColsumChunk = 2048;
 LowpDenseOperator *make_lowp_dense_operator(const double *dH, int n, int kind, cudaStream_t s,

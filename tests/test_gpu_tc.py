@@ -143,3 +143,46 @@ def test_device_stop_matches_host_checks(cuda, monkeypatch, prec):
         check_pairs(H, X, v, 16)
         runs[mode] = rep
     assert runs["1"]["ipt_iterations"] <= runs["0"]["ipt_iterations"]
+
+
+@pytest.mark.parametrize("prec", ["fp16", "bf16"])
+def test_host_entry_pinned_matches_pageable(cuda, prec):
+    """ipt_block_solve_dense on pinned host memory reads H over the host link
+    inside its first (fused) pass; on pageable memory it copies H first.  Both
+    run the same kernels on the same numbers: identical results."""
+    import ctypes as C
+    from block_ipt_gb300 import _lib
+    torch = cuda
+    n, k = 1536, 12
+    H, _ = workloads.dense_config1(n, seed=21)
+    H = np.asfortranarray(H)
+    X1, v1, r1 = api.block_solve_dense(H, k, prec)
+    pinned = torch.from_numpy(H.T.copy()).pin_memory()  # row-major H^T = column-major H
+    opt = api.block_options(prec)
+    X2 = np.zeros((n, k), order="F")
+    v2 = np.zeros(k)
+    rep = _lib.IPTBlockReport()
+    st = _lib.load().ipt_block_solve_dense(C.c_void_p(pinned.data_ptr()), n, k, C.byref(opt),
+                                           C.c_void_p(X2.ctypes.data), C.c_void_p(v2.ctypes.data),
+                                           C.byref(rep))
+    assert st == 0
+    assert r1["converged"] == 1 and rep.converged == 1
+    assert np.array_equal(v1, v2)
+    assert np.array_equal(X1, X2)
+    check_pairs(H, X2, v2, k)
+
+
+def test_fused_setup_matches_two_pass(cuda, monkeypatch):
+    """The fused setup pass (per-row FP16 scales) and the two-pass setup (one
+    global scale) reach the same certified eigenpairs."""
+    H, _ = workloads.dense_config1(2048, seed=22)
+    monkeypatch.setenv("IPT_GB300_FUSED_SETUP", "1")
+    X1, v1, r1 = api.block_solve_dense(H, 16, "fp16")
+    monkeypatch.setenv("IPT_GB300_FUSED_SETUP", "0")
+    X2, v2, r2 = api.block_solve_dense(H, 16, "fp16")
+    assert r1["converged"] == 1 and r2["converged"] == 1
+    check_pairs(H, X1, v1, 16)
+    check_pairs(H, X2, v2, 16)
+    hn = np.abs(H).sum(axis=1).max()
+    assert np.abs(v1 - v2).max() <= 1e-10 * hn
+    assert abs(r1["matrix_norm_inf"] - hn) <= 1e-12 * hn
