@@ -559,12 +559,13 @@ __global__ void __launch_bounds__(256)
 }
 
 // Fused setup of a symmetric H: one CTA per column c (= row c of Delta).
-// Pass 0 stages the column in shared memory and finds its largest
-// off-diagonal |h| (integer max of the bit patterns); the row's FP16 scale is
-// the largest power of two 2^s2 with 2^s2 max <= 16384 (BF16/TF32: 1).
-// Pass 1 writes row c of Delta, the double-FP32 split of column c, optionally
-// the FP64 column (when the source is host memory), and forms the exact
-// double-float column sum.  The CTA's thread 0 then stores 2^-s2, the
+// Pass 0 reads the column (writing the FP64 device copy when the source is
+// host memory) and finds its largest off-diagonal |h| (integer max of the bit
+// patterns); the row's FP16 scale is the largest power of two 2^s2 with
+// 2^s2 max <= 16384 (BF16/TF32: 1).  Pass 1 re-reads the column from device
+// memory (L2-resident by then: the source over the host link is read once)
+// and writes row c of Delta and the double-FP32 split of column c, and forms
+// the exact double-float column sum.  The CTA's thread 0 then stores 2^-s2, the
 // diagonal entry, the column sum (atomic max: hnorm), its maximum and whether
 // d_{c+1} < d_c.  No FP64 arithmetic per entry (the conversions run on the
 // integer pipe), so the pass streams at memory (or host link) speed.
@@ -575,19 +576,19 @@ __global__ void __launch_bounds__(256)
                        float *__restrict__ lo, float *__restrict__ inv_row,
                        double *__restrict__ diag, DenseStats *__restrict__ stats, int vec)
 {
-    extern __shared__ __align__(16) double colbuf[];  // n doubles
     __shared__ unsigned long long wmax[8];
     __shared__ float wS[8], wC[8];
     __shared__ int s2_sh;
     const int c = blockIdx.x;
     const int tid = threadIdx.x;
     const double *scol = src + (size_t)c * n;
+    double *ccol = copy != nullptr ? copy + (size_t)c * n : nullptr;
     unsigned long long m = 0;
-    if (vec) {  // n even, src 16-byte aligned
+    if (vec) {  // n even, src (and copy) 16-byte aligned
         const double2 *s2v = reinterpret_cast<const double2 *>(scol);
         for (int q = tid; q < n / 2; q += 256) {
             const double2 v = s2v[q];
-            reinterpret_cast<double2 *>(colbuf)[q] = v;
+            if (ccol != nullptr) reinterpret_cast<double2 *>(ccol)[q] = v;
             const int l = 2 * q;
             const unsigned long long a0 =
                 (unsigned long long)__double_as_longlong(v.x) & 0x7FFFFFFFFFFFFFFFULL;
@@ -599,7 +600,7 @@ __global__ void __launch_bounds__(256)
     } else {
         for (int l = tid; l < n; l += 256) {
             const double v = scol[l];
-            colbuf[l] = v;
+            if (ccol != nullptr) ccol[l] = v;
             const unsigned long long a =
                 (unsigned long long)__double_as_longlong(v) & 0x7FFFFFFFFFFFFFFFULL;
             if (l != c && a > m) m = a;
@@ -626,11 +627,22 @@ __global__ void __launch_bounds__(256)
     __syncthreads();
     const int s2 = s2_sh;
     const double scale = ldexp(1.0, s2);
+    // the block's pass-0 writes of the copy are visible after the barrier;
+    // pass 1 reads with ld.global.cg (coherent at L2), never through the
+    // read-only path, since the copy is written by this kernel
+    const double *rcol = ccol != nullptr ? ccol : scol;
     LP *orow = delta + (size_t)c * ldp;
     float S = 0.0f, C = 0.0f;
     for (int l = 2 * tid; l < ldp; l += 512) {  // ldp is a multiple of 64: l + 1 < ldp
-        const double h0 = l < n ? colbuf[l] : 0.0;
-        const double h1 = l + 1 < n ? colbuf[l + 1] : 0.0;
+        double h0 = 0.0, h1 = 0.0;
+        if (vec && l + 1 < n) {
+            const double2 v = __ldcg(reinterpret_cast<const double2 *>(rcol + l));
+            h0 = v.x;
+            h1 = v.y;
+        } else {
+            if (l < n) h0 = __ldcg(rcol + l);
+            if (l + 1 < n) h1 = __ldcg(rcol + l + 1);
+        }
         float a0, a1, b0, b1;
         float v0 = sym_entry(h0, s2, scale, a0, b0);
         float v1 = sym_entry(h1, s2, scale, a1, b1);
@@ -645,21 +657,18 @@ __global__ void __launch_bounds__(256)
                 *reinterpret_cast<float2 *>(hi + o) = make_float2(a0, a1);
                 *reinterpret_cast<float2 *>(lo + o) = make_float2(b0, b1);
             }
-            if (copy != nullptr) *reinterpret_cast<double2 *>(copy + o) = make_double2(h0, h1);
         } else {
             if (l < n) {
                 if (hi != nullptr) {
                     hi[o] = a0;
                     lo[o] = b0;
                 }
-                if (copy != nullptr) copy[o] = h0;
             }
             if (l + 1 < n) {
                 if (hi != nullptr) {
                     hi[o + 1] = a1;
                     lo[o + 1] = b1;
                 }
-                if (copy != nullptr) copy[o + 1] = h1;
             }
         }
     }
@@ -680,7 +689,7 @@ __global__ void __launch_bounds__(256)
             atomicMax(&stats->hnorm_bits, (unsigned long long)__double_as_longlong(colsum));
         }
         if (wmax[0] > 0) atomicMax(&stats->maxabs_bits, wmax[0]);
-        const double dc = colbuf[c];
+        const double dc = __ldcg(rcol + c);
         diag[c] = dc;
         if (c + 1 < n && src[(size_t)(c + 1) * ((size_t)n + 1)] < dc) {
             atomicAdd(&stats->descents, 1ULL);
@@ -1200,16 +1209,13 @@ struct LowpDense final : LowpDenseOperator {
         if (su.fused_src != nullptr && symmetric && n <= kFusedSetupMaxN && su.diag != nullptr &&
             su.stats != nullptr) {
             IPTGB_CHECK(inv_rows.alloc((size_t)n, s));
-            const size_t smem = (size_t)n * sizeof(double);
             auto kfn = fused_setup_kernel<LP>;
-            IPTGB_CUDA(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                            (int)smem));
             const int vec = (n % 2 == 0) &&
                             ((reinterpret_cast<uintptr_t>(su.fused_src) & 15) == 0) &&
                             ((reinterpret_cast<uintptr_t>(split_hi) & 7) == 0) &&
                             ((reinterpret_cast<uintptr_t>(split_lo) & 7) == 0) &&
                             ((reinterpret_cast<uintptr_t>(su.fused_copy) & 15) == 0);
-            kfn<<<n, 256, smem, s>>>(su.fused_src, n, ldp,
+            kfn<<<n, 256, 0, s>>>(su.fused_src, n, ldp,
                                      LowpTypes<LP>::kind == kLowpF16 ? 1 : 0, su.fused_copy,
                                      delta.ptr, split_hi, split_lo, inv_rows.ptr, su.diag,
                                      su.stats, vec);
