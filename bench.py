@@ -42,7 +42,7 @@ sys.path.insert(0, ROOT)
 METRIC = "time to k eigenpairs at ||r||<=1e-8, mixed+learned vs plain FP64 IPT, 1xGB300"
 WORKLOAD = ("dense symmetric n=8192 k=32, d_i=i/8+U(0,0.1), h_ij~N(0,0.02^2)exp(-|i-j|/256), "
             "seed 0; FP16 tcgen05 IPT + refinement against FP64-accurate (double-FP32) defects, "
-            "FP64 CholQR2/Rayleigh-Ritz, to scaled residual 1e-8")
+            "FP64-accurate (double-FP32) CholQR/Rayleigh-Ritz, to scaled residual 1e-8")
 PRODUCTS_FILE = os.path.join(ROOT, "oracle", "plain_ipt_products.json")
 MEASURED_PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
 # DRAM bytes (read + write) per launch from one ncu capture of each kernel on
@@ -51,7 +51,10 @@ MEASURED_PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
 # keyed by (kernel, n, k, precision).
 NCU_TRAFFIC = {("dense64_partial", 8192, 32, "fp16"): 567.5e6,
                ("df64_partial", 8192, 32, "fp16"): 1111.3e6,
-               ("tc_partial", 8192, 32, "fp16"): 137.9e6}
+               # steady state inside a solve, with the L2-kept share of Delta
+               # (profiles/tc_partial_fp16_n8192_k32_l2keep.md); a cold launch
+               # moves 137.9 MB (profiles/tc_partial_fp16_n8192_k32.md)
+               ("tc_partial", 8192, 32, "fp16"): 94.8e6}
 
 
 def parse():
