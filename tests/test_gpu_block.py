@@ -162,3 +162,21 @@ def test_trace_marks(cuda):
     assert np.all(np.diff(gpu) >= 0) and np.all(np.diff(host) >= 0)
     api.block_solve_dense_device(dH.data_ptr(), 1024, 16, dX.data_ptr(), dv.data_ptr(), "fp16")
     assert api.trace_read() == []
+
+
+@pytest.mark.parametrize("df", ["0", "1"])
+def test_block_csr_davidson_products_fp64_and_double_float(cuda, monkeypatch, df):
+    """The Davidson solve with its Gram/tall products in FP64 and in
+    double-float (the default from 16384 rows) reaches the LAPACK pairs."""
+    from scipy.sparse import csr_matrix, random as sprandom
+    monkeypatch.setenv("IPT_GB300_DF_DAVIDSON", df)
+    rng = np.random.default_rng(15)
+    n = 2500
+    A = sprandom(n, n, density=0.004, random_state=rng, format="csr") * 0.05
+    A = A + A.T
+    d = np.sort(rng.uniform(0, 250, n))
+    H = (A + csr_matrix((d, (np.arange(n), np.arange(n))), shape=(n, n))).tocsr()
+    H.sort_indices()
+    X, v, rep = api.block_solve_csr(H.indptr, H.indices, H.data, n, 10, "fp64", strategy=1)
+    assert rep["converged"] == 1
+    check_pairs(H.toarray(), X, v, 10)
