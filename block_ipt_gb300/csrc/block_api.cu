@@ -67,10 +67,23 @@ struct CsrApply final : Fp64Apply {
     const int *col_ind = nullptr;
     const double *vals = nullptr;
     int n = 0;
+    int nnz = 0;
     cudaStream_t s = nullptr;
+    // double-float products (with the Davidson products' policy): the values
+    // split into (hi, lo) floats at the first product
+    bool df = false;
+    DeviceBuffer<float> vsplit;
     int apply(const double *V, int c, double *AV) override
     {
         KernelTimerScope timer(kProfCsrProduct, s);
+        if (df && nnz > 0) {
+            if (vsplit.ptr == nullptr) {
+                IPTGB_CHECK(vsplit.alloc(2 * (size_t)nnz, s));
+                IPTGB_CHECK(launch_df_split(vals, (size_t)nnz, vsplit.ptr, vsplit.ptr + nnz, s));
+            }
+            return launch_csr_df_spmm(row_ptr, col_ind, vsplit.ptr, vsplit.ptr + nnz, n, V, c,
+                                      AV, s);
+        }
         return launch_csr64_spmm(row_ptr, col_ind, vals, n, V, c, AV, s);
     }
 };
@@ -737,7 +750,9 @@ int csr_block_device(const int *row_ptr, const int *col_ind, const double *vals,
     apply.col_ind = col_ind;
     apply.vals = vals;
     apply.n = n;
+    apply.nnz = nnz;
     apply.s = s;
+    apply.df = davidson_df_products(n);
     std::unique_ptr<IptStage> stage(make_fp64_csr_stage(row_ptr, col_ind, vals, n, dd, s));
     std::unique_ptr<LearnedCorrection> learned;
     LearnedCorrection *corr = hook;

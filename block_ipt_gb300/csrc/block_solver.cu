@@ -30,6 +30,12 @@ constexpr double kLearnedDrop = 0.75;
 // Rows from which the Davidson products switch to double-float.
 constexpr int kDfDavidsonMinRows = 16384;
 
+bool davidson_df_products(int n)
+{
+    const int knob = env_int("IPT_GB300_DF_DAVIDSON", -1);
+    return knob >= 0 ? knob != 0 : n >= kDfDavidsonMinRows;
+}
+
 void fill_default_options(IPTBlockOptions *opt)
 {
     memset(opt, 0, sizeof(*opt));
@@ -130,15 +136,7 @@ int block_solve(const BlockSolveInput &in, double *X_out, double *values_out,
     int dev = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&ops.sms, cudaDevAttrMultiProcessorCount, dev);
-    // Large bases: the Gram and tall products (most of a sparse Davidson
-    // solve's time in FP64) run in double-float on the FP32 pipe, ~48 bits,
-    // far below the 1e-8 residual they serve; small problems keep FP64, where
-    // these products cost little (tuning knob IPT_GB300_DF_DAVIDSON: 0 off,
-    // 1 always).
-    {
-        const int knob = env_int("IPT_GB300_DF_DAVIDSON", -1);
-        ops.df_products = knob >= 0 ? knob != 0 : n >= kDfDavidsonMinRows;
-    }
+    ops.df_products = davidson_df_products(n);
 
     const size_t nb = (size_t)n * (size_t)maxb;
     DeviceBuffer<double> V, AV, Vt, AVt, Xr, AXr, R, Xbest, small;

@@ -110,6 +110,13 @@ IptStage *make_lowp_stage_on(LowpDenseOperator *op, const double *d, int n, cuda
 
 void fill_default_options(IPTBlockOptions *opt);
 
+// Large bases: the Davidson solver's Gram and tall products and the sparse
+// products run in double-float on the FP32 pipe (~48 bits, far below the
+// 1e-8 residual they serve; several times faster on GB300); small problems
+// keep FP64, where these products cost little.  From 16384 rows; tuning
+// knob IPT_GB300_DF_DAVIDSON (0 off, 1 always).
+bool davidson_df_products(int n);
+
 // Low-precision dense IPT stage on the tensor cores (k_tc.cu); nullptr if the
 // precision is not supported on this device.
 IptStage *make_lowp_dense_stage(const double *dH, int n, const double *d, int precision,

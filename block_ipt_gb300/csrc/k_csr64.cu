@@ -12,6 +12,7 @@
 // streams with shuffles.  Works for any sparsity pattern; rows are
 // independent, so no atomics and deterministic results.
 #include "common.cuh"
+#include "dfloat.cuh"
 #include "kernels.cuh"
 #include "reduce.cuh"
 
@@ -114,6 +115,114 @@ int launch_csr64_spmm(const int *row_ptr, const int *col_ind, const double *vals
     }
     IPTGB_LAUNCH();
     return IPT_CUDA_SUCCESS;
+}
+
+// ---------------------------------------------------------------------------
+// The same SpMM in double-float arithmetic on the FP32 pipe: the values as
+// (hi, lo) floats split once per solve, X as a row-major block of (hi, lo)
+// pairs, df_acc per term (~48 bits).  On GB300 the FP64 kernel above is bound
+// by the FP64 pipe at ~81 % of its peak; this one does ~5x more terms per
+// second and is limited by the gathers of X instead.
+// ---------------------------------------------------------------------------
+// Xr2[c * ldr + j] = split(X[c + j * n]) as float2 (hi, lo); 0 beyond k.
+__global__ void rowmajor_split_kernel(const double *__restrict__ X, int n, int k,
+                                      float2 *__restrict__ Xr2, int ldr)
+{
+    __shared__ double t[32][33];
+    pdl_wait();  // programmatic dependent launch: predecessor done
+    pdl_trigger();
+    const int r0 = blockIdx.x * 32;
+    const int c0 = blockIdx.y * 32;
+    for (int y = threadIdx.y; y < 32; y += blockDim.y) {
+        const int j = c0 + y;
+        const int r = r0 + threadIdx.x;
+        t[y][threadIdx.x] = (j < k && r < n) ? X[(size_t)r + (size_t)j * n] : 0.0;
+    }
+    __syncthreads();
+    for (int y = threadIdx.y; y < 32; y += blockDim.y) {
+        const int r = r0 + y;
+        const int j = c0 + threadIdx.x;
+        if (r < n && j < ldr) {
+            const dfloat v = df_from_double(t[threadIdx.x][y]);
+            Xr2[(size_t)r * ldr + j] = make_float2(v.hi, v.lo);
+        }
+    }
+}
+
+template <int BN>
+__global__ void __launch_bounds__(kCsrWarpsPerBlock * 32)
+csr_df_spmm_kernel(const int *__restrict__ row_ptr, const int *__restrict__ col_ind,
+                   const float *__restrict__ vh, const float *__restrict__ vl, int n,
+                   const float2 *__restrict__ Xr2, int ldr, int k, double *__restrict__ Y)
+{
+    pdl_wait();  // programmatic dependent launch: predecessor done
+    pdl_trigger();
+    constexpr int LPN = BN / 4;          // lanes per nonzero
+    constexpr int STREAMS = 32 / LPN;    // nonzeros in flight per warp
+    const int lane = threadIdx.x & 31;
+    const int row = blockIdx.x * kCsrWarpsPerBlock + (threadIdx.x >> 5);
+    if (row >= n) {
+        return;
+    }
+    const int sub = lane % LPN;
+    const int q = lane / LPN;
+    const int col0 = blockIdx.y * BN + 4 * sub;
+    float S[4] = {0.f, 0.f, 0.f, 0.f}, s[4] = {0.f, 0.f, 0.f, 0.f};
+    const int pbeg = row_ptr[row];
+    const int pend = row_ptr[row + 1];
+    const float2 *xb = Xr2 + col0;
+    for (int p = pbeg + q; p < pend; p += STREAMS) {
+        const float h = __ldg(vh + p);
+        const float l = __ldg(vl + p);
+        const int c = __ldg(col_ind + p);
+        const float4 *x = reinterpret_cast<const float4 *>(xb + (size_t)c * ldr);
+        const float4 x01 = __ldg(x);      // (hi, lo) of columns col0, col0 + 1
+        const float4 x23 = __ldg(x + 1);  // and col0 + 2, col0 + 3
+        df_acc(S[0], s[0], h, l, x01.x, x01.y);
+        df_acc(S[1], s[1], h, l, x01.z, x01.w);
+        df_acc(S[2], s[2], h, l, x23.x, x23.y);
+        df_acc(S[3], s[3], h, l, x23.z, x23.w);
+    }
+#pragma unroll
+    for (int off = 16; off >= LPN; off >>= 1) {
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const dfloat o = {__shfl_xor_sync(0xffffffffu, S[j], off),
+                              __shfl_xor_sync(0xffffffffu, s[j], off)};
+            const dfloat t = df_add(dfloat{S[j], s[j]}, o);
+            S[j] = t.hi;
+            s[j] = t.lo;
+        }
+    }
+    if (q == 0) {
+        double *y = Y + row;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            if (col0 + j < k) y[(size_t)(col0 + j) * n] = (double)S[j] + (double)s[j];
+        }
+    }
+}
+
+int launch_csr_df_spmm(const int *row_ptr, const int *col_ind, const float *vh, const float *vl,
+                       int n, const double *X, int k, double *Y, cudaStream_t stream)
+{
+    if (n <= 0 || k <= 0) {
+        return IPT_CUDA_SUCCESS;
+    }
+    const int bn = k <= 4 ? 4 : (k <= 8 ? 8 : 16);
+    const int nblk = (k + bn - 1) / bn;
+    const int ldr = nblk * bn;
+    DeviceBuffer<float2> Xr2;
+    IPTGB_CHECK(Xr2.alloc((size_t)n * ldr, stream));
+    IPTGB_CHECK(launch_pdl(rowmajor_split_kernel, dim3((n + 31) / 32, (ldr + 31) / 32),
+                           dim3(32, 8), 0, stream, X, n, k, Xr2.ptr, ldr));
+    dim3 grid((n + kCsrWarpsPerBlock - 1) / kCsrWarpsPerBlock, nblk);
+    const dim3 threads(kCsrWarpsPerBlock * 32);
+    auto kernel = bn == 4 ? csr_df_spmm_kernel<4>
+                  : bn == 8 ? csr_df_spmm_kernel<8>
+                            : csr_df_spmm_kernel<16>;
+    return launch_pdl(kernel, grid, threads, 0, stream, row_ptr, col_ind, vh, vl, n,
+                      (const float2 *)Xr2.ptr, ldr, k, Y);
 }
 
 int launch_ipt_update_from_y(const double *Y, int n, int k, const double *X, const double *d,

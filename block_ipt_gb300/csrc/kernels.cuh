@@ -41,6 +41,9 @@ int launch_dense32_partial(const float *H, int n, long long ldh, const float *X,
 int launch_sum_partials(const double *P, int S, size_t elems, double *Y, cudaStream_t stream);
 // Double-FP32 (hi + lo) FP64-accurate products (k_df64.cu).
 int launch_df_split(const double *A, size_t count, float *hi, float *lo, cudaStream_t stream);
+// Y = H X for CSR H with double-float values (vh, vl) (k_csr64.cu)
+int launch_csr_df_spmm(const int *row_ptr, const int *col_ind, const float *vh, const float *vl,
+                       int n, const double *X, int k, double *Y, cudaStream_t stream);
 // K slices of the double-FP32 product for an n x k block
 int df64_split_for(int n, int k, int sms);
 // Y = the sum of launch_df64_partial's S slices (which hold double-float
