@@ -45,8 +45,8 @@ struct CorrectionArgs {
 
 // A replacement for the plain diagonal correction (k_mlp.cu).  bind() gives
 // the per-row off-diagonal coupling ||H[i, j != i]||_2 (device) and
-// ||H||_inf before the solve; learned() says whether the driver should judge
-// the step (accept, or reject and redo it with the plain correction).
+// ||H||_inf before the solve; learned() says whether the Davidson solver should
+// check the step (accept, or reject and redo it with the plain correction).
 struct LearnedCorrection {
     virtual ~LearnedCorrection() = default;
     virtual void bind(const double *row_coupling, double hnorm) = 0;
