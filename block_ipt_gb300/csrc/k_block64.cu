@@ -317,20 +317,24 @@ __global__ void __launch_bounds__(kTallThreads)
         __syncthreads();
         if (row < n) {
             const int lc = min(kTallK, m - l0);
-            // all of the row's A values in flight at once (the kernel is
-            // latency-bound at a few warps per SM otherwise)
-            double av[kTallK];
+            // groups of 8 A values in flight per thread: enough loads per
+            // warp without the register cost of a whole chunk (which limits
+            // the resident warps)
 #pragma unroll
-            for (int l = 0; l < kTallK; ++l) {
-                av[l] = l < lc ? A[(size_t)row + (size_t)(l0 + l) * lda] : 0.0;
-            }
+            for (int g = 0; g < kTallK; g += 8) {
+                double av[8];
 #pragma unroll
-            for (int l = 0; l < kTallK; ++l) {
-                if (l < lc) {
-                    const dfloat a = df_from_double(av[l]);
+                for (int u = 0; u < 8; ++u) {
+                    av[u] = g + u < lc ? A[(size_t)row + (size_t)(l0 + g + u) * lda] : 0.0;
+                }
 #pragma unroll
-                    for (int j = 0; j < TC; ++j) {
-                        df_acc(S[j], sl[j], a.hi, a.lo, bsh[l][j], bsl[l][j]);
+                for (int u = 0; u < 8; ++u) {
+                    if (g + u < lc) {
+                        const dfloat a = df_from_double(av[u]);
+#pragma unroll
+                        for (int j = 0; j < TC; ++j) {
+                            df_acc(S[j], sl[j], a.hi, a.lo, bsh[g + u][j], bsl[g + u][j]);
+                        }
                     }
                 }
             }
