@@ -88,7 +88,9 @@ int cholqr(BlockOps &ops, const double *B, int n, int c, double *dst, double *G,
            int *st_dev, int *st_host, cudaStream_t s)
 {
     IPTGB_CHECK(ops.gram(B, n, c, B, n, c, n, G, c));
-    IPTGB_CHECK(ops.chol_inverse(G, c, Rinv, st_dev));
+    // the factor in double-float with the double-float products (the FP64
+    // one-CTA factorisation is latency-bound on GB300's FP64 pipe)
+    IPTGB_CHECK(ops.chol_inverse(G, c, Rinv, st_dev, nullptr, ops.df_products));
     IPTGB_CHECK(ops.tall_gemm(B, n, Rinv, c, dst, n, n, c, c));
     IPTGB_CUDA(cudaMemcpyAsync(st_host, st_dev, sizeof(int), cudaMemcpyDeviceToHost, s));
     IPTGB_CUDA(cudaStreamSynchronize(s));
