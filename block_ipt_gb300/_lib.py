@@ -216,6 +216,13 @@ SIGNATURES = [
     ("ipt_block_default_options", None, [C.POINTER(IPTBlockOptions)]),
     ("ipt_block_cholesky_inverse", _i, [_vp, _i, _vp, C.POINTER(C.c_int), _i, _vp]),
     ("ipt_block_split_double", _i, [_vp, C.c_longlong, _vp, _vp, _vp]),
+    ("ipt_block_cluster_ranges", _i, [_vp, _vp, _vp, _i, _i, _i, _i, C.c_double, _i,
+                                      C.c_double, _vp, _i, C.POINTER(C.c_int),
+                                      C.POINTER(C.c_int)]),
+    ("ipt_block_cluster_basis", _i, [_vp, _vp, _vp, _i, _i, _vp, _vp, _i, _i, C.c_double,
+                                     C.c_double, _vp, _vp, _vp, _vp]),
+    ("ipt_block_cluster_update", _i, [_vp, _vp, _vp, _i, _i, _i, C.c_double, _vp,
+                                      C.POINTER(C.c_int), _vp]),
     ("ipt_block_split_double_host", _i, [_vp, C.c_longlong, _vp, _vp]),
     ("ipt_block_symmetric_eig", _i, [_vp, _i, _vp, _vp, _vp]),
     ("ipt_block_mlp_param_count", _i, []),

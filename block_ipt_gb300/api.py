@@ -44,6 +44,8 @@ def _take_result(res, status, what):
         "rayleigh_ritz_time_sec": res.rayleigh_ritz_time_sec,
         "davidson_time_sec": res.davidson_time_sec,
         "davidson_residual_after": res.davidson_residual_after,
+        "adaptive_added_indices": res.adaptive_added_indices.decode(),
+        "adaptive_target_block": (res.adaptive_target_block_start, res.adaptive_target_block_end),
     }
     lib.ipt_cuda_free_result(C.byref(res))
     return vec, val, info
@@ -355,3 +357,46 @@ def trace_read():
     gpu = (C.c_longlong * max(1, m))()
     _check(lib.ipt_block_trace_read(m, labels, host, gpu), "ipt_block_trace_read")
     return [(labels[i].decode(), host[i], gpu[i]) for i in range(m)]
+
+
+# ---- block-cluster path (include/ipt_block.h) ------------------------------------
+def cluster_ranges(col_ptr, row_ind, values, n, k, requested_k=None, threshold=0.0,
+                   adaptive=False, coupling_tau=0.1):
+    """Cluster ranges of a symmetric CSC matrix with ascending diagonal
+    (ipt_block_cluster_ranges): ([(first, last), ...], limit_hit)."""
+    cp, ri, va = _i32(col_ptr), _i32(row_ind), _f64(values)
+    lib = _lib.load()
+    cap = max(1, n)
+    out = np.zeros(2 * cap, dtype=np.int32)
+    cnt, lim = C.c_int(0), C.c_int(0)
+    st = lib.ipt_block_cluster_ranges(_ptr(cp), _ptr(ri), _ptr(va), n, len(ri), k,
+                                      k if requested_k is None else requested_k, threshold,
+                                      int(bool(adaptive)), coupling_tau, _ptr(out), cap,
+                                      C.byref(cnt), C.byref(lim))
+    _check(st, "ipt_block_cluster_ranges")
+    return [(int(out[2 * i]), int(out[2 * i + 1])) for i in range(cnt.value)], bool(lim.value)
+
+
+def cluster_basis(d_row_ptr, d_col_ind, d_vals, n, nnz, d_diag, ranges, maxiter, tol,
+                  d_basis, damping=1.0, stream=None):
+    """Block-cluster basis on the device (ipt_block_cluster_basis); returns
+    (iterations, residuals) per cluster."""
+    rg = np.ascontiguousarray(np.asarray(ranges, dtype=np.int32).reshape(-1))
+    nc = rg.size // 2
+    it = np.zeros(nc, dtype=np.int32)
+    res = np.zeros(nc, dtype=np.float64)
+    st = _lib.load().ipt_block_cluster_basis(d_row_ptr, d_col_ind, d_vals, n, nnz, d_diag,
+                                             _ptr(rg), nc, maxiter, tol, damping, d_basis,
+                                             _ptr(it), _ptr(res), _stream_ptr(stream))
+    _check(st, "ipt_block_cluster_basis")
+    return it, res
+
+
+def cluster_update(d_basis, d_y, d_diag, n, first, m, d_next, damping=1.0, stream=None):
+    """One block-cluster update of cluster [first, first+m) on the device
+    (ipt_block_cluster_update); returns the singular flag."""
+    sing = C.c_int(0)
+    st = _lib.load().ipt_block_cluster_update(d_basis, d_y, d_diag, n, first, m, damping,
+                                              d_next, C.byref(sing), _stream_ptr(stream))
+    _check(st, "ipt_block_cluster_update")
+    return bool(sing.value)

@@ -9,9 +9,11 @@
 #include <climits>
 #include <memory>
 #include <numeric>
+#include <string>
 #include <vector>
 
 #include "block_solver.h"
+#include "cluster.h"
 #include "common.cuh"
 #include "fpconv.cuh"
 #include "ipt_plain.h"
@@ -659,7 +661,8 @@ int dense_block_device(const double *dH_in, int n, int k, const IPTBlockOptions 
 int csr_block_device(const int *row_ptr, const int *col_ind, const double *vals, int n, int nnz,
                      int k, const IPTBlockOptions *options, const double *d_diag_sorted,
                      double *d_vectors, double *d_values, IPTBlockReport *report,
-                     LearnedCorrection *hook = nullptr)
+                     LearnedCorrection *hook = nullptr, const double *d_initial = nullptr,
+                     int initial_cols = 0)
 {
     IPTBlockOptions opt;
     if (options != nullptr) {
@@ -768,7 +771,7 @@ int csr_block_device(const int *row_ptr, const int *col_ind, const double *vals,
     }
     DeviceBuffer<double> Xfb;
     bool done = false;
-    if (opt.strategy == IPT_BLOCK_STRATEGY_REFINE && k <= 64) {
+    if (opt.strategy == IPT_BLOCK_STRATEGY_REFINE && k <= 64 && d_initial == nullptr) {
         RefineInput rin;
         rin.apply = &apply;
         rin.d = dd;
@@ -796,6 +799,9 @@ int csr_block_device(const int *row_ptr, const int *col_ind, const double *vals,
         if (Xfb.ptr != nullptr) {
             in.initial = Xfb.ptr;
             in.initial_cols = k;
+        } else if (d_initial != nullptr) {
+            in.initial = d_initial;
+            in.initial_cols = initial_cols;
         }
         IPTGB_CHECK(block_solve(in, d_vectors, d_values, report, s));
         if (Xfb.ptr != nullptr) {
@@ -1027,6 +1033,9 @@ int ipt_block_sparse_host_entry(const int *col_ptr, const int *row_ind, const do
     strcpy(result->best_so_far_source, "none");
     result->best_so_far_max_residual = NAN;
     result->best_so_far_max_residual_index = -1;
+    result->adaptive_coupling_tau = NAN;
+    result->adaptive_target_block_start = -1;
+    result->adaptive_target_block_end = -1;
     if (!validate_csc(col_ptr, row_ind, n, nnz)) {
         return IPT_CUDA_INVALID_ARGUMENT;
     }
@@ -1049,9 +1058,49 @@ int ipt_block_sparse_host_entry(const int *col_ptr, const int *row_ind, const do
     }
     IPTBlockOptions opt;
     fill_default_options(&opt);
-    opt.ipt_maxiter = env_int("IPT_BLOCK_CLUSTER_MAXITER", maxiter > 0 ? maxiter : 100);
-    opt.ipt_tol = env_double("IPT_BLOCK_CLUSTER_TOL", use_tol ? tol : 1e-12);
-    opt.oversample = env_int("IPT_BLOCK_CLUSTER_OVERSAMPLE", 0);
+    int block_maxiter = env_int("IPT_BLOCK_CLUSTER_MAXITER", maxiter > 0 ? maxiter : 100);
+    if (block_maxiter <= 0) block_maxiter = 100;
+    const double block_tol = env_double("IPT_BLOCK_CLUSTER_TOL", use_tol ? tol : 1e-12);
+    const double damping = env_double("IPT_BLOCK_CLUSTER_DAMPING", 1.0);
+    // cluster ranges of the diagonal-sorted matrix (ipt_cuda.cu:4555-4688);
+    // for a symmetric matrix the prepared CSR arrays are also its CSC arrays
+    const int adaptive = env_flag("IPT_BLOCK_CLUSTER_ADAPTIVE", 0);
+    const double coupling_tau = env_double("IPT_BLOCK_CLUSTER_COUPLING_TAU", 0.1);
+    const int oversample = adaptive ? 0 : env_int("IPT_BLOCK_CLUSTER_OVERSAMPLE", 0);
+    const int target_k = oversample > 0 ? (oversample > n - k ? n : k + oversample) : k;
+    ClusterRanges cr;
+    cluster_ranges(prep.row_ptr.data(), prep.col_ind.data(), prep.vals.data(), n, target_k, k,
+                   env_double("IPT_DEGENERACY_THRESHOLD", 0.0), adaptive, coupling_tau, &cr);
+    int basis_cols = 0;
+    for (const auto &r : cr.ranges) {
+        basis_cols += r.second - r.first + 1;
+        if (r.first <= k - 1 && k - 1 <= r.second) {
+            result->adaptive_target_block_start = r.first;
+            result->adaptive_target_block_end = r.second;
+        }
+    }
+    result->oversample = oversample;
+    result->adaptive_block_enabled = adaptive;
+    result->adaptive_coupling_tau = coupling_tau;
+    result->adaptive_limit_hit = cr.limit_hit;
+    {
+        std::string added;
+        for (int i : cr.added) added += (added.empty() ? "" : ";") + std::to_string(i);
+        snprintf(result->adaptive_added_indices, sizeof(result->adaptive_added_indices), "%s",
+                 added.empty() ? "none" : added.c_str());
+    }
+    if (cr.too_large || basis_cols < k) {
+        ipt_cuda_free_result(result);
+        return IPT_CUDA_INVALID_ARGUMENT;
+    }
+    if (basis_cols > 112) {
+        // the projected eigensolve keeps the basis in one CTA's shared memory
+        fprintf(stderr, "ipt_gb300: block-cluster basis of %d columns exceeds 112\n", basis_cols);
+        ipt_cuda_free_result(result);
+        return IPT_CUDA_INVALID_ARGUMENT;
+    }
+    opt.oversample = basis_cols - k;
+    opt.strategy = IPT_BLOCK_STRATEGY_DAVIDSON;
     const int enrich = env_flag("IPT_DAVIDSON_ENRICH", 0);
     const int steps = std::max(0, env_int("IPT_DAVIDSON_STEPS", 1)) +
                       std::max(0, env_int("IPT_DAVIDSON_EXTRA_STEPS", 0));
@@ -1093,10 +1142,44 @@ int ipt_block_sparse_host_entry(const int *col_ptr, const int *row_ind, const do
                              cudaMemcpyHostToDevice, s) != cudaSuccess)) {
             status = IPT_CUDA_CUDA_ERROR;
         }
-        if (status == IPT_CUDA_SUCCESS) {
-            status = csr_block_device(rp.ptr, ci.ptr, cv.ptr, n, prep.nnz, k, &opt, dd.ptr, dX.ptr,
-                                      dv.ptr, &rep);
+        // the block-cluster basis (k_cluster.cu), then Rayleigh-Ritz and the
+        // Davidson enrichment from it
+        DeviceBuffer<double> basis;
+        std::vector<int> rg((size_t)cr.ranges.size() * 2), cl_it(cr.ranges.size());
+        std::vector<double> cl_res(cr.ranges.size());
+        for (size_t c = 0; c < cr.ranges.size(); ++c) {
+            rg[2 * c] = cr.ranges[c].first;
+            rg[2 * c + 1] = cr.ranges[c].second;
         }
+        if (status == IPT_CUDA_SUCCESS) status = basis.alloc((size_t)n * basis_cols, s);
+        if (status == IPT_CUDA_SUCCESS) {
+            auto tb = std::chrono::steady_clock::now();
+            int bad = -1;
+            status = cluster_basis_solve(rp.ptr, ci.ptr, cv.ptr, n, dd.ptr, rg.data(),
+                                         (int)cr.ranges.size(), block_maxiter, block_tol, damping,
+                                         basis.ptr, cl_it.data(), cl_res.data(), &bad, s);
+            if (status != IPT_CUDA_SUCCESS && bad >= 0) {
+                fprintf(stderr,
+                        "ipt_gb300: block-cluster solve failed for block=%d:%d size=%d\n",
+                        cr.ranges[(size_t)bad].first, cr.ranges[(size_t)bad].second,
+                        cr.ranges[(size_t)bad].second - cr.ranges[(size_t)bad].first + 1);
+            }
+            result->iteration_time_sec =
+                std::chrono::duration<double>(std::chrono::steady_clock::now() - tb).count();
+        }
+        if (status == IPT_CUDA_SUCCESS) {
+            for (size_t c = 0; c < cr.ranges.size(); ++c) {
+                const int w = cr.ranges[c].second - cr.ranges[c].first + 1;
+                result->iterations = std::max(result->iterations, cl_it[c]);
+                result->matvecs += (long long)cl_it[c] * w;
+                if (isfinite(cl_res[c]) && !(cl_res[c] <= result->fixed_point_residual)) {
+                    result->fixed_point_residual = cl_res[c];
+                }
+            }
+            status = csr_block_device(rp.ptr, ci.ptr, cv.ptr, n, prep.nnz, k, &opt, dd.ptr, dX.ptr,
+                                      dv.ptr, &rep, nullptr, basis.ptr, basis_cols);
+        }
+        basis.release();
         if (status == IPT_CUDA_SUCCESS &&
             (cudaMemcpyAsync(result->vectors, dX.ptr, (size_t)n * k * sizeof(double),
                              cudaMemcpyDeviceToHost, s) != cudaSuccess ||
@@ -1123,11 +1206,8 @@ int ipt_block_sparse_host_entry(const int *col_ptr, const int *row_ind, const do
     unpermute_vectors(prep, result->vectors, k);
     result->n = n;
     result->k = k;
-    result->iterations = rep.ipt_iterations;
     result->basis_cols = rep.basis_cols;
-    result->matvecs = rep.fp64_matvecs;
-    result->fixed_point_residual = rep.ipt_fixed_point_residual;
-    result->iteration_time_sec = rep.ipt_ms * 1e-3;
+    result->matvecs += rep.fp64_matvecs;
     result->rayleigh_ritz_time_sec = rep.rayleigh_ritz_ms * 1e-3;
     result->davidson_time_sec = rep.davidson_ms * 1e-3;
     result->solve_time_sec = rep.total_ms * 1e-3;
@@ -1149,9 +1229,6 @@ int ipt_block_sparse_host_entry(const int *col_ptr, const int *row_ind, const do
     result->cluster_residual_max = NAN;
     result->pair28_best_residual = NAN;
     result->pair29_best_residual = NAN;
-    result->adaptive_coupling_tau = NAN;
-    result->adaptive_target_block_start = -1;
-    result->adaptive_target_block_end = -1;
     result->basis_orthogonality_frobenius_error = NAN;
     result->basis_orthogonality_max_abs_error = NAN;
     result->ritz_vectors_orthogonality_frobenius_error = NAN;

@@ -1,0 +1,52 @@
+// cluster.h - the block-cluster path (internal): cluster ranges on the host
+// (prep.cpp) and the block-cluster basis solve on the device (k_cluster.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stddef.h>
+
+#include <utility>
+#include <vector>
+
+namespace iptgb {
+
+// The reference's default limit on a cluster's width (IPT_MAX_LIFT_BLOCK_SIZE,
+// IPT_C_GPU/src/ipt_preparation.cu:20); the update kernel holds one m x (m+1)
+// system per row in shared memory up to this width.
+constexpr int kClusterMaxWidth = 64;
+
+struct ClusterRanges {
+    std::vector<std::pair<int, int>> ranges;  // inclusive, ascending, disjoint
+    std::vector<int> added;                   // indices added by the adaptive expansion
+    int limit_hit = 0;
+    int too_large = 0;                        // a cluster exceeds max_block_size
+    int max_block_size = kClusterMaxWidth;
+};
+
+// Cluster ranges of the k targets (the basis target: requested + oversample)
+// of a symmetric CSC matrix whose diagonal is ascending (prep.cpp;
+// ipt_preparation.cu:502-644, ipt_cuda.cu:4114-4272); the adaptive expansion
+// grows the cluster of target requested_k - 1.
+void cluster_ranges(const int *col_ptr, const int *row_ind, const double *vals, int n, int k,
+                    int requested_k, double degeneracy_threshold, int adaptive,
+                    double coupling_tau, ClusterRanges *out);
+
+size_t cluster_update_smem(int m);
+
+// One update launch over C clusters (info4: {first, m, column offset, 0}).
+int launch_cluster_update(const double *X, const double *Y, const double *d, int n,
+                          const int *info4, const int *active, int C, int max_m, size_t smem,
+                          double damping, double *Xn, int *flags, cudaStream_t s);
+
+// The block-cluster basis (n x sum of widths, column-major, cluster after
+// cluster) of a CSR matrix with ascending diagonal d; ranges holds C
+// inclusive (first, last) pairs.  iterations / residuals (host, C entries)
+// receive each cluster's iteration count and last fixed-point residual.
+// IPT_CUDA_INVALID_ARGUMENT for a singular row system or a non-finite
+// iterate, with the first such cluster in *first_error_cluster.
+int cluster_basis_solve(const int *row_ptr, const int *col_ind, const double *vals, int n,
+                        const double *d, const int *ranges, int C, int maxiter, double tol,
+                        double damping, double *X, int *iterations, double *residuals,
+                        int *first_error_cluster, cudaStream_t s);
+
+}  // namespace iptgb

@@ -1,0 +1,466 @@
+// k_cluster.cu - the block-cluster basis solve of the IPT_BLOCK_CLUSTER path.
+//
+// The reference iterates, for every cluster c of diagonal positions
+// [first, last] (m = last - first + 1 <= 64), the block fixed point
+//     Y = H X,  h = Y[first:last, :],
+//     X'[i, :] = e_{i - first}^T                          for i in the cluster,
+//     (d_i I - h^T) X'[i, :]^T = d_i X[i, :]^T - Y[i, :]^T  otherwise,
+// from the identity columns, until ||X' - X||_F / max(1, ||X||_F) <= tol
+// (IPT_C_GPU/src/ipt_cuda.cu:2871-3037), solving each row's m x m system by
+// Gauss-Jordan elimination with partial pivoting in one CTA per row
+// (ipt_block_cluster_update_kernel, ipt_cuda.cu:2280-2384), one cluster
+// after the other, with a device-to-host read of a singular flag and two
+// norms per iteration.
+//
+// Here all clusters iterate together: one CSR product covers the columns of
+// every cluster still iterating, one update launch solves every (row,
+// cluster) system, one norm launch and a one-CTA finish kernel decide per
+// cluster whether it has converged, and the host reads one small status
+// block per iteration.  A converged cluster is frozen: its columns are not
+// updated again, so every cluster ends with exactly the iterate the
+// reference's own loop for it returns.
+//
+// The update gives each row's system to a team of T lanes (T the power of
+// two >= m, at most 32; several teams share a warp when m < 32), with the
+// augmented matrix in shared memory, row e of it owned by lane e mod T.  The
+// pivot is the first row holding the largest |entry| (the reference's
+// sequential scan with a strict comparison); a NaN diagonal entry, a pivot
+// that is not finite or not above 64 DBL_EPSILON is singular.  The
+// elimination keeps the reference's operations (row swap, division of the
+// pivot row by the pivot, a[e][j] -= a[e][p] a[p][j] as one FMA) so that the
+// CPU restatement of this kernel reproduces it bit for bit.
+#include <float.h>
+#include <math.h>
+#include <string.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "cluster.h"
+#include "common.cuh"
+#include "ipt_plain.h"
+#include "kernels.cuh"
+#include "reduce.cuh"
+
+namespace iptgb {
+
+constexpr int kClusterThreads = 128;
+constexpr int kClusterNormSlices = 64;
+
+__host__ __device__ __forceinline__ int cluster_team(int m)
+{
+    int t = 1;
+    while (t < m && t < 32) t <<= 1;
+    return t;
+}
+
+size_t cluster_update_smem(int m)
+{
+    const int teams = kClusterThreads / cluster_team(m);
+    return ((size_t)m * m + (size_t)teams * m * (m + 1)) * sizeof(double);
+}
+
+// info[c] = {first, m, column offset, 0}; active[c] != 0 while c iterates.
+__global__ void __launch_bounds__(kClusterThreads)
+cluster_update_kernel(const double *__restrict__ X, const double *__restrict__ Y,
+                      const double *__restrict__ d, int n, const int4 *__restrict__ info,
+                      const int *__restrict__ active, double damping, double *__restrict__ Xn,
+                      int *__restrict__ flags)
+{
+    pdl_wait();  // programmatic dependent launch: predecessor done
+    pdl_trigger();
+    const int c = blockIdx.y;
+    if (active[c] == 0) return;
+    const int4 ci = info[c];
+    const int first = ci.x, m = ci.y, off = ci.z;
+    const int T = cluster_team(m);
+    const int teams = blockDim.x / T;
+    const int ld = m + 1;
+    extern __shared__ double cl_smem[];
+    double *h = cl_smem;  // h[u + e m] = Y[first + u, off + e]
+    const int team = threadIdx.x / T;
+    const int t = threadIdx.x % T;
+    double *aug = cl_smem + (size_t)m * m + (size_t)team * m * ld;
+    const unsigned lane = threadIdx.x & 31u;
+    const unsigned tmask =
+        T == 32 ? 0xffffffffu : (((1u << T) - 1u) << (lane / (unsigned)T * (unsigned)T));
+    const double *Xc = X + (size_t)off * n;
+    const double *Yc = Y + (size_t)off * n;
+    double *Xnc = Xn + (size_t)off * n;
+    for (int i = threadIdx.x; i < m * m; i += blockDim.x) {
+        const int u = i % m, e = i / m;
+        h[i] = Yc[(size_t)(first + u) + (size_t)e * n];
+    }
+    __syncthreads();
+    for (int row0 = blockIdx.x * teams; row0 < n; row0 += gridDim.x * teams) {
+        const int row = row0 + team;
+        if (row >= n) continue;
+        if (row >= first && row < first + m) {
+            for (int e = t; e < m; e += T) Xnc[(size_t)row + (size_t)e * n] = row == first + e ? 1.0 : 0.0;
+            continue;
+        }
+        const double dr = d[row];
+        for (int e = t; e < m; e += T) {
+            double *a = aug + (size_t)e * ld;
+            for (int u = 0; u < m; ++u) a[u] = (e == u ? dr : 0.0) - h[u + e * m];
+            a[m] = fma(dr, Xc[(size_t)row + (size_t)e * n], -Yc[(size_t)row + (size_t)e * n]);
+        }
+        __syncwarp(tmask);
+        bool singular = false;
+        for (int p = 0; p < m; ++p) {
+            double best = -1.0;
+            int bi = m;
+            bool diag_nan = false;
+            for (int e = t; e < m; e += T) {
+                if (e < p) continue;
+                const double v = fabs(aug[(size_t)e * ld + p]);
+                if (v != v) {
+                    diag_nan = diag_nan || e == p;
+                } else if (v > best || (v == best && e < bi)) {
+                    best = v;
+                    bi = e;
+                }
+            }
+            for (int o = T >> 1; o >= 1; o >>= 1) {
+                const double ov = __shfl_xor_sync(tmask, best, o, T);
+                const int oi = __shfl_xor_sync(tmask, bi, o, T);
+                if (ov > best || (ov == best && oi < bi)) {
+                    best = ov;
+                    bi = oi;
+                }
+            }
+            diag_nan = __any_sync(tmask, diag_nan);
+            if (diag_nan || !isfinite(best) || best <= 64.0 * DBL_EPSILON) {
+                singular = true;
+                break;
+            }
+            double *ap = aug + (size_t)p * ld;
+            if (bi != p) {
+                double *aq = aug + (size_t)bi * ld;
+                for (int j = p + t; j <= m; j += T) {
+                    const double tmp = ap[j];
+                    ap[j] = aq[j];
+                    aq[j] = tmp;
+                }
+            }
+            __syncwarp(tmask);
+            const double pv = ap[p];
+            __syncwarp(tmask);
+            for (int j = p + t; j <= m; j += T) ap[j] = ap[j] / pv;
+            __syncwarp(tmask);
+            for (int e = t; e < m; e += T) {
+                if (e == p) continue;
+                double *a = aug + (size_t)e * ld;
+                const double f = a[p];
+                for (int j = p; j <= m; ++j) a[j] = fma(-f, ap[j], a[j]);
+            }
+            __syncwarp(tmask);
+        }
+        if (!singular) {
+            for (int e = t; e < m; e += T) {
+                double v = aug[(size_t)e * ld + m];
+                if (damping < 1.0) v = fma(damping, v, (1.0 - damping) * Xc[(size_t)row + (size_t)e * n]);
+                if (!isfinite(v)) {
+                    singular = true;
+                    v = 0.0;
+                }
+                Xnc[(size_t)row + (size_t)e * n] = v;
+            }
+        }
+        if (singular) atomicOr(&flags[c], 1);
+        __syncwarp(tmask);
+    }
+}
+
+// Per cluster and slice: sum (Xn - X)^2 and sum X^2 over the cluster's
+// columns (contiguous in column-major order), in a fixed order.
+__global__ void cluster_norms_kernel(const double *__restrict__ X, const double *__restrict__ Xn,
+                                     int n, const int4 *__restrict__ info,
+                                     const int *__restrict__ active, double2 *__restrict__ part)
+{
+    pdl_wait();  // programmatic dependent launch: predecessor done
+    pdl_trigger();
+    const int c = blockIdx.y;
+    if (active[c] == 0) return;
+    const int4 ci = info[c];
+    const size_t beg = (size_t)ci.z * n;
+    const size_t cnt = (size_t)ci.y * n;
+    double dd = 0.0, bb = 0.0;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < cnt;
+         i += (size_t)gridDim.x * blockDim.x) {
+        const double x = X[beg + i];
+        const double dx = Xn[beg + i] - x;
+        dd = fma(dx, dx, dd);
+        bb = fma(x, x, bb);
+    }
+    const double2 s = block_sum2(dd, bb);
+    if (threadIdx.x == 0) part[(size_t)c * gridDim.x + blockIdx.x] = s;
+}
+
+// One thread per cluster: the fixed-point residual, the stop decision and
+// the status block st = {error, clusters still iterating, active[0..C)}.
+__global__ void cluster_finish_kernel(const double2 *__restrict__ part, int slices, int C,
+                                      int *__restrict__ active, int *__restrict__ iters,
+                                      int *__restrict__ flags, double *__restrict__ resid,
+                                      int maxiter, double tol, int *__restrict__ st)
+{
+    pdl_wait();  // programmatic dependent launch: predecessor done
+    pdl_trigger();
+    __shared__ int live;
+    __shared__ int err;
+    if (threadIdx.x == 0) {
+        live = 0;
+        err = 0;
+    }
+    __syncthreads();
+    for (int c = threadIdx.x; c < C; c += blockDim.x) {
+        if (active[c] == 0) continue;
+        double dd = 0.0, bb = 0.0;
+        for (int s = 0; s < slices; ++s) {
+            const double2 p = part[(size_t)c * slices + s];
+            dd += p.x;
+            bb += p.y;
+        }
+        const double dn = sqrt(dd), bn = sqrt(bb);
+        if ((flags[c] & 1) != 0 || !isfinite(dn) || !isfinite(bn) || bn <= 0.0) {
+            flags[c] |= 2;
+            active[c] = 0;
+            atomicOr(&err, 1);
+            continue;
+        }
+        const int it = iters[c] + 1;
+        iters[c] = it;
+        const double r = dn / fmax(1.0, bn);
+        resid[c] = r;
+        if (r <= tol || it >= maxiter) {
+            active[c] = 0;
+        } else {
+            atomicAdd(&live, 1);
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        st[0] = err;
+        st[1] = live;
+    }
+    for (int c = threadIdx.x; c < C; c += blockDim.x) st[2 + c] = active[c];
+}
+
+// Columns of the identity start: X[first_c + j, off_c + j] = 1.
+__global__ void cluster_identity_kernel(double *__restrict__ X, int n, const int4 *__restrict__ info)
+{
+    pdl_wait();  // programmatic dependent launch: predecessor done
+    pdl_trigger();
+    const int4 ci = info[blockIdx.y];
+    const size_t cnt = (size_t)ci.y * n;
+    double *Xc = X + (size_t)ci.z * n;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < cnt;
+         i += (size_t)gridDim.x * blockDim.x) {
+        const int j = (int)(i / (size_t)n);
+        const int r = (int)(i - (size_t)j * n);
+        Xc[i] = r == ci.x + j ? 1.0 : 0.0;
+    }
+}
+
+// The clusters whose last iterate sits in the scratch buffer (an odd
+// iteration count) are copied into the result.
+__global__ void cluster_collect_kernel(double *__restrict__ X, const double *__restrict__ B, int n,
+                                       const int4 *__restrict__ info, const int *__restrict__ iters)
+{
+    pdl_wait();  // programmatic dependent launch: predecessor done
+    pdl_trigger();
+    const int c = blockIdx.y;
+    if ((iters[c] & 1) == 0) return;
+    const int4 ci = info[c];
+    const size_t beg = (size_t)ci.z * n;
+    const size_t cnt = (size_t)ci.y * n;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < cnt;
+         i += (size_t)gridDim.x * blockDim.x) {
+        X[beg + i] = B[beg + i];
+    }
+}
+
+static int cluster_grid_x(int n, int C, int teams)
+{
+    const int sms = device_sm_count();
+    const int want = std::max(1, (8 * sms + C - 1) / std::max(1, C));
+    return std::max(1, std::min((n + teams - 1) / teams, want));
+}
+
+static int set_cluster_smem(size_t bytes)
+{
+    static size_t set = 0;
+    if (bytes > 48 * 1024 && bytes > set) {
+        IPTGB_CUDA(cudaFuncSetAttribute(cluster_update_kernel,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+        set = bytes;
+    }
+    return IPT_CUDA_SUCCESS;
+}
+
+// smem: the largest cluster_update_smem() over the clusters (it is not
+// monotonic in m: the team count drops when m passes a power of two).
+int launch_cluster_update(const double *X, const double *Y, const double *d, int n,
+                          const int *info4, const int *active, int C, int max_m, size_t smem,
+                          double damping, double *Xn, int *flags, cudaStream_t s)
+{
+    IPTGB_CHECK(set_cluster_smem(smem));
+    const int teams = kClusterThreads / cluster_team(max_m);
+    dim3 grid(cluster_grid_x(n, C, teams), C);
+    return launch_pdl(cluster_update_kernel, grid, dim3(kClusterThreads), smem, s, X, Y, d, n,
+                      reinterpret_cast<const int4 *>(info4), active, damping, Xn, flags);
+}
+
+int cluster_basis_solve(const int *row_ptr, const int *col_ind, const double *vals, int n,
+                        const double *d, const int *ranges, int C, int maxiter, double tol,
+                        double damping, double *X, int *iterations, double *residuals,
+                        int *first_error_cluster, cudaStream_t s)
+{
+    if (first_error_cluster != nullptr) *first_error_cluster = -1;
+    if (C <= 0 || n <= 0 || ranges == nullptr || X == nullptr || d == nullptr ||
+        row_ptr == nullptr) {
+        return IPT_CUDA_INVALID_ARGUMENT;
+    }
+    std::vector<int> info((size_t)C * 4);
+    int cols = 0, max_m = 0;
+    size_t smem = 0;
+    for (int c = 0; c < C; ++c) {
+        const int first = ranges[2 * c], last = ranges[2 * c + 1];
+        const int m = last - first + 1;
+        if (first < 0 || last >= n || m < 1 || m > kClusterMaxWidth ||
+            (c > 0 && first <= ranges[2 * c - 1])) {
+            return IPT_CUDA_INVALID_ARGUMENT;  // ranges must be ascending and disjoint
+        }
+        info[4 * c] = first;
+        info[4 * c + 1] = m;
+        info[4 * c + 2] = cols;
+        info[4 * c + 3] = 0;
+        cols += m;
+        max_m = std::max(max_m, m);
+        smem = std::max(smem, cluster_update_smem(m));
+    }
+    if (!(damping > 0.0 && damping <= 1.0)) damping = 1.0;  // ipt_cuda.cu:4289-4294
+    const double eff_tol = tol > 0.0 ? tol : 1.0e-12;
+    const size_t nb = (size_t)n * cols;
+    DeviceBuffer<double> B, Y, R;
+    DeviceBuffer<int> I;
+    DeviceBuffer<double2> part;
+    IPTGB_CHECK(B.alloc(nb, s));
+    IPTGB_CHECK(Y.alloc(nb, s));
+    IPTGB_CHECK(R.alloc((size_t)C, s));
+    // info (4C) | active (C) | iters (C) | flags (C) | status (2 + C)
+    IPTGB_CHECK(I.alloc((size_t)C * 8 + 2, s));
+    IPTGB_CHECK(part.alloc((size_t)C * kClusterNormSlices, s));
+    int *d_info = I.ptr;
+    int *d_active = d_info + 4 * C;
+    int *d_iters = d_active + C;
+    int *d_flags = d_iters + C;
+    int *d_st = d_flags + C;
+    std::vector<int> init((size_t)C * 8 + 2, 0);
+    memcpy(init.data(), info.data(), info.size() * sizeof(int));
+    for (int c = 0; c < C; ++c) init[(size_t)4 * C + c] = maxiter > 0 ? 1 : 0;
+    IPTGB_CUDA(cudaMemcpyAsync(I.ptr, init.data(), init.size() * sizeof(int),
+                               cudaMemcpyHostToDevice, s));
+    IPTGB_CHECK(launch_pdl(cluster_identity_kernel, dim3(std::max(1, std::min(64, blocks_for((size_t)n * max_m))), C),
+                           dim3(kThreads), 0, s, X, n, reinterpret_cast<const int4 *>(d_info)));
+    std::vector<int> hst((size_t)C + 2, 0);
+    std::vector<char> live((size_t)C, maxiter > 0 ? 1 : 0);
+    double *cur = X, *nxt = B.ptr;
+    bool failed = false;
+    for (int it = 0; it < maxiter; ++it) {
+        // the product covers the column span of the clusters still iterating
+        int lo = -1, hi = -1;
+        for (int c = 0; c < C; ++c) {
+            if (!live[(size_t)c]) continue;
+            if (lo < 0) lo = info[4 * c + 2];
+            hi = info[4 * c + 2] + info[4 * c + 1];
+        }
+        if (lo < 0) break;
+        IPTGB_CHECK(launch_csr64_spmm(row_ptr, col_ind, vals, n, cur + (size_t)lo * n, hi - lo,
+                                      Y.ptr + (size_t)lo * n, s));
+        IPTGB_CHECK(launch_cluster_update(cur, Y.ptr, d, n, d_info, d_active, C, max_m, smem,
+                                          damping, nxt, d_flags, s));
+        IPTGB_CHECK(launch_pdl(cluster_norms_kernel, dim3(kClusterNormSlices, C), dim3(kThreads), 0,
+                               s, cur, nxt, n, reinterpret_cast<const int4 *>(d_info), d_active,
+                               part.ptr));
+        IPTGB_CHECK(launch_pdl(cluster_finish_kernel, dim3(1), dim3(128), 0, s, part.ptr,
+                               kClusterNormSlices, C, d_active, d_iters, d_flags, R.ptr, maxiter,
+                               eff_tol, d_st));
+        IPTGB_CUDA(cudaMemcpyAsync(hst.data(), d_st, hst.size() * sizeof(int),
+                                   cudaMemcpyDeviceToHost, s));
+        IPTGB_CUDA(cudaStreamSynchronize(s));
+        std::swap(cur, nxt);
+        if (hst[0] != 0) {
+            failed = true;
+            break;
+        }
+        for (int c = 0; c < C; ++c) live[(size_t)c] = (char)(hst[(size_t)2 + c] != 0);
+        if (hst[1] == 0) break;
+    }
+    // every cluster's last iterate into X
+    IPTGB_CHECK(launch_pdl(cluster_collect_kernel, dim3(std::max(1, std::min(64, blocks_for((size_t)n * max_m))), C),
+                           dim3(kThreads), 0, s, X, B.ptr, n,
+                           reinterpret_cast<const int4 *>(d_info), d_iters));
+    std::vector<int> h_it((size_t)C), h_fl((size_t)C);
+    std::vector<double> h_r((size_t)C);
+    IPTGB_CUDA(cudaMemcpyAsync(h_it.data(), d_iters, (size_t)C * sizeof(int),
+                               cudaMemcpyDeviceToHost, s));
+    IPTGB_CUDA(cudaMemcpyAsync(h_fl.data(), d_flags, (size_t)C * sizeof(int),
+                               cudaMemcpyDeviceToHost, s));
+    IPTGB_CUDA(cudaMemcpyAsync(h_r.data(), R.ptr, (size_t)C * sizeof(double),
+                               cudaMemcpyDeviceToHost, s));
+    IPTGB_CUDA(cudaStreamSynchronize(s));
+    for (int c = 0; c < C; ++c) {
+        if (iterations != nullptr) iterations[c] = h_it[(size_t)c];
+        if (residuals != nullptr) residuals[c] = h_it[(size_t)c] > 0 ? h_r[(size_t)c] : NAN;
+        if (failed && h_fl[(size_t)c] != 0 && first_error_cluster != nullptr &&
+            *first_error_cluster < 0) {
+            *first_error_cluster = c;
+        }
+    }
+    return failed ? IPT_CUDA_INVALID_ARGUMENT : IPT_CUDA_SUCCESS;
+}
+
+}  // namespace iptgb
+
+#define IPT_API extern "C" __attribute__((visibility("default")))
+
+using namespace iptgb;
+
+IPT_API int ipt_block_cluster_basis(const int *d_row_ptr, const int *d_col_ind,
+                                    const double *d_vals, int n, int nnz, const double *d_diag,
+                                    const int *ranges, int nclusters, int maxiter, double tol,
+                                    double damping, double *d_basis, int *iterations,
+                                    double *residuals, void *stream)
+{
+    if (d_row_ptr == nullptr || (nnz > 0 && (d_col_ind == nullptr || d_vals == nullptr)) ||
+        d_diag == nullptr || d_basis == nullptr || ranges == nullptr || n <= 0 || nnz < 0 ||
+        nclusters <= 0 || maxiter < 0) {
+        return IPT_CUDA_INVALID_ARGUMENT;
+    }
+    return cluster_basis_solve(d_row_ptr, d_col_ind, d_vals, n, d_diag, ranges, nclusters,
+                               maxiter, tol, damping, d_basis, iterations, residuals, nullptr,
+                               (cudaStream_t)stream);
+}
+
+IPT_API int ipt_block_cluster_update(const double *d_basis, const double *d_y,
+                                     const double *d_diag, int n, int first, int m,
+                                     double damping, double *d_next, int *singular, void *stream)
+{
+    if (d_basis == nullptr || d_y == nullptr || d_diag == nullptr || d_next == nullptr || n <= 0 ||
+        m < 1 || m > kClusterMaxWidth || first < 0 || first + m > n) {
+        return IPT_CUDA_INVALID_ARGUMENT;
+    }
+    cudaStream_t s = (cudaStream_t)stream;
+    DeviceBuffer<int> I;
+    IPTGB_CHECK(I.alloc(6, s));
+    const int h[6] = {first, m, 0, 0, 1, 0};  // info, active, flags
+    IPTGB_CUDA(cudaMemcpyAsync(I.ptr, h, sizeof(h), cudaMemcpyHostToDevice, s));
+    IPTGB_CHECK(launch_cluster_update(d_basis, d_y, d_diag, n, I.ptr, I.ptr + 4, 1, m,
+                                      cluster_update_smem(m), damping, d_next, I.ptr + 5, s));
+    int flag = 0;
+    IPTGB_CUDA(cudaMemcpyAsync(&flag, I.ptr + 5, sizeof(int), cudaMemcpyDeviceToHost, s));
+    IPTGB_CUDA(cudaStreamSynchronize(s));
+    if (singular != nullptr) *singular = flag & 1;
+    return IPT_CUDA_SUCCESS;
+}

@@ -127,6 +127,54 @@ int ipt_block_solve_csr(const int *row_ptr, const int *col_ind, const double *va
  * eigenvectors d_Z (m*m, column-major); synchronises `stream`. */
 int ipt_block_symmetric_eig(const double *d_T, int m, double *d_w, double *d_Z, void *stream);
 
+/* ---- block-cluster path (the reference's IPT_BLOCK_CLUSTER) --------------
+ *
+ * Host only.  Cluster ranges of a symmetric CSC matrix whose diagonal is
+ * ascending (the prepared, diagonal-sorted matrix): the targets 0..k-1 are
+ * joined with the rows whose diagonal gap is numerically zero or small
+ * against their coupling, as the reference's degenerate-subspace detection
+ * (IPT_C_GPU/src/ipt_preparation.cu:502-644, environment knobs
+ * IPT_EPS_MULTIPLIER, IPT_REL_GAP_TOL, IPT_COUPLING_GAP_RATIO_TOL,
+ * IPT_COUPLING_ETA, IPT_MAX_LIFT_BLOCK_SIZE); targets left alone become
+ * singleton clusters (IPT_C_GPU/src/ipt_cuda.cu:4114-4132); with `adaptive`
+ * the cluster of target requested_k-1 grows by its most strongly coupled
+ * outside rows while |H_ij|/gap > coupling_tau (ipt_cuda.cu:4134-4272).
+ * ranges receives `*count` inclusive (first, last) pairs in ascending order.
+ * IPT_CUDA_INVALID_ARGUMENT for invalid input, a cluster wider than the
+ * limit (ipt_cuda.cu:4619-4632) or capacity < *count. */
+int ipt_block_cluster_ranges(const int *col_ptr, const int *row_ind, const double *vals, int n,
+                             int nnz, int k, int requested_k, double degeneracy_threshold,
+                             int adaptive, double coupling_tau, int *ranges, int capacity,
+                             int *count, int *limit_hit);
+
+/* Block-cluster basis (replaces ipt_block_cluster_solve_basis_gpu, one call
+ * per cluster, IPT_C_GPU/src/ipt_cuda.cu:2871-3037): for each of the
+ * `nclusters` host ranges (inclusive, ascending, disjoint, width <= 64) the
+ * fixed point X'[i,:] = (d_i I - h^T)^{-1} (d_i X[i,:] - Y[i,:]) with
+ * Y = H X, h = Y[first..last, :] and identity rows inside the cluster, from
+ * the identity columns, until ||X'-X||_F / max(1, ||X||_F) <= tol (tol <= 0:
+ * 1e-12) or maxiter; damping outside (0, 1] counts as 1.  H is device CSR
+ * (0-based) with ascending diagonal d_diag; d_basis (n x sum of widths,
+ * column-major) gets the clusters' columns one after the other; iterations
+ * and residuals (host, nclusters) the per-cluster iteration counts and last
+ * fixed-point residuals.  IPT_CUDA_INVALID_ARGUMENT for a singular row system
+ * or a non-finite iterate.  Synchronises `stream`. */
+int ipt_block_cluster_basis(const int *d_row_ptr, const int *d_col_ind, const double *d_vals,
+                            int n, int nnz, const double *d_diag, const int *ranges,
+                            int nclusters, int maxiter, double tol, double damping,
+                            double *d_basis, int *iterations, double *residuals, void *stream);
+
+/* One block-cluster update of a single cluster [first, first+m) (replaces
+ * ipt_block_cluster_update_kernel, IPT_C_GPU/src/ipt_cuda.cu:2280-2384):
+ * d_next from d_basis and d_y = H d_basis (both n x m, device), with the
+ * kernel's damping rule (value = (1-damping) x + damping value when
+ * damping < 1).  *singular = 1 when a row system is singular (pivot not above
+ * 64 DBL_EPSILON or not finite) or a value is not finite.  Synchronises
+ * `stream`. */
+int ipt_block_cluster_update(const double *d_basis, const double *d_y, const double *d_diag,
+                             int n, int first, int m, double damping, double *d_next,
+                             int *singular, void *stream);
+
 /* Cholesky factor inverse of a small SPD Gram matrix (m <= 112, column-major,
  * device): G = R^T R, d_Rinv = R^{-1} (upper triangular, column-major), the
  * step of CholQR that replaces the reference's cusolverDnDpotrf + cublasDtrsm

@@ -11,7 +11,8 @@ libraries:
   oracle/_ref/libref_dense.so   ref_ipt_cpu_reference, ref_fill_perturbative_matrix,
                                 ref_max_relative_residual
   oracle/_ref/libref_sparse.so  ref_sparse_ipt_cpu_reference, ref_build_banded_csc,
-                                ref_h20_w_csc, ref_prepare_sparse_csc_sorted
+                                ref_h20_w_csc, ref_prepare_sparse_csc_sorted,
+                                ref_block_cluster_prepare, ref_block_cluster_solve_basis
 
 Nothing from the reference is copied into the repository; the outputs are
 git-ignored.  The reference path only exists in the build container, so the
@@ -117,6 +118,48 @@ extern "C" int ref_prepare_sparse_csc_sorted(const int *col_ptr, const int *row_
     int out = p.nnz;
     ipt_prepared_csc_free(&p);
     return out;
+}
+/* Block-cluster preparation (ipt_block_cluster_prepare, ipt_cuda.cu:4555-4688):
+ * the cluster ranges of the diagonal-sorted matrix; returns the range count,
+ * or -status. */
+extern "C" int ref_block_cluster_prepare(const int *col_ptr, const int *row_ind,
+                                         const double *values, int n, int k, int nnz,
+                                         int *out_ranges, int capacity, int *out_limit_hit,
+                                         int *out_added, int added_capacity, int *out_added_count) {
+    IPTCudaResult r;
+    memset(&r, 0, sizeof(r));
+    IPTBlockClusterPreparation p;
+    int s = ipt_block_cluster_prepare(col_ptr, row_ind, values, n, k, nnz, 100, 0.0, 0, &r, &p);
+    if (s != 0) return -s;
+    int cnt = (int)p.ranges.size();
+    for (int i = 0; i < cnt && i < capacity; ++i) {
+        out_ranges[2 * i] = p.ranges[i].first;
+        out_ranges[2 * i + 1] = p.ranges[i].second;
+    }
+    *out_limit_hit = p.adaptive_limit_hit;
+    *out_added_count = (int)p.adaptive_added_indices.size();
+    for (int i = 0; i < *out_added_count && i < added_capacity; ++i) {
+        out_added[i] = p.adaptive_added_indices[i];
+    }
+    return cnt;
+}
+/* The reference's CPU block-cluster basis solve of one cluster
+ * (ipt_block_cluster_solve_basis, ipt_cuda.cu:4274-4395) on a sorted CSC;
+ * returns 1 on success, 0 when a row system is singular or an entry is not
+ * finite. */
+extern "C" int ref_block_cluster_solve_basis(const int *col_ptr, const int *row_ind,
+                                             const double *values, int n, int nnz,
+                                             const double *diag, int first, int last,
+                                             int maxiter, double tol, double damping,
+                                             double *basis_out, int *iterations) {
+    std::vector<int> cp(col_ptr, col_ptr + n + 1), ri(row_ind, row_ind + nnz);
+    std::vector<double> va(values, values + nnz), d(diag, diag + n), b;
+    int it = 0;
+    int ok = ipt_block_cluster_solve_basis(cp, ri, va, d, first, last, maxiter, tol, damping,
+                                           &b, &it);
+    if (ok) memcpy(basis_out, b.data(), b.size() * sizeof(double));
+    *iterations = it;
+    return ok;
 }
 '''
 

@@ -535,3 +535,145 @@ ORACLE_API int oracle_ipt_dense_products_to_residual(const double *matrix, int n
     free(x); free(y); free(diag); free(cdiag);
     return found;
 }
+
+/* ---- block-cluster path ----------------------------------------------------
+ * One block-cluster update of the cluster [first, first + m): the GPU kernel
+ * ipt_block_cluster_update_kernel (IPT_C_GPU/src/ipt_cuda.cu:2280-2384) row
+ * by row.  basis and y (= H basis) are n x m, column-major; rows inside the
+ * cluster get the identity, every other row i solves
+ *   (d_i I - h^T) x = d_i basis[i, :] - y[i, :],  h[u + e m] = y[first + u, e]
+ * by Gauss-Jordan elimination with partial pivoting: the pivot is the first
+ * row with the largest |entry| (the reference's scan, strict comparison),
+ * singular when that entry is not finite or not above 64 DBL_EPSILON.  The
+ * products are placed as the library's CUDA kernel places them (the right
+ * side fma(d, x, -y), the elimination a[e][j] = fma(-a[e][p], a[p][j],
+ * a[e][j]), the damping fma(damping, v, (1 - damping) x)), so that both give
+ * the same bits.  Returns 1 if a row system is singular or a value is not
+ * finite (its entries are then 0 or unset), 0 otherwise. */
+ORACLE_API int oracle_cluster_update(const double *basis, const double *y, const double *diag,
+                                     int n, int first, int m, double damping, double *next)
+{
+    const int ld = m + 1;
+    double *aug = (double *)malloc((size_t)m * (size_t)ld * sizeof(double));
+    int singular_any = 0;
+    for (int row = 0; row < n; ++row) {
+        if (row >= first && row < first + m) {
+            for (int e = 0; e < m; ++e) {
+                next[(size_t)row + (size_t)e * n] = row == first + e ? 1.0 : 0.0;
+            }
+            continue;
+        }
+        const double dr = diag[row];
+        for (int e = 0; e < m; ++e) {
+            double *a = aug + (size_t)e * ld;
+            for (int u = 0; u < m; ++u) {
+                a[u] = (e == u ? dr : 0.0) - y[(size_t)(first + u) + (size_t)e * n];
+            }
+            a[m] = fma(dr, basis[(size_t)row + (size_t)e * n], -y[(size_t)row + (size_t)e * n]);
+        }
+        int singular = 0;
+        for (int p = 0; p < m && !singular; ++p) {
+            int piv = p;
+            double pa = fabs(aug[(size_t)p * ld + p]);
+            for (int c = p + 1; c < m; ++c) {
+                const double ca = fabs(aug[(size_t)c * ld + p]);
+                if (ca > pa) {
+                    pa = ca;
+                    piv = c;
+                }
+            }
+            if (!isfinite(pa) || pa <= 64.0 * 2.220446049250313e-16) {
+                singular = 1;
+                break;
+            }
+            double *ap = aug + (size_t)p * ld;
+            if (piv != p) {
+                double *aq = aug + (size_t)piv * ld;
+                for (int j = p; j <= m; ++j) {
+                    const double t = ap[j];
+                    ap[j] = aq[j];
+                    aq[j] = t;
+                }
+            }
+            const double pv = ap[p];
+            for (int j = p; j <= m; ++j) ap[j] = ap[j] / pv;
+            for (int e = 0; e < m; ++e) {
+                if (e == p) continue;
+                double *a = aug + (size_t)e * ld;
+                const double f = a[p];
+                for (int j = p; j <= m; ++j) a[j] = fma(-f, ap[j], a[j]);
+            }
+        }
+        if (!singular) {
+            for (int e = 0; e < m; ++e) {
+                double v = aug[(size_t)e * ld + m];
+                if (damping < 1.0) {
+                    v = fma(damping, v, (1.0 - damping) * basis[(size_t)row + (size_t)e * n]);
+                }
+                if (!isfinite(v)) {
+                    singular = 1;
+                    v = 0.0;
+                }
+                next[(size_t)row + (size_t)e * n] = v;
+            }
+        }
+        singular_any |= singular;
+    }
+    free(aug);
+    return singular_any;
+}
+
+/* The block-cluster basis of each cluster in turn, as
+ * ipt_block_cluster_solve_basis_gpu (IPT_C_GPU/src/ipt_cuda.cu:2871-3037):
+ * identity start, Y = H X (CSR rows summed in stored order), one update,
+ * residual ||X' - X||_F / max(1, ||X||_F), stop at tol (tol <= 0: 1e-12) or
+ * maxiter; damping outside (0, 1] counts as 1.  ranges: nclusters inclusive
+ * (first, last) pairs; basis: n x sum of widths.  Returns 0, or 1 + the
+ * index of the first cluster whose row system was singular or whose iterate
+ * or norms were not finite. */
+ORACLE_API int oracle_cluster_basis(const int *row_ptr, const int *col_ind, const double *values,
+                                    const double *diag, int n, const int *ranges, int nclusters,
+                                    int maxiter, double tol, double damping, double *basis,
+                                    int *iterations, double *residuals)
+{
+    const double eff_tol = tol > 0.0 ? tol : 1.0e-12;
+    if (!(damping > 0.0 && damping <= 1.0)) damping = 1.0;
+    size_t off = 0;
+    for (int c = 0; c < nclusters; ++c) {
+        const int first = ranges[2 * c], m = ranges[2 * c + 1] - ranges[2 * c] + 1;
+        const size_t cnt = (size_t)n * (size_t)m;
+        double *x = basis + off * (size_t)n;
+        double *y = (double *)malloc(cnt * sizeof(double));
+        double *nx = (double *)malloc(cnt * sizeof(double));
+        for (size_t i = 0; i < cnt; ++i) {
+            const int j = (int)(i / (size_t)n), r = (int)(i % (size_t)n);
+            x[i] = r == first + j ? 1.0 : 0.0;
+        }
+        iterations[c] = 0;
+        residuals[c] = NAN;
+        for (int it = 0; it < maxiter; ++it) {
+            oracle_csr_matmul(row_ptr, col_ind, values, n, x, m, y);
+            int bad = oracle_cluster_update(x, y, diag, n, first, m, damping, nx);
+            double dd = 0.0, bb = 0.0;
+            for (size_t i = 0; i < cnt; ++i) {
+                const double dx = nx[i] - x[i];
+                dd += dx * dx;
+                bb += x[i] * x[i];
+            }
+            const double dn = sqrt(dd), bn = sqrt(bb);
+            if (bad || !isfinite(dn) || !isfinite(bn) || bn <= 0.0) {
+                free(y);
+                free(nx);
+                return 1 + c;
+            }
+            memcpy(x, nx, cnt * sizeof(double));
+            iterations[c] = it + 1;
+            residuals[c] = dn / fmax(1.0, bn);
+            if (residuals[c] <= eff_tol) break;
+        }
+        free(y);
+        free(nx);
+        off += (size_t)m;
+    }
+    return 0;
+}

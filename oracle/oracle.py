@@ -60,6 +60,10 @@ def lib():
         L.oracle_ipt_dense_products_to_residual.restype = i
         L.oracle_ipt_dense_products_to_residual.argtypes = [vp, i, i, i, d, d, vp]
         L.oracle_num_threads.restype = i
+        L.oracle_cluster_update.restype = i
+        L.oracle_cluster_update.argtypes = [vp, vp, vp, i, i, i, d, vp]
+        L.oracle_cluster_basis.restype = i
+        L.oracle_cluster_basis.argtypes = [vp, vp, vp, vp, i, vp, i, i, d, d, vp, vp, vp]
         _lib = L
     return _lib
 
@@ -251,8 +255,251 @@ def ref_lib(which):
             L.ref_h20_w_csc.argtypes = [vp, vp, vp]
             L.ref_prepare_sparse_csc_sorted.restype = i
             L.ref_prepare_sparse_csc_sorted.argtypes = [vp, vp, vp, i, i, i, vp, vp, vp, vp, vp]
+            L.ref_block_cluster_prepare.restype = i
+            L.ref_block_cluster_prepare.argtypes = [vp, vp, vp, i, i, i, vp, i, vp, vp, i, vp]
+            L.ref_block_cluster_solve_basis.restype = i
+            L.ref_block_cluster_solve_basis.argtypes = [vp, vp, vp, i, i, vp, i, i, i,
+                                                        C.c_double, C.c_double, vp, vp]
         _ref[which] = L
     return _ref[which]
+
+
+# ---- block-cluster path ---------------------------------------------------------
+def cluster_test_matrix(n, seed, coupling=0.05, groups=3, density=0.05):
+    """Symmetric CSC test matrix for the block-cluster path: ascending
+    diagonal with planted exact and near (1e-13) degeneracies among the
+    lowest entries, random symmetric off-diagonal entries of the given
+    scale.  Returns (col_ptr, row_ind, values, dense H)."""
+    rng = np.random.default_rng(seed)
+    d = np.sort(rng.uniform(0, n, n))
+    for g in range(groups):
+        i = int(rng.integers(0, min(n - 4, 12)))
+        w = int(rng.integers(2, 4))
+        d[i:i + w] = d[i] + (rng.uniform(0, 1e-13, w) if g % 2 else 0.0)
+    d = np.sort(d)
+    mask = rng.uniform(size=(n, n)) < density
+    A = np.triu(np.where(mask, rng.normal(scale=coupling, size=(n, n)), 0.0), 1)
+    H = np.diag(d) + A + A.T
+    cp, ri, va = [0], [], []
+    for c in range(n):
+        for r in range(n):
+            if H[r, c] != 0.0 or r == c:
+                ri.append(r)
+                va.append(H[r, c])
+        cp.append(len(ri))
+    return (np.array(cp, np.int32), np.array(ri, np.int32), np.array(va, np.float64),
+            np.asfortranarray(H))
+
+
+def cluster_update(basis, y, diag, first, damping=1.0):
+    """One block-cluster update (oracle_cluster_update); returns (next, singular)."""
+    basis = np.asfortranarray(basis, dtype=np.float64)
+    y = np.asfortranarray(y, dtype=np.float64)
+    diag = np.ascontiguousarray(diag, dtype=np.float64)
+    n, m = basis.shape
+    nxt = np.zeros((n, m), dtype=np.float64, order="F")
+    s = lib().oracle_cluster_update(_p(basis), _p(y), _p(diag), n, first, m, damping, _p(nxt))
+    return nxt, bool(s)
+
+
+def cluster_basis(row_ptr, col_ind, vals, diag, ranges, maxiter, tol, damping=1.0):
+    """Block-cluster basis of every cluster (oracle_cluster_basis); returns
+    (basis, iterations, residuals, status) with status 0 or 1 + the failing
+    cluster."""
+    rp = np.ascontiguousarray(row_ptr, dtype=np.int32)
+    ci = np.ascontiguousarray(col_ind, dtype=np.int32)
+    va = np.ascontiguousarray(vals, dtype=np.float64)
+    dg = np.ascontiguousarray(diag, dtype=np.float64)
+    rg = np.ascontiguousarray(np.asarray(ranges, dtype=np.int32).reshape(-1))
+    C_ = rg.size // 2
+    n = rp.size - 1
+    cols = int(sum(rg[2 * c + 1] - rg[2 * c] + 1 for c in range(C_)))
+    X = np.zeros((n, cols), dtype=np.float64, order="F")
+    it = np.zeros(C_, dtype=np.int32)
+    res = np.zeros(C_, dtype=np.float64)
+    st = lib().oracle_cluster_basis(_p(rp), _p(ci if ci.size else np.zeros(1, np.int32)),
+                                    _p(va if va.size else np.zeros(1)), _p(dg), n, _p(rg), C_,
+                                    maxiter, tol, damping, _p(X), _p(it), _p(res))
+    return X, it, res, st
+
+
+def cluster_ranges(cp, ri, va, n, k, requested_k=None, threshold=0.0, adaptive=False,
+                   tau=0.1, eps_multiplier=1000.0, rel_gap_tol=1e-12, ratio_tol=0.2,
+                   eta=0.02, max_block=64):
+    """Cluster ranges of the block-cluster path for a CSC matrix with
+    ascending diagonal, restated in Python (small n): degenerate-subspace
+    detection IPT_C_GPU/src/ipt_preparation.cu:345-644, singleton targets
+    IPT_C_GPU/src/ipt_cuda.cu:4114-4132, adaptive expansion :4134-4272.
+    Returns (ranges, added, limit_hit, too_large)."""
+    import math
+    requested_k = k if requested_k is None else requested_k
+    eps = np.finfo(np.float64).eps
+    diag = [0.0] * n
+    for c in range(n):
+        for p_ in range(cp[c], cp[c + 1]):
+            if ri[p_] == c:
+                diag[c] = float(va[p_])
+                break
+    tau_num = eps_multiplier * eps * max(1.0, max(abs(x) for x in diag))
+    rt = max(ratio_tol, eps)
+    cs = [0.0] * n
+    rs = [0.0] * n
+    for c in range(n):
+        for p_ in range(cp[c], cp[c + 1]):
+            r = int(ri[p_])
+            if r != c:
+                cs[c] = max(cs[c], abs(va[p_]))
+                rs[r] = max(rs[r], abs(va[p_]))
+    off = [max(cs[i], rs[i]) for i in range(n)]
+
+    def floor_(a, b):
+        return max(max(threshold, tau_num), rel_gap_tol * max(1.0, abs(a), abs(b)))
+
+    def entry(r, c):
+        for p_ in range(cp[c], cp[c + 1]):
+            if ri[p_] == r:
+                return float(va[p_])
+        return 0.0
+
+    parent = list(range(n))
+    rank = [0] * n
+
+    def find(x):
+        while parent[x] != x:
+            parent[x] = parent[parent[x]]
+            x = parent[x]
+        return x
+
+    def unite(a, b):
+        a, b = find(a), find(b)
+        if a == b:
+            return
+        if rank[a] < rank[b]:
+            a, b = b, a
+        parent[b] = a
+        if rank[a] == rank[b]:
+            rank[a] += 1
+
+    order = sorted(range(n), key=lambda i: (diag[i], i))
+    for col in range(min(k, n)):
+        dc = diag[col]
+        w = max(floor_(dc, dc), off[col] / rt)
+        for row in order:
+            dr = diag[row]
+            if row == col or dr < dc - w or dr > dc + w:
+                continue
+            cpl = max(abs(entry(row, col)), abs(entry(col, row)))
+            if not cpl > 0.0:
+                cpl = eta * min(off[row], off[col])
+            gap = abs(dr - dc)
+            fl = floor_(dr, dc)
+            if gap <= fl or (cpl > 0.0 and cpl / max(gap, fl) >= rt):
+                unite(row, col)
+    comp = {}
+    for i in range(n):
+        r = find(i)
+        lo, hi, t = comp.get(r, (n, -1, False))
+        comp[r] = (min(lo, i), max(hi, i), t or i < k)
+    rg = sorted((lo, hi) for lo, hi, t in comp.values() if t and lo < hi)
+    merged = []
+    for a, b in rg:
+        if merged and a <= merged[-1][1] + 1:
+            merged[-1] = (merged[-1][0], max(merged[-1][1], b))
+        else:
+            merged.append((a, b))
+    too_large = any(b - a + 1 > max_block for a, b in merged)
+    covered = set()
+    for a, b in merged:
+        covered.update(range(a, b + 1))
+    merged += [(t, t) for t in range(min(k, n)) if t not in covered]
+    ranges = sorted(merged)
+    added, limit_hit = [], False
+    if adaptive and not too_large:
+        def degenerate(a, b):
+            g = max(1e-14, 1000.0 * eps * max(1.0, abs(diag[a]), abs(diag[b])))
+            return abs(diag[a] - diag[b]) <= g
+        while True:
+            tid = next((i for i, (a, b) in enumerate(ranges) if a <= requested_k - 1 <= b), -1)
+            if tid < 0:
+                break
+            first, last = ranges[tid]
+            best, best_row = 0.0, -1
+            for col in range(first, last + 1):
+                for p_ in range(cp[col], cp[col + 1]):
+                    row = int(ri[p_])
+                    if first <= row <= last:
+                        continue
+                    ratio = abs(va[p_]) / max(abs(diag[col] - diag[row]), 1e-14)
+                    if max(last, row) - min(first, row) + 1 > max_block:
+                        limit_hit = limit_hit or ratio > tau
+                        continue
+                    if ratio > best:
+                        best, best_row = ratio, row
+            if best_row < 0 or best <= tau:
+                break
+            pf, pl = min(first, best_row), max(last, best_row)
+            grew = True
+            while grew:
+                grew = False
+                if pf > 0 and degenerate(pf, pf - 1):
+                    pf -= 1
+                    grew = True
+                if pl + 1 < n and degenerate(pl, pl + 1):
+                    pl += 1
+                    grew = True
+            if pl - pf + 1 > max_block:
+                limit_hit = True
+                break
+            added += [i for i in range(pf, pl + 1) if i < first or i > last]
+            ranges[tid] = (pf, pl)
+            ranges.sort()
+            m2 = []
+            for a, b in ranges:
+                if not m2 or a > m2[-1][1]:
+                    m2.append((a, b))
+                else:
+                    m2[-1] = (m2[-1][0], max(m2[-1][1], b))
+            ranges = m2
+    del math
+    return ranges, sorted(set(added)), limit_hit, too_large
+
+
+def ref_cluster_prepare(cp, ri, va, n, k):
+    """The reference's own block-cluster preparation (needs oracle/_ref):
+    ranges of the diagonal-sorted matrix, (ranges, added, limit_hit) or a
+    negative status."""
+    L = ref_lib("sparse")
+    cp = np.ascontiguousarray(cp, dtype=np.int32)
+    ri = np.ascontiguousarray(ri, dtype=np.int32)
+    va = np.ascontiguousarray(va, dtype=np.float64)
+    cap = n
+    rg = np.zeros(2 * cap, dtype=np.int32)
+    lim = np.zeros(1, dtype=np.int32)
+    added = np.zeros(n, dtype=np.int32)
+    na = np.zeros(1, dtype=np.int32)
+    cnt = L.ref_block_cluster_prepare(_p(cp), _p(ri), _p(va), n, k, int(cp[-1]), _p(rg), cap,
+                                      _p(lim), _p(added), n, _p(na))
+    if cnt < 0:
+        return cnt
+    return ([(int(rg[2 * i]), int(rg[2 * i + 1])) for i in range(cnt)],
+            [int(x) for x in added[:na[0]]], bool(lim[0]))
+
+
+def ref_cluster_solve_basis(cp, ri, va, diag, first, last, maxiter, tol, damping=1.0):
+    """The reference's CPU block-cluster basis solve of one cluster (needs
+    oracle/_ref); (basis, iterations) or None when it reports failure."""
+    L = ref_lib("sparse")
+    cp = np.ascontiguousarray(cp, dtype=np.int32)
+    ri = np.ascontiguousarray(ri, dtype=np.int32)
+    va = np.ascontiguousarray(va, dtype=np.float64)
+    dg = np.ascontiguousarray(diag, dtype=np.float64)
+    n = cp.size - 1
+    m = last - first + 1
+    X = np.zeros((n, m), dtype=np.float64, order="F")
+    it = np.zeros(1, dtype=np.int32)
+    ok = L.ref_block_cluster_solve_basis(_p(cp), _p(ri), _p(va), n, int(cp[-1]), _p(dg), first,
+                                         last, maxiter, tol, damping, _p(X), _p(it))
+    return (X, int(it[0])) if ok else None
 
 
 # ---- matrix-free FCI-like construction (fci_oracle.c) -------------------------

@@ -1,0 +1,176 @@
+"""Block-cluster path on the GPU: the update kernel bit for bit against the
+oracle's restatement, the basis solve against the oracle and the
+reference's own CPU solve (committed fixtures), and the IPT_BLOCK_CLUSTER
+entry end to end."""
+import os
+
+import numpy as np
+import pytest
+
+from block_ipt_gb300 import api
+from oracle import oracle
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "cluster_kat.npz")
+
+
+def dev(torch, a, dtype=None):
+    t = torch.from_numpy(np.ascontiguousarray(a.T if a.ndim == 2 else a))
+    return t.cuda() if dtype is None else t.to(dtype).cuda()
+
+
+def to_f(torch, t, n, m):
+    return t.cpu().numpy().T.copy(order="F") if m > 0 else t.cpu().numpy()
+
+
+def update_case(rng, n, m, first):
+    d = np.sort(rng.uniform(0, n, n))
+    X = rng.standard_normal((n, m))
+    Y = rng.standard_normal((n, m)) * 0.5 + d[:, None] * X
+    return d, np.asfortranarray(X), np.asfortranarray(Y)
+
+
+@pytest.mark.parametrize("m", [1, 2, 3, 4, 5, 7, 8, 9, 16, 17, 31, 32, 33, 48, 64])
+@pytest.mark.parametrize("damping", [1.0, 0.6])
+def test_update_bit_exact(cuda, m, damping):
+    torch = cuda
+    rng = np.random.default_rng(100 + m)
+    n = 300
+    first = int(rng.integers(0, n - m))
+    d, X, Y = update_case(rng, n, m, first)
+    want, sing = oracle.cluster_update(X, Y, d, first, damping)
+    assert not sing
+    dX, dY, dd = dev(torch, X), dev(torch, Y), dev(torch, d)
+    dN = torch.zeros((m, n), dtype=torch.float64, device="cuda")
+    s = api.cluster_update(dX.data_ptr(), dY.data_ptr(), dd.data_ptr(), n, first, m, dN.data_ptr(),
+                           damping)
+    got = dN.cpu().numpy().T
+    assert not s
+    assert np.array_equal(got.view(np.uint64), want.view(np.uint64)), np.abs(got - want).max()
+    np.testing.assert_array_equal(got[first:first + m], np.eye(m))
+
+
+@pytest.mark.parametrize("m", [1, 3, 40])
+def test_update_singular_flag(cuda, m):
+    """A row whose system is singular (d_i I - h^T with a zero pivot) or whose
+    solution is not finite sets the flag, as in the oracle."""
+    torch = cuda
+    rng = np.random.default_rng(7)
+    n = 120
+    first = 10
+    d, X, Y = update_case(rng, n, m, first)
+    # h = Y[first:first+m, :] = diag(d[50]) makes row 50's matrix exactly zero
+    Y[first:first + m, :] = 0.0
+    Y[np.arange(first, first + m), np.arange(m)] = d[50]
+    want, sing = oracle.cluster_update(X, Y, d, first)
+    assert sing
+    dX, dY, dd = dev(torch, X), dev(torch, Y), dev(torch, d)
+    dN = torch.zeros((m, n), dtype=torch.float64, device="cuda")
+    assert api.cluster_update(dX.data_ptr(), dY.data_ptr(), dd.data_ptr(), n, first, m,
+                              dN.data_ptr())
+    # a NaN on the right side: the value is not finite
+    d, X, Y = update_case(rng, n, m, first)
+    Y[77, 0] = np.nan
+    want, sing = oracle.cluster_update(X, Y, d, first)
+    assert sing
+    dX, dY = dev(torch, X), dev(torch, Y)
+    assert api.cluster_update(dX.data_ptr(), dY.data_ptr(), dd.data_ptr(), n, first, m,
+                              dN.data_ptr())
+
+
+def run_basis(torch, cp, ri, va, diag, ranges, maxiter, tol, damping):
+    n = cp.size - 1
+    cols = int(sum(b - a + 1 for a, b in ranges))
+    drp, dci = dev(torch, cp.astype(np.int32)), dev(torch, ri.astype(np.int32))
+    dva, dd = dev(torch, va), dev(torch, diag)
+    dB = torch.zeros((cols, n), dtype=torch.float64, device="cuda")
+    it, res = api.cluster_basis(drp.data_ptr(), dci.data_ptr(), dva.data_ptr(), n, ri.size,
+                                dd.data_ptr(), ranges, maxiter, tol, dB.data_ptr(), damping)
+    return dB.cpu().numpy().T.copy(order="F"), it, res
+
+
+def test_basis_matches_reference_fixtures(cuda):
+    """Each fixture (the reference's own CPU solve): the GPU basis and
+    iteration counts against it and against the oracle."""
+    kat = np.load(GOLDEN)
+    for c in [str(x) for x in kat["cases"]]:
+        k, adaptive, damping, maxiter, tol = kat[c + "_params"]
+        cp, ri, va = kat[c + "_prep_col_ptr"], kat[c + "_prep_row_ind"], kat[c + "_prep_values"]
+        diag = kat[c + "_prep_diag"]
+        ranges = [tuple(r) for r in kat[c + "_ranges"].tolist()]
+        X, it, res = run_basis(cuda, cp, ri, va, diag, ranges, int(maxiter), tol, damping)
+        Xo, ito, reso, st = oracle.cluster_basis(cp, ri, va, diag, ranges, int(maxiter), tol,
+                                                 damping)
+        assert st == 0
+        ref = kat[c + "_basis"]
+        scale = max(1.0, np.abs(ref).max())
+        assert np.abs(X - ref).max() / scale <= 1e-11, c
+        assert np.abs(X - Xo).max() / scale <= 1e-12, c
+        np.testing.assert_array_equal(it, kat[c + "_iterations"])
+        np.testing.assert_array_equal(it, ito)
+        # the residuals near convergence are differences at rounding level
+        np.testing.assert_allclose(res, reso, rtol=1e-3, atol=1e-14)
+
+
+def test_basis_sweep_against_oracle(cuda):
+    worst = 0.0
+    for seed in range(10):
+        for coupling in (0.01, 0.3):
+            n = 80 + 7 * seed
+            cp, ri, va, H = oracle.cluster_test_matrix(n, seed, coupling)
+            ranges, _, _, _ = oracle.cluster_ranges(cp, ri, va, n, 8,
+                                                    adaptive=bool(seed % 2))
+            diag = np.diag(H).copy()
+            for damping in (1.0, 0.8):
+                X, it, _ = run_basis(cuda, cp, ri, va, diag, ranges, 50, 1e-12, damping)
+                Xo, ito, _, st = oracle.cluster_basis(cp, ri, va, diag, ranges, 50, 1e-12,
+                                                      damping)
+                assert st == 0
+                err = np.abs(X - Xo).max() / max(1.0, np.abs(Xo).max())
+                worst = max(worst, err)
+                assert np.all(np.abs(it - ito) <= 1), (it, ito)
+    assert worst <= 1e-12, worst
+
+
+def test_basis_rejects_bad_ranges(cuda):
+    torch = cuda
+    cp, ri, va, H = oracle.cluster_test_matrix(30, 1, 0.1)
+    for ranges in ([(3, 2)], [(0, 4), (4, 6)], [(0, 64)], [(28, 30)]):
+        with pytest.raises(Exception):
+            run_basis(torch, cp, ri, va, np.diag(H).copy(), ranges, 10, 1e-12, 1.0)
+
+
+@pytest.mark.parametrize("adaptive,n,seed,k", [("0", 90, 5, 6), ("1", 56, 5, 4)])
+def test_block_cluster_entry_degenerate(cuda, monkeypatch, adaptive, n, seed, k):
+    """ipt_cuda_sparse_csc_tol with IPT_BLOCK_CLUSTER on a matrix with planted
+    degeneracies: the cluster basis, Rayleigh-Ritz and the Davidson
+    enrichment give the lowest eigenpairs (ipt_cuda.cu:4712-5016)."""
+    monkeypatch.setenv("IPT_BLOCK_CLUSTER", "1")
+    monkeypatch.setenv("IPT_BLOCK_CLUSTER_ADAPTIVE", adaptive)
+    monkeypatch.setenv("IPT_DAVIDSON_ENRICH", "1")
+    monkeypatch.setenv("IPT_DAVIDSON_STEPS", "40")
+    cp, ri, va, H = oracle.cluster_test_matrix(n, seed, 0.3)
+    X, v, info = api.ipt_cuda_sparse_csc_tol(cp, ri, va, n, k, 1e-12, 200)
+    w, _ = oracle.eigh_lowest(H, k)
+    scale = np.abs(H).sum(1).max()
+    np.testing.assert_allclose(v, w, atol=1e-9 * scale)
+    np.testing.assert_allclose(np.linalg.norm(X, axis=0), 1.0, atol=1e-10)
+    assert np.abs(H @ X - X * v).max() <= 1e-7 * scale
+    assert info["iterations"] > 0 and info["basis_cols"] >= k
+    want = oracle.cluster_ranges(cp, ri, va, n, k, adaptive=adaptive == "1")
+    added = ";".join(str(i) for i in want[1]) or "none"
+    assert info["adaptive_added_indices"] == added
+
+
+def test_block_cluster_entry_singular_block(cuda, monkeypatch):
+    """A cluster whose row system turns singular makes the entry fail with
+    an invalid argument, as the oracle's (and the reference's) block solve
+    does (ipt_cuda.cu:2994-3000, 4872-4881: no identity fallback)."""
+    monkeypatch.setenv("IPT_BLOCK_CLUSTER", "1")
+    n, k = 90, 6
+    cp, ri, va, H = oracle.cluster_test_matrix(n, 2, 0.3)
+    ranges, _, _, _ = oracle.cluster_ranges(cp, ri, va, n, k)
+    assert oracle.cluster_basis(cp, ri, va, np.diag(H).copy(), ranges, 200, 1e-12)[3] != 0
+    with pytest.raises(Exception):
+        api.ipt_cuda_sparse_csc_tol(cp, ri, va, n, k, 1e-12, 200)
