@@ -266,7 +266,7 @@ def profile_snapshot(lib):
     name = C.c_char_p()
     ms = C.c_double()
     cnt = C.c_longlong()
-    for kid in range(9):
+    for kid in range(10):
         lib.ipt_block_profile_read(kid, C.byref(name), C.byref(ms), C.byref(cnt))
         out[name.value.decode()] = (ms.value, cnt.value)
     return out
@@ -337,6 +337,7 @@ def fci_section(args, torch, lib, stream, flush, dev):
         learned_part = learned_section(args, torch, dev, stream, flush, solve, opt, e0, e1,
                                        times, rep)
     achieved = (2.0 * Hs.nnz * cols * len(times)) / (cp_ms * 1e-3) / 1e12 if cp_ms else None
+    cluster = cluster_part(args, torch, lib, stream, flush, dev, Hs, drp, dci, dvv, k, e0, e1)
     return {"workload": "FCI-like CSR, 10 orbitals 5a/5b, n=%d nnz=%d, k=%d, seed 0" % (n, Hs.nnz, k),
             "ms": statistics.mean(times), "report": {kk: rep[kk] for kk in (
                 "converged", "ipt_iterations", "davidson_steps", "restarts", "basis_cols",
@@ -345,7 +346,60 @@ def fci_section(args, torch, lib, stream, flush, dev):
             "csr_product": {"launches": cp_cnt, "ms_per_solve": cp_ms / len(times),
                             "achieved_fp64_tflops": achieved},
             "kernel_ms": {kk: round(val[0] / len(times), 4) for kk, val in prof.items() if val[1]},
-            "learned": learned_part}
+            "learned": learned_part, "block_cluster": cluster}
+
+
+def gj_fmas(m):
+    """FMAs of one row's Gauss-Jordan elimination of an m x (m+1) system."""
+    return (m - 1) * ((m + 1) * (m + 2) // 2 - 1)
+
+
+def cluster_part(args, torch, lib, stream, flush, dev, Hs, drp, dci, dvv, k, e0, e1):
+    """The block-cluster basis (the reference's IPT_BLOCK_CLUSTER stage) of
+    the same matrix: cluster ranges of the k targets on the host, the basis
+    solve on the device (CSR products + the Gauss-Jordan update kernel), and
+    the update kernel's FP64 roofline."""
+    from block_ipt_gb300 import api
+    n = Hs.shape[0]
+    ranges, _ = api.cluster_ranges(Hs.indptr, Hs.indices, Hs.data, n, k)
+    dd = torch.from_numpy(Hs.diagonal().copy()).to(dev)
+    cols = sum(b - a + 1 for a, b in ranges)
+    dB = torch.empty((cols, n), dtype=torch.float64, device=dev)
+
+    def run():
+        return api.cluster_basis(drp.data_ptr(), dci.data_ptr(), dvv.data_ptr(), n, int(Hs.nnz),
+                                 dd.data_ptr(), ranges, 100, 1e-12, dB.data_ptr(),
+                                 stream=stream.cuda_stream)
+
+    run()
+    times = []
+    for _ in range(max(1, args.fci_steps)):
+        flush.zero_()
+        e0.record(stream)
+        its, res = run()
+        e1.record(stream)
+        e1.synchronize()
+        times.append(e0.elapsed_time(e1))
+    lib.ipt_block_profile_reset()
+    lib.ipt_block_profile_enable(1)
+    run()
+    torch.cuda.synchronize()
+    lib.ipt_block_profile_enable(0)
+    prof = profile_snapshot(lib)
+    up_ms, up_cnt = prof["cluster_update"]
+    flops = sum(2.0 * gj_fmas(b - a + 1) * (n - (b - a + 1)) * int(its[c])
+                for c, (a, b) in enumerate(ranges))
+    peak = C.c_double(0.0)
+    lib.ipt_block_measure_fp64_peak(C.byref(peak))
+    ach = flops / (up_ms * 1e-3) / 1e12 if up_ms else None
+    return {"ranges": [list(r) for r in ranges if r[1] > r[0]], "clusters": len(ranges),
+            "basis_cols": cols, "iterations": [int(x) for x in its],
+            "max_fixed_point_residual": float(np.nanmax(res)), "ms": statistics.mean(times),
+            "update": {"launches": up_cnt, "ms_per_solve": up_ms, "fp64_tflops": ach,
+                       "peak_tflops": peak.value, "frac": ach / peak.value if ach else None,
+                       "bound": "fp64",
+                       "flops_per_solve": flops},
+            "csr_product_ms_per_solve": prof["csr_product"][0]}
 
 
 def learned_section(args, torch, dev, stream, flush, solve, opt, e0, e1, plain_times, plain_rep):

@@ -1155,7 +1155,7 @@ int ipt_block_sparse_host_entry(const int *col_ptr, const int *row_ind, const do
         if (status == IPT_CUDA_SUCCESS) {
             auto tb = std::chrono::steady_clock::now();
             int bad = -1;
-            status = cluster_basis_solve(rp.ptr, ci.ptr, cv.ptr, n, dd.ptr, rg.data(),
+            status = cluster_basis_solve(rp.ptr, ci.ptr, cv.ptr, n, prep.nnz, dd.ptr, rg.data(),
                                          (int)cr.ranges.size(), block_maxiter, block_tol, damping,
                                          basis.ptr, cl_it.data(), cl_res.data(), &bad, s);
             if (status != IPT_CUDA_SUCCESS && bad >= 0) {

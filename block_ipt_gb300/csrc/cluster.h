@@ -39,13 +39,14 @@ int launch_cluster_update(const double *X, const double *Y, const double *d, int
                           double damping, double *Xn, int *flags, cudaStream_t s);
 
 // The block-cluster basis (n x sum of widths, column-major, cluster after
-// cluster) of a CSR matrix with ascending diagonal d; ranges holds C
+// cluster) of a CSR matrix with ascending diagonal d (products in
+// double-float from 16384 rows, davidson_df_products); ranges holds C
 // inclusive (first, last) pairs.  iterations / residuals (host, C entries)
 // receive each cluster's iteration count and last fixed-point residual.
 // IPT_CUDA_INVALID_ARGUMENT for a singular row system or a non-finite
 // iterate, with the first such cluster in *first_error_cluster.
 int cluster_basis_solve(const int *row_ptr, const int *col_ind, const double *vals, int n,
-                        const double *d, const int *ranges, int C, int maxiter, double tol,
+                        int nnz, const double *d, const int *ranges, int C, int maxiter, double tol,
                         double damping, double *X, int *iterations, double *residuals,
                         int *first_error_cluster, cudaStream_t s);
 

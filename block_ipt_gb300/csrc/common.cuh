@@ -116,7 +116,8 @@ enum ProfiledKernel {
     kProfGram = 6,          // FP64 Gram products
     kProfTallGemm = 7,      // FP64 tall-by-small products
     kProfMlp = 8,           // learned-preconditioner kernels
-    kProfCount = 9
+    kProfClusterUpdate = 9, // block-cluster Gauss-Jordan update
+    kProfCount = 10
 };
 bool profile_enabled();
 // Phase marks (ipt_block_trace_*): when enabled, a one-thread kernel writes

@@ -20,15 +20,19 @@
 // updated again, so every cluster ends with exactly the iterate the
 // reference's own loop for it returns.
 //
-// The update gives each row's system to a team of T lanes (T the power of
-// two >= m, at most 32; several teams share a warp when m < 32), with the
-// augmented matrix in shared memory, row e of it owned by lane e mod T.  The
-// pivot is the first row holding the largest |entry| (the reference's
-// sequential scan with a strict comparison); a NaN diagonal entry, a pivot
-// that is not finite or not above 64 DBL_EPSILON is singular.  The
-// elimination keeps the reference's operations (row swap, division of the
-// pivot row by the pivot, a[e][j] -= a[e][p] a[p][j] as one FMA) so that the
-// CPU restatement of this kernel reproduces it bit for bit.
+// The update gives each row's system to a team of T lanes, with the
+// augmented matrix in shared memory and row e of it owned by lane e mod T.
+// On GB300 the FP64 pipe (about 2 operations per clock per SM) is the bound,
+// so the kernel keeps FP64 instructions to the elimination itself: T is the
+// smallest power of two for which the CTA's 128/T systems fit in ~96 KB of
+// shared memory (T = 1 up to m = 8: every lane works on its own row's
+// system), the pivot search compares |entries| as integers, a pivot row is
+// scaled by one reciprocal, and the column just eliminated (never read
+// again) is not updated.  The pivot is the first row holding the largest
+// |entry| (the reference's sequential scan with a strict comparison); a NaN
+// diagonal entry, a pivot that is not finite or not above 64 DBL_EPSILON is
+// singular.  The CPU restatement of this kernel (the oracle) performs the
+// same operations in the same order and reproduces it bit for bit.
 #include <float.h>
 #include <math.h>
 #include <string.h>
@@ -36,6 +40,7 @@
 #include <algorithm>
 #include <vector>
 
+#include "block_solver.h"
 #include "cluster.h"
 #include "common.cuh"
 #include "ipt_plain.h"
@@ -46,11 +51,17 @@ namespace iptgb {
 
 constexpr int kClusterThreads = 128;
 constexpr int kClusterNormSlices = 64;
+constexpr size_t kClusterSmemBudget = 96 * 1024;
 
+// Lanes per row system (a power of two, at most 32).
 __host__ __device__ __forceinline__ int cluster_team(int m)
 {
     int t = 1;
-    while (t < m && t < 32) t <<= 1;
+    while (t < 32 && (size_t)(kClusterThreads / t) * m * (m + 1) * sizeof(double) +
+                             (size_t)m * m * sizeof(double) >
+                         kClusterSmemBudget) {
+        t <<= 1;
+    }
     return t;
 }
 
@@ -60,7 +71,13 @@ size_t cluster_update_smem(int m)
     return ((size_t)m * m + (size_t)teams * m * (m + 1)) * sizeof(double);
 }
 
+constexpr uint64_t kAbsMask = 0x7FFFFFFFFFFFFFFFull;
+constexpr uint64_t kInfBits = 0x7FF0000000000000ull;
+constexpr uint64_t kTinyPivotBits = 0x3D10000000000000ull;  // 64 DBL_EPSILON = 2^-46
+
 // info[c] = {first, m, column offset, 0}; active[c] != 0 while c iterates.
+// Element (e, j) of a team's augmented system sits at ((e (m+1) + j) teams +
+// team): the teams of a warp touch consecutive words.
 __global__ void __launch_bounds__(kClusterThreads)
 cluster_update_kernel(const double *__restrict__ X, const double *__restrict__ Y,
                       const double *__restrict__ d, int n, const int4 *__restrict__ info,
@@ -80,7 +97,8 @@ cluster_update_kernel(const double *__restrict__ X, const double *__restrict__ Y
     double *h = cl_smem;  // h[u + e m] = Y[first + u, off + e]
     const int team = threadIdx.x / T;
     const int t = threadIdx.x % T;
-    double *aug = cl_smem + (size_t)m * m + (size_t)team * m * ld;
+    double *aug = cl_smem + (size_t)m * m + team;
+#define AUG(e, j) aug[((size_t)(e) * ld + (j)) * teams]
     const unsigned lane = threadIdx.x & 31u;
     const unsigned tmask =
         T == 32 ? 0xffffffffu : (((1u << T) - 1u) << (lane / (unsigned)T * (unsigned)T));
@@ -101,72 +119,73 @@ cluster_update_kernel(const double *__restrict__ X, const double *__restrict__ Y
         }
         const double dr = d[row];
         for (int e = t; e < m; e += T) {
-            double *a = aug + (size_t)e * ld;
-            for (int u = 0; u < m; ++u) a[u] = (e == u ? dr : 0.0) - h[u + e * m];
-            a[m] = fma(dr, Xc[(size_t)row + (size_t)e * n], -Yc[(size_t)row + (size_t)e * n]);
+            for (int u = 0; u < m; ++u) {
+                const double hv = h[u + e * m];
+                AUG(e, u) = u == e ? dr - hv : -hv;
+            }
+            AUG(e, m) = fma(dr, Xc[(size_t)row + (size_t)e * n], -Yc[(size_t)row + (size_t)e * n]);
         }
         __syncwarp(tmask);
         bool singular = false;
         for (int p = 0; p < m; ++p) {
-            double best = -1.0;
+            // pivot: largest |entry| of column p in rows p.., first on ties,
+            // compared as integers (the order of non-negative doubles)
+            uint64_t best = 0;
             int bi = m;
             bool diag_nan = false;
-            for (int e = t; e < m; e += T) {
-                if (e < p) continue;
-                const double v = fabs(aug[(size_t)e * ld + p]);
-                if (v != v) {
+            for (int e = t + ((p - t + T - 1) / T) * T; e < m; e += T) {
+                const uint64_t key = (uint64_t)__double_as_longlong(AUG(e, p)) & kAbsMask;
+                if (key > kInfBits) {
                     diag_nan = diag_nan || e == p;
-                } else if (v > best || (v == best && e < bi)) {
-                    best = v;
+                } else if (key > best || (key == best && e < bi)) {
+                    best = key;
                     bi = e;
                 }
             }
             for (int o = T >> 1; o >= 1; o >>= 1) {
-                const double ov = __shfl_xor_sync(tmask, best, o, T);
+                const uint64_t ok = __shfl_xor_sync(tmask, (unsigned long long)best, o, T);
                 const int oi = __shfl_xor_sync(tmask, bi, o, T);
-                if (ov > best || (ov == best && oi < bi)) {
-                    best = ov;
+                if (ok > best || (ok == best && oi < bi)) {
+                    best = ok;
                     bi = oi;
                 }
             }
-            diag_nan = __any_sync(tmask, diag_nan);
-            if (diag_nan || !isfinite(best) || best <= 64.0 * DBL_EPSILON) {
+            if (T > 1) diag_nan = __any_sync(tmask, diag_nan);
+            if (diag_nan || best >= kInfBits || best <= kTinyPivotBits) {
                 singular = true;
                 break;
             }
-            double *ap = aug + (size_t)p * ld;
             if (bi != p) {
-                double *aq = aug + (size_t)bi * ld;
                 for (int j = p + t; j <= m; j += T) {
-                    const double tmp = ap[j];
-                    ap[j] = aq[j];
-                    aq[j] = tmp;
+                    const double tmp = AUG(p, j);
+                    AUG(p, j) = AUG(bi, j);
+                    AUG(bi, j) = tmp;
                 }
+                __syncwarp(tmask);
             }
+            const double r = 1.0 / AUG(p, p);
             __syncwarp(tmask);
-            const double pv = ap[p];
-            __syncwarp(tmask);
-            for (int j = p + t; j <= m; j += T) ap[j] = ap[j] / pv;
+            for (int j = p + 1 + t; j <= m; j += T) AUG(p, j) = AUG(p, j) * r;
             __syncwarp(tmask);
             for (int e = t; e < m; e += T) {
                 if (e == p) continue;
-                double *a = aug + (size_t)e * ld;
-                const double f = a[p];
-                for (int j = p; j <= m; ++j) a[j] = fma(-f, ap[j], a[j]);
+                const double f = AUG(e, p);
+                for (int j = p + 1; j <= m; ++j) AUG(e, j) = fma(-f, AUG(p, j), AUG(e, j));
             }
             __syncwarp(tmask);
         }
         if (!singular) {
             for (int e = t; e < m; e += T) {
-                double v = aug[(size_t)e * ld + m];
+                double v = AUG(e, m);
                 if (damping < 1.0) v = fma(damping, v, (1.0 - damping) * Xc[(size_t)row + (size_t)e * n]);
-                if (!isfinite(v)) {
+                if (((uint64_t)__double_as_longlong(v) & kInfBits) == kInfBits) {
                     singular = true;
                     v = 0.0;
                 }
                 Xnc[(size_t)row + (size_t)e * n] = v;
             }
         }
+#undef AUG
         if (singular) atomicOr(&flags[c], 1);
         __syncwarp(tmask);
     }
@@ -312,7 +331,7 @@ int launch_cluster_update(const double *X, const double *Y, const double *d, int
 }
 
 int cluster_basis_solve(const int *row_ptr, const int *col_ind, const double *vals, int n,
-                        const double *d, const int *ranges, int C, int maxiter, double tol,
+                        int nnz, const double *d, const int *ranges, int C, int maxiter, double tol,
                         double damping, double *X, int *iterations, double *residuals,
                         int *first_error_cluster, cudaStream_t s)
 {
@@ -363,6 +382,14 @@ int cluster_basis_solve(const int *row_ptr, const int *col_ind, const double *va
                                cudaMemcpyHostToDevice, s));
     IPTGB_CHECK(launch_pdl(cluster_identity_kernel, dim3(std::max(1, std::min(64, blocks_for((size_t)n * max_m))), C),
                            dim3(kThreads), 0, s, X, n, reinterpret_cast<const int4 *>(d_info)));
+    // large matrices: the products in double-float on the FP32 pipe, the
+    // Davidson products' policy (davidson_df_products)
+    DeviceBuffer<float> vsplit;
+    const bool df = nnz > 0 && davidson_df_products(n);
+    if (df) {
+        IPTGB_CHECK(vsplit.alloc(2 * (size_t)nnz, s));
+        IPTGB_CHECK(launch_df_split(vals, (size_t)nnz, vsplit.ptr, vsplit.ptr + nnz, s));
+    }
     std::vector<int> hst((size_t)C + 2, 0);
     std::vector<char> live((size_t)C, maxiter > 0 ? 1 : 0);
     double *cur = X, *nxt = B.ptr;
@@ -376,10 +403,22 @@ int cluster_basis_solve(const int *row_ptr, const int *col_ind, const double *va
             hi = info[4 * c + 2] + info[4 * c + 1];
         }
         if (lo < 0) break;
-        IPTGB_CHECK(launch_csr64_spmm(row_ptr, col_ind, vals, n, cur + (size_t)lo * n, hi - lo,
-                                      Y.ptr + (size_t)lo * n, s));
-        IPTGB_CHECK(launch_cluster_update(cur, Y.ptr, d, n, d_info, d_active, C, max_m, smem,
-                                          damping, nxt, d_flags, s));
+        {
+            KernelTimerScope timer(kProfCsrProduct, s);
+            if (df) {
+                IPTGB_CHECK(launch_csr_df_spmm(row_ptr, col_ind, vsplit.ptr, vsplit.ptr + nnz, n,
+                                               cur + (size_t)lo * n, hi - lo,
+                                               Y.ptr + (size_t)lo * n, s));
+            } else {
+                IPTGB_CHECK(launch_csr64_spmm(row_ptr, col_ind, vals, n, cur + (size_t)lo * n,
+                                              hi - lo, Y.ptr + (size_t)lo * n, s));
+            }
+        }
+        {
+            KernelTimerScope timer(kProfClusterUpdate, s);
+            IPTGB_CHECK(launch_cluster_update(cur, Y.ptr, d, n, d_info, d_active, C, max_m, smem,
+                                              damping, nxt, d_flags, s));
+        }
         IPTGB_CHECK(launch_pdl(cluster_norms_kernel, dim3(kClusterNormSlices, C), dim3(kThreads), 0,
                                s, cur, nxt, n, reinterpret_cast<const int4 *>(d_info), d_active,
                                part.ptr));
@@ -438,7 +477,7 @@ IPT_API int ipt_block_cluster_basis(const int *d_row_ptr, const int *d_col_ind,
         nclusters <= 0 || maxiter < 0) {
         return IPT_CUDA_INVALID_ARGUMENT;
     }
-    return cluster_basis_solve(d_row_ptr, d_col_ind, d_vals, n, d_diag, ranges, nclusters,
+    return cluster_basis_solve(d_row_ptr, d_col_ind, d_vals, n, nnz, d_diag, ranges, nclusters,
                                maxiter, tol, damping, d_basis, iterations, residuals, nullptr,
                                (cudaStream_t)stream);
 }

@@ -22,7 +22,8 @@ std::vector<Pending> g_pending;
 double g_ms[kProfCount] = {};
 long long g_count[kProfCount] = {};
 const char *kNames[kProfCount] = {"lowp_product", "lowp_update", "fp64_product", "fp64_update",
-                                  "csr_product", "small_eig", "gram", "tall_gemm", "mlp"};
+                                  "csr_product", "small_eig", "gram", "tall_gemm", "mlp",
+                                  "cluster_update"};
 
 void drain_locked()
 {

@@ -157,8 +157,10 @@ int ipt_block_cluster_ranges(const int *col_ptr, const int *row_ind, const doubl
  * (0-based) with ascending diagonal d_diag; d_basis (n x sum of widths,
  * column-major) gets the clusters' columns one after the other; iterations
  * and residuals (host, nclusters) the per-cluster iteration counts and last
- * fixed-point residuals.  IPT_CUDA_INVALID_ARGUMENT for a singular row system
- * or a non-finite iterate.  Synchronises `stream`. */
+ * fixed-point residuals.  From 16384 rows the products H X are formed in
+ * double-float arithmetic (about 48 bits, the Davidson products' policy,
+ * tuning knob IPT_GB300_DF_DAVIDSON).  IPT_CUDA_INVALID_ARGUMENT for a
+ * singular row system or a non-finite iterate.  Synchronises `stream`. */
 int ipt_block_cluster_basis(const int *d_row_ptr, const int *d_col_ind, const double *d_vals,
                             int n, int nnz, const double *d_diag, const int *ranges,
                             int nclusters, int maxiter, double tol, double damping,
@@ -365,7 +367,7 @@ long long ipt_block_launch_count(void);
  * its own stream.  Kernel ids: 0 low-precision product (tcgen05 / FP32 SIMT),
  * 1 low-precision update, 2 FP64 dense product, 3 FP64 update / partial sum,
  * 4 FP64 CSR product, 5 small eigensolver, 6 Gram products, 7 tall-by-small
- * products, 8 learned-preconditioner kernels. */
+ * products, 8 learned-preconditioner kernels, 9 block-cluster update. */
 void ipt_block_profile_enable(int on);
 void ipt_block_profile_reset(void);
 int ipt_block_profile_read(int kernel, const char **name, double *total_ms, long long *launches);

@@ -544,12 +544,15 @@ ORACLE_API int oracle_ipt_dense_products_to_residual(const double *matrix, int n
  *   (d_i I - h^T) x = d_i basis[i, :] - y[i, :],  h[u + e m] = y[first + u, e]
  * by Gauss-Jordan elimination with partial pivoting: the pivot is the first
  * row with the largest |entry| (the reference's scan, strict comparison),
- * singular when that entry is not finite or not above 64 DBL_EPSILON.  The
- * products are placed as the library's CUDA kernel places them (the right
- * side fma(d, x, -y), the elimination a[e][j] = fma(-a[e][p], a[p][j],
- * a[e][j]), the damping fma(damping, v, (1 - damping) x)), so that both give
- * the same bits.  Returns 1 if a row system is singular or a value is not
- * finite (its entries are then 0 or unset), 0 otherwise. */
+ * singular when that entry is NaN on the diagonal, not finite, or not above
+ * 64 DBL_EPSILON.  The arithmetic is the library's CUDA kernel's, operation
+ * for operation, so that both give the same bits: the off-diagonal entries
+ * -h, the diagonal d_i - h, the right side fma(d_i, x, -y); per step one
+ * reciprocal r = 1 / pivot, the pivot row's later columns times r, the
+ * elimination a[e][j] = fma(-a[e][p], a[p][j], a[e][j]) for j > p (column p
+ * is never read again); the damping fma(damping, v, (1 - damping) x).  The
+ * reference divides by the pivot instead (one rounding apart).  Returns 1 if
+ * a row system is singular or a value is not finite, 0 otherwise. */
 ORACLE_API int oracle_cluster_update(const double *basis, const double *y, const double *diag,
                                      int n, int first, int m, double damping, double *next)
 {
@@ -567,12 +570,13 @@ ORACLE_API int oracle_cluster_update(const double *basis, const double *y, const
         for (int e = 0; e < m; ++e) {
             double *a = aug + (size_t)e * ld;
             for (int u = 0; u < m; ++u) {
-                a[u] = (e == u ? dr : 0.0) - y[(size_t)(first + u) + (size_t)e * n];
+                const double hv = y[(size_t)(first + u) + (size_t)e * n];
+                a[u] = u == e ? dr - hv : -hv;
             }
             a[m] = fma(dr, basis[(size_t)row + (size_t)e * n], -y[(size_t)row + (size_t)e * n]);
         }
         int singular = 0;
-        for (int p = 0; p < m && !singular; ++p) {
+        for (int p = 0; p < m; ++p) {
             int piv = p;
             double pa = fabs(aug[(size_t)p * ld + p]);
             for (int c = p + 1; c < m; ++c) {
@@ -595,13 +599,13 @@ ORACLE_API int oracle_cluster_update(const double *basis, const double *y, const
                     aq[j] = t;
                 }
             }
-            const double pv = ap[p];
-            for (int j = p; j <= m; ++j) ap[j] = ap[j] / pv;
+            const double r = 1.0 / ap[p];
+            for (int j = p + 1; j <= m; ++j) ap[j] = ap[j] * r;
             for (int e = 0; e < m; ++e) {
                 if (e == p) continue;
                 double *a = aug + (size_t)e * ld;
                 const double f = a[p];
-                for (int j = p; j <= m; ++j) a[j] = fma(-f, ap[j], a[j]);
+                for (int j = p + 1; j <= m; ++j) a[j] = fma(-f, ap[j], a[j]);
             }
         }
         if (!singular) {
