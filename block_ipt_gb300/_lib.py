@@ -219,6 +219,9 @@ SIGNATURES = [
     ("ipt_block_cluster_ranges", _i, [_vp, _vp, _vp, _i, _i, _i, _i, C.c_double, _i,
                                       C.c_double, _vp, _i, C.POINTER(C.c_int),
                                       C.POINTER(C.c_int)]),
+    ("ipt_block_prepare_csc", _i, [_vp, _vp, _vp, _i, _i, _i, _i, C.c_double, _vp, _vp, _vp,
+                                   _i, C.POINTER(C.c_int), _vp, _vp, _vp, _vp, _i, _vp, _i,
+                                   C.POINTER(C.c_int)]),
     ("ipt_block_cluster_basis", _i, [_vp, _vp, _vp, _i, _i, _vp, _vp, _i, _i, C.c_double,
                                      C.c_double, _vp, _vp, _vp, _vp]),
     ("ipt_block_cluster_update", _i, [_vp, _vp, _vp, _i, _i, _i, C.c_double, _vp,

@@ -400,3 +400,29 @@ def cluster_update(d_basis, d_y, d_diag, n, first, m, d_next, damping=1.0, strea
                                               d_next, C.byref(sing), _stream_ptr(stream))
     _check(st, "ipt_block_cluster_update")
     return bool(sing.value)
+
+
+def prepare_csc(col_ptr, row_ind, values, n, k, lift=True, threshold=0.0):
+    """The plain sparse path's host preparation (ipt_block_prepare_csc): a dict
+    of the prepared CSC, diagonal, permutation and lifting rotations."""
+    cp, ri, va = _i32(col_ptr), _i32(row_ind), _f64(values)
+    lib = _lib.load()
+    cap = max(4 * len(ri), n * n, 16)
+    ocp = np.zeros(n + 1, np.int32)
+    ori = np.zeros(cap, np.int32)
+    ova = np.zeros(cap)
+    od = np.zeros(n)
+    op = np.zeros(n, np.int32)
+    rf = np.zeros(n, np.int32)
+    rs = np.zeros(n, np.int32)
+    rv = np.zeros(max(1, 64 * 64 * n))
+    nnz, rc = C.c_int(0), C.c_int(0)
+    st = lib.ipt_block_prepare_csc(_ptr(cp), _ptr(ri), _ptr(va), n, k, len(ri), int(bool(lift)),
+                                   threshold, _ptr(ocp), _ptr(ori), _ptr(ova), cap, C.byref(nnz),
+                                   _ptr(od), _ptr(op), _ptr(rf), _ptr(rs), n, _ptr(rv), rv.size,
+                                   C.byref(rc))
+    _check(st, "ipt_block_prepare_csc")
+    r = rc.value
+    return {"col_ptr": ocp, "row_ind": ori[:nnz.value], "values": ova[:nnz.value], "diag": od,
+            "perm": op, "rot_first": rf[:r], "rot_size": rs[:r],
+            "rot_values": rv[:int(sum(int(m) * int(m) for m in rs[:r]))]}

@@ -554,7 +554,9 @@ static int ipt_sparse_host_entry(const int *col_ptr, const int *row_ind, const d
     }
     auto t0 = std::chrono::steady_clock::now();
     PreparedCsr prep;
-    int status = prepare_csc(col_ptr, row_ind, vals, n, nnz, true, &prep);
+    // the reference's plain sparse path lifts degeneracies (ipt_cuda.cu:5077-5090)
+    int status = prepare_csc(col_ptr, row_ind, vals, n, nnz, true, &prep, k,
+                             env_double("IPT_DEGENERACY_THRESHOLD", 0.0));
     if (status != IPT_CUDA_SUCCESS) {
         ipt_cuda_free_result(result);
         return status;

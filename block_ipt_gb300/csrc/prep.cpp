@@ -15,6 +15,18 @@ namespace iptgb {
 
 double env_double(const char *name, double default_value);
 int env_int(const char *name, int default_value);
+int lift_degeneracies(std::vector<int> *cp, std::vector<int> *ri, std::vector<double> *va, int n,
+                      int k, double degeneracy_threshold, std::vector<double> *diag,
+                      std::vector<int> *rot_first, std::vector<int> *rot_size,
+                      std::vector<double> *rot_values);
+
+#define IPTGB_PREP_CHECK(expr)                  \
+    do {                                        \
+        const int prep_status_ = (expr);        \
+        if (prep_status_ != IPT_CUDA_SUCCESS) { \
+            return prep_status_;                \
+        }                                       \
+    } while (0)
 
 bool validate_csc(const int *col_ptr, const int *row_ind, int n, int nnz)
 {
@@ -73,8 +85,43 @@ void csc_to_csr(const int *col_ptr, const int *row_ind, const double *vals, int 
     }
 }
 
+static int prepare_sorted(const int *col_ptr, const int *row_ind, const double *vals, int n,
+                          int nnz, bool sort_diagonal, PreparedCsr *out);
+
 int prepare_csc(const int *col_ptr, const int *row_ind, const double *vals, int n, int nnz,
-                bool sort_diagonal, PreparedCsr *out)
+                bool sort_diagonal, PreparedCsr *out, int lift_k, double degeneracy_threshold)
+{
+    IPTGB_PREP_CHECK(prepare_sorted(col_ptr, row_ind, vals, n, nnz, sort_diagonal, out));
+    out->rot_first.clear();
+    out->rot_size.clear();
+    out->rot_values.clear();
+    if (lift_k <= 0) return IPT_CUDA_SUCCESS;
+    // the lifting works on the CSC arrays of the sorted matrix: the input as
+    // given when the order did not change, else the permuted matrix
+    std::vector<int> cp, ri;
+    std::vector<double> va;
+    if (!out->permuted) {
+        cp.assign(col_ptr, col_ptr + (size_t)n + 1U);
+        ri.assign(row_ind, row_ind + (size_t)nnz);
+        va.assign(vals, vals + (size_t)nnz);
+    } else {
+        csc_to_csr(out->row_ptr.data(), out->col_ind.data(), out->vals.data(), n, out->nnz, &cp,
+                   &ri, &va);
+    }
+    std::vector<double> diag;
+    IPTGB_PREP_CHECK(lift_degeneracies(&cp, &ri, &va, n, lift_k, degeneracy_threshold, &diag,
+                                       &out->rot_first, &out->rot_size, &out->rot_values));
+    if (!out->rot_first.empty()) {
+        csc_to_csr(cp.data(), ri.data(), va.data(), n, (int)ri.size(), &out->row_ptr,
+                   &out->col_ind, &out->vals);
+        out->nnz = (int)out->col_ind.size();
+        out->diag = diag;
+    }
+    return IPT_CUDA_SUCCESS;
+}
+
+static int prepare_sorted(const int *col_ptr, const int *row_ind, const double *vals, int n,
+                          int nnz, bool sort_diagonal, PreparedCsr *out)
 {
     if (out == nullptr || vals == nullptr || !validate_csc(col_ptr, row_ind, n, nnz)) {
         return IPT_CUDA_INVALID_ARGUMENT;
@@ -183,10 +230,28 @@ int prepare_csc(const int *col_ptr, const int *row_ind, const double *vals, int 
 
 void unpermute_vectors(const PreparedCsr &prep, double *vectors, int k)
 {
+    const int n = prep.n;
+    // the lifting rotations, last first: v[block] <- Q v[block]
+    // (ipt_apply_prepared_q_to_vectors, ipt_preparation.cu:1222-1268)
+    size_t vofs = prep.rot_values.size();
+    for (size_t r = prep.rot_first.size(); r-- > 0;) {
+        const int first = prep.rot_first[r], m = prep.rot_size[r];
+        vofs -= (size_t)m * (size_t)m;
+        const double *q = prep.rot_values.data() + vofs;
+        std::vector<double> t((size_t)m);
+        for (int j = 0; j < k; ++j) {
+            double *v = vectors + (size_t)j * (size_t)n + first;
+            for (int i = 0; i < m; ++i) {
+                double s = 0.0;
+                for (int l = 0; l < m; ++l) s += q[(size_t)i + (size_t)l * (size_t)m] * v[l];
+                t[(size_t)i] = s;
+            }
+            std::memcpy(v, t.data(), (size_t)m * sizeof(double));
+        }
+    }
     if (!prep.permuted) {
         return;
     }
-    const int n = prep.n;
     std::vector<double> tmp((size_t)n);
     for (int j = 0; j < k; ++j) {
         double *v = vectors + (size_t)j * (size_t)n;
@@ -354,21 +419,46 @@ static void adaptive_expand(const int *col_ptr, const int *row_ind, const double
     out->added.erase(std::unique(out->added.begin(), out->added.end()), out->added.end());
 }
 
-void cluster_ranges(const int *col_ptr, const int *row_ind, const double *vals, int n, int k,
-                    int requested_k, double degeneracy_threshold, int adaptive,
-                    double coupling_tau, ClusterRanges *out)
+// Sum of the stored entries at (row, col) of a CSC matrix (duplicates add,
+// ipt_preparation.cu:830-843) and the diagonal read that way (:845-858).
+static double csc_value_sum(const int *col_ptr, const int *row_ind, const double *vals, int row,
+                            int col)
 {
-    *out = ClusterRanges();
-    const GapOptions o = gap_options(degeneracy_threshold);
-    out->max_block_size = o.max_block_size;
-    std::vector<double> diag;
-    csc_diagonal(col_ptr, row_ind, vals, n, &diag);
+    double v = 0.0;
+    for (int p = col_ptr[col]; p < col_ptr[col + 1]; ++p) {
+        if (row_ind[p] == row) v += vals[p];
+    }
+    return v;
+}
+
+static void csc_diagonal_sum(const int *col_ptr, const int *row_ind, const double *vals, int n,
+                             std::vector<double> *diag)
+{
+    diag->assign((size_t)n, 0.0);
+    for (int c = 0; c < n; ++c) (*diag)[(size_t)c] = csc_value_sum(col_ptr, row_ind, vals, c, c);
+}
+
+namespace {
+
+// What the subspace detection and the gap check share: the numeric gap
+// scale, the strongest off-diagonal entry of every index, and the indices
+// in ascending diagonal order.
+struct GapScan {
+    double tau_num = 0.0;
+    std::vector<double> off, sorted_diag;
+    std::vector<int> order;
+};
+
+GapScan gap_scan(const int *col_ptr, const int *row_ind, const double *vals, int n,
+                 const std::vector<double> &diag, const GapOptions &o)
+{
+    GapScan g;
     double dmax = 0.0;
     for (double v : diag) dmax = std::max(dmax, std::fabs(v));
-    const double tau_num = o.eps_multiplier * std::numeric_limits<double>::epsilon() *
-                           std::max(1.0, dmax);
+    g.tau_num = o.eps_multiplier * std::numeric_limits<double>::epsilon() * std::max(1.0, dmax);
     // strongest off-diagonal entry of each row and column (ipt_preparation.cu:353-380)
-    std::vector<double> cs((size_t)n, 0.0), rs((size_t)n, 0.0), off((size_t)n);
+    std::vector<double> cs((size_t)n, 0.0), rs((size_t)n, 0.0);
+    g.off.resize((size_t)n);
     for (int c = 0; c < n; ++c) {
         for (int p = col_ptr[c]; p < col_ptr[c + 1]; ++p) {
             const int r = row_ind[p];
@@ -378,38 +468,60 @@ void cluster_ranges(const int *col_ptr, const int *row_ind, const double *vals, 
             rs[(size_t)r] = std::max(rs[(size_t)r], a);
         }
     }
-    for (int i = 0; i < n; ++i) off[(size_t)i] = std::max(cs[(size_t)i], rs[(size_t)i]);
-    std::vector<int> order((size_t)n);
-    std::iota(order.begin(), order.end(), 0);
-    std::stable_sort(order.begin(), order.end(),
+    for (int i = 0; i < n; ++i) g.off[(size_t)i] = std::max(cs[(size_t)i], rs[(size_t)i]);
+    g.order.resize((size_t)n);
+    std::iota(g.order.begin(), g.order.end(), 0);
+    std::stable_sort(g.order.begin(), g.order.end(),
                      [&](int a, int b) { return diag[(size_t)a] < diag[(size_t)b]; });
-    std::vector<double> sd((size_t)n);
-    for (int i = 0; i < n; ++i) sd[(size_t)i] = diag[(size_t)order[(size_t)i]];
-    // union every target with the rows whose gap is numerically zero or small
-    // against their coupling (ipt_preparation.cu:425-455, 502-611)
-    DisjointSets sets(n);
+    g.sorted_diag.resize((size_t)n);
+    for (int i = 0; i < n; ++i) g.sorted_diag[(size_t)i] = diag[(size_t)g.order[(size_t)i]];
+    return g;
+}
+
+// Calls join(row, col) for every target col < k and every other index row
+// whose gap to it is numerically zero or small against their coupling
+// (ipt_preparation.cu:383-455 and the candidate loops of :502-611, 658-757).
+template <class Join>
+void for_each_close_pair(const int *col_ptr, const int *row_ind, const double *vals, int n,
+                         const std::vector<double> &diag, int k, const GapOptions &o,
+                         const GapScan &g, Join join)
+{
     for (int col = 0; col < std::min(k, n); ++col) {
         const double dc = diag[(size_t)col];
         const double window =
-            std::max(gap_floor(dc, dc, tau_num, o), off[(size_t)col] / o.ratio_tol);
+            std::max(gap_floor(dc, dc, g.tau_num, o), g.off[(size_t)col] / o.ratio_tol);
+        const auto &sd = g.sorted_diag;
         const size_t lo = (size_t)(std::lower_bound(sd.begin(), sd.end(), dc - window) - sd.begin());
         const size_t hi = (size_t)(std::upper_bound(sd.begin(), sd.end(), dc + window) - sd.begin());
         for (size_t q = lo; q < hi; ++q) {
-            const int row = order[q];
+            const int row = g.order[q];
             if (row == col) continue;
             const double dr = diag[(size_t)row];
             double coupling = std::max(std::fabs(csc_entry(col_ptr, row_ind, vals, row, col)),
                                        std::fabs(csc_entry(col_ptr, row_ind, vals, col, row)));
             if (!(coupling > 0.0)) {
-                coupling = o.eta * std::min(off[(size_t)row], off[(size_t)col]);
+                coupling = o.eta * std::min(g.off[(size_t)row], g.off[(size_t)col]);
             }
             const double gap = std::fabs(dr - dc);
-            const double fl = gap_floor(dr, dc, tau_num, o);
-            const bool join =
-                gap <= fl || (coupling > 0.0 && coupling / std::max(gap, fl) >= o.ratio_tol);
-            if (join) sets.unite(row, col);
+            const double fl = gap_floor(dr, dc, g.tau_num, o);
+            if (gap <= fl || (coupling > 0.0 && coupling / std::max(gap, fl) >= o.ratio_tol)) {
+                join(row, col);
+            }
         }
     }
+}
+
+// The index ranges spanned by the groups of close indices that contain a
+// target, merged when they overlap or touch (ipt_preparation.cu:502-645).
+std::vector<std::pair<int, int>> degenerate_subspaces(const int *col_ptr, const int *row_ind,
+                                                      const double *vals, int n,
+                                                      const std::vector<double> &diag, int k,
+                                                      const GapOptions &o, int *too_large)
+{
+    const GapScan g = gap_scan(col_ptr, row_ind, vals, n, diag, o);
+    DisjointSets sets(n);
+    for_each_close_pair(col_ptr, row_ind, vals, n, diag, k, o, g,
+                        [&](int row, int col) { sets.unite(row, col); });
     std::vector<int> cmin((size_t)n, n), cmax((size_t)n, -1), target((size_t)n, 0);
     for (int i = 0; i < n; ++i) {
         const int r = sets.find(i);
@@ -423,7 +535,6 @@ void cluster_ranges(const int *col_ptr, const int *row_ind, const double *vals, 
             rg.emplace_back(cmin[(size_t)r], cmax[(size_t)r]);
         }
     }
-    // merge overlapping or touching ranges (ipt_preparation.cu:480-500)
     std::sort(rg.begin(), rg.end());
     std::vector<std::pair<int, int>> merged;
     for (const auto &r : rg) {
@@ -433,9 +544,37 @@ void cluster_ranges(const int *col_ptr, const int *row_ind, const double *vals, 
             merged.push_back(r);
         }
     }
+    *too_large = 0;
     for (const auto &r : merged) {
-        if (r.second - r.first + 1 > o.max_block_size) out->too_large = 1;
+        if (r.second - r.first + 1 > o.max_block_size) *too_large = 1;
     }
+    return merged;
+}
+
+// Number of (target, index) pairs still close after lifting
+// (ipt_validate_target_gaps, ipt_preparation.cu:658-757).
+int target_gap_violations(const int *col_ptr, const int *row_ind, const double *vals, int n,
+                          const std::vector<double> &diag, int k, const GapOptions &o)
+{
+    const GapScan g = gap_scan(col_ptr, row_ind, vals, n, diag, o);
+    int bad = 0;
+    for_each_close_pair(col_ptr, row_ind, vals, n, diag, k, o, g, [&](int, int) { ++bad; });
+    return bad;
+}
+
+}  // namespace
+
+void cluster_ranges(const int *col_ptr, const int *row_ind, const double *vals, int n, int k,
+                    int requested_k, double degeneracy_threshold, int adaptive,
+                    double coupling_tau, ClusterRanges *out)
+{
+    *out = ClusterRanges();
+    const GapOptions o = gap_options(degeneracy_threshold);
+    out->max_block_size = o.max_block_size;
+    std::vector<double> diag;
+    csc_diagonal_sum(col_ptr, row_ind, vals, n, &diag);
+    std::vector<std::pair<int, int>> merged =
+        degenerate_subspaces(col_ptr, row_ind, vals, n, diag, k, o, &out->too_large);
     // singleton clusters for the targets not covered (ipt_cuda.cu:4114-4132)
     std::vector<char> covered((size_t)n, 0);
     for (const auto &r : merged) {
@@ -450,6 +589,226 @@ void cluster_ranges(const int *col_ptr, const int *row_ind, const double *vals, 
         adaptive_expand(col_ptr, row_ind, vals, diag, requested_k, o.max_block_size,
                         coupling_tau, out);
     }
+}
+
+// ---- degeneracy lifting -------------------------------------------------------
+// The reference's plain sparse path rotates every group of close target
+// indices into the eigenbasis of its diagonal block before the IPT
+// iteration and rotates the result back (ipt_preparation.cu:1296-1338,
+// 1222-1294, driven by :1436-1592).  The rotated matrix must carry the same
+// bits as the reference's, so the local Jacobi eigensolver, the order in
+// which the similarity transform emits and merges entries, and the
+// summation orders follow the reference step for step.
+
+// Classical Jacobi on a symmetric m x m block: rotate away the largest
+// off-diagonal entry until none exceeds 1e-14 or 64 m^2 rotations were made
+// (ipt_preparation.cu:759-828).  V receives the accumulated rotations.
+static void jacobi_symmetric(const std::vector<double> &block, int m, std::vector<double> *V)
+{
+    std::vector<double> a = block;
+    auto A = [&](int r, int c) -> double & { return a[(size_t)r + (size_t)c * (size_t)m]; };
+    V->assign((size_t)m * (size_t)m, 0.0);
+    for (int i = 0; i < m; ++i) (*V)[(size_t)i * (size_t)(m + 1)] = 1.0;
+    for (int rot = 0; rot < 64 * m * m; ++rot) {
+        int p = 0, q = 1;
+        double big = 0.0;
+        for (int c = 1; c < m; ++c) {
+            for (int r = 0; r < c; ++r) {
+                if (std::fabs(A(r, c)) > big) {
+                    big = std::fabs(A(r, c));
+                    p = r;
+                    q = c;
+                }
+            }
+        }
+        if (big <= 1.0e-14) break;
+        const double app = A(p, p), aqq = A(q, q), apq = A(p, q);
+        const double theta = (aqq - app) / (2.0 * apq);
+        const double t = (theta >= 0.0 ? 1.0 : -1.0) / (std::fabs(theta) + std::sqrt(1.0 + theta * theta));
+        const double cs = 1.0 / std::sqrt(1.0 + t * t);
+        const double sn = t * cs;
+        for (int r = 0; r < m; ++r) {
+            if (r == p || r == q) continue;
+            const double arp = A(r, p), arq = A(r, q);
+            const double np_ = cs * arp - sn * arq;
+            const double nq = sn * arp + cs * arq;
+            A(r, p) = np_;
+            A(p, r) = np_;
+            A(r, q) = nq;
+            A(q, r) = nq;
+        }
+        A(p, p) = cs * cs * app - 2.0 * sn * cs * apq + sn * sn * aqq;
+        A(q, q) = sn * sn * app + 2.0 * sn * cs * apq + cs * cs * aqq;
+        A(p, q) = 0.0;
+        A(q, p) = 0.0;
+        for (int r = 0; r < m; ++r) {
+            double &vp = (*V)[(size_t)r + (size_t)p * (size_t)m];
+            double &vq = (*V)[(size_t)r + (size_t)q * (size_t)m];
+            const double x = vp, y = vq;
+            vp = cs * x - sn * y;
+            vq = sn * x + cs * y;
+        }
+    }
+}
+
+// Eigenvectors of a symmetric block in ascending order of their Rayleigh
+// quotients v^T B v (ipt_preparation.cu:916-977).
+static void sorted_symmetric_eigenvectors(const std::vector<double> &block, int m,
+                                          std::vector<double> *V)
+{
+    jacobi_symmetric(block, m, V);
+    std::vector<double> lam((size_t)m, 0.0);
+    for (int j = 0; j < m; ++j) {
+        const double *v = V->data() + (size_t)j * (size_t)m;
+        double s = 0.0;
+        for (int r = 0; r < m; ++r) {
+            for (int i = 0; i < m; ++i) s += v[r] * block[(size_t)r + (size_t)i * (size_t)m] * v[i];
+        }
+        lam[(size_t)j] = s;
+    }
+    std::vector<int> idx((size_t)m);
+    std::iota(idx.begin(), idx.end(), 0);
+    std::stable_sort(idx.begin(), idx.end(), [&](int a, int b) { return lam[(size_t)a] < lam[(size_t)b]; });
+    std::vector<double> sorted((size_t)m * (size_t)m);
+    for (int j = 0; j < m; ++j) {
+        std::copy(V->begin() + (size_t)idx[(size_t)j] * (size_t)m,
+                  V->begin() + (size_t)(idx[(size_t)j] + 1) * (size_t)m,
+                  sorted.begin() + (size_t)j * (size_t)m);
+    }
+    V->swap(sorted);
+}
+
+// H <- Q^T H Q on the block [first, first + m) (Q = V, orthogonal): column
+// lists rebuilt entry by entry, then sorted by row, duplicates summed in
+// that order and exact zeros dropped (ipt_preparation.cu:1109-1220).
+static void rotate_block_csc(std::vector<int> *col_ptr, std::vector<int> *row_ind,
+                             std::vector<double> *vals, int n, int first, int m,
+                             const std::vector<double> &V)
+{
+    std::vector<std::vector<std::pair<int, double>>> cols((size_t)n);
+    auto Q = [&](int r, int c) { return V[(size_t)r + (size_t)c * (size_t)m]; };
+    for (int c = 0; c < n; ++c) {
+        const int cl = c - first;
+        const bool c_in = cl >= 0 && cl < m;
+        for (int p = (*col_ptr)[(size_t)c]; p < (*col_ptr)[(size_t)c + 1]; ++p) {
+            const int r = (*row_ind)[(size_t)p];
+            const int rl = r - first;
+            const bool r_in = rl >= 0 && rl < m;
+            const double v = (*vals)[(size_t)p];
+            if (!r_in && !c_in) {
+                cols[(size_t)c].emplace_back(r, v);
+            } else if (!r_in) {
+                for (int j = 0; j < m; ++j) {
+                    const double w = v * Q(cl, j);
+                    if (w != 0.0) cols[(size_t)(first + j)].emplace_back(r, w);
+                }
+            } else if (!c_in) {
+                for (int i = 0; i < m; ++i) {
+                    const double w = Q(rl, i) * v;  // (Q^T)[i, rl]
+                    if (w != 0.0) cols[(size_t)c].emplace_back(first + i, w);
+                }
+            } else {
+                for (int j = 0; j < m; ++j) {
+                    const double qj = Q(cl, j);
+                    if (qj == 0.0) continue;
+                    for (int i = 0; i < m; ++i) {
+                        const double w = Q(rl, i) * v * qj;
+                        if (w != 0.0) cols[(size_t)(first + j)].emplace_back(first + i, w);
+                    }
+                }
+            }
+        }
+    }
+    col_ptr->assign((size_t)n + 1U, 0);
+    row_ind->clear();
+    vals->clear();
+    for (int c = 0; c < n; ++c) {
+        auto &e = cols[(size_t)c];
+        std::sort(e.begin(), e.end(), [](const std::pair<int, double> &x,
+                                         const std::pair<int, double> &y) { return x.first < y.first; });
+        (*col_ptr)[(size_t)c] = (int)row_ind->size();
+        for (size_t i = 0; i < e.size(); ++i) {
+            const int r = e[i].first;
+            double v = e[i].second;
+            while (i + 1 < e.size() && e[i + 1].first == r) v += e[++i].second;
+            if (v != 0.0) {
+                row_ind->push_back(r);
+                vals->push_back(v);
+            }
+        }
+    }
+    (*col_ptr)[(size_t)n] = (int)row_ind->size();
+}
+
+// Real symmetric within 1e-12 relative, entry by entry (ipt_preparation.cu:860-883).
+static bool csc_is_symmetric(const std::vector<int> &cp, const std::vector<int> &ri,
+                             const std::vector<double> &va, int n)
+{
+    for (int c = 0; c < n; ++c) {
+        for (int p = cp[(size_t)c]; p < cp[(size_t)c + 1]; ++p) {
+            const int r = ri[(size_t)p];
+            const double v = va[(size_t)p];
+            const double t = csc_value_sum(cp.data(), ri.data(), va.data(), c, r);
+            const double scale = std::max(1.0, std::max(std::fabs(v), std::fabs(t)));
+            if (std::fabs(v - t) > 1.0e-12 * scale) return false;
+        }
+    }
+    return true;
+}
+
+int lift_degeneracies(std::vector<int> *cp, std::vector<int> *ri, std::vector<double> *va, int n,
+                      int k, double degeneracy_threshold, std::vector<double> *diag,
+                      std::vector<int> *rot_first, std::vector<int> *rot_size,
+                      std::vector<double> *rot_values)
+{
+    const GapOptions o = gap_options(degeneracy_threshold);
+    const int mr = env_int("IPT_MAX_LIFT_ROUNDS", 3);
+    const int rounds = mr > 0 ? mr : 3;
+    const bool symmetric = csc_is_symmetric(*cp, *ri, *va, n);
+    bool clean = false;
+    for (int round = 0; round < rounds; ++round) {
+        csc_diagonal_sum(cp->data(), ri->data(), va->data(), n, diag);
+        int too_large = 0;
+        const auto subspaces =
+            degenerate_subspaces(cp->data(), ri->data(), va->data(), n, *diag, k, o, &too_large);
+        if (too_large) return IPT_CUDA_INVALID_ARGUMENT;
+        if (subspaces.empty()) {
+            clean = target_gap_violations(cp->data(), ri->data(), va->data(), n, *diag, k, o) == 0;
+            break;
+        }
+        // a non-symmetric block would need a general real eigensolver; the
+        // reference then calls LAPACK dgeev when it is linked in and fails
+        // the preparation otherwise, which is what happens here
+        if (!symmetric) return IPT_CUDA_INVALID_ARGUMENT;
+        for (const auto &sub : subspaces) {
+            const int first = sub.first, m = sub.second - sub.first + 1;
+            std::vector<double> block((size_t)m * (size_t)m, 0.0);
+            for (int c = 0; c < m; ++c) {
+                for (int p = (*cp)[(size_t)(first + c)]; p < (*cp)[(size_t)(first + c) + 1]; ++p) {
+                    const int r = (*ri)[(size_t)p] - first;
+                    if (r >= 0 && r < m) block[(size_t)r + (size_t)c * (size_t)m] += (*va)[(size_t)p];
+                }
+            }
+            std::vector<double> V;
+            sorted_symmetric_eigenvectors(block, m, &V);
+            rotate_block_csc(cp, ri, va, n, first, m, V);
+            rot_first->push_back(first);
+            rot_size->push_back(m);
+            rot_values->insert(rot_values->end(), V.begin(), V.end());
+        }
+        csc_diagonal_sum(cp->data(), ri->data(), va->data(), n, diag);
+        if (target_gap_violations(cp->data(), ri->data(), va->data(), n, *diag, k, o) == 0) {
+            clean = true;
+            break;
+        }
+    }
+    if (!clean) {
+        csc_diagonal_sum(cp->data(), ri->data(), va->data(), n, diag);
+        if (target_gap_violations(cp->data(), ri->data(), va->data(), n, *diag, k, o) > 0) {
+            return IPT_CUDA_INVALID_ARGUMENT;
+        }
+    }
+    return IPT_CUDA_SUCCESS;
 }
 
 }  // namespace iptgb
@@ -484,5 +843,46 @@ IPT_API int ipt_block_cluster_ranges(const int *col_ptr, const int *row_ind, con
         ranges[2 * i] = cr.ranges[i].first;
         ranges[2 * i + 1] = cr.ranges[i].second;
     }
+    return IPT_CUDA_SUCCESS;
+}
+
+// Host only: the sparse preparation of the plain path (ipt_prepare_sparse_csc,
+// IPT_C_GPU/src/ipt_preparation.cu:1375-1648) for checking: the prepared
+// matrix as CSC, its diagonal, basis_to_original, and the lifting rotations.
+IPT_API int ipt_block_prepare_csc(const int *col_ptr, const int *row_ind, const double *vals,
+                                  int n, int k, int nnz, int lift, double degeneracy_threshold,
+                                  int *out_col_ptr, int *out_row_ind, double *out_vals,
+                                  int capacity, int *out_nnz, double *out_diag, int *out_perm,
+                                  int *rot_first, int *rot_size, int rot_capacity,
+                                  double *rot_values, int rot_values_capacity, int *rot_count)
+{
+    if (out_nnz != nullptr) *out_nnz = 0;
+    if (rot_count != nullptr) *rot_count = 0;
+    if (out_nnz == nullptr || rot_count == nullptr || k <= 0 || k > n) {
+        return IPT_CUDA_INVALID_ARGUMENT;
+    }
+    iptgb::PreparedCsr prep;
+    const int st = iptgb::prepare_csc(col_ptr, row_ind, vals, n, nnz, true, &prep,
+                                      lift ? k : 0, degeneracy_threshold);
+    if (st != IPT_CUDA_SUCCESS) return st;
+    std::vector<int> cp, ri;
+    std::vector<double> va;
+    iptgb::csc_to_csr(prep.row_ptr.data(), prep.col_ind.data(), prep.vals.data(), n, prep.nnz,
+                      &cp, &ri, &va);
+    *out_nnz = prep.nnz;
+    *rot_count = (int)prep.rot_first.size();
+    if (prep.nnz > capacity || *rot_count > rot_capacity ||
+        (int)prep.rot_values.size() > rot_values_capacity || out_col_ptr == nullptr ||
+        out_diag == nullptr || out_perm == nullptr) {
+        return IPT_CUDA_INVALID_ARGUMENT;
+    }
+    std::copy(cp.begin(), cp.end(), out_col_ptr);
+    std::copy(ri.begin(), ri.end(), out_row_ind);
+    std::copy(va.begin(), va.end(), out_vals);
+    std::copy(prep.diag.begin(), prep.diag.end(), out_diag);
+    for (int i = 0; i < n; ++i) out_perm[i] = prep.permuted ? prep.perm[(size_t)i] : i;
+    std::copy(prep.rot_first.begin(), prep.rot_first.end(), rot_first);
+    std::copy(prep.rot_size.begin(), prep.rot_size.end(), rot_size);
+    std::copy(prep.rot_values.begin(), prep.rot_values.end(), rot_values);
     return IPT_CUDA_SUCCESS;
 }

@@ -17,6 +17,10 @@ struct PreparedCsr {
     std::vector<double> diag;
     std::vector<int> perm;
     bool permuted = false;
+    // degeneracy lifting: block r covers [rot_first[r], rot_first[r] + rot_size[r])
+    // and its rotation (column-major) follows the previous ones in rot_values
+    std::vector<int> rot_first, rot_size;
+    std::vector<double> rot_values;
 };
 
 // CSC validation (IPT_C_GPU/src/ipt_preparation.cu:148-169).
@@ -32,12 +36,19 @@ void csc_diagonal(const int *col_ptr, const int *row_ind, const double *vals, in
 // duplicates and drops explicit zeros (ipt_permute_csc, :210-262).  The
 // result is emitted as CSR of the same matrix (a transpose of the CSC arrays)
 // so that the gather kernels compute H X for any sparsity pattern.
-// Returns IPT_CUDA_SUCCESS or IPT_CUDA_INVALID_ARGUMENT.
+// With lift_k > 0 the groups of numerically close indices around the lift_k
+// targets are then rotated into the eigenbasis of their diagonal blocks, in
+// up to IPT_MAX_LIFT_ROUNDS rounds (ipt_preparation.cu:1436-1592; the plain
+// sparse path of the reference always lifts).  Returns IPT_CUDA_SUCCESS or
+// IPT_CUDA_INVALID_ARGUMENT (also when a group is too wide, the gaps stay
+// unresolved, or a group of a non-symmetric matrix would need lifting).
 int prepare_csc(const int *col_ptr, const int *row_ind, const double *vals, int n, int nnz,
-                bool sort_diagonal, PreparedCsr *out);
+                bool sort_diagonal, PreparedCsr *out, int lift_k = 0,
+                double degeneracy_threshold = 0.0);
 
-// Scatter sorted-basis rows back to the original order, in place
-// (ipt_apply_prepared_q_to_vectors without rotations, ipt_preparation.cu:1276-1293).
+// Take prepared-basis rows back to the caller's basis, in place: the lifting
+// rotations, then the permutation (ipt_apply_prepared_q_to_vectors,
+// ipt_preparation.cu:1222-1293).
 void unpermute_vectors(const PreparedCsr &prep, double *vectors_col_major, int k);
 
 // CSC -> CSR transpose keeping duplicates and storage order (stable by column).

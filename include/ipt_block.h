@@ -147,6 +147,27 @@ int ipt_block_cluster_ranges(const int *col_ptr, const int *row_ind, const doubl
                              int adaptive, double coupling_tau, int *ranges, int capacity,
                              int *count, int *limit_hit);
 
+/* Host only.  The plain sparse path's preparation, for checking (replaces
+ * the static ipt_prepare_sparse_csc, IPT_C_GPU/src/ipt_preparation.cu:1375-1648):
+ * validation, stable diagonal sort and symmetric permutation, then (lift != 0)
+ * the degeneracy lifting of the k targets: groups of numerically close indices
+ * rotated into the eigenbasis of their diagonal blocks (classical Jacobi), up
+ * to IPT_MAX_LIFT_ROUNDS rounds.  Outputs the prepared matrix as CSC
+ * (out_col_ptr n+1, out_row_ind / out_vals `capacity`, *out_nnz), its
+ * diagonal (n), basis_to_original (n), and *rot_count rotations: block r
+ * covers [rot_first[r], rot_first[r] + rot_size[r]) and its rotation matrix
+ * (column-major) follows the previous ones in rot_values.
+ * IPT_CUDA_INVALID_ARGUMENT for invalid input, capacities too small, a group
+ * wider than IPT_MAX_LIFT_BLOCK_SIZE, gaps still unresolved after the
+ * rounds, or a group of a non-symmetric matrix (which the reference lifts only
+ * when LAPACK dgeev is linked in). */
+int ipt_block_prepare_csc(const int *col_ptr, const int *row_ind, const double *vals, int n,
+                          int k, int nnz, int lift, double degeneracy_threshold, int *out_col_ptr,
+                          int *out_row_ind, double *out_vals, int capacity, int *out_nnz,
+                          double *out_diag, int *out_perm, int *rot_first, int *rot_size,
+                          int rot_capacity, double *rot_values, int rot_values_capacity,
+                          int *rot_count);
+
 /* Block-cluster basis (replaces ipt_block_cluster_solve_basis_gpu, one call
  * per cluster, IPT_C_GPU/src/ipt_cuda.cu:2871-3037): for each of the
  * `nclusters` host ranges (inclusive, ascending, disjoint, width <= 64) the

@@ -12,7 +12,8 @@ libraries:
                                 ref_max_relative_residual
   oracle/_ref/libref_sparse.so  ref_sparse_ipt_cpu_reference, ref_build_banded_csc,
                                 ref_h20_w_csc, ref_prepare_sparse_csc_sorted,
-                                ref_block_cluster_prepare, ref_block_cluster_solve_basis
+                                ref_block_cluster_prepare, ref_block_cluster_solve_basis,
+                                ref_prepare_sparse_csc_lifted
 
 Nothing from the reference is copied into the repository; the outputs are
 git-ignored.  The reference path only exists in the build container, so the
@@ -116,6 +117,45 @@ extern "C" int ref_prepare_sparse_csc_sorted(const int *col_ptr, const int *row_
     memcpy(out_diag, p.diagonal, (size_t)n * sizeof(double));
     for (int i = 0; i < n; ++i) out_perm[i] = p.basis_to_original ? p.basis_to_original[i] : i;
     int out = p.nnz;
+    ipt_prepared_csc_free(&p);
+    return out;
+}
+/* The plain path's preparation with degeneracy lifting (ipt_prepare_sparse_csc
+ * with lift = 1): returns the prepared nnz (or -status) and fills the CSC,
+ * diagonal, basis_to_original and the rotations; when vectors is not NULL the
+ * reference's back-transform (ipt_apply_prepared_q_to_vectors) is applied to
+ * them in place (n x kv, prepared basis -> caller's basis). */
+extern "C" int ref_prepare_sparse_csc_lifted(const int *col_ptr, const int *row_ind,
+                                             const double *values, int n, int k, int nnz,
+                                             double threshold, int *out_col_ptr,
+                                             int *out_row_ind, double *out_values, int capacity,
+                                             double *out_diag, int *out_perm, int *rot_first,
+                                             int *rot_size, double *rot_values, int rot_cap,
+                                             int rot_values_cap, int *rot_count,
+                                             double *vectors, int kv) {
+    IPTPreparedCsc p;
+    int s = ipt_prepare_sparse_csc(col_ptr, row_ind, values, n, k, nnz, 1, 1, threshold, &p);
+    if (s != 0) return -s;
+    int out = p.nnz;
+    *rot_count = p.rotation_count;
+    if (p.nnz <= capacity && p.rotation_count <= rot_cap &&
+        p.rotation_values_count <= rot_values_cap) {
+        memcpy(out_col_ptr, p.col_ptr, (size_t)(n + 1) * sizeof(int));
+        if (p.nnz > 0) {
+            memcpy(out_row_ind, p.row_ind, (size_t)p.nnz * sizeof(int));
+            memcpy(out_values, p.values, (size_t)p.nnz * sizeof(double));
+        }
+        memcpy(out_diag, p.diagonal, (size_t)n * sizeof(double));
+        for (int i = 0; i < n; ++i) out_perm[i] = p.basis_to_original ? p.basis_to_original[i] : i;
+        if (p.rotation_count > 0) {
+            memcpy(rot_first, p.rotation_starts, (size_t)p.rotation_count * sizeof(int));
+            memcpy(rot_size, p.rotation_sizes, (size_t)p.rotation_count * sizeof(int));
+            memcpy(rot_values, p.rotation_values, (size_t)p.rotation_values_count * sizeof(double));
+        }
+        if (vectors != NULL && kv > 0) ipt_apply_prepared_q_to_vectors(&p, vectors, kv);
+    } else {
+        out = -1000;
+    }
     ipt_prepared_csc_free(&p);
     return out;
 }

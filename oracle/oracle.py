@@ -255,6 +255,10 @@ def ref_lib(which):
             L.ref_h20_w_csc.argtypes = [vp, vp, vp]
             L.ref_prepare_sparse_csc_sorted.restype = i
             L.ref_prepare_sparse_csc_sorted.argtypes = [vp, vp, vp, i, i, i, vp, vp, vp, vp, vp]
+            L.ref_prepare_sparse_csc_lifted.restype = i
+            L.ref_prepare_sparse_csc_lifted.argtypes = [vp, vp, vp, i, i, i, C.c_double, vp, vp,
+                                                        vp, i, vp, vp, vp, vp, vp, i, i, vp, vp,
+                                                        i]
             L.ref_block_cluster_prepare.restype = i
             L.ref_block_cluster_prepare.argtypes = [vp, vp, vp, i, i, i, vp, i, vp, vp, i, vp]
             L.ref_block_cluster_solve_basis.restype = i
@@ -483,6 +487,56 @@ def ref_cluster_prepare(cp, ri, va, n, k):
         return cnt
     return ([(int(rg[2 * i]), int(rg[2 * i + 1])) for i in range(cnt)],
             [int(x) for x in added[:na[0]]], bool(lim[0]))
+
+
+def ref_prepare_lifted(cp, ri, va, n, k, threshold=0.0, vectors=None):
+    """The reference's plain-path preparation with degeneracy lifting (needs
+    oracle/_ref): a dict of the prepared CSC, diagonal, permutation and
+    rotations, with the back-transformed copy of `vectors` (prepared basis ->
+    caller's basis) when given; a negative status when it fails."""
+    L = ref_lib("sparse")
+    cp = np.ascontiguousarray(cp, dtype=np.int32)
+    ri = np.ascontiguousarray(ri, dtype=np.int32)
+    va = np.ascontiguousarray(va, dtype=np.float64)
+    cap = max(4 * ri.size, n * n, 16)
+    ocp = np.zeros(n + 1, np.int32)
+    ori = np.zeros(cap, np.int32)
+    ova = np.zeros(cap)
+    od = np.zeros(n)
+    op = np.zeros(n, np.int32)
+    rf = np.zeros(n, np.int32)
+    rs = np.zeros(n, np.int32)
+    rv = np.zeros(max(1, 64 * 64 * n))
+    rc = np.zeros(1, np.int32)
+    V = None if vectors is None else np.array(vectors, dtype=np.float64, order="F", copy=True)
+    nnz = L.ref_prepare_sparse_csc_lifted(_p(cp), _p(ri), _p(va), n, k, int(cp[-1]), threshold,
+                                          _p(ocp), _p(ori), _p(ova), cap, _p(od), _p(op), _p(rf),
+                                          _p(rs), _p(rv), n, rv.size, _p(rc), _p(V),
+                                          0 if V is None else V.shape[1])
+    if nnz < 0:
+        return nnz
+    r = int(rc[0])
+    return {"col_ptr": ocp, "row_ind": ori[:nnz], "values": ova[:nnz], "diag": od, "perm": op,
+            "rot_first": rf[:r], "rot_size": rs[:r],
+            "rot_values": rv[:int(sum(int(m) * int(m) for m in rs[:r]))], "vectors": V}
+
+
+def unprepare_vectors(X, perm, rot_first, rot_size, rot_values):
+    """Prepared-basis vectors back to the caller's basis: the lifting
+    rotations last first (v[block] <- Q v[block]), then basis_to_original
+    (restates IPT_C_GPU/src/ipt_preparation.cu:1222-1293)."""
+    X = np.array(X, dtype=np.float64, order="F", copy=True)
+    ofs = int(sum(int(m) * int(m) for m in rot_size))
+    for first, m in reversed(list(zip(rot_first, rot_size))):
+        first, m = int(first), int(m)
+        ofs -= m * m
+        Q = np.asarray(rot_values[ofs:ofs + m * m]).reshape((m, m), order="F")
+        for j in range(X.shape[1]):
+            blk = X[first:first + m, j].copy()
+            X[first:first + m, j] = [sum(Q[i, l] * blk[l] for l in range(m)) for i in range(m)]
+    out = np.empty_like(X)
+    out[np.asarray(perm), :] = X
+    return out
 
 
 def ref_cluster_solve_basis(cp, ri, va, diag, first, last, maxiter, tol, damping=1.0):

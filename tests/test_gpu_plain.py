@@ -171,3 +171,36 @@ def test_sparse_device_entry(cuda, golden):
     lib.ipt_cuda_free_device_result(dvec, dval)
     assert np.abs(X - arrays["sparse_%s_vectors" % name]).max() <= 1e-8
     assert np.abs(v - arrays["sparse_%s_values" % name]).max() <= 1e-8
+
+
+def test_sparse_lifted_degenerate_targets(cuda):
+    """Degenerate targets: the plain sparse path lifts them as the reference
+    does (ipt_cuda.cu:5077-5090, fixtures from the reference's preparation):
+    the result is the oracle's IPT on the prepared (rotated) matrix, rotated
+    back; a matrix whose preparation the reference rejects is rejected."""
+    import os
+    from scipy.sparse import csc_matrix
+    z = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden",
+                             "lift_kat.npz"))
+    lifted = 0
+    for c in [str(x) for x in z["cases"]]:
+        n, k, ncp, nri = (int(x) for x in z[c + "_params"])
+        cp, ri = z[c + "_in"][:ncp], z[c + "_in"][ncp:ncp + nri]
+        va = z[c + "_in_values"]
+        if int(z[c + "_status"][0]) != 0:
+            with pytest.raises(Exception):
+                api.ipt_cuda_sparse_csc(cp, ri, va, n, k, 40)
+            continue
+        X, v, _ = api.ipt_cuda_sparse_csc(cp, ri, va, n, k, 40)
+        Hp = csc_matrix((z[c + "_values"], z[c + "_row_ind"], z[c + "_col_ptr"]),
+                        shape=(n, n)).tocsr()
+        Hp.sort_indices()
+        Xo, vo, _, _ = oracle.ipt_csr(Hp.indptr, Hp.indices, Hp.data, z[c + "_diag"], n, k, 40)
+        Xb = oracle.unprepare_vectors(Xo, z[c + "_perm"], z[c + "_rot_first"],
+                                      z[c + "_rot_size"], z[c + "_rot_values"])
+        assert np.abs(X - Xb).max() <= 1e-10, c
+        assert np.abs(v - vo).max() <= 1e-10, c
+        H = oracle.csc_to_dense(cp, ri, va, n)
+        assert oracle.max_relative_residual(H, X, v) <= 1e-8, c
+        lifted += len(z[c + "_rot_first"]) > 0
+    assert lifted >= 4

@@ -1,0 +1,116 @@
+"""The plain sparse path's host preparation with degeneracy lifting
+(ipt_block_prepare_csc) against the reference's own preparation, bit for
+bit: the committed fixtures (tests/golden/make_lift_golden.py) and, where
+oracle/_ref was built, a sweep; the oracle's back-transform against the
+reference's."""
+import os
+
+import numpy as np
+import pytest
+from scipy.sparse import csc_matrix
+
+from block_ipt_gb300 import api
+from oracle import oracle
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "lift_kat.npz")
+KEYS = ("col_ptr", "row_ind", "values", "diag", "perm", "rot_first", "rot_size", "rot_values")
+
+
+def bits(a):
+    a = np.asarray(a)
+    return a.view(np.uint64) if a.dtype == np.float64 else a.astype(np.int64)
+
+
+def case_input(z, c):
+    n, k, ncp, nri = (int(x) for x in z[c + "_params"])
+    ints = z[c + "_in"]
+    return ints[:ncp], ints[ncp:ncp + nri], z[c + "_in_values"], n, k
+
+
+@pytest.fixture(scope="module")
+def kat():
+    return np.load(GOLDEN)
+
+
+def test_lifted_preparation_matches_reference_fixtures(lib, kat):
+    rotated = 0
+    for c in [str(x) for x in kat["cases"]]:
+        cp, ri, va, n, k = case_input(kat, c)
+        if int(kat[c + "_status"][0]) != 0:
+            with pytest.raises(Exception):
+                api.prepare_csc(cp, ri, va, n, k)
+            continue
+        got = api.prepare_csc(cp, ri, va, n, k)
+        for key in KEYS:
+            want = kat[c + "_" + key]
+            assert np.array_equal(bits(got[key]), bits(want)), (c, key)
+        rotated += len(got["rot_first"]) > 0
+    assert rotated >= 4
+
+
+def test_oracle_back_transform_matches_reference(kat):
+    for c in [str(x) for x in kat["cases"]]:
+        if int(kat[c + "_status"][0]) != 0:
+            continue
+        out = oracle.unprepare_vectors(kat[c + "_vectors_in"], kat[c + "_perm"],
+                                       kat[c + "_rot_first"], kat[c + "_rot_size"],
+                                       kat[c + "_rot_values"])
+        assert np.array_equal(bits(out), bits(kat[c + "_vectors_out"])), c
+
+
+def test_no_lifting_on_the_reference_test_matrices(lib, golden):
+    """The reference's own sparse cases (banded n = 64, H2O "W") have no
+    degenerate targets: lifting leaves them as the sort-only preparation."""
+    arrays, meta = golden
+    for case in meta["sparse"]:
+        name = case["name"]
+        cp = arrays["sparse_%s_col_ptr" % name]
+        ri = arrays["sparse_%s_row_ind" % name]
+        va = arrays["sparse_%s_values_csc" % name]
+        got = api.prepare_csc(cp, ri, va, case["n"], case["k"])
+        assert len(got["rot_first"]) == 0
+        np.testing.assert_array_equal(got["diag"], arrays["sparse_%s_prep_diag" % name])
+        np.testing.assert_array_equal(got["perm"], arrays["sparse_%s_prep_perm" % name])
+
+
+def test_lifted_blocks_are_orthogonal_rotations(lib, kat):
+    for c in [str(x) for x in kat["cases"]]:
+        if int(kat[c + "_status"][0]) != 0:
+            continue
+        cp, ri, va, n, k = case_input(kat, c)
+        got = api.prepare_csc(cp, ri, va, n, k)
+        ofs = 0
+        for m in got["rot_size"]:
+            Q = got["rot_values"][ofs:ofs + m * m].reshape((m, m), order="F")
+            np.testing.assert_allclose(Q.T @ Q, np.eye(m), atol=1e-13)
+            ofs += m * m
+        # the prepared matrix is the rotated, permuted input (eigenvalues kept)
+        H = csc_matrix((va, ri, cp), shape=(n, n)).toarray()
+        Hp = csc_matrix((got["values"], got["row_ind"], got["col_ptr"]), shape=(n, n)).toarray()
+        np.testing.assert_allclose(np.linalg.eigvalsh(0.5 * (Hp + Hp.T)),
+                                   np.linalg.eigvalsh(H), atol=1e-12 * np.abs(H).max())
+
+
+@pytest.mark.skipif(not oracle.ref_available(), reason="oracle/_ref not built here")
+def test_lifted_preparation_sweep_against_reference(lib):
+    ok = rotated = rejected = 0
+    for seed in range(20):
+        for coupling in (0.01, 0.3, 2.0):
+            n = 30 + seed
+            _, _, _, H = oracle.cluster_test_matrix(n, seed, coupling)
+            P = np.random.default_rng(seed).permutation(n)
+            S = csc_matrix(H[np.ix_(P, P)])
+            S.sort_indices()
+            for k in (1, 3, 6):
+                ref = oracle.ref_prepare_lifted(S.indptr, S.indices, S.data, n, k)
+                if isinstance(ref, int):
+                    with pytest.raises(Exception):
+                        api.prepare_csc(S.indptr, S.indices, S.data, n, k)
+                    rejected += 1
+                    continue
+                got = api.prepare_csc(S.indptr, S.indices, S.data, n, k)
+                for key in KEYS:
+                    assert np.array_equal(bits(got[key]), bits(ref[key])), (seed, coupling, k, key)
+                ok += 1
+                rotated += len(ref["rot_first"]) > 0
+    assert ok > 50 and rotated > 10 and rejected > 10
