@@ -180,6 +180,12 @@ class IPTBatchReport(C.Structure):
                 ("latency_ms", C.c_double), ("completion_ms", C.c_double)]
 
 
+class IPTCscCacheInfo(C.Structure):
+    _fields_ = [("magic", C.c_char * 9), ("version", C.c_int), ("n", C.c_int), ("nnz", C.c_int),
+                ("matrix_inf_norm", C.c_double), ("norb", C.c_int), ("nelec", C.c_int),
+                ("neleca", C.c_int), ("nelecb", C.c_int), ("na", C.c_int), ("nb", C.c_int)]
+
+
 # (name, restype, argtypes) of every exported entry point
 _vp = C.c_void_p
 SIGNATURES = [
@@ -219,6 +225,11 @@ SIGNATURES = [
     ("ipt_block_cluster_ranges", _i, [_vp, _vp, _vp, _i, _i, _i, _i, C.c_double, _i,
                                       C.c_double, _vp, _i, C.POINTER(C.c_int),
                                       C.POINTER(C.c_int)]),
+    ("ipt_block_csc_cache_info", _i, [C.c_char_p, C.POINTER(IPTCscCacheInfo)]),
+    ("ipt_block_csc_cache_read", _i, [C.c_char_p, _vp, _vp, _vp, _vp, _i, _i,
+                                      C.POINTER(IPTCscCacheInfo)]),
+    ("ipt_block_csc_cache_write", _i, [C.c_char_p, C.POINTER(IPTCscCacheInfo), _vp, _vp, _vp,
+                                       _vp]),
     ("ipt_block_prepare_csc", _i, [_vp, _vp, _vp, _i, _i, _i, _i, C.c_double, _vp, _vp, _vp,
                                    _i, C.POINTER(C.c_int), _vp, _vp, _vp, _vp, _i, _vp, _i,
                                    C.POINTER(C.c_int)]),

@@ -7,6 +7,7 @@ as 2-D numpy arrays (copied to column-major doubles); sparse input is CSC.
 Every call goes through libipt_gb300.so; nothing here computes on the CPU.
 """
 import ctypes as C
+import os
 
 import numpy as np
 
@@ -426,3 +427,49 @@ def prepare_csc(col_ptr, row_ind, values, n, k, lift=True, threshold=0.0):
     return {"col_ptr": ocp, "row_ind": ori[:nnz.value], "values": ova[:nnz.value], "diag": od,
             "perm": op, "rot_first": rf[:r], "rot_size": rs[:r],
             "rot_values": rv[:int(sum(int(m) * int(m) for m in rs[:r]))]}
+
+
+# ---- the reference's binary CSC matrix cache (include/ipt_block.h) -------------
+_CACHE_FIELDS = ("norb", "nelec", "neleca", "nelecb", "na", "nb")
+
+
+def read_csc_cache(path):
+    """A cache file of the reference's molecule benchmarks: (col_ptr, row_ind,
+    values, diagonal, info dict)."""
+    lib = _lib.load()
+    info = _lib.IPTCscCacheInfo()
+    p = os.fsencode(path)
+    _check(lib.ipt_block_csc_cache_info(p, C.byref(info)), "ipt_block_csc_cache_info")
+    n, nnz = info.n, info.nnz
+    cp = np.zeros(n + 1, np.int32)
+    ri = np.zeros(max(1, nnz), np.int32)
+    va = np.zeros(max(1, nnz))
+    dg = np.zeros(n)
+    _check(lib.ipt_block_csc_cache_read(p, _ptr(cp), _ptr(ri), _ptr(va), _ptr(dg), n, nnz,
+                                        C.byref(info)), "ipt_block_csc_cache_read")
+    meta = {"magic": info.magic.decode(), "version": info.version, "n": n, "nnz": nnz,
+            "matrix_inf_norm": info.matrix_inf_norm}
+    meta.update({f: getattr(info, f) for f in _CACHE_FIELDS})
+    return cp, ri[:nnz], va[:nnz], dg, meta
+
+
+def write_csc_cache(path, col_ptr, row_ind, values, diagonal, magic="IPTGENC1",
+                    matrix_inf_norm=None, **counts):
+    """Write a cache file in the reference's layout (counts: norb, nelec,
+    neleca, nelecb, na, nb; the norm defaults to max row sum of |H|)."""
+    cp, ri, va, dg = _i32(col_ptr), _i32(row_ind), _f64(values), _f64(diagonal)
+    n = len(cp) - 1
+    if matrix_inf_norm is None:
+        rows = np.zeros(n)
+        np.add.at(rows, ri, np.abs(va))
+        matrix_inf_norm = float(rows.max()) if n else 0.0
+    info = _lib.IPTCscCacheInfo()
+    info.magic = magic.encode()[:8]
+    info.version = 1
+    info.n, info.nnz = n, len(ri)
+    info.matrix_inf_norm = matrix_inf_norm
+    for f in _CACHE_FIELDS:
+        setattr(info, f, int(counts.get(f, 0)))
+    _check(_lib.load().ipt_block_csc_cache_write(os.fsencode(path), C.byref(info), _ptr(cp),
+                                                 _ptr(ri), _ptr(va), _ptr(dg)),
+           "ipt_block_csc_cache_write")

@@ -168,6 +168,44 @@ int ipt_block_prepare_csc(const int *col_ptr, const int *row_ind, const double *
                           int rot_capacity, double *rot_values, int rot_values_capacity,
                           int *rot_count);
 
+/* ---- the reference's binary CSC matrix cache (host only) -----------------
+ *
+ * The file its molecule benchmarks write for a generated FCI Hamiltonian
+ * (write_ch4_matrix_cache / read_ch4_matrix_cache,
+ * IPT_C_GPU/test/sparse/CH4/benchmark_ch4_sto6g_fci_15876_ipt.cu:1015-1121):
+ * a 56-byte little-endian header (magic "IPT" + tag + "C1", version 1, n,
+ * nnz, ||H||_inf, orbital and electron counts), then int32 col_ptr[n+1],
+ * int32 row_ind[nnz], double values[nnz], double diagonal[n]. */
+typedef struct {
+    char magic[9];          /* e.g. "IPTCH4C1", NUL-terminated */
+    int version;            /* 1 */
+    int n;
+    int nnz;
+    double matrix_inf_norm;
+    int norb;
+    int nelec;
+    int neleca;
+    int nelecb;
+    int na;
+    int nb;
+} IPTCscCacheInfo;
+
+/* The header of a cache file; IPT_CUDA_INVALID_ARGUMENT if it is not one. */
+int ipt_block_csc_cache_info(const char *path, IPTCscCacheInfo *info);
+
+/* The whole file into caller arrays (n_capacity >= n, nnz_capacity >= nnz,
+ * from ipt_block_csc_cache_info).  IPT_CUDA_INVALID_ARGUMENT for a short or
+ * foreign file, arrays that are not a valid CSC, or a norm that is negative
+ * or not finite (the reference's checks). */
+int ipt_block_csc_cache_read(const char *path, int *col_ptr, int *row_ind, double *values,
+                             double *diagonal, int n_capacity, int nnz_capacity,
+                             IPTCscCacheInfo *info);
+
+/* Write a cache file (info->magic and the counts from the caller; version
+ * 1); the data go to path.tmp, renamed over path when complete. */
+int ipt_block_csc_cache_write(const char *path, const IPTCscCacheInfo *info, const int *col_ptr,
+                              const int *row_ind, const double *values, const double *diagonal);
+
 /* Block-cluster basis (replaces ipt_block_cluster_solve_basis_gpu, one call
  * per cluster, IPT_C_GPU/src/ipt_cuda.cu:2871-3037): for each of the
  * `nclusters` host ranges (inclusive, ascending, disjoint, width <= 64) the

@@ -268,6 +268,41 @@ def ref_lib(which):
     return _ref[which]
 
 
+# ---- the reference's binary CSC matrix cache -------------------------------------
+def reference_csc_cache_bytes(magic, cp, ri, va, dg, norm, counts=(0, 0, 0, 0, 0, 0), version=1):
+    """A cache file as the reference's benchmarks write it: the header struct
+    (IPT_C_GPU/test/sparse/CH4/benchmark_ch4_sto6g_fci_15876_ipt.cu:182-194,
+    natural alignment: four zero bytes after nnz, 56 bytes) and the arrays in
+    the order of its writer (:1015-1066)."""
+    import struct
+    n, nnz = len(cp) - 1, len(ri)
+    head = struct.pack("<8sIii4xd6i", magic, version, n, nnz, norm, *counts)
+    return (head + np.asarray(cp, "<i4").tobytes() + np.asarray(ri, "<i4").tobytes()
+            + np.asarray(va, "<f8").tobytes() + np.asarray(dg, "<f8").tobytes())
+
+
+def parse_reference_csc_cache(data):
+    """Parse cache bytes the way the reference's inspection script does
+    (IPT_C_GPU/results/sparse/CH4_K30_debug/inspect_csc_bin.py:7-57)."""
+    import struct
+    magic, mol, version, n = struct.unpack_from("<4s4sii", data, 0)
+    nnz = struct.unpack_from("<q", data, 16)[0]
+    norm = struct.unpack_from("<d", data, 24)[0]
+    counts = struct.unpack_from("<iiiiii", data, 32)
+    o = 56
+    cp = np.frombuffer(data, "<i4", n + 1, o)
+    o += 4 * (n + 1)
+    ri = np.frombuffer(data, "<i4", nnz, o)
+    o += 4 * nnz
+    va = np.frombuffer(data, "<f8", nnz, o)
+    o += 8 * nnz
+    dg = np.frombuffer(data, "<f8", n, o)
+    assert o + 8 * n == len(data)
+    return {"magic": (magic + mol).decode(), "version": version, "n": n, "nnz": nnz,
+            "norm": norm, "counts": counts, "col_ptr": cp, "row_ind": ri, "values": va,
+            "diag": dg}
+
+
 # ---- block-cluster path ---------------------------------------------------------
 def cluster_test_matrix(n, seed, coupling=0.05, groups=3, density=0.05):
     """Symmetric CSC test matrix for the block-cluster path: ascending
