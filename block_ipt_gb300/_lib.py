@@ -186,6 +186,14 @@ class IPTCscCacheInfo(C.Structure):
                 ("neleca", C.c_int), ("nelecb", C.c_int), ("na", C.c_int), ("nb", C.c_int)]
 
 
+class ACXCudaResult(C.Structure):
+    _fields_ = [("n", C.c_int), ("k", C.c_int), ("iterations", C.c_int), ("f_calls", C.c_int),
+                ("converged", C.c_int), ("time_sec", C.c_double),
+                ("iteration_time_sec", C.c_double), ("finalization_time_sec", C.c_double),
+                ("max_residual", C.c_double), ("fixed_point_residual", C.c_double),
+                ("d_vectors", C.c_void_p), ("d_values", C.c_void_p)]
+
+
 # (name, restype, argtypes) of every exported entry point
 _vp = C.c_void_p
 SIGNATURES = [
@@ -225,6 +233,10 @@ SIGNATURES = [
     ("ipt_block_cluster_ranges", _i, [_vp, _vp, _vp, _i, _i, _i, _i, C.c_double, _i,
                                       C.c_double, _vp, _i, C.POINTER(C.c_int),
                                       C.POINTER(C.c_int)]),
+    ("acx_cuda_status_string", C.c_char_p, [_i]),
+    ("acx_cuda_reset_result", None, [C.POINTER(ACXCudaResult)]),
+    ("acx_cuda_free_result", None, [C.POINTER(ACXCudaResult)]),
+    ("acx_cuda_device_tol", _i, [_vp, _i, _i, C.c_double, _i, _vp, C.POINTER(ACXCudaResult)]),
     ("ipt_block_csc_cache_info", _i, [C.c_char_p, C.POINTER(IPTCscCacheInfo)]),
     ("ipt_block_csc_cache_read", _i, [C.c_char_p, _vp, _vp, _vp, _vp, _i, _i,
                                       C.POINTER(IPTCscCacheInfo)]),

@@ -681,3 +681,137 @@ ORACLE_API int oracle_cluster_basis(const int *row_ptr, const int *col_ind, cons
     }
     return 0;
 }
+
+/* ---- ACX extrapolation (dense FP64) -------------------------------------------
+ * IPT_C_GPU/src/ACX/acx_cuda.cu:390-620: from the identity columns, each step
+ * evaluates f1 = F(X) (residuals ||HX_j - X_j (HX)_jj|| and the map with the
+ * denominator guard |d_j - d_i| <= DBL_EPSILON, :109-172), stops once
+ * ||f1 - X||_F / ||X||_F < min(tol, 1e-12), else extrapolates with order 2
+ * (odd steps, :190-240) or order 3 (even steps, :242-296).  Products sum the
+ * inner index in ascending order; the map and the extrapolation place their
+ * FMAs as the library's CUDA kernels do.  Returns 0, 1 (invalid argument or
+ * a zero norm) or 5 (zero denominator); info = {iterations, f_calls,
+ * converged}, res = {max_residual, fixed_point_residual}; vectors_out gets
+ * the last F(X), values_out diag(H F(X)). */
+static int oracle_acx_map(const double *H, const double *d, int n, int k, const double *x,
+                          double *y, double *resid)
+{
+    int bad = 0;
+    oracle_dense_matmul(y, H, x, n, k);
+    for (int c = 0; c < k; ++c) {
+        double *yc = y + (size_t)c * n;
+        const double *xc = x + (size_t)c * n;
+        const double m = yc[c];
+        const double u = fma(-d[c], xc[c], m);
+        double rr = 0.0;
+        for (int i = 0; i < n; ++i) {
+            const double yi = yc[i], xi = xc[i];
+            const double r = fma(-xi, m, yi);
+            rr = fma(r, r, rr);
+            double v = 1.0;
+            if (i != c) {
+                const double den = d[c] - d[i];
+                if (fabs(den) <= 2.220446049250313e-16) {
+                    bad = 1;
+                    v = 0.0;
+                } else {
+                    v = fma(-xi, u, fma(-d[i], xi, yi)) / den;
+                }
+            }
+            yc[i] = v;
+        }
+        resid[c] = sqrt(rr);
+    }
+    return bad;
+}
+
+ORACLE_API int oracle_acx_dense(const double *H, int n, int k, double tol, int maxiter,
+                                double *vectors_out, double *values_out, int *info, double *res)
+{
+    if (H == NULL || n <= 0 || k <= 0 || k > n || !(tol > 0.0) || maxiter <= 0) return 1;
+    const size_t e = (size_t)n * (size_t)k;
+    const double stop_tol = tol < 1.0e-12 ? tol : 1.0e-12;
+    double *d = (double *)malloc((size_t)n * sizeof(double));
+    double *x = (double *)calloc(e, sizeof(double));
+    double *f1 = (double *)malloc(e * sizeof(double));
+    double *f2 = (double *)malloc(e * sizeof(double));
+    double *f3 = (double *)malloc(e * sizeof(double));
+    double *resid = (double *)malloc((size_t)k * sizeof(double));
+    int status = 0;
+    info[0] = info[1] = info[2] = 0;
+    res[0] = res[1] = NAN;
+    for (int i = 0; i < n; ++i) d[i] = H[(size_t)i + (size_t)i * n];
+    for (int c = 0; c < k; ++c) x[(size_t)c + (size_t)c * n] = 1.0;
+    for (int iter = 1; iter <= maxiter; ++iter) {
+        const int order = (iter % 2 == 1) ? 2 : 3;
+        info[0] = iter;
+        if (oracle_acx_map(H, d, n, k, x, f1, resid)) {
+            status = 5;
+            break;
+        }
+        info[1] += 1;
+        double mx = 0.0, dd = 0.0, bb = 0.0;
+        for (int c = 0; c < k; ++c) mx = resid[c] > mx ? resid[c] : mx;
+        res[0] = mx;
+        for (size_t i = 0; i < e; ++i) {
+            const double t = f1[i] - x[i];
+            dd = fma(t, t, dd);
+            bb = fma(x[i], x[i], bb);
+        }
+        if (!(bb > 0.0) || !isfinite(bb)) {
+            status = 1;
+            break;
+        }
+        res[1] = sqrt(dd) / sqrt(bb);
+        if (res[1] < stop_tol) {
+            info[2] = 1;
+            break;
+        }
+        oracle_acx_map(H, d, n, k, f1, f2, resid);
+        info[1] += 1;
+        if (order == 3) {
+            oracle_acx_map(H, d, n, k, f2, f3, resid);
+            info[1] += 1;
+        }
+        for (int c = 0; c < k; ++c) {
+            const size_t b = (size_t)c * n;
+            double num = 0.0, den = 0.0;
+            for (int i = 0; i < n; ++i) {
+                const double d2 = fma(-2.0, f1[b + i], f2[b + i]) + x[b + i];
+                if (order == 2) {
+                    const double d1 = f1[b + i] - x[b + i];
+                    num = fma(d2, d1, num);
+                    den = fma(d2, d2, den);
+                } else {
+                    const double d3 = fma(3.0, f1[b + i], fma(-3.0, f2[b + i], f3[b + i])) - x[b + i];
+                    num = fma(d3, d2, num);
+                    den = fma(d3, d3, den);
+                }
+            }
+            const double g = den > 0.0 ? fabs(num / den) : 0.0, g2 = g * g, g3 = g2 * g;
+            for (int i = 0; i < n; ++i) {
+                const double xi = x[b + i];
+                const double d1 = f1[b + i] - xi;
+                const double d2 = fma(-2.0, f1[b + i], f2[b + i]) + xi;
+                if (order == 2) {
+                    x[b + i] = xi + fma(2.0 * g, d1, g2 * d2);
+                } else {
+                    const double d3 = fma(3.0, f1[b + i], fma(-3.0, f2[b + i], f3[b + i])) - xi;
+                    x[b + i] = xi + fma(3.0 * g, d1, fma(3.0 * g2, d2, g3 * d3));
+                }
+            }
+        }
+    }
+    if (status == 0) {
+        memcpy(vectors_out, f1, e * sizeof(double));
+        oracle_dense_matmul(f2, H, f1, n, k);
+        for (int c = 0; c < k; ++c) values_out[c] = f2[(size_t)c + (size_t)c * n];
+    }
+    free(d);
+    free(x);
+    free(f1);
+    free(f2);
+    free(f3);
+    free(resid);
+    return status;
+}

@@ -60,6 +60,8 @@ def lib():
         L.oracle_ipt_dense_products_to_residual.restype = i
         L.oracle_ipt_dense_products_to_residual.argtypes = [vp, i, i, i, d, d, vp]
         L.oracle_num_threads.restype = i
+        L.oracle_acx_dense.restype = i
+        L.oracle_acx_dense.argtypes = [vp, i, i, d, i, vp, vp, vp, vp]
         L.oracle_cluster_update.restype = i
         L.oracle_cluster_update.argtypes = [vp, vp, vp, i, i, i, d, vp]
         L.oracle_cluster_basis.restype = i
@@ -266,6 +268,35 @@ def ref_lib(which):
                                                         C.c_double, C.c_double, vp, vp]
         _ref[which] = L
     return _ref[which]
+
+
+# ---- ACX extrapolation ------------------------------------------------------------
+def acx_dense(H, k, tol, maxiter):
+    """ACX over the dense IPT map (oracle_acx_dense): (vectors, values, info,
+    status) with info = iterations, f_calls, converged, max_residual,
+    fixed_point_residual."""
+    H = np.asfortranarray(H, dtype=np.float64)
+    n = H.shape[0]
+    X = np.zeros((n, k), dtype=np.float64, order="F")
+    v = np.zeros(k)
+    info = np.zeros(3, dtype=np.int32)
+    res = np.zeros(2)
+    st = lib().oracle_acx_dense(_p(H), n, k, tol, maxiter, _p(X), _p(v), _p(info), _p(res))
+    return X, v, {"iterations": int(info[0]), "f_calls": int(info[1]),
+                  "converged": int(info[2]), "max_residual": float(res[0]),
+                  "fixed_point_residual": float(res[1])}, st
+
+
+def acx_test_matrix(n, epsilon, seed):
+    """Symmetric dense matrix of the reference's ACX benchmark shape
+    (IPT_C_GPU/test/ACX/benchmark_acx_cuda_sweep.cu:284-313): diagonal
+    row + 1 + eps u, off-diagonal eps (u_ij + u_ji) / 2, with u uniform in
+    [0, 1) from numpy's seeded generator standing in for its hash."""
+    rng = np.random.default_rng(seed)
+    U = rng.uniform(size=(n, n))
+    H = 0.5 * epsilon * (U + U.T)
+    H[np.diag_indices(n)] = np.arange(1, n + 1) + epsilon * np.diag(U)
+    return np.asfortranarray(H)
 
 
 # ---- the reference's binary CSC matrix cache -------------------------------------
