@@ -76,6 +76,7 @@ def parse():
     ap.add_argument("--no-learned", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--no-fci-free", action="store_true")
+    ap.add_argument("--no-acx", action="store_true")
     ap.add_argument("--fci-free-orbitals", type=int, default=14)
     ap.add_argument("--batch", type=int, default=512)
     ap.add_argument("--batch-steps", type=int, default=3)
@@ -347,6 +348,50 @@ def fci_section(args, torch, lib, stream, flush, dev):
                             "achieved_fp64_tflops": achieved},
             "kernel_ms": {kk: round(val[0] / len(times), 4) for kk, val in prof.items() if val[1]},
             "learned": learned_part, "block_cluster": cluster}
+
+
+def acx_section(torch, lib, dH, n, k):
+    """ACX extrapolation over the FP64 IPT map (the reference's
+    acx_cuda_device_tol) on the headline matrix: steps, map evaluations,
+    wall time as the reference reports it (result->time_sec), the FP64 check."""
+    res = _lib_mod().ACXCudaResult()
+    lib.acx_cuda_device_tol(C.c_void_p(dH.data_ptr()), n, k, 1e-12, 200, None, C.byref(res))
+    lib.acx_cuda_free_result(C.byref(res))  # warm-up
+    torch.cuda.synchronize()
+    res = _lib_mod().ACXCudaResult()
+    st = lib.acx_cuda_device_tol(C.c_void_p(dH.data_ptr()), n, k, 1e-12, 200, None, C.byref(res))
+    if st != 0:
+        return {"status": st}
+    X = torch.empty((k, n), dtype=torch.float64, device=dH.device)
+    v = torch.empty(k, dtype=torch.float64, device=dH.device)
+    rt = _cudart()
+    rt.cudaMemcpy(C.c_void_p(X.data_ptr()), C.c_void_p(res.d_vectors), C.c_size_t(8 * n * k), 3)
+    rt.cudaMemcpy(C.c_void_p(v.data_ptr()), C.c_void_p(res.d_values), C.c_size_t(8 * k), 3)
+    Xc = X.T
+    R = dH @ Xc - Xc * v[None, :]
+    hn = float(dH.abs().sum(dim=1).max())
+    check = float((R.norm(dim=0) / (torch.clamp(Xc.norm(dim=0), min=1.0) * max(1.0, hn))).max())
+    out = {"workload": "dense n=%d, k=%d (the headline matrix), tol 1e-12" % (n, k),
+           "ms": res.time_sec * 1e3, "iteration_ms": res.iteration_time_sec * 1e3,
+           "iterations": res.iterations, "f_calls": res.f_calls, "converged": res.converged,
+           "fixed_point_residual": res.fixed_point_residual, "max_scaled_residual": check}
+    lib.acx_cuda_free_result(C.byref(res))
+    return out
+
+
+def _lib_mod():
+    from block_ipt_gb300 import _lib
+    return _lib
+
+
+def _cudart():
+    for name in ("libcudart.so", "/usr/local/cuda/lib64/libcudart.so", "libcudart.so.13",
+                 "libcudart.so.12"):
+        try:
+            return C.CDLL(name)
+        except OSError:
+            continue
+    raise OSError("libcudart not found")
 
 
 def gj_fmas(m):
@@ -759,6 +804,13 @@ def run_ours(args):
     if not args.no_fci_free and rank == 0:
         fci_free = fci_free_section(args, torch, dev, mlp_params)
 
+    acx = None
+    if not args.no_acx and rank == 0:
+        try:
+            acx = acx_section(torch, lib, dH, n, k)
+        except Exception as exc:  # a side measurement never takes the headline line down
+            acx = {"error": repr(exc)}
+
     cpu = None
     if not args.no_cpu and rank == 0:
         prods = plain_products(n, k, args.seed)
@@ -807,6 +859,7 @@ def run_ours(args):
             "fci_config3": fci,
             "batched_config2": batched,
             "matrix_free_config4": fci_free,
+            "acx_fp64": acx,
         }
         print(json.dumps(line), flush=True)
     if world > 1:
