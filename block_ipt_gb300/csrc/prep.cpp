@@ -740,15 +740,37 @@ static void rotate_block_csc(std::vector<int> *col_ptr, std::vector<int> *row_in
     (*col_ptr)[(size_t)n] = (int)row_ind->size();
 }
 
-// Real symmetric within 1e-12 relative, entry by entry (ipt_preparation.cu:860-883).
+// Real symmetric within 1e-12 relative, entry by entry (ipt_preparation.cu:860-883):
+// each stored (r, c, v) against the sum of the stored entries at (c, r).  The
+// sums come from a copy of every column sorted by row (stable, so duplicates
+// add in storage order, as a scan of the column would), found by binary
+// search: O(nnz log) instead of a column scan per entry.
 static bool csc_is_symmetric(const std::vector<int> &cp, const std::vector<int> &ri,
                              const std::vector<double> &va, int n)
 {
+    const size_t nnz = ri.size();
+    std::vector<std::pair<int, double>> sorted(nnz);
+    for (size_t p = 0; p < nnz; ++p) sorted[p] = std::make_pair(ri[p], va[p]);
+    for (int c = 0; c < n; ++c) {
+        std::stable_sort(sorted.begin() + cp[(size_t)c], sorted.begin() + cp[(size_t)c + 1],
+                         [](const std::pair<int, double> &a, const std::pair<int, double> &b) {
+                             return a.first < b.first;
+                         });
+    }
+    auto sum_at = [&](int row, int col) {
+        auto b = sorted.begin() + cp[(size_t)col], e = sorted.begin() + cp[(size_t)col + 1];
+        auto it = std::lower_bound(b, e, row, [](const std::pair<int, double> &a, int r) {
+            return a.first < r;
+        });
+        double v = 0.0;
+        for (; it != e && it->first == row; ++it) v += it->second;
+        return v;
+    };
     for (int c = 0; c < n; ++c) {
         for (int p = cp[(size_t)c]; p < cp[(size_t)c + 1]; ++p) {
             const int r = ri[(size_t)p];
             const double v = va[(size_t)p];
-            const double t = csc_value_sum(cp.data(), ri.data(), va.data(), c, r);
+            const double t = sum_at(c, r);
             const double scale = std::max(1.0, std::max(std::fabs(v), std::fabs(t)));
             if (std::fabs(v - t) > 1.0e-12 * scale) return false;
         }
@@ -764,7 +786,8 @@ int lift_degeneracies(std::vector<int> *cp, std::vector<int> *ri, std::vector<do
     const GapOptions o = gap_options(degeneracy_threshold);
     const int mr = env_int("IPT_MAX_LIFT_ROUNDS", 3);
     const int rounds = mr > 0 ? mr : 3;
-    const bool symmetric = csc_is_symmetric(*cp, *ri, *va, n);
+    // symmetry of the matrix as it enters the rounds; only a lift needs it
+    int symmetric = -1;
     bool clean = false;
     for (int round = 0; round < rounds; ++round) {
         csc_diagonal_sum(cp->data(), ri->data(), va->data(), n, diag);
@@ -779,7 +802,8 @@ int lift_degeneracies(std::vector<int> *cp, std::vector<int> *ri, std::vector<do
         // a non-symmetric block would need a general real eigensolver; the
         // reference then calls LAPACK dgeev when it is linked in and fails
         // the preparation otherwise, which is what happens here
-        if (!symmetric) return IPT_CUDA_INVALID_ARGUMENT;
+        if (symmetric < 0) symmetric = csc_is_symmetric(*cp, *ri, *va, n) ? 1 : 0;
+        if (symmetric == 0) return IPT_CUDA_INVALID_ARGUMENT;
         for (const auto &sub : subspaces) {
             const int first = sub.first, m = sub.second - sub.first + 1;
             std::vector<double> block((size_t)m * (size_t)m, 0.0);

@@ -114,3 +114,30 @@ def test_lifted_preparation_sweep_against_reference(lib):
                 ok += 1
                 rotated += len(ref["rot_first"]) > 0
     assert ok > 50 and rotated > 10 and rejected > 10
+
+
+@pytest.mark.skipif(not oracle.ref_available(), reason="oracle/_ref not built here")
+def test_non_symmetric_matrices_against_reference(lib):
+    """A non-symmetric matrix whose targets need a lift is rejected, as the
+    reference rejects it without LAPACK dgeev; one without degenerate
+    targets is prepared as the reference prepares it."""
+    rejected = accepted = 0
+    for seed in range(6):
+        n = 30
+        _, _, _, H = oracle.cluster_test_matrix(n, seed, 0.3)
+        H = H.copy()
+        H[0, 5] += 0.01
+        S = csc_matrix(H)
+        S.sort_indices()
+        for k in (1, 3, 6):
+            ref = oracle.ref_prepare_lifted(S.indptr, S.indices, S.data, n, k)
+            if isinstance(ref, int):
+                with pytest.raises(Exception):
+                    api.prepare_csc(S.indptr, S.indices, S.data, n, k)
+                rejected += 1
+            else:
+                got = api.prepare_csc(S.indptr, S.indices, S.data, n, k)
+                for key in KEYS:
+                    assert np.array_equal(bits(got[key]), bits(ref[key])), (seed, k, key)
+                accepted += 1
+    assert rejected >= 3 and accepted >= 6
