@@ -194,6 +194,18 @@ class ACXCudaResult(C.Structure):
                 ("d_vectors", C.c_void_p), ("d_values", C.c_void_p)]
 
 
+class ACXMixedTF32CudaResult(C.Structure):
+    _fields_ = [("n", C.c_int), ("k", C.c_int), ("tf32_iterations", C.c_int),
+                ("fp64_iterations", C.c_int), ("tf32_f_calls", C.c_int),
+                ("fp64_f_calls", C.c_int), ("tf32_converged", C.c_int),
+                ("fp64_converged", C.c_int), ("tf32_time_sec", C.c_double),
+                ("fp64_time_sec", C.c_double), ("total_time_sec", C.c_double),
+                ("finalization_time_sec", C.c_double),
+                ("tf32_fixed_point_residual", C.c_double),
+                ("fp64_fixed_point_residual", C.c_double), ("fp64_max_residual", C.c_double),
+                ("d_vectors", C.c_void_p), ("d_values", C.c_void_p)]
+
+
 # (name, restype, argtypes) of every exported entry point
 _vp = C.c_void_p
 SIGNATURES = [
@@ -236,6 +248,11 @@ SIGNATURES = [
     ("acx_cuda_status_string", C.c_char_p, [_i]),
     ("acx_cuda_reset_result", None, [C.POINTER(ACXCudaResult)]),
     ("acx_cuda_free_result", None, [C.POINTER(ACXCudaResult)]),
+    ("acx_mixed_precision_tf32_cuda_reset_result", None, [C.POINTER(ACXMixedTF32CudaResult)]),
+    ("acx_mixed_precision_tf32_cuda_free_result", None, [C.POINTER(ACXMixedTF32CudaResult)]),
+    ("acx_mixed_precision_tf32_cuda_device_tol", _i, [_vp, _i, _i, C.c_double, _i, C.c_double,
+                                                      _i, _vp,
+                                                      C.POINTER(ACXMixedTF32CudaResult)]),
     ("acx_cuda_device_tol", _i, [_vp, _i, _i, C.c_double, _i, _vp, C.POINTER(ACXCudaResult)]),
     ("ipt_block_csc_cache_info", _i, [C.c_char_p, C.POINTER(IPTCscCacheInfo)]),
     ("ipt_block_csc_cache_read", _i, [C.c_char_p, _vp, _vp, _vp, _vp, _i, _i,

@@ -45,6 +45,41 @@ typedef struct {
     double *d_values;
 } ACXCudaResult;
 
+/* Mixed ACX (replaces IPT_C_GPU/src/ACX/acx_mixed_precision_cuda.cu:19-48,
+ * 811-905): the extrapolation first on the map with Delta and the diagonal in
+ * FP32 until ||F(X) - X|| / ||X|| <= tf32_tol (or tf32_maxiter steps), then
+ * the FP64 extrapolation from that block to min(fp64_tol, 1e-12).  The FP32
+ * stage multiplies with this library's FP32 split-K kernel where the
+ * reference uses a TF32 GEMM (no operand rounded to 10 bits).  The vectors
+ * are the FP64 stage's F(X) when it converged, else its last extrapolated X.
+ * A NULL handle is an invalid argument, as in the reference. */
+typedef struct {
+    int n;
+    int k;
+    int tf32_iterations;
+    int fp64_iterations;
+    int tf32_f_calls;
+    int fp64_f_calls;
+    int tf32_converged;
+    int fp64_converged;
+    double tf32_time_sec;
+    double fp64_time_sec;
+    double total_time_sec;
+    double finalization_time_sec;
+    double tf32_fixed_point_residual;
+    double fp64_fixed_point_residual;
+    double fp64_max_residual;
+    double *d_vectors;
+    double *d_values;
+} ACXMixedTF32CudaResult;
+
+void acx_mixed_precision_tf32_cuda_reset_result(ACXMixedTF32CudaResult *result);
+void acx_mixed_precision_tf32_cuda_free_result(ACXMixedTF32CudaResult *result);
+int acx_mixed_precision_tf32_cuda_device_tol(const double *d_matrix_col_major, int n, int k,
+                                             double tf32_tol, int tf32_maxiter, double fp64_tol,
+                                             int fp64_maxiter, cublasHandle_t handle,
+                                             ACXMixedTF32CudaResult *result);
+
 const char *acx_cuda_status_string(int status);
 void acx_cuda_reset_result(ACXCudaResult *result);
 void acx_cuda_free_result(ACXCudaResult *result);

@@ -725,10 +725,25 @@ static int oracle_acx_map(const double *H, const double *d, int n, int k, const 
     return bad;
 }
 
+static int oracle_acx_run(const double *H, int n, int k, double tol, int maxiter,
+                          const double *initial, double *vectors_out, double *values_out,
+                          int *info, double *res);
+
 ORACLE_API int oracle_acx_dense(const double *H, int n, int k, double tol, int maxiter,
                                 double *vectors_out, double *values_out, int *info, double *res)
 {
     if (H == NULL || n <= 0 || k <= 0 || k > n || !(tol > 0.0) || maxiter <= 0) return 1;
+    return oracle_acx_run(H, n, k, tol, maxiter, NULL, vectors_out, values_out, info, res);
+}
+
+/* The FP64 loop from the identity (initial == NULL: the result is the last
+ * F(X)) or from a start block (the mixed ACX's second stage,
+ * acx_mixed_precision_cuda.cu:575-809: F(X) when the stop was met, else the
+ * extrapolated X). */
+static int oracle_acx_run(const double *H, int n, int k, double tol, int maxiter,
+                          const double *initial, double *vectors_out, double *values_out,
+                          int *info, double *res)
+{
     const size_t e = (size_t)n * (size_t)k;
     const double stop_tol = tol < 1.0e-12 ? tol : 1.0e-12;
     double *d = (double *)malloc((size_t)n * sizeof(double));
@@ -740,8 +755,13 @@ ORACLE_API int oracle_acx_dense(const double *H, int n, int k, double tol, int m
     int status = 0;
     info[0] = info[1] = info[2] = 0;
     res[0] = res[1] = NAN;
+    int final_is_x = initial != NULL;
     for (int i = 0; i < n; ++i) d[i] = H[(size_t)i + (size_t)i * n];
-    for (int c = 0; c < k; ++c) x[(size_t)c + (size_t)c * n] = 1.0;
+    if (initial != NULL) {
+        memcpy(x, initial, e * sizeof(double));
+    } else {
+        for (int c = 0; c < k; ++c) x[(size_t)c + (size_t)c * n] = 1.0;
+    }
     for (int iter = 1; iter <= maxiter; ++iter) {
         const int order = (iter % 2 == 1) ? 2 : 3;
         info[0] = iter;
@@ -765,6 +785,7 @@ ORACLE_API int oracle_acx_dense(const double *H, int n, int k, double tol, int m
         res[1] = sqrt(dd) / sqrt(bb);
         if (res[1] < stop_tol) {
             info[2] = 1;
+            final_is_x = 0;
             break;
         }
         oracle_acx_map(H, d, n, k, f1, f2, resid);
@@ -803,6 +824,7 @@ ORACLE_API int oracle_acx_dense(const double *H, int n, int k, double tol, int m
         }
     }
     if (status == 0) {
+        if (final_is_x) memcpy(f1, x, e * sizeof(double));
         memcpy(vectors_out, f1, e * sizeof(double));
         oracle_dense_matmul(f2, H, f1, n, k);
         for (int c = 0; c < k; ++c) values_out[c] = f2[(size_t)c + (size_t)c * n];
@@ -813,5 +835,145 @@ ORACLE_API int oracle_acx_dense(const double *H, int n, int k, double tol, int m
     free(f2);
     free(f3);
     free(resid);
+    return status;
+}
+
+/* Mixed ACX, IPT_C_GPU/src/ACX/acx_mixed_precision_cuda.cu:360-573 then
+ * :575-809: the extrapolation on the map with Delta (zero diagonal) and the
+ * diagonal in FP32 (products summed in FP32, inner index ascending; the map
+ * (y - x u) / (d_c - d_r) with the FLT_EPSILON guard; FP32 extrapolation,
+ * step length from FP64 sums of its FP32 inner products) until the residual
+ * is <= tf32_tol, the block (F(X) if the stop was met, else X) widened to
+ * FP64, then oracle_acx_run from it.  The reference's TF32 GEMM is an FP32
+ * product here, as in the library.  info = {tf32 iterations, tf32 f_calls,
+ * tf32 converged, fp64 iterations, fp64 f_calls, fp64 converged}; res =
+ * {tf32 fixed-point residual, fp64 max residual, fp64 fixed-point residual}. */
+ORACLE_API int oracle_acx_mixed(const double *H, int n, int k, double tf32_tol, int tf32_maxiter,
+                                double fp64_tol, int fp64_maxiter, double *vectors_out,
+                                double *values_out, int *info, double *res)
+{
+    if (H == NULL || n <= 0 || k <= 0 || k > n || !(tf32_tol > 0.0) || !(fp64_tol > 0.0) ||
+        tf32_maxiter <= 0 || fp64_maxiter <= 0) {
+        return 1;
+    }
+    const size_t e = (size_t)n * (size_t)k;
+    float *D = (float *)malloc((size_t)n * (size_t)n * sizeof(float));
+    float *d = (float *)malloc((size_t)n * sizeof(float));
+    float *x = (float *)calloc(e, sizeof(float));
+    float *f[3];
+    for (int i = 0; i < 3; ++i) f[i] = (float *)malloc(e * sizeof(float));
+    double *initial = (double *)malloc(e * sizeof(double));
+    int status = 0;
+    for (int i = 0; i < 6; ++i) info[i] = 0;
+    res[0] = res[1] = res[2] = NAN;
+    for (size_t i = 0; i < (size_t)n * (size_t)n; ++i) {
+        const int r = (int)(i % (size_t)n), c = (int)(i / (size_t)n);
+        D[i] = r == c ? 0.0f : (float)H[i];
+        if (r == c) d[r] = (float)H[i];
+    }
+    for (int c = 0; c < k; ++c) x[(size_t)c + (size_t)c * n] = 1.0f;
+    const float *final_block = x;
+    for (int iter = 1; iter <= tf32_maxiter && status == 0; ++iter) {
+        const int order = (iter % 2 == 1) ? 2 : 3;
+        info[0] = iter;
+        const float *src = x;
+        for (int step = 0; step < (order == 2 ? 2 : 3); ++step) {
+            float *y = f[step];
+            for (int c = 0; c < k; ++c) {
+                const float *xc = src + (size_t)c * n;
+                float *yc = y + (size_t)c * n;
+                for (int r = 0; r < n; ++r) {
+                    float acc = 0.0f;
+                    for (int l = 0; l < n; ++l) acc += D[(size_t)r + (size_t)l * n] * xc[l];
+                    yc[r] = acc;
+                }
+                const float u = yc[c];
+                for (int i = 0; i < n; ++i) {
+                    float v = 1.0f;
+                    if (i != c) {
+                        const float den = d[c] - d[i];
+                        if (fabsf(den) <= 1.1920928955078125e-07f) {
+                            status = 5;
+                            v = 0.0f;
+                        } else {
+                            v = fmaf(-xc[i], u, yc[i]) / den;
+                        }
+                    }
+                    yc[i] = v;
+                }
+            }
+            info[1] += 1;
+            if (status != 0) break;
+            if (step == 0) {
+                double dd = 0.0, bb = 0.0;
+                for (size_t i = 0; i < e; ++i) {
+                    const double b = (double)x[i], t = (double)f[0][i] - b;
+                    dd = fma(t, t, dd);
+                    bb = fma(b, b, bb);
+                }
+                if (!(bb > 0.0) || !isfinite(bb)) {
+                    status = 1;
+                    break;
+                }
+                res[0] = sqrt(dd) / sqrt(bb);
+                if (res[0] <= tf32_tol) {
+                    info[2] = 1;
+                    final_block = f[0];
+                    break;
+                }
+            }
+            src = y;
+        }
+        if (status != 0 || info[2]) break;
+        for (int c = 0; c < k; ++c) {
+            const size_t b = (size_t)c * n;
+            const float *f1 = f[0] + b, *f2 = f[1] + b, *f3 = f[2] + b;
+            float *xc = x + b;
+            float num = 0.0f, den = 0.0f;
+            for (int i = 0; i < n; ++i) {
+                const float d2 = fmaf(-2.0f, f1[i], f2[i]) + xc[i];
+                if (order == 2) {
+                    const float d1 = f1[i] - xc[i];
+                    num = fmaf(d2, d1, num);
+                    den = fmaf(d2, d2, den);
+                } else {
+                    const float d3 = fmaf(3.0f, f1[i], fmaf(-3.0f, f2[i], f3[i])) - xc[i];
+                    num = fmaf(d3, d2, num);
+                    den = fmaf(d3, d3, den);
+                }
+            }
+            const double sd = (double)den > 0.0 ? fabs((double)num / (double)den) : 0.0;
+            const float g = (float)sd, g2 = g * g, g3 = g2 * g;
+            for (int i = 0; i < n; ++i) {
+                const float xi = xc[i];
+                const float d1 = f1[i] - xi;
+                const float d2 = fmaf(-2.0f, f1[i], f2[i]) + xi;
+                if (order == 2) {
+                    xc[i] = xi + fmaf(2.0f * g, d1, g2 * d2);
+                } else {
+                    const float d3 = fmaf(3.0f, f1[i], fmaf(-3.0f, f2[i], f3[i])) - xi;
+                    xc[i] = xi + fmaf(3.0f * g, d1, fmaf(3.0f * g2, d2, g3 * d3));
+                }
+            }
+        }
+        final_block = x;
+    }
+    if (status == 0) {
+        int info64[3];
+        double res64[2];
+        for (size_t i = 0; i < e; ++i) initial[i] = (double)final_block[i];
+        status = oracle_acx_run(H, n, k, fp64_tol, fp64_maxiter, initial, vectors_out, values_out,
+                                info64, res64);
+        info[3] = info64[0];
+        info[4] = info64[1];
+        info[5] = info64[2];
+        res[1] = res64[0];
+        res[2] = res64[1];
+    }
+    free(D);
+    free(d);
+    free(x);
+    for (int i = 0; i < 3; ++i) free(f[i]);
+    free(initial);
     return status;
 }

@@ -60,6 +60,8 @@ def lib():
         L.oracle_ipt_dense_products_to_residual.restype = i
         L.oracle_ipt_dense_products_to_residual.argtypes = [vp, i, i, i, d, d, vp]
         L.oracle_num_threads.restype = i
+        L.oracle_acx_mixed.restype = i
+        L.oracle_acx_mixed.argtypes = [vp, i, i, d, i, d, i, vp, vp, vp, vp]
         L.oracle_acx_dense.restype = i
         L.oracle_acx_dense.argtypes = [vp, i, i, d, i, vp, vp, vp, vp]
         L.oracle_cluster_update.restype = i
@@ -285,6 +287,24 @@ def acx_dense(H, k, tol, maxiter):
     return X, v, {"iterations": int(info[0]), "f_calls": int(info[1]),
                   "converged": int(info[2]), "max_residual": float(res[0]),
                   "fixed_point_residual": float(res[1])}, st
+
+
+def acx_mixed(H, k, tf32_tol, tf32_maxiter, fp64_tol, fp64_maxiter):
+    """Mixed ACX (oracle_acx_mixed): (vectors, values, info, status)."""
+    H = np.asfortranarray(H, dtype=np.float64)
+    n = H.shape[0]
+    X = np.zeros((n, k), dtype=np.float64, order="F")
+    v = np.zeros(k)
+    info = np.zeros(6, dtype=np.int32)
+    res = np.zeros(3)
+    st = lib().oracle_acx_mixed(_p(H), n, k, tf32_tol, tf32_maxiter, fp64_tol, fp64_maxiter,
+                                _p(X), _p(v), _p(info), _p(res))
+    keys = ("tf32_iterations", "tf32_f_calls", "tf32_converged", "fp64_iterations",
+            "fp64_f_calls", "fp64_converged")
+    out = {kk: int(x) for kk, x in zip(keys, info)}
+    out.update({"tf32_fixed_point_residual": float(res[0]), "fp64_max_residual": float(res[1]),
+                "fp64_fixed_point_residual": float(res[2])})
+    return X, v, out, st
 
 
 def acx_test_matrix(n, epsilon, seed):

@@ -25,3 +25,13 @@ def test_acx_oracle_status_codes():
     assert oracle.acx_dense(H, 4, 0.0, 10)[3] == 1
     H[7, 7] = H[3, 3]
     assert oracle.acx_dense(H, 4, 1e-12, 10)[3] == 5
+
+
+def test_mixed_acx_oracle_reaches_the_fp64_fixed_point():
+    H = oracle.acx_test_matrix(96, 0.06, seed=5)
+    X, v, info, st = oracle.acx_mixed(H, 8, 1e-5, 100, 1e-12, 100)
+    Xp, vp, ip, sp = oracle.acx_dense(H, 8, 1e-12, 100)
+    assert st == 0 == sp and info["fp64_converged"] == 1 and info["tf32_converged"] == 1
+    assert np.abs(X - Xp).max() <= 1e-11
+    assert info["fp64_f_calls"] < ip["f_calls"]
+    assert oracle.acx_mixed(H, 8, 0.0, 100, 1e-12, 100)[3] == 1

@@ -73,3 +73,54 @@ def test_acx_status_codes(cuda):
         res = _lib.ACXCudaResult()
         assert lib.acx_cuda_device_tol(C.c_void_p(1), n, k, tol, it, None, C.byref(res)) == 1
     assert lib.acx_cuda_device_tol(None, 8, 2, 1e-12, 10, None, C.byref(res)) == 1
+
+
+def run_mixed(torch, H, k, tf32_tol, tf32_maxiter, fp64_tol, fp64_maxiter, handle=True):
+    lib = _lib.load()
+    n = H.shape[0]
+    dH = torch.from_numpy(np.ascontiguousarray(H.T)).cuda()
+    res = _lib.ACXMixedTF32CudaResult()
+    h = C.c_void_p(torch.cuda.current_blas_handle()) if handle else None
+    st = lib.acx_mixed_precision_tf32_cuda_device_tol(C.c_void_p(dH.data_ptr()), n, k, tf32_tol,
+                                                      tf32_maxiter, fp64_tol, fp64_maxiter, h,
+                                                      C.byref(res))
+    torch.cuda.synchronize()
+    if st != 0:
+        assert not res.d_vectors and not res.d_values
+        return st, None, None, res
+    X = device_to_host(C.c_void_p(res.d_vectors), np.zeros((k, n))).T
+    v = device_to_host(C.c_void_p(res.d_values), np.zeros(k))
+    info = {f: getattr(res, f) for f, _ in _lib.ACXMixedTF32CudaResult._fields_
+            if not f.startswith("d_")}
+    lib.acx_mixed_precision_tf32_cuda_free_result(C.byref(res))
+    return st, X, v, info
+
+
+@pytest.mark.parametrize("n,k,eps", [(300, 8, 0.06), (400, 40, 0.2)])
+def test_mixed_acx_matches_oracle(cuda, n, k, eps):
+    """FP32 stage, then FP64 from its block: the oracle's counts (the FP32
+    stage within one step, its sums run in another order) and the same FP64
+    fixed point as the plain ACX."""
+    H = oracle.acx_test_matrix(n, eps, seed=n + 7)
+    st, X, v, info = run_mixed(cuda, H, k, 1e-5, 100, 1e-12, 100)
+    Xo, vo, io, so = oracle.acx_mixed(H, k, 1e-5, 100, 1e-12, 100)
+    assert st == 0 and so == 0
+    assert info["tf32_converged"] == 1 == io["tf32_converged"]
+    assert info["fp64_converged"] == 1 == io["fp64_converged"]
+    assert abs(info["tf32_iterations"] - io["tf32_iterations"]) <= 1
+    assert np.abs(X - Xo).max() <= 1e-10
+    Xp, vp, _, _ = oracle.acx_dense(H, k, 1e-12, 200)
+    assert np.abs(X - Xp).max() <= 1e-10
+    assert np.abs(v - vp).max() <= 1e-10 * np.abs(H).sum(1).max()
+    assert info["fp64_f_calls"] < oracle.acx_dense(H, k, 1e-12, 200)[2]["f_calls"]
+
+
+def test_mixed_acx_status_codes(cuda):
+    H = oracle.acx_test_matrix(64, 0.06, seed=1)
+    st, _, _, res = run_mixed(cuda, H, 4, 1e-5, 50, 1e-12, 50, handle=False)
+    assert st == 1 and np.isnan(res.tf32_time_sec)
+    st, _, _, _ = run_mixed(cuda, H, 4, 0.0, 50, 1e-12, 50)
+    assert st == 1
+    H[5, 5] = H[2, 2]
+    st, _, _, _ = run_mixed(cuda, H, 4, 1e-5, 50, 1e-12, 50)
+    assert st == 5 and oracle.acx_mixed(H, 4, 1e-5, 50, 1e-12, 50)[3] == 5
