@@ -277,7 +277,7 @@ int ipt_cuda_device_tol_noalloc(const double *d_matrix_col_major, int n, int k, 
  * a per-row scale of the diagonal correction (clamped to [-2, 3]; 1 is the
  * plain preconditioner); IPTBlockOptions.preconditioner = IPT_BLOCK_PRECOND_MLP
  * with mlp_params = the trained parameters enables it.  Every learned step is
- * judged by the FP64 residual and redone with the diagonal correction when
+ * checked against the FP64 residual and redone with the diagonal correction when
  * the largest scaled residual does not drop (IPTBlockReport counts accepted
  * and rejected learned steps).
  *
