@@ -278,10 +278,12 @@ double seconds_since(std::chrono::steady_clock::time_point t)
     return std::chrono::duration<double>(std::chrono::steady_clock::now() - t).count();
 }
 
+// grid-stride kernels: at most eight CTAs per SM
 int grid_cap(size_t count)
 {
     const int b = blocks_for(count);
-    return b < 8 * 152 ? b : 8 * 152;
+    const int cap = 8 * device_sm_count();
+    return b < cap ? b : cap;
 }
 
 // The FP64 ACX loop (acx_cuda.cu:390-620).  From the identity (initial ==
