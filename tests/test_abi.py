@@ -125,3 +125,33 @@ def test_free_result_resets_fields(lib):
     assert res.best_so_far_step == -1
     assert res.pair28_lock_state == b"unknown"
     lib.ipt_cuda_free_result(None)
+
+
+def test_new_entries_reject_bad_arguments_before_device_work(lib):
+    """The block-cluster, ACX and cache entries validate their arguments on
+    the host before any CUDA call (fake device pointers are never touched)."""
+    fake = C.c_void_p(16)
+    it = (C.c_int * 4)()
+    rs = (C.c_double * 4)()
+    for ranges in ([3, 2], [0, 4, 4, 6], [0, 64], [28, 30]):
+        rg = (C.c_int * len(ranges))(*ranges)
+        st = lib.ipt_block_cluster_basis(fake, fake, fake, 30, 10, fake, rg, len(ranges) // 2, 10,
+                                         1e-12, 1.0, fake, it, rs, None)
+        assert st == _lib.IPT_CUDA_INVALID_ARGUMENT, ranges
+    rg = (C.c_int * 2)(0, 1)
+    assert lib.ipt_block_cluster_basis(None, fake, fake, 30, 10, fake, rg, 1, 10, 1e-12, 1.0,
+                                       fake, it, rs, None) == _lib.IPT_CUDA_INVALID_ARGUMENT
+    sing = C.c_int(0)
+    for first, m in ((0, 0), (0, 65), (-1, 2), (29, 2)):
+        assert lib.ipt_block_cluster_update(fake, fake, fake, 30, first, m, 1.0, fake,
+                                            C.byref(sing), None) == _lib.IPT_CUDA_INVALID_ARGUMENT
+    res = _lib.ACXCudaResult()
+    for n, k, tol, mi in ((0, 1, 1e-12, 5), (8, 9, 1e-12, 5), (8, 2, -1.0, 5), (8, 2, 1e-12, 0)):
+        assert lib.acx_cuda_device_tol(fake, n, k, tol, mi, None, C.byref(res)) == 1
+    assert lib.acx_cuda_status_string(5) == b"zero diagonal denominator"
+    mres = _lib.ACXMixedTF32CudaResult()
+    assert lib.acx_mixed_precision_tf32_cuda_device_tol(fake, 8, 2, 1e-5, 10, 1e-12, 10, None,
+                                                        C.byref(mres)) == 1
+    assert mres.tf32_time_sec != mres.tf32_time_sec  # reset to NaN
+    info = _lib.IPTCscCacheInfo()
+    assert lib.ipt_block_csc_cache_info(b"", C.byref(info)) == _lib.IPT_CUDA_INVALID_ARGUMENT
