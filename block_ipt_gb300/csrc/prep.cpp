@@ -889,10 +889,20 @@ IPT_API int ipt_block_prepare_csc(const int *col_ptr, const int *row_ind, const 
     const int st = iptgb::prepare_csc(col_ptr, row_ind, vals, n, nnz, true, &prep,
                                       lift ? k : 0, degeneracy_threshold);
     if (st != IPT_CUDA_SUCCESS) return st;
+    // the prepared CSC: the input arrays themselves when neither the sort nor
+    // a lift changed the matrix (the reference keeps them as given), else the
+    // transpose of the prepared CSR (columns sorted by row, as the reference
+    // rebuilds them)
     std::vector<int> cp, ri;
     std::vector<double> va;
-    iptgb::csc_to_csr(prep.row_ptr.data(), prep.col_ind.data(), prep.vals.data(), n, prep.nnz,
-                      &cp, &ri, &va);
+    if (!prep.permuted && prep.rot_first.empty()) {
+        cp.assign(col_ptr, col_ptr + (size_t)n + 1U);
+        ri.assign(row_ind, row_ind + (size_t)nnz);
+        va.assign(vals, vals + (size_t)nnz);
+    } else {
+        iptgb::csc_to_csr(prep.row_ptr.data(), prep.col_ind.data(), prep.vals.data(), n,
+                          prep.nnz, &cp, &ri, &va);
+    }
     *out_nnz = prep.nnz;
     *rot_count = (int)prep.rot_first.size();
     if (prep.nnz > capacity || *rot_count > rot_capacity ||

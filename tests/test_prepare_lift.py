@@ -141,3 +141,46 @@ def test_non_symmetric_matrices_against_reference(lib):
                     assert np.array_equal(bits(got[key]), bits(ref[key])), (seed, k, key)
                 accepted += 1
     assert rejected >= 3 and accepted >= 6
+
+
+@pytest.mark.skipif(not oracle.ref_available(), reason="oracle/_ref not built here")
+def test_duplicates_zeros_and_unsorted_columns_against_reference(lib):
+    """Inputs with split (duplicate) entries, explicit zeros and shuffled
+    columns, permuted or not: the same prepared arrays as the reference."""
+    ok = 0
+    for seed in range(24):
+        rng = np.random.default_rng(seed)
+        n = 30 + seed % 10
+        _, _, _, H = oracle.cluster_test_matrix(n, seed, [0.01, 0.3, 2.0][seed % 3])
+        P = rng.permutation(n) if seed % 2 else np.arange(n)
+        H = H[np.ix_(P, P)]
+        cp, ri, va = [0], [], []
+        for c in range(n):
+            ents = []
+            for r in range(n):
+                v = H[r, c]
+                if v != 0 or r == c:
+                    if rng.uniform() < 0.2 and r != c:
+                        a = rng.uniform()
+                        ents += [(r, v * a), (r, v * (1 - a))]
+                    else:
+                        ents.append((r, v))
+            if rng.uniform() < 0.3:
+                ents.append((int(rng.integers(0, n)), 0.0))
+            if seed % 4 == 3:
+                rng.shuffle(ents)
+            ri += [e[0] for e in ents]
+            va += [e[1] for e in ents]
+            cp.append(len(ri))
+        cp, ri, va = np.array(cp, np.int32), np.array(ri, np.int32), np.array(va)
+        for k in (1, 3, 6):
+            ref = oracle.ref_prepare_lifted(cp, ri, va, n, k)
+            if isinstance(ref, int):
+                with pytest.raises(Exception):
+                    api.prepare_csc(cp, ri, va, n, k)
+                continue
+            got = api.prepare_csc(cp, ri, va, n, k)
+            for key in KEYS:
+                assert np.array_equal(bits(got[key]), bits(ref[key])), (seed, k, key)
+            ok += 1
+    assert ok >= 15
