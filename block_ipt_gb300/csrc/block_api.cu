@@ -1068,9 +1068,20 @@ int ipt_block_sparse_host_entry(const int *col_ptr, const int *row_ind, const do
     const double coupling_tau = env_double("IPT_BLOCK_CLUSTER_COUPLING_TAU", 0.1);
     const int oversample = adaptive ? 0 : env_int("IPT_BLOCK_CLUSTER_OVERSAMPLE", 0);
     const int target_k = oversample > 0 ? (oversample > n - k ? n : k + oversample) : k;
+    // the reference scans its permuted CSC, merged and sorted even when the
+    // order did not change (ipt_cuda.cu:4568-4575); for a symmetric matrix
+    // the permuted CSC equals the prepared CSR
     ClusterRanges cr;
-    cluster_ranges(prep.row_ptr.data(), prep.col_ind.data(), prep.vals.data(), n, target_k, k,
-                   env_double("IPT_DEGENERACY_THRESHOLD", 0.0), adaptive, coupling_tau, &cr);
+    if (prep.permuted) {
+        cluster_ranges(prep.row_ptr.data(), prep.col_ind.data(), prep.vals.data(), n, target_k, k,
+                       env_double("IPT_DEGENERACY_THRESHOLD", 0.0), adaptive, coupling_tau, &cr);
+    } else {
+        std::vector<int> mcp, mri;
+        std::vector<double> mva;
+        merge_csc_columns(col_ptr, row_ind, vals, n, &mcp, &mri, &mva);
+        cluster_ranges(mcp.data(), mri.data(), mva.data(), n, target_k, k,
+                       env_double("IPT_DEGENERACY_THRESHOLD", 0.0), adaptive, coupling_tau, &cr);
+    }
     int basis_cols = 0;
     for (const auto &r : cr.ranges) {
         basis_cols += r.second - r.first + 1;

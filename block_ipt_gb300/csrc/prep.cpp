@@ -262,6 +262,36 @@ void unpermute_vectors(const PreparedCsr &prep, double *vectors, int k)
     }
 }
 
+// Each column sorted by row, duplicates summed in that order, exact zeros
+// dropped: the reference's permutation step with the identity order
+// (ipt_permute_csc, ipt_preparation.cu:210-262), which its block-cluster
+// preparation always applies (ipt_cuda.cu:4568-4575).
+void merge_csc_columns(const int *col_ptr, const int *row_ind, const double *vals, int n,
+                       std::vector<int> *cp, std::vector<int> *ri, std::vector<double> *va)
+{
+    cp->assign((size_t)n + 1U, 0);
+    ri->clear();
+    va->clear();
+    std::vector<std::pair<int, double>> e;
+    for (int c = 0; c < n; ++c) {
+        e.clear();
+        for (int p = col_ptr[c]; p < col_ptr[c + 1]; ++p) e.emplace_back(row_ind[p], vals[p]);
+        std::sort(e.begin(), e.end(), [](const std::pair<int, double> &x,
+                                         const std::pair<int, double> &y) { return x.first < y.first; });
+        (*cp)[(size_t)c] = (int)ri->size();
+        for (size_t i = 0; i < e.size(); ++i) {
+            const int r = e[i].first;
+            double v = e[i].second;
+            while (i + 1 < e.size() && e[i + 1].first == r) v += e[++i].second;
+            if (v != 0.0) {
+                ri->push_back(r);
+                va->push_back(v);
+            }
+        }
+    }
+    (*cp)[(size_t)n] = (int)ri->size();
+}
+
 // ---- block-cluster ranges ---------------------------------------------------
 // Restated from the reference's degenerate-subspace detection
 // (IPT_C_GPU/src/ipt_preparation.cu:345-644) and the block-cluster
@@ -840,9 +870,10 @@ int lift_degeneracies(std::vector<int> *cp, std::vector<int> *ri, std::vector<do
 #define IPT_API extern "C" __attribute__((visibility("default")))
 
 // Host only: the cluster ranges of the block-cluster path for a symmetric
-// CSC matrix with ascending diagonal.  Returns IPT_CUDA_INVALID_ARGUMENT for
-// invalid input, a cluster wider than the limit (ipt_cuda.cu:4619-4632), or a
-// capacity below the cluster count (*count is set either way).
+// CSC matrix with ascending diagonal (columns merged and sorted first).
+// Returns IPT_CUDA_INVALID_ARGUMENT for invalid input, a cluster wider than
+// the limit (ipt_cuda.cu:4619-4632), or a capacity below the cluster count
+// (*count is set either way).
 IPT_API int ipt_block_cluster_ranges(const int *col_ptr, const int *row_ind, const double *vals,
                                      int n, int nnz, int k, int requested_k,
                                      double degeneracy_threshold, int adaptive,
@@ -855,9 +886,14 @@ IPT_API int ipt_block_cluster_ranges(const int *col_ptr, const int *row_ind, con
         requested_k > k || !iptgb::validate_csc(col_ptr, row_ind, n, nnz)) {
         return IPT_CUDA_INVALID_ARGUMENT;
     }
+    // merged and sorted first, as the reference's block-cluster preparation
+    // always does (a no-op for a prepared matrix)
+    std::vector<int> mcp, mri;
+    std::vector<double> mva;
+    iptgb::merge_csc_columns(col_ptr, row_ind, vals, n, &mcp, &mri, &mva);
     iptgb::ClusterRanges cr;
-    iptgb::cluster_ranges(col_ptr, row_ind, vals, n, k, requested_k, degeneracy_threshold,
-                          adaptive, coupling_tau, &cr);
+    iptgb::cluster_ranges(mcp.data(), mri.data(), mva.data(), n, k, requested_k,
+                          degeneracy_threshold, adaptive, coupling_tau, &cr);
     *count = (int)cr.ranges.size();
     if (limit_hit != nullptr) *limit_hit = cr.limit_hit;
     if (cr.too_large || *count > capacity || ranges == nullptr) {

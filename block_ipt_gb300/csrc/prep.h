@@ -51,6 +51,11 @@ int prepare_csc(const int *col_ptr, const int *row_ind, const double *vals, int 
 // ipt_preparation.cu:1222-1293).
 void unpermute_vectors(const PreparedCsr &prep, double *vectors_col_major, int k);
 
+// Columns sorted by row, duplicates summed, exact zeros dropped (the
+// reference's identity permutation, ipt_preparation.cu:210-262).
+void merge_csc_columns(const int *col_ptr, const int *row_ind, const double *vals, int n,
+                       std::vector<int> *cp, std::vector<int> *ri, std::vector<double> *va);
+
 // CSC -> CSR transpose keeping duplicates and storage order (stable by column).
 void csc_to_csr(const int *col_ptr, const int *row_ind, const double *vals, int n, int nnz,
                 std::vector<int> *row_ptr, std::vector<int> *col_ind, std::vector<double> *out);

@@ -130,7 +130,9 @@ int ipt_block_symmetric_eig(const double *d_T, int m, double *d_w, double *d_Z, 
 /* ---- block-cluster path (the reference's IPT_BLOCK_CLUSTER) --------------
  *
  * Host only.  Cluster ranges of a symmetric CSC matrix whose diagonal is
- * ascending (the prepared, diagonal-sorted matrix): the targets 0..k-1 are
+ * ascending (the prepared, diagonal-sorted matrix; its columns are first
+ * sorted by row with duplicates summed and zeros dropped, as the reference's
+ * block-cluster preparation does, ipt_cuda.cu:4568-4575): the targets 0..k-1 are
  * joined with the rows whose diagonal gap is numerically zero or small
  * against their coupling, as the reference's degenerate-subspace detection
  * (IPT_C_GPU/src/ipt_preparation.cu:502-644, environment knobs

@@ -126,3 +126,42 @@ def test_oracle_against_reference_code_sweep(monkeypatch):
                     err = np.abs(X[:, off:off + m] - Xr).max() / max(1.0, np.abs(Xr).max())
                     assert err <= 1e-11 and itr == its[c]
                     off += m
+
+
+@pytest.mark.skipif(not oracle.ref_available(), reason="oracle/_ref not built here")
+def test_ranges_with_duplicates_and_unsorted_columns_against_reference(lib, monkeypatch):
+    """Split (duplicate) entries and shuffled columns: the library merges the
+    columns first, as the reference's block-cluster preparation does, and
+    finds the reference's clusters."""
+    checked = 0
+    for seed in range(16):
+        rng = np.random.default_rng(seed)
+        n = 30 + seed % 10
+        _, _, _, H = oracle.cluster_test_matrix(n, seed, [0.01, 0.3, 2.0][seed % 3])
+        cp, ri, va = [0], [], []
+        for c in range(n):
+            ents = []
+            for r in range(n):
+                v = H[r, c]
+                if v != 0 or r == c:
+                    if rng.uniform() < 0.2 and r != c:
+                        a = rng.uniform()
+                        ents += [(r, v * a), (r, v * (1 - a))]
+                    else:
+                        ents.append((r, v))
+            if seed % 4 == 3:
+                rng.shuffle(ents)
+            ri += [e[0] for e in ents]
+            va += [e[1] for e in ents]
+            cp.append(len(ri))
+        cp, ri, va = np.array(cp, np.int32), np.array(ri, np.int32), np.array(va)
+        for k in (3, 6):
+            for adaptive in (0, 1):
+                monkeypatch.setenv("IPT_BLOCK_CLUSTER_ADAPTIVE", str(adaptive))
+                ref = oracle.ref_cluster_prepare(cp, ri, va, n, k)
+                if isinstance(ref, int):
+                    continue
+                got, lim = api.cluster_ranges(cp, ri, va, n, k, adaptive=bool(adaptive))
+                assert got == ref[0] and lim == ref[2], (seed, k, adaptive)
+                checked += 1
+    assert checked >= 40
