@@ -92,6 +92,24 @@ def dist_env():
     return world, rank, local
 
 
+def max_over_ranks(value, world, device="cpu"):
+    """The N > 1 rule of the timed region: every rank's time, then the
+    maximum over ranks (all ranks receive it).  World size 1 needs no
+    process group."""
+    import torch
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    if world > 1:
+        import torch.distributed as dist
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        dist.barrier()
+    return float(t.item())
+
+
+def replica_seed(seed, rank):
+    """Replicas only: each rank solves its own instance of the workload."""
+    return seed + rank
+
+
 def plain_products(n, k, seed):
     try:
         with open(PRODUCTS_FILE) as f:
@@ -623,7 +641,7 @@ def run_ours(args):
     n, k = args.n, args.k
     # one independent instance per rank ("replicas only": the dense solve is
     # not sharded), seeded by rank
-    H, _ = workloads.dense_config1(n, seed=args.seed + rank)
+    H, _ = workloads.dense_config1(n, seed=replica_seed(args.seed, rank))
     H = np.asfortranarray(H)
     hnorm = float(np.abs(H).sum(axis=1).max())
     H_pinned = torch.from_numpy(H.T.copy()).pin_memory()  # row-major view of H^T = col-major H
@@ -682,12 +700,7 @@ def run_ours(args):
     prof = profile_snapshot(lib)
     if args.trace and rank == 0:
         write_trace(args.trace, api, torch, lambda: solve(args.precision), flush)
-    ms_mine = statistics.mean(times)
-    t = torch.tensor([ms_mine], device=dev)
-    if world > 1:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        dist.barrier()
-    ms = float(t.item())
+    ms = max_over_ranks(statistics.mean(times), world, dev)
 
     # eigenvalues against LAPACK (once, outside the timed region)
     vals = dv.cpu().numpy()
