@@ -306,13 +306,14 @@ static int cluster_grid_x(int n, int C, int teams)
     return std::max(1, std::min((n + teams - 1) / teams, want));
 }
 
+// The opt-in shared-memory size is an attribute of the current device's
+// context, so it is set at every launch that needs more than 48 KB (a cheap
+// host call; no cache shared between threads or devices).
 static int set_cluster_smem(size_t bytes)
 {
-    static size_t set = 0;
-    if (bytes > 48 * 1024 && bytes > set) {
+    if (bytes > 48 * 1024) {
         IPTGB_CUDA(cudaFuncSetAttribute(cluster_update_kernel,
                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
-        set = bytes;
     }
     return IPT_CUDA_SUCCESS;
 }
