@@ -307,13 +307,20 @@ static int cluster_grid_x(int n, int C, int teams)
 }
 
 // The opt-in shared-memory size is an attribute of the current device's
-// context, so it is set at every launch that needs more than 48 KB (a cheap
-// host call; no cache shared between threads or devices).
+// context: every launch that needs more than 48 KB sets it (a cheap host
+// call), always to the largest size any width up to 64 needs, so launches
+// from several threads or on several devices never undercut each other.
 static int set_cluster_smem(size_t bytes)
 {
+    static const size_t largest = [] {
+        size_t mx = 0;
+        for (int m = 1; m <= kClusterMaxWidth; ++m) mx = std::max(mx, cluster_update_smem(m));
+        return mx;
+    }();
     if (bytes > 48 * 1024) {
         IPTGB_CUDA(cudaFuncSetAttribute(cluster_update_kernel,
-                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)std::max(bytes, largest)));
     }
     return IPT_CUDA_SUCCESS;
 }
