@@ -15,14 +15,16 @@ is checked in FP64 (torch DGEMM residual, LAPACK eigenvalues).
   plain_fp64   the same code with an FP64 IPT stage (ms), and the speed-up
   roofline     dominant kernel of the timed region, from live CUDA-event
                timings of every launch (ipt_block_profile_*)
-  cpu_baseline the oracle restatement of the reference's CPU IPT, one
-               iteration timed on all host cores and scaled by the block
-               products plain IPT needs on this matrix
+  cpu_baseline the oracle restatement of the reference's CPU IPT: one
+               complete solve of this matrix on all host cores, stopped at
+               the scaled residual 1e-8; beside it one iteration on one core
+               and LAPACK dsyevd (scipy, all host cores)
   fci_config3  FCI-like CSR (n = 63,504, k = 16), plain and learned Davidson
   batched_config2      512 dense instances, persistent kernel under a graph
   matrix_free_config4  matrix-free FCI-like sigma, 14 orbitals (n = 11.8M)
 
-`--impl reference` times the reference's CPU path alone (rank 0 only).
+`--impl reference` times the reference's CPU path alone (rank 0 only): every
+step is one complete tolerance-stopped plain-IPT solve of the same matrix.
 """
 import argparse
 import ctypes as C
@@ -40,10 +42,10 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "time to k eigenpairs at ||r||<=1e-8, mixed+learned vs plain FP64 IPT, 1xGB300"
-WORKLOAD = ("dense symmetric n=8192 k=32, d_i=i/8+U(0,0.1), h_ij~N(0,0.02^2)exp(-|i-j|/256), "
-            "seed 0; FP16 tcgen05 IPT + refinement against FP64-accurate (double-FP32) defects, "
-            "FP64-accurate (double-FP32) CholQR/Rayleigh-Ritz, to scaled residual 1e-8")
-PRODUCTS_FILE = os.path.join(ROOT, "oracle", "plain_ipt_products.json")
+METHOD = ("FP16 tcgen05 IPT + refinement against FP64-accurate defects, FP64-accurate "
+          "CholQR/Rayleigh-Ritz, to scaled residual 1e-8")
+REFERENCE_PATH = ("the reference's CPU plain IPT (runtests.cu:98-174 semantics, oracle port) "
+                  "stopped at the scaled residual 1e-8")
 MEASURED_PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
 # DRAM bytes (read + write) per launch from one ncu capture of each kernel on
 # this workload (profiles/dense64_partial_fp64_n8192_k32.md,
@@ -110,52 +112,79 @@ def replica_seed(seed, rank):
     return seed + rank
 
 
-def plain_products(n, k, seed):
-    try:
-        with open(PRODUCTS_FILE) as f:
-            tab = json.load(f)
-        ent = tab.get("dense_config1_n%d_k%d_seed%d" % (n, k, seed))
-        if ent and ent["products"] > 0:
-            return int(ent["products"])
-    except OSError:
-        pass
-    return None
+def workload_name(n, k, seed):
+    return ("dense symmetric n=%d k=%d, d_i=i/8+U(0,0.1), h_ij~N(0,0.02^2)exp(-|i-j|/256), seed %d"
+            % (n, k, seed))
+
+
+def bench_config(args):
+    """The workload description both arms print (identical dictionaries)."""
+    return {"workload": workload_name(args.n, args.k, args.seed), "n": args.n, "k": args.k,
+            "seed": args.seed, "target": "k lowest eigenpairs, scaled residual <= 1e-8",
+            "l2": "256 MB buffer written between timed GPU steps (inputs also > L2)",
+            "parallelism": "replicas only (one instance per GPU)"}
 
 
 # ---------------------------------------------------------------------------
 # CPU baseline: the reference's CPU IPT (oracle port or oracle/_ref)
 # ---------------------------------------------------------------------------
-def cpu_iteration_seconds(H, k, reps=1):
-    """Seconds per plain-IPT iteration of the reference CPU path on this host.
-    Uses the reference's own compiled code where it was built for this host,
-    else the oracle restatement on all host cores."""
+def cpu_solve(H, k):
+    """One complete plain-IPT solve of H by the reference's CPU algorithm
+    (the oracle's restatement of runtests.cu:98-174, on all host cores),
+    iterated until the scaled eigen-residual of every column is <= 1e-8.
+    Returns (ms, block products, final scaled residual)."""
     from oracle import oracle
-    kind = "port"
-    cores = oracle.num_threads()
-    fn = None
-    if oracle.ref_available():
-        try:
-            L = oracle.ref_lib("dense")
-            n = H.shape[0]
-            X = np.zeros((n, k), order="F")
-            v = np.zeros(k)
+    t0 = time.perf_counter()
+    cnt, res = oracle.products_to_residual(H, k, 2000, 1e-8)
+    ms = (time.perf_counter() - t0) * 1e3
+    if cnt <= 0:
+        raise RuntimeError("CPU plain IPT did not reach the scaled residual 1e-8")
+    return ms, cnt, res
 
-            def fn(it):
-                L.ref_ipt_cpu_reference(C.c_void_p(H.ctypes.data), n, k, it,
-                                        C.c_void_p(X.ctypes.data), C.c_void_p(v.ctypes.data))
-            kind = "reference"
-            cores = 1
-        except OSError:
-            fn = None
-    if fn is None:
-        def fn(it):
-            oracle.ipt_dense(H, k, it)
-    times = []
-    for _ in range(reps):
+
+def cpu_one_core_iteration(H, k):
+    """One plain-IPT iteration of the same CPU code on a single host core:
+    one block product and the update, plus the product that returns the
+    eigenvalues (ms)."""
+    from oracle import oracle
+    cores = oracle.num_threads()
+    oracle.set_num_threads(1)
+    try:
         t0 = time.perf_counter()
-        fn(1)
-        times.append(time.perf_counter() - t0)
-    return statistics.median(times), kind, cores
+        oracle.ipt_dense(H, k, 1)
+        return (time.perf_counter() - t0) * 1e3
+    finally:
+        oracle.set_num_threads(cores)
+
+
+def blas_threads():
+    try:
+        import threadpoolctl
+        info = threadpoolctl.threadpool_info()
+        if info:
+            return max(int(x.get("num_threads", 0)) for x in info)
+    except ImportError:
+        pass
+    for var in ("OPENBLAS_NUM_THREADS", "OMP_NUM_THREADS"):
+        if os.environ.get(var):
+            return int(os.environ[var])
+    return os.cpu_count()
+
+
+def dsyevd_leg(H, k):
+    """LAPACK dsyevd (scipy, divide and conquer, all eigenpairs) on the
+    same matrix, timed once; returns the report and the k lowest values."""
+    from oracle import oracle
+    t0 = time.perf_counter()
+    w, _ = oracle.dsyevd_lowest(H, k)
+    ms = (time.perf_counter() - t0) * 1e3
+    return {"ms": ms, "threads": blas_threads(),
+            "routine": "scipy.linalg.lapack.dsyevd, compute_v=1 (full spectrum)"}, w
+
+
+def cpu_sample_text(n, k, cnt):
+    return ("one complete solve per step: plain IPT from the identity block (n=%d, k=%d) until "
+            "every scaled residual is <= 1e-8 (%d block products)" % (n, k, cnt))
 
 
 def run_reference(args):
@@ -167,28 +196,22 @@ def run_reference(args):
     oracle.build()
     H, _ = workloads.dense_config1(args.n, seed=args.seed)
     H = np.asfortranarray(H)
-    prods = plain_products(args.n, args.k, args.seed)
-    if prods is None:
-        prods, _ = oracle.products_to_residual(H, args.k, 2000, 1e-8)
     for _ in range(args.warmup):
-        cpu_iteration_seconds(H, args.k)
-    samples = []
-    kind, cores = "port", 1
+        cpu_solve(H, args.k)
+    samples, cnt, res = [], 0, None
     for _ in range(args.steps):
-        t, kind, cores = cpu_iteration_seconds(H, args.k)
-        samples.append(t * prods * 1e3)
+        ms, cnt, res = cpu_solve(H, args.k)
+        samples.append(ms)
     value = statistics.mean(samples)
+    cores = oracle.num_threads()
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "ms",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": value,
         "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic",
-        "config": {"workload": WORKLOAD, "n": args.n, "k": args.k, "seed": args.seed,
-                   "path": "reference CPU plain IPT (runtests.cu:98-174 semantics)"},
-        "cpu_baseline": {"value": value, "unit": "ms", "cores": cores, "kind": kind,
-                         "sample": "1 plain-IPT iteration per step (n=%d, k=%d), scaled by the "
-                                   "%d block products plain IPT needs to reach the scaled "
-                                   "residual 1e-8" % (args.n, args.k, prods)},
+        "data": "synthetic", "config": bench_config(args), "path": REFERENCE_PATH,
+        "cpu_baseline": {"value": value, "unit": "ms", "cores": cores, "kind": "port",
+                         "sample": cpu_sample_text(args.n, args.k, cnt),
+                         "final_scaled_residual": res},
         "e2e": {"value": value, "unit": "ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -702,12 +725,13 @@ def run_ours(args):
         write_trace(args.trace, api, torch, lambda: solve(args.precision), flush)
     ms = max_over_ranks(statistics.mean(times), world, dev)
 
-    # eigenvalues against LAPACK (once, outside the timed region)
+    # eigenvalues against LAPACK dsyevd (once, outside the timed region; its
+    # time is reported beside the CPU baseline)
     vals = dv.cpu().numpy()
     dlambda = None
+    dsyevd = None
     if not args.no_lapack and rank == 0:
-        from oracle import oracle
-        w, _ = oracle.eigh_lowest(H, k)
+        dsyevd, w = dsyevd_leg(H, k)
         dlambda = float(np.abs(vals - w).max() / hnorm)
 
     # plain FP64 IPT path of the same code (FP64 IPT steps to the same
@@ -826,13 +850,14 @@ def run_ours(args):
 
     cpu = None
     if not args.no_cpu and rank == 0:
-        prods = plain_products(n, k, args.seed)
-        sec, kind, cores = cpu_iteration_seconds(H, k)
-        if prods:
-            cpu = {"value": sec * prods * 1e3, "unit": "ms", "cores": cores, "kind": kind,
-                   "sample": "1 plain-IPT iteration (n=%d, k=%d) timed, scaled by the %d block "
-                             "products plain IPT needs to reach the scaled residual 1e-8"
-                             % (n, k, prods)}
+        from oracle import oracle
+        cpu_ms, cnt, cres = cpu_solve(H, k)
+        cpu = {"value": cpu_ms, "unit": "ms", "cores": oracle.num_threads(), "kind": "port",
+               "sample": cpu_sample_text(n, k, cnt), "final_scaled_residual": cres,
+               "one_core": {"ms": cpu_one_core_iteration(H, k), "cores": 1,
+                            "sample": "one plain-IPT iteration (one block product and the "
+                                      "update) plus the eigenvalue product, n=%d k=%d" % (n, k)},
+               "dsyevd": dsyevd}
 
     if rank == 0:
         line = {
@@ -840,11 +865,11 @@ def run_ours(args):
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": False,
             "scaling": "weak", "vs_baseline": None, "dtype": "%s+f64" % args.precision,
             "data": "synthetic",
-            "config": {"workload": WORKLOAD, "n": n, "k": k, "seed": args.seed,
-                       "precision": args.precision,
-                       "learned_preconditioner": "acts on Davidson steps; this workload converges in the mixed refinement, so it is timed on the FCI-like workload (fci_config3.learned)",
-                       "l2": "256 MB buffer written between timed steps (inputs also > L2)",
-                       "parallelism": "replicas only (one instance per GPU)"},
+            "config": bench_config(args),
+            "method": METHOD.replace("FP16", args.precision.upper()),
+            "learned_preconditioner": "acts on Davidson steps; this workload converges in the "
+                                      "mixed refinement, so it is timed on the FCI-like "
+                                      "workload (fci_config3.learned)",
             "e2e": ({"value": e2e_ms, "unit": "ms", "h2d_bytes_per_step": 8 * n * n,
                      "d2h_bytes_per_step": 8 * n * k + 8 * k} if e2e_ms is not None else None),
             "gpu_launches": launches,

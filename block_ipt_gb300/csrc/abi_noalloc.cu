@@ -13,17 +13,17 @@
 // library holds until the process exits.
 //
 // Host code may not use the array's name as a device address; the address
-// is looked up with cudaGetSymbolAddress once per device, with that device
-// current, on the first call made on it.  That first call should therefore
-// come before any stream capture.  All calls share the one array and it
-// keeps the last call's contents: the parts that must start at zero are
-// cleared on every call, and calls that overlap on the GPU (two streams, two
-// threads, one device) race on the scratch and must be serialised by the
-// caller.
+// is looked up with cudaGetSymbolAddress on every call, with the caller's
+// device current (a cheap host call, and it stays valid after a
+// cudaDeviceReset reloads the module).  Every iteration reads the two norms
+// back and synchronises the stream, so the entry must never be called inside
+// a stream capture.  All calls share the one array and it keeps the last
+// call's contents: the parts that must start at zero are cleared on every
+// call, and calls that overlap on the GPU (two streams, two threads, one
+// device) race on the scratch and must be serialised by the caller.
 #include <math.h>
 
 #include <climits>
-#include <mutex>
 
 #include "common.cuh"
 #include "kernels.cuh"
@@ -35,34 +35,22 @@ namespace {
 
 constexpr size_t kNoallocScratchBytes = 16u << 20;  // 16 MiB
 constexpr size_t kNoallocDoubles = kNoallocScratchBytes / sizeof(double);
-constexpr int kNoallocMaxDevices = 64;
 
 __device__ __align__(256) double g_noalloc_scratch[kNoallocDoubles];
 
-std::mutex g_setup_mu;
-double *g_scratch_addr[kNoallocMaxDevices] = {};
-
-// Device address of the scratch array for the current device (set-up on the
-// first call per device).
+// Device address of the scratch array for the current device, looked up on
+// every call: a cached address would dangle once cudaDeviceReset has
+// reloaded the module.
 int scratch_for_current_device(double **out)
 {
-    int dev = 0;
-    IPTGB_CUDA(cudaGetDevice(&dev));
-    if (dev < 0 || dev >= kNoallocMaxDevices) {
-        return IPT_CUDA_INVALID_ARGUMENT;
+    void *p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || p == nullptr) {
+        fprintf(stderr, "ipt_gb300: cudaGetSymbolAddress(no-alloc scratch) failed: %s\n",
+                cudaGetErrorString(e));
+        return IPT_CUDA_CUDA_ERROR;
     }
-    std::lock_guard<std::mutex> lock(g_setup_mu);
-    if (g_scratch_addr[dev] == nullptr) {
-        void *p = nullptr;
-        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess || p == nullptr) {
-            fprintf(stderr, "ipt_gb300: cudaGetSymbolAddress(no-alloc scratch) failed: %s\n",
-                    cudaGetErrorString(e));
-            return IPT_CUDA_CUDA_ERROR;
-        }
-        g_scratch_addr[dev] = static_cast<double *>(p);
-    }
-    *out = g_scratch_addr[dev];
+    *out = static_cast<double *>(p);
     return IPT_CUDA_SUCCESS;
 }
 

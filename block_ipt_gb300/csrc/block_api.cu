@@ -1041,20 +1041,19 @@ int ipt_block_sparse_host_entry(const int *col_ptr, const int *row_ind, const do
     }
     PreparedCsr prep;
     IPTGB_CHECK(prepare_csc(col_ptr, row_ind, vals, n, nnz, true, &prep));
-    // symmetry check on the transposed arrays, O(nnz)
-    {
-        std::vector<int> rp, ci;
-        std::vector<double> cv;
-        csc_to_csr(prep.row_ptr.data(), prep.col_ind.data(), prep.vals.data(), n, prep.nnz, &rp,
-                   &ci, &cv);
-        for (size_t p = 0; p < cv.size(); ++p) {
-            const double a = cv[p], b = prep.vals[p];
-            if (ci[p] != prep.col_ind[p] ||
-                fabs(a - b) > 1e-12 * std::max(1.0, std::max(fabs(a), fabs(b)))) {
-                ipt_cuda_free_result(result);
-                return IPT_CUDA_INVALID_ARGUMENT;
-            }
-        }
+    // The reference's block-cluster preparation always merges and sorts the
+    // columns (duplicates summed, exact zeros dropped; ipt_cuda.cu:4568-4575)
+    // and then requires a real symmetric matrix (4586-4595).  A permuted
+    // preparation is merged already; otherwise merge the caller's arrays.
+    std::vector<int> mcp, mri;
+    std::vector<double> mva;
+    if (!prep.permuted) merge_csc_columns(col_ptr, row_ind, vals, n, &mcp, &mri, &mva);
+    const int *m_ptr = prep.permuted ? prep.row_ptr.data() : mcp.data();
+    const int *m_idx = prep.permuted ? prep.col_ind.data() : mri.data();
+    const double *m_val = prep.permuted ? prep.vals.data() : mva.data();
+    if (!merged_is_symmetric(m_ptr, m_idx, m_val, n)) {
+        ipt_cuda_free_result(result);
+        return IPT_CUDA_INVALID_ARGUMENT;
     }
     IPTBlockOptions opt;
     fill_default_options(&opt);
@@ -1072,16 +1071,8 @@ int ipt_block_sparse_host_entry(const int *col_ptr, const int *row_ind, const do
     // order did not change (ipt_cuda.cu:4568-4575); for a symmetric matrix
     // the permuted CSC equals the prepared CSR
     ClusterRanges cr;
-    if (prep.permuted) {
-        cluster_ranges(prep.row_ptr.data(), prep.col_ind.data(), prep.vals.data(), n, target_k, k,
-                       env_double("IPT_DEGENERACY_THRESHOLD", 0.0), adaptive, coupling_tau, &cr);
-    } else {
-        std::vector<int> mcp, mri;
-        std::vector<double> mva;
-        merge_csc_columns(col_ptr, row_ind, vals, n, &mcp, &mri, &mva);
-        cluster_ranges(mcp.data(), mri.data(), mva.data(), n, target_k, k,
-                       env_double("IPT_DEGENERACY_THRESHOLD", 0.0), adaptive, coupling_tau, &cr);
-    }
+    cluster_ranges(m_ptr, m_idx, m_val, n, target_k, k,
+                   env_double("IPT_DEGENERACY_THRESHOLD", 0.0), adaptive, coupling_tau, &cr);
     int basis_cols = 0;
     for (const auto &r : cr.ranges) {
         basis_cols += r.second - r.first + 1;

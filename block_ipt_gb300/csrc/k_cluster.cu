@@ -308,8 +308,10 @@ static int cluster_grid_x(int n, int C, int teams)
 
 // The opt-in shared-memory size is an attribute of the current device's
 // context: every launch that needs more than 48 KB sets it (a cheap host
-// call), always to the largest size any width up to 64 needs, so launches
-// from several threads or on several devices never undercut each other.
+// call), to the largest size any width up to 64 needs, clamped to what the
+// current device allows, so launches from several threads never undercut
+// each other; only a launch that itself needs more than the device allows
+// fails.
 static int set_cluster_smem(size_t bytes)
 {
     static const size_t largest = [] {
@@ -318,9 +320,17 @@ static int set_cluster_smem(size_t bytes)
         return mx;
     }();
     if (bytes > 48 * 1024) {
+        int dev = 0, optin = 0;
+        IPTGB_CUDA(cudaGetDevice(&dev));
+        IPTGB_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+        if (bytes > (size_t)optin) {
+            fprintf(stderr, "ipt_gb300: block-cluster update needs %zu bytes of shared memory, "
+                            "the device allows %d\n", bytes, optin);
+            return IPT_CUDA_INVALID_ARGUMENT;
+        }
         IPTGB_CUDA(cudaFuncSetAttribute(cluster_update_kernel,
                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        (int)std::max(bytes, largest)));
+                                        (int)std::min(std::max(bytes, largest), (size_t)optin)));
     }
     return IPT_CUDA_SUCCESS;
 }

@@ -292,6 +292,31 @@ void merge_csc_columns(const int *col_ptr, const int *row_ind, const double *val
     (*cp)[(size_t)n] = (int)ri->size();
 }
 
+// Real-symmetry test of a merged compressed matrix (every column - or row -
+// sorted, no duplicates): each stored entry (r, c) against the value stored
+// at (c, r), 0 when absent, within 1e-12 * max(1, |a|, |b|).  The test is
+// the reference's (ipt_csc_is_hermitian_real, ipt_preparation.cu:860-883,
+// which scans the merged, permuted CSC of its block-cluster preparation);
+// the lookup is a binary search in the sorted column instead of a scan.  The
+// test reads the same whether the arrays are CSC or CSR, since a matrix is
+// symmetric exactly when its transpose is.
+bool merged_is_symmetric(const int *ptr, const int *idx, const double *vals, int n)
+{
+    for (int c = 0; c < n; ++c) {
+        for (int p = ptr[c]; p < ptr[c + 1]; ++p) {
+            const int r = idx[p];
+            const double a = vals[p];
+            double b = 0.0;
+            const int *lo = idx + ptr[r], *hi = idx + ptr[r + 1];
+            const int *it = std::lower_bound(lo, hi, c);
+            if (it != hi && *it == c) b = vals[it - idx];
+            const double scale = std::max(1.0, std::max(fabs(a), fabs(b)));
+            if (fabs(a - b) > 1e-12 * scale) return false;
+        }
+    }
+    return true;
+}
+
 // ---- block-cluster ranges ---------------------------------------------------
 // Restated from the reference's degenerate-subspace detection
 // (IPT_C_GPU/src/ipt_preparation.cu:345-644) and the block-cluster

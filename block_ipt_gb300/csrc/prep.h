@@ -56,6 +56,10 @@ void unpermute_vectors(const PreparedCsr &prep, double *vectors_col_major, int k
 void merge_csc_columns(const int *col_ptr, const int *row_ind, const double *vals, int n,
                        std::vector<int> *cp, std::vector<int> *ri, std::vector<double> *va);
 
+// Real-symmetry test of merged compressed arrays (sorted, no duplicates),
+// by value lookup within 1e-12 * max(1, |a|, |b|) (ipt_preparation.cu:860-883).
+bool merged_is_symmetric(const int *ptr, const int *idx, const double *vals, int n);
+
 // CSC -> CSR transpose keeping duplicates and storage order (stable by column).
 void csc_to_csr(const int *col_ptr, const int *row_ind, const double *vals, int n, int nnz,
                 std::vector<int> *row_ptr, std::vector<int> *col_ind, std::vector<double> *out);

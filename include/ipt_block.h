@@ -262,10 +262,10 @@ int ipt_block_cholesky_inverse(const double *d_G, int m, double *d_Rinv, int *sh
  * loading the library keeps until exit, so n*k is limited to about 1.0e6
  * (2*n*k + n + n*k/128 doubles); larger sizes return
  * IPT_CUDA_INVALID_ARGUMENT with a message on stderr.  Runs on `stream`
- * (cudaStream_t, NULL = legacy default stream).  The first call on a device
- * looks up the scratch address and should come before any stream capture.
- * Calls share the scratch: calls that overlap on the GPU race and must be
- * serialised by the caller. */
+ * (cudaStream_t, NULL = legacy default stream).  Every iteration reads two
+ * norms back and synchronises the stream, so the entry must never be called
+ * inside a stream capture.  Calls share the scratch: calls that overlap on
+ * the GPU race and must be serialised by the caller. */
 int ipt_cuda_device_tol_noalloc(const double *d_matrix_col_major, int n, int k, double tol,
                                 int maxiter, void *stream, double *d_vectors, double *d_values,
                                 int *iterations_done_out, double *fixed_point_residual_out);

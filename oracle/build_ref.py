@@ -16,15 +16,24 @@ libraries:
                                 ref_prepare_sparse_csc_lifted
 
 Nothing from the reference is copied into the repository; the outputs are
-git-ignored.  The reference path only exists in the build container, so the
-recipe is skipped (returns False) where it is absent.
+git-ignored.  The reference tree is found through the IPT_REFERENCE_ROOT
+environment variable (the IPT_C_GPU directory), or the first command-line
+argument, falling back to /root/reference/IPT_C_GPU; where it is absent the
+recipe is skipped (returns False).
 """
 import os
 import shutil
 import subprocess
 import sys
 
-REF_ROOT = "/root/reference/IPT_C_GPU"
+DEFAULT_REF_ROOT = "/root/reference/IPT_C_GPU"
+
+
+def ref_root(argv=None):
+    """The reference's IPT_C_GPU directory: argument, environment, default."""
+    if argv:
+        return argv[0]
+    return os.environ.get("IPT_REFERENCE_ROOT", DEFAULT_REF_ROOT)
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "_ref")
 
@@ -204,9 +213,10 @@ extern "C" int ref_block_cluster_solve_basis(const int *col_ptr, const int *row_
 '''
 
 
-def build(verbose=False):
+def build(verbose=False, root=None):
     """Build oracle/_ref/*.so from the reference sources; False if absent."""
-    if not os.path.isdir(REF_ROOT):
+    root = root or ref_root()
+    if not os.path.isdir(root):
         return False
     nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
     os.makedirs(OUT, exist_ok=True)
@@ -215,7 +225,7 @@ def build(verbose=False):
         src = os.path.join(OUT, "ref_%s_wrap.cu" % name)
         lib = os.path.join(OUT, "libref_%s.so" % name)
         with open(src, "w") as f:
-            f.write(text % {"ref": REF_ROOT})
+            f.write(text % {"ref": root})
         cmd = [nvcc, "-O2", "-std=c++14", "-shared", "-Xcompiler", "-fPIC",
                "-Xcompiler", "-ffp-contract=off", "-w",
                "-gencode", "arch=compute_103a,code=sm_103a",
@@ -234,4 +244,4 @@ def build(verbose=False):
 
 
 if __name__ == "__main__":
-    sys.exit(0 if build(verbose=True) else 1)
+    sys.exit(0 if build(verbose=True, root=ref_root(sys.argv[1:])) else 1)

@@ -465,6 +465,16 @@ ORACLE_API int oracle_num_threads(void)
 #endif
 }
 
+/* Thread count of the following oracle calls (a timed single-core sample). */
+ORACLE_API void oracle_set_num_threads(int threads)
+{
+#ifdef _OPENMP
+    omp_set_num_threads(threads > 0 ? threads : 1);
+#else
+    (void)threads;
+#endif
+}
+
 /* Plain IPT with the eigen-residual read off every step: for the block X
  * entering a step, r_j = H x_j - lambda_j x_j with lambda_j = (H X)_jj equals
  * (d_j - d_i)(F(X) - X)_ij entrywise (zero on the target row).  Returns the

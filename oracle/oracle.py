@@ -60,6 +60,7 @@ def lib():
         L.oracle_ipt_dense_products_to_residual.restype = i
         L.oracle_ipt_dense_products_to_residual.argtypes = [vp, i, i, i, d, d, vp]
         L.oracle_num_threads.restype = i
+        L.oracle_set_num_threads.argtypes = [i]
         L.oracle_acx_mixed.restype = i
         L.oracle_acx_mixed.argtypes = [vp, i, i, d, i, d, i, vp, vp, vp, vp]
         L.oracle_acx_dense.restype = i
@@ -151,6 +152,11 @@ def products_to_residual(H, k, maxiter, res_tol=1e-8):
 
 def num_threads():
     return lib().oracle_num_threads()
+
+
+def set_num_threads(threads):
+    """Thread count of the oracle's following calls."""
+    lib().oracle_set_num_threads(int(threads))
 
 
 def max_relative_residual(H, X, v):

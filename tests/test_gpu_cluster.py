@@ -174,3 +174,63 @@ def test_block_cluster_entry_singular_block(cuda, monkeypatch):
     assert oracle.cluster_basis(cp, ri, va, np.diag(H).copy(), ranges, 200, 1e-12)[3] != 0
     with pytest.raises(Exception):
         api.ipt_cuda_sparse_csc_tol(cp, ri, va, n, k, 1e-12, 200)
+
+
+def one_sided_storage(cp, ri, va, n, seed):
+    """The same matrix stored unevenly: some entries above the diagonal split
+    into two duplicates (their mirror stays one entry), explicit zeros added
+    on one side only, a 1e-15 entry whose mirror is absent, and shuffled
+    columns."""
+    rng = np.random.default_rng(seed)
+    ncp, nri, nva = [0], [], []
+    for c in range(n):
+        ents = []
+        for p in range(cp[c], cp[c + 1]):
+            r, v = int(ri[p]), float(va[p])
+            if r < c and rng.uniform() < 0.3:
+                a = rng.uniform()
+                ents += [(r, v * a), (r, v - v * a)]
+            else:
+                ents.append((r, v))
+        if c + 2 < n and rng.uniform() < 0.2:
+            ents.append((c + 2, 0.0))
+        if c == n // 2:
+            ents.append((n - 1, 1e-15))
+        rng.shuffle(ents)
+        nri += [e[0] for e in ents]
+        nva += [e[1] for e in ents]
+        ncp.append(len(nri))
+    return np.array(ncp, np.int32), np.array(nri, np.int32), np.array(nva)
+
+
+@pytest.mark.parametrize("adaptive", ["0", "1"])
+def test_block_cluster_entry_uneven_storage(cuda, monkeypatch, adaptive):
+    """A symmetric matrix stored with one-sided duplicates and explicit zeros
+    passes the entry's symmetry check (the reference merges the columns and
+    compares values by lookup, ipt_preparation.cu:860-883) and gives the
+    same eigenpairs as its clean storage, whether or not the diagonal needs
+    sorting."""
+    monkeypatch.setenv("IPT_BLOCK_CLUSTER", "1")
+    monkeypatch.setenv("IPT_BLOCK_CLUSTER_ADAPTIVE", adaptive)
+    monkeypatch.setenv("IPT_DAVIDSON_ENRICH", "1")
+    monkeypatch.setenv("IPT_DAVIDSON_STEPS", "40")
+    n, k = 90, 6
+    cp, ri, va, H = oracle.cluster_test_matrix(n, 5, 0.3)
+    for shuffle_diag in (False, True):
+        if shuffle_diag:
+            # a diagonal out of ascending order takes the permuted preparation
+            perm = np.random.default_rng(1).permutation(n)
+            Hp = H[perm][:, perm]
+            cols = [np.nonzero(Hp[:, c])[0] for c in range(n)]
+            cp = np.cumsum([0] + [len(x) for x in cols]).astype(np.int32)
+            ri = np.concatenate(cols).astype(np.int32)
+            va = np.concatenate([Hp[x, c] for c, x in enumerate(cols)])
+            Href = Hp
+        else:
+            Href = H
+        ucp, uri, uva = one_sided_storage(cp, ri, va, n, 7)
+        X, v, info = api.ipt_cuda_sparse_csc_tol(ucp, uri, uva, n, k, 1e-12, 200)
+        w, _ = oracle.eigh_lowest(Href, k)
+        scale = np.abs(Href).sum(1).max()
+        np.testing.assert_allclose(v, w, atol=1e-9 * scale)
+        assert np.abs(Href @ X - X * v).max() <= 1e-7 * scale
