@@ -133,6 +133,17 @@ class _MixedResult(C.Structure):
     ]
 
 
+class IPTRayleighMixedCudaDeviceResult(C.Structure):
+    _fields_ = [
+        ("n", _i), ("k", _i), ("tf32_iterations", _i), ("fp64_iterations", _i),
+        ("tf32_time_sec", _d), ("orthogonalize_time_sec", _d),
+        ("rayleigh_transform_time_sec", _d), ("fp64_time_sec", _d),
+        ("backtransform_time_sec", _d), ("total_time_sec", _d),
+        ("tf32_fixed_point_residual", _d), ("fp64_fixed_point_residual", _d),
+        ("d_vectors", C.c_void_p), ("d_values", C.c_void_p),
+    ]
+
+
 class IPTBlockOptions(C.Structure):
     _fields_ = [
         ("ipt_precision", _i), ("oversample", _i), ("ipt_maxiter", _i), ("ipt_tol", _d),
@@ -239,6 +250,11 @@ SIGNATURES = [
     ("ipt_mixed_precision_cuda_free_device_result", None, [C.POINTER(_MixedResult)]),
     ("ipt_mixed_precision_fp32_cuda_free_device_result", None, [C.POINTER(_MixedResult)]),
     ("ipt_mixed_precision_tf32_cuda_free_device_result", None, [C.POINTER(_MixedResult)]),
+    ("ipt_rayleigh_mixed_tf32_cuda_device_tol", _i, [_vp, _i, _i, _d, _i, _d, _i, _vp,
+                                                     C.POINTER(IPTRayleighMixedCudaDeviceResult)]),
+    ("ipt_rayleigh_mixed_cuda_free_device_result", None,
+     [C.POINTER(IPTRayleighMixedCudaDeviceResult)]),
+    ("ipt_block_householder_signs", _i, [_vp, _i, _i, _vp]),
     ("ipt_block_default_options", None, [C.POINTER(IPTBlockOptions)]),
     ("ipt_block_cholesky_inverse", _i, [_vp, _i, _vp, C.POINTER(C.c_int), _i, _vp]),
     ("ipt_block_split_double", _i, [_vp, C.c_longlong, _vp, _vp, _vp]),

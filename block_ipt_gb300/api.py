@@ -473,3 +473,35 @@ def write_csc_cache(path, col_ptr, row_ind, values, diagonal, magic="IPTGENC1",
     _check(_lib.load().ipt_block_csc_cache_write(os.fsencode(path), C.byref(info), _ptr(cp),
                                                  _ptr(ri), _ptr(va), _ptr(dg)),
            "ipt_block_csc_cache_write")
+
+
+# ---- Rayleigh-mixed (device buffers) ---------------------------------------
+def householder_signs(top, n):
+    """Column signs of a LAPACK Householder QR from the top k x k block of
+    an orthonormal CholQR factor (ipt_block_householder_signs)."""
+    T = _f64(top)
+    k = T.shape[0]
+    out = np.zeros(k)
+    st = _lib.load().ipt_block_householder_signs(_ptr(T), k, n, _ptr(out))
+    if st != _lib.IPT_CUDA_SUCCESS:
+        raise IPTError(st, "ipt_block_householder_signs")
+    return out
+
+
+def rayleigh_mixed_tf32_device(d_matrix_ptr, n, k, tf32_tol, tf32_maxiter, fp64_tol,
+                               fp64_maxiter, handle):
+    """ipt_rayleigh_mixed_tf32_cuda_device_tol on a device matrix; returns the
+    result struct (device vectors/values owned by the caller, released by
+    free_rayleigh_result)."""
+    res = _lib.IPTRayleighMixedCudaDeviceResult()
+    st = _lib.load().ipt_rayleigh_mixed_tf32_cuda_device_tol(
+        C.c_void_p(d_matrix_ptr), n, k, float(tf32_tol), int(tf32_maxiter), float(fp64_tol),
+        int(fp64_maxiter), C.c_void_p(handle), C.byref(res))
+    if st != _lib.IPT_CUDA_SUCCESS:
+        raise IPTError(st, "ipt_rayleigh_mixed_tf32_cuda_device_tol")
+    return res
+
+
+def free_rayleigh_result(res):
+    _lib.load().ipt_rayleigh_mixed_cuda_free_device_result(C.byref(res))
+

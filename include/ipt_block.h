@@ -418,6 +418,17 @@ int ipt_block_split_double(const double *d_in, long long count, float *d_hi, flo
                            void *stream);
 int ipt_block_split_double_host(const double *in, long long count, float *hi, float *lo);
 
+/* ---- Householder column signs -------------------------------------------- */
+
+/* Part of the orthonormalisation step of ipt_rayleigh_mixed_tf32_cuda_device_tol,
+ * which replaces the reference's Householder QR (cusolverDnDgeqrf/Dorgqr,
+ * IPT_C_GPU/src/mixed_precision/ipt_rayleigh_mixed_cuda.cu:141-254) by
+ * CholQR.  Given the top k x k block (column-major) of an orthonormal
+ * n x k factor Q_c whose R has a positive diagonal, signs[j] is the sign of
+ * the j-th diagonal entry of R in a LAPACK Householder QR of the same
+ * block, so that Q_c diag(signs) is the Householder factor.  Host-only. */
+int ipt_block_householder_signs(const double *top, int k, int n, double *signs);
+
 /* ---- instrumentation ---------------------------------------------------- */
 
 /* Number of kernels this library has launched in the calling process. */

@@ -263,6 +263,26 @@ typedef struct {
     double *d_values;
 } IPTMixedTF32CudaDeviceResult;
 
+/* Rayleigh-mixed device result
+ * (IPT_C_GPU/src/mixed_precision/ipt_rayleigh_mixed_cuda.cu:19-34; the same
+ * struct in IPT_C_GPU/mixed/ipt_rayleigh_mixed_mpqr_cuda.cu:19-34). */
+typedef struct {
+    int n;
+    int k;
+    int tf32_iterations;
+    int fp64_iterations;
+    double tf32_time_sec;
+    double orthogonalize_time_sec;
+    double rayleigh_transform_time_sec;
+    double fp64_time_sec;
+    double backtransform_time_sec;
+    double total_time_sec;
+    double tf32_fixed_point_residual;
+    double fp64_fixed_point_residual;
+    double *d_vectors;
+    double *d_values;
+} IPTRayleighMixedCudaDeviceResult;
+
 /* --- utilities: IPT_C_GPU/src/ipt_cuda.cu:262-264 ------------------------ */
 const char *ipt_cuda_status_string(int status);
 void ipt_cuda_free_result(IPTCudaResult *result);
@@ -340,6 +360,22 @@ int ipt_mixed_precision_tf32_cuda_device_tol(
     const double *d_matrix_col_major, int n, int k, double tf32_tol,
     int tf32_maxiter, double fp64_tol, int fp64_maxiter,
     cublasHandle_t handle, IPTMixedTF32CudaDeviceResult *result);
+
+/* --- Rayleigh-mixed, device buffers:
+ *     IPT_C_GPU/src/mixed_precision/ipt_rayleigh_mixed_cuda.cu:36-41 (driver
+ *     :274-400; mixed-CholQR twin IPT_C_GPU/mixed/ipt_rayleigh_mixed_mpqr_cuda.cu:406-538).
+ * TF32 IPT of the k lowest diagonal positions to tf32_tol (tensor cores),
+ * orthonormal basis Q of that block with the column signs of a Householder
+ * QR, B = sym(Q^T H Q), FP64 IPT on the k x k matrix B to fp64_tol, and the
+ * vectors Q Z (n x k, column-major, Z with Z_jj = 1) and values (B Z)_jj in
+ * cudaMalloc'd buffers that ipt_rayleigh_mixed_cuda_free_device_result
+ * releases.  Runs on the handle's stream. ------------------------------- */
+void ipt_rayleigh_mixed_cuda_free_device_result(
+    IPTRayleighMixedCudaDeviceResult *result);
+int ipt_rayleigh_mixed_tf32_cuda_device_tol(
+    const double *d_matrix_col_major, int n, int k, double tf32_tol,
+    int tf32_maxiter, double fp64_tol, int fp64_maxiter,
+    cublasHandle_t handle, IPTRayleighMixedCudaDeviceResult *result);
 
 #ifdef __cplusplus
 }

@@ -218,6 +218,23 @@ def dsyevd_lowest(H, k):
     return w[:k], V[:, :k]
 
 
+def rayleigh_mixed(H, k, lowp_tol, lowp_maxiter, fp64_tol, fp64_maxiter):
+    """The reference's Rayleigh-mixed driver
+    (IPT_C_GPU/src/mixed_precision/ipt_rayleigh_mixed_cuda.cu:274-400) with an
+    FP64 first stage in place of its TF32 one: plain IPT to lowp_tol, the
+    Householder QR of that block (LAPACK dgeqrf/dorgqr through numpy, the
+    convention of its cusolverDnDgeqrf/Dorgqr, :141-254), B = sym(Q^T H Q)
+    (:84-106, :338-343), plain IPT on the k x k matrix B to fp64_tol (:358)
+    and the vectors Q Z (:370).  Returns (vectors, values, Q, fp64 iterations,
+    fp64 fixed-point residual)."""
+    X0, _, _, _ = ipt_dense(H, k, lowp_maxiter, tol=lowp_tol, use_tol=True)
+    Q, _ = np.linalg.qr(X0)
+    B = Q.T @ (np.asarray(H, dtype=np.float64) @ Q)
+    B = 0.5 * (B + B.T)
+    Z, vals, it, fp = ipt_dense(B, k, fp64_maxiter, tol=fp64_tol, use_tol=True)
+    return Q @ Z, vals, Q, it, fp
+
+
 def cholqr(X):
     """CholQR: X = Q R with R from the FP64 Gram matrix."""
     G = X.T @ X
