@@ -783,35 +783,12 @@ def run_ours(args):
         assert rep.converged == 1
     e2e_ms = statistics.mean(e2e) if e2e else None
 
-    # roofline of the dominant kernel of the timed region
-    dom = max(prof.items(), key=lambda kv: kv[1][0])
-    name, (tot_ms, cnt) = dom
+    # roofline of the dominant kernel of the timed region (the larger of the
+    # low-precision product and the FP64-accurate product, by total time)
     steps = args.steps
     avg_rep = reports[-1]
     with open(MEASURED_PEAKS) as f:
         peaks = json.load(f)
-    roofline = None
-    fp64_peak = C.c_double(0.0)
-    lib.ipt_block_measure_fp64_peak(C.byref(fp64_peak))
-    FP64_PEAK_TFLOPS = fp64_peak.value
-    if name == "fp64_product":
-        terms = n * n * sum(r["fp64_matvecs"] for r in prof_reports)
-        fp32_peak = C.c_double(0.0)
-        lib.ipt_block_measure_fp32_peak(C.byref(fp32_peak))
-        FP32_PEAK_TFLOPS = fp32_peak.value
-        # the mixed solve forms its FP64-accurate products in double-FP32
-        # arithmetic: 12 FP32-pipe instructions per term (k_df64.cu)
-        achieved = 12.0 * terms / (tot_ms * 1e-3) / 1e12
-        peak_ops = FP32_PEAK_TFLOPS / 2.0
-        roofline = {"kernel": "df64_partial_kernel (double-FP32 FP64-accurate product, split-K)",
-                    "bound": "fp32_pipe", "achieved": achieved, "peak": peak_ops,
-                    "unit": "T FP32-pipe instructions/s", "frac": achieved / peak_ops,
-                    "fp64_equivalent_tflops": 2.0 * terms / (tot_ms * 1e-3) / 1e12,
-                    "traffic": NCU_TRAFFIC.get(("df64_partial", n, k, args.precision)),
-                    "traffic_unit": "bytes per launch (ncu dram__bytes_read.sum + write.sum)",
-                    "peak_source": "ipt_block_measure_fp32_peak (FFMA throughput kernel, run "
-                                   "live; MEASURED_PEAKS.json has no FP32 entry), as instructions/s",
-                    "launches": cnt, "avg_launch_ms": tot_ms / max(1, cnt)}
     lp_ms, lp_cnt = prof["lowp_product"]
     ldp = (n + 63) // 64 * 64
     esize = 2 if args.precision in ("fp16", "bf16") else 4
@@ -824,9 +801,31 @@ def run_ours(args):
                      "traffic_unit": "bytes per launch (ncu dram__bytes_read.sum + write.sum)",
                      "launches": lp_cnt,
                      "avg_launch_ms": lp_ms / max(1, lp_cnt),
-                     "algorithmic_bytes_per_launch": lp_bytes}
-    if roofline is None:
-        roofline = roofline_lowp
+                     "algorithmic_bytes_per_launch": lp_bytes,
+                     "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)"}
+    # the FP64-accurate products of the refinement (k columns each): six FP16
+    # digit slices of Delta streamed once per product, the X slices written
+    # and read, X read and H X written (k_oz.cu); bound: HBM.  Its timer spans
+    # the X split, the tensor-core product and the finish kernel.
+    fp_ms, fp_cnt = prof["fp64_product"]
+    cp = (k + 15) // 16 * 16
+    acc_bytes = 12 * n * ldp + 24 * cp * ldp + 16 * n * k
+    acc_ach = acc_bytes / (fp_ms / max(1, fp_cnt) * 1e-3) / 1e9 if fp_cnt else None
+    # MMA work: slice s times B rows (6 - s) cp, over every (row, K) pair
+    mma_flops = 2.0 * ((n + 127) // 128 * 128) * ldp * sum((6 - s) * cp for s in range(6))
+    roofline_accurate = {
+        "kernel": "oz_product_kernel (FP64-accurate product: 6+6 FP16 digit slices, tcgen05 "
+                  "+ TMA, persistent)",
+        "bound": "hbm", "achieved": acc_ach, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+        "frac": (acc_ach / peaks["hbm_gbs"]) if acc_ach else None,
+        "traffic": NCU_TRAFFIC.get(("oz_product", n, k, args.precision)),
+        "traffic_unit": "bytes per launch (ncu dram__bytes_read.sum + write.sum)",
+        "launches": fp_cnt, "avg_launch_ms": fp_ms / max(1, fp_cnt),
+        "algorithmic_bytes_per_launch": acc_bytes,
+        "tensor_tflops": (mma_flops / (fp_ms / max(1, fp_cnt) * 1e-3) / 1e12) if fp_cnt else None,
+        "tensor_peak_tflops": peaks["bf16_tflops"],
+        "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)"}
+    roofline = roofline_accurate if fp_ms > lp_ms else roofline_lowp
 
     fci = None
     mlp_params = None
@@ -875,6 +874,7 @@ def run_ours(args):
             "gpu_launches": launches,
             "roofline": roofline,
             "roofline_lowp": roofline_lowp,
+            "roofline_accurate": roofline_accurate,
             "cpu_baseline": cpu,
             "clocks": clocks,
             "plain_fp64_ms": plain,

@@ -255,6 +255,8 @@ SIGNATURES = [
     ("ipt_rayleigh_mixed_cuda_free_device_result", None,
      [C.POINTER(IPTRayleighMixedCudaDeviceResult)]),
     ("ipt_block_householder_signs", _i, [_vp, _i, _i, _vp]),
+    ("ipt_block_accurate_product", _i, [_vp, _i, _vp, _i, _vp, _vp]),
+    ("ipt_block_accurate_split_host", _i, [_vp, C.c_longlong, _d, C.POINTER(_i), _vp]),
     ("ipt_block_default_options", None, [C.POINTER(IPTBlockOptions)]),
     ("ipt_block_cholesky_inverse", _i, [_vp, _i, _vp, C.POINTER(C.c_int), _i, _vp]),
     ("ipt_block_split_double", _i, [_vp, C.c_longlong, _vp, _vp, _vp]),

@@ -18,6 +18,7 @@
 #include "fpconv.cuh"
 #include "ipt_plain.h"
 #include "lowp.h"
+#include "oz_product.h"
 #include "prep.h"
 #include "reduce.cuh"
 
@@ -30,6 +31,9 @@ namespace iptgb {
 // ---------------------------------------------------------------------------
 struct DenseApply final : Fp64Apply {
     const double *H = nullptr;
+    // optional split-operand product on the tensor cores (k_oz.cu), the
+    // default of the mixed solve
+    OzProduct *oz = nullptr;
     // optional double-FP32 copy of H: products in double-float arithmetic on
     // the FP32 pipe (k_df64.cu) instead of FP64 FMAs
     const float *Hh = nullptr;
@@ -41,6 +45,10 @@ struct DenseApply final : Fp64Apply {
     DeviceBuffer<float> Xs;
     int apply(const double *V, int c, double *AV) override
     {
+        if (oz != nullptr) {
+            KernelTimerScope timer(kProfFp64Product, s);
+            return oz->apply(V, n, c, AV, n);
+        }
         const int S = Hh != nullptr ? df64_split_for(n, c, sms) : dense64_split_for(n, c, sms);
         const size_t need = (size_t)S * (size_t)n * (size_t)c;
         if (P.count < need) {
@@ -459,13 +467,25 @@ int dense_block_device(const double *dH_in, int n, int k, const IPTBlockOptions 
                                                            : kLowpTF32;
     double hnorm = 0.0, maxabs_off = 0.0;
     unsigned long long descents = 0;
-    // The mixed-precision solve forms its FP64-accurate products in
-    // double-FP32 arithmetic (one split of H per solve); the plain FP64
-    // path keeps FP64 FMAs throughout.
+    // The mixed-precision solve forms its FP64-accurate products on the
+    // tensor cores from digit slices of Delta (one split per solve, k_oz.cu);
+    // tuning knob IPT_GB300_ACCURATE_PRODUCT = df selects double-FP32
+    // arithmetic on the FP32 pipe instead, fp64 (or IPT_GB300_FP64_DFMA=1)
+    // FP64 FMAs.  The plain FP64 path keeps FP64 FMAs throughout.
+    const char *ap = getenv("IPT_GB300_ACCURATE_PRODUCT");
+    const bool want_fp64 = env_flag("IPT_GB300_FP64_DFMA", 0) ||
+                           (ap != nullptr && strcmp(ap, "fp64") == 0);
+    const bool want_df = ap != nullptr && strcmp(ap, "df") == 0;
+    const bool use_oz = lowp_mode && !want_fp64 && !want_df;
     DeviceBuffer<float> Hsplit;
+    OzDelta ozd;
+    OzProduct ozp;
     const size_t mat = (size_t)n * n;
-    if (lowp_mode && !env_flag("IPT_GB300_FP64_DFMA", 0)) {
+    if (lowp_mode && want_df) {
         IPTGB_CHECK(Hsplit.alloc(2 * mat, s));
+    }
+    if (use_oz) {
+        IPTGB_CHECK(ozd.init_storage(n, s));
     }
     std::unique_ptr<LowpDenseOperator> lowp;
     int st = IPT_CUDA_SUCCESS;
@@ -486,6 +506,10 @@ int dense_block_device(const double *dH_in, int n, int k, const IPTBlockOptions 
         su.fused_copy = host_src != nullptr ? const_cast<double *>(dH_in) : nullptr;
         su.diag = d.ptr;
         su.stats = stats.ptr;
+        if (use_oz) {
+            su.oz = ozd.A.ptr;
+            su.oz_rowexp = ozd.rowexp.ptr;
+        }
         lowp.reset(make_lowp_dense_operator(dH_in, n, kind, s, &st, &su));
         if (lowp == nullptr) {
             return st != IPT_CUDA_SUCCESS ? st : IPT_CUDA_INVALID_ARGUMENT;
@@ -548,6 +572,13 @@ int dense_block_device(const double *dH_in, int n, int k, const IPTBlockOptions 
     if (Hsplit.ptr != nullptr) {
         apply.Hh = Hsplit.ptr;
         apply.Hl = Hsplit.ptr + mat;
+    }
+    if (use_oz) {
+        // the fused pass wrote the slices of the (unpermuted) matrix; any
+        // other path splits the matrix the solve iterates on
+        if (!fused) IPTGB_CHECK(ozd.split_from(dH, n, s));
+        IPTGB_CHECK(ozp.bind(&ozd, d.ptr, s));
+        apply.oz = &ozp;
     }
     if (lowp_mode && fused) {
         trace_mark("dense:operator_done", s);

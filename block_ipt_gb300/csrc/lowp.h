@@ -1,6 +1,7 @@
 // lowp.h - low-precision (tensor-core) dense IPT operator (internal).
 #pragma once
 
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 #include "ipt_plain.h"
@@ -74,6 +75,12 @@ struct LowpDenseSetup {
     double *diag = nullptr;         // n entries
     DenseStats *stats = nullptr;    // device, zeroed by the caller
     bool fused_done = false;        // out
+    // fused setup only: the digit slices of Delta for the FP64-accurate
+    // tensor-core product ([kOzSlices][n][ldp] FP16, ldp = n rounded up to
+    // 64) and their row exponents (oz.cuh)
+    __half *oz = nullptr;
+    int *oz_rowexp = nullptr;
+    bool oz_done = false;           // out
 };
 constexpr int kLowpColsumChunk = 2048;
 LowpDenseOperator *make_lowp_dense_operator(const double *dH, int n, int kind, cudaStream_t s,

@@ -418,6 +418,31 @@ int ipt_block_split_double(const double *d_in, long long count, float *d_hi, flo
                            void *stream);
 int ipt_block_split_double_host(const double *in, long long count, float *hi, float *lo);
 
+/* ---- FP64-accurate product on the tensor cores ------------------------------ */
+
+/* Y = H X for a column-major n x n H and n x c X (device buffers, ld n),
+ * the FP64-accurate block product that replaces the reference's FP64
+ * cublasDgemm (IPT_C_GPU/src/mixed_precision/ipt_mixed_precision_cuda.cu:
+ * 917,958) in this library's mixed solve.  The diagonal of H is applied in
+ * FP64; H minus its diagonal runs on the FP16 tensor cores by an error-free
+ * split of both operands into six 8-bit digit slices with one power-of-two
+ * scale per row of H and per column of X (Ozaki, Ogita, Oishi and Rump,
+ * Numer. Algorithms 59 (2012); the fixed-point form of Mukunoki et al., ISC
+ * 2020).  The error of an entry is below about 2^-46 times
+ * max_l |H_il| max_l |X_lc| times the number of terms, plus the rounding of
+ * |H_ii X_ic|.  The solver splits H once per solve; this entry splits it on
+ * every call (for checking and one-off products).  Runs on `stream`
+ * (cudaStream_t, NULL = legacy default stream) and synchronises it. */
+int ipt_block_accurate_product(const double *d_H, int n, const double *d_X, int c,
+                               double *d_Y, void *stream);
+
+/* The split of the product above on the host, for checking: the exponent e
+ * with max_abs < 2^e (*exponent_out; 0 when max_abs is 0, INT_MAX for a
+ * non-finite max_abs) and the six digits of round(v 2^(48 - e)) in balanced
+ * base 256 (digits_out[6 i + s], s = 0 most significant) of every value. */
+int ipt_block_accurate_split_host(const double *values, long long count, double max_abs,
+                                  int *exponent_out, int *digits_out);
+
 /* ---- Householder column signs -------------------------------------------- */
 
 /* Part of the orthonormalisation step of ipt_rayleigh_mixed_tf32_cuda_device_tol,

@@ -235,6 +235,101 @@ def rayleigh_mixed(H, k, lowp_tol, lowp_maxiter, fp64_tol, fp64_maxiter):
     return Q @ Z, vals, Q, it, fp
 
 
+# ---- split-operand FP64-accurate product ------------------------------------
+# Restatement of the library's error-free split (block_ipt_gb300/csrc/oz.cuh),
+# itself the fixed-point form of Ozaki, Ogita, Oishi and Rump (Numer.
+# Algorithms 59, 2012): checker only.
+OZ_SLICES = 6
+OZ_NONFINITE = 0x7FFFFFFF
+
+
+def accurate_exponent(max_abs):
+    """Smallest e with |max_abs| < 2^e (0 for 0, OZ_NONFINITE for Inf/NaN)."""
+    b = int(np.array([max_abs], dtype=np.float64).view(np.uint64)[0]) & 0x7FFFFFFFFFFFFFFF
+    if b == 0:
+        return 0
+    E = b >> 52
+    if E == 2047:
+        return OZ_NONFINITE
+    if E == 0:
+        return b.bit_length() + 0 - 1074
+    return E - 1022
+
+
+def accurate_fixed(values, e):
+    """round(v 2^(48 - e)) (half away from zero) as int64; 0 for non-finite."""
+    v = np.ascontiguousarray(values, dtype=np.float64).ravel()
+    out = np.zeros(v.size, dtype=np.int64)
+    if e == OZ_NONFINITE:
+        return out
+    for idx, b in enumerate(v.view(np.uint64).tolist()):
+        neg = b >> 63
+        b &= 0x7FFFFFFFFFFFFFFF
+        E = b >> 52
+        if E == 2047 or b == 0:
+            continue
+        if E == 0:
+            M, x = b, -1074
+        else:
+            M, x = (b & 0xFFFFFFFFFFFFF) | (1 << 52), E - 1075
+        sh = e - 48 - x
+        if sh >= 60:
+            q = 0
+        elif sh > 0:
+            q = (M >> sh) + ((M >> (sh - 1)) & 1)
+        else:
+            q = M << (-sh)
+        out[idx] = -q if neg else q
+    return out
+
+
+def accurate_digits(q):
+    """Balanced base-256 digits [count, 6] of fixed-point values (s = 0 most
+    significant; digit 0 in [-256, 256], the others in [-128, 127])."""
+    q = np.array(q, dtype=np.int64)
+    d = np.zeros((q.size, OZ_SLICES), dtype=np.int64)
+    for s in range(OZ_SLICES - 1, 0, -1):
+        r = ((q + 128) & 255) - 128
+        d[:, s] = r
+        q = (q - r) >> 8
+    d[:, 0] = q
+    return d
+
+
+def accurate_product_emulated(H, X):
+    """The split-operand product as the library defines it, in exact
+    integer arithmetic rounded once at the end: Delta = H - diag(H) split
+    per row, X per column, the digit pairs of levels 0..5 summed exactly,
+    plus diag(H) X in FP64."""
+    H = np.asarray(H, dtype=np.float64)
+    X = np.asarray(X, dtype=np.float64)
+    n, c = H.shape[0], X.shape[1]
+    D = H.copy()
+    np.fill_diagonal(D, 0.0)
+    er = [accurate_exponent(np.abs(D[i]).max()) for i in range(n)]
+    fc = [accurate_exponent(np.abs(X[:, j]).max()) for j in range(c)]
+    A = np.stack([accurate_digits(accurate_fixed(D[i], er[i])) for i in range(n)])  # n, n, 6
+    B = np.stack([accurate_digits(accurate_fixed(X[:, j], fc[j])) for j in range(c)])  # c, n, 6
+    levels = [np.zeros((n, c)) for _ in range(OZ_SLICES)]
+    for s in range(OZ_SLICES):
+        for t in range(OZ_SLICES - s):
+            # digit products < 2^16, sums over n < 2^53: exact in FP64
+            levels[s + t] += A[:, :, s].astype(np.float64) @ B[:, :, t].T.astype(np.float64)
+    Y = np.empty((n, c))
+    d = np.diag(H)
+    for i in range(n):
+        for j in range(c):
+            if er[i] == OZ_NONFINITE or fc[j] == OZ_NONFINITE:
+                Y[i, j] = np.nan
+                continue
+            V = 0
+            for l in range(OZ_SLICES):
+                V += int(levels[l][i, j]) << (8 * (OZ_SLICES - 1 - l))
+            y = float(np.ldexp(float(V), er[i] + fc[j] - 16 - 8 * (OZ_SLICES - 1)))
+            Y[i, j] = y + d[i] * X[i, j]
+    return Y
+
+
 def cholqr(X):
     """CholQR: X = Q R with R from the FP64 Gram matrix."""
     G = X.T @ X
