@@ -501,7 +501,7 @@ def learned_section(args, torch, dev, stream, flush, solve, opt, e0, e1, plain_t
     held = learned.device_csr(torch, 8, 4, 4, 9, device=dev)
     rows = torch.empty((1_500_000, learned.ROW), dtype=torch.float32, device=dev)
     got = learned.collect(torch, held, 16, rows, 0)
-    loss_plain, loss_mlp = learned.correction_losses(torch, params, rows, got)
+    loss_plain, loss_neumann, loss_mlp = learned.correction_losses(torch, params, rows, got)
     del rows
     opt.preconditioner = 1
     opt.mlp_params = C.c_void_p(params.data_ptr())
@@ -519,11 +519,13 @@ def learned_section(args, torch, dev, stream, flush, solve, opt, e0, e1, plain_t
     return {"ms": statistics.mean(times), "plain_ms": statistics.mean(plain_times),
             "steps": rep["davidson_steps"], "plain_steps": plain_rep["davidson_steps"],
             "fp64_matvecs": rep["fp64_matvecs"], "plain_fp64_matvecs": plain_rep["fp64_matvecs"],
+            "precond_matvecs": rep["precond_matvecs"],
             "converged": rep["converged"], "max_scaled_residual": rep["max_scaled_residual"],
             "mlp_steps_accepted": rep["mlp_steps_accepted"],
             "mlp_steps_rejected": rep["mlp_steps_rejected"],
             "train_s": train_s, "train_rows": info["rows_total"],
-            "heldout_correction_error": {"plain": loss_plain, "learned": loss_mlp,
+            "heldout_correction_error": {"plain": loss_plain, "two_term_neumann": loss_neumann,
+                                         "learned": loss_mlp,
                                          "instance": "8 orbitals 4a/4b seed 9"},
             "_params": params}
 
@@ -645,6 +647,7 @@ def fci_free_section(args, torch, dev, mlp_params=None):
                      "max_scaled_residual": rep["max_scaled_residual"],
                      "mlp_steps_accepted": rep["mlp_steps_accepted"],
                      "mlp_steps_rejected": rep["mlp_steps_rejected"],
+                     "precond_matvecs": rep["precond_matvecs"],
                      "lowest": dv.cpu().numpy()[:3].tolist()}
     return out
 

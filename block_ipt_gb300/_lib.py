@@ -162,7 +162,7 @@ class IPTBlockReport(C.Structure):
         ("ipt_fixed_point_residual", _d), ("max_scaled_residual", _d),
         ("matrix_norm_inf", _d), ("ipt_ms", _d), ("rayleigh_ritz_ms", _d),
         ("davidson_ms", _d), ("total_ms", _d), ("mlp_steps_accepted", _i),
-        ("mlp_steps_rejected", _i),
+        ("mlp_steps_rejected", _i), ("precond_matvecs", C.c_longlong),
     ]
 
     def as_dict(self):
@@ -203,6 +203,18 @@ class ACXCudaResult(C.Structure):
                 ("iteration_time_sec", C.c_double), ("finalization_time_sec", C.c_double),
                 ("max_residual", C.c_double), ("fixed_point_residual", C.c_double),
                 ("d_vectors", C.c_void_p), ("d_values", C.c_void_p)]
+
+
+class ACXRayleighMixedTF32CudaResult(C.Structure):
+    _fields_ = [
+        ("n", _i), ("k", _i), ("tf32_iterations", _i), ("fp64_iterations", _i),
+        ("tf32_f_calls", _i), ("fp64_f_calls", _i), ("tf32_converged", _i),
+        ("fp64_converged", _i), ("tf32_time_sec", _d), ("orthogonalize_time_sec", _d),
+        ("rayleigh_transform_time_sec", _d), ("fp64_time_sec", _d),
+        ("finalization_time_sec", _d), ("backtransform_time_sec", _d), ("total_time_sec", _d),
+        ("tf32_fixed_point_residual", _d), ("fp64_fixed_point_residual", _d),
+        ("fp64_max_residual", _d), ("d_vectors", C.c_void_p), ("d_values", C.c_void_p),
+    ]
 
 
 class ACXMixedTF32CudaResult(C.Structure):
@@ -272,6 +284,12 @@ SIGNATURES = [
                                                       _i, _vp,
                                                       C.POINTER(ACXMixedTF32CudaResult)]),
     ("acx_cuda_device_tol", _i, [_vp, _i, _i, C.c_double, _i, _vp, C.POINTER(ACXCudaResult)]),
+    ("acx_rayleigh_mixed_tf32_cuda_reset_result", None,
+     [C.POINTER(ACXRayleighMixedTF32CudaResult)]),
+    ("acx_rayleigh_mixed_tf32_cuda_free_result", None,
+     [C.POINTER(ACXRayleighMixedTF32CudaResult)]),
+    ("acx_rayleigh_mixed_tf32_cuda_device_tol", _i, [_vp, _i, _i, _d, _i, _d, _i, _vp,
+                                                     C.POINTER(ACXRayleighMixedTF32CudaResult)]),
     ("ipt_block_csc_cache_info", _i, [C.c_char_p, C.POINTER(IPTCscCacheInfo)]),
     ("ipt_block_csc_cache_read", _i, [C.c_char_p, _vp, _vp, _vp, _vp, _i, _i,
                                       C.POINTER(IPTCscCacheInfo)]),

@@ -41,6 +41,7 @@
 #include "common.cuh"
 #include "ipt_plain.h"
 #include "lowp.h"
+#include "rayleigh.h"
 
 #define IPT_API extern "C" __attribute__((visibility("default")))
 
@@ -137,6 +138,64 @@ int cholqr_fp64(BlockOps &ops, const double *B, int n, int k, double *dst, doubl
     return h == 0 ? IPT_CUDA_SUCCESS : IPT_CUDA_INVALID_ARGUMENT;
 }
 
+}  // namespace
+
+namespace iptgb {
+
+// Q = the orthonormal basis of X0 (n x k) with the column signs of LAPACK's
+// Householder QR: CholQR2 in FP64, then the signs from the top k x k block.
+// X0 is overwritten.
+int householder_basis(BlockOps &ops, double *X0, int n, int k, double *Q, cudaStream_t s)
+{
+    DeviceBuffer<double> G, Rinv, sg;
+    DeviceBuffer<int> idx, st;
+    IPTGB_CHECK(G.alloc((size_t)k * k, s));
+    IPTGB_CHECK(Rinv.alloc((size_t)k * k, s));
+    IPTGB_CHECK(st.alloc(1, s));
+    IPTGB_CHECK(cholqr_fp64(ops, X0, n, k, Q, G.ptr, Rinv.ptr, st.ptr, s));
+    IPTGB_CHECK(cholqr_fp64(ops, Q, n, k, X0, G.ptr, Rinv.ptr, st.ptr, s));
+    std::vector<double> top((size_t)k * k);
+    IPTGB_CUDA(cudaMemcpy2DAsync(top.data(), (size_t)k * sizeof(double), X0,
+                                 (size_t)n * sizeof(double), (size_t)k * sizeof(double), (size_t)k,
+                                 cudaMemcpyDeviceToHost, s));
+    IPTGB_CUDA(cudaStreamSynchronize(s));
+    std::vector<double> signs;
+    householder_signs(top, k, n, &signs);
+    std::vector<int> id((size_t)k);
+    for (int j = 0; j < k; ++j) id[(size_t)j] = j;
+    IPTGB_CHECK(sg.alloc((size_t)k, s));
+    IPTGB_CHECK(idx.alloc((size_t)k, s));
+    IPTGB_CUDA(cudaMemcpyAsync(sg.ptr, signs.data(), (size_t)k * sizeof(double),
+                               cudaMemcpyHostToDevice, s));
+    IPTGB_CUDA(cudaMemcpyAsync(idx.ptr, id.data(), (size_t)k * sizeof(int),
+                               cudaMemcpyHostToDevice, s));
+    IPTGB_CHECK(ops.gather_columns(X0, n, idx.ptr, sg.ptr, n, k, Q, n));
+    // the host vectors must outlive the asynchronous copies
+    IPTGB_CUDA(cudaStreamSynchronize(s));
+    return IPT_CUDA_SUCCESS;
+}
+
+// B = (Q^T H Q + (Q^T H Q)^T) / 2 in FP64 (k x k), H column-major n x n.
+int projected_matrix(BlockOps &ops, const double *dH, int n, const double *Q, int k, double *B,
+                     cudaStream_t s)
+{
+    const size_t elems = (size_t)n * k;
+    DeviceBuffer<double> AQ, P;
+    IPTGB_CHECK(AQ.alloc(elems, s));
+    const int S = dense64_split_for(n, k, ops.sms);
+    IPTGB_CHECK(P.alloc((size_t)S * elems, s));
+    IPTGB_CHECK(launch_dense64_partial(dH, n, n, Q, n, k, P.ptr, S, s));
+    IPTGB_CHECK(launch_sum_partials(P.ptr, S, elems, AQ.ptr, s));
+    IPTGB_CHECK(ops.gram(Q, n, k, AQ.ptr, n, k, n, B, k));
+    symmetrize_kernel<<<(k * k + 255) / 256, 256, 0, s>>>(B, k);
+    IPTGB_LAUNCH();
+    return IPT_CUDA_SUCCESS;
+}
+
+}  // namespace iptgb
+
+namespace {
+
 int rayleigh_run(const double *dH, int n, int k, double tf32_tol, int tf32_maxiter,
                  double fp64_tol, int fp64_maxiter, cudaStream_t s,
                  IPTRayleighMixedCudaDeviceResult *out)
@@ -151,8 +210,7 @@ int rayleigh_run(const double *dH, int n, int k, double tf32_tol, int tf32_maxit
         }
     } guard{ev};
     const size_t elems = (size_t)n * k;
-    DeviceBuffer<double> d, X0, Q, AQ, P, B, G, Rinv, sg, Z;
-    DeviceBuffer<int> idx, st;
+    DeviceBuffer<double> d, X0, Q, B, Z;
     IPTGB_CHECK(d.alloc((size_t)n, s));
     IPTGB_CHECK(X0.alloc(elems, s));
 
@@ -183,44 +241,13 @@ int rayleigh_run(const double *dH, int n, int k, double tf32_tol, int tf32_maxit
     } og{&ops};
     IPTGB_CUDA(cudaEventRecord(ev[2], s));
     IPTGB_CHECK(Q.alloc(elems, s));
-    IPTGB_CHECK(G.alloc((size_t)k * k, s));
-    IPTGB_CHECK(Rinv.alloc((size_t)k * k, s));
-    IPTGB_CHECK(st.alloc(1, s));
-    IPTGB_CHECK(cholqr_fp64(ops, X0.ptr, n, k, Q.ptr, G.ptr, Rinv.ptr, st.ptr, s));
-    IPTGB_CHECK(cholqr_fp64(ops, Q.ptr, n, k, X0.ptr, G.ptr, Rinv.ptr, st.ptr, s));
-    {
-        std::vector<double> top((size_t)k * k);
-        IPTGB_CUDA(cudaMemcpy2DAsync(top.data(), (size_t)k * sizeof(double), X0.ptr,
-                                     (size_t)n * sizeof(double), (size_t)k * sizeof(double),
-                                     (size_t)k, cudaMemcpyDeviceToHost, s));
-        IPTGB_CUDA(cudaStreamSynchronize(s));
-        std::vector<double> signs;
-        householder_signs(top, k, n, &signs);
-        std::vector<int> id((size_t)k);
-        for (int j = 0; j < k; ++j) id[(size_t)j] = j;
-        IPTGB_CHECK(sg.alloc((size_t)k, s));
-        IPTGB_CHECK(idx.alloc((size_t)k, s));
-        IPTGB_CUDA(cudaMemcpyAsync(sg.ptr, signs.data(), (size_t)k * sizeof(double),
-                                   cudaMemcpyHostToDevice, s));
-        IPTGB_CUDA(cudaMemcpyAsync(idx.ptr, id.data(), (size_t)k * sizeof(int),
-                                   cudaMemcpyHostToDevice, s));
-        IPTGB_CHECK(ops.gather_columns(X0.ptr, n, idx.ptr, sg.ptr, n, k, Q.ptr, n));
-        // the host vectors must outlive the asynchronous copies
-        IPTGB_CUDA(cudaStreamSynchronize(s));
-    }
+    IPTGB_CHECK(householder_basis(ops, X0.ptr, n, k, Q.ptr, s));
     IPTGB_CUDA(cudaEventRecord(ev[3], s));
 
     // 3. B = sym(Q^T H Q) in FP64
     IPTGB_CUDA(cudaEventRecord(ev[4], s));
-    IPTGB_CHECK(AQ.alloc(elems, s));
     IPTGB_CHECK(B.alloc((size_t)k * k, s));
-    const int S = dense64_split_for(n, k, ops.sms);
-    IPTGB_CHECK(P.alloc((size_t)S * elems, s));
-    IPTGB_CHECK(launch_dense64_partial(dH, n, n, Q.ptr, n, k, P.ptr, S, s));
-    IPTGB_CHECK(launch_sum_partials(P.ptr, S, elems, AQ.ptr, s));
-    IPTGB_CHECK(ops.gram(Q.ptr, n, k, AQ.ptr, n, k, n, B.ptr, k));
-    symmetrize_kernel<<<(k * k + 255) / 256, 256, 0, s>>>(B.ptr, k);
-    IPTGB_LAUNCH();
+    IPTGB_CHECK(projected_matrix(ops, dH, n, Q.ptr, k, B.ptr, s));
     IPTGB_CUDA(cudaEventRecord(ev[5], s));
 
     // 4. FP64 IPT on the k x k matrix

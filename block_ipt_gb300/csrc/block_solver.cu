@@ -23,9 +23,13 @@
 
 namespace iptgb {
 
-// Required relative drop of the largest scaled residual for a learned
-// Davidson step to be kept.
+// A learned Davidson step is kept when the largest scaled residual drops at
+// least as much as a plain diagonal step is expected to: the geometric mean
+// of the drops of this solve's plain steps, kPlainDropPrior before the first
+// plain step, and in any case below kLearnedDrop of its value.  Tuning knob
+// IPT_GB300_MLP_ACCEPT replaces the required factor.
 constexpr double kLearnedDrop = 0.75;
+constexpr double kPlainDropPrior = 0.5;
 
 // Rows from which the Davidson products switch to double-float.
 constexpr int kDfDavidsonMinRows = 16384;
@@ -268,6 +272,15 @@ int block_solve(const BlockSolveInput &in, double *X_out, double *values_out,
     int restarts = 0;
     bool learned_on = true;
     int learned_rejects = 0;
+    double plain_log_drop = 0.0;
+    int plain_drops = 0;
+    const double forced_accept = env_double("IPT_GB300_MLP_ACCEPT", 0.0);
+    auto required_drop = [&]() -> double {
+        if (forced_accept > 0.0) return forced_accept;
+        const double expect =
+            plain_drops > 0 ? exp(plain_log_drop / plain_drops) : kPlainDropPrior;
+        return std::min(kLearnedDrop, expect);
+    };
     while (best > tol && steps < opt.davidson_maxsteps) {
         // pairs that still need a correction (ipt_cuda.cu:774-797)
         int nsel = 0;
@@ -317,6 +330,7 @@ int block_solve(const BlockSolveInput &in, double *X_out, double *values_out,
             double *T = Vt.ptr;  // n x nsel scratch
             if (in.learned != nullptr && (use_learned || !in.learned->learned())) {
                 CorrectionArgs ca;
+                ca.apply = in.precond_apply != nullptr ? in.precond_apply : in.apply;
                 ca.V = V.ptr;
                 ca.m = m;
                 ca.R = R.ptr;
@@ -329,6 +343,7 @@ int block_solve(const BlockSolveInput &in, double *X_out, double *values_out,
                 ca.n = n;
                 ca.clip = clip;
                 IPTGB_CHECK(in.learned->correct(ca, T));
+                rep->precond_matvecs += nsel;
             } else {
                 IPTGB_CHECK(ops.diag_correction(R.ptr, in.d, theta, sel, nsel, n, clip, T));
             }
@@ -399,8 +414,12 @@ int block_solve(const BlockSolveInput &in, double *X_out, double *values_out,
             m += c;
             IPTGB_CHECK(rayleigh_ritz());
             const double after = max_res();
+            if (!judged && isfinite(before) && before > 0.0 && isfinite(after) && after > 0.0) {
+                plain_log_drop += log(std::min(1.0, after / before));
+                ++plain_drops;
+            }
             if (judged) {
-                if (!(after < kLearnedDrop * before)) {
+                if (!(after < required_drop() * before)) {
                     // reject: restore the basis and the previous Ritz state
                     reject_learned();
                     m -= c;

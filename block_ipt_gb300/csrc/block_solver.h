@@ -30,6 +30,9 @@ struct IptStage {
 // residual norms rnorm (k), the clip of the diagonal correction, and the
 // current orthonormal search space V (n x m).
 struct CorrectionArgs {
+    // products H T for the correction's own terms (a preconditioner may use
+    // a lower-precision operator than the solve's FP64-accurate one)
+    Fp64Apply *apply = nullptr;
     const double *V = nullptr;
     int m = 0;
     const double *R = nullptr;
@@ -72,6 +75,8 @@ struct BlockSolveInput {
     const double *initial = nullptr;  // optional start block (n x initial_cols), skips the IPT stage
     int initial_cols = 0;
     Fp64Apply *apply = nullptr;
+    // operator for the learned correction's products (nullptr: `apply`)
+    Fp64Apply *precond_apply = nullptr;
     IptStage *ipt = nullptr;
     LearnedCorrection *learned = nullptr;
     const double *d = nullptr;  // device diagonal, ascending

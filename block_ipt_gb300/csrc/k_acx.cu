@@ -27,6 +27,7 @@
 
 #include "../../include/acx_cuda.h"
 #include "common.cuh"
+#include "rayleigh.h"
 #include "ipt_plain.h"
 #include "kernels.cuh"
 #include "reduce.cuh"
@@ -629,3 +630,146 @@ IPT_API int acx_mixed_precision_tf32_cuda_device_tol(const double *d_matrix_col_
     result->d_values = r64.d_values;
     return ACX_CUDA_SUCCESS;
 }
+
+// ---------------------------------------------------------------------------
+// Rayleigh ACX (IPT_C_GPU/src/ACX/acx_rayleigh_mixed_precision_cuda.cu:289-434)
+// ---------------------------------------------------------------------------
+IPT_API void acx_rayleigh_mixed_tf32_cuda_reset_result(ACXRayleighMixedTF32CudaResult *result)
+{
+    if (result == nullptr) return;
+    memset(result, 0, sizeof(*result));
+    result->tf32_time_sec = NAN;
+    result->orthogonalize_time_sec = NAN;
+    result->rayleigh_transform_time_sec = NAN;
+    result->fp64_time_sec = NAN;
+    result->finalization_time_sec = NAN;
+    result->backtransform_time_sec = NAN;
+    result->total_time_sec = NAN;
+    result->tf32_fixed_point_residual = NAN;
+    result->fp64_fixed_point_residual = NAN;
+    result->fp64_max_residual = NAN;
+}
+
+IPT_API void acx_rayleigh_mixed_tf32_cuda_free_result(ACXRayleighMixedTF32CudaResult *result)
+{
+    if (result == nullptr) return;
+    cudaFree(result->d_vectors);
+    cudaFree(result->d_values);
+    acx_rayleigh_mixed_tf32_cuda_reset_result(result);
+}
+
+namespace {
+
+// Largest k of the Rayleigh ACX: the CholQR's Cholesky inverse holds two
+// k x k FP64 matrices in one CTA's shared memory.
+constexpr int kAcxRayleighMaxK = 112;
+
+int acx_rayleigh_run(const double *dH, int n, int k, double tf32_tol, int tf32_maxiter,
+                     double fp64_tol, int fp64_maxiter, cudaStream_t s,
+                     ACXRayleighMixedTF32CudaResult *out)
+{
+    const size_t elems = (size_t)n * (size_t)k;
+    DeviceBuffer<double> X0, Q, B;
+    IPTGB_CHECK(X0.alloc(elems, s));
+    // 1. ACX of the low-precision map (the reference's TF32 ACX stage)
+    auto t = std::chrono::steady_clock::now();
+    IPTGB_CHECK(acx_fp32_run(dH, n, k, tf32_tol, tf32_maxiter, s, X0.ptr, &out->tf32_iterations,
+                             &out->tf32_f_calls, &out->tf32_converged,
+                             &out->tf32_fixed_point_residual));
+    IPTGB_CUDA(cudaStreamSynchronize(s));
+    out->tf32_time_sec = seconds_since(t);
+    // 2. orthonormal basis; the reference normalises the columns first, which
+    // changes neither the span nor the Householder column signs
+    BlockOps ops;
+    ops.stream = s;
+    ops.sms = device_sm_count();
+    struct OpsGuard {
+        BlockOps *o;
+        ~OpsGuard() { o->release(); }
+    } og{&ops};
+    t = std::chrono::steady_clock::now();
+    IPTGB_CHECK(Q.alloc(elems, s));
+    IPTGB_CHECK(householder_basis(ops, X0.ptr, n, k, Q.ptr, s));
+    IPTGB_CUDA(cudaStreamSynchronize(s));
+    out->orthogonalize_time_sec = seconds_since(t);
+    // 3. B = sym(Q^T H Q)
+    t = std::chrono::steady_clock::now();
+    IPTGB_CHECK(B.alloc((size_t)k * k, s));
+    IPTGB_CHECK(projected_matrix(ops, dH, n, Q.ptr, k, B.ptr, s));
+    IPTGB_CUDA(cudaStreamSynchronize(s));
+    out->rayleigh_transform_time_sec = seconds_since(t);
+    // 4. FP64 ACX on the k x k matrix
+    t = std::chrono::steady_clock::now();
+    ACXCudaResult r64;
+    acx_cuda_reset_result(&r64);
+    int st = acx_fp64_run(B.ptr, k, k, fp64_tol, fp64_maxiter, nullptr, s, &r64);
+    if (st != ACX_CUDA_SUCCESS) return st;
+    out->fp64_time_sec = seconds_since(t);
+    out->fp64_iterations = r64.iterations;
+    out->fp64_f_calls = r64.f_calls;
+    out->fp64_converged = r64.converged;
+    out->finalization_time_sec = r64.finalization_time_sec;
+    out->fp64_fixed_point_residual = r64.fixed_point_residual;
+    out->fp64_max_residual = r64.max_residual;
+    // 5. vectors = Q Z
+    t = std::chrono::steady_clock::now();
+    double *vecs = nullptr;
+    if (cudaMalloc((void **)&vecs, elems * sizeof(double)) != cudaSuccess) {
+        acx_cuda_free_result(&r64);
+        return ACX_CUDA_ALLOCATION_FAILED;
+    }
+    st = ops.tall_gemm(Q.ptr, n, r64.d_vectors, k, vecs, n, n, k, k);
+    if (st == IPT_CUDA_SUCCESS && cudaStreamSynchronize(s) != cudaSuccess) {
+        st = ACX_CUDA_CUDA_ERROR;
+    }
+    if (st != IPT_CUDA_SUCCESS) {
+        cudaFree(vecs);
+        acx_cuda_free_result(&r64);
+        return st;
+    }
+    out->backtransform_time_sec = seconds_since(t);
+    cudaFree(r64.d_vectors);
+    out->d_vectors = vecs;
+    out->d_values = r64.d_values;
+    out->total_time_sec = out->tf32_time_sec + out->orthogonalize_time_sec +
+                          out->rayleigh_transform_time_sec + out->fp64_time_sec +
+                          out->backtransform_time_sec;
+    out->n = n;
+    out->k = k;
+    return ACX_CUDA_SUCCESS;
+}
+
+}  // namespace
+
+IPT_API int acx_rayleigh_mixed_tf32_cuda_device_tol(const double *d_matrix_col_major, int n,
+                                                    int k, double tf32_tol, int tf32_maxiter,
+                                                    double fp64_tol, int fp64_maxiter,
+                                                    cublasHandle_t handle,
+                                                    ACXRayleighMixedTF32CudaResult *result)
+{
+    if (result == nullptr) return ACX_CUDA_INVALID_ARGUMENT;
+    acx_rayleigh_mixed_tf32_cuda_reset_result(result);
+    if (d_matrix_col_major == nullptr || handle == nullptr || n <= 0 || k <= 0 || k > n ||
+        !(tf32_tol > 0.0) || !(fp64_tol > 0.0) || tf32_maxiter <= 0 || fp64_maxiter <= 0) {
+        return ACX_CUDA_INVALID_ARGUMENT;
+    }
+    if ((size_t)n * (size_t)k > (size_t)INT_MAX || (size_t)k * (size_t)k > (size_t)INT_MAX) {
+        return ACX_CUDA_INVALID_ARGUMENT;
+    }
+    if (k > kAcxRayleighMaxK) {
+        fprintf(stderr, "ipt_gb300: acx_rayleigh_mixed_tf32_cuda_device_tol supports k <= %d "
+                        "(got %d)\n", kAcxRayleighMaxK, k);
+        return ACX_CUDA_INVALID_ARGUMENT;
+    }
+    cudaStream_t s = nullptr;
+    if (cublasGetStream(handle, &s) != CUBLAS_STATUS_SUCCESS) return ACX_CUDA_CUBLAS_ERROR;
+    const int st = acx_rayleigh_run(d_matrix_col_major, n, k, tf32_tol, tf32_maxiter, fp64_tol,
+                                    fp64_maxiter, s, result);
+    if (st != ACX_CUDA_SUCCESS) {
+        cudaFree(result->d_vectors);
+        cudaFree(result->d_values);
+        acx_rayleigh_mixed_tf32_cuda_reset_result(result);
+    }
+    return st;
+}
+

@@ -655,6 +655,17 @@ struct FciOperator final : Fp64Apply {
     int apply(const double *V, int c, double *AV) override { return sigma(V, c, AV, precision); }
 };
 
+// The same operator at a fixed precision: the learned correction's own
+// products (a preconditioner term needs no FP64 accuracy), BF16 sigma.
+struct FciFixedPrecision final : Fp64Apply {
+    FciOperator *op = nullptr;
+    int precision = kFciBF16;
+    int apply(const double *V, int c, double *AV) override
+    {
+        return op->sigma(V, c, AV, precision);
+    }
+};
+
 }  // namespace iptgb
 
 // ---------------------------------------------------------------------------
@@ -778,8 +789,11 @@ IPT_API int ipt_block_solve_fci(const IPTFciSpec *spec, int k, const IPTBlockOpt
         learned.reset(make_learned_correction(opt.mlp_params, s));
         learned->bind(coupling.ptr, hnorm);
     }
+    FciFixedPrecision precond_op;
+    precond_op.op = &op;
     BlockSolveInput in;
     in.apply = &op;
+    in.precond_apply = &precond_op;
     in.learned = learned.get();
     in.d = op.diag.ptr;
     in.n = (int)n;

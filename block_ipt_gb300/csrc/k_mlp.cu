@@ -3,32 +3,30 @@
 // t_i = r_i / (d_i - theta) of the reference's Davidson step
 // (IPT_C_GPU/src/ipt_cuda.cu:2449-2465, clip rule :3389-3403).
 //
-// The plain correction t = r / clip(d - theta) is first projected against the
-// current search space V (the solver projects every correction before it
-// enters V, so only (I - V V^T) t matters).  Features of row i for a
-// selected Ritz pair (theta, x, r), all O(1):
-//   f0 = t_i sqrt(n) / ||t||        projected plain correction, normalised
-//   f1 = r_i sqrt(n) / ||r||        residual
-//   f2 = x_i sqrt(n)                Ritz vector (unit norm)
-//   f3 = asinh((d_i - theta) / s_i) gap in units of the row's off-diagonal
-//                                   coupling s_i = ||H[i, j != i]||_2
+// The exact correction of a Ritz pair (theta, x, r) is (H - theta)^-1 r; with
+// H = D + Delta its Neumann series starts t1 + u with the plain correction
+// t1 = (D - theta)^-1 r and the second-order term u = -(D - theta)^-1 Delta t1,
+// which costs one product with H (H t1, the diagonal part taken off).  The
+// learned correction is t_i = t1_i + o_i u_i with the network's per-row
+// weight o_i clamped to [kWeightLo, kWeightHi]: o = 0 everywhere is the
+// plain preconditioner, o = 1 the two-term Neumann correction, and the
+// output bias starts at 1.  Features of row i, all O(1):
+//   f0 = t1_i sqrt(n) / ||t1||       plain correction, normalised
+//   f1 = u_i sqrt(n) / ||t1||        second-order term, same units
+//   f2 = x_i sqrt(n)                 Ritz vector (unit norm)
+//   f3 = asinh((d_i - theta) / s_i)  gap in units of the row's off-diagonal
+//                                    coupling s_i = ||H[i, j != i]||_2
 //   f4 = asinh(s_i / (|d_i - theta| + clip))
 //   f5 = log10(||r|| / max(1, ||H||_inf)) / 8   convergence level
-// Output o_i is a per-row scale of the projected plain correction: the
-// learned correction is t'_i = clamp(o_i, -2, 3) t_i, so the network can only
-// re-weight (or flip) rows of the diagonal correction and never spreads
-// mass onto rows where the plain correction is zero; o = 1 everywhere is the
-// plain preconditioner, and the output bias starts at 1.
 //
 // Training target (what the collector records while the plain solver runs
 // against the converged eigenvectors x*): the part of the exact error that
 // lies outside the current search space V, e = (I - V V^T)(s x*_l - x)
-// (x*_l the converged vector that overlaps x most, s its sign) - the
-// component a correction has to add, since the search space already holds
-// the rest - scaled by the least-squares fit e ~ alpha t of the projected
-// plain correction; per row the ideal scale y_i = e_i / (alpha t_i) with weight
-// w_i = f0_i^2, so that the weighted loss sum_i w_i (o_i - y_i)^2 equals
-// ||o o t - e / alpha||^2 in the units of f0.
+// (x*_l the converged vector that overlaps x most, s its sign), scaled by
+// the least-squares fit e ~ alpha (I - V V^T)(t1 + u); per row the weight
+// that reproduces it, y_i = (e_i / alpha - t1_i) / u_i, with weight
+// w_i = f1_i^2, so that the weighted loss sum_i w_i (o_i - y_i)^2 equals
+// ||t1 + o o u - e / alpha||^2 in the units of f1.
 //
 // Training runs on the GPU: a fused forward/backward kernel over 128-row
 // tiles of a batch (per-tile gradient partials, no atomics) and an Adam
@@ -78,13 +76,17 @@ __device__ __forceinline__ float clampf(float v, float lim)
     return fminf(fmaxf(v, -lim), lim);
 }
 
-__device__ __forceinline__ void row_features(double t, double tn, double r, double rn, double x,
+// Range of the learned weight of the second-order term.
+constexpr float kWeightLo = -1.f;
+constexpr float kWeightHi = 3.f;
+
+__device__ __forceinline__ void row_features(double t, double tn, double u, double rn, double x,
                                              double delta, double sigma, double clip,
                                              double hnorm, int n, float f[kIn])
 {
     const double sn = sqrt((double)n);
     f[0] = clampf((float)(tn > 0.0 ? t * sn / tn : 0.0), 40.f);
-    f[1] = clampf((float)(rn > 0.0 ? r * sn / rn : 0.0), 40.f);
+    f[1] = clampf((float)(tn > 0.0 ? u * sn / tn : 0.0), 40.f);
     f[2] = clampf((float)(x * sn), 40.f);
     const double s = sigma + 1e-12 * fmax(1.0, fabs(hnorm));
     f[3] = clampf((float)asinh(delta / s), 40.f);
@@ -323,12 +325,32 @@ __global__ void mlp_adam_kernel(float *__restrict__ params, float *__restrict__ 
 }
 
 // ---------------------------------------------------------------------------
-// Davidson use: features of every (row, selected pair) and the fused MLP
-// inference.  T holds the plain diagonal correction on entry (n x nsel) and
-// the learned correction clamp(o, -2, 3) T on exit.
+// Davidson use.  second_order_kernel turns U = H t1 into the second-order
+// term u = -(D - theta)^-1 (H t1 - D t1) (denominators clipped like the plain
+// correction); mlp_correct_kernel computes the features of every (row,
+// selected pair), runs the MLP and leaves t1 + clamp(o) u in T.
 // ---------------------------------------------------------------------------
+__device__ __forceinline__ double clipped_gap(double d, double theta, double clip)
+{
+    double den = d - theta;
+    if (fabs(den) < clip) den = den < 0.0 ? -clip : clip;
+    return den;
+}
+
+__global__ void second_order_kernel(const double *__restrict__ T, const double *__restrict__ d,
+                                    const double *__restrict__ theta, const int *__restrict__ sel,
+                                    int nsel, int n, double clip, double *__restrict__ U)
+{
+    const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (size_t)n * nsel) return;
+    const int i = (int)(idx % (size_t)n);
+    const int c = (int)(idx / (size_t)n);
+    const double den = clipped_gap(d[i], theta[sel[c]], clip);
+    U[idx] = -(U[idx] - d[i] * T[idx]) / den;
+}
+
 __global__ void __launch_bounds__(256)
-mlp_correct_kernel(const float *__restrict__ params, const double *__restrict__ R,
+mlp_correct_kernel(const float *__restrict__ params, const double *__restrict__ U,
                    const double *__restrict__ X, const double *__restrict__ d,
                    const double *__restrict__ theta, const int *__restrict__ sel, int nsel,
                    int n, double clip, double hnorm, const double *__restrict__ sigma,
@@ -343,11 +365,17 @@ mlp_correct_kernel(const float *__restrict__ params, const double *__restrict__ 
     const int c = (int)(idx / (size_t)n);
     const int j = sel[c];
     float f[kIn];
-    const double tn = tnorm[c];
-    row_features(T[idx], tn, R[(size_t)i + (size_t)j * n], rnorm[j], X[(size_t)i + (size_t)j * n],
-                 d[i] - theta[j], sigma[i], clip, hnorm, n, f);
-    const float o = fminf(fmaxf(forward_row(P, f), -2.f), 3.f);
-    T[idx] *= (double)o;
+    const double u = U[idx];
+    row_features(T[idx], tnorm[c], u, rnorm[j], X[(size_t)i + (size_t)j * n], d[i] - theta[j],
+                 sigma[i], clip, hnorm, n, f);
+    const float o = fminf(fmaxf(forward_row(P, f), kWeightLo), kWeightHi);
+    T[idx] = fma((double)o, u, T[idx]);
+}
+
+__global__ void add_kernel(double *__restrict__ A, const double *__restrict__ B, size_t count)
+{
+    const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e < count) A[e] += B[e];
 }
 
 // Collector: E[:, c] = s_c Xstar[:, l_c] - X[:, sel_c] (n x nsel).
@@ -364,7 +392,8 @@ __global__ void collect_error_kernel(const double *__restrict__ Xstar, const int
 }
 
 // Collector pass 1: per selected pair c: dots[3c] = <E_c, T_c>,
-// dots[3c+1] = <T_c, T_c>, dots[3c+2] = <E_c, E_c>.
+// dots[3c+1] = <T_c, T_c>, dots[3c+2] = <E_c, E_c> (T: the projected
+// two-term correction).
 __global__ void collect_dots_kernel(const double *__restrict__ E, const double *__restrict__ T,
                                     int n, double *__restrict__ dots)
 {
@@ -389,9 +418,12 @@ __global__ void collect_dots_kernel(const double *__restrict__ E, const double *
 
 // Collector pass 2: rows (f0..f5, target scale, weight) of the valid pairs;
 // slot[c] >= 0 is the pair's first row in `out`, alpha[c] the fit of E by T_c.
+// Collector pass 2: rows (f0..f5, target weight, row weight) of the valid
+// pairs; slot[c] >= 0 is the pair's first row in `out`, alpha[c] the fit of
+// E by the projected two-term correction.
 __global__ void collect_rows_kernel(const double *__restrict__ E, const double *__restrict__ alpha,
                                     const long long *__restrict__ slot,
-                                    const double *__restrict__ R, const double *__restrict__ X,
+                                    const double *__restrict__ U, const double *__restrict__ X,
                                     const double *__restrict__ d, const double *__restrict__ theta,
                                     const int *__restrict__ sel, int nsel, int n, double clip,
                                     double hnorm, const double *__restrict__ sigma,
@@ -408,18 +440,16 @@ __global__ void collect_rows_kernel(const double *__restrict__ E, const double *
     const double tn = tnorm[c];
     float f[kIn];
     const double x = X[(size_t)i + (size_t)j * n];
-    row_features(T[idx], tn, R[(size_t)i + (size_t)j * n], rnorm[j], x, d[i] - theta[j], sigma[i],
-                 clip, hnorm, n, f);
-    const double e = E[idx];
-    const double t = T[idx];
-    // ideal per-row scale of the plain correction; rows where the plain
-    // correction vanishes carry (almost) no weight
-    const double y = fabs(t) > 0.0 ? e / (alpha[c] * t) : 1.0;
+    const double u = U[idx];
+    row_features(T[idx], tn, u, rnorm[j], x, d[i] - theta[j], sigma[i], clip, hnorm, n, f);
+    // the per-row weight of u that reproduces the scaled exact error; rows
+    // where u vanishes carry (almost) no weight
+    const double y = fabs(u) > 0.0 ? (E[idx] / alpha[c] - T[idx]) / u : 1.0;
     float *o = out + (size_t)(slot[c] + i) * kRow;
 #pragma unroll
     for (int q = 0; q < kIn; ++q) o[q] = f[q];
     o[kIn] = clampf((float)y, 5.f);
-    o[kIn + 1] = f[0] * f[0];
+    o[kIn + 1] = f[1] * f[1];
 }
 
 // Row coupling s_i = ||H[i, j != i]||_2 of a CSR matrix (one warp per row).
@@ -483,6 +513,23 @@ static int project_out(BlockOps &ops, const CorrectionArgs &a, double *T, Device
     return ops.tall_gemm(a.V, a.n, G.ptr, a.m, T, a.n, a.n, a.m, a.nsel, -1.0, 1.0);
 }
 
+// t1 (plain correction, in T) and the second-order term u (in U) of the
+// selected pairs; tn = ||t1|| per pair.
+static int plain_and_second_order(BlockOps &ops, const CorrectionArgs &a, double *T,
+                                  DeviceBuffer<double> &U, double *tn)
+{
+    cudaStream_t s = ops.stream;
+    const size_t nc = (size_t)a.n * a.nsel;
+    IPTGB_CHECK(ops.diag_correction(a.R, a.d, a.theta, a.sel, a.nsel, a.n, a.clip, T));
+    if (U.count < nc) IPTGB_CHECK(U.alloc(nc, s));
+    if (a.apply == nullptr) return IPT_CUDA_INVALID_ARGUMENT;
+    IPTGB_CHECK(a.apply->apply(T, a.nsel, U.ptr));
+    mlp::second_order_kernel<<<blocks_for(nc), kThreads, 0, s>>>(T, a.d, a.theta, a.sel, a.nsel,
+                                                                 a.n, a.clip, U.ptr);
+    IPTGB_LAUNCH();
+    return ops.column_norms(T, a.n, a.n, a.nsel, tn);
+}
+
 namespace {
 
 // The learned correction used by the Davidson driver.
@@ -491,7 +538,7 @@ struct MlpCorrection final : LearnedCorrection {
     const double *sigma = nullptr;
     double hnorm = 1.0;
     BlockOps ops;
-    DeviceBuffer<double> tn, G;
+    DeviceBuffer<double> tn, U;
     void bind(const double *row_coupling, double h) override
     {
         sigma = row_coupling;
@@ -501,12 +548,10 @@ struct MlpCorrection final : LearnedCorrection {
     int correct(const CorrectionArgs &a, double *T) override
     {
         KernelTimerScope timer(kProfMlp, ops.stream);
-        IPTGB_CHECK(ops.diag_correction(a.R, a.d, a.theta, a.sel, a.nsel, a.n, a.clip, T));
         if (tn.count < (size_t)a.nsel) IPTGB_CHECK(tn.alloc((size_t)a.nsel, ops.stream));
-        IPTGB_CHECK(project_out(ops, a, T, G));
-        IPTGB_CHECK(ops.column_norms(T, a.n, a.n, a.nsel, tn.ptr));
+        IPTGB_CHECK(plain_and_second_order(ops, a, T, U, tn.ptr));
         mlp::mlp_correct_kernel<<<blocks_for((size_t)a.n * a.nsel), 256, 0, ops.stream>>>(
-            params, a.R, a.X, a.d, a.theta, a.sel, a.nsel, a.n, a.clip, hnorm, sigma, tn.ptr,
+            params, U.ptr, a.X, a.d, a.theta, a.sel, a.nsel, a.n, a.clip, hnorm, sigma, tn.ptr,
             a.rnorm, T);
         IPTGB_LAUNCH();
         return IPT_CUDA_SUCCESS;
@@ -516,7 +561,7 @@ struct MlpCorrection final : LearnedCorrection {
 
 }  // namespace
 
-// Records (features, exact-correction target) rows while returning the plain
+// Records (features, target, weight) rows while returning the plain
 // diagonal correction, so the solver follows the plain trajectory; with
 // `params` set it returns the learned correction instead, so that rows are
 // recorded along the learned trajectory (for a further round of training).
@@ -530,7 +575,7 @@ struct MlpCollector final : LearnedCorrection {
     long long capacity = 0;
     long long count = 0;
     BlockOps ops;
-    DeviceBuffer<double> tn, Xs, O, dots, sgn_d, alpha_d, E, G;
+    DeviceBuffer<double> tn, Xs, O, dots, sgn_d, alpha_d, E, G, U, B;
     DeviceBuffer<int> lidx_d;
     DeviceBuffer<long long> slot_d;
     void bind(const double *row_coupling, double h) override
@@ -542,12 +587,11 @@ struct MlpCollector final : LearnedCorrection {
     int correct(const CorrectionArgs &a, double *T) override
     {
         cudaStream_t s = ops.stream;
-        IPTGB_CHECK(ops.diag_correction(a.R, a.d, a.theta, a.sel, a.nsel, a.n, a.clip, T));
-        if (count + (long long)a.nsel * a.n > capacity || sigma == nullptr) {
-            return IPT_CUDA_SUCCESS;
-        }
         const int c = a.nsel;
         const int n = a.n;
+        if (count + (long long)a.nsel * a.n > capacity || sigma == nullptr) {
+            return ops.diag_correction(a.R, a.d, a.theta, a.sel, a.nsel, a.n, a.clip, T);
+        }
         if (tn.count < (size_t)c) {
             IPTGB_CHECK(tn.alloc((size_t)c, s));
             IPTGB_CHECK(dots.alloc(3 * (size_t)c, s));
@@ -560,9 +604,9 @@ struct MlpCollector final : LearnedCorrection {
         if (Xs.count < (size_t)n * c) {
             IPTGB_CHECK(Xs.alloc((size_t)n * c, s));
             IPTGB_CHECK(E.alloc((size_t)n * c, s));
+            IPTGB_CHECK(B.alloc((size_t)n * c, s));
         }
-        IPTGB_CHECK(project_out(ops, a, T, G));
-        IPTGB_CHECK(ops.column_norms(T, n, n, c, tn.ptr));
+        IPTGB_CHECK(plain_and_second_order(ops, a, T, U, tn.ptr));
         // overlaps of the current Ritz vectors with the converged ones
         IPTGB_CHECK(ops.gather_columns(a.X, n, a.sel, nullptr, n, c, Xs.ptr, n));
         IPTGB_CHECK(ops.gram(Xstar, n, kstar, Xs.ptr, n, c, n, O.ptr, kstar));
@@ -587,9 +631,16 @@ struct MlpCollector final : LearnedCorrection {
         mlp::collect_error_kernel<<<blocks_for((size_t)n * c), kThreads, 0, s>>>(
             Xstar, lidx_d.ptr, sgn_d.ptr, a.X, a.sel, c, n, E.ptr);
         IPTGB_LAUNCH();
-        // keep only the part of the error outside the search space (two passes)
+        // keep only the part of the error outside the search space (two
+        // passes), and fit it by the projected two-term correction t1 + u
         for (int pass = 0; pass < 2; ++pass) IPTGB_CHECK(project_out(ops, a, E.ptr, G));
-        mlp::collect_dots_kernel<<<c, 256, 0, s>>>(E.ptr, T, n, dots.ptr);
+        IPTGB_CUDA(cudaMemcpyAsync(B.ptr, T, (size_t)n * c * sizeof(double),
+                                   cudaMemcpyDeviceToDevice, s));
+        mlp::add_kernel<<<blocks_for((size_t)n * c), kThreads, 0, s>>>(B.ptr, U.ptr,
+                                                                      (size_t)n * c);
+        IPTGB_LAUNCH();
+        IPTGB_CHECK(project_out(ops, a, B.ptr, G));
+        mlp::collect_dots_kernel<<<c, 256, 0, s>>>(E.ptr, B.ptr, n, dots.ptr);
         IPTGB_LAUNCH();
         std::vector<double> hd(3 * (size_t)c);
         IPTGB_CUDA(cudaMemcpyAsync(hd.data(), dots.ptr, hd.size() * sizeof(double),
@@ -601,7 +652,7 @@ struct MlpCollector final : LearnedCorrection {
             const double et = hd[3 * (size_t)q], tt = hd[3 * (size_t)q + 1],
                          ee = hd[3 * (size_t)q + 2];
             // skip pairs whose exact correction is (numerically) orthogonal to
-            // the plain one, or already converged
+            // the two-term one, or already converged
             if (!(tt > 0.0) || !(ee > 1e-28) || fabs(et) < 0.05 * sqrt(tt * ee)) continue;
             al[(size_t)q] = et / tt;
             slot[(size_t)q] = count;
@@ -612,12 +663,12 @@ struct MlpCollector final : LearnedCorrection {
         IPTGB_CUDA(cudaMemcpyAsync(slot_d.ptr, slot.data(), (size_t)c * sizeof(long long),
                                    cudaMemcpyHostToDevice, s));
         mlp::collect_rows_kernel<<<blocks_for((size_t)n * c), kThreads, 0, s>>>(
-            E.ptr, alpha_d.ptr, slot_d.ptr, a.R, a.X, a.d, a.theta, a.sel, c, n, a.clip, hnorm,
+            E.ptr, alpha_d.ptr, slot_d.ptr, U.ptr, a.X, a.d, a.theta, a.sel, c, n, a.clip, hnorm,
             sigma, tn.ptr, a.rnorm, T, out);
         IPTGB_LAUNCH();
         if (params != nullptr) {
             mlp::mlp_correct_kernel<<<blocks_for((size_t)n * c), 256, 0, s>>>(
-                params, a.R, a.X, a.d, a.theta, a.sel, c, n, a.clip, hnorm, sigma, tn.ptr,
+                params, U.ptr, a.X, a.d, a.theta, a.sel, c, n, a.clip, hnorm, sigma, tn.ptr,
                 a.rnorm, T);
             IPTGB_LAUNCH();
         }

@@ -52,12 +52,14 @@ constexpr int kThreads = 192;                 // warps 0-3 epilogue, 4 producer,
 constexpr int kProducerWarp = 4;
 constexpr int kMmaWarp = 5;
 constexpr int kASlots = 8;
-constexpr int kBSlots = 2;
+constexpr int kMaxBSlots = 4;   // B ring depth: 4 chunks for cp <= 32, else 2
 constexpr int kChunksPerPeriod = kOzPeriod / kChunk;
 constexpr int kMaxPieces = 12;
 
 struct Params {
     int n, C, cp;
+    int b_slots;   // B ring depth
+    int acc_bufs;  // TMEM accumulator sets (2: the epilogue drains one while the MMAs fill the other)
     int nchunks, periods;
     long long items;
     int maxslots;
@@ -95,10 +97,12 @@ oz_product_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
 {
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = smem_raw + ((1024u - (tc::smem_u32(smem_raw) & 1023u)) & 1023u);
+    const int kBSlots = prm.b_slots;
     uint8_t *a_ring = smem;
     uint8_t *b_ring = smem + (size_t)kASlots * kABytes;
     uint64_t *bars = reinterpret_cast<uint64_t *>(b_ring + (size_t)kBSlots * prm.b_bytes);
-    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 2 * kASlots + 2 * kBSlots + 3);
+    uint32_t *tmem_slot =
+        reinterpret_cast<uint32_t *>(bars + 2 * kASlots + 2 * kMaxBSlots + 5);
     __shared__ volatile int abort_flag;
     __shared__ int a_issued, b_issued;
 
@@ -112,9 +116,11 @@ oz_product_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
     auto a_empty = [&](int q) { return bar0 + 8u * (uint32_t)(kASlots + q); };
     auto b_full = [&](int q) { return bar0 + 8u * (uint32_t)(2 * kASlots + q); };
     auto b_empty = [&](int q) { return bar0 + 8u * (uint32_t)(2 * kASlots + kBSlots + q); };
-    const uint32_t acc_full = bar0 + 8u * (uint32_t)(2 * kASlots + 2 * kBSlots);
-    const uint32_t acc_empty = acc_full + 8u;
-    const uint32_t mma_done = acc_full + 16u;
+    // acc_full(b), acc_empty(b) for the accumulator sets b = 0, 1; mma_done
+    const uint32_t acc_base = bar0 + 8u * (uint32_t)(2 * kASlots + 2 * kMaxBSlots);
+    auto acc_full = [&](int b) { return acc_base + 8u * (uint32_t)b; };
+    auto acc_empty = [&](int b) { return acc_base + 16u + 8u * (uint32_t)b; };
+    const uint32_t mma_done = acc_base + 32u;
     const uint32_t a_base = tc::smem_u32(a_ring);
     const uint32_t b_base = tc::smem_u32(b_ring);
 
@@ -127,8 +133,10 @@ oz_product_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
             tc::mbar_init(b_full(q), 1);
             tc::mbar_init(b_empty(q), 1);
         }
-        tc::mbar_init(acc_full, 1);
-        tc::mbar_init(acc_empty, 4);  // one arrival per epilogue warp
+        for (int b = 0; b < 2; ++b) {
+            tc::mbar_init(acc_full(b), 1);
+            tc::mbar_init(acc_empty(b), 4);  // one arrival per epilogue warp
+        }
         tc::mbar_init(mma_done, 1);
         abort_flag = 0;
         a_issued = 0;
@@ -149,7 +157,7 @@ oz_product_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
     const uint32_t tmem = *tmem_slot;
 
     if (warp == kProducerWarp && lane == 0) {
-        // ---- TMA producer: per chunk the six A slices, then the B chunk ----
+        // ---- TMA producer: per chunk the B chunk, then the six A slices ----
         const uint64_t pol = tc::l2_stream_policy();
         int ac = 0, bc = 0;
         bool waited = false;
@@ -159,6 +167,41 @@ oz_product_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
             const int c0 = per * kChunksPerPeriod;
             const int c1 = min(prm.nchunks, c0 + kChunksPerPeriod);
             for (int c = c0; c < c1 && !abort_flag; ++c) {
+                if (!waited) {
+                    // Delta's slices do not depend on the preceding kernel: the
+                    // first chunk's slices are requested before waiting for the
+                    // grid that wrote the X slices
+                    for (int s = 0; s < kOzSlices; ++s) {
+                        tc::mbar_expect_tx(a_full(s), kABytes);
+                        tc::tma_load_3d_hint(a_base + (uint32_t)s * kABytes, &tmA, c * kChunk,
+                                             tile * kBM, s, a_full(s), pol);
+                    }
+                    ac = kOzSlices;
+                    pdl_wait();
+                    waited = true;
+                    const uint32_t dst = b_base;
+                    tc::mbar_expect_tx(b_full(0), prm.b_bytes);
+                    tc::tma_load_2d(dst, &tmB, c * kChunk, 0, b_full(0));
+                    tc::tma_load_2d(dst + (uint32_t)(3 * CP * 128), &tmB, c * kChunk, 3 * CP,
+                                    b_full(0));
+                    bc = 1;
+                    continue;
+                }
+                {
+                    const int q = bc % kBSlots;
+                    const int r = bc / kBSlots;
+                    if (r > 0 &&
+                        !tc::mbar_wait(b_empty(q), (uint32_t)((r - 1) & 1), err, 12, false)) {
+                        abort_flag = 1;
+                        break;
+                    }
+                    const uint32_t dst = b_base + (uint32_t)q * prm.b_bytes;
+                    tc::mbar_expect_tx(b_full(q), prm.b_bytes);
+                    tc::tma_load_2d(dst, &tmB, c * kChunk, 0, b_full(q));
+                    tc::tma_load_2d(dst + (uint32_t)(3 * CP * 128), &tmB, c * kChunk, 3 * CP,
+                                    b_full(q));
+                    ++bc;
+                }
                 for (int s = 0; s < kOzSlices; ++s) {
                     const int q = ac % kASlots;
                     const int r = ac / kASlots;
@@ -172,25 +215,6 @@ oz_product_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
                                          tile * kBM, s, a_full(q), pol);
                     ++ac;
                 }
-                if (abort_flag) break;
-                if (!waited) {
-                    // the X slices come from the preceding kernel
-                    pdl_wait();
-                    waited = true;
-                }
-                const int q = bc % kBSlots;
-                const int r = bc / kBSlots;
-                if (r > 0 &&
-                    !tc::mbar_wait(b_empty(q), (uint32_t)((r - 1) & 1), err, 12, false)) {
-                    abort_flag = 1;
-                    break;
-                }
-                const uint32_t dst = b_base + (uint32_t)q * prm.b_bytes;
-                tc::mbar_expect_tx(b_full(q), prm.b_bytes);
-                tc::tma_load_2d(dst, &tmB, c * kChunk, 0, b_full(q));
-                tc::tma_load_2d(dst + (uint32_t)(3 * CP * 128), &tmB, c * kChunk, 3 * CP,
-                                b_full(q));
-                ++bc;
             }
         }
         if (!waited) pdl_wait();
@@ -200,12 +224,19 @@ oz_product_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
         // ---- tcgen05.mma issuer ----
         int ac = 0, bc = 0;
         int k = 0;
+        const int nb = prm.acc_bufs;
         for (long long it = it0; it < it1 && !abort_flag; ++it, ++k) {
-            if (k > 0 && !tc::mbar_wait(acc_empty, (uint32_t)((k - 1) & 1), err, 13, false)) {
+            // accumulator set k % nb: wait until the epilogue has drained its
+            // previous use (item k - nb)
+            const int ab = k % nb;
+            const int use = k / nb;
+            if (use > 0 &&
+                !tc::mbar_wait(acc_empty(ab), (uint32_t)((use - 1) & 1), err, 13, false)) {
                 abort_flag = 1;
                 break;
             }
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const uint32_t acc_tmem = tmem + (uint32_t)(ab * kOzSlices * CP);
             const int per = (int)(it % prm.periods);
             const int c0 = per * kChunksPerPeriod;
             const int c1 = min(prm.nchunks, c0 + kChunksPerPeriod);
@@ -232,7 +263,7 @@ oz_product_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
                             if (prm.pc_s[pc] != s) continue;
                             const uint64_t bd =
                                 tc::sw128_desc(bsm + (uint32_t)prm.pc_brow[pc] * 128u);
-                            tc::umma<kLowpF16>(tmem + (uint32_t)prm.pc_dcol[pc],
+                            tc::umma<kLowpF16>(acc_tmem + (uint32_t)prm.pc_dcol[pc],
                                                ad + (uint64_t)(2 * kk), bd + (uint64_t)(2 * kk),
                                                prm.pc_idesc[pc],
                                                (first && s == 0 && kk == 0) ? 0u : 1u);
@@ -246,7 +277,7 @@ oz_product_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
                 first = false;
             }
             if (abort_flag) break;
-            tc::umma_commit(acc_full);
+            tc::umma_commit(acc_full(ab));
         }
         tc::umma_commit(mma_done);
     } else if (warp < 4) {
@@ -257,11 +288,15 @@ oz_product_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
             Hs[j] = 0.0f;
             Ls[j] = 0.0f;
         }
-        const uint32_t lane_addr = tmem + ((uint32_t)(warp * 32) << 16);
         const int row_local = warp * 32 + lane;
+        const int nb = prm.acc_bufs;
         int k = 0;
         for (long long it = it0; it < it1; ++it, ++k) {
-            const bool ok = tc::mbar_wait(acc_full, (uint32_t)(k & 1), err, 16, true);
+            const int ab = k % nb;
+            const uint32_t lane_addr =
+                tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(ab * kOzSlices * CP);
+            const bool ok =
+                tc::mbar_wait(acc_full(ab), (uint32_t)((k / nb) & 1), err, 16, true);
             // warp-uniform decision: the TMEM loads below are warp-collective
             if (__any_sync(0xffffffffu, !ok || abort_flag)) {
                 abort_flag = 1;
@@ -271,9 +306,7 @@ oz_product_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
 #pragma unroll
             for (int g = 0; g < CP / 16; ++g) {
                 float v0[16], v1[16], v2[16];
-                tc::tmem_ld_16cols(lane_addr + (uint32_t)(0 * CP + 16 * g), v0);
-                tc::tmem_ld_16cols(lane_addr + (uint32_t)(1 * CP + 16 * g), v1);
-                tc::tmem_ld_16cols(lane_addr + (uint32_t)(2 * CP + 16 * g), v2);
+                tc::tmem_ld_16cols_x3(lane_addr + (uint32_t)(16 * g), CP, v0, v1, v2);
                 float hh[16], ll[16];
 #pragma unroll
                 for (int j = 0; j < 16; ++j) {
@@ -282,9 +315,7 @@ oz_product_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
                     two_sum(h, v2[j] * 0x1p-16f, hh[j], e2);
                     ll[j] = e1 + e2;
                 }
-                tc::tmem_ld_16cols(lane_addr + (uint32_t)(3 * CP + 16 * g), v0);
-                tc::tmem_ld_16cols(lane_addr + (uint32_t)(4 * CP + 16 * g), v1);
-                tc::tmem_ld_16cols(lane_addr + (uint32_t)(5 * CP + 16 * g), v2);
+                tc::tmem_ld_16cols_x3(lane_addr + (uint32_t)(3 * CP + 16 * g), CP, v0, v1, v2);
 #pragma unroll
                 for (int j = 0; j < 16; ++j) {
                     const float l = ll[j] + (v0[j] * 0x1p-24f + (v1[j] * 0x1p-32f +
@@ -297,7 +328,7 @@ oz_product_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
             }
             asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
             __syncwarp();
-            if (lane == 0) mbar_arrive(acc_empty);
+            if (lane == 0) mbar_arrive(acc_empty(ab));
             const long long tile = it / prm.periods;
             const bool last = (it + 1 == it1) || ((it + 1) / prm.periods != tile);
             if (last) {
@@ -326,8 +357,9 @@ oz_product_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
             for (int i = max(0, ai - kASlots); i < ai; ++i) {
                 tc::mbar_wait(a_full(i % kASlots), (uint32_t)((i / kASlots) & 1), err, 18, true);
             }
-            for (int i = max(0, bi - kBSlots); i < bi; ++i) {
-                tc::mbar_wait(b_full(i % kBSlots), (uint32_t)((i / kBSlots) & 1), err, 19, true);
+            for (int i = max(0, bi - prm.b_slots); i < bi; ++i) {
+                tc::mbar_wait(b_full(i % prm.b_slots), (uint32_t)((i / prm.b_slots) & 1), err,
+                              19, true);
             }
         }
     }
@@ -338,39 +370,44 @@ oz_product_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
     }
 }
 
-// B slices of X (columns c < C; zero rows for C <= c < cp): row t * cp + c
-// of B holds digit t of column c along K, zero beyond n.  One CTA per column.
-__global__ void oz_slice_x_kernel(const double *__restrict__ X, long long ldx, int n, int C,
-                                  int cp, int ldp, __half *__restrict__ B, int *__restrict__ colexp)
+// Column maxima of |X| as bit patterns (colmax zeroed by the caller): grid
+// (column, row chunk), atomicMax per CTA.
+__global__ void oz_colmax_kernel(const double *__restrict__ X, long long ldx, int n,
+                                 unsigned long long *__restrict__ colmax)
 {
     pdl_wait();
-    __shared__ unsigned long long wmax[32];
     const int c = blockIdx.x;
     const double *xc = X + (size_t)c * ldx;
     unsigned long long m = 0;
-    if (c < C) {
-        for (int j = threadIdx.x; j < n; j += blockDim.x) {
-            const unsigned long long a =
-                (unsigned long long)__double_as_longlong(xc[j]) & 0x7FFFFFFFFFFFFFFFULL;
-            m = a > m ? a : m;
-        }
+    for (int j = blockIdx.y * blockDim.x + threadIdx.x; j < n; j += gridDim.y * blockDim.x) {
+        const unsigned long long a =
+            (unsigned long long)__double_as_longlong(xc[j]) & 0x7FFFFFFFFFFFFFFFULL;
+        m = a > m ? a : m;
     }
     for (int off = 16; off > 0; off >>= 1) {
         const unsigned long long o = __shfl_xor_sync(0xffffffffu, m, off);
         m = o > m ? o : m;
     }
-    if ((threadIdx.x & 31) == 0) wmax[threadIdx.x >> 5] = m;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        for (int w = 1; w < (int)(blockDim.x >> 5); ++w) m = wmax[w] > m ? wmax[w] : m;
-        wmax[0] = m;
-    }
-    __syncthreads();
-    const int e = oz_exponent(wmax[0]);
-    if (threadIdx.x == 0 && c < C) colexp[c] = e;
+    if ((threadIdx.x & 31) == 0 && m != 0) atomicMax(colmax + c, m);
+    pdl_trigger();
+}
+
+// B slices of X (columns c < C; zero rows for C <= c < cp): row t * cp + c
+// of B holds digit t of column c along K, zero beyond n.  Grid (column, K
+// chunk); colexp[c] records the column's exponent.
+__global__ void oz_slice_x_kernel(const double *__restrict__ X, long long ldx, int n, int C,
+                                  int cp, int ldp, const unsigned long long *__restrict__ colmax,
+                                  __half *__restrict__ B, int *__restrict__ colexp)
+{
+    pdl_wait();
+    const int c = blockIdx.x;
+    const int e = c < C ? oz_exponent(colmax[c]) : 0;
+    if (blockIdx.y == 0 && threadIdx.x == 0 && c < C) colexp[c] = e;
+    const double *xc = X + (size_t)c * ldx;
     __half2 *row = reinterpret_cast<__half2 *>(B + (size_t)c * ldp);
     const size_t stride = (size_t)cp * (size_t)ldp / 2;
-    for (int j = 2 * threadIdx.x; j < ldp; j += 2 * blockDim.x) {
+    for (int j = 2 * (blockIdx.y * blockDim.x + threadIdx.x); j < ldp;
+         j += 2 * gridDim.y * blockDim.x) {
         const double v0 = (c < C && j < n) ? xc[j] : 0.0;
         const double v1 = (c < C && j + 1 < n) ? xc[j + 1] : 0.0;
         oz_store_pair(v0, v1, e, row + j / 2, stride);
@@ -440,7 +477,7 @@ __global__ void oz_slice_h_kernel(const double *__restrict__ H, int n, int ldp,
         const int l = l0 + ly;
         const double v = (i < n && l < n && l != i) ? H[(size_t)i + (size_t)l * n] : 0.0;
         int dd[kOzSlices];
-        oz_digits_of(oz_fixed(v, e), dd);
+        oz_digits_fast(v, e, dd);
 #pragma unroll
         for (int s = 0; s < kOzSlices; ++s) dg[s][tx][ly] = (short)dd[s];
     }
@@ -524,6 +561,7 @@ int OzProduct::apply_group(const double *X, long long ldx, int C, double *Y, lon
     if (cp != cp_cur) {
         IPTGB_CHECK(B.alloc((size_t)kOzSlices * cp * ldp, s));
         IPTGB_CHECK(colexp.alloc((size_t)cp, s));
+        IPTGB_CHECK(colmax.alloc((size_t)cp, s));
         IPTGB_CHECK(make_map(&mapB, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, B.ptr, ldp, kOzSlices * cp,
                              3 * cp));
         cp_cur = cp;
@@ -546,6 +584,8 @@ int OzProduct::apply_group(const double *X, long long ldx, int C, double *Y, lon
     }
     prm.maxslots = maxslots;
     prm.b_bytes = (uint32_t)(kOzSlices * cp * 128);
+    prm.b_slots = cp <= 32 ? oz::kMaxBSlots : 2;
+    prm.acc_bufs = 2 * kOzSlices * cp <= 512 ? 2 : 1;
     // MMA pieces: slice s multiplies B rows [0, (6 - s) cp) into TMEM
     // columns [s cp, 6 cp), in pieces of at most 256 columns
     const int per_piece = 256 / cp;
@@ -567,11 +607,17 @@ int OzProduct::apply_group(const double *X, long long ldx, int C, double *Y, lon
     const size_t pneed = (size_t)tiles * maxslots * C * oz::kBM;
     if (P.count < pneed) IPTGB_CHECK(P.alloc(pneed, s));
     const size_t smem = 1024 + (size_t)oz::kASlots * oz::kABytes +
-                        (size_t)oz::kBSlots * prm.b_bytes +
-                        (2 * oz::kASlots + 2 * oz::kBSlots + 3) * 8 + 16;
+                        (size_t)prm.b_slots * prm.b_bytes +
+                        (2 * oz::kASlots + 2 * oz::kMaxBSlots + 5) * 8 + 16;
 
-    IPTGB_CHECK(launch_pdl(oz::oz_slice_x_kernel, dim3(cp), dim3(256), 0, s, X, ldx, n, C, cp,
-                           ldp, B.ptr, colexp.ptr));
+    // X split: column maxima, then the digit slices (grids of about 4 CTAs per SM)
+    IPTGB_CUDA(cudaMemsetAsync(colmax.ptr, 0, (size_t)cp * sizeof(unsigned long long), s));
+    const int ychunks = std::max(1, std::min((n + 2047) / 2048, (4 * sms + cp - 1) / cp));
+    IPTGB_CHECK(launch_pdl(oz::oz_colmax_kernel, dim3(C, ychunks), dim3(256), 0, s, X, ldx, n,
+                           colmax.ptr));
+    IPTGB_CHECK(launch_pdl(oz::oz_slice_x_kernel, dim3(cp, ychunks), dim3(256), 0, s, X, ldx, n,
+                           C, cp, ldp, (const unsigned long long *)colmax.ptr, B.ptr,
+                           colexp.ptr));
     int st;
     switch (cp) {
     case 16: st = launch_product<16>(dl->mapA, mapB, prm, grid, smem, P.ptr, err.ptr, s); break;

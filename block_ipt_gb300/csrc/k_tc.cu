@@ -56,7 +56,8 @@ __global__ void __launch_bounds__(kThreads, 1)
 tc_partial_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                   int n, int p, int p_pad, int stages, int tmem_cols, int chunks_total,
                   int chunks_per_split, int kchunk_elems, uint32_t idesc, float *__restrict__ P,
-                  int *err, float a_keep, const double *hist, int step, double stop_tol)
+                  int *err, float a_keep, const double *hist, int step, double stop_tol,
+                  long long spin)
 {
     // the iteration already met its tolerance on the device: nothing to do
     // (the history is written by the previous update: wait for it first)
@@ -137,7 +138,7 @@ tc_partial_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
         for (; i < nchunks; ++i) {
             const int s = i % stages;
             const int r = i / stages;
-            if (r > 0 && !mbar_wait(empty_bar(s), (uint32_t)((r - 1) & 1), err, 1, false)) {
+            if (r > 0 && !mbar_wait(empty_bar(s), (uint32_t)((r - 1) & 1), err, 1, false, spin)) {
                 abort_flag = 1;
                 break;
             }
@@ -162,7 +163,7 @@ tc_partial_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
         for (int i = 0; i < nchunks; ++i) {
             const int s = i % stages;
             const int r = i / stages;
-            if (!mbar_wait(full_bar(s), (uint32_t)(r & 1), err, 2, false)) {
+            if (!mbar_wait(full_bar(s), (uint32_t)(r & 1), err, 2, false, spin)) {
                 abort_flag = 1;
                 break;
             }
@@ -184,10 +185,11 @@ tc_partial_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
     __syncwarp();
 
     // ---- epilogue: TMEM -> registers -> partial block ----
-    const bool ok = mbar_wait(accum_bar, 0u, err, 3, true);
-    __syncwarp();
+    const bool ok0 = mbar_wait(accum_bar, 0u, err, 3, true, spin);
+    // warp-uniform: the TMEM loads below are warp-collective
+    const bool ok = __all_sync(0xffffffffu, ok0 && !abort_flag);
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    if (ok && !abort_flag) {
+    if (ok) {
         const int row = rb * kBM + warp * 32 + lane;
         for (int cb = 0; cb < p_pad; cb += 32) {
             float v[32];
@@ -205,7 +207,10 @@ tc_partial_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
     if (abort_flag && threadIdx.x == 0) {
-        // drain copies this CTA may still have in flight (bounded)
+        // before TMEM and shared memory are released: the MMAs this CTA
+        // issued (the issuer always commits the accumulator barrier last) and
+        // the copies it may still have in flight, each with the full bound
+        mbar_wait(accum_bar, 0u, err, 5, true);
         const int issued = issued_count;
         for (int i = max(0, issued - stages); i < issued; ++i) {
             mbar_wait(full_bar(i % stages), (uint32_t)((i / stages) & 1), err, 4, true);
@@ -1204,7 +1209,7 @@ struct LowpDense final : LowpDenseOperator {
         return launch_pdl(tc::tc_partial_kernel<LowpTypes<LP>::kind>, grid, dim3(tc::kThreads),
                           smem_bytes, s, mapA, mapB[cur], n, p, p_pad, stages, tmem_cols,
                           chunks_total, chunks_per_split, (int)kchunk, idesc, P.ptr, err.ptr,
-                          a_keep, hist, step, tol);
+                          a_keep, hist, step, tol, spin);
     }
 
     int step(int want_norms, NormScratch *ns) override
@@ -1314,6 +1319,11 @@ struct LowpDense final : LowpDenseOperator {
     uint32_t idesc = 0;
     double scale = 1.0;
     float a_keep = 0.0f;  // fraction of Delta kept in L2 (evict_last) across products
+    // polls of a pipeline wait before the kernel gives up (tuning and test
+    // knob IPT_GB300_SPIN_LIMIT; the drain before TMEM is released always
+    // uses the full bound)
+    long long spin = env_int("IPT_GB300_SPIN_LIMIT", 0) > 0 ? env_int("IPT_GB300_SPIN_LIMIT", 0)
+                                                             : tc::kSpinLimit;
     // per-row 1/scale of Delta (row i scaled by its own power of two) when the
     // fused setup pass built Delta; empty: one scale for the whole matrix
     DeviceBuffer<float> inv_rows;

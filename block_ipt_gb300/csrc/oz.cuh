@@ -109,6 +109,56 @@ OZ_HD void oz_digits_of(int64_t q, int (&d)[kOzSlices])
     d[0] = (int)q;
 }
 
+// The same digits as oz_digits_of(oz_fixed(v, e)) in 32-bit integer
+// arithmetic except one 64-bit shift: with q = H 2^24 + L (0 <= L < 2^24) the
+// three low digits depend only on L (carry c in {0, 1} out of them) and the
+// three high ones on H + c.
+OZ_HD void oz_digits_fast(double v, int e, int (&d)[kOzSlices])
+{
+    uint64_t b;
+#if defined(__CUDA_ARCH__)
+    b = (uint64_t)__double_as_longlong(v);
+#else
+    __builtin_memcpy(&b, &v, sizeof(b));
+#endif
+    const uint32_t hi = (uint32_t)(b >> 32);
+    const int E = (int)((hi >> 20) & 0x7FF);
+    const int sh = E == 0 ? e - 48 + 1074 : e - 48 - (E - 1075);
+    if (E == 2047 || e == kOzNonFinite || sh <= 0 || (b << 1) == 0) {
+        oz_digits_of(oz_fixed(v, e), d);  // zero, non-finite, or a subnormal-scale row
+        return;
+    }
+    uint32_t L;
+    int32_t H;
+    if (sh >= 60) {
+        L = 0;
+        H = 0;
+    } else {
+        const uint64_t M = E == 0 ? (b & 0x000FFFFFFFFFFFFFULL)
+                                  : ((b & 0x000FFFFFFFFFFFFFULL) | 0x0010000000000000ULL);
+        const uint64_t q = (M + (1ULL << (sh - 1))) >> sh;  // < 2^48 + 1
+        const bool neg = (hi >> 31) != 0;
+        const uint64_t qs = neg ? (uint64_t)0 - q : q;
+        L = (uint32_t)qs & 0xFFFFFFu;
+        H = (int32_t)((int64_t)qs >> 24);
+    }
+    int32_t t = (int32_t)L;
+#pragma unroll
+    for (int s = kOzSlices - 1; s >= 3; --s) {
+        const int32_t r = ((t + 128) & 255) - 128;
+        d[s] = r;
+        t = (t - r) >> 8;
+    }
+    int32_t u = H + t;
+#pragma unroll
+    for (int s = 2; s >= 1; --s) {
+        const int32_t r = ((u + 128) & 255) - 128;
+        d[s] = r;
+        u = (u - r) >> 8;
+    }
+    d[0] = u;
+}
+
 }  // namespace iptgb
 
 #if defined(__CUDACC__)
@@ -130,8 +180,8 @@ __device__ __forceinline__ void oz_store_pair(double v0, double v1, int e, __hal
                                               size_t slice_stride)
 {
     int a[kOzSlices], b[kOzSlices];
-    oz_digits_of(oz_fixed(v0, e), a);
-    oz_digits_of(oz_fixed(v1, e), b);
+    oz_digits_fast(v0, e, a);
+    oz_digits_fast(v1, e, b);
 #pragma unroll
     for (int s = 0; s < kOzSlices; ++s) {
         dst[(size_t)s * slice_stride] = oz_digit_pair(a[s], b[s]);

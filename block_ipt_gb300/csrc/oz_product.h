@@ -35,6 +35,7 @@ struct OzProduct {
     int cp_cur = 0;
     DeviceBuffer<__half> B;
     DeviceBuffer<int> colexp;
+    DeviceBuffer<unsigned long long> colmax;
     DeviceBuffer<double> P;
     DeviceBuffer<int> err;
     CUtensorMap mapB;

@@ -50,9 +50,9 @@ __device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity)
 
 // Bounded wait; returns false (and records `code`) after kSpinLimit polls.
 __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int *err, int code,
-                                          bool sleepy)
+                                          bool sleepy, long long limit = kSpinLimit)
 {
-    for (long long it = 0; it < kSpinLimit; ++it) {
+    for (long long it = 0; it < limit; ++it) {
         if (mbar_try_wait(bar, parity)) {
             return true;
         }
@@ -194,6 +194,34 @@ __device__ __forceinline__ void tmem_ld_16cols(uint32_t taddr, float (&v)[16])
 #pragma unroll
     for (int i = 0; i < 16; ++i) {
         v[i] = __uint_as_float(r[i]);
+    }
+}
+
+// Three 16-column loads at taddr, taddr + stride, taddr + 2 stride with one
+// wait for all of them.
+__device__ __forceinline__ void tmem_ld_16cols_x3(uint32_t taddr, int stride, float (&a)[16],
+                                                  float (&b)[16], float (&c)[16])
+{
+    uint32_t r[48];
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+        asm volatile(
+            "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+            "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, [%16];"
+            : "=r"(r[16 * q + 0]), "=r"(r[16 * q + 1]), "=r"(r[16 * q + 2]),
+              "=r"(r[16 * q + 3]), "=r"(r[16 * q + 4]), "=r"(r[16 * q + 5]),
+              "=r"(r[16 * q + 6]), "=r"(r[16 * q + 7]), "=r"(r[16 * q + 8]),
+              "=r"(r[16 * q + 9]), "=r"(r[16 * q + 10]), "=r"(r[16 * q + 11]),
+              "=r"(r[16 * q + 12]), "=r"(r[16 * q + 13]), "=r"(r[16 * q + 14]),
+              "=r"(r[16 * q + 15])
+            : "r"(taddr + (uint32_t)(q * stride)));
+    }
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 16; ++i) {
+        a[i] = __uint_as_float(r[i]);
+        b[i] = __uint_as_float(r[16 + i]);
+        c[i] = __uint_as_float(r[32 + i]);
     }
 }
 

@@ -14,7 +14,7 @@ import numpy as np
 
 from . import api, workloads
 
-ROW = 8  # floats per training row: 6 features, target scale, weight
+ROW = 8  # floats per training row: 6 features, target weight of the second-order term, row weight
 TRAIN_SPECS = ((6, 3, 3, 1), (6, 3, 3, 2), (6, 3, 3, 3), (8, 4, 4, 1), (8, 4, 4, 2))
 
 
@@ -65,15 +65,18 @@ def train(torch, rows, count, steps=3000, batch=4096, lr=1e-3, seed=11, init_see
 
 
 def correction_losses(torch, params, rows, count):
-    """Weighted correction error of the plain preconditioner (scale 1) and of
-    the network (scale clamped to [-2, 3] as in the solver) on rows[:count]."""
+    """Weighted correction error, on rows[:count], of the plain preconditioner
+    (weight 0 on the second-order term), of the two-term Neumann correction
+    (weight 1) and of the network (weight clamped to [-1, 3] as in the
+    solver)."""
     R = rows[:count]
     out = torch.empty(count, dtype=torch.float32, device=rows.device)
     api.mlp_forward(params.data_ptr(), R.data_ptr(), count, ROW, out.data_ptr())
     w, y = R[:, 7], R[:, 6]
-    plain = torch.mean(w * (1.0 - y) ** 2).item()
-    mlp = torch.mean(w * (out.clamp(-2.0, 3.0) - y) ** 2).item()
-    return plain, mlp
+    plain = torch.mean(w * y ** 2).item()
+    neumann = torch.mean(w * (1.0 - y) ** 2).item()
+    mlp = torch.mean(w * (out.clamp(-1.0, 3.0) - y) ** 2).item()
+    return plain, neumann, mlp
 
 
 def build(torch, k=16, specs=TRAIN_SPECS, dagger=True, capacity=8_000_000, steps=3000,

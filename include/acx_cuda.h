@@ -73,6 +73,42 @@ typedef struct {
     double *d_values;
 } ACXMixedTF32CudaResult;
 
+/* Rayleigh ACX result (IPT_C_GPU/src/ACX/acx_rayleigh_mixed_precision_cuda.cu:19-42). */
+typedef struct {
+    int n;
+    int k;
+    int tf32_iterations;
+    int fp64_iterations;
+    int tf32_f_calls;
+    int fp64_f_calls;
+    int tf32_converged;
+    int fp64_converged;
+    double tf32_time_sec;
+    double orthogonalize_time_sec;
+    double rayleigh_transform_time_sec;
+    double fp64_time_sec;
+    double finalization_time_sec;
+    double backtransform_time_sec;
+    double total_time_sec;
+    double tf32_fixed_point_residual;
+    double fp64_fixed_point_residual;
+    double fp64_max_residual;
+    double *d_vectors;
+    double *d_values;
+} ACXRayleighMixedTF32CudaResult;
+
+/* IPT_C_GPU/src/ACX/acx_rayleigh_mixed_precision_cuda.cu:44-51 (driver
+ * :289-434): ACX of the low-precision map to tf32_tol (the FP32 stage of
+ * acx_mixed_precision_tf32_cuda_device_tol), an orthonormal basis Q of that
+ * block with the column signs of a Householder QR, B = sym(Q^T H Q), FP64 ACX
+ * on the k x k matrix B to fp64_tol, and the vectors Q Z.  k <= 112. */
+void acx_rayleigh_mixed_tf32_cuda_reset_result(ACXRayleighMixedTF32CudaResult *result);
+void acx_rayleigh_mixed_tf32_cuda_free_result(ACXRayleighMixedTF32CudaResult *result);
+int acx_rayleigh_mixed_tf32_cuda_device_tol(const double *d_matrix_col_major, int n, int k,
+                                            double tf32_tol, int tf32_maxiter, double fp64_tol,
+                                            int fp64_maxiter, cublasHandle_t handle,
+                                            ACXRayleighMixedTF32CudaResult *result);
+
 void acx_mixed_precision_tf32_cuda_reset_result(ACXMixedTF32CudaResult *result);
 void acx_mixed_precision_tf32_cuda_free_result(ACXMixedTF32CudaResult *result);
 int acx_mixed_precision_tf32_cuda_device_tol(const double *d_matrix_col_major, int n, int k,

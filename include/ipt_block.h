@@ -92,6 +92,7 @@ typedef struct {
     double total_ms;
     int mlp_steps_accepted;
     int mlp_steps_rejected;
+    long long precond_matvecs;  /* block-product columns of the learned correction itself */
 } IPTBlockReport;
 
 void ipt_block_default_options(IPTBlockOptions *options);
@@ -274,17 +275,23 @@ int ipt_cuda_device_tol_noalloc(const double *d_matrix_col_major, int n, int k, 
 
 /* No counterpart in the reference, whose Davidson step uses the diagonal
  * correction t_i = r_i / (d_i - theta) (IPT_C_GPU/src/ipt_cuda.cu:2449-2465).
- * A per-row MLP (IPT_BLOCK_MLP_FEATURES -> 64 -> 64 -> 1, ReLU, FP32
- * parameters on the device) maps six row features of a selected Ritz pair to
- * a per-row scale of the diagonal correction (clamped to [-2, 3]; 1 is the
- * plain preconditioner); IPTBlockOptions.preconditioner = IPT_BLOCK_PRECOND_MLP
- * with mlp_params = the trained parameters enables it.  Every learned step is
- * checked against the FP64 residual and redone with the diagonal correction when
- * the largest scaled residual does not drop (IPTBlockReport counts accepted
- * and rejected learned steps).
+ * The learned correction is t1 + o o u: t1 the plain diagonal correction,
+ * u = -(D - theta)^-1 (H - D) t1 the second term of the Neumann series of
+ * (H - theta)^-1 r (one block product per step, counted in
+ * IPTBlockReport.precond_matvecs), and o a per-row weight from an MLP
+ * (IPT_BLOCK_MLP_FEATURES -> 64 -> 64 -> 1, ReLU, FP32 parameters on the
+ * device; clamped to [-1, 3]; o = 0 is the plain preconditioner) fed with
+ * six row features of the selected Ritz pair.  IPTBlockOptions.preconditioner
+ * = IPT_BLOCK_PRECOND_MLP with mlp_params = the trained parameters enables it.
+ * Every learned step is checked against the FP64 residual: unless the largest
+ * scaled residual drops at least as much as a plain step is expected to (the
+ * geometric mean drop of the solve's plain steps, 0.5 before the first, and
+ * never less than a 25 % cut) the step is redone with the diagonal
+ * correction; two rejections in a row switch the learned correction off
+ * (IPTBlockReport counts accepted and rejected learned steps).
  *
- * Training rows are 8 floats: the 6 features, the target scale and its weight;
- * the loss is the mean of weight * (MLP(features) - target)^2. */
+ * Training rows are 8 floats: the 6 features, the target weight and its row
+ * weight; the loss is the mean of weight * (MLP(features) - target)^2. */
 #define IPT_BLOCK_MLP_FEATURES 6
 #define IPT_BLOCK_MLP_ROW 8
 

@@ -425,6 +425,24 @@ def acx_mixed(H, k, tf32_tol, tf32_maxiter, fp64_tol, fp64_maxiter):
     return X, v, out, st
 
 
+def acx_rayleigh(H, k, lowp_tol, lowp_maxiter, fp64_tol, fp64_maxiter):
+    """The reference's Rayleigh ACX driver
+    (IPT_C_GPU/src/ACX/acx_rayleigh_mixed_precision_cuda.cu:289-434) with an
+    FP64 first stage in place of its TF32 one: ACX to lowp_tol, Householder
+    QR of that block (numpy = LAPACK dgeqrf/dorgqr, the convention of its
+    cusolverDnDgeqrf/Dorgqr), B = sym(Q^T H Q), FP64 ACX on B to fp64_tol
+    and the vectors Q Z.  Returns (vectors, values, Q, info of the FP64 stage,
+    status)."""
+    X0, _, _, st = acx_dense(H, k, lowp_tol, lowp_maxiter)
+    if st != 0:
+        return None, None, None, None, st
+    Q, _ = np.linalg.qr(X0)
+    B = Q.T @ (np.asarray(H, dtype=np.float64) @ Q)
+    B = 0.5 * (B + B.T)
+    Z, vals, info, st = acx_dense(B, k, fp64_tol, fp64_maxiter)
+    return (Q @ Z if st == 0 else None), vals, Q, info, st
+
+
 def acx_test_matrix(n, epsilon, seed):
     """Symmetric dense matrix of the reference's ACX benchmark shape
     (IPT_C_GPU/test/ACX/benchmark_acx_cuda_sweep.cu:284-313): diagonal
@@ -432,6 +450,38 @@ def acx_test_matrix(n, epsilon, seed):
     [0, 1) from numpy's seeded generator standing in for its hash."""
     rng = np.random.default_rng(seed)
     U = rng.uniform(size=(n, n))
+    H = 0.5 * epsilon * (U + U.T)
+    H[np.diag_indices(n)] = np.arange(1, n + 1) + epsilon * np.diag(U)
+    return np.asfortranarray(H)
+
+
+def _splitmix64_u64(x):
+    """splitmix64 on numpy uint64 arrays (wrapping arithmetic)."""
+    x = x + np.uint64(0x9E3779B97F4A7C15)
+    x = (x ^ (x >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+    x = (x ^ (x >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+    return x ^ (x >> np.uint64(31))
+
+
+ACX_SWEEP_SEED = 20260615
+
+
+def acx_sweep_matrix(n, epsilon, base_seed=ACX_SWEEP_SEED):
+    """The matrix of the reference's ACX sweep benchmark, bit for bit:
+    seed = base_seed + n + splitmix64(bits(epsilon)) mod 1000000007
+    (IPT_C_GPU/test/ACX/benchmark_acx_cuda_sweep.cu:25,273-282,880-882);
+    u(row, col) = splitmix64(seed + n c1 ^ (row+1) c2 ^ (col+1) c3) >> 11
+    scaled to [0, 1) (:256-271); diagonal row + 1 + eps u(row, row),
+    off-diagonal eps (u(row, col) + u(col, row)) / 2 (:284-313)."""
+    with np.errstate(over="ignore"):
+        ebits = np.array([epsilon], dtype=np.float64).view(np.uint64)
+        off = int(_splitmix64_u64(ebits)[0]) % 1000000007
+        seed = np.uint64((base_seed + n + off) & 0xFFFFFFFFFFFFFFFF)
+        base = seed + np.uint64(n) * np.uint64(0xD1B54A32D192ED03)
+        r = (np.arange(n, dtype=np.uint64) + np.uint64(1)) * np.uint64(0x9E3779B97F4A7C15)
+        c = (np.arange(n, dtype=np.uint64) + np.uint64(1)) * np.uint64(0xBF58476D1CE4E5B9)
+        x = (base ^ r[:, None]) ^ c[None, :]  # x[row, col]
+        U = (_splitmix64_u64(x) >> np.uint64(11)).astype(np.float64) * (1.0 / 9007199254740992.0)
     H = 0.5 * epsilon * (U + U.T)
     H[np.diag_indices(n)] = np.arange(1, n + 1) + epsilon * np.diag(U)
     return np.asfortranarray(H)

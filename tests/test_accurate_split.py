@@ -53,3 +53,24 @@ def test_split_matches_oracle(lib):
 def test_split_nonfinite_row(lib):
     e, d = host_split(lib, np.array([1.0, np.nan, np.inf]), np.inf)
     assert e == 0x7FFFFFFF and not d.any()
+
+
+def test_fast_digit_extraction_is_identical(tmp_path):
+    """The kernels' 32-bit digit extraction (oz_digits_fast) equals the 64-bit
+    definition (oz_digits_of of oz_fixed) on 3 million values (compiled with
+    the host C++ compiler from the library's own header)."""
+    import os
+    import shutil
+    import subprocess
+    cxx = shutil.which("g++") or shutil.which("c++")
+    if cxx is None:
+        import pytest
+        pytest.skip("no C++ compiler")
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    exe = str(tmp_path / "oz_eq")
+    subprocess.run([cxx, "-O2", "-std=c++17", "-I", os.path.join(root, "block_ipt_gb300", "csrc"),
+                    os.path.join(root, "tests", "cpp", "oz_digits_equivalence.cpp"), "-o", exe],
+                   check=True)
+    out = subprocess.run([exe], capture_output=True, text=True)
+    assert out.returncode == 0, out.stdout
+    assert "mismatches 0" in out.stdout

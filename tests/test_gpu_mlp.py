@@ -118,10 +118,11 @@ def test_collector_rows(cuda):
     assert got > 0 and got % csr["n"] == 0
     R = rows[:got].cpu().numpy()
     assert np.isfinite(R).all()
-    # f0 is a unit-RMS normalisation of each pair's correction; weight = f0^2
-    assert np.allclose(R[:, 7], R[:, 0] ** 2, rtol=1e-6)
-    per_pair = R[:, 7].reshape(-1, csr["n"]).mean(axis=1)
+    # f0 is a unit-RMS normalisation of each pair's plain correction; the
+    # row weight is f1^2, the second-order term in the same units
+    per_pair = (R[:, 0] ** 2).reshape(-1, csr["n"]).mean(axis=1)
     assert np.allclose(per_pair, 1.0, rtol=2e-2)
+    assert np.allclose(R[:, 7], R[:, 1] ** 2, rtol=1e-6)
 
 
 @pytest.fixture(scope="module")
@@ -132,38 +133,63 @@ def trained(cuda):
 
 
 def test_learned_correction_beats_plain_on_held_out(cuda, trained):
-    """What the trained network gains: on a held-out instance of the family
-    (8 orbitals, seed 9), its corrections are closer to the exact corrections
-    than the plain diagonal ones, and the learned Davidson solve reaches the
-    same eigenpairs."""
+    """What the trained network gains: on held-out instances of the family
+    (8 orbitals seed 9, and the 10-orbital size it was not trained at), its
+    corrections are closer to the exact corrections than the plain diagonal
+    ones, and the learned Davidson solve reaches the same eigenpairs in fewer
+    steps and with fewer block-product columns in total (its own
+    second-order products included) than the plain one."""
     torch = cuda
     params, info = trained
     assert info["loss_last"] < info["loss_first"]
     csr = learned.device_csr(torch, 8, 4, 4, 9)
     rows = torch.empty((1_500_000, 8), dtype=torch.float32, device="cuda")
     got = learned.collect(torch, csr, 16, rows, 0)
-    plain, mlp = learned.correction_losses(torch, params, rows, got)
-    assert mlp < 0.97 * plain, (plain, mlp)
-    _, wp, rp = learned.solve_csr(torch, csr, 16, strategy=1, davidson_maxsteps=100)
-    _, wl, rl = learned.solve_csr(torch, csr, 16, strategy=1, davidson_maxsteps=100,
-                                  preconditioner=1, mlp_params=params.data_ptr())
-    assert rp["converged"] == 1 and rl["converged"] == 1
-    assert rl["max_scaled_residual"] <= 1e-8
-    assert (wl - wp).abs().max().item() <= 1e-10 * rp["matrix_norm_inf"]
-    assert rl["mlp_steps_accepted"] > 0
-    assert rl["davidson_steps"] <= 1.5 * rp["davidson_steps"] + 2
+    plain, neumann, mlp = learned.correction_losses(torch, params, rows, got)
+    assert mlp < 0.8 * plain, (plain, neumann, mlp)
+    del rows
+    for spec in ((8, 4, 4, 9), (10, 5, 5, 4)):
+        csr = learned.device_csr(torch, *spec)
+        _, wp, rp = learned.solve_csr(torch, csr, 16, strategy=1, davidson_maxsteps=100)
+        _, wl, rl = learned.solve_csr(torch, csr, 16, strategy=1, davidson_maxsteps=100,
+                                      preconditioner=1, mlp_params=params.data_ptr())
+        assert rp["converged"] == 1 and rl["converged"] == 1
+        assert rl["max_scaled_residual"] <= 1e-8
+        assert (wl - wp).abs().max().item() <= 1e-10 * rp["matrix_norm_inf"]
+        assert rl["mlp_steps_accepted"] > 0
+        assert rl["davidson_steps"] < rp["davidson_steps"], (spec, rl, rp)
+        assert rl["fp64_matvecs"] + rl["precond_matvecs"] < rp["fp64_matvecs"], (spec, rl, rp)
 
 
-def test_rejected_learned_steps_fall_back_to_plain(cuda):
-    """A network that outputs scale 0 (an empty correction) is rejected by the
-    FP64 residual test, switched off after two rejections, and the plain
-    correction finishes the solve with the same eigenpairs."""
+def test_zero_network_is_the_plain_preconditioner(cuda, monkeypatch):
+    """A network that outputs weight 0 everywhere gives the plain diagonal
+    correction: with every step accepted (IPT_GB300_MLP_ACCEPT), the learned
+    solve follows the plain solve step for step."""
     torch = cuda
+    monkeypatch.setenv("IPT_GB300_MLP_ACCEPT", "1e30")
     P = torch.zeros(api.mlp_param_count(), dtype=torch.float32, device="cuda")
     csr = learned.device_csr(torch, 6, 3, 3, 2)
     _, wp, rp = learned.solve_csr(torch, csr, 16, strategy=1, davidson_maxsteps=100)
     _, wl, rl = learned.solve_csr(torch, csr, 16, strategy=1, davidson_maxsteps=100,
                                   preconditioner=1, mlp_params=P.data_ptr())
+    assert rl["converged"] == 1
+    assert rl["davidson_steps"] == rp["davidson_steps"]
+    assert rl["fp64_matvecs"] == rp["fp64_matvecs"]
+    assert (wl - wp).abs().max().item() <= 1e-10 * rp["matrix_norm_inf"]
+
+
+def test_rejected_learned_steps_fall_back_to_plain(cuda, trained, monkeypatch):
+    """With an acceptance bar no step can meet (IPT_GB300_MLP_ACCEPT), every
+    learned step is rejected by the FP64 residual test, the learned
+    correction is switched off after two rejections, and the plain
+    correction finishes the solve with the same eigenpairs."""
+    torch = cuda
+    params, _ = trained
+    monkeypatch.setenv("IPT_GB300_MLP_ACCEPT", "1e-30")
+    csr = learned.device_csr(torch, 6, 3, 3, 2)
+    _, wp, rp = learned.solve_csr(torch, csr, 16, strategy=1, davidson_maxsteps=100)
+    _, wl, rl = learned.solve_csr(torch, csr, 16, strategy=1, davidson_maxsteps=100,
+                                  preconditioner=1, mlp_params=params.data_ptr())
     assert rl["converged"] == 1
     assert rl["mlp_steps_rejected"] == 2 and rl["mlp_steps_accepted"] == 0
     assert (wl - wp).abs().max().item() <= 1e-10 * rp["matrix_norm_inf"]
