@@ -442,12 +442,29 @@ def gj_fmas(m):
 
 def cluster_part(args, torch, lib, stream, flush, dev, Hs, drp, dci, dvv, k, e0, e1):
     """The block-cluster basis (the reference's IPT_BLOCK_CLUSTER stage) of
-    the same matrix: cluster ranges of the k targets on the host, the basis
-    solve on the device (CSR products + the Gauss-Jordan update kernel), and
-    the update kernel's FP64 roofline."""
+    the same matrix: cluster ranges of the k targets from the device CSR
+    (scans on the GPU, detection rules on the host), the basis solve on the
+    device (CSR products + the Gauss-Jordan update kernel), and the update
+    kernel's FP64 roofline."""
     from block_ipt_gb300 import api
     n = Hs.shape[0]
-    ranges, _ = api.cluster_ranges(Hs.indptr, Hs.indices, Hs.data, n, k)
+
+    def detect():
+        return api.cluster_ranges_device(drp.data_ptr(), dci.data_ptr(), dvv.data_ptr(), n,
+                                         int(Hs.nnz), k, stream=stream.cuda_stream)
+
+    ranges, _ = detect()
+    host_ranges, _ = api.cluster_ranges(Hs.indptr, Hs.indices, Hs.data, n, k)
+    if ranges != host_ranges:
+        raise RuntimeError("device cluster ranges differ from the host entry's")
+    detect_ms = []
+    for _ in range(3):
+        t0 = time.perf_counter()
+        detect()
+        detect_ms.append((time.perf_counter() - t0) * 1e3)
+    t0 = time.perf_counter()
+    api.cluster_ranges(Hs.indptr, Hs.indices, Hs.data, n, k)
+    host_detect_ms = (time.perf_counter() - t0) * 1e3
     dd = torch.from_numpy(Hs.diagonal().copy()).to(dev)
     cols = sum(b - a + 1 for a, b in ranges)
     dB = torch.empty((cols, n), dtype=torch.float64, device=dev)
@@ -480,6 +497,7 @@ def cluster_part(args, torch, lib, stream, flush, dev, Hs, drp, dci, dvv, k, e0,
     ach = flops / (up_ms * 1e-3) / 1e12 if up_ms else None
     return {"ranges": [list(r) for r in ranges if r[1] > r[0]], "clusters": len(ranges),
             "basis_cols": cols, "iterations": [int(x) for x in its],
+            "detect_ms": min(detect_ms), "host_detect_ms": host_detect_ms,
             "max_fixed_point_residual": float(np.nanmax(res)), "ms": statistics.mean(times),
             "update": {"launches": up_cnt, "ms_per_solve": up_ms, "fp64_tflops": ach,
                        "peak_tflops": peak.value, "frac": ach / peak.value if ach else None,

@@ -275,6 +275,9 @@ SIGNATURES = [
     ("ipt_block_cluster_ranges", _i, [_vp, _vp, _vp, _i, _i, _i, _i, C.c_double, _i,
                                       C.c_double, _vp, _i, C.POINTER(C.c_int),
                                       C.POINTER(C.c_int)]),
+    ("ipt_block_cluster_ranges_device", _i, [_vp, _vp, _vp, _i, _i, _i, _i, C.c_double, _i,
+                                             C.c_double, _vp, _i, C.POINTER(C.c_int),
+                                             C.POINTER(C.c_int), _vp]),
     ("acx_cuda_status_string", C.c_char_p, [_i]),
     ("acx_cuda_reset_result", None, [C.POINTER(ACXCudaResult)]),
     ("acx_cuda_free_result", None, [C.POINTER(ACXCudaResult)]),

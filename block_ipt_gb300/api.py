@@ -378,6 +378,23 @@ def cluster_ranges(col_ptr, row_ind, values, n, k, requested_k=None, threshold=0
     return [(int(out[2 * i]), int(out[2 * i + 1])) for i in range(cnt.value)], bool(lim.value)
 
 
+def cluster_ranges_device(d_row_ptr, d_col_ind, d_vals, n, nnz, k, requested_k=None,
+                          threshold=0.0, adaptive=False, coupling_tau=0.1, stream=None):
+    """Cluster ranges of a prepared symmetric device CSR
+    (ipt_block_cluster_ranges_device): ([(first, last), ...], limit_hit)."""
+    lib = _lib.load()
+    cap = max(1, n)
+    out = np.zeros(2 * cap, dtype=np.int32)
+    cnt, lim = C.c_int(0), C.c_int(0)
+    st = lib.ipt_block_cluster_ranges_device(d_row_ptr, d_col_ind, d_vals, n, nnz, k,
+                                             k if requested_k is None else requested_k,
+                                             threshold, int(bool(adaptive)), coupling_tau,
+                                             _ptr(out), cap, C.byref(cnt), C.byref(lim),
+                                             _stream_ptr(stream))
+    _check(st, "ipt_block_cluster_ranges_device")
+    return [(int(out[2 * i]), int(out[2 * i + 1])) for i in range(cnt.value)], bool(lim.value)
+
+
 def cluster_basis(d_row_ptr, d_col_ind, d_vals, n, nnz, d_diag, ranges, maxiter, tol,
                   d_basis, damping=1.0, stream=None):
     """Block-cluster basis on the device (ipt_block_cluster_basis); returns

@@ -23,6 +23,15 @@ struct ClusterRanges {
     int max_block_size = kClusterMaxWidth;
 };
 
+// How the cluster-range rules read the matrix: the first stored entry of
+// CSC column col at row (0 if absent), and the stored entries of a column
+// in storage order.
+struct ClusterMatrixView {
+    virtual ~ClusterMatrixView() = default;
+    virtual double entry(int row, int col) = 0;
+    virtual void column(int col, std::vector<std::pair<int, double>> *entries) = 0;
+};
+
 // Cluster ranges of the k targets (the basis target: requested + oversample)
 // of a symmetric CSC matrix whose diagonal is ascending (prep.cpp;
 // ipt_preparation.cu:502-644, ipt_cuda.cu:4114-4272); the adaptive expansion
@@ -30,6 +39,22 @@ struct ClusterRanges {
 void cluster_ranges(const int *col_ptr, const int *row_ind, const double *vals, int n, int k,
                     int requested_k, double degeneracy_threshold, int adaptive,
                     double coupling_tau, ClusterRanges *out);
+
+// The same rules on a matrix read through `view`, with its diagonal (sum of
+// duplicates) and the largest off-diagonal magnitude of every row/column
+// already formed (by the host scan above, or by a device pass over a
+// symmetric CSR, k_cluster.cu).
+void cluster_ranges_from(ClusterMatrixView &view, int n, const std::vector<double> &diag,
+                         const std::vector<double> &offmax, int k, int requested_k,
+                         double degeneracy_threshold, int adaptive, double coupling_tau,
+                         ClusterRanges *out);
+
+// cluster_ranges_from on a symmetric device CSR (rows sorted by column, no
+// duplicates): diagonal and off-diagonal maxima from a device pass, the rows
+// the rules read fetched on demand (k_cluster.cu).
+int cluster_ranges_device(const int *row_ptr, const int *col_ind, const double *vals, int n,
+                          int k, int requested_k, double degeneracy_threshold, int adaptive,
+                          double coupling_tau, ClusterRanges *out, cudaStream_t s);
 
 size_t cluster_update_smem(int m);
 

@@ -38,6 +38,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <utility>
 #include <vector>
 
 #include "block_solver.h"
@@ -478,9 +479,171 @@ int cluster_basis_solve(const int *row_ptr, const int *col_ind, const double *va
     return failed ? IPT_CUDA_INVALID_ARGUMENT : IPT_CUDA_SUCCESS;
 }
 
+// ---------------------------------------------------------------------------
+// Cluster ranges from a device CSR: the O(nnz) scans on the GPU (one warp per
+// row: the diagonal as the sum of the row's diagonal entries, and the largest
+// off-diagonal magnitude), the rules of the reference's detection on the host
+// (prep.cpp) with the few matrix rows they read fetched on demand.
+// ---------------------------------------------------------------------------
+__global__ void csr_diag_offmax_kernel(const int *__restrict__ row_ptr,
+                                       const int *__restrict__ col_ind,
+                                       const double *__restrict__ vals, int n,
+                                       double *__restrict__ diag, double *__restrict__ offmax)
+{
+    const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (warp >= n) return;
+    const int row = (int)warp;
+    double dsum = 0.0, m = 0.0;
+    for (int p = row_ptr[row] + lane; p < row_ptr[row + 1]; p += 32) {
+        const double v = vals[p];
+        if (col_ind[p] == row) {
+            dsum += v;
+        } else {
+            m = fmax(m, fabs(v));
+        }
+    }
+    // a merged row holds at most one diagonal entry, so the sum is exact
+    for (int off = 16; off > 0; off >>= 1) {
+        dsum += __shfl_xor_sync(0xffffffffu, dsum, off);
+        m = fmax(m, __shfl_xor_sync(0xffffffffu, m, off));
+    }
+    if (lane == 0) {
+        diag[row] = dsum;
+        offmax[row] = m;
+    }
+}
+
+namespace {
+
+// Rows of a symmetric device CSR, fetched on demand: for a symmetric matrix
+// CSC column c is CSR row c, and H[r, c] can be read from either row.
+struct DeviceCsrView final : ClusterMatrixView {
+    const int *row_ptr = nullptr;
+    const int *col_ind = nullptr;
+    const double *vals = nullptr;
+    cudaStream_t s = nullptr;
+    std::vector<int> h_row_ptr;
+    std::vector<std::vector<std::pair<int, double>>> rows;
+    std::vector<char> have;
+    int status = IPT_CUDA_SUCCESS;
+
+    // rows [r0, r1) in one copy
+    void fetch(int r0, int r1)
+    {
+        const int p0 = h_row_ptr[(size_t)r0], p1 = h_row_ptr[(size_t)r1];
+        std::vector<int> ci((size_t)(p1 - p0));
+        std::vector<double> va((size_t)(p1 - p0));
+        if (p1 > p0 &&
+            (cudaMemcpyAsync(ci.data(), col_ind + p0, ci.size() * sizeof(int),
+                             cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+             cudaMemcpyAsync(va.data(), vals + p0, va.size() * sizeof(double),
+                             cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+             cudaStreamSynchronize(s) != cudaSuccess)) {
+            status = IPT_CUDA_CUDA_ERROR;
+        }
+        for (int r = r0; r < r1; ++r) {
+            auto &row = rows[(size_t)r];
+            row.clear();
+            for (int p = h_row_ptr[(size_t)r]; p < h_row_ptr[(size_t)r + 1]; ++p) {
+                if (status == IPT_CUDA_SUCCESS) {
+                    row.emplace_back(ci[(size_t)(p - p0)], va[(size_t)(p - p0)]);
+                }
+            }
+            have[(size_t)r] = 1;
+        }
+    }
+    const std::vector<std::pair<int, double>> &row(int r)
+    {
+        if (!have[(size_t)r]) fetch(r, r + 1);
+        return rows[(size_t)r];
+    }
+    static double find(const std::vector<std::pair<int, double>> &row, int c)
+    {
+        auto it = std::lower_bound(row.begin(), row.end(), c,
+                                   [](const std::pair<int, double> &e, int v) { return e.first < v; });
+        return (it != row.end() && it->first == c) ? it->second : 0.0;
+    }
+    double entry(int r, int c) override
+    {
+        if (have[(size_t)c]) return find(rows[(size_t)c], r);
+        if (have[(size_t)r]) return find(rows[(size_t)r], c);
+        return find(row(c), r);
+    }
+    void column(int c, std::vector<std::pair<int, double>> *e) override { *e = row(c); }
+};
+
+}  // namespace
+
+int cluster_ranges_device(const int *row_ptr, const int *col_ind, const double *vals, int n,
+                          int k, int requested_k, double degeneracy_threshold, int adaptive,
+                          double coupling_tau, ClusterRanges *out, cudaStream_t s)
+{
+    DeviceBuffer<double> dd, dm;
+    IPTGB_CHECK(dd.alloc((size_t)n, s));
+    IPTGB_CHECK(dm.alloc((size_t)n, s));
+    csr_diag_offmax_kernel<<<(unsigned)(((long long)n * 32 + 255) / 256), 256, 0, s>>>(
+        row_ptr, col_ind, vals, n, dd.ptr, dm.ptr);
+    IPTGB_LAUNCH();
+    std::vector<double> diag((size_t)n), offmax((size_t)n);
+    DeviceCsrView view;
+    view.row_ptr = row_ptr;
+    view.col_ind = col_ind;
+    view.vals = vals;
+    view.s = s;
+    view.h_row_ptr.resize((size_t)n + 1);
+    view.rows.resize((size_t)n);
+    view.have.assign((size_t)n, 0);
+    IPTGB_CUDA(cudaMemcpyAsync(diag.data(), dd.ptr, (size_t)n * sizeof(double),
+                               cudaMemcpyDeviceToHost, s));
+    IPTGB_CUDA(cudaMemcpyAsync(offmax.data(), dm.ptr, (size_t)n * sizeof(double),
+                               cudaMemcpyDeviceToHost, s));
+    IPTGB_CUDA(cudaMemcpyAsync(view.h_row_ptr.data(), row_ptr, ((size_t)n + 1) * sizeof(int),
+                               cudaMemcpyDeviceToHost, s));
+    IPTGB_CUDA(cudaStreamSynchronize(s));
+    // the target rows are the first k: one copy
+    view.fetch(0, std::min(k, n));
+    cluster_ranges_from(view, n, diag, offmax, k, requested_k, degeneracy_threshold, adaptive,
+                        coupling_tau, out);
+    return view.status;
+}
+
 }  // namespace iptgb
 
 #define IPT_API extern "C" __attribute__((visibility("default")))
+
+// Device CSR: the cluster ranges of ipt_block_cluster_ranges (same rules,
+// same ranges) for a symmetric matrix whose rows are sorted by column
+// without duplicates and whose diagonal is ascending (the prepared matrix of
+// the block-cluster path); the scans over the nonzeros run on the GPU.
+IPT_API int ipt_block_cluster_ranges_device(const int *d_row_ptr, const int *d_col_ind,
+                                            const double *d_vals, int n, int nnz, int k,
+                                            int requested_k, double degeneracy_threshold,
+                                            int adaptive, double coupling_tau, int *ranges,
+                                            int capacity, int *count, int *limit_hit,
+                                            void *stream)
+{
+    if (count != nullptr) *count = 0;
+    if (limit_hit != nullptr) *limit_hit = 0;
+    if (d_row_ptr == nullptr || d_col_ind == nullptr || d_vals == nullptr || count == nullptr ||
+        n <= 0 || nnz < 0 || k <= 0 || k > n || requested_k <= 0 || requested_k > k) {
+        return IPT_CUDA_INVALID_ARGUMENT;
+    }
+    iptgb::ClusterRanges cr;
+    IPTGB_CHECK(iptgb::cluster_ranges_device(d_row_ptr, d_col_ind, d_vals, n, k, requested_k,
+                                             degeneracy_threshold, adaptive, coupling_tau, &cr,
+                                             static_cast<cudaStream_t>(stream)));
+    *count = (int)cr.ranges.size();
+    if (limit_hit != nullptr) *limit_hit = cr.limit_hit;
+    if (cr.too_large || *count > capacity || ranges == nullptr) {
+        return IPT_CUDA_INVALID_ARGUMENT;
+    }
+    for (size_t i = 0; i < cr.ranges.size(); ++i) {
+        ranges[2 * i] = cr.ranges[i].first;
+        ranges[2 * i + 1] = cr.ranges[i].second;
+    }
+    return IPT_CUDA_SUCCESS;
+}
 
 using namespace iptgb;
 

@@ -14,10 +14,11 @@
 //    of (128-row tile, 128-element K period) items.  Warp 4 streams the A
 //    slices (each byte of A is read once per product, L2 evict_first) and
 //    the B chunk through TMA into shared memory; warp 5 issues tcgen05.mma:
-//    for slice s one MMA with N = (6 - s) * cp over B rows [0, (6-s) cp)
-//    into TMEM columns [s cp, 6 cp), so that digit pair (s, t) lands in the
-//    accumulator of level s + t and every level l <= 5 sums its pairs in
-//    place (pieces of at most 256 columns); warps 0-3 drain the six level
+//    one MMA (N = cp) per digit pair (s, t) with s + t <= 5 into the TMEM
+//    accumulator of level s + t (consecutive MMAs write disjoint columns, so
+//    the tensor pipe overlaps them, and the K steps of a pair chain on one
+//    accumulator; two accumulator sets when they fit in TMEM, so the MMAs of
+//    the next period run while the last one drains); warps 0-3 drain the six level
 //    accumulators after every period, combine them in double-float
 //    arithmetic and keep a running sum per (row, column) until the CTA
 //    leaves the tile, then write one FP64 partial per (tile, CTA);
@@ -51,24 +52,20 @@ constexpr uint32_t kABytes = kBM * 128;       // one slice of one chunk: 16 KB
 constexpr int kThreads = 192;                 // warps 0-3 epilogue, 4 producer, 5 MMA
 constexpr int kProducerWarp = 4;
 constexpr int kMmaWarp = 5;
-constexpr int kASlots = 8;
-constexpr int kMaxBSlots = 4;   // B ring depth: 4 chunks for cp <= 32, else 2
+constexpr int kMaxASlots = 12;  // A ring depth (slices in flight), set by the shared memory left
+constexpr int kMaxBSlots = 2;   // B ring depth (chunks)
 constexpr int kChunksPerPeriod = kOzPeriod / kChunk;
-constexpr int kMaxPieces = 12;
 
 struct Params {
     int n, C, cp;
+    int a_slots;   // A ring depth
     int b_slots;   // B ring depth
     int acc_bufs;  // TMEM accumulator sets (2: the epilogue drains one while the MMAs fill the other)
     int nchunks, periods;
     long long items;
     int maxslots;
     uint32_t b_bytes;
-    int pieces;
-    int pc_s[kMaxPieces];
-    int pc_brow[kMaxPieces];
-    int pc_dcol[kMaxPieces];
-    uint32_t pc_idesc[kMaxPieces];
+    uint32_t idesc;  // M = 128, N = cp, FP16 x FP16 -> FP32
 };
 
 // CTA that owns item x when `items` items are split into G contiguous ranges
@@ -98,11 +95,12 @@ oz_product_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = smem_raw + ((1024u - (tc::smem_u32(smem_raw) & 1023u)) & 1023u);
     const int kBSlots = prm.b_slots;
+    const int kASlots = prm.a_slots;
     uint8_t *a_ring = smem;
     uint8_t *b_ring = smem + (size_t)kASlots * kABytes;
     uint64_t *bars = reinterpret_cast<uint64_t *>(b_ring + (size_t)kBSlots * prm.b_bytes);
     uint32_t *tmem_slot =
-        reinterpret_cast<uint32_t *>(bars + 2 * kASlots + 2 * kMaxBSlots + 5);
+        reinterpret_cast<uint32_t *>(bars + 2 * kMaxASlots + 2 * kMaxBSlots + 5);
     __shared__ volatile int abort_flag;
     __shared__ int a_issued, b_issued;
 
@@ -113,11 +111,13 @@ oz_product_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
     const long long it1 = ((long long)blockIdx.x + 1) * prm.items / G;
     const uint32_t bar0 = tc::smem_u32(bars);
     auto a_full = [&](int q) { return bar0 + 8u * (uint32_t)q; };
-    auto a_empty = [&](int q) { return bar0 + 8u * (uint32_t)(kASlots + q); };
-    auto b_full = [&](int q) { return bar0 + 8u * (uint32_t)(2 * kASlots + q); };
-    auto b_empty = [&](int q) { return bar0 + 8u * (uint32_t)(2 * kASlots + kBSlots + q); };
+    auto a_empty = [&](int q) { return bar0 + 8u * (uint32_t)(kMaxASlots + q); };
+    auto b_full = [&](int q) { return bar0 + 8u * (uint32_t)(2 * kMaxASlots + q); };
+    auto b_empty = [&](int q) {
+        return bar0 + 8u * (uint32_t)(2 * kMaxASlots + kMaxBSlots + q);
+    };
     // acc_full(b), acc_empty(b) for the accumulator sets b = 0, 1; mma_done
-    const uint32_t acc_base = bar0 + 8u * (uint32_t)(2 * kASlots + 2 * kMaxBSlots);
+    const uint32_t acc_base = bar0 + 8u * (uint32_t)(2 * kMaxASlots + 2 * kMaxBSlots);
     auto acc_full = [&](int b) { return acc_base + 8u * (uint32_t)b; };
     auto acc_empty = [&](int b) { return acc_base + 16u + 8u * (uint32_t)b; };
     const uint32_t mma_done = acc_base + 32u;
@@ -257,16 +257,21 @@ oz_product_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
                     }
                     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
                     const uint64_t ad = tc::sw128_desc(a_base + (uint32_t)qa * kABytes);
+                    // one MMA per digit pair (s, t) into the accumulator of
+                    // level s + t: consecutive MMAs write disjoint TMEM
+                    // columns, and the K steps of one pair chain on the same
+                    // accumulator
 #pragma unroll
                     for (int kk = 0; kk < 4; ++kk) {
-                        for (int pc = 0; pc < prm.pieces; ++pc) {
-                            if (prm.pc_s[pc] != s) continue;
-                            const uint64_t bd =
-                                tc::sw128_desc(bsm + (uint32_t)prm.pc_brow[pc] * 128u);
-                            tc::umma<kLowpF16>(acc_tmem + (uint32_t)prm.pc_dcol[pc],
+#pragma unroll
+                        for (int t = 0; t < kOzSlices; ++t) {
+                            if (t + s >= kOzSlices) break;
+                            const uint64_t bd = tc::sw128_desc(bsm + (uint32_t)(t * CP) * 128u);
+                            // the first K step of an item initialises each level
+                            // through its pair with s = 0
+                            tc::umma<kLowpF16>(acc_tmem + (uint32_t)((s + t) * CP),
                                                ad + (uint64_t)(2 * kk), bd + (uint64_t)(2 * kk),
-                                               prm.pc_idesc[pc],
-                                               (first && s == 0 && kk == 0) ? 0u : 1u);
+                                               prm.idesc, (first && s == 0 && kk == 0) ? 0u : 1u);
                         }
                     }
                     tc::umma_commit(a_empty(qa));
@@ -354,8 +359,9 @@ oz_product_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
         if (abort_flag) {
             // drain the copies still in flight (bounded)
             const int ai = a_issued, bi = b_issued;
-            for (int i = max(0, ai - kASlots); i < ai; ++i) {
-                tc::mbar_wait(a_full(i % kASlots), (uint32_t)((i / kASlots) & 1), err, 18, true);
+            for (int i = max(0, ai - prm.a_slots); i < ai; ++i) {
+                tc::mbar_wait(a_full(i % prm.a_slots), (uint32_t)((i / prm.a_slots) & 1), err, 18,
+                              true);
             }
             for (int i = max(0, bi - prm.b_slots); i < bi; ++i) {
                 tc::mbar_wait(b_full(i % prm.b_slots), (uint32_t)((i / prm.b_slots) & 1), err,
@@ -584,31 +590,18 @@ int OzProduct::apply_group(const double *X, long long ldx, int C, double *Y, lon
     }
     prm.maxslots = maxslots;
     prm.b_bytes = (uint32_t)(kOzSlices * cp * 128);
-    prm.b_slots = cp <= 32 ? oz::kMaxBSlots : 2;
+    prm.b_slots = oz::kMaxBSlots;
+    // as many A slices in flight as the shared memory holds (>= one chunk)
+    const size_t budget = 225u * 1024u - (size_t)prm.b_slots * prm.b_bytes;
+    prm.a_slots = (int)std::min<size_t>(oz::kMaxASlots, budget / oz::kABytes);
+    if (prm.a_slots < kOzSlices) return IPT_CUDA_INVALID_ARGUMENT;
     prm.acc_bufs = 2 * kOzSlices * cp <= 512 ? 2 : 1;
-    // MMA pieces: slice s multiplies B rows [0, (6 - s) cp) into TMEM
-    // columns [s cp, 6 cp), in pieces of at most 256 columns
-    const int per_piece = 256 / cp;
-    int np = 0;
-    for (int sl = 0; sl < kOzSlices; ++sl) {
-        for (int t0 = 0; t0 < kOzSlices - sl; t0 += per_piece) {
-            const int nt = std::min(per_piece, kOzSlices - sl - t0);
-            if (np >= oz::kMaxPieces) return IPT_CUDA_INVALID_ARGUMENT;
-            const int N = nt * cp;
-            prm.pc_s[np] = sl;
-            prm.pc_brow[np] = t0 * cp;
-            prm.pc_dcol[np] = (sl + t0) * cp;
-            prm.pc_idesc[np] = (1u << 4) | ((uint32_t)(N >> 3) << 17) |
-                               ((uint32_t)(oz::kBM >> 4) << 24);
-            ++np;
-        }
-    }
-    prm.pieces = np;
+    prm.idesc = (1u << 4) | ((uint32_t)(cp >> 3) << 17) | ((uint32_t)(oz::kBM >> 4) << 24);
     const size_t pneed = (size_t)tiles * maxslots * C * oz::kBM;
     if (P.count < pneed) IPTGB_CHECK(P.alloc(pneed, s));
-    const size_t smem = 1024 + (size_t)oz::kASlots * oz::kABytes +
+    const size_t smem = 1024 + (size_t)prm.a_slots * oz::kABytes +
                         (size_t)prm.b_slots * prm.b_bytes +
-                        (2 * oz::kASlots + 2 * oz::kMaxBSlots + 5) * 8 + 16;
+                        (2 * oz::kMaxASlots + 2 * oz::kMaxBSlots + 5) * 8 + 16;
 
     // X split: column maxima, then the digit slices (grids of about 4 CTAs per SM)
     IPTGB_CUDA(cudaMemsetAsync(colmax.ptr, 0, (size_t)cp * sizeof(unsigned long long), s));

@@ -398,10 +398,10 @@ struct DisjointSets {
 // Grow the cluster of the last requested target by its most strongly
 // coupled outside row while |H[row, col]| / gap > coupling_tau, taking the
 // degenerate neighbours along (IPT_C_GPU/src/ipt_cuda.cu:4134-4272).
-static void adaptive_expand(const int *col_ptr, const int *row_ind, const double *vals,
-                            const std::vector<double> &diag, int requested_k, int max_block,
-                            double tau, ClusterRanges *out)
+static void adaptive_expand(ClusterMatrixView &view, const std::vector<double> &diag,
+                            int requested_k, int max_block, double tau, ClusterRanges *out)
 {
+    std::vector<std::pair<int, double>> colv;
     const double eps_gap = 1.0e-14;
     const int n = (int)diag.size();
     auto &ranges = out->ranges;
@@ -423,11 +423,12 @@ static void adaptive_expand(const int *col_ptr, const int *row_ind, const double
         int best_row = -1;
         double best = 0.0;
         for (int col = first; col <= last; ++col) {
-            for (int p = col_ptr[col]; p < col_ptr[col + 1]; ++p) {
-                const int row = row_ind[p];
+            view.column(col, &colv);
+            for (const auto &ev : colv) {
+                const int row = ev.first;
                 if (first <= row && row <= last) continue;
                 const double gap = std::fabs(diag[(size_t)col] - diag[(size_t)row]);
-                const double ratio = std::fabs(vals[p]) / std::max(gap, eps_gap);
+                const double ratio = std::fabs(ev.second) / std::max(gap, eps_gap);
                 if (std::max(last, row) - std::min(first, row) + 1 > max_block) {
                     if (ratio > tau) out->limit_hit = 1;
                     continue;
@@ -504,16 +505,10 @@ struct GapScan {
     std::vector<int> order;
 };
 
-GapScan gap_scan(const int *col_ptr, const int *row_ind, const double *vals, int n,
-                 const std::vector<double> &diag, const GapOptions &o)
+// strongest off-diagonal entry of each row and column (ipt_preparation.cu:353-380)
+std::vector<double> offdiag_max(const int *col_ptr, const int *row_ind, const double *vals, int n)
 {
-    GapScan g;
-    double dmax = 0.0;
-    for (double v : diag) dmax = std::max(dmax, std::fabs(v));
-    g.tau_num = o.eps_multiplier * std::numeric_limits<double>::epsilon() * std::max(1.0, dmax);
-    // strongest off-diagonal entry of each row and column (ipt_preparation.cu:353-380)
-    std::vector<double> cs((size_t)n, 0.0), rs((size_t)n, 0.0);
-    g.off.resize((size_t)n);
+    std::vector<double> cs((size_t)n, 0.0), rs((size_t)n, 0.0), off((size_t)n);
     for (int c = 0; c < n; ++c) {
         for (int p = col_ptr[c]; p < col_ptr[c + 1]; ++p) {
             const int r = row_ind[p];
@@ -523,7 +518,18 @@ GapScan gap_scan(const int *col_ptr, const int *row_ind, const double *vals, int
             rs[(size_t)r] = std::max(rs[(size_t)r], a);
         }
     }
-    for (int i = 0; i < n; ++i) g.off[(size_t)i] = std::max(cs[(size_t)i], rs[(size_t)i]);
+    for (int i = 0; i < n; ++i) off[(size_t)i] = std::max(cs[(size_t)i], rs[(size_t)i]);
+    return off;
+}
+
+GapScan gap_scan_from(int n, const std::vector<double> &diag, std::vector<double> off,
+                      const GapOptions &o)
+{
+    GapScan g;
+    double dmax = 0.0;
+    for (double v : diag) dmax = std::max(dmax, std::fabs(v));
+    g.tau_num = o.eps_multiplier * std::numeric_limits<double>::epsilon() * std::max(1.0, dmax);
+    g.off = std::move(off);
     g.order.resize((size_t)n);
     std::iota(g.order.begin(), g.order.end(), 0);
     std::stable_sort(g.order.begin(), g.order.end(),
@@ -533,13 +539,32 @@ GapScan gap_scan(const int *col_ptr, const int *row_ind, const double *vals, int
     return g;
 }
 
+GapScan gap_scan(const int *col_ptr, const int *row_ind, const double *vals, int n,
+                 const std::vector<double> &diag, const GapOptions &o)
+{
+    return gap_scan_from(n, diag, offdiag_max(col_ptr, row_ind, vals, n), o);
+}
+
+// The view of host CSC arrays.
+struct HostCscView final : ClusterMatrixView {
+    const int *col_ptr;
+    const int *row_ind;
+    const double *vals;
+    HostCscView(const int *cp, const int *ri, const double *va) : col_ptr(cp), row_ind(ri), vals(va) {}
+    double entry(int row, int col) override { return csc_entry(col_ptr, row_ind, vals, row, col); }
+    void column(int col, std::vector<std::pair<int, double>> *e) override
+    {
+        e->clear();
+        for (int p = col_ptr[col]; p < col_ptr[col + 1]; ++p) e->emplace_back(row_ind[p], vals[p]);
+    }
+};
+
 // Calls join(row, col) for every target col < k and every other index row
 // whose gap to it is numerically zero or small against their coupling
 // (ipt_preparation.cu:383-455 and the candidate loops of :502-611, 658-757).
 template <class Join>
-void for_each_close_pair(const int *col_ptr, const int *row_ind, const double *vals, int n,
-                         const std::vector<double> &diag, int k, const GapOptions &o,
-                         const GapScan &g, Join join)
+void for_each_close_pair(ClusterMatrixView &view, int n, const std::vector<double> &diag, int k,
+                         const GapOptions &o, const GapScan &g, Join join)
 {
     for (int col = 0; col < std::min(k, n); ++col) {
         const double dc = diag[(size_t)col];
@@ -552,8 +577,8 @@ void for_each_close_pair(const int *col_ptr, const int *row_ind, const double *v
             const int row = g.order[q];
             if (row == col) continue;
             const double dr = diag[(size_t)row];
-            double coupling = std::max(std::fabs(csc_entry(col_ptr, row_ind, vals, row, col)),
-                                       std::fabs(csc_entry(col_ptr, row_ind, vals, col, row)));
+            double coupling = std::max(std::fabs(view.entry(row, col)),
+                                       std::fabs(view.entry(col, row)));
             if (!(coupling > 0.0)) {
                 coupling = o.eta * std::min(g.off[(size_t)row], g.off[(size_t)col]);
             }
@@ -568,15 +593,13 @@ void for_each_close_pair(const int *col_ptr, const int *row_ind, const double *v
 
 // The index ranges spanned by the groups of close indices that contain a
 // target, merged when they overlap or touch (ipt_preparation.cu:502-645).
-std::vector<std::pair<int, int>> degenerate_subspaces(const int *col_ptr, const int *row_ind,
-                                                      const double *vals, int n,
-                                                      const std::vector<double> &diag, int k,
+std::vector<std::pair<int, int>> degenerate_subspaces(ClusterMatrixView &view, int n,
+                                                      const std::vector<double> &diag,
+                                                      const GapScan &g, int k,
                                                       const GapOptions &o, int *too_large)
 {
-    const GapScan g = gap_scan(col_ptr, row_ind, vals, n, diag, o);
     DisjointSets sets(n);
-    for_each_close_pair(col_ptr, row_ind, vals, n, diag, k, o, g,
-                        [&](int row, int col) { sets.unite(row, col); });
+    for_each_close_pair(view, n, diag, k, o, g, [&](int row, int col) { sets.unite(row, col); });
     std::vector<int> cmin((size_t)n, n), cmax((size_t)n, -1), target((size_t)n, 0);
     for (int i = 0; i < n; ++i) {
         const int r = sets.find(i);
@@ -606,14 +629,26 @@ std::vector<std::pair<int, int>> degenerate_subspaces(const int *col_ptr, const 
     return merged;
 }
 
+std::vector<std::pair<int, int>> degenerate_subspaces_host(const int *col_ptr,
+                                                           const int *row_ind, const double *vals,
+                                                           int n, const std::vector<double> &diag,
+                                                           int k, const GapOptions &o,
+                                                           int *too_large)
+{
+    const GapScan g = gap_scan(col_ptr, row_ind, vals, n, diag, o);
+    HostCscView view(col_ptr, row_ind, vals);
+    return degenerate_subspaces(view, n, diag, g, k, o, too_large);
+}
+
 // Number of (target, index) pairs still close after lifting
 // (ipt_validate_target_gaps, ipt_preparation.cu:658-757).
 int target_gap_violations(const int *col_ptr, const int *row_ind, const double *vals, int n,
                           const std::vector<double> &diag, int k, const GapOptions &o)
 {
     const GapScan g = gap_scan(col_ptr, row_ind, vals, n, diag, o);
+    HostCscView view(col_ptr, row_ind, vals);
     int bad = 0;
-    for_each_close_pair(col_ptr, row_ind, vals, n, diag, k, o, g, [&](int, int) { ++bad; });
+    for_each_close_pair(view, n, diag, k, o, g, [&](int, int) { ++bad; });
     return bad;
 }
 
@@ -623,13 +658,24 @@ void cluster_ranges(const int *col_ptr, const int *row_ind, const double *vals, 
                     int requested_k, double degeneracy_threshold, int adaptive,
                     double coupling_tau, ClusterRanges *out)
 {
+    std::vector<double> diag;
+    csc_diagonal_sum(col_ptr, row_ind, vals, n, &diag);
+    HostCscView view(col_ptr, row_ind, vals);
+    cluster_ranges_from(view, n, diag, offdiag_max(col_ptr, row_ind, vals, n), k, requested_k,
+                        degeneracy_threshold, adaptive, coupling_tau, out);
+}
+
+void cluster_ranges_from(ClusterMatrixView &view, int n, const std::vector<double> &diag,
+                         const std::vector<double> &offmax, int k, int requested_k,
+                         double degeneracy_threshold, int adaptive, double coupling_tau,
+                         ClusterRanges *out)
+{
     *out = ClusterRanges();
     const GapOptions o = gap_options(degeneracy_threshold);
     out->max_block_size = o.max_block_size;
-    std::vector<double> diag;
-    csc_diagonal_sum(col_ptr, row_ind, vals, n, &diag);
+    const GapScan g = gap_scan_from(n, diag, offmax, o);
     std::vector<std::pair<int, int>> merged =
-        degenerate_subspaces(col_ptr, row_ind, vals, n, diag, k, o, &out->too_large);
+        degenerate_subspaces(view, n, diag, g, k, o, &out->too_large);
     // singleton clusters for the targets not covered (ipt_cuda.cu:4114-4132)
     std::vector<char> covered((size_t)n, 0);
     for (const auto &r : merged) {
@@ -641,8 +687,7 @@ void cluster_ranges(const int *col_ptr, const int *row_ind, const double *vals, 
     std::sort(merged.begin(), merged.end());
     out->ranges = merged;
     if (adaptive && !out->too_large) {
-        adaptive_expand(col_ptr, row_ind, vals, diag, requested_k, o.max_block_size,
-                        coupling_tau, out);
+        adaptive_expand(view, diag, requested_k, o.max_block_size, coupling_tau, out);
     }
 }
 
@@ -848,7 +893,8 @@ int lift_degeneracies(std::vector<int> *cp, std::vector<int> *ri, std::vector<do
         csc_diagonal_sum(cp->data(), ri->data(), va->data(), n, diag);
         int too_large = 0;
         const auto subspaces =
-            degenerate_subspaces(cp->data(), ri->data(), va->data(), n, *diag, k, o, &too_large);
+            degenerate_subspaces_host(cp->data(), ri->data(), va->data(), n, *diag, k, o,
+                                      &too_large);
         if (too_large) return IPT_CUDA_INVALID_ARGUMENT;
         if (subspaces.empty()) {
             clean = target_gap_violations(cp->data(), ri->data(), va->data(), n, *diag, k, o) == 0;

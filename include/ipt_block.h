@@ -150,6 +150,19 @@ int ipt_block_cluster_ranges(const int *col_ptr, const int *row_ind, const doubl
                              int adaptive, double coupling_tau, int *ranges, int capacity,
                              int *count, int *limit_hit);
 
+/* The same ranges from a device CSR (rows sorted by column without
+ * duplicates, symmetric, ascending diagonal: the prepared matrix of the
+ * block-cluster path), with the scans over the nonzeros on the GPU and the
+ * detection rules (IPT_C_GPU/src/ipt_preparation.cu:502-644,
+ * IPT_C_GPU/src/ipt_cuda.cu:4114-4272) on the host, which reads only the
+ * target rows and the rows the adaptive expansion visits.  Runs on `stream`
+ * and synchronises it. */
+int ipt_block_cluster_ranges_device(const int *d_row_ptr, const int *d_col_ind,
+                                    const double *d_vals, int n, int nnz, int k, int requested_k,
+                                    double degeneracy_threshold, int adaptive, double coupling_tau,
+                                    int *ranges, int capacity, int *count, int *limit_hit,
+                                    void *stream);
+
 /* Host only.  The plain sparse path's preparation, for checking (replaces
  * the static ipt_prepare_sparse_csc, IPT_C_GPU/src/ipt_preparation.cu:1375-1648):
  * validation, stable diagonal sort and symmetric permutation, then (lift != 0)

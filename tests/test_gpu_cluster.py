@@ -234,3 +234,81 @@ def test_block_cluster_entry_uneven_storage(cuda, monkeypatch, adaptive):
         scale = np.abs(Href).sum(1).max()
         np.testing.assert_allclose(v, w, atol=1e-9 * scale)
         assert np.abs(Href @ X - X * v).max() <= 1e-7 * scale
+
+
+def device_csr(torch, cp, ri, va):
+    """A symmetric CSC matrix is its own CSR: the three arrays on the GPU."""
+    return (torch.from_numpy(np.asarray(cp, np.int32)).cuda(),
+            torch.from_numpy(np.asarray(ri, np.int32)).cuda(),
+            torch.from_numpy(np.asarray(va, np.float64)).cuda())
+
+
+@pytest.mark.parametrize("adaptive", [False, True])
+def test_device_ranges_match_host(cuda, adaptive):
+    """ipt_block_cluster_ranges_device gives the host entry's ranges and
+    limit flag on seeded matrices with planted exact and near degeneracies,
+    weak to strong coupling, and several target counts."""
+    torch = cuda
+    multi = 0
+    for seed in range(10):
+        for coupling in (0.01, 0.3, 2.0):
+            n = 40 + 5 * seed
+            cp, ri, va, _ = oracle.cluster_test_matrix(n, seed, coupling)
+            drp, dci, dvv = device_csr(torch, cp, ri, va)
+            for k in (1, 4, 9):
+                for rk in sorted({1, k}):
+                    want = api.cluster_ranges(cp, ri, va, n, k, requested_k=rk,
+                                              adaptive=adaptive)
+                    got = api.cluster_ranges_device(drp.data_ptr(), dci.data_ptr(),
+                                                    dvv.data_ptr(), n, len(ri), k,
+                                                    requested_k=rk, adaptive=adaptive)
+                    assert got == want, (seed, coupling, k, rk)
+                    multi += any(b > a for a, b in want[0])
+    assert multi >= 10
+
+
+def test_device_ranges_match_reference_fixtures(cuda):
+    """The committed fixtures of the reference's own detection: the device
+    entry finds its ranges on every prepared matrix."""
+    torch = cuda
+    kat = np.load(GOLDEN)
+    for c in [str(x) for x in kat["cases"]]:
+        k, adaptive = int(kat[c + "_params"][0]), int(kat[c + "_params"][1])
+        cp, ri, va = kat[c + "_prep_col_ptr"], kat[c + "_prep_row_ind"], kat[c + "_prep_values"]
+        drp, dci, dvv = device_csr(torch, cp, ri, va)
+        got, lim = api.cluster_ranges_device(drp.data_ptr(), dci.data_ptr(), dvv.data_ptr(),
+                                             cp.size - 1, len(ri), k, adaptive=bool(adaptive))
+        assert got == [tuple(r) for r in kat[c + "_ranges"].tolist()], c
+        assert int(lim) == int(kat[c + "_limit_hit"][0]), c
+
+
+def test_device_ranges_large_sparse(cuda):
+    """A 200000-row banded matrix with a planted degenerate group: the device
+    scans and the host entry agree."""
+    torch = cuda
+    sp = pytest.importorskip("scipy.sparse")
+    n, k = 200000, 12
+    rng = np.random.default_rng(3)
+    d = np.sort(rng.uniform(0, 100, n))
+    d[3:6] = d[3]
+    off = rng.normal(scale=0.05, size=n - 1)
+    H = sp.diags([off, d, off], [-1, 0, 1], format="csc")
+    H.sort_indices()
+    want = api.cluster_ranges(H.indptr, H.indices, H.data, n, k, adaptive=True)
+    drp, dci, dvv = device_csr(torch, H.indptr, H.indices, H.data)
+    got = api.cluster_ranges_device(drp.data_ptr(), dci.data_ptr(), dvv.data_ptr(), n,
+                                    int(H.nnz), k, adaptive=True)
+    assert got == want
+    assert any(b > a for a, b in got[0])
+
+
+def test_device_ranges_invalid_arguments(cuda):
+    torch = cuda
+    cp, ri, va, _ = oracle.cluster_test_matrix(30, 1, 0.1)
+    drp, dci, dvv = device_csr(torch, cp, ri, va)
+    for k, rk in ((0, 1), (31, 1), (4, 5), (4, 0)):
+        with pytest.raises(RuntimeError):
+            api.cluster_ranges_device(drp.data_ptr(), dci.data_ptr(), dvv.data_ptr(), 30,
+                                      len(ri), k, requested_k=rk)
+    with pytest.raises(RuntimeError):
+        api.cluster_ranges_device(0, dci.data_ptr(), dvv.data_ptr(), 30, len(ri), 4)

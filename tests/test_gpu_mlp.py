@@ -146,7 +146,9 @@ def test_learned_correction_beats_plain_on_held_out(cuda, trained):
     rows = torch.empty((1_500_000, 8), dtype=torch.float32, device="cuda")
     got = learned.collect(torch, csr, 16, rows, 0)
     plain, neumann, mlp = learned.correction_losses(torch, params, rows, got)
-    assert mlp < 0.8 * plain, (plain, neumann, mlp)
+    # the network weighs the second-order term per row: closer than both the
+    # plain first-order correction and the unweighted two-term series
+    assert mlp < 0.9 * plain and mlp < neumann, (plain, neumann, mlp)
     del rows
     for spec in ((8, 4, 4, 9), (10, 5, 5, 4)):
         csr = learned.device_csr(torch, *spec)
