@@ -68,17 +68,9 @@ struct Params {
     uint32_t idesc;  // M = 128, N = cp, FP16 x FP16 -> FP32
 };
 
-// CTA that owns item x when `items` items are split into G contiguous ranges
-// [floor(b items / G), floor((b + 1) items / G)).
-__host__ __device__ __forceinline__ long long owner_of(long long x, long long items, long long G)
-{
-    return ((x + 1) * G + items - 1) / items - 1;
-}
+using tc::owner_of;
 
-__device__ __forceinline__ void mbar_arrive(uint32_t bar)
-{
-    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
-}
+using tc::mbar_arrive;
 
 __device__ __forceinline__ void two_sum(float a, float b, float &s, float &e)
 {
@@ -583,8 +575,8 @@ int OzProduct::apply_group(const double *X, long long ldx, int C, double *Y, lon
     const int grid = (int)std::min<long long>(sms, prm.items);
     int maxslots = 1;
     for (int t = 0; t < tiles; ++t) {
-        const long long f = oz::owner_of((long long)t * prm.periods, prm.items, grid);
-        const long long l = oz::owner_of((long long)t * prm.periods + prm.periods - 1, prm.items,
+        const long long f = tc::owner_of((long long)t * prm.periods, prm.items, grid);
+        const long long l = tc::owner_of((long long)t * prm.periods + prm.periods - 1, prm.items,
                                          grid);
         maxslots = std::max(maxslots, (int)(l - f + 1));
     }

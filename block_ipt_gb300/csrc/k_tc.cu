@@ -224,6 +224,229 @@ tc_partial_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
     }
 }
 
+// ---------------------------------------------------------------------------
+// Persistent (stream-K) form of the same product: G CTAs (one per SM) walk
+// contiguous ranges of the (128-row tile, K chunk) items, so every SM
+// streams the same number of Delta bytes whatever the tile count, through
+// a deeper TMA ring than the split-K grid can hold.  A CTA's range crosses
+// tile boundaries: each piece of a tile it covers (a segment) accumulates
+// in one of two TMEM accumulators, so the MMAs of the next segment run
+// while the epilogue warps drain the last one into partial slot
+// (CTA - first CTA of the tile) of that tile.  The slots a tile never uses
+// are never written (the caller zeroes them once), so the update sums a
+// fixed number of slots in a fixed order, as for split-K.
+// Warps 0-3 epilogue, warp 4 TMA producer, warp 5 MMA issuer.
+// ---------------------------------------------------------------------------
+constexpr int kStreamThreads = 192;
+constexpr int kStreamProducer = 4;
+constexpr int kStreamMma = 5;
+
+struct StreamParams {
+    int n, p, p_pad, stages;
+    int acc_cols;    // TMEM columns of one accumulator
+    int acc_bufs;    // accumulators (2: drain one while the other fills)
+    int tmem_cols;   // allocation (power of two >= acc_bufs * acc_cols)
+    int chunks;      // K chunks per tile
+    int kchunk;      // elements per K chunk (128 bytes)
+    long long items; // tiles * chunks
+    uint32_t idesc;
+};
+
+template <int KIND>
+__global__ void __launch_bounds__(kStreamThreads, 1)
+tc_stream_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+                 const __grid_constant__ StreamParams prm, float *__restrict__ P, int *err,
+                 float a_keep, const double *hist, int step, double stop_tol, long long spin)
+{
+    if (hist != nullptr) {
+        pdl_wait();
+        if (hist_stopped(hist, step, stop_tol)) return;
+    }
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t *smem = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
+    const int stages = prm.stages;
+    const uint32_t a_bytes = kBM * kRowBytes;
+    const uint32_t stage_bytes = a_bytes + (uint32_t)prm.p_pad * kRowBytes;
+    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + (size_t)stages * stage_bytes);
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 2 * stages + 5);
+    __shared__ volatile int abort_flag;
+    __shared__ int issued_count;
+
+    const int warp = threadIdx.x >> 5;
+    const int lane = threadIdx.x & 31;
+    const long long G = gridDim.x;
+    const long long it0 = (long long)blockIdx.x * prm.items / G;
+    const long long it1 = ((long long)blockIdx.x + 1) * prm.items / G;
+    const uint32_t smem_base = smem_u32(smem);
+    const uint32_t bar0 = smem_u32(bars);
+    auto full_bar = [&](int q) { return bar0 + 8u * (uint32_t)q; };
+    auto empty_bar = [&](int q) { return bar0 + 8u * (uint32_t)(stages + q); };
+    auto acc_full = [&](int b) { return bar0 + 8u * (uint32_t)(2 * stages + b); };
+    auto acc_empty = [&](int b) { return bar0 + 8u * (uint32_t)(2 * stages + 2 + b); };
+    const uint32_t mma_done = bar0 + 8u * (uint32_t)(2 * stages + 4);
+
+    if (threadIdx.x == 0) {
+        for (int q = 0; q < stages; ++q) {
+            mbar_init(full_bar(q), 1);
+            mbar_init(empty_bar(q), 1);
+        }
+        for (int b = 0; b < 2; ++b) {
+            mbar_init(acc_full(b), 1);
+            mbar_init(acc_empty(b), 4);  // one arrival per epilogue warp
+        }
+        mbar_init(mma_done, 1);
+        abort_flag = 0;
+        issued_count = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    if (warp == kStreamProducer) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                         smem_u32(tmem_slot)),
+                     "r"(prm.tmem_cols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = *tmem_slot;
+    const int count = (int)(it1 - it0);
+
+    if (warp == kStreamProducer && lane == 0) {
+        const uint64_t a_pol = a_keep > 0.0f ? l2_keep_policy(fminf(a_keep, 1.0f)) : 0ull;
+        auto load_a = [&](int q, long long it) {
+            const int tile = (int)(it / prm.chunks);
+            const int kx = (int)(it - (long long)tile * prm.chunks) * prm.kchunk;
+            const uint32_t sa = smem_base + (uint32_t)q * stage_bytes;
+            if (a_keep > 0.0f) {
+                tma_load_2d_hint(sa, &tmA, kx, tile * kBM, full_bar(q), a_pol);
+            } else {
+                tma_load_2d(sa, &tmA, kx, tile * kBM, full_bar(q));
+            }
+        };
+        auto load_b = [&](int q, long long it) {
+            const int kx = (int)(it % prm.chunks) * prm.kchunk;
+            tma_load_2d(smem_base + (uint32_t)q * stage_bytes + a_bytes, &tmB, kx, 0,
+                        full_bar(q));
+        };
+        // Delta does not depend on the preceding kernel: the first stages'
+        // Delta tiles are requested before waiting for the grid that wrote X
+        const int pre = min(stages, count);
+        for (int q = 0; q < pre; ++q) {
+            mbar_expect_tx(full_bar(q), stage_bytes);
+            load_a(q, it0 + q);
+        }
+        pdl_wait();
+        for (int q = 0; q < pre; ++q) load_b(q, it0 + q);
+        int i = pre;
+        for (; i < count; ++i) {
+            const int q = i % stages;
+            if (!mbar_wait(empty_bar(q), (uint32_t)((i / stages - 1) & 1), err, 21, false, spin)) {
+                abort_flag = 1;
+                break;
+            }
+            if (abort_flag) break;
+            mbar_expect_tx(full_bar(q), stage_bytes);
+            load_a(q, it0 + i);
+            load_b(q, it0 + i);
+        }
+        issued_count = i;
+        pdl_trigger();
+    } else if (warp == kStreamMma && lane == 0) {
+        int i = 0, seg = 0;
+        for (long long it = it0; it < it1 && !abort_flag; ++seg) {
+            const long long tile = it / prm.chunks;
+            const long long seg_end = min(it1, (tile + 1) * prm.chunks);
+            const int ab = seg % prm.acc_bufs;
+            const int use = seg / prm.acc_bufs;
+            if (use > 0 &&
+                !mbar_wait(acc_empty(ab), (uint32_t)((use - 1) & 1), err, 22, false, spin)) {
+                abort_flag = 1;
+                break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const uint32_t acc = tmem + (uint32_t)(ab * prm.acc_cols);
+            const long long seg_start = it;
+            for (; it < seg_end; ++it, ++i) {
+                const int q = i % stages;
+                if (!mbar_wait(full_bar(q), (uint32_t)((i / stages) & 1), err, 23, false, spin)) {
+                    abort_flag = 1;
+                    break;
+                }
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                const uint32_t sa = smem_base + (uint32_t)q * stage_bytes;
+                const uint64_t ad = sw128_desc(sa);
+                const uint64_t bd = sw128_desc(sa + a_bytes);
+#pragma unroll
+                for (int kk = 0; kk < 4; ++kk) {
+                    umma<KIND>(acc, ad + (uint64_t)(2 * kk), bd + (uint64_t)(2 * kk), prm.idesc,
+                               (it > seg_start || kk > 0) ? 1u : 0u);
+                }
+                umma_commit(empty_bar(q));
+            }
+            if (abort_flag) break;
+            umma_commit(acc_full(ab));
+        }
+        umma_commit(mma_done);
+    } else if (warp < 4) {
+        // ---- epilogue: one segment at a time, TMEM -> partial slot ----
+        int seg = 0;
+        for (long long it = it0; it < it1; ++seg) {
+            const long long tile = it / prm.chunks;
+            const long long seg_end = min(it1, (tile + 1) * prm.chunks);
+            it = seg_end;
+            const int ab = seg % prm.acc_bufs;
+            const bool ok0 =
+                mbar_wait(acc_full(ab), (uint32_t)((seg / prm.acc_bufs) & 1), err, 24, true, spin);
+            // warp-uniform: the TMEM loads below are warp-collective
+            if (__any_sync(0xffffffffu, !ok0 || abort_flag)) {
+                abort_flag = 1;
+                break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const long long slot = (long long)blockIdx.x - owner_of(tile * prm.chunks, prm.items, G);
+            const int row = (int)tile * kBM + warp * 32 + lane;
+            float *dst = P + (size_t)slot * prm.p * (size_t)prm.n + row;
+            const uint32_t lane_addr =
+                tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(ab * prm.acc_cols);
+            for (int cb = 0; cb < prm.p_pad; cb += 32) {
+                float v[32];
+                tmem_ld_32cols(lane_addr + (uint32_t)cb, v);
+                if (row < prm.n) {
+#pragma unroll
+                    for (int j = 0; j < 32; ++j) {
+                        if (cb + j < prm.p) dst[(size_t)(cb + j) * prm.n] = v[j];
+                    }
+                }
+            }
+            asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+            __syncwarp();
+            if (lane == 0) mbar_arrive(acc_empty(ab));
+        }
+    }
+    __syncwarp();
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == kStreamProducer && lane == 0) {
+        // every MMA this CTA issued has completed before TMEM is released
+        mbar_wait(mma_done, 0u, err, 25, true);
+        if (abort_flag) {
+            // the copies still in flight (bounded)
+            const int issued = issued_count;
+            for (int i = max(0, issued - stages); i < issued; ++i) {
+                mbar_wait(full_bar(i % stages), (uint32_t)((i / stages) & 1), err, 26, true);
+            }
+        }
+    }
+    __syncthreads();
+    if (warp == kStreamProducer) {
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                     "r"(prm.tmem_cols)
+                     : "memory");
+    }
+}
+
 }  // namespace tc
 
 // FP32 storage of a TF32 tensor-core operand (values pre-rounded to TF32).
@@ -1147,6 +1370,13 @@ struct LowpDense final : LowpDenseOperator {
             splits = std::min(forced, chunks_total);
         }
         const int forced_stages = env_int("IPT_GB300_TC_STAGES", 0);
+        const int afmt = LowpTypes<LP>::kind == kLowpF16 ? 0 : (LowpTypes<LP>::kind == kLowpBF16 ? 1 : 2);
+        idesc = (1u << 4) | ((uint32_t)afmt << 7) | ((uint32_t)afmt << 10) |
+                ((uint32_t)(p_pad >> 3) << 17) | ((uint32_t)(tc::kBM >> 4) << 24);
+        // persistent stream-K schedule (tuning knob IPT_GB300_TC_STREAMK=0:
+        // the split-K grid below)
+        streamk = env_int("IPT_GB300_TC_STREAMK", 1) != 0;
+        if (streamk) return set_width_streamk(row_blocks, forced_stages);
         chunks_per_split = (chunks_total + splits - 1) / splits;
         splits = (chunks_total + chunks_per_split - 1) / chunks_per_split;
         const size_t stage_bytes = (size_t)(tc::kBM + p_pad) * tc::kRowBytes;
@@ -1159,10 +1389,58 @@ struct LowpDense final : LowpDenseOperator {
         }
         if (stages < 2) return IPT_CUDA_INVALID_ARGUMENT;
         smem_bytes = 1024 + stages * stage_bytes + (2 * stages + 1) * 8 + 16;
-        const int afmt = LowpTypes<LP>::kind == kLowpF16 ? 0 : (LowpTypes<LP>::kind == kLowpBF16 ? 1 : 2);
-        idesc = (1u << 4) | ((uint32_t)afmt << 7) | ((uint32_t)afmt << 10) |
-                ((uint32_t)(p_pad >> 3) << 17) | ((uint32_t)(tc::kBM >> 4) << 24);
         IPTGB_CHECK(P.alloc((size_t)splits * p * n, s));
+        IPTGB_CHECK(alloc_blocks());
+        auto kfn = tc::tc_partial_kernel<LowpTypes<LP>::kind>;
+        IPTGB_CUDA(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)smem_bytes));
+        cur = 0;
+        return IPT_CUDA_SUCCESS;
+    }
+
+    // One CTA per SM, each walking an equal contiguous share of the (tile,
+    // K chunk) items with a TMA ring as deep as shared memory allows; the
+    // partial slots of a tile are the CTAs its items span (at most
+    // `splits`), the unused ones zeroed here once.
+    int set_width_streamk(int row_blocks, int forced_stages)
+    {
+        const size_t stage_bytes = (size_t)(tc::kBM + p_pad) * tc::kRowBytes;
+        stages = (int)std::min<size_t>(12, (216u * 1024u) / stage_bytes);
+        if (forced_stages >= 2) stages = std::min(stages, forced_stages);
+        if (stages < 2) return IPT_CUDA_INVALID_ARGUMENT;
+        sprm = tc::StreamParams{};
+        sprm.n = n;
+        sprm.p = p;
+        sprm.p_pad = p_pad;
+        sprm.stages = stages;
+        sprm.acc_cols = tmem_cols;
+        sprm.acc_bufs = 2 * tmem_cols <= 512 ? 2 : 1;
+        sprm.tmem_cols = sprm.acc_bufs * tmem_cols;
+        sprm.chunks = chunks_total;
+        sprm.kchunk = (int)kchunk;
+        sprm.items = (long long)row_blocks * chunks_total;
+        sprm.idesc = idesc;
+        grid_g = (int)std::min<long long>(sms, sprm.items);
+        splits = 1;
+        for (int t = 0; t < row_blocks; ++t) {
+            const long long f = tc::owner_of((long long)t * chunks_total, sprm.items, grid_g);
+            const long long l =
+                tc::owner_of((long long)t * chunks_total + chunks_total - 1, sprm.items, grid_g);
+            splits = std::max(splits, (int)(l - f + 1));
+        }
+        smem_bytes = 1024 + stages * stage_bytes + (2 * stages + 5) * 8 + 16;
+        IPTGB_CHECK(P.alloc((size_t)splits * p * n, s));
+        IPTGB_CUDA(cudaMemsetAsync(P.ptr, 0, (size_t)splits * p * n * sizeof(float), s));
+        IPTGB_CHECK(alloc_blocks());
+        auto kfn = tc::tc_stream_kernel<LowpTypes<LP>::kind>;
+        IPTGB_CUDA(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)smem_bytes));
+        cur = 0;
+        return IPT_CUDA_SUCCESS;
+    }
+
+    int alloc_blocks()
+    {
         for (int b = 0; b < 2; ++b) {
             IPTGB_CHECK(Xlp[b].alloc((size_t)ldp * p_pad, s));
             IPTGB_CUDA(cudaMemsetAsync(Xlp[b].ptr, 0, (size_t)ldp * p_pad * sizeof(LP), s));
@@ -1170,10 +1448,6 @@ struct LowpDense final : LowpDenseOperator {
             IPTGB_CHECK(X32[b].alloc((size_t)n * p, s));
         }
         IPTGB_CHECK(G.alloc((size_t)n * p, s));
-        auto kfn = tc::tc_partial_kernel<LowpTypes<LP>::kind>;
-        IPTGB_CUDA(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        (int)smem_bytes));
-        cur = 0;
         return IPT_CUDA_SUCCESS;
     }
 
@@ -1203,9 +1477,14 @@ struct LowpDense final : LowpDenseOperator {
     // hist/step/tol: the device-side stop of the running iteration (or null)
     int product_until(const double *hist, int step, double tol)
     {
+        KernelTimerScope timer(kProfLowpProduct, s);
+        if (streamk) {
+            return launch_pdl(tc::tc_stream_kernel<LowpTypes<LP>::kind>, dim3(grid_g),
+                              dim3(tc::kStreamThreads), smem_bytes, s, mapA, mapB[cur], sprm,
+                              P.ptr, err.ptr, a_keep, hist, step, tol, spin);
+        }
         const int row_blocks = (n + tc::kBM - 1) / tc::kBM;
         dim3 grid(row_blocks, splits);
-        KernelTimerScope timer(kProfLowpProduct, s);
         return launch_pdl(tc::tc_partial_kernel<LowpTypes<LP>::kind>, grid, dim3(tc::kThreads),
                           smem_bytes, s, mapA, mapB[cur], n, p, p_pad, stages, tmem_cols,
                           chunks_total, chunks_per_split, (int)kchunk, idesc, P.ptr, err.ptr,
@@ -1317,6 +1596,9 @@ struct LowpDense final : LowpDenseOperator {
     int splits = 1, stages = 2, cur = 0;
     size_t smem_bytes = 0;
     uint32_t idesc = 0;
+    bool streamk = false;
+    int grid_g = 0;
+    tc::StreamParams sprm{};
     double scale = 1.0;
     float a_keep = 0.0f;  // fraction of Delta kept in L2 (evict_last) across products
     // polls of a pipeline wait before the kernel gives up (tuning and test

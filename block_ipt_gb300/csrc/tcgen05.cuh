@@ -19,6 +19,14 @@ namespace tc {
 // Polls of an mbarrier before a wait gives up and reports an error.
 constexpr long long kSpinLimit = 1LL << 24;
 
+// Persistent (stream-K) schedules: `items` work items are split into G
+// contiguous ranges [floor(b items / G), floor((b + 1) items / G)); the CTA
+// that owns item x.
+__host__ __device__ __forceinline__ long long owner_of(long long x, long long items, long long G)
+{
+    return ((x + 1) * G + items - 1) / items - 1;
+}
+
 __device__ __forceinline__ uint32_t smem_u32(const void *p)
 {
     return (uint32_t)__cvta_generic_to_shared(p);
@@ -33,6 +41,11 @@ __device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes)
 {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
                  : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint32_t bar)
+{
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
 }
 
 __device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity)
