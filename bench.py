@@ -552,8 +552,10 @@ def batch_section(args, torch, dev):
     """The batched dense workload: 512 independent instances, n ~ U{64..2048},
     k ~ U{4..16}, sigma ~ U(0.01, 0.1), configs[0] construction per instance
     (generated on the device, same hashes as block_ipt_gb300.workloads), solved
-    by the persistent batched kernel replayed as one CUDA graph, FP64 and
-    mixed (FP32 sweeps then FP64 certification), launch shape autotuned."""
+    by the persistent batched kernel replayed as one CUDA graph, launch shape
+    autotuned: FP64 sweeps on the FP64 pipe, the same sweeps in double-float
+    arithmetic, and mixed (FP32 sweeps, then double-float or FP64-pipe
+    certifying sweeps)."""
     from block_ipt_gb300 import api, workloads
     specs = workloads.batch_config2(args.batch, seed=args.seed)
     bufs, inst = [], []
@@ -570,8 +572,12 @@ def batch_section(args, torch, dev):
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     stream = torch.cuda.current_stream(dev)
-    for prec in ("fp64", "fp32"):
-        plan = api.BatchPlan(inst, prec)
+    from block_ipt_gb300 import _lib
+    for name, prec, cert in (("fp64", "fp64", _lib.IPT_BLOCK_FP64),
+                             ("fp64_double_float", "fp64", _lib.IPT_BLOCK_DF64),
+                             ("mixed", "fp32", _lib.IPT_BLOCK_DF64),
+                             ("mixed_fp64_certify", "fp32", _lib.IPT_BLOCK_FP64)):
+        plan = api.BatchPlan(inst, prec, certify_precision=cert)
         threads, chunk, _ = plan.autotune(stream.cuda_stream)
         plan.run(stream.cuda_stream)
         times = []
@@ -585,7 +591,7 @@ def batch_section(args, torch, dev):
         plan.close()
         lat = np.array([r["latency_ms"] for r in reps])
         ms = statistics.median(times)
-        out["fp64" if prec == "fp64" else "mixed"] = {
+        out[name] = {
             "ms_per_batch": ms, "instances_per_s": len(specs) / (ms * 1e-3),
             "p50_latency_ms": float(np.percentile(lat, 50)),
             "p99_latency_ms": float(np.percentile(lat, 99)),

@@ -24,6 +24,7 @@ IPT_BLOCK_FP16 = 1
 IPT_BLOCK_BF16 = 2
 IPT_BLOCK_TF32 = 3
 IPT_BLOCK_FP32 = 4
+IPT_BLOCK_DF64 = 5
 IPT_BLOCK_STRATEGY_REFINE = 0
 IPT_BLOCK_STRATEGY_DAVIDSON = 1
 IPT_BLOCK_PRECOND_DIAGONAL = 0
@@ -182,7 +183,7 @@ class IPTBatchInstance(C.Structure):
 class IPTBatchOptions(C.Structure):
     _fields_ = [("precision", C.c_int), ("residual_tol", C.c_double), ("maxiter", C.c_int),
                 ("lowp_maxiter", C.c_int), ("lowp_tol", C.c_double), ("threads", C.c_int),
-                ("chunk", C.c_int)]
+                ("chunk", C.c_int), ("certify_precision", C.c_int)]
 
 
 class IPTBatchReport(C.Structure):

@@ -17,10 +17,16 @@
 //
 // Mixed precision: the sweeps first run the product in FP32 (H converted on
 // load, X staged in FP32, FP32 accumulation) until the fixed-point residual
-// ||X' - X||_F / ||X||_F reaches lowp_tol, then switch to FP64 sweeps, which
-// certify and refine the block (the reference's mixed scheme: low-precision
-// IPT, then FP64 IPT; IPT_C_GPU/src/mixed_precision/
-// ipt_mixed_precision_cuda.cu:1153-1225).
+// ||X' - X||_F / ||X||_F reaches lowp_tol, then switch to FP64-accurate
+// sweeps, which certify and refine the block (the reference's mixed scheme:
+// low-precision IPT, then FP64 IPT; IPT_C_GPU/src/mixed_precision/
+// ipt_mixed_precision_cuda.cu:1153-1225).  Those run on the FP64 pipe or, by
+// default after FP32 sweeps, in double-float arithmetic on the FP32 pipe:
+// every H entry split once into an exact (hi, lo) float pair on the integer
+// pipe, X staged as (hi, lo) pairs, each term accumulated by an exact
+// two-product and two-sum (12 FP32 operations, about 2^-48 relative), so
+// that a sweep costs about a fifth of its FP64-pipe time on GB300, whose
+// FP64 pipe retires 1/64 of the FP32 rate.
 //
 // Scheduling: one CTA per instance at a time; CTAs take instances from a
 // device counter in descending order of cost n^2 k (longest first), so the
@@ -37,6 +43,7 @@
 #include <vector>
 
 #include "common.cuh"
+#include "dfloat.cuh"
 #include "reduce.cuh"
 
 #define IPT_API extern "C" __attribute__((visibility("default")))
@@ -74,6 +81,7 @@ struct Params {
     int *counter;
     Out *out;
     int mixed;
+    int certify_df;  // FP64-accurate sweeps in double-float (FP32 pipe)
     double tol;
     int maxiter;
     int lowp_maxiter;
@@ -126,6 +134,60 @@ __device__ double product(const Inst &I, const double *__restrict__ X, T *xs, bo
 #pragma unroll
             for (int j = 0; j < kKMax; ++j) {
                 if (j < k) I.y[(size_t)i * k + j] = (double)acc[j];
+            }
+            hinf = fmax(hinf, rs);
+        }
+    }
+    return hinf;
+}
+
+// Y = H X in double-float arithmetic (see the file header); with `rowsum`,
+// also the largest absolute row sum of H.
+template <int L>
+__device__ double product_df(const Inst &I, const double *__restrict__ X, float2 *xs, bool rowsum)
+{
+    const int n = I.n, k = I.k;
+    const int tid = threadIdx.x;
+    double hinf = 0.0;
+    for (int rb = 0; rb < n; rb += blockDim.x) {
+        const int i = rb + tid;
+        float S[kKMax], e[kKMax];
+#pragma unroll
+        for (int j = 0; j < kKMax; ++j) {
+            S[j] = 0.0f;
+            e[j] = 0.0f;
+        }
+        double rs = 0.0;
+        for (int l0 = 0; l0 < n; l0 += L) {
+            const int lc = min(L, n - l0);
+            __syncthreads();
+            for (int q = tid; q < L * kKMax; q += blockDim.x) {
+                const int l = q / kKMax;
+                const int j = q - l * kKMax;
+                float2 v = make_float2(0.0f, 0.0f);
+                if (l < lc && j < k) {
+                    const dfloat d = df_from_double(X[(size_t)(l0 + l) * k + j]);
+                    v = make_float2(d.hi, d.lo);
+                }
+                xs[q] = v;
+            }
+            __syncthreads();
+            if (i < n) {
+                const double *hc = I.H + (size_t)l0 * n + i;
+                for (int l = 0; l < lc; ++l) {
+                    const double hd = hc[(size_t)l * n];
+                    if (rowsum) rs += fabs(hd);
+                    const dfloat h = df_from_double(hd);
+                    const float2 *xr = xs + l * kKMax;
+#pragma unroll
+                    for (int j = 0; j < kKMax; ++j) df_acc(S[j], e[j], h.hi, h.lo, xr[j].x, xr[j].y);
+                }
+            }
+        }
+        if (i < n) {
+#pragma unroll
+            for (int j = 0; j < kKMax; ++j) {
+                if (j < k) I.y[(size_t)i * k + j] = (double)S[j] + (double)e[j];
             }
             hinf = fmax(hinf, rs);
         }
@@ -187,7 +249,9 @@ batch_ipt_kernel(Params p)
             __syncthreads();
             if (tid < 3 * kKMax + 3) sums[tid] = 0.0;
             double hs;
-            if (fp64) {
+            if (fp64 && p.certify_df) {
+                hs = product_df<L>(I, X, reinterpret_cast<float2 *>(xs64), hinf < 0.0);
+            } else if (fp64) {
                 hs = product<double, L>(I, X, xs64, hinf < 0.0);
             } else {
                 hs = product<float, L>(I, X, xs32, hinf < 0.0);
@@ -321,6 +385,7 @@ struct BatchPlan {
     batch::Out *out = nullptr;
     double *pool = nullptr;
     int mixed = 0;
+    int certify_df = 0;
     double tol = 1e-8;
     int maxiter = 100;
     int lowp_maxiter = 200;
@@ -334,8 +399,8 @@ struct BatchPlan {
 
     int launch(cudaStream_t s)
     {
-        batch::Params p{inst, order, count, counter, out, mixed, tol, maxiter, lowp_maxiter,
-                        lowp_tol};
+        batch::Params p{inst, order, count, counter, out, mixed, certify_df, tol, maxiter,
+                        lowp_maxiter, lowp_tol};
         IPTGB_CUDA(cudaMemsetAsync(counter, 0, sizeof(int), s));
         if (chunk == 64) {
             batch::batch_ipt_kernel<64><<<ctas, threads, 0, s>>>(p);
@@ -408,6 +473,7 @@ IPT_API void ipt_block_batch_default_options(IPTBatchOptions *o)
     o->lowp_tol = 1e-6;
     o->threads = 0;
     o->chunk = 0;
+    o->certify_precision = -1;
 }
 
 IPT_API int ipt_block_batch_plan_create(const IPTBatchInstance *instances, int count,
@@ -422,7 +488,9 @@ IPT_API int ipt_block_batch_plan_create(const IPTBatchInstance *instances, int c
     if ((opt.precision != IPT_BLOCK_FP64 && opt.precision != IPT_BLOCK_FP32) ||
         !(opt.residual_tol > 0.0) || opt.maxiter <= 0 || opt.lowp_maxiter < 0 ||
         (opt.threads != 0 && opt.threads != 128 && opt.threads != 256 && opt.threads != 512) ||
-        (opt.chunk != 0 && opt.chunk != 64 && opt.chunk != 128)) {
+        (opt.chunk != 0 && opt.chunk != 64 && opt.chunk != 128) ||
+        (opt.certify_precision != -1 && opt.certify_precision != IPT_BLOCK_FP64 &&
+         opt.certify_precision != IPT_BLOCK_DF64)) {
         return IPT_CUDA_INVALID_ARGUMENT;
     }
     size_t pool = 0;
@@ -437,6 +505,8 @@ IPT_API int ipt_block_batch_plan_create(const IPTBatchInstance *instances, int c
     auto *P = new BatchPlan();
     P->count = count;
     P->mixed = opt.precision == IPT_BLOCK_FP32 ? 1 : 0;
+    P->certify_df = opt.certify_precision == IPT_BLOCK_DF64 ||
+                    (opt.certify_precision == -1 && P->mixed);
     P->tol = opt.residual_tol;
     P->maxiter = opt.maxiter;
     P->lowp_maxiter = opt.lowp_maxiter;

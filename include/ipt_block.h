@@ -37,7 +37,9 @@ enum {
     IPT_BLOCK_FP16 = 1, /* FP16 tensor cores (tcgen05), FP32 accumulation */
     IPT_BLOCK_BF16 = 2, /* BF16 tensor cores (tcgen05), FP32 accumulation */
     IPT_BLOCK_TF32 = 3, /* TF32 tensor cores (tcgen05), FP32 accumulation */
-    IPT_BLOCK_FP32 = 4  /* FP32 SIMT sweeps, then FP64 (batched solver only) */
+    IPT_BLOCK_FP32 = 4, /* FP32 SIMT sweeps, then FP64 (batched solver only) */
+    IPT_BLOCK_DF64 = 5  /* FP64-accurate double-float arithmetic on the FP32 pipe
+                           (batched solver's certifying sweeps only) */
 };
 
 /* Solver strategy.  REFINE (default): IPT fixed point refined to the FP64
@@ -350,7 +352,10 @@ int ipt_block_mlp_collect_csr(const int *d_row_ptr, const int *d_col_ind,
  * the scaled eigen-residual residual_tol (residuals r_j = H x_j - (HX)_jj x_j,
  * the IPT map's own) and returning the certified block and its Rayleigh
  * quotients x_j^T H x_j / x_j^T x_j.  precision IPT_BLOCK_FP32 runs FP32
- * sweeps to lowp_tol first, then the FP64 sweeps.  The plan owns all
+ * sweeps to lowp_tol first, then the FP64-accurate sweeps; those run on the
+ * FP64 pipe (certify_precision IPT_BLOCK_FP64) or in double-float arithmetic
+ * on the FP32 pipe (IPT_BLOCK_DF64, about 2^-48 relative per term; the
+ * default after FP32 sweeps).  The plan owns all
  * scratch and a captured CUDA graph of the whole batch; run() launches the
  * graph, autotune() times the launch shapes on the real batch and
  * re-captures the fastest.  Instance pointers must stay valid for the
@@ -371,6 +376,9 @@ typedef struct {
     double lowp_tol;      /* FP32 fixed-point residual at which to switch */
     int threads;          /* 0 = default (512) or 128 / 256 / 512 */
     int chunk;            /* 0 = default (128) or 64 / 128 rows of H per stage */
+    int certify_precision; /* -1 = default (IPT_BLOCK_DF64 after FP32 sweeps,
+                              IPT_BLOCK_FP64 otherwise), IPT_BLOCK_FP64 or
+                              IPT_BLOCK_DF64 */
 } IPTBatchOptions;
 
 typedef struct {

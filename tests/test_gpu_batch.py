@@ -80,6 +80,33 @@ def test_batch_mixed_precision(cuda):
     plan32.close()
 
 
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_batch_certifying_sweeps_fp64_and_double_float(cuda, precision):
+    """The certifying sweeps on the FP64 pipe and in double-float arithmetic
+    reach the same certified eigenpairs (scaled residual <= 1e-8 checked on
+    the host, eigenvalues within 1e-10 ||H||_inf of each other)."""
+    torch = cuda
+    Hs, dev, inst = make_batch(torch, SMALL)
+    vals = {}
+    for cert in (_lib.IPT_BLOCK_FP64, _lib.IPT_BLOCK_DF64):
+        plan = api.BatchPlan(inst, precision, certify_precision=cert)
+        plan.run()
+        torch.cuda.synchronize()
+        reps = plan.reports()
+        plan.close()
+        vals[cert] = [d[2].cpu().numpy().copy() for d in dev]
+        for H, (_, dX, dv), r in zip(Hs, dev, reps):
+            assert r["converged"] == 1 and r["max_scaled_residual"] <= 1e-8
+            hn = np.abs(H).sum(axis=1).max()
+            X = dX.T.cpu().numpy()
+            res = H @ X - X * dv.cpu().numpy()[None, :]
+            sc = np.linalg.norm(res, axis=0) / (max(1.0, hn) *
+                                                 np.maximum(1.0, np.linalg.norm(X, axis=0)))
+            assert sc.max() <= 1e-8
+    for H, a, b in zip(Hs, vals[_lib.IPT_BLOCK_FP64], vals[_lib.IPT_BLOCK_DF64]):
+        assert np.abs(a - b).max() <= 1e-10 * np.abs(H).sum(axis=1).max()
+
+
 def test_batch_graph_replay_and_autotune_are_deterministic(cuda):
     torch = cuda
     Hs, dev, inst = make_batch(torch, SMALL)
