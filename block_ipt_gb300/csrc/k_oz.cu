@@ -14,11 +14,15 @@
 //    of (128-row tile, 128-element K period) items.  Warp 4 streams the A
 //    slices (each byte of A is read once per product, L2 evict_first) and
 //    the B chunk through TMA into shared memory; warp 5 issues tcgen05.mma:
-//    one MMA (N = cp) per digit pair (s, t) with s + t <= 5 into the TMEM
-//    accumulator of level s + t (consecutive MMAs write disjoint columns, so
-//    the tensor pipe overlaps them, and the K steps of a pair chain on one
-//    accumulator; two accumulator sets when they fit in TMEM, so the MMAs of
-//    the next period run while the last one drains); warps 0-3 drain the six level
+//    per A slice s and K step one MMA of N = (6 - s) cp (two above N = 256)
+//    that adds every pair (s, t), t <= 5 - s, into the TMEM accumulator of
+//    level s + t (the B slices are consecutive rows, the level accumulators
+//    consecutive columns).  One thread issues every MMA of the SM and each
+//    issue costs it about 50-65 cycles whatever N, so the kernel issues as
+//    few and as wide MMAs as the level structure allows (24 per 64-element K
+//    chunk; one per pair took 84).  Two accumulator sets when they fit in
+//    TMEM, so the MMAs of the next period run while the last one drains;
+//    warps 0-3 drain the six level
 //    accumulators after every period, combine them in double-float
 //    arithmetic and keep a running sum per (row, column) until the CTA
 //    leaves the tile, then write one FP64 partial per (tile, CTA);
@@ -152,6 +156,8 @@ oz_product_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
         // ---- TMA producer: per chunk the B chunk, then the six A slices ----
         const uint64_t pol = tc::l2_stream_policy();
         int ac = 0, bc = 0;
+        int aq = 0, bq = 0;            // ring slots of copy ac / bc
+        uint32_t apar = 0, bpar = 0;   // parities of their rounds
         bool waited = false;
         for (long long it = it0; it < it1 && !abort_flag; ++it) {
             const int tile = (int)(it / prm.periods);
@@ -169,6 +175,8 @@ oz_product_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
                                              tile * kBM, s, a_full(s), pol);
                     }
                     ac = kOzSlices;
+                    aq = kOzSlices % kASlots;
+                    apar = kOzSlices >= kASlots ? 1u : 0u;
                     pdl_wait();
                     waited = true;
                     const uint32_t dst = b_base;
@@ -177,35 +185,43 @@ oz_product_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
                     tc::tma_load_2d(dst + (uint32_t)(3 * CP * 128), &tmB, c * kChunk, 3 * CP,
                                     b_full(0));
                     bc = 1;
+                    bq = 1 % kBSlots;
+                    bpar = kBSlots == 1 ? 1u : 0u;
                     continue;
                 }
                 {
-                    const int q = bc % kBSlots;
-                    const int r = bc / kBSlots;
-                    if (r > 0 &&
-                        !tc::mbar_wait(b_empty(q), (uint32_t)((r - 1) & 1), err, 12, false)) {
+                    // slot bq of the B ring, round bc / kBSlots (kept incrementally:
+                    // this one thread issues every copy of the SM)
+                    if (bc >= kBSlots &&
+                        !tc::mbar_wait(b_empty(bq), bpar ^ 1u, err, 12, false)) {
                         abort_flag = 1;
                         break;
                     }
-                    const uint32_t dst = b_base + (uint32_t)q * prm.b_bytes;
-                    tc::mbar_expect_tx(b_full(q), prm.b_bytes);
-                    tc::tma_load_2d(dst, &tmB, c * kChunk, 0, b_full(q));
+                    const uint32_t dst = b_base + (uint32_t)bq * prm.b_bytes;
+                    tc::mbar_expect_tx(b_full(bq), prm.b_bytes);
+                    tc::tma_load_2d(dst, &tmB, c * kChunk, 0, b_full(bq));
                     tc::tma_load_2d(dst + (uint32_t)(3 * CP * 128), &tmB, c * kChunk, 3 * CP,
-                                    b_full(q));
+                                    b_full(bq));
                     ++bc;
+                    if (++bq == kBSlots) {
+                        bq = 0;
+                        bpar ^= 1u;
+                    }
                 }
                 for (int s = 0; s < kOzSlices; ++s) {
-                    const int q = ac % kASlots;
-                    const int r = ac / kASlots;
-                    if (r > 0 && !tc::mbar_wait(a_empty(q), (uint32_t)((r - 1) & 1), err, 11,
-                                                false)) {
+                    if (ac >= kASlots &&
+                        !tc::mbar_wait(a_empty(aq), apar ^ 1u, err, 11, false)) {
                         abort_flag = 1;
                         break;
                     }
-                    tc::mbar_expect_tx(a_full(q), kABytes);
-                    tc::tma_load_3d_hint(a_base + (uint32_t)q * kABytes, &tmA, c * kChunk,
-                                         tile * kBM, s, a_full(q), pol);
+                    tc::mbar_expect_tx(a_full(aq), kABytes);
+                    tc::tma_load_3d_hint(a_base + (uint32_t)aq * kABytes, &tmA, c * kChunk,
+                                         tile * kBM, s, a_full(aq), pol);
                     ++ac;
+                    if (++aq == kASlots) {
+                        aq = 0;
+                        apar ^= 1u;
+                    }
                 }
             }
         }
@@ -214,7 +230,11 @@ oz_product_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
         b_issued = bc;
     } else if (warp == kMmaWarp && lane == 0) {
         // ---- tcgen05.mma issuer ----
+        // instruction descriptor without its N field (bits 17-22)
+        const uint32_t ibase = prm.idesc & ~(0x3Fu << 17);
         int ac = 0, bc = 0;
+        int aq = 0, bq = 0;
+        uint32_t apar = 0, bpar = 0;
         int k = 0;
         const int nb = prm.acc_bufs;
         for (long long it = it0; it < it1 && !abort_flag; ++it, ++k) {
@@ -234,43 +254,57 @@ oz_product_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
             const int c1 = min(prm.nchunks, c0 + kChunksPerPeriod);
             bool first = true;
             for (int c = c0; c < c1 && !abort_flag; ++c) {
-                const int qb = bc % kBSlots;
-                if (!tc::mbar_wait(b_full(qb), (uint32_t)((bc / kBSlots) & 1), err, 14, false)) {
+                const int qb = bq;
+                if (!tc::mbar_wait(b_full(qb), bpar, err, 14, false)) {
                     abort_flag = 1;
                     break;
                 }
                 const uint32_t bsm = b_base + (uint32_t)qb * prm.b_bytes;
                 for (int s = 0; s < kOzSlices; ++s) {
-                    const int qa = ac % kASlots;
-                    if (!tc::mbar_wait(a_full(qa), (uint32_t)((ac / kASlots) & 1), err, 15,
-                                       false)) {
+                    const int qa = aq;
+                    if (!tc::mbar_wait(a_full(qa), apar, err, 15, false)) {
                         abort_flag = 1;
                         break;
                     }
                     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
                     const uint64_t ad = tc::sw128_desc(a_base + (uint32_t)qa * kABytes);
-                    // one MMA per digit pair (s, t) into the accumulator of
-                    // level s + t: consecutive MMAs write disjoint TMEM
-                    // columns, and the K steps of one pair chain on the same
-                    // accumulator
+                    // one MMA for every pair (s, t <= 5 - s): the B slices t
+                    // lie in consecutive rows, so an MMA of N = (6 - s) cp
+                    // rows written at column s cp puts pair (s, t) into the
+                    // accumulator of level s + t (two MMAs when N exceeds
+                    // 256).  The first K step of an item (s = 0, which covers
+                    // every level) initialises the accumulators.
+                    const int nt = kOzSlices - s;
+                    const int t1 = nt * CP > 256 ? nt / 2 : nt;
+                    const uint64_t bd0 = tc::sw128_desc(bsm);
+                    const uint64_t bd1 = tc::sw128_desc(bsm + (uint32_t)(t1 * CP) * 128u);
+                    const uint32_t id0 = ibase | ((uint32_t)(t1 * CP) >> 3 << 17);
+                    const uint32_t id1 = ibase | ((uint32_t)((nt - t1) * CP) >> 3 << 17);
+                    const uint32_t acc_first = (first && s == 0) ? 0u : 1u;
 #pragma unroll
                     for (int kk = 0; kk < 4; ++kk) {
-#pragma unroll
-                        for (int t = 0; t < kOzSlices; ++t) {
-                            if (t + s >= kOzSlices) break;
-                            const uint64_t bd = tc::sw128_desc(bsm + (uint32_t)(t * CP) * 128u);
-                            // the first K step of an item initialises each level
-                            // through its pair with s = 0
-                            tc::umma<kLowpF16>(acc_tmem + (uint32_t)((s + t) * CP),
-                                               ad + (uint64_t)(2 * kk), bd + (uint64_t)(2 * kk),
-                                               prm.idesc, (first && s == 0 && kk == 0) ? 0u : 1u);
+                        const uint32_t accum = kk > 0 ? 1u : acc_first;
+                        tc::umma<kLowpF16>(acc_tmem + (uint32_t)(s * CP), ad + (uint64_t)(2 * kk),
+                                           bd0 + (uint64_t)(2 * kk), id0, accum);
+                        if (t1 < nt) {
+                            tc::umma<kLowpF16>(acc_tmem + (uint32_t)((s + t1) * CP),
+                                               ad + (uint64_t)(2 * kk), bd1 + (uint64_t)(2 * kk),
+                                               id1, accum);
                         }
                     }
                     tc::umma_commit(a_empty(qa));
                     ++ac;
+                    if (++aq == kASlots) {
+                        aq = 0;
+                        apar ^= 1u;
+                    }
                 }
                 tc::umma_commit(b_empty(qb));
                 ++bc;
+                if (++bq == kBSlots) {
+                    bq = 0;
+                    bpar ^= 1u;
+                }
                 first = false;
             }
             if (abort_flag) break;

@@ -314,52 +314,73 @@ tc_stream_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant_
     const int count = (int)(it1 - it0);
 
     if (warp == kStreamProducer && lane == 0) {
+        // the loop bodies keep their indices incremental: this one thread
+        // issues every copy of the SM, so a division per chunk would slow it
         const uint64_t a_pol = a_keep > 0.0f ? l2_keep_policy(fminf(a_keep, 1.0f)) : 0ull;
-        auto load_a = [&](int q, long long it) {
-            const int tile = (int)(it / prm.chunks);
-            const int kx = (int)(it - (long long)tile * prm.chunks) * prm.kchunk;
+        const int tile0 = (int)(it0 / prm.chunks);
+        const int c00 = (int)(it0 - (long long)tile0 * prm.chunks);
+        auto load_a = [&](int q, int tile, int c) {
             const uint32_t sa = smem_base + (uint32_t)q * stage_bytes;
             if (a_keep > 0.0f) {
-                tma_load_2d_hint(sa, &tmA, kx, tile * kBM, full_bar(q), a_pol);
+                tma_load_2d_hint(sa, &tmA, c * prm.kchunk, tile * kBM, full_bar(q), a_pol);
             } else {
-                tma_load_2d(sa, &tmA, kx, tile * kBM, full_bar(q));
+                tma_load_2d(sa, &tmA, c * prm.kchunk, tile * kBM, full_bar(q));
             }
         };
-        auto load_b = [&](int q, long long it) {
-            const int kx = (int)(it % prm.chunks) * prm.kchunk;
-            tma_load_2d(smem_base + (uint32_t)q * stage_bytes + a_bytes, &tmB, kx, 0,
+        auto load_b = [&](int q, int c) {
+            tma_load_2d(smem_base + (uint32_t)q * stage_bytes + a_bytes, &tmB, c * prm.kchunk, 0,
                         full_bar(q));
         };
         // Delta does not depend on the preceding kernel: the first stages'
         // Delta tiles are requested before waiting for the grid that wrote X
         const int pre = min(stages, count);
+        int tile = tile0, c = c00;
         for (int q = 0; q < pre; ++q) {
             mbar_expect_tx(full_bar(q), stage_bytes);
-            load_a(q, it0 + q);
+            load_a(q, tile, c);
+            if (++c == prm.chunks) {
+                c = 0;
+                ++tile;
+            }
         }
         pdl_wait();
-        for (int q = 0; q < pre; ++q) load_b(q, it0 + q);
-        int i = pre;
+        {
+            int cb = c00;
+            for (int q = 0; q < pre; ++q) {
+                load_b(q, cb);
+                if (++cb == prm.chunks) cb = 0;
+            }
+        }
+        int i = pre, q = 0;
+        uint32_t parity = 0;  // of the empty barriers' first reuse
         for (; i < count; ++i) {
-            const int q = i % stages;
-            if (!mbar_wait(empty_bar(q), (uint32_t)((i / stages - 1) & 1), err, 21, false, spin)) {
+            if (!mbar_wait(empty_bar(q), parity, err, 21, false, spin)) {
                 abort_flag = 1;
                 break;
             }
             if (abort_flag) break;
             mbar_expect_tx(full_bar(q), stage_bytes);
-            load_a(q, it0 + i);
-            load_b(q, it0 + i);
+            load_a(q, tile, c);
+            load_b(q, c);
+            if (++c == prm.chunks) {
+                c = 0;
+                ++tile;
+            }
+            if (++q == stages) {
+                q = 0;
+                parity ^= 1u;
+            }
         }
         issued_count = i;
         pdl_trigger();
     } else if (warp == kStreamMma && lane == 0) {
-        int i = 0, seg = 0;
+        int q = 0, seg = 0;
+        uint32_t parity = 0;
         for (long long it = it0; it < it1 && !abort_flag; ++seg) {
             const long long tile = it / prm.chunks;
-            const long long seg_end = min(it1, (tile + 1) * prm.chunks);
-            const int ab = seg % prm.acc_bufs;
-            const int use = seg / prm.acc_bufs;
+            const int seg_len = (int)(min(it1, (tile + 1) * prm.chunks) - it);
+            const int ab = seg & (prm.acc_bufs - 1);
+            const int use = prm.acc_bufs == 2 ? seg >> 1 : seg;
             if (use > 0 &&
                 !mbar_wait(acc_empty(ab), (uint32_t)((use - 1) & 1), err, 22, false, spin)) {
                 abort_flag = 1;
@@ -367,10 +388,8 @@ tc_stream_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant_
             }
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
             const uint32_t acc = tmem + (uint32_t)(ab * prm.acc_cols);
-            const long long seg_start = it;
-            for (; it < seg_end; ++it, ++i) {
-                const int q = i % stages;
-                if (!mbar_wait(full_bar(q), (uint32_t)((i / stages) & 1), err, 23, false, spin)) {
+            for (int x = 0; x < seg_len; ++x) {
+                if (!mbar_wait(full_bar(q), parity, err, 23, false, spin)) {
                     abort_flag = 1;
                     break;
                 }
@@ -381,11 +400,16 @@ tc_stream_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant_
 #pragma unroll
                 for (int kk = 0; kk < 4; ++kk) {
                     umma<KIND>(acc, ad + (uint64_t)(2 * kk), bd + (uint64_t)(2 * kk), prm.idesc,
-                               (it > seg_start || kk > 0) ? 1u : 0u);
+                               (x > 0 || kk > 0) ? 1u : 0u);
                 }
                 umma_commit(empty_bar(q));
+                if (++q == stages) {
+                    q = 0;
+                    parity ^= 1u;
+                }
             }
             if (abort_flag) break;
+            it += seg_len;
             umma_commit(acc_full(ab));
         }
         umma_commit(mma_done);
