@@ -1397,10 +1397,14 @@ struct LowpDense final : LowpDenseOperator {
         const int afmt = LowpTypes<LP>::kind == kLowpF16 ? 0 : (LowpTypes<LP>::kind == kLowpBF16 ? 1 : 2);
         idesc = (1u << 4) | ((uint32_t)afmt << 7) | ((uint32_t)afmt << 10) |
                 ((uint32_t)(p_pad >> 3) << 17) | ((uint32_t)(tc::kBM >> 4) << 24);
-        // persistent stream-K schedule (tuning knob IPT_GB300_TC_STREAMK=0:
-        // the split-K grid below)
-        streamk = env_int("IPT_GB300_TC_STREAMK", 1) != 0;
-        if (streamk) return set_width_streamk(row_blocks, forced_stages);
+        // persistent stream-K schedule with two CTAs per SM (tuning knob
+        // IPT_GB300_TC_STREAMK: 1 = one CTA per SM with a deeper ring, 0 =
+        // the split-K grid below).  Measured per product (FP16, k = 32):
+        // n = 8192 22.1 us (one CTA per SM 28.0, split-K 23.3); n = 16384
+        // 91-93 us for all three, 0.85-0.87 of the measured HBM bandwidth.
+        const int sk = env_int("IPT_GB300_TC_STREAMK", 2);
+        streamk = sk > 0;
+        if (streamk) return set_width_streamk(row_blocks, forced_stages, std::min(sk, 2));
         chunks_per_split = (chunks_total + splits - 1) / splits;
         splits = (chunks_total + chunks_per_split - 1) / chunks_per_split;
         const size_t stage_bytes = (size_t)(tc::kBM + p_pad) * tc::kRowBytes;
@@ -1426,10 +1430,10 @@ struct LowpDense final : LowpDenseOperator {
     // K chunk) items with a TMA ring as deep as shared memory allows; the
     // partial slots of a tile are the CTAs its items span (at most
     // `splits`), the unused ones zeroed here once.
-    int set_width_streamk(int row_blocks, int forced_stages)
+    int set_width_streamk(int row_blocks, int forced_stages, int per_sm)
     {
         const size_t stage_bytes = (size_t)(tc::kBM + p_pad) * tc::kRowBytes;
-        stages = (int)std::min<size_t>(12, (216u * 1024u) / stage_bytes);
+        stages = (int)std::min<size_t>(12, (per_sm == 2 ? 108u : 216u) * 1024u / stage_bytes);
         if (forced_stages >= 2) stages = std::min(stages, forced_stages);
         if (stages < 2) return IPT_CUDA_INVALID_ARGUMENT;
         sprm = tc::StreamParams{};
@@ -1444,7 +1448,7 @@ struct LowpDense final : LowpDenseOperator {
         sprm.kchunk = (int)kchunk;
         sprm.items = (long long)row_blocks * chunks_total;
         sprm.idesc = idesc;
-        grid_g = (int)std::min<long long>(sms, sprm.items);
+        grid_g = (int)std::min<long long>((long long)sms * per_sm, sprm.items);
         splits = 1;
         for (int t = 0; t < row_blocks; ++t) {
             const long long f = tc::owner_of((long long)t * chunks_total, sprm.items, grid_g);

@@ -66,24 +66,25 @@ def test_lowp_iterates_track_fp64(cuda, kind, n, k):
 @pytest.mark.parametrize("kind", ["fp16", "tf32"])
 @pytest.mark.parametrize("n,k", [(300, 8), (777, 40), (2048, 33), (4100, 16)])
 def test_stream_and_split_schedules(cuda, monkeypatch, kind, n, k):
-    """The persistent stream-K product (default) and the split-K grid
-    (IPT_GB300_TC_STREAMK=0) both track the FP64 iterates; the stream-K
-    result is the same bits on a second run (fixed slot order)."""
+    """The persistent stream-K product with two CTAs per SM (default) or one
+    (IPT_GB300_TC_STREAMK=1) and the split-K grid (=0) all track the FP64
+    iterates; the stream-K result is the same bits on a second run (fixed
+    slot order)."""
     H, _ = workloads.dense_config0(n, seed=5, sigma=0.05)
     m = 4
     Xo, _, _, _ = oracle.ipt_dense(H, k, m + 1)
     tol = KINDS[kind][1]
     got = {}
-    for mode in ("1", "0"):
+    for mode in ("2", "1", "0"):
         monkeypatch.setenv("IPT_GB300_TC_STREAMK", mode)
         X, v, info = run_mixed(cuda, H, k, kind, 1e-300, m, 1e300, 1)
         assert info["lowp_iterations"] == m
         err = np.abs(X - Xo).max() / np.abs(Xo).max()
         assert err <= tol, (mode, err)
         got[mode] = X
-    monkeypatch.setenv("IPT_GB300_TC_STREAMK", "1")
+    monkeypatch.setenv("IPT_GB300_TC_STREAMK", "2")
     X2, _, _ = run_mixed(cuda, H, k, kind, 1e-300, m, 1e300, 1)
-    assert np.array_equal(X2, got["1"])
+    assert np.array_equal(X2, got["2"])
 
 
 @pytest.mark.parametrize("kind", ["fp16", "tf32", "fp32"])
