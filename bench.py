@@ -79,6 +79,7 @@ def parse():
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--no-fci-free", action="store_true")
     ap.add_argument("--no-acx", action="store_true")
+    ap.add_argument("--no-lowp-sweep", action="store_true")
     ap.add_argument("--fci-free-orbitals", type=int, default=14)
     ap.add_argument("--batch", type=int, default=512)
     ap.add_argument("--batch-steps", type=int, default=3)
@@ -389,6 +390,73 @@ def fci_section(args, torch, lib, stream, flush, dev):
                             "achieved_fp64_tflops": achieved},
             "kernel_ms": {kk: round(val[0] / len(times), 4) for kk, val in prof.items() if val[1]},
             "learned": learned_part, "block_cluster": cluster}
+
+
+def lowp_sweep_section(torch, lib, dev, k, peak):
+    """The low-precision tensor-core product on its own, per launch, inside
+    30-step fixed-iteration FP16 IPT runs (ipt_mixed_precision_cuda_device_tol):
+    n = 8192 (FP16 Delta 134 MB, about L2's size) and n = 16384 (537 MB, four
+    times L2), with the default L2 hint and without it (IPT_GB300_L2_KEEP_PCT=0:
+    every byte of Delta from DRAM).  Synthetic matrices of the headline
+    family (diagonal i/8, off-diagonal 0.02 N(0,1) exp(-|i-j|/256)), made on
+    the device."""
+    import os
+    from block_ipt_gb300 import _lib
+    out = []
+    for n in (8192, 16384):
+        g = torch.Generator(device=dev)
+        g.manual_seed(n)
+        idx = torch.arange(n, device=dev, dtype=torch.float64)
+        H = torch.empty((n, n), dtype=torch.float64, device=dev)
+        for r0 in range(0, n, 2048):
+            r1 = min(n, r0 + 2048)
+            H[r0:r1] = 0.02 * torch.randn((r1 - r0, n), generator=g, device=dev,
+                                          dtype=torch.float64) * torch.exp(
+                -(idx[r0:r1, None] - idx[None, :]).abs() / 256.0)
+        H = torch.triu(H, 1)
+        H = H + H.T
+        H.diagonal().copy_(idx / 8.0)
+        ldp = (n + 63) // 64 * 64
+        alg = 2 * n * ldp + 2 * ldp * ((k + 15) // 16 * 16)
+        for keep in (None, "0"):
+            old = os.environ.pop("IPT_GB300_L2_KEEP_PCT", None)
+            if keep is not None:
+                os.environ["IPT_GB300_L2_KEEP_PCT"] = keep
+            try:
+                res = _lib._MixedResult()
+
+                def run():
+                    st = lib.ipt_mixed_precision_cuda_device_tol(
+                        C.c_void_p(H.data_ptr()), n, k, 1e-300, 30, 1e300, 1,
+                        C.c_void_p(torch.cuda.current_blas_handle()), C.byref(res))
+                    if st != 0:
+                        raise RuntimeError("mixed IPT status %d" % st)
+                    lib.ipt_mixed_precision_cuda_free_device_result(C.byref(res))
+
+                run()
+                torch.cuda.synchronize()
+                lib.ipt_block_profile_reset()
+                lib.ipt_block_profile_enable(1)
+                run()
+                run()
+                torch.cuda.synchronize()
+                lib.ipt_block_profile_enable(0)
+                ms, cnt = profile_snapshot(lib)["lowp_product"]
+            finally:
+                os.environ.pop("IPT_GB300_L2_KEEP_PCT", None)
+                if old is not None:
+                    os.environ["IPT_GB300_L2_KEEP_PCT"] = old
+            per = ms / max(1, cnt)
+            ach = alg / (per * 1e-3) / 1e9
+            traffic = NCU_TRAFFIC.get(("tc_stream", n, keep or "default"))
+            out.append({"n": n, "l2_keep": "default" if keep is None else "off",
+                        "us_per_launch": per * 1e3, "launches": cnt,
+                        "algorithmic_bytes": alg, "achieved_gbs": ach, "frac": ach / peak,
+                        "dram_bytes_per_launch": traffic,
+                        "dram_only_frac": (traffic / (per * 1e-3) / 1e9 / peak) if traffic else None})
+        del H
+        torch.cuda.empty_cache()
+    return out
 
 
 def acx_section(torch, lib, dH, n, k):
@@ -821,11 +889,18 @@ def run_ours(args):
     esize = 2 if args.precision in ("fp16", "bf16") else 4
     lp_bytes = n * ldp * esize + ldp * ((k + 8 + 15) // 16 * 16) * esize
     lp_ach = lp_bytes / (lp_ms / max(1, lp_cnt) * 1e-3) / 1e9 if lp_cnt else None
-    roofline_lowp = {"kernel": "tc_partial_kernel (tcgen05 + TMA, %s)" % args.precision,
+    lp_traffic = NCU_TRAFFIC.get(("tc_stream", n, k, args.precision))
+    lp_dram = (lp_traffic / (lp_ms / max(1, lp_cnt) * 1e-3) / 1e9) if (lp_traffic and lp_cnt) else None
+    roofline_lowp = {"kernel": "tc_stream_kernel (tcgen05 + TMA, persistent stream-K, %s)"
+                               % args.precision,
                      "bound": "hbm", "achieved": lp_ach, "peak": peaks["hbm_gbs"],
                      "unit": "GB/s", "frac": (lp_ach / peaks["hbm_gbs"]) if lp_ach else None,
-                     "traffic": NCU_TRAFFIC.get(("tc_partial", n, k, args.precision)),
+                     "traffic": lp_traffic,
                      "traffic_unit": "bytes per launch (ncu dram__bytes_read.sum + write.sum)",
+                     "dram_only_achieved": lp_dram,
+                     "dram_only_frac": (lp_dram / peaks["hbm_gbs"]) if lp_dram else None,
+                     "dram_only_note": "DRAM bytes of a launch inside the solve (the L2-kept share "
+                                       "of Delta is not counted) over the same live launch time",
                      "launches": lp_cnt,
                      "avg_launch_ms": lp_ms / max(1, lp_cnt),
                      "algorithmic_bytes_per_launch": lp_bytes,
@@ -866,6 +941,13 @@ def run_ours(args):
     fci_free = None
     if not args.no_fci_free and rank == 0:
         fci_free = fci_free_section(args, torch, dev, mlp_params)
+
+    lowp_sweep = None
+    if not args.no_lowp_sweep and rank == 0:
+        try:
+            lowp_sweep = lowp_sweep_section(torch, lib, dev, k, peaks["hbm_gbs"])
+        except Exception as exc:  # a side measurement never takes the headline line down
+            lowp_sweep = {"error": repr(exc)}
 
     acx = None
     if not args.no_acx and rank == 0:
@@ -925,6 +1007,7 @@ def run_ours(args):
             "batched_config2": batched,
             "matrix_free_config4": fci_free,
             "acx_fp64": acx,
+            "lowp_product_sweep": lowp_sweep,
         }
         print(json.dumps(line), flush=True)
     if world > 1:
