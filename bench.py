@@ -53,10 +53,17 @@ MEASURED_PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
 # keyed by (kernel, n, k, precision).
 NCU_TRAFFIC = {("dense64_partial", 8192, 32, "fp16"): 567.5e6,
                ("df64_partial", 8192, 32, "fp16"): 1111.3e6,
-               # steady state inside a solve, with the L2-kept share of Delta
-               # (profiles/tc_partial_fp16_n8192_k32_l2keep.md); a cold launch
-               # moves 137.9 MB (profiles/tc_partial_fp16_n8192_k32.md)
-               ("tc_partial", 8192, 32, "fp16"): 94.8e6}
+               # launches inside 30-step FP16 runs of the n = 8192 / 16384
+               # matrices with the L2-kept share of Delta, caches not flushed
+               # between launches (profiles/tc_stream_fp16_n8192_k32.md); the
+               # same figure stands for the product inside the dense solve
+               ("tc_stream", 8192, 32, "fp16"): 95.5e6,
+               ("tc_stream", 8192, "default"): 95.5e6,
+               ("tc_stream", 8192, "0"): 141.6e6,
+               ("tc_stream", 16384, "default"): 553.0e6,
+               # one cold launch at n = 8192, 32 columns
+               # (profiles/oz_product_n8192_c32.md)
+               ("oz_product", 8192, 32, "fp16"): 811.5e6}
 
 
 def parse():

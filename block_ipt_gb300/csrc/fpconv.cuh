@@ -31,24 +31,6 @@ IPTGB_HD int clz32_hd(uint32_t x)
 #endif
 }
 
-// Bits of RN_float(h) for |h| in the normal float range; returns false when
-// the entry needs the FP64 instruction (zero, subnormal, out of range, or a
-// rounding to infinity).
-IPTGB_HD bool double_to_float_bits(uint64_t b, uint32_t *bits)
-{
-    const uint32_t h32 = (uint32_t)(b >> 32);
-    const uint32_t l32 = (uint32_t)b;
-    const uint32_t e = (h32 >> 20) & 0x7FFu;
-    if (e - 897u >= 254u) return false;
-    const uint32_t f = (h32 & 0x80000000u) | ((e - 896u) << 23) | ((h32 & 0xFFFFFu) << 3) |
-                       (l32 >> 29);
-    const uint32_t rem = l32 & 0x1FFFFFFFu;
-    const uint32_t r = f + ((rem > 0x10000000u || (rem == 0x10000000u && (f & 1u))) ? 1u : 0u);
-    if ((r & 0x7F800000u) == 0x7F800000u) return false;
-    *bits = r;
-    return true;
-}
-
 // Bits of (hi, lo) for the common case; returns false when the entry needs
 // the FP64 instructions (|h| outside the normal float range, an overflow of
 // hi, or a remainder below the normal float range).

@@ -44,7 +44,6 @@
 
 #include "common.cuh"
 #include "dfloat.cuh"
-#include "fpconv.cuh"
 #include "reduce.cuh"
 
 #define IPT_API extern "C" __attribute__((visibility("default")))
@@ -96,22 +95,6 @@ __device__ __forceinline__ unsigned long long global_ns()
     return t;
 }
 
-// H entry in the arithmetic type; the float rounding on the integer pipe
-// (GB300's FP64 pipe, which also runs double -> float conversions, would
-// bound the FP32 sweeps otherwise).
-template <typename T>
-__device__ __forceinline__ T arith_from_double(double v)
-{
-    return (T)v;
-}
-template <>
-__device__ __forceinline__ float arith_from_double<float>(double v)
-{
-    uint32_t b;
-    return double_to_float_bits((uint64_t)__double_as_longlong(v), &b) ? __uint_as_float(b)
-                                                                       : __double2float_rn(v);
-}
-
 // Y = H X for one instance (rows strided over the block), T the arithmetic
 // type.  With `rowsum`, also returns the largest absolute row sum of H.
 template <typename T, int L>
@@ -132,7 +115,7 @@ __device__ double product(const Inst &I, const double *__restrict__ X, T *xs, bo
             for (int e = tid; e < L * kKMax; e += blockDim.x) {
                 const int l = e / kKMax;
                 const int j = e - l * kKMax;
-                xs[e] = (l < lc && j < k) ? arith_from_double<T>(X[(size_t)(l0 + l) * k + j]) : T(0);
+                xs[e] = (l < lc && j < k) ? (T)X[(size_t)(l0 + l) * k + j] : T(0);
             }
             __syncthreads();
             if (i < n) {
@@ -140,7 +123,7 @@ __device__ double product(const Inst &I, const double *__restrict__ X, T *xs, bo
                 for (int l = 0; l < lc; ++l) {
                     const double hd = hc[(size_t)l * n];
                     if (rowsum) rs += fabs(hd);
-                    const T h = arith_from_double<T>(hd);
+                    const T h = (T)hd;
                     const T *xr = xs + l * kKMax;
 #pragma unroll
                     for (int j = 0; j < kKMax; ++j) acc[j] = fma(h, xr[j], acc[j]);

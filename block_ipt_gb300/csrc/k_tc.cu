@@ -966,6 +966,39 @@ __device__ __forceinline__ float &f4_at(float4 &v, int i)
     return i == 0 ? v.x : (i == 1 ? v.y : (i == 2 ? v.z : v.w));
 }
 
+// The sum over the product's partial slots of four rows (row0..row0+3) of
+// column col, and of the diagonal entry (col, col), in slot order: the loads
+// of up to kSlotsUnrolled slots are issued together (the update is bound by
+// their latency, not by bandwidth), the adds keep the fixed order.
+constexpr int kSlotsUnrolled = 8;
+
+__device__ __forceinline__ void sum_slots4(const float *__restrict__ P, int S, int p, int n,
+                                           int col, int row0, float4 &y, float &c)
+{
+    float4 v[kSlotsUnrolled];
+    float d[kSlotsUnrolled];
+#pragma unroll
+    for (int s = 0; s < kSlotsUnrolled; ++s) {
+        if (s < S) {
+            const float *base = P + ((size_t)s * p + col) * (size_t)n;
+            v[s] = *reinterpret_cast<const float4 *>(base + row0);
+            d[s] = base[col];
+        }
+    }
+#pragma unroll
+    for (int s = 0; s < kSlotsUnrolled; ++s) {
+        if (s < S) {
+            y = f4_add(y, v[s]);
+            c += d[s];
+        }
+    }
+    for (int s = kSlotsUnrolled; s < S; ++s) {
+        const float *base = P + ((size_t)s * p + col) * (size_t)n;
+        y = f4_add(y, *reinterpret_cast<const float4 *>(base + row0));
+        c += base[col];
+    }
+}
+
 template <typename LP>
 __global__ void lowp_update4_kernel(const float *__restrict__ P, int S, int n, int p,
                                     float inv_scale, const float *__restrict__ inv_row,
@@ -1001,11 +1034,7 @@ __global__ void lowp_update4_kernel(const float *__restrict__ P, int S, int n, i
         const size_t e = (size_t)col * n + row0;
         float4 y = make_float4(0.f, 0.f, 0.f, 0.f);
         float c = 0.0f;
-        for (int s = 0; s < S; ++s) {
-            const float *base = P + ((size_t)s * p + col) * (size_t)n;
-            y = f4_add(y, *reinterpret_cast<const float4 *>(base + row0));
-            c += base[col];
-        }
+        sum_slots4(P, S, p, n, col, row0, y, c);
         const float4 x = *reinterpret_cast<const float4 *>(X + e);
         const float4 g = *reinterpret_cast<const float4 *>(G + e);
         const float4 ir = inv_row != nullptr
@@ -1173,11 +1202,7 @@ __global__ void refine_update4_kernel(const float *__restrict__ P, int S, int n,
         const size_t e = (size_t)col * n + row0;
         float4 y = make_float4(0.f, 0.f, 0.f, 0.f);
         float b = 0.0f;
-        for (int s = 0; s < S; ++s) {
-            const float *base = P + ((size_t)s * p + col) * (size_t)n;
-            y = f4_add(y, *reinterpret_cast<const float4 *>(base + row0));
-            b += base[col];
-        }
+        sum_slots4(P, S, p, n, col, row0, y, b);
         const float4 ir = inv_row != nullptr
                               ? *reinterpret_cast<const float4 *>(inv_row + row0)
                               : make_float4(inv_scale, inv_scale, inv_scale, inv_scale);
