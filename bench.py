@@ -57,12 +57,12 @@ NCU_TRAFFIC = {("dense64_partial", 8192, 32, "fp16"): 567.5e6,
                # matrices with the L2-kept share of Delta, caches not flushed
                # between launches (profiles/tc_stream_fp16_n8192_k32.md); the
                # same figure stands for the product inside the dense solve
-               ("tc_stream", 8192, 32, "fp16"): 95.5e6,
-               ("tc_stream", 8192, "default"): 95.5e6,
-               ("tc_stream", 8192, "0"): 141.6e6,
-               ("tc_stream", 16384, "default"): 553.0e6,
+               ("tc_stream", 8192, 32, "fp16"): 95.7e6,
+               ("tc_stream", 8192, "default"): 95.7e6,
+               ("tc_stream", 8192, "0"): 141.9e6,
+               ("tc_stream", 16384, "default"): 554.4e6,
                # one cold launch at n = 8192, 32 columns
-               # (profiles/oz_product_n8192_c32.md)
+               # (profiles/oz_product_n4096_n8192_c32.md)
                ("oz_product", 8192, 32, "fp16"): 811.5e6}
 
 
