@@ -436,9 +436,10 @@ bool options_valid(const IPTBlockOptions *o)
 }  // namespace
 
 // host_src (optional): a device-accessible pointer to H in pinned host
-// memory; dH_in is then an uninitialised device buffer that the solve fills
-// (the fused setup pass reads the host copy once, at the host link's speed,
-// and writes everything it derives from H in the same pass).
+// memory; dH_in is then an uninitialised device buffer that the solve fills.
+// The mixed solve's setup reads only the upper triangle of the host copy
+// (H is symmetric), in column chunks that cross the host link while the
+// setup pass of the chunks already there runs beside them.
 int dense_block_device(const double *dH_in, int n, int k, const IPTBlockOptions *options,
                        double *d_vectors, double *d_values, IPTBlockReport *report,
                        const double *host_src = nullptr)
@@ -502,8 +503,11 @@ int dense_block_device(const double *dH_in, int n, int k, const IPTBlockOptions 
         su.symmetric = true;
         su.split_hi = Hsplit.ptr;
         su.split_lo = Hsplit.ptr ? Hsplit.ptr + mat : nullptr;
-        su.fused_src = host_src != nullptr ? host_src : dH_in;
+        // from pinned host memory only the upper triangle crosses the host
+        // link (H is symmetric); the pass mirrors it into the device copy
+        su.fused_src = dH_in;
         su.fused_copy = host_src != nullptr ? const_cast<double *>(dH_in) : nullptr;
+        su.upper_host = host_src;
         su.diag = d.ptr;
         su.stats = stats.ptr;
         if (use_oz) {

@@ -29,6 +29,7 @@
 #include <algorithm>
 #include <memory>
 #include <utility>
+#include <vector>
 
 #include "block_solver.h"
 #include "common.cuh"
@@ -688,12 +689,12 @@ __global__ void __launch_bounds__(256)
                        double *__restrict__ copy, LP *__restrict__ delta, float *__restrict__ hi,
                        float *__restrict__ lo, float *__restrict__ inv_row,
                        double *__restrict__ diag, DenseStats *__restrict__ stats, int vec,
-                       __half *__restrict__ oz, int *__restrict__ oz_rowexp)
+                       __half *__restrict__ oz, int *__restrict__ oz_rowexp, int c0)
 {
     __shared__ unsigned long long wmax[8];
     __shared__ float wS[8], wC[8];
     __shared__ int s2_sh;
-    const int c = blockIdx.x;
+    const int c = c0 + blockIdx.x;
     const int tid = threadIdx.x;
     const double *scol = src + (size_t)c * n;
     double *ccol = copy != nullptr ? copy + (size_t)c * n : nullptr;
@@ -817,6 +818,54 @@ __global__ void __launch_bounds__(256)
         }
         inv_row[c] = (float)ldexp(1.0, -s2);
         if (oz_rowexp != nullptr) oz_rowexp[c] = oz_e;
+    }
+}
+
+// Upper triangle of a symmetric H (column-major, ld = n) in pinned host
+// memory -> the full matrix in device memory, for the column blocks
+// [jb0, jb1) of 32 columns: tile (ib, jb), ib <= jb, is read once over the
+// host link (rows i <= j only) and written at (ib, jb) and, through shared
+// memory, transposed at (jb, ib).  A persistent grid of a few CTAs walks the
+// tiles, so the setup kernels of finished chunks keep SM slots beside it;
+// each thread keeps four host loads in flight.
+__global__ void __launch_bounds__(256)
+upper_to_device_kernel(const double *__restrict__ host, int n, int jb0, int jb1,
+                       double *__restrict__ dev)
+{
+    __shared__ double t[32][33];
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    // tiles of column block jb: ib = 0..jb; linear index over the chunk
+    const long long base = (long long)jb0 * (jb0 + 1) / 2;
+    const long long total = (long long)jb1 * (jb1 + 1) / 2 - base;
+    for (long long q = blockIdx.x; q < total; q += gridDim.x) {
+        // column block jb with base + q in [jb (jb + 1) / 2, (jb + 1) (jb + 2) / 2)
+        const long long g = base + q;
+        int jb = (int)((sqrt(8.0 * (double)g + 1.0) - 1.0) * 0.5);
+        while ((long long)(jb + 1) * (jb + 2) / 2 <= g) ++jb;
+        while ((long long)jb * (jb + 1) / 2 > g) --jb;
+        const int ib = (int)(g - (long long)jb * (jb + 1) / 2);
+        const int i0 = ib * 32, j0 = jb * 32;
+        const int i = i0 + tx;
+        double v[4];
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+            const int j = j0 + ty + 8 * r;
+            v[r] = (j < n && i <= j) ? host[(size_t)j * n + i] : 0.0;
+        }
+        __syncthreads();  // the previous tile's transpose has read t
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+            const int j = j0 + ty + 8 * r;
+            t[ty + 8 * r][tx] = v[r];
+            if (j < n && i <= j) dev[(size_t)j * n + i] = v[r];
+        }
+        __syncthreads();
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+            const int ii = ty + 8 * r;
+            const int row = j0 + tx, col = i0 + ii;  // entry (j, i) of the lower part
+            if (row < n && col < row) dev[(size_t)col * n + row] = t[tx][ii];
+        }
     }
 }
 
@@ -1317,11 +1366,15 @@ struct LowpDense final : LowpDenseOperator {
                             ((reinterpret_cast<uintptr_t>(split_hi) & 7) == 0) &&
                             ((reinterpret_cast<uintptr_t>(split_lo) & 7) == 0) &&
                             ((reinterpret_cast<uintptr_t>(su.fused_copy) & 15) == 0);
-            kfn<<<n, 256, 0, s>>>(su.fused_src, n, ldp,
-                                     LowpTypes<LP>::kind == kLowpF16 ? 1 : 0, su.fused_copy,
-                                     delta.ptr, split_hi, split_lo, inv_rows.ptr, su.diag,
-                                     su.stats, vec, su.oz, su.oz_rowexp);
-            IPTGB_LAUNCH();
+            if (su.upper_host != nullptr && su.fused_copy != nullptr) {
+                IPTGB_CHECK(upper_pipeline(su, split_hi, split_lo));
+            } else {
+                kfn<<<n, 256, 0, s>>>(su.fused_src, n, ldp,
+                                         LowpTypes<LP>::kind == kLowpF16 ? 1 : 0, su.fused_copy,
+                                         delta.ptr, split_hi, split_lo, inv_rows.ptr, su.diag,
+                                         su.stats, vec, su.oz, su.oz_rowexp, 0);
+                IPTGB_LAUNCH();
+            }
             scale = 1.0;  // per-row scales in inv_rows
             su.fused_done = true;
             su.split_done = split_hi != nullptr;
@@ -1375,6 +1428,74 @@ struct LowpDense final : LowpDenseOperator {
         IPTGB_CHECK(err.alloc(1, s));
         IPTGB_CUDA(cudaMemsetAsync(err.ptr, 0, sizeof(int), s));
         return IPT_CUDA_SUCCESS;
+    }
+
+    // Setup from the upper triangle of H in pinned host memory: column
+    // chunks in decreasing order cross the host link on stream s (a chunk's
+    // columns are then complete: their lower parts are the transposes of
+    // tiles of higher columns), and the setup of each chunk runs on a second
+    // stream behind its transfer.  Only n (n + 1) / 2 entries cross the link.
+    int upper_pipeline(LowpDenseSetup &su, float *split_hi, float *split_lo)
+    {
+        const int nb = (n + 31) / 32;
+        const int chunk_blocks = std::max(1, std::min(nb, 16));  // 512 columns
+        cudaStream_t s2 = nullptr;
+        IPTGB_CUDA(cudaStreamCreateWithFlags(&s2, cudaStreamNonBlocking));
+        std::vector<cudaEvent_t> evs;
+        int st = IPT_CUDA_SUCCESS;
+        auto fail = [&](int code) {
+            st = code;
+        };
+        cudaEvent_t done = nullptr;
+        if (cudaEventCreateWithFlags(&done, cudaEventDisableTiming) != cudaSuccess) {
+            cudaStreamDestroy(s2);
+            return IPT_CUDA_CUDA_ERROR;
+        }
+        const int vec = (n % 2 == 0) &&
+                        ((reinterpret_cast<uintptr_t>(su.fused_copy) & 15) == 0) &&
+                        ((reinterpret_cast<uintptr_t>(split_hi) & 7) == 0) &&
+                        ((reinterpret_cast<uintptr_t>(split_lo) & 7) == 0);
+        // s2 starts after everything queued on s so far (allocations, zeroed stats)
+        if (cudaEventRecord(done, s) != cudaSuccess || cudaStreamWaitEvent(s2, done, 0) != cudaSuccess) {
+            fail(IPT_CUDA_CUDA_ERROR);
+        }
+        for (int jb1 = nb; jb1 > 0 && st == IPT_CUDA_SUCCESS; jb1 -= chunk_blocks) {
+            const int jb0 = std::max(0, jb1 - chunk_blocks);
+            upper_to_device_kernel<<<std::max(1, sms), 256, 0, s>>>(su.upper_host, n, jb0, jb1,
+                                                                   su.fused_copy);
+            if (cudaGetLastError() != cudaSuccess) {
+                fail(IPT_CUDA_CUDA_ERROR);
+                break;
+            }
+            count_launch();
+            cudaEvent_t ev = nullptr;
+            if (cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) != cudaSuccess) {
+                fail(IPT_CUDA_CUDA_ERROR);
+                break;
+            }
+            evs.push_back(ev);
+            if (cudaEventRecord(ev, s) != cudaSuccess || cudaStreamWaitEvent(s2, ev, 0) != cudaSuccess) {
+                fail(IPT_CUDA_CUDA_ERROR);
+                break;
+            }
+            const int c0 = jb0 * 32, c1 = std::min(n, jb1 * 32);
+            fused_setup_kernel<LP><<<c1 - c0, 256, 0, s2>>>(
+                su.fused_copy, n, ldp, LowpTypes<LP>::kind == kLowpF16 ? 1 : 0, nullptr, delta.ptr,
+                split_hi, split_lo, inv_rows.ptr, su.diag, su.stats, vec, su.oz, su.oz_rowexp, c0);
+            if (cudaGetLastError() != cudaSuccess) {
+                fail(IPT_CUDA_CUDA_ERROR);
+                break;
+            }
+            count_launch();
+        }
+        // s continues after the last setup
+        if (cudaEventRecord(done, s2) != cudaSuccess || cudaStreamWaitEvent(s, done, 0) != cudaSuccess) {
+            fail(IPT_CUDA_CUDA_ERROR);
+        }
+        for (cudaEvent_t ev : evs) cudaEventDestroy(ev);
+        cudaEventDestroy(done);
+        cudaStreamDestroy(s2);
+        return st;
     }
 
     // Delta is streamed once per product; when it is larger than about

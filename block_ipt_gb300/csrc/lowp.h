@@ -72,6 +72,13 @@ struct LowpDenseSetup {
     // fused_copy also the FP64 matrix itself (when fused_src is host memory).
     const double *fused_src = nullptr;
     double *fused_copy = nullptr;
+    // fused setup from pinned host memory read by its upper triangle only
+    // (device-accessible pointer; H symmetric): column chunks of the upper
+    // triangle cross the host link in decreasing column order into
+    // fused_copy, mirrored there into the full matrix, and the setup of each
+    // chunk runs on a second stream while the next chunk crosses the link
+    // (fused_src is then not used)
+    const double *upper_host = nullptr;
     double *diag = nullptr;         // n entries
     DenseStats *stats = nullptr;    // device, zeroed by the caller
     bool fused_done = false;        // out

@@ -196,6 +196,35 @@ def test_host_entry_pinned_matches_pageable(cuda, prec):
     check_pairs(H, X2, v2, k)
 
 
+@pytest.mark.parametrize("n", [1000, 2085])
+def test_host_entry_pinned_reads_only_the_upper_triangle(cuda, n):
+    """From pinned host memory the mixed solve moves only the upper triangle
+    of H across the host link (column chunks mirrored on the device): with
+    NaN in every entry below the diagonal of the host copy it returns the
+    same bits as the solve of the symmetric matrix from pageable memory."""
+    import ctypes as C
+    from block_ipt_gb300 import _lib
+    torch = cuda
+    k = 12
+    H, _ = workloads.dense_config1(n, seed=23)
+    H = np.asfortranarray(H)
+    X1, v1, r1 = api.block_solve_dense(H, k, "fp16")
+    Hu = H.copy(order="F")
+    Hu[np.tril_indices(n, -1)] = np.nan
+    pinned = torch.from_numpy(Hu.T.copy()).pin_memory()  # row-major H^T = column-major H
+    opt = api.block_options("fp16")
+    X2 = np.zeros((n, k), order="F")
+    v2 = np.zeros(k)
+    rep = _lib.IPTBlockReport()
+    st = _lib.load().ipt_block_solve_dense(C.c_void_p(pinned.data_ptr()), n, k, C.byref(opt),
+                                           C.c_void_p(X2.ctypes.data), C.c_void_p(v2.ctypes.data),
+                                           C.byref(rep))
+    assert st == 0 and rep.converged == 1 and r1["converged"] == 1
+    assert np.array_equal(v1, v2)
+    assert np.array_equal(X1, X2)
+    check_pairs(H, X2, v2, k)
+
+
 def test_fused_setup_matches_two_pass(cuda, monkeypatch):
     """The fused setup pass (per-row FP16 scales) and the two-pass setup (one
     global scale) reach the same certified eigenpairs."""
