@@ -257,7 +257,8 @@ template <int KIND>
 __global__ void __launch_bounds__(kStreamThreads, 1)
 tc_stream_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                  const __grid_constant__ StreamParams prm, float *__restrict__ P, int *err,
-                 float a_keep, const double *hist, int step, double stop_tol, long long spin)
+                 float a_keep, const double *hist, int step, double stop_tol, long long spin,
+                 int reverse)
 {
     if (hist != nullptr) {
         pdl_wait();
@@ -313,13 +314,37 @@ tc_stream_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant_
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = *tmem_slot;
     const int count = (int)(it1 - it0);
+    // traversal direction: every other product walks its items backwards, so
+    // it starts on the bytes of Delta the previous product read last (still
+    // in L2)
+    const long long first_it = reverse ? it1 - 1 : it0;
+    // items of the segment (one tile's part of this CTA's range) that starts
+    // at item `it` in traversal order
+    auto seg_len_at = [&](long long it) {
+        const long long tile = it / prm.chunks;
+        return reverse ? (int)(it - max(it0, tile * prm.chunks) + 1)
+                       : (int)(min(it1, (tile + 1) * prm.chunks) - it);
+    };
 
     if (warp == kStreamProducer && lane == 0) {
         // the loop bodies keep their indices incremental: this one thread
         // issues every copy of the SM, so a division per chunk would slow it
         const uint64_t a_pol = a_keep > 0.0f ? l2_keep_policy(fminf(a_keep, 1.0f)) : 0ull;
-        const int tile0 = (int)(it0 / prm.chunks);
-        const int c00 = (int)(it0 - (long long)tile0 * prm.chunks);
+        const int tile0 = (int)(first_it / prm.chunks);
+        const int c00 = (int)(first_it - (long long)tile0 * prm.chunks);
+        auto advance = [&](int &tile, int &c) {
+            if (reverse) {
+                if (c == 0) {
+                    c = prm.chunks - 1;
+                    --tile;
+                } else {
+                    --c;
+                }
+            } else if (++c == prm.chunks) {
+                c = 0;
+                ++tile;
+            }
+        };
         auto load_a = [&](int q, int tile, int c) {
             const uint32_t sa = smem_base + (uint32_t)q * stage_bytes;
             if (a_keep > 0.0f) {
@@ -339,17 +364,14 @@ tc_stream_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant_
         for (int q = 0; q < pre; ++q) {
             mbar_expect_tx(full_bar(q), stage_bytes);
             load_a(q, tile, c);
-            if (++c == prm.chunks) {
-                c = 0;
-                ++tile;
-            }
+            advance(tile, c);
         }
         pdl_wait();
         {
-            int cb = c00;
+            int tb = tile0, cb = c00;
             for (int q = 0; q < pre; ++q) {
                 load_b(q, cb);
-                if (++cb == prm.chunks) cb = 0;
+                advance(tb, cb);
             }
         }
         int i = pre, q = 0;
@@ -363,10 +385,7 @@ tc_stream_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant_
             mbar_expect_tx(full_bar(q), stage_bytes);
             load_a(q, tile, c);
             load_b(q, c);
-            if (++c == prm.chunks) {
-                c = 0;
-                ++tile;
-            }
+            advance(tile, c);
             if (++q == stages) {
                 q = 0;
                 parity ^= 1u;
@@ -377,9 +396,9 @@ tc_stream_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant_
     } else if (warp == kStreamMma && lane == 0) {
         int q = 0, seg = 0;
         uint32_t parity = 0;
-        for (long long it = it0; it < it1 && !abort_flag; ++seg) {
-            const long long tile = it / prm.chunks;
-            const int seg_len = (int)(min(it1, (tile + 1) * prm.chunks) - it);
+        long long it = first_it;
+        for (int done = 0; done < count && !abort_flag; ++seg) {
+            const int seg_len = seg_len_at(it);
             const int ab = seg & (prm.acc_bufs - 1);
             const int use = prm.acc_bufs == 2 ? seg >> 1 : seg;
             if (use > 0 &&
@@ -410,17 +429,20 @@ tc_stream_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant_
                 }
             }
             if (abort_flag) break;
-            it += seg_len;
+            it += reverse ? -seg_len : seg_len;
+            done += seg_len;
             umma_commit(acc_full(ab));
         }
         umma_commit(mma_done);
     } else if (warp < 4) {
         // ---- epilogue: one segment at a time, TMEM -> partial slot ----
         int seg = 0;
-        for (long long it = it0; it < it1; ++seg) {
+        long long it = first_it;
+        for (int done = 0; done < count; ++seg) {
             const long long tile = it / prm.chunks;
-            const long long seg_end = min(it1, (tile + 1) * prm.chunks);
-            it = seg_end;
+            const int seg_len = seg_len_at(it);
+            it += reverse ? -seg_len : seg_len;
+            done += seg_len;
             const int ab = seg % prm.acc_bufs;
             const bool ok0 =
                 mbar_wait(acc_full(ab), (uint32_t)((seg / prm.acc_bufs) & 1), err, 24, true, spin);
@@ -1595,6 +1617,9 @@ struct LowpDense final : LowpDenseOperator {
         sprm.items = (long long)row_blocks * chunks_total;
         sprm.idesc = idesc;
         grid_g = (int)std::min<long long>((long long)sms * per_sm, sprm.items);
+        // tuning knob IPT_GB300_TC_ALTERNATE=0: every product walks forwards
+        alternate = env_int("IPT_GB300_TC_ALTERNATE", 1) != 0;
+        products = 0;
         splits = 1;
         for (int t = 0; t < row_blocks; ++t) {
             const long long f = tc::owner_of((long long)t * chunks_total, sprm.items, grid_g);
@@ -1653,9 +1678,10 @@ struct LowpDense final : LowpDenseOperator {
     {
         KernelTimerScope timer(kProfLowpProduct, s);
         if (streamk) {
+            const int reverse = alternate ? (int)(products++ & 1) : 0;
             return launch_pdl(tc::tc_stream_kernel<LowpTypes<LP>::kind>, dim3(grid_g),
                               dim3(tc::kStreamThreads), smem_bytes, s, mapA, mapB[cur], sprm,
-                              P.ptr, err.ptr, a_keep, hist, step, tol, spin);
+                              P.ptr, err.ptr, a_keep, hist, step, tol, spin, reverse);
         }
         const int row_blocks = (n + tc::kBM - 1) / tc::kBM;
         dim3 grid(row_blocks, splits);
@@ -1771,6 +1797,8 @@ struct LowpDense final : LowpDenseOperator {
     size_t smem_bytes = 0;
     uint32_t idesc = 0;
     bool streamk = false;
+    bool alternate = true;  // every other product walks its items backwards
+    long long products = 0;
     int grid_g = 0;
     tc::StreamParams sprm{};
     double scale = 1.0;
