@@ -1500,6 +1500,7 @@ struct LowpDense final : LowpDenseOperator {
                 fail(IPT_CUDA_CUDA_ERROR);
                 break;
             }
+            trace_mark(jb1 == nb ? "upper:first_chunk_moved" : (jb0 == 0 ? "upper:last_chunk_moved" : "upper:chunk_moved"), s);
             const int c0 = jb0 * 32, c1 = std::min(n, jb1 * 32);
             fused_setup_kernel<LP><<<c1 - c0, 256, 0, s2>>>(
                 su.fused_copy, n, ldp, LowpTypes<LP>::kind == kLowpF16 ? 1 : 0, nullptr, delta.ptr,
@@ -1510,6 +1511,7 @@ struct LowpDense final : LowpDenseOperator {
             }
             count_launch();
         }
+        trace_mark("upper:setups_done", s2);
         // s continues after the last setup
         if (cudaEventRecord(done, s2) != cudaSuccess || cudaStreamWaitEvent(s, done, 0) != cudaSuccess) {
             fail(IPT_CUDA_CUDA_ERROR);

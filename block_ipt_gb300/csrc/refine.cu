@@ -107,8 +107,14 @@ __global__ void defect_partial_kernel(const double *__restrict__ X, const double
     }
 }
 
+// Per column: the scaled residual, the largest |R0_ij| and the power-of-two
+// scale sigma_j = 2^floor(log2(1024 / max_i |R0_ij|)) (1 for a zero or
+// non-finite column, clamped to [1e-20, 1e20]) that brings the correction's
+// right-hand side into the low-precision operand's range.  floor(log2(x)) is
+// read from the exponent bits of x, exactly.
 __global__ void defect_finish_kernel(const double *__restrict__ P, int chunks, int k, double hnorm,
-                                     double *__restrict__ scaled, double *__restrict__ colmax)
+                                     double *__restrict__ scaled, double *__restrict__ colmax,
+                                     float *__restrict__ sigma)
 {
     pdl_wait();  // programmatic dependent launch: predecessor done
     pdl_trigger();
@@ -123,6 +129,13 @@ __global__ void defect_finish_kernel(const double *__restrict__ P, int chunks, i
     }
     scaled[j] = sqrt(rs) / (fmax(1.0, hnorm) * fmax(1.0, sqrt(xs)));
     colmax[j] = mx;
+    float sg = 1.0f;
+    if (mx > 0.0 && isfinite(mx)) {
+        const double x = 1024.0 / mx;
+        const int e = (int)(((unsigned long long)__double_as_longlong(x) >> 52) & 0x7FF) - 1023;
+        sg = (float)ldexp(1.0, e);
+    }
+    sigma[j] = fminf(fmaxf(sg, 1e-20f), 1e20f);
 }
 
 __global__ void add_kernel(double *__restrict__ X, const double *__restrict__ D, size_t count)
@@ -183,8 +196,7 @@ int refine_solve(const RefineInput &in, double *X_out, double *values_out, IPTBl
     float *sigma = reinterpret_cast<float *>(rnorm + k);  // k floats
     int *st_dev = reinterpret_cast<int *>(rnorm + 2 * k);
     double *P = rnorm + 3 * k;
-    std::vector<double> h_scaled((size_t)k), h_colmax((size_t)k);
-    std::vector<float> h_sigma((size_t)k);
+    std::vector<double> h_scaled((size_t)k);
     int h_status = 0;
 
     cudaEvent_t ev[4];
@@ -232,10 +244,8 @@ int refine_solve(const RefineInput &in, double *X_out, double *values_out, IPTBl
                                (const double *)X.ptr, (const double *)HX.ptr, in.d, n, k, R0.ptr,
                                c, P, in.lowp != nullptr ? 1 : 0));
         IPTGB_CHECK(launch_pdl(defect_finish_kernel, dim3(blocks_for(k)), dim3(kThreads), 0, s,
-                               (const double *)P, chunks, k, in.hnorm, scaled, colmax));
+                               (const double *)P, chunks, k, in.hnorm, scaled, colmax, sigma));
         IPTGB_CUDA(cudaMemcpyAsync(h_scaled.data(), scaled, (size_t)k * sizeof(double),
-                                   cudaMemcpyDeviceToHost, s));
-        IPTGB_CUDA(cudaMemcpyAsync(h_colmax.data(), colmax, (size_t)k * sizeof(double),
                                    cudaMemcpyDeviceToHost, s));
         IPTGB_CUDA(cudaStreamSynchronize(s));
         double mx = 0.0;
@@ -267,14 +277,7 @@ int refine_solve(const RefineInput &in, double *X_out, double *values_out, IPTBl
             break;
         }
         if (in.lowp != nullptr) {
-            for (int j = 0; j < k; ++j) {
-                const double m = h_colmax[(size_t)j];
-                h_sigma[(size_t)j] =
-                    (m > 0.0 && isfinite(m)) ? (float)ldexp(1.0, (int)floor(log2(1024.0 / m))) : 1.0f;
-                h_sigma[(size_t)j] = std::min(std::max(h_sigma[(size_t)j], 1e-20f), 1e20f);
-            }
-            IPTGB_CUDA(cudaMemcpyAsync(sigma, h_sigma.data(), (size_t)k * sizeof(float),
-                                       cudaMemcpyHostToDevice, s));
+            // sigma: written by defect_finish_kernel
             trace_mark("refine:correction", s);
             IPTGB_CHECK(in.lowp->refine_begin(R0.ptr, X.ptr, c, sigma));
             // device-side stop at inner_tol; the history is read every `check` steps

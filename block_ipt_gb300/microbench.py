@@ -10,7 +10,10 @@ library on cuda:0 (each prints one line and exits 0 on success):
         three runs; prints the per-launch time of the low-precision product;
     python -m block_ipt_gb300.microbench solve N [K]
         two FP16 mixed dense solves (ipt_block_solve_dense_device) of the
-        headline-family matrix.
+        headline-family matrix;
+    python -m block_ipt_gb300.microbench solve_host N [K]
+        FP16 mixed solves of it through the host entry from pinned memory,
+        with the phase marks of the last.
 
 Environment knobs of the library (IPT_GB300_*) apply as usual."""
 import ctypes as C
@@ -103,11 +106,51 @@ def solve(n, k=32):
         raise SystemExit(1)
 
 
+def solve_host(n, k=32):
+    """Three FP16 mixed solves through the host entry with H in pinned memory
+    (ipt_block_solve_dense); prints the wall time of the last and its phase
+    marks (GPU global timer and host clock)."""
+    torch = _torch()
+    import time
+    from . import _lib, api, workloads
+    lib = _lib.load()
+    H, _ = workloads.dense_config1(n, seed=0)
+    pinned = torch.from_numpy(np.asfortranarray(H).T.copy()).pin_memory()
+    del H
+    opt = api.block_options("fp16")
+    X = np.zeros((n, k), order="F")
+    v = np.zeros(k)
+    rep = _lib.IPTBlockReport()
+
+    def run():
+        st = lib.ipt_block_solve_dense(C.c_void_p(pinned.data_ptr()), n, k, C.byref(opt),
+                                       C.c_void_p(X.ctypes.data), C.c_void_p(v.ctypes.data),
+                                       C.byref(rep))
+        if st != 0:
+            raise SystemExit("ipt_block_solve_dense status %d" % st)
+
+    run()
+    run()
+    api.trace_enable(True)
+    t0 = time.perf_counter()
+    run()
+    ms = (time.perf_counter() - t0) * 1e3
+    marks = api.trace_read()
+    api.trace_enable(False)
+    print("host dense FP16 solve n=%d k=%d from pinned memory: %.3f ms, converged %d"
+          % (n, k, ms, rep.converged))
+    g0 = marks[0][2] if marks else 0
+    h0 = marks[0][1] if marks else 0
+    for label, host_ns, gpu_ns in marks:
+        print("  %-32s gpu %9.1f us  host %9.1f us" % (label, (gpu_ns - g0) / 1e3,
+                                                     (host_ns - h0) / 1e3))
+
+
 def main(argv):
-    if len(argv) < 2 or argv[0] not in ("accurate", "lowp", "solve"):
+    if len(argv) < 2 or argv[0] not in ("accurate", "lowp", "solve", "solve_host"):
         raise SystemExit(__doc__)
     args = [int(a) for a in argv[1:]]
-    {"accurate": accurate, "lowp": lowp, "solve": solve}[argv[0]](*args)
+    {"accurate": accurate, "lowp": lowp, "solve": solve, "solve_host": solve_host}[argv[0]](*args)
 
 
 if __name__ == "__main__":
