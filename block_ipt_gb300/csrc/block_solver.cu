@@ -47,7 +47,7 @@ void fill_default_options(IPTBlockOptions *opt)
     opt->oversample = -1;  // automatic
     opt->ipt_maxiter = 60;
     opt->ipt_tol = 1e-4;
-    opt->ipt_check_every = 1;
+    opt->ipt_check_every = 8;  // each read-back idles the GPU for a host round trip
     opt->residual_tol = 1e-8;
     opt->davidson_maxsteps = 40;
     opt->max_basis = 0;

@@ -847,9 +847,10 @@ __global__ void __launch_bounds__(256)
 // memory -> the full matrix in device memory, for the column blocks
 // [jb0, jb1) of 32 columns: tile (ib, jb), ib <= jb, is read once over the
 // host link (rows i <= j only) and written at (ib, jb) and, through shared
-// memory, transposed at (jb, ib).  A persistent grid of a few CTAs walks the
-// tiles, so the setup kernels of finished chunks keep SM slots beside it;
-// each thread keeps four host loads in flight.
+// memory, transposed at (jb, ib).  A persistent grid of four CTAs per SM
+// walks the tiles, each thread with four host loads in flight: host-memory
+// reads wait about 11 us under load on GB300 (211 GB/s needs ~2.4 MB in
+// flight); the setup kernels of finished chunks keep SM slots beside it.
 __global__ void __launch_bounds__(256)
 upper_to_device_kernel(const double *__restrict__ host, int n, int jb0, int jb1,
                        double *__restrict__ dev)
@@ -1483,8 +1484,8 @@ struct LowpDense final : LowpDenseOperator {
         }
         for (int jb1 = nb; jb1 > 0 && st == IPT_CUDA_SUCCESS; jb1 -= chunk_blocks) {
             const int jb0 = std::max(0, jb1 - chunk_blocks);
-            upper_to_device_kernel<<<std::max(1, sms), 256, 0, s>>>(su.upper_host, n, jb0, jb1,
-                                                                   su.fused_copy);
+            upper_to_device_kernel<<<std::max(1, 4 * sms), 256, 0, s>>>(su.upper_host, n, jb0,
+                                                                       jb1, su.fused_copy);
             if (cudaGetLastError() != cudaSuccess) {
                 fail(IPT_CUDA_CUDA_ERROR);
                 break;

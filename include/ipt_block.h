@@ -62,7 +62,8 @@ typedef struct {
     int oversample;         /* extra IPT columns carried into Rayleigh-Ritz (>= 0) */
     int ipt_maxiter;        /* IPT iterations before Rayleigh-Ritz */
     double ipt_tol;         /* stop the IPT stage once ||F(X)-X||_F/||X||_F <= ipt_tol */
-    int ipt_check_every;    /* fixed-point residual read back every this many iterations */
+    int ipt_check_every;    /* fixed-point residual read back every this many iterations
+                               (default 8) */
     double residual_tol;    /* scaled residual target (default 1e-8) */
     int davidson_maxsteps;  /* Davidson steps after the first Rayleigh-Ritz */
     int max_basis;          /* restart size; 0 = automatic */
