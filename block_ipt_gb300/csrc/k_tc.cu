@@ -844,51 +844,73 @@ __global__ void __launch_bounds__(256)
 }
 
 // Upper triangle of a symmetric H (column-major, ld = n) in pinned host
-// memory -> the full matrix in device memory, for the column blocks
-// [jb0, jb1) of 32 columns: tile (ib, jb), ib <= jb, is read once over the
-// host link (rows i <= j only) and written at (ib, jb) and, through shared
-// memory, transposed at (jb, ib).  A persistent grid of four CTAs per SM
-// walks the tiles, each thread with four host loads in flight: host-memory
-// reads wait about 11 us under load on GB300 (211 GB/s needs ~2.4 MB in
-// flight); the setup kernels of finished chunks keep SM slots beside it.
+// memory -> device memory, columns [c0, c1): column j's rows 0..j, read as
+// one contiguous run (16-byte loads, four in flight per thread: host-memory
+// reads wait about 11 us under load on GB300, and 211 GB/s over the host
+// link needs ~2.4 MB in flight, i.e. four such CTAs per SM).  CTA b takes
+// the columns c1 - 1 - b, c1 - 1 - b - G, ...: neighbouring columns are
+// nearly the same length, so the CTAs stay balanced.
 __global__ void __launch_bounds__(256)
-upper_to_device_kernel(const double *__restrict__ host, int n, int jb0, int jb1,
-                       double *__restrict__ dev)
+upper_copy_kernel(const double *__restrict__ host, int n, int c0, int c1, double *__restrict__ dev)
+{
+    for (int j = c1 - 1 - (int)blockIdx.x; j >= c0; j -= (int)gridDim.x) {
+        const size_t off = (size_t)j * n;  // n even: 16-byte aligned
+        const int pairs = (j + 1) / 2;     // rows 0 .. 2 pairs - 1
+        const double2 *src = reinterpret_cast<const double2 *>(host + off);
+        double2 *dst = reinterpret_cast<double2 *>(dev + off);
+        for (int q0 = threadIdx.x; q0 < pairs; q0 += 4 * blockDim.x) {
+            double2 v[4];
+#pragma unroll
+            for (int r = 0; r < 4; ++r) {
+                const int q = q0 + r * (int)blockDim.x;
+                if (q < pairs) v[r] = src[q];
+            }
+#pragma unroll
+            for (int r = 0; r < 4; ++r) {
+                const int q = q0 + r * (int)blockDim.x;
+                if (q < pairs) dst[q] = v[r];
+            }
+        }
+        if ((j & 1) == 0 && threadIdx.x == 0) dev[off + j] = host[off + j];  // the diagonal
+    }
+}
+
+// Lower triangle of the columns [c0, c1) of the device copy from the upper
+// triangle: entry (j, i), j > i, = entry (i, j) of column j.  32 x 32 tiles
+// (ib = column block of i in the chunk, jb >= ib) through shared memory.
+__global__ void __launch_bounds__(256)
+mirror_lower_kernel(double *__restrict__ dev, int n, int ib0, int ib1)
 {
     __shared__ double t[32][33];
     const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
-    // tiles of column block jb: ib = 0..jb; linear index over the chunk
-    const long long base = (long long)jb0 * (jb0 + 1) / 2;
-    const long long total = (long long)jb1 * (jb1 + 1) / 2 - base;
-    for (long long q = blockIdx.x; q < total; q += gridDim.x) {
-        // column block jb with base + q in [jb (jb + 1) / 2, (jb + 1) (jb + 2) / 2)
-        const long long g = base + q;
-        int jb = (int)((sqrt(8.0 * (double)g + 1.0) - 1.0) * 0.5);
-        while ((long long)(jb + 1) * (jb + 2) / 2 <= g) ++jb;
-        while ((long long)jb * (jb + 1) / 2 > g) --jb;
-        const int ib = (int)(g - (long long)jb * (jb + 1) / 2);
-        const int i0 = ib * 32, j0 = jb * 32;
-        const int i = i0 + tx;
-        double v[4];
-#pragma unroll
-        for (int r = 0; r < 4; ++r) {
-            const int j = j0 + ty + 8 * r;
-            v[r] = (j < n && i <= j) ? host[(size_t)j * n + i] : 0.0;
+    const int nb = (n + 31) / 32;
+    // tiles (ib, jb) with ib0 <= ib < ib1, ib <= jb < nb, numbered row by
+    // row (nb - ib tiles in row ib)
+    for (long long q = blockIdx.x;; q += gridDim.x) {
+        long long rem = q;
+        int ib = ib0;
+        while (ib < ib1 && rem >= nb - ib) {
+            rem -= nb - ib;
+            ++ib;
         }
-        __syncthreads();  // the previous tile's transpose has read t
+        if (ib >= ib1) break;
+        const int jb = ib + (int)rem;
+        const int i0 = ib * 32, j0 = jb * 32;
+        // read tile rows i0.., columns j0.. (upper part: i < j) of column j
 #pragma unroll
         for (int r = 0; r < 4; ++r) {
-            const int j = j0 + ty + 8 * r;
-            t[ty + 8 * r][tx] = v[r];
-            if (j < n && i <= j) dev[(size_t)j * n + i] = v[r];
+            const int j = j0 + ty + 8 * r, i = i0 + tx;
+            t[ty + 8 * r][tx] = (j < n && i < j) ? dev[(size_t)j * n + i] : 0.0;
         }
         __syncthreads();
+        // write column i (i0 + ii), rows j0 + tx (> i)
 #pragma unroll
         for (int r = 0; r < 4; ++r) {
             const int ii = ty + 8 * r;
-            const int row = j0 + tx, col = i0 + ii;  // entry (j, i) of the lower part
-            if (row < n && col < row) dev[(size_t)col * n + row] = t[tx][ii];
+            const int i = i0 + ii, j = j0 + tx;
+            if (j < n && i < j) dev[(size_t)i * n + j] = t[tx][ii];
         }
+        __syncthreads();
     }
 }
 
@@ -1484,8 +1506,9 @@ struct LowpDense final : LowpDenseOperator {
         }
         for (int jb1 = nb; jb1 > 0 && st == IPT_CUDA_SUCCESS; jb1 -= chunk_blocks) {
             const int jb0 = std::max(0, jb1 - chunk_blocks);
-            upper_to_device_kernel<<<std::max(1, 4 * sms), 256, 0, s>>>(su.upper_host, n, jb0,
-                                                                       jb1, su.fused_copy);
+            const int c0 = jb0 * 32, c1 = std::min(n, jb1 * 32);
+            upper_copy_kernel<<<std::max(1, 4 * sms), 256, 0, s>>>(su.upper_host, n, c0, c1,
+                                                                  su.fused_copy);
             if (cudaGetLastError() != cudaSuccess) {
                 fail(IPT_CUDA_CUDA_ERROR);
                 break;
@@ -1502,7 +1525,12 @@ struct LowpDense final : LowpDenseOperator {
                 break;
             }
             trace_mark(jb1 == nb ? "upper:first_chunk_moved" : (jb0 == 0 ? "upper:last_chunk_moved" : "upper:chunk_moved"), s);
-            const int c0 = jb0 * 32, c1 = std::min(n, jb1 * 32);
+            mirror_lower_kernel<<<2 * std::max(1, sms), 256, 0, s2>>>(su.fused_copy, n, jb0, jb1);
+            if (cudaGetLastError() != cudaSuccess) {
+                fail(IPT_CUDA_CUDA_ERROR);
+                break;
+            }
+            count_launch();
             fused_setup_kernel<LP><<<c1 - c0, 256, 0, s2>>>(
                 su.fused_copy, n, ldp, LowpTypes<LP>::kind == kLowpF16 ? 1 : 0, nullptr, delta.ptr,
                 split_hi, split_lo, inv_rows.ptr, su.diag, su.stats, vec, su.oz, su.oz_rowexp, c0);
