@@ -505,10 +505,10 @@ int dense_block_device(const double *dH_in, int n, int k, const IPTBlockOptions 
         su.split_lo = Hsplit.ptr ? Hsplit.ptr + mat : nullptr;
         // from pinned host memory only the upper triangle crosses the host
         // link (H is symmetric); the pass mirrors it into the device copy
-        // (n even, 16-byte aligned: the copy moves 16-byte pairs; otherwise
-        // the pass reads all of H from the host copy)
-        const bool upper = host_src != nullptr && n % 2 == 0 &&
-                           (reinterpret_cast<uintptr_t>(host_src) & 15) == 0;
+        // (an 8-byte aligned host copy; otherwise the pass reads all of H
+        // from it)
+        const bool upper = host_src != nullptr &&
+                           (reinterpret_cast<uintptr_t>(host_src) & 7) == 0;
         su.fused_src = host_src != nullptr && !upper ? host_src : dH_in;
         su.fused_copy = host_src != nullptr ? const_cast<double *>(dH_in) : nullptr;
         su.upper_host = upper ? host_src : nullptr;

@@ -851,8 +851,29 @@ __global__ void __launch_bounds__(256)
 // the columns c1 - 1 - b, c1 - 1 - b - G, ...: neighbouring columns are
 // nearly the same length, so the CTAs stay balanced.
 __global__ void __launch_bounds__(256)
-upper_copy_kernel(const double *__restrict__ host, int n, int c0, int c1, double *__restrict__ dev)
+upper_copy_kernel(const double *__restrict__ host, int n, int c0, int c1, double *__restrict__ dev,
+                  int pairs_ok)
 {
+    if (!pairs_ok) {
+        // odd n or an 8-byte aligned host copy: 8-byte loads, four in flight
+        for (int j = c1 - 1 - (int)blockIdx.x; j >= c0; j -= (int)gridDim.x) {
+            const size_t off = (size_t)j * n;
+            for (int q0 = threadIdx.x; q0 <= j; q0 += 4 * blockDim.x) {
+                double v[4];
+#pragma unroll
+                for (int r = 0; r < 4; ++r) {
+                    const int q = q0 + r * (int)blockDim.x;
+                    if (q <= j) v[r] = host[off + q];
+                }
+#pragma unroll
+                for (int r = 0; r < 4; ++r) {
+                    const int q = q0 + r * (int)blockDim.x;
+                    if (q <= j) dev[off + q] = v[r];
+                }
+            }
+        }
+        return;
+    }
     for (int j = c1 - 1 - (int)blockIdx.x; j >= c0; j -= (int)gridDim.x) {
         const size_t off = (size_t)j * n;  // n even: 16-byte aligned
         const int pairs = (j + 1) / 2;     // rows 0 .. 2 pairs - 1
@@ -1500,6 +1521,9 @@ struct LowpDense final : LowpDenseOperator {
                         ((reinterpret_cast<uintptr_t>(su.fused_copy) & 15) == 0) &&
                         ((reinterpret_cast<uintptr_t>(split_hi) & 7) == 0) &&
                         ((reinterpret_cast<uintptr_t>(split_lo) & 7) == 0);
+        const int pairs_ok = (n % 2 == 0) &&
+                             ((reinterpret_cast<uintptr_t>(su.upper_host) & 15) == 0) &&
+                             ((reinterpret_cast<uintptr_t>(su.fused_copy) & 15) == 0);
         // s2 starts after everything queued on s so far (allocations, zeroed stats)
         if (cudaEventRecord(done, s) != cudaSuccess || cudaStreamWaitEvent(s2, done, 0) != cudaSuccess) {
             fail(IPT_CUDA_CUDA_ERROR);
@@ -1508,7 +1532,7 @@ struct LowpDense final : LowpDenseOperator {
             const int jb0 = std::max(0, jb1 - chunk_blocks);
             const int c0 = jb0 * 32, c1 = std::min(n, jb1 * 32);
             upper_copy_kernel<<<std::max(1, 4 * sms), 256, 0, s>>>(su.upper_host, n, c0, c1,
-                                                                  su.fused_copy);
+                                                                  su.fused_copy, pairs_ok);
             if (cudaGetLastError() != cudaSuccess) {
                 fail(IPT_CUDA_CUDA_ERROR);
                 break;

@@ -138,6 +138,24 @@ __global__ void defect_finish_kernel(const double *__restrict__ P, int chunks, i
     sigma[j] = fminf(fmaxf(sg, 1e-20f), 1e20f);
 }
 
+// Steps launched past a correction check before the host waits for its
+// norms (each step ~25 us at n = 8192; a host round trip ~40 us).
+constexpr int kLookahead = 2;
+
+// Per host thread: a small page-locked buffer the check norms are copied
+// into, so that the copy is asynchronous (allocated on the thread's first
+// refinement and kept for the life of the process).
+double *pinned_check_norms()
+{
+    static thread_local double *buf = nullptr;
+    if (buf == nullptr) {
+        void *p = nullptr;
+        if (cudaMallocHost(&p, 4 * sizeof(double)) != cudaSuccess) return nullptr;
+        buf = static_cast<double *>(p);
+    }
+    return buf;
+}
+
 __global__ void add_kernel(double *__restrict__ X, const double *__restrict__ D, size_t count)
 {
     const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -235,6 +253,14 @@ int refine_solve(const RefineInput &in, double *X_out, double *values_out, IPTBl
     bool conv = false;
     SolveScratch scratch;
     IPTGB_CHECK(scratch.init(elems, s));
+    double *check_norms = pinned_check_norms();
+    if (check_norms == nullptr) return IPT_CUDA_ALLOCATION_FAILED;
+    cudaEvent_t check_ev = nullptr;
+    IPTGB_CUDA(cudaEventCreateWithFlags(&check_ev, cudaEventDisableTiming));
+    struct EventGuard {
+        cudaEvent_t e;
+        ~EventGuard() { cudaEventDestroy(e); }
+    } check_guard{check_ev};
     for (; outer < max_outer; ++outer) {
         trace_mark("refine:defect", s);
         IPTGB_CHECK(in.apply->apply(X.ptr, k, HX.ptr));
@@ -287,27 +313,39 @@ int refine_solve(const RefineInput &in, double *X_out, double *values_out, IPTBl
             }
             const int check = std::max(1, in.opt.ipt_check_every);
             int ran = 0;
+            // A check's norms are copied to pinned memory and the next
+            // kLookahead steps are launched before the host waits for them,
+            // so the GPU keeps iterating through the host's round trip; a
+            // correction that met inner_tol at the check takes those steps
+            // too (they only refine it further).
+            int pending = -1;
             for (int i = 0; i < in.inner_maxiter; ++i) {
                 const int want = ((i + 1) % check == 0) || i + 1 == in.inner_maxiter;
                 IPTGB_CHECK(in.lowp->refine_step(device_stop ? 0 : want, &scratch.ns));
                 ran = i + 1;
                 if (want) {
                     trace_mark("refine:correction_check", s);
-                    int stopped_at = -1;
-                    double rel = NAN;
                     if (device_stop) {
+                        int stopped_at = -1;
+                        double rel = NAN;
                         IPTGB_CHECK(scratch.read_history(i + 1, &stopped_at, &rel, s));
-                    } else {
-                        IPTGB_CUDA(cudaMemcpyAsync(scratch.host_norms, scratch.ns.norms,
-                                                   2 * sizeof(double), cudaMemcpyDeviceToHost, s));
-                        IPTGB_CUDA(cudaStreamSynchronize(s));
-                        rel = scratch.host_norms[0] / scratch.host_norms[1];
+                        if (stopped_at >= 0) {
+                            ran = stopped_at + 1;
+                            break;
+                        }
+                        if (!(rel > in.inner_tol)) break;  // non-finite: stop
+                        continue;
                     }
-                    if (stopped_at >= 0) {
-                        ran = stopped_at + 1;
-                        break;
-                    }
-                    if (!(rel > in.inner_tol)) break;  // non-finite: stop
+                    IPTGB_CUDA(cudaMemcpyAsync(check_norms, scratch.ns.norms, 2 * sizeof(double),
+                                               cudaMemcpyDeviceToHost, s));
+                    IPTGB_CUDA(cudaEventRecord(check_ev, s));
+                    pending = i;
+                }
+                if (pending >= 0 && (i - pending >= kLookahead || i + 1 == in.inner_maxiter)) {
+                    IPTGB_CUDA(cudaEventSynchronize(check_ev));
+                    pending = -1;
+                    const double rel = check_norms[0] / check_norms[1];
+                    if (!(rel > in.inner_tol)) break;  // met (or non-finite): stop
                 }
             }
             rep->lowp_matvecs += (long long)ran * k;

@@ -108,7 +108,8 @@ int ipt_block_solve_dense_device(const double *d_matrix_col_major, int n, int k,
 
 /* Dense symmetric H in host memory; vectors (n*k) and values (k) are host
  * buffers.  Copies H in, solves, copies the pairs out.  When H is in
- * page-locked memory and the solve is a mixed one (n <= 16384), only its
+ * page-locked memory (8-byte aligned) and the solve is a mixed one
+ * (n <= 16384), only its
  * upper triangle (diagonal included) is read, as LAPACK's dsyevd with
  * UPLO = 'U' does: n (n + 1) / 2 entries cross the host link in column
  * chunks while the setup pass of the chunks already on the device runs;
