@@ -845,28 +845,30 @@ __global__ void __launch_bounds__(256)
 
 // Upper triangle of a symmetric H (column-major, ld = n) in pinned host
 // memory -> device memory, columns [c0, c1): column j's rows 0..j, read as
-// one contiguous run (16-byte loads, four in flight per thread: host-memory
-// reads wait about 11 us under load on GB300, and 211 GB/s over the host
-// link needs ~2.4 MB in flight, i.e. four such CTAs per SM).  CTA b takes
-// the columns c1 - 1 - b, c1 - 1 - b - G, ...: neighbouring columns are
-// nearly the same length, so the CTAs stay balanced.
+// one contiguous run (16-byte loads, kCopyInFlight in flight per thread:
+// host-memory reads wait about 11 us under load on GB300, and 211 GB/s
+// over the host link needs ~2.4 MB in flight, i.e. two such CTAs per SM,
+// which leaves the rest of each SM to the setup pass of finished chunks).
+// CTA b takes the columns c1 - 1 - b, c1 - 1 - b - G, ...: neighbouring
+// columns are nearly the same length, so the CTAs stay balanced.
+constexpr int kCopyInFlight = 8;
 __global__ void __launch_bounds__(256)
 upper_copy_kernel(const double *__restrict__ host, int n, int c0, int c1, double *__restrict__ dev,
                   int pairs_ok)
 {
     if (!pairs_ok) {
-        // odd n or an 8-byte aligned host copy: 8-byte loads, four in flight
+        // odd n or an 8-byte aligned host copy: 8-byte loads
         for (int j = c1 - 1 - (int)blockIdx.x; j >= c0; j -= (int)gridDim.x) {
             const size_t off = (size_t)j * n;
-            for (int q0 = threadIdx.x; q0 <= j; q0 += 4 * blockDim.x) {
-                double v[4];
+            for (int q0 = threadIdx.x; q0 <= j; q0 += kCopyInFlight * blockDim.x) {
+                double v[kCopyInFlight];
 #pragma unroll
-                for (int r = 0; r < 4; ++r) {
+                for (int r = 0; r < kCopyInFlight; ++r) {
                     const int q = q0 + r * (int)blockDim.x;
                     if (q <= j) v[r] = host[off + q];
                 }
 #pragma unroll
-                for (int r = 0; r < 4; ++r) {
+                for (int r = 0; r < kCopyInFlight; ++r) {
                     const int q = q0 + r * (int)blockDim.x;
                     if (q <= j) dev[off + q] = v[r];
                 }
@@ -879,15 +881,15 @@ upper_copy_kernel(const double *__restrict__ host, int n, int c0, int c1, double
         const int pairs = (j + 1) / 2;     // rows 0 .. 2 pairs - 1
         const double2 *src = reinterpret_cast<const double2 *>(host + off);
         double2 *dst = reinterpret_cast<double2 *>(dev + off);
-        for (int q0 = threadIdx.x; q0 < pairs; q0 += 4 * blockDim.x) {
-            double2 v[4];
+        for (int q0 = threadIdx.x; q0 < pairs; q0 += kCopyInFlight * blockDim.x) {
+            double2 v[kCopyInFlight];
 #pragma unroll
-            for (int r = 0; r < 4; ++r) {
+            for (int r = 0; r < kCopyInFlight; ++r) {
                 const int q = q0 + r * (int)blockDim.x;
                 if (q < pairs) v[r] = src[q];
             }
 #pragma unroll
-            for (int r = 0; r < 4; ++r) {
+            for (int r = 0; r < kCopyInFlight; ++r) {
                 const int q = q0 + r * (int)blockDim.x;
                 if (q < pairs) dst[q] = v[r];
             }
@@ -1505,8 +1507,12 @@ struct LowpDense final : LowpDenseOperator {
     {
         const int nb = (n + 31) / 32;
         const int chunk_blocks = std::max(1, std::min(nb, 16));  // 512 columns
+        // the setup stream gets the highest priority: its CTAs take SM slots
+        // as they free up, ahead of later work on s
+        int prio_lo = 0, prio_hi = 0;
+        cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi);
         cudaStream_t s2 = nullptr;
-        IPTGB_CUDA(cudaStreamCreateWithFlags(&s2, cudaStreamNonBlocking));
+        IPTGB_CUDA(cudaStreamCreateWithPriority(&s2, cudaStreamNonBlocking, prio_hi));
         std::vector<cudaEvent_t> evs;
         int st = IPT_CUDA_SUCCESS;
         auto fail = [&](int code) {
@@ -1531,7 +1537,7 @@ struct LowpDense final : LowpDenseOperator {
         for (int jb1 = nb; jb1 > 0 && st == IPT_CUDA_SUCCESS; jb1 -= chunk_blocks) {
             const int jb0 = std::max(0, jb1 - chunk_blocks);
             const int c0 = jb0 * 32, c1 = std::min(n, jb1 * 32);
-            upper_copy_kernel<<<std::max(1, 4 * sms), 256, 0, s>>>(su.upper_host, n, c0, c1,
+            upper_copy_kernel<<<std::max(1, 2 * sms), 256, 0, s>>>(su.upper_host, n, c0, c1,
                                                                   su.fused_copy, pairs_ok);
             if (cudaGetLastError() != cudaSuccess) {
                 fail(IPT_CUDA_CUDA_ERROR);
