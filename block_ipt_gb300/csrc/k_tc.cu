@@ -494,6 +494,343 @@ tc_stream_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant_
     }
 }
 
+// ---------------------------------------------------------------------------
+// Symmetric form of the product (FP16 / BF16 Delta): Delta = Delta^T, so only
+// its upper 128 x 128 tiles (ib <= jb) are read, each once, and used twice:
+// as the K-major A operand for Y[ib] += T X[jb] and, through an MN-major
+// descriptor of the same shared-memory tile (the TMA's 128-byte swizzled
+// rows of 64 columns are MN-major atoms of the transpose: LBO = the 16 KB
+// between the two 64-column halves, SBO = 1 KB per 8 rows), for
+// Y[jb] += T^T X[ib].  Half of Delta's bytes per product, which at n = 8192
+// (67 MB) stays resident in L2 across the products of a solve.
+//
+// Work: super-tiles (IB, JB), IB <= JB, of 4 x 4 tiles, one CTA each at a
+// time; a super-tile keeps 4 row accumulators R[a] (MMA1, rows 4 IB + a) and
+// 4 column accumulators C[b] (MMA2, rows 4 JB + b) in TMEM, and the 8 X blocks
+// it needs in shared memory, while its tiles stream through a TMA ring.
+// Output row block r (super-block R = r / 4) receives its R-partials in
+// slots JB - R (JB = R .. nS - 1) and its C-partials in slots nS - R + IB
+// (IB = 0 .. R): every one of the nS + 1 slots of every row block is written
+// once per product (zeros for an accumulator no tile reaches), so the update
+// sums a fixed number of slots in a fixed order.
+// Warps 0-3 epilogue, warp 4 TMA producer, warp 5 MMA issuer.
+// ---------------------------------------------------------------------------
+constexpr int kSymG = 4;             // tiles per super-tile side
+constexpr uint32_t kSymTileBytes = 2 * kBM * kRowBytes;  // 128 x 128 FP16 = 32 KB
+
+struct SymParams {
+    int n, p, p_pad, nb, nS, stages;
+    int items;       // nS (nS + 1) / 2 super-tiles
+    uint32_t idesc;  // M = 128, N = p_pad, K-major A
+};
+
+__device__ __forceinline__ uint64_t mn_sw128_desc(uint32_t saddr)
+{
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr >> 4) & 0x3FFFu);
+    d |= (uint64_t)(16384u >> 4) << 16;  // LBO: next 64 MN elements (the second half)
+    d |= (uint64_t)(1024u >> 4) << 32;   // SBO: next 8 K rows
+    d |= (uint64_t)1 << 46;
+    d |= (uint64_t)2 << 61;
+    return d;
+}
+
+// super-tile index -> (IB, JB), IB <= JB, row by row
+__device__ __forceinline__ void sym_item(int it, int nS, int &IB, int &JB)
+{
+    int ib = 0, rem = it;
+    while (rem >= nS - ib) {
+        rem -= nS - ib;
+        ++ib;
+    }
+    IB = ib;
+    JB = ib + rem;
+}
+
+template <int KIND>
+__global__ void __launch_bounds__(kStreamThreads, 1)
+tc_sym_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+              const __grid_constant__ SymParams prm, float *__restrict__ P, int *err, float a_keep,
+              const double *hist, int step, double stop_tol, long long spin)
+{
+    if (hist != nullptr) {
+        pdl_wait();
+        if (hist_stopped(hist, step, stop_tol)) return;
+    }
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t *smem = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
+    const int stages = prm.stages;
+    const uint32_t bbox = (uint32_t)prm.p_pad * kRowBytes;  // one 64-wide K box of X
+    const uint32_t bblk = 2 * bbox;                          // one 128-row block of X
+    uint8_t *a_ring = smem;
+    uint8_t *b_area = smem + (size_t)stages * kSymTileBytes;  // 8 blocks: rows 0-3, cols 4-7
+    uint64_t *bars = reinterpret_cast<uint64_t *>(b_area + (size_t)2 * kSymG * bblk);
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 2 * stages + 5);
+    __shared__ volatile int abort_flag;
+    __shared__ int issued_count;
+
+    const int warp = threadIdx.x >> 5;
+    const int lane = threadIdx.x & 31;
+    const uint32_t a_base = smem_u32(a_ring);
+    const uint32_t b_base = smem_u32(b_area);
+    const uint32_t bar0 = smem_u32(bars);
+    auto full_bar = [&](int q) { return bar0 + 8u * (uint32_t)q; };
+    auto empty_bar = [&](int q) { return bar0 + 8u * (uint32_t)(stages + q); };
+    const uint32_t b_full = bar0 + 8u * (uint32_t)(2 * stages);
+    const uint32_t b_free = b_full + 8u;    // MMAs of a super-tile done: X blocks reusable
+    const uint32_t acc_full = b_full + 16u;
+    const uint32_t acc_empty = b_full + 24u;
+    const uint32_t mma_done = b_full + 32u;
+
+    if (threadIdx.x == 0) {
+        for (int q = 0; q < stages; ++q) {
+            mbar_init(full_bar(q), 1);
+            mbar_init(empty_bar(q), 1);
+        }
+        mbar_init(b_full, 1);
+        mbar_init(b_free, 1);
+        mbar_init(acc_full, 1);
+        mbar_init(acc_empty, 4);
+        mbar_init(mma_done, 1);
+        abort_flag = 0;
+        issued_count = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    if (warp == kStreamProducer) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                         smem_u32(tmem_slot)),
+                     "r"(512)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = *tmem_slot;
+    const int nb = prm.nb, nS = prm.nS;
+    const int G = gridDim.x;
+    // the tiles of super-tile (IB, JB) in order: a-major, then b
+    auto tile_ok = [&](int IB, int JB, int a, int b) {
+        const int ib = kSymG * IB + a, jb = kSymG * JB + b;
+        return ib < nb && jb < nb && ib <= jb;
+    };
+
+    if (warp == kStreamProducer && lane == 0) {
+        const uint64_t pol = a_keep > 0.0f ? l2_keep_policy(fminf(a_keep, 1.0f)) : 0ull;
+        int q = 0;
+        uint32_t parity = 0;
+        int issued = 0;
+        bool waited = false;
+        int st = 0;
+        for (int it = blockIdx.x; it < prm.items && !abort_flag; it += G, ++st) {
+            int IB, JB;
+            sym_item(it, nS, IB, JB);
+            // Delta tiles first (no dependence on the preceding kernel); the
+            // X blocks after the grid that wrote X is done and, from the
+            // second super-tile on, after the MMAs of the previous one
+            int pre_done = 0;
+            auto issue_tile = [&](int a, int b) -> bool {
+                if (issued >= stages &&
+                    !mbar_wait(empty_bar(q), parity ^ 1u, err, 31, false, spin)) {
+                    abort_flag = 1;
+                    return false;
+                }
+                const uint32_t dst = a_base + (uint32_t)q * kSymTileBytes;
+                const int row = (kSymG * IB + a) * kBM, col = (kSymG * JB + b) * kBM;
+                mbar_expect_tx(full_bar(q), kSymTileBytes);
+                if (a_keep > 0.0f) {
+                    tma_load_2d_hint(dst, &tmA, col, row, full_bar(q), pol);
+                    tma_load_2d_hint(dst + kSymTileBytes / 2, &tmA, col + 64, row, full_bar(q), pol);
+                } else {
+                    tma_load_2d(dst, &tmA, col, row, full_bar(q));
+                    tma_load_2d(dst + kSymTileBytes / 2, &tmA, col + 64, row, full_bar(q));
+                }
+                ++issued;
+                if (++q == stages) {
+                    q = 0;
+                    parity ^= 1u;
+                }
+                return true;
+            };
+            int a = 0, b = 0;
+            // prefetch up to `stages` tiles before the X blocks
+            for (; a < kSymG && pre_done < stages; ) {
+                if (tile_ok(IB, JB, a, b)) {
+                    if (!issue_tile(a, b)) break;
+                    ++pre_done;
+                }
+                if (++b == kSymG) {
+                    b = 0;
+                    ++a;
+                }
+            }
+            if (abort_flag) break;
+            if (!waited) {
+                pdl_wait();
+                waited = true;
+            }
+            if (st > 0 && !mbar_wait(b_free, (uint32_t)((st - 1) & 1), err, 32, false, spin)) {
+                abort_flag = 1;
+                break;
+            }
+            mbar_expect_tx(b_full, 2u * kSymG * bblk);
+            for (int g = 0; g < 2 * kSymG; ++g) {
+                // blocks 0-3: X rows of row blocks 4 IB + g (MMA2's K); 4-7:
+                // X rows of column blocks 4 JB + g - 4 (MMA1's K)
+                const int blk = g < kSymG ? kSymG * IB + g : kSymG * JB + g - kSymG;
+                const uint32_t dst = b_base + (uint32_t)g * bblk;
+                tma_load_2d(dst, &tmB, blk * kBM, 0, b_full);
+                tma_load_2d(dst + bbox, &tmB, blk * kBM + 64, 0, b_full);
+            }
+            for (; a < kSymG && !abort_flag; ) {
+                if (tile_ok(IB, JB, a, b) && !issue_tile(a, b)) break;
+                if (++b == kSymG) {
+                    b = 0;
+                    ++a;
+                }
+            }
+        }
+        if (!waited) pdl_wait();
+        issued_count = issued;
+        pdl_trigger();
+    } else if (warp == kStreamMma && lane == 0) {
+        const uint32_t id_k = prm.idesc;
+        const uint32_t id_mn = prm.idesc | (1u << 15);  // A transposed (MN-major)
+        int q = 0;
+        uint32_t parity = 0;
+        int st = 0;
+        for (int it = blockIdx.x; it < prm.items && !abort_flag; it += G, ++st) {
+            int IB, JB;
+            sym_item(it, nS, IB, JB);
+            if (st > 0 && !mbar_wait(acc_empty, (uint32_t)((st - 1) & 1), err, 33, false, spin)) {
+                abort_flag = 1;
+                break;
+            }
+            if (!mbar_wait(b_full, (uint32_t)(st & 1), err, 34, false, spin)) {
+                abort_flag = 1;
+                break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            uint32_t r_started = 0, c_started = 0;
+            for (int a = 0; a < kSymG && !abort_flag; ++a) {
+                for (int b = 0; b < kSymG; ++b) {
+                    if (!tile_ok(IB, JB, a, b)) continue;
+                    if (!mbar_wait(full_bar(q), parity, err, 35, false, spin)) {
+                        abort_flag = 1;
+                        break;
+                    }
+                    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                    const uint32_t ta = a_base + (uint32_t)q * kSymTileBytes;
+                    const uint32_t xr = b_base + (uint32_t)a * bblk;            // X[ib]
+                    const uint32_t xc = b_base + (uint32_t)(kSymG + b) * bblk;  // X[jb]
+                    const uint32_t accR = tmem + (uint32_t)(a * prm.p_pad);
+                    const uint32_t accC = tmem + (uint32_t)((kSymG + b) * prm.p_pad);
+                    const bool diag = kSymG * IB + a == kSymG * JB + b;
+#pragma unroll
+                    for (int kk = 0; kk < 8; ++kk) {
+                        const uint32_t h = (uint32_t)(kk >> 2), sub = (uint32_t)(kk & 3);
+                        // Y[ib] += T X[jb]: K = columns j of the tile
+                        umma<KIND>(accR, sw128_desc(ta + h * (kSymTileBytes / 2)) + 2 * sub,
+                                   sw128_desc(xc + h * bbox) + 2 * sub, id_k,
+                                   ((r_started >> a) & 1u) | (kk > 0 ? 1u : 0u));
+                    }
+                    r_started |= 1u << a;
+                    if (!diag) {
+#pragma unroll
+                        for (int kk = 0; kk < 8; ++kk) {
+                            const uint32_t h = (uint32_t)(kk >> 2), sub = (uint32_t)(kk & 3);
+                            // Y[jb] += T^T X[ib]: K = rows i of the tile, 16 per step
+                            umma<KIND>(accC, mn_sw128_desc(ta + (uint32_t)kk * 2048u),
+                                       sw128_desc(xr + h * bbox) + 2 * sub, id_mn,
+                                       ((c_started >> b) & 1u) | (kk > 0 ? 1u : 0u));
+                        }
+                        c_started |= 1u << b;
+                    }
+                    umma_commit(empty_bar(q));
+                    if (++q == stages) {
+                        q = 0;
+                        parity ^= 1u;
+                    }
+                }
+            }
+            if (abort_flag) break;
+            umma_commit(b_free);
+            umma_commit(acc_full);
+        }
+        umma_commit(mma_done);
+    } else if (warp < 4) {
+        // ---- epilogue: 8 accumulators of a super-tile -> their slots ----
+        int st = 0;
+        for (int it = blockIdx.x; it < prm.items; it += G, ++st) {
+            int IB, JB;
+            sym_item(it, nS, IB, JB);
+            const bool ok0 = mbar_wait(acc_full, (uint32_t)(st & 1), err, 36, true, spin);
+            if (__any_sync(0xffffffffu, !ok0 || abort_flag)) {
+                abort_flag = 1;
+                break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            for (int g = 0; g < 2 * kSymG; ++g) {
+                const bool row_role = g < kSymG;
+                const int blk = row_role ? kSymG * IB + g : kSymG * JB + g - kSymG;
+                if (blk >= nb) continue;
+                // did any tile of the super-tile reach this accumulator?
+                bool touched = false;
+                for (int o = 0; o < kSymG; ++o) {
+                    if (row_role) {
+                        touched = touched || tile_ok(IB, JB, g, o);
+                    } else {
+                        touched = touched || (tile_ok(IB, JB, o, g - kSymG) &&
+                                              kSymG * IB + o != blk);
+                    }
+                }
+                const int R = blk / kSymG;
+                const int slot = row_role ? JB - IB : nS - R + IB;
+                const int row = blk * kBM + warp * 32 + lane;
+                float *dst = P + (size_t)slot * prm.p * (size_t)prm.n + row;
+                for (int cb = 0; cb < prm.p_pad; cb += 32) {
+                    float v[32];
+                    if (touched) {
+                        tmem_ld_32cols(tmem + ((uint32_t)(warp * 32) << 16) +
+                                           (uint32_t)(g * prm.p_pad + cb),
+                                       v);
+                    } else {
+#pragma unroll
+                        for (int j = 0; j < 32; ++j) v[j] = 0.0f;
+                    }
+                    if (row < prm.n) {
+#pragma unroll
+                        for (int j = 0; j < 32; ++j) {
+                            if (cb + j < prm.p) dst[(size_t)(cb + j) * prm.n] = v[j];
+                        }
+                    }
+                }
+            }
+            asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+            __syncwarp();
+            if (lane == 0) mbar_arrive(acc_empty);
+        }
+    }
+    __syncwarp();
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == kStreamProducer && lane == 0) {
+        mbar_wait(mma_done, 0u, err, 37, true);
+        if (abort_flag) {
+            const int issued = issued_count;
+            for (int i = max(0, issued - stages); i < issued; ++i) {
+                mbar_wait(full_bar(i % stages), (uint32_t)((i / stages) & 1), err, 38, true);
+            }
+        }
+    }
+    __syncthreads();
+    if (warp == kStreamProducer) {
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(512)
+                     : "memory");
+    }
+}
+
 }  // namespace tc
 
 // FP32 storage of a TF32 tensor-core operand (values pre-rounded to TF32).
@@ -935,6 +1272,49 @@ mirror_lower_kernel(double *__restrict__ dev, int n, int ib0, int ib1)
         }
         __syncthreads();
     }
+}
+
+__device__ __forceinline__ float lp_to_float(__half v) { return __half2float(v); }
+__device__ __forceinline__ float lp_to_float(__nv_bfloat16 v) { return __bfloat162float(v); }
+__device__ __forceinline__ float lp_to_float(tf32_t v) { return v.v; }
+__device__ __forceinline__ float lp_to_float(float v) { return v; }
+
+// One common power-of-two scale for every row of a per-row scaled Delta (so
+// that the stored matrix is symmetric again, for the symmetric product):
+// the largest 1 / scale over the rows (one CTA), then each row multiplied by
+// its own 1 / scale over that largest one (a power of two <= 1: exact unless
+// an entry leaves FP16's normal range) and given the common 1 / scale.
+__global__ void __launch_bounds__(256) max_inv_row_kernel(const float *__restrict__ inv_row, int n,
+                                                          float *__restrict__ out)
+{
+    __shared__ float w[8];
+    float m = 0.0f;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) m = fmaxf(m, inv_row[i]);
+    for (int off = 16; off > 0; off >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, off));
+    if ((threadIdx.x & 31) == 0) w[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int k = 1; k < 8; ++k) m = fmaxf(m, w[k]);
+        out[0] = fmaxf(m, w[0]);
+    }
+}
+
+template <typename LP>
+__global__ void __launch_bounds__(256) common_row_scale_kernel(LP *__restrict__ delta, int ldp,
+                                                               float *__restrict__ inv_row,
+                                                               const float *__restrict__ gmax)
+{
+    const int row = blockIdx.x;
+    const float g = gmax[0];
+    const float f = inv_row[row] / g;  // power of two, <= 1
+    if (f != 1.0f) {
+        LP *r = delta + (size_t)row * ldp;
+        for (int l = threadIdx.x; l < ldp; l += blockDim.x) {
+            r[l] = to_lp<LP>(lp_to_float(r[l]) * f);
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) inv_row[row] = g;
 }
 
 __global__ void max_abs_offdiag_kernel(const double *__restrict__ H, int n,
@@ -1414,6 +1794,7 @@ struct LowpDense final : LowpDenseOperator {
         LowpDenseSetup none;
         LowpDenseSetup &su = setup != nullptr ? *setup : none;
         const bool symmetric = su.symmetric;
+        symmetric_delta = symmetric;
         float *split_hi = symmetric ? su.split_hi : nullptr;
         float *split_lo = symmetric ? su.split_lo : nullptr;
         if (split_hi == nullptr || split_lo == nullptr) split_hi = split_lo = nullptr;
@@ -1444,6 +1825,7 @@ struct LowpDense final : LowpDenseOperator {
                 IPTGB_LAUNCH();
             }
             scale = 1.0;  // per-row scales in inv_rows
+            per_row_scales = true;
             su.fused_done = true;
             su.split_done = split_hi != nullptr;
             su.oz_done = su.oz != nullptr && su.oz_rowexp != nullptr;
@@ -1631,6 +2013,14 @@ struct LowpDense final : LowpDenseOperator {
         // the split-K grid below).  Measured per product (FP16, k = 32):
         // n = 8192 22.1 us (one CTA per SM 28.0, split-K 23.3); n = 16384
         // 91-93 us for all three, 0.85-0.87 of the measured HBM bandwidth.
+        // symmetric form (FP16 / BF16, p_pad <= 64): half of Delta's bytes;
+        // tuning knob IPT_GB300_TC_SYM (0 = off, 2 = also below n = 6144)
+        const int sym_knob = env_int("IPT_GB300_TC_SYM", 1);
+        sym = false;
+        if (LowpTypes<LP>::kind != kLowpTF32 && p_pad <= 64 && symmetric_delta &&
+            (sym_knob >= 2 || (sym_knob == 1 && n >= 6144))) {
+            return set_width_sym(row_blocks);
+        }
         const int sk = env_int("IPT_GB300_TC_STREAMK", 2);
         streamk = sk > 0;
         if (streamk) return set_width_streamk(row_blocks, forced_stages, std::min(sk, 2));
@@ -1651,6 +2041,57 @@ struct LowpDense final : LowpDenseOperator {
         auto kfn = tc::tc_partial_kernel<LowpTypes<LP>::kind>;
         IPTGB_CUDA(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         (int)smem_bytes));
+        cur = 0;
+        return IPT_CUDA_SUCCESS;
+    }
+
+    // Symmetric product: super-tiles of 4 x 4 upper tiles, one per CTA at a
+    // time; nS + 1 partial slots per row block, every one written each
+    // product.  Delta's upper half is marked evict_last when it fits in L2.
+    int set_width_sym(int row_blocks)
+    {
+        sprm_sym = tc::SymParams{};
+        sprm_sym.n = n;
+        sprm_sym.p = p;
+        sprm_sym.p_pad = p_pad;
+        sprm_sym.nb = row_blocks;
+        sprm_sym.nS = (row_blocks + tc::kSymG - 1) / tc::kSymG;
+        sprm_sym.items = sprm_sym.nS * (sprm_sym.nS + 1) / 2;
+        sprm_sym.idesc = idesc;
+        const size_t bbytes = (size_t)2 * tc::kSymG * 2 * p_pad * tc::kRowBytes;
+        const size_t budget = 220u * 1024u;
+        if (bbytes + 2 * tc::kSymTileBytes > budget) return IPT_CUDA_INVALID_ARGUMENT;
+        stages = (int)std::min<size_t>(6, (budget - bbytes) / tc::kSymTileBytes);
+        sprm_sym.stages = stages;
+        smem_bytes = 1024 + (size_t)stages * tc::kSymTileBytes + bbytes + (2 * stages + 5) * 8 + 16;
+        grid_g = std::min(sprm_sym.items, sms);
+        splits = sprm_sym.nS + 1;
+        IPTGB_CHECK(P.alloc((size_t)splits * p * n, s));
+        IPTGB_CHECK(alloc_blocks());
+        auto kfn = tc::tc_sym_kernel<LowpTypes<LP>::kind>;
+        IPTGB_CUDA(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)smem_bytes));
+        // the upper half of Delta: all of it evict_last when it fits in 70 %
+        // of L2, else the share that does
+        int dev = 0, l2 = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, dev);
+        const double half = 0.5 * (double)n * (double)ldp * esize;
+        a_keep_sym = l2 > 0 ? (float)std::min(1.0, 0.7 * l2 / half) : 0.0f;
+        const int pct = env_int("IPT_GB300_L2_KEEP_PCT", -1);
+        if (pct >= 0) a_keep_sym = std::min(pct, 100) / 100.0f;
+        if (per_row_scales) {
+            // the fused setup scaled each row on its own: one common scale
+            DeviceBuffer<float> gmax;
+            IPTGB_CHECK(gmax.alloc(1, s));
+            max_inv_row_kernel<<<1, 256, 0, s>>>(inv_rows.ptr, n, gmax.ptr);
+            IPTGB_LAUNCH();
+            common_row_scale_kernel<LP><<<n, 256, 0, s>>>(delta.ptr, ldp, inv_rows.ptr, gmax.ptr);
+            IPTGB_LAUNCH();
+            per_row_scales = false;
+        }
+        sym = true;
+        streamk = false;
         cur = 0;
         return IPT_CUDA_SUCCESS;
     }
@@ -1738,6 +2179,11 @@ struct LowpDense final : LowpDenseOperator {
     int product_until(const double *hist, int step, double tol)
     {
         KernelTimerScope timer(kProfLowpProduct, s);
+        if (sym) {
+            return launch_pdl(tc::tc_sym_kernel<LowpTypes<LP>::kind>, dim3(grid_g),
+                              dim3(tc::kStreamThreads), smem_bytes, s, mapA, mapB[cur], sprm_sym,
+                              P.ptr, err.ptr, a_keep_sym, hist, step, tol, spin);
+        }
         if (streamk) {
             const int reverse = alternate ? (int)(products++ & 1) : 0;
             return launch_pdl(tc::tc_stream_kernel<LowpTypes<LP>::kind>, dim3(grid_g),
@@ -1857,6 +2303,11 @@ struct LowpDense final : LowpDenseOperator {
     int splits = 1, stages = 2, cur = 0;
     size_t smem_bytes = 0;
     uint32_t idesc = 0;
+    bool sym = false;
+    bool symmetric_delta = false;  // H symmetric: Delta == Delta^T up to row scales
+    bool per_row_scales = false;   // rows of the stored Delta carry their own scales
+    tc::SymParams sprm_sym{};
+    float a_keep_sym = 0.0f;
     bool streamk = false;
     bool alternate = true;  // every other product walks its items backwards
     long long products = 0;

@@ -87,6 +87,30 @@ def test_stream_and_split_schedules(cuda, monkeypatch, kind, n, k):
     assert np.array_equal(X2, got["2"])
 
 
+
+@pytest.mark.parametrize("prec", ["fp16", "bf16"])
+@pytest.mark.parametrize("n", [700, 2085, 6200])
+def test_symmetric_product_solve(cuda, monkeypatch, prec, n):
+    """The block solver's symmetric product (Delta's upper 128 x 128 tiles,
+    each used as A and, through an MN-major descriptor, as A^T;
+    IPT_GB300_TC_SYM=2 forces it below its default n = 6144) gives the
+    certified eigenpairs of the stream-K product, the same bits on a second
+    run, and the same IPT iteration count."""
+    H, _ = workloads.dense_config1(n, seed=31)
+    k = 24
+    monkeypatch.setenv("IPT_GB300_TC_SYM", "0")
+    X0, v0, r0 = api.block_solve_dense(H, k, prec)
+    monkeypatch.setenv("IPT_GB300_TC_SYM", "2")
+    X1, v1, r1 = api.block_solve_dense(H, k, prec)
+    X2, v2, r2 = api.block_solve_dense(H, k, prec)
+    assert r0["converged"] == 1 and r1["converged"] == 1
+    check_pairs(H, X1, v1, k)
+    hn = np.abs(H).sum(axis=1).max()
+    assert np.abs(v1 - v0).max() <= 1e-10 * hn
+    assert np.array_equal(X1, X2) and np.array_equal(v1, v2)
+    assert abs(r1["ipt_iterations"] - r0["ipt_iterations"]) <= 8
+
+
 @pytest.mark.parametrize("kind", ["fp16", "tf32", "fp32"])
 def test_mixed_converges_to_fp64_fixed_point(cuda, kind):
     H = oracle.perturbative_matrix(96, 1)
