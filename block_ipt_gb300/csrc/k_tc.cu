@@ -2013,9 +2013,13 @@ struct LowpDense final : LowpDenseOperator {
         // the split-K grid below).  Measured per product (FP16, k = 32):
         // n = 8192 22.1 us (one CTA per SM 28.0, split-K 23.3); n = 16384
         // 91-93 us for all three, 0.85-0.87 of the measured HBM bandwidth.
-        // symmetric form (FP16 / BF16, p_pad <= 64): half of Delta's bytes;
-        // tuning knob IPT_GB300_TC_SYM (0 = off, 2 = also below n = 6144)
-        const int sym_knob = env_int("IPT_GB300_TC_SYM", 1);
+        // symmetric form (FP16 / BF16, p_pad <= 64): half of Delta's bytes,
+        // twice the MMAs per byte.  Off by default: measured at n = 8192,
+        // k = 32 it took 27 us per product against 21 us for stream-K (one
+        // super-tile per SM leaves the MMA issue, the TMA ring and the
+        // epilogue in series) and its 17 partial slots per row slow the
+        // update.  Tuning knob IPT_GB300_TC_SYM: 1 = from n = 6144, 2 = always.
+        const int sym_knob = env_int("IPT_GB300_TC_SYM", 0);
         sym = false;
         if (LowpTypes<LP>::kind != kLowpTF32 && p_pad <= 64 && symmetric_delta &&
             (sym_knob >= 2 || (sym_knob == 1 && n >= 6144))) {

@@ -92,10 +92,10 @@ def test_stream_and_split_schedules(cuda, monkeypatch, kind, n, k):
 @pytest.mark.parametrize("n", [700, 2085, 6200])
 def test_symmetric_product_solve(cuda, monkeypatch, prec, n):
     """The block solver's symmetric product (Delta's upper 128 x 128 tiles,
-    each used as A and, through an MN-major descriptor, as A^T;
-    IPT_GB300_TC_SYM=2 forces it below its default n = 6144) gives the
-    certified eigenpairs of the stream-K product, the same bits on a second
-    run, and the same IPT iteration count."""
+    each used as A and, through an MN-major descriptor, as A^T; enabled with
+    IPT_GB300_TC_SYM=2) gives the certified eigenpairs of the stream-K
+    product, the same bits on a second run, and about the same IPT
+    iteration count."""
     H, _ = workloads.dense_config1(n, seed=31)
     k = 24
     monkeypatch.setenv("IPT_GB300_TC_SYM", "0")
