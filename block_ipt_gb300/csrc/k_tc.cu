@@ -1184,7 +1184,7 @@ __global__ void __launch_bounds__(256)
 // memory -> device memory, columns [c0, c1): column j's rows 0..j, read as
 // one contiguous run (16-byte loads, kCopyInFlight in flight per thread:
 // host-memory reads wait about 11 us under load on GB300, and 211 GB/s
-// over the host link needs ~2.4 MB in flight, i.e. two such CTAs per SM,
+// over the host link needs ~2.4 MB in flight, i.e. one such CTA per SM,
 // which leaves the rest of each SM to the setup pass of finished chunks).
 // CTA b takes the columns c1 - 1 - b, c1 - 1 - b - G, ...: neighbouring
 // columns are nearly the same length, so the CTAs stay balanced.
@@ -1919,8 +1919,8 @@ struct LowpDense final : LowpDenseOperator {
         for (int jb1 = nb; jb1 > 0 && st == IPT_CUDA_SUCCESS; jb1 -= chunk_blocks) {
             const int jb0 = std::max(0, jb1 - chunk_blocks);
             const int c0 = jb0 * 32, c1 = std::min(n, jb1 * 32);
-            upper_copy_kernel<<<std::max(1, 2 * sms), 256, 0, s>>>(su.upper_host, n, c0, c1,
-                                                                  su.fused_copy, pairs_ok);
+            upper_copy_kernel<<<std::max(1, sms), 256, 0, s>>>(su.upper_host, n, c0, c1,
+                                                              su.fused_copy, pairs_ok);
             if (cudaGetLastError() != cudaSuccess) {
                 fail(IPT_CUDA_CUDA_ERROR);
                 break;
