@@ -139,7 +139,13 @@ struct Fp64Stage final : IptStage {
         double fpres = NAN;
         int status = IPT_CUDA_SUCCESS;
         for (int it = 0; it < maxiter; ++it) {
-            const int want = ((it + 1) % check_every == 0) || it + 1 == maxiter;
+            // the first kFirstChecks steps are always checked, so a map that
+            // diverges from the start stops after the same few steps whatever
+            // check_every is (a diverged block would reach Rayleigh-Ritz as
+            // non-finite columns, and the identity restart is a worse start)
+            constexpr int kFirstChecks = 4;
+            const int want = it < kFirstChecks || ((it + 1) % check_every == 0) ||
+                             it + 1 == maxiter;
             status = op->step(x, y, d, want, &scratch.ns);
             if (status != IPT_CUDA_SUCCESS) break;
             done = it + 1;
