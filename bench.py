@@ -663,6 +663,7 @@ def batch_section(args, torch, dev):
             e1.synchronize()
             times.append(e0.elapsed_time(e1))
         reps = plan.reports()
+        shape = plan.shape()
         plan.close()
         lat = np.array([r["latency_ms"] for r in reps])
         ms = statistics.median(times)
@@ -674,7 +675,7 @@ def batch_section(args, torch, dev):
             "max_scaled_residual": float(max(r["max_scaled_residual"] for r in reps)),
             "mean_sweeps": float(np.mean([r["iterations"] for r in reps])),
             "mean_fp64_sweeps": float(np.mean([r["fp64_iterations"] for r in reps])),
-            "autotuned": {"threads": threads, "chunk": chunk}, "graph_launches": len(times) + 1}
+            "autotuned": shape, "graph_launches": len(times) + 1}
     # eigenvalue check of a few instances against LAPACK
     worst = 0.0
     for b in range(0, len(specs), max(1, len(specs) // 4)):

@@ -321,6 +321,7 @@ SIGNATURES = [
     ("ipt_block_batch_plan_autotune", _i, [_vp, _vp, C.POINTER(_i), C.POINTER(_i),
                                            C.POINTER(_d)]),
     ("ipt_block_batch_plan_reports", _i, [_vp, C.POINTER(IPTBatchReport)]),
+    ("ipt_block_batch_plan_shape", _i, [_vp] + [C.POINTER(C.c_int)] * 5),
     ("ipt_block_batch_plan_destroy", _i, [_vp]),
     ("ipt_block_mlp_init", _i, [_vp, C.c_ulonglong, _vp]),
     ("ipt_block_mlp_forward", _i, [_vp, _vp, C.c_longlong, _i, _vp, _vp]),

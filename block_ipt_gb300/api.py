@@ -291,6 +291,13 @@ class BatchPlan:
                "ipt_block_batch_plan_reports")
         return [{f: getattr(r, f) for f, _ in _lib.IPTBatchReport._fields_} for r in arr]
 
+    def shape(self):
+        v = [C.c_int(0) for _ in range(5)]
+        _check(self._lib.ipt_block_batch_plan_shape(self._plan, *[C.byref(x) for x in v]),
+               "ipt_block_batch_plan_shape")
+        return dict(zip(("threads", "chunk", "cluster", "ctas", "team_instances"),
+                        (x.value for x in v)))
+
     def close(self):
         if self._plan:
             self._lib.ipt_block_batch_plan_destroy(self._plan)

@@ -13,7 +13,12 @@ library on cuda:0 (each prints one line and exits 0 on success):
         headline-family matrix;
     python -m block_ipt_gb300.microbench solve_host N [K]
         FP16 mixed solves of it through the host entry from pinned memory,
-        with the phase marks of the last.
+        with the phase marks of the last;
+    python -m block_ipt_gb300.microbench batch COUNT [MIXED] [THREADS] [RUNS]
+        the batched solver on the first COUNT instances of the 512-instance
+        batched workload (MIXED = 1: FP32 sweeps and double-float
+        certification, 0: FP64 sweeps), default launch shape with THREADS
+        (256) per CTA, RUNS (2) graph launches, the last one timed.
 
 Environment knobs of the library (IPT_GB300_*) apply as usual."""
 import ctypes as C
@@ -146,11 +151,43 @@ def solve_host(n, k=32):
                                                      (host_ns - h0) / 1e3))
 
 
+def batch(count, mixed=1, threads=256, runs=2):
+    torch = _torch()
+    from . import api, workloads
+    specs = workloads.batch_config2(512, seed=0)[:count]
+    bufs, inst = [], []
+    for n, k, sig, seed in specs:
+        H, _ = workloads.batch_instance_torch(torch, n, sig, seed)
+        dX = torch.empty((k, n), dtype=torch.float64, device="cuda")
+        dv = torch.empty(k, dtype=torch.float64, device="cuda")
+        bufs.append((H, dX, dv))
+        inst.append((H.data_ptr(), n, k, dX.data_ptr(), dv.data_ptr()))
+    plan = api.BatchPlan(inst, "fp32" if mixed else "fp64", threads=threads)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    for _ in range(max(1, runs)):
+        torch.cuda.synchronize()
+        e0.record()
+        plan.run(torch.cuda.current_stream().cuda_stream)
+        e1.record()
+        e1.synchronize()
+    reps = plan.reports()
+    shape = plan.shape()
+    plan.close()
+    conv = sum(r["converged"] for r in reps)
+    print("batch of %d (%s): %.3f ms, converged %d, shape %s"
+          % (count, "mixed" if mixed else "fp64", e0.elapsed_time(e1), conv, shape))
+    if conv != count:
+        raise SystemExit(1)
+
+
 def main(argv):
-    if len(argv) < 2 or argv[0] not in ("accurate", "lowp", "solve", "solve_host"):
+    cmds = {"accurate": accurate, "lowp": lowp, "solve": solve, "solve_host": solve_host,
+            "batch": batch}
+    if len(argv) < 2 or argv[0] not in cmds:
         raise SystemExit(__doc__)
     args = [int(a) for a in argv[1:]]
-    {"accurate": accurate, "lowp": lowp, "solve": solve, "solve_host": solve_host}[argv[0]](*args)
+    cmds[argv[0]](*args)
 
 
 if __name__ == "__main__":

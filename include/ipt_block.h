@@ -405,6 +405,11 @@ int ipt_block_batch_plan_run(void *plan, void *stream);
 int ipt_block_batch_plan_autotune(void *plan, void *stream, int *threads, int *chunk,
                                   double *best_ms);
 int ipt_block_batch_plan_reports(void *plan, IPTBatchReport *reports);
+/* The launch shape in use: threads per CTA, rows of H per stage, cluster size
+ * of the launch (1: no clusters), the number of CTAs, and how many of the
+ * most expensive instances a whole cluster solves together. */
+int ipt_block_batch_plan_shape(void *plan, int *threads, int *chunk, int *cluster, int *ctas,
+                               int *team_instances);
 int ipt_block_batch_plan_destroy(void *plan);
 
 /* ---- matrix-free FCI-like Hamiltonians ------------------------------------ */

@@ -146,6 +146,43 @@ def test_batch_config2_shape(cuda):
     plan.close()
 
 
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_batch_cluster_teams_match_single_cta_solves(cuda, monkeypatch, precision):
+    """The most expensive instances are solved by a whole thread-block cluster
+    (rows split over its CTAs, sums exchanged through distributed shared
+    memory): the same blocks, sweep counts and eigenpairs as when every
+    instance runs on one CTA, and the LAPACK eigenvalues."""
+    torch = cuda
+    specs = [(2048, 16, 0.05, 31), (1536, 9, 0.1, 32), (1100, 13, 0.02, 33), (640, 4, 0.08, 34),
+             (300, 16, 0.06, 35), (96, 5, 0.03, 36), (257, 12, 0.1, 37), (64, 4, 0.01, 38)]
+    Hs, dev, inst = make_batch(torch, specs)
+    results = {}
+    for pct in ("25", "0"):
+        monkeypatch.setenv("IPT_GB300_BATCH_TEAM_PCT", pct)
+        plan = api.BatchPlan(inst, precision)
+        shape = plan.shape()
+        plan.run()
+        torch.cuda.synchronize()
+        reps = plan.reports()
+        plan.close()
+        if pct == "0":
+            assert shape["cluster"] == 1 and shape["team_instances"] == 0
+        else:
+            assert shape["cluster"] > 1 and shape["team_instances"] >= 2, shape
+        results[pct] = ([d[1].cpu().numpy().copy() for d in dev],
+                        [d[2].cpu().numpy().copy() for d in dev], reps)
+    (Xt, vt, rt), (Xs, vs, rs) = results["25"], results["0"]
+    for (n, k, _, _), H, a, b, va, vb, ra, rb in zip(specs, Hs, Xt, Xs, vt, vs, rt, rs):
+        assert ra["converged"] == 1 and rb["converged"] == 1
+        assert ra["iterations"] == rb["iterations"]
+        assert ra["fp64_iterations"] == rb["fp64_iterations"]
+        assert np.abs(a - b).max() <= 1e-12
+        hn = np.abs(H).sum(axis=1).max()
+        assert np.abs(va - vb).max() <= 1e-12 * hn
+        w = np.linalg.eigvalsh(H)[:k]
+        assert np.abs(np.sort(va) - w).max() <= 1e-10 * hn
+
+
 def test_batch_invalid_arguments(cuda):
     torch = cuda
     lib = _lib.load()
