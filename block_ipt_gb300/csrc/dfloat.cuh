@@ -106,6 +106,18 @@ __device__ __forceinline__ void df_acc(float &S, float &s, float ah, float al, f
     s = __fadd_rn(s, __fadd_rn(err, t));
 }
 
+// |h| = |hi| + sgn(hi) lo added to a double-float sum (S, C) on the FP32 pipe
+__device__ __forceinline__ void df_abs_add(float &S, float &C, float hi, float lo)
+{
+    const float a = fabsf(hi);
+    const float bl = hi < 0.0f ? -lo : lo;
+    const float t = __fadd_rn(S, a);
+    const float bp = __fsub_rn(t, S);
+    const float err = __fadd_rn(__fsub_rn(S, __fsub_rn(t, bp)), __fsub_rn(a, bp));
+    S = t;
+    C = __fadd_rn(C, __fadd_rn(err, bl));
+}
+
 // exact conversions
 __device__ __forceinline__ dfloat df_from_double(double v)
 {

@@ -84,10 +84,22 @@ struct Inst {
     const double *H;
     double *vectors;  // output n x k column-major
     double *values;   // output k
-    double *xa;       // scratch, row-major n x k
+    // FP64 scratch: two X blocks (n x KP, row-major, columns k..KP-1 zero),
+    // Y and G_ij = 1/(d_j - d_i) (n x k each), and, for double-float sweeps,
+    // the exact (hi, lo) float split of the two X blocks (n x KP each)
+    double *xa;
     double *xb;
     double *y;
-    float *h32;       // scratch n x n (mixed plans): FP32 rounding of H
+    double *g;
+    float2 *xsa;
+    float2 *xsb;
+    // FP32 scratch of mixed plans: two X blocks (n x KP), Y and G (n x k), and
+    // the FP32 rounding of H (n x n, written by the first FP32 sweep)
+    float *xa32;
+    float *xb32;
+    float *y32;
+    float *g32;
+    float *h32;
     int n;
     int k;
 };
@@ -120,21 +132,30 @@ struct Params {
 
 // arithmetic of one sweep's product
 enum Kind {
-    kF64 = 0,       // FP64 FMAs on H
-    kF32First = 1,  // FP32 FMAs, H rounded on load and written to h32
-    kF32 = 2,       // FP32 FMAs on h32
-    kDF = 3         // double-float terms on the exact (hi, lo) split of H
+    kF64 = 0,       // FP64 FMAs on H, FP64 X and Y
+    kF32First = 1,  // FP32 FMAs, H rounded on load and written to h32, FP32 X and Y
+    kF32 = 2,       // FP32 FMAs on h32, FP32 X and Y
+    kDF = 3         // double-float terms on the exact (hi, lo) split of H and X, FP64 Y
 };
 
 template <int L>
 struct Shared {
-    double xs[L * kKMax];         // staged X chunk (double, float or float2 entries)
+    double xs[2][L * kKMax];      // staged X chunks (double, float or float2 entries)
     double red[kMaxWarps][kRed];  // per-warp partial sums
     double part[2][kRed];         // this CTA's sums of the last two sweeps (read by the cluster)
     double tot[kRed];
     double lam[kKMax];
+    float lamf[kKMax];  // lam of an FP32 sweep
     int cur;
 };
+
+// The CTA's Shared<L>, in dynamic shared memory.
+extern __shared__ __align__(16) double g_batch_smem[];
+template <int L>
+__device__ __forceinline__ Shared<L> &smem()
+{
+    return *reinterpret_cast<Shared<L> *>(g_batch_smem);
+}
 
 __device__ __forceinline__ unsigned long long global_ns()
 {
@@ -155,33 +176,40 @@ __device__ __forceinline__ double warp_max_d(double x)
     return x;
 }
 
-// X chunk rows [l0, l0 + lc) into shared memory as KIND's operand type, KP
-// entries per row (zero past k).  X rows of other CTAs of a cluster were
-// written on other SMs: read through L2.
-template <int KIND, int KP, int L>
-__device__ __forceinline__ void stage_x(Shared<L> &sm, const double *__restrict__ X, int l0,
-                                        int lc, int k)
+// Bytes of one staged X entry of a sweep: FP64 X, FP32 X, or an X (hi, lo) pair.
+template <int KIND>
+struct EntryBytes {
+    static constexpr int value = KIND == kF32 || KIND == kF32First ? 4 : 8;
+};
+
+// Rows [l0, l0 + lc) of a KP-padded X block (row-major, 16-byte aligned) into
+// shared memory by 16-byte asynchronous copies through L2 (X rows of other
+// CTAs of a cluster were written on other SMs), committed as one group.
+template <int KIND, int KP>
+__device__ __forceinline__ void stage_async(double *xs, const void *X, int l0, int lc)
 {
-    for (int e = threadIdx.x; e < lc * KP; e += blockDim.x) {
-        const int l = e / KP;
-        const int j = e - l * KP;
-        const double v = j < k ? __ldcg(X + (size_t)(l0 + l) * k + j) : 0.0;
-        if (KIND == kF64) {
-            sm.xs[e] = v;
-        } else if (KIND == kDF) {
-            const dfloat d = df_from_double(v);
-            reinterpret_cast<float2 *>(sm.xs)[e] = make_float2(d.hi, d.lo);
-        } else {
-            reinterpret_cast<float *>(sm.xs)[e] = __double2float_rn(v);
-        }
+    constexpr int kRowBytes = KP * EntryBytes<KIND>::value;  // a multiple of 16
+    const char *src = static_cast<const char *>(X) + (size_t)l0 * kRowBytes;
+    const uint32_t dst = (uint32_t)__cvta_generic_to_shared(xs);
+    const int bytes = lc * kRowBytes;
+    for (int o = 16 * (int)threadIdx.x; o < bytes; o += 16 * (int)blockDim.x) {
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst + (uint32_t)o),
+                     "l"(src + o)
+                     : "memory");
     }
+    asm volatile("cp.async.commit_group;" ::: "memory");
 }
 
-// One column l of H (held in h: double for kF64/kF32First/kDF, float for
-// kF32) times the staged X row xr, into the row's accumulators.
+__device__ __forceinline__ void stage_wait()
+{
+    asm volatile("cp.async.wait_group 0;" ::: "memory");
+}
+
+// One column l of H (held in h: double for kF64/kF32First/kDF, float for kF32)
+// times the staged X row xrow, into the row's accumulators.
 template <int KIND, int KP>
-__device__ __forceinline__ void term(double h, float hf, const double *xrow, double *a64,
-                                     float *a32, float *e32)
+__device__ __forceinline__ void term(double h, float hf, float hl, const double *xrow,
+                                     double *a64, float *a32, float *e32)
 {
     if (KIND == kF64) {
         const double2 *xr = reinterpret_cast<const double2 *>(xrow);
@@ -192,13 +220,12 @@ __device__ __forceinline__ void term(double h, float hf, const double *xrow, dou
             a64[2 * q + 1] = fma(h, x.y, a64[2 * q + 1]);
         }
     } else if (KIND == kDF) {
-        const dfloat d = df_from_double(h);
         const float4 *xr = reinterpret_cast<const float4 *>(xrow);
 #pragma unroll
         for (int q = 0; q < KP / 2; ++q) {
             const float4 x = xr[q];
-            df_acc(a32[2 * q], e32[2 * q], d.hi, d.lo, x.x, x.y);
-            df_acc(a32[2 * q + 1], e32[2 * q + 1], d.hi, d.lo, x.z, x.w);
+            df_acc(a32[2 * q], e32[2 * q], hf, hl, x.x, x.y);
+            df_acc(a32[2 * q + 1], e32[2 * q + 1], hf, hl, x.z, x.w);
         }
     } else {
         const float4 *xr = reinterpret_cast<const float4 *>(xrow);
@@ -213,12 +240,36 @@ __device__ __forceinline__ void term(double h, float hf, const double *xrow, dou
     }
 }
 
-// Rows [r0, r1) of Y = H X in KIND's arithmetic.  With `rowsum`, also returns
-// the largest absolute row sum of those rows (from the FP64 entries).
-template <int KIND, int KP, int L>
-__device__ double product(const Inst &I, const double *__restrict__ X, Shared<L> &sm, int r0,
-                          int r1, bool rowsum)
+// One entry h = H[i, l] (FP64) of a sweep that reads H: the row sum of the
+// first sweep, the FP32 copy of the first FP32 sweep, the exact split of a
+// double-float sweep; then its term.
+template <int KIND, int KP>
+__device__ __forceinline__ void entry_term(const Inst &I, size_t off, double h, bool rowsum,
+                                           double &rs, const double *xrow, double *a64,
+                                           float *a32, float *e32)
 {
+    if (rowsum) rs += fabs(h);
+    if (KIND == kF64) {
+        term<KIND, KP>(h, 0.0f, 0.0f, xrow, a64, a32, e32);
+    } else if (KIND == kDF) {
+        const dfloat d = df_from_double(h);
+        term<KIND, KP>(h, d.hi, d.lo, xrow, a64, a32, e32);
+    } else {
+        const float hf = __double2float_rn(h);
+        I.h32[off] = hf;
+        term<KIND, KP>(h, hf, 0.0f, xrow, a64, a32, e32);
+    }
+}
+
+// Rows [r0, r1) of Y = H X in KIND's arithmetic.  With `rowsum`, also returns
+// the largest absolute row sum of those rows.  X chunks of L rows are copied
+// into two shared-memory buffers asynchronously, one chunk ahead of use, so
+// each chunk costs one barrier and no exposed L2 latency.
+template <int KIND, int KP, int L>
+__device__ __forceinline__ double product(const Inst &I, const void *X, void *Yv, int r0, int r1,
+                                          bool rowsum)
+{
+    Shared<L> &sm = smem<L>();
     // loads in flight per thread: FP32 entries are half the bytes
     constexpr int U = KIND == kF32 ? 16 : 8;
     // entries of one staged X row, in doubles
@@ -238,77 +289,72 @@ __device__ double product(const Inst &I, const double *__restrict__ X, Shared<L>
 #pragma unroll
         for (int j = 0; j < (KIND == kDF ? KP : 1); ++j) e32[j] = 0.0f;
         double rs = 0.0;
+        __syncthreads();  // both buffers free (previous row block or sweep done)
+        stage_async<KIND, KP>(sm.xs[0], X, 0, min(L, n));
+        int buf = 0;
         for (int l0 = 0; l0 < n; l0 += L) {
             const int lc = min(L, n - l0);
-            __syncthreads();
-            stage_x<KIND, KP, L>(sm, X, l0, lc, k);
-            __syncthreads();
-            if (!row) continue;
-            const size_t base = (size_t)l0 * n + i;
-            int l = 0;
-            for (; l + U <= lc; l += U) {
-                double hd[KIND == kF32 ? 1 : U];
-                float hf[KIND == kF32 ? U : 1];
-                if (KIND == kF32) {
-                    // written by this thread in the first FP32 sweep: plain loads
-                    const float *p = I.h32 + base + (size_t)l * n;
-#pragma unroll
-                    for (int u = 0; u < U; ++u) {
-                        hf[u] = *p;
-                        p += n;
-                    }
-                } else {
-                    const double *p = I.H + base + (size_t)l * n;
-#pragma unroll
-                    for (int u = 0; u < U; ++u) {
-                        hd[u] = __ldg(p);
-                        p += n;
-                    }
-                }
-#pragma unroll
-                for (int u = 0; u < U; ++u) {
-                    const double *xrow = sm.xs + (l + u) * XD;
+            stage_wait();
+            __syncthreads();  // chunk l0 staged; everyone done with the other buffer
+            if (l0 + L < n) stage_async<KIND, KP>(sm.xs[buf ^ 1], X, l0 + L, min(L, n - l0 - L));
+            if (row) {
+                const double *xs = sm.xs[buf];
+                const size_t base = (size_t)l0 * n + i;
+                int l = 0;
+                for (; l + U <= lc; l += U) {
+                    double hd[KIND == kF32 ? 1 : U];
+                    float hv[KIND == kF32 ? U : 1];
                     if (KIND == kF32) {
-                        term<KIND, KP>(0.0, hf[u], xrow, a64, a32, e32);
-                    } else {
-                        if (rowsum) rs += fabs(hd[u]);
-                        float h32 = 0.0f;
-                        if (KIND == kF32First) {
-                            h32 = __double2float_rn(hd[u]);
-                            I.h32[base + (size_t)(l + u) * n] = h32;
+                        // written by this thread in the first FP32 sweep: plain loads
+                        const float *p = I.h32 + base + (size_t)l * n;
+#pragma unroll
+                        for (int u = 0; u < U; ++u) {
+                            hv[u] = *p;
+                            p += n;
                         }
-                        term<KIND, KP>(hd[u], h32, xrow, a64, a32, e32);
+                    } else {
+                        const double *p = I.H + base + (size_t)l * n;
+#pragma unroll
+                        for (int u = 0; u < U; ++u) {
+                            hd[u] = __ldg(p);
+                            p += n;
+                        }
+                    }
+#pragma unroll
+                    for (int u = 0; u < U; ++u) {
+                        const double *xrow = xs + (l + u) * XD;
+                        if (KIND == kF32) {
+                            term<KIND, KP>(0.0, hv[u], 0.0f, xrow, a64, a32, e32);
+                        } else {
+                            entry_term<KIND, KP>(I, base + (size_t)(l + u) * n, hd[u], rowsum,
+                                                 rs, xrow, a64, a32, e32);
+                        }
+                    }
+                }
+                for (; l < lc; ++l) {
+                    const double *xrow = xs + l * XD;
+                    const size_t off = base + (size_t)l * n;
+                    if (KIND == kF32) {
+                        term<KIND, KP>(0.0, I.h32[off], 0.0f, xrow, a64, a32, e32);
+                    } else {
+                        entry_term<KIND, KP>(I, off, __ldg(I.H + off), rowsum, rs, xrow, a64,
+                                             a32, e32);
                     }
                 }
             }
-            for (; l < lc; ++l) {
-                const double *xrow = sm.xs + l * XD;
-                const size_t off = base + (size_t)l * n;
-                if (KIND == kF32) {
-                    term<KIND, KP>(0.0, I.h32[off], xrow, a64, a32, e32);
-                } else {
-                    const double h = __ldg(I.H + off);
-                    if (rowsum) rs += fabs(h);
-                    float h32 = 0.0f;
-                    if (KIND == kF32First) {
-                        h32 = __double2float_rn(h);
-                        I.h32[off] = h32;
-                    }
-                    term<KIND, KP>(h, h32, xrow, a64, a32, e32);
-                }
-            }
+            buf ^= 1;
         }
         if (row) {
-            double *yr = I.y + (size_t)i * k;
 #pragma unroll
             for (int j = 0; j < KP; ++j) {
                 if (j < k) {
                     if (KIND == kF64) {
-                        yr[j] = a64[j];
+                        static_cast<double *>(Yv)[(size_t)i * k + j] = a64[j];
                     } else if (KIND == kDF) {
-                        yr[j] = (double)a32[j] + (double)e32[j];
+                        static_cast<double *>(Yv)[(size_t)i * k + j] =
+                            (double)a32[j] + (double)e32[j];
                     } else {
-                        yr[j] = (double)a32[j];
+                        static_cast<float *>(Yv)[(size_t)i * k + j] = a32[j];
                     }
                 }
             }
@@ -319,37 +365,27 @@ __device__ double product(const Inst &I, const double *__restrict__ X, Shared<L>
 }
 
 template <int KIND, int L>
-__device__ __forceinline__ double product_kp(const Inst &I, const double *X, Shared<L> &sm, int r0,
+__device__ __forceinline__ double product_kp(const Inst &I, const void *X, void *Y, int r0,
                                              int r1, bool rowsum)
 {
     switch ((I.k + 3) >> 2) {
-    case 1: return product<KIND, 4, L>(I, X, sm, r0, r1, rowsum);
-    case 2: return product<KIND, 8, L>(I, X, sm, r0, r1, rowsum);
-    case 3: return product<KIND, 12, L>(I, X, sm, r0, r1, rowsum);
-    default: return product<KIND, 16, L>(I, X, sm, r0, r1, rowsum);
-    }
-}
-
-template <int L>
-__device__ __forceinline__ double product_any(int kind, const Inst &I, const double *X,
-                                              Shared<L> &sm, int r0, int r1, bool rowsum)
-{
-    switch (kind) {
-    case kF64: return product_kp<kF64, L>(I, X, sm, r0, r1, rowsum);
-    case kF32First: return product_kp<kF32First, L>(I, X, sm, r0, r1, rowsum);
-    case kF32: return product_kp<kF32, L>(I, X, sm, r0, r1, rowsum);
-    default: return product_kp<kDF, L>(I, X, sm, r0, r1, rowsum);
+    case 1: return product<KIND, 4, L>(I, X, Y, r0, r1, rowsum);
+    case 2: return product<KIND, 8, L>(I, X, Y, r0, r1, rowsum);
+    case 3: return product<KIND, 12, L>(I, X, Y, r0, r1, rowsum);
+    default: return product<KIND, 16, L>(I, X, Y, r0, r1, rowsum);
     }
 }
 
 // Solve instance order[q]: alone (TEAM false, rows [0, n)) or as CTA `rank`
 // of a cluster of `team` CTAs (rows in contiguous ranges of a multiple of 32).
 template <int L, bool TEAM>
-__device__ void solve(const Params &p, int q, Shared<L> &sm, int rank, int team)
+__device__ void solve(const Params &p, int q, int rank, int team)
 {
+    Shared<L> &sm = smem<L>();
     const int id = p.order[q];
     const Inst I = p.inst[id];
     const int n = I.n, k = I.k;
+    const int KP = (k + 3) & ~3;
     const int tid = threadIdx.x;
     const int lane = tid & 31;
     const int warp = tid >> 5;
@@ -369,15 +405,35 @@ __device__ void solve(const Params &p, int q, Shared<L> &sm, int rank, int team)
     };
     Out o{};
     if (tid == 0 && rank == 0) o.t_start = global_ns();
-    // X = the first k unit vectors (own rows)
-    for (size_t e = (size_t)r0 * k + tid; e < (size_t)r1 * k; e += blockDim.x) {
-        const int i = (int)(e / k);
-        const int j = (int)(e - (size_t)i * k);
-        I.xa[e] = i == j ? 1.0 : 0.0;
+    // own rows: X = the first k unit vectors (both buffers padded with zeros),
+    // G_ij = 1/(d_j - d_i) (the reference's factor, IPT_C_GPU/src/ipt_cuda.cu:
+    // 1369-1443), and their FP32 / split copies
+    for (size_t e = (size_t)r0 * KP + tid; e < (size_t)r1 * KP; e += blockDim.x) {
+        const int i = (int)(e / KP);
+        const int j = (int)(e - (size_t)i * KP);
+        const double x = i == j && j < k ? 1.0 : 0.0;
+        I.xa[e] = x;
+        I.xb[e] = 0.0;
+        if (p.certify_df) {
+            I.xsa[e] = make_float2((float)x, 0.0f);
+            I.xsb[e] = make_float2(0.0f, 0.0f);
+        }
+        if (p.mixed) {
+            I.xa32[e] = (float)x;
+            I.xb32[e] = 0.0f;
+        }
+        if (j < k) {
+            const size_t eg = (size_t)i * k + j;
+            const double g =
+                i == j ? 0.0 : 1.0 / (I.H[(size_t)j * n + j] - I.H[(size_t)i * n + i]);
+            I.g[eg] = g;
+            if (p.mixed) I.g32[eg] = (float)g;
+        }
     }
     team_sync();
-    double *X = I.xa;
-    double *Xn = I.xb;
+    double *X = I.xa, *Xn = I.xb;
+    float2 *Xs = I.xsa, *Xsn = I.xsb;
+    float *X32 = I.xa32, *Xn32 = I.xb32;
     bool fp64 = !p.mixed;
     bool h32_ready = false;
     double hinf = -1.0;
@@ -390,57 +446,89 @@ __device__ void solve(const Params &p, int q, Shared<L> &sm, int rank, int team)
         if (lane == 0) {
             for (int c = 0; c < kRed; ++c) sm.red[warp][c] = 0.0;
         }
-        const int kind = fp64 ? (p.certify_df ? kDF : kF64) : (h32_ready ? kF32 : kF32First);
         const bool first = hinf < 0.0;
-        double hs = product_any<L>(kind, I, X, sm, r0, r1, first);
-        if (kind == kF32First) h32_ready = true;
+        double hs;
+        if (fp64 && p.certify_df) {
+            hs = product_kp<kDF, L>(I, Xs, I.y, r0, r1, first);
+        } else if (fp64) {
+            hs = product_kp<kF64, L>(I, X, I.y, r0, r1, first);
+        } else if (h32_ready) {
+            hs = product_kp<kF32, L>(I, X32, I.y32, r0, r1, first);
+        } else {
+            hs = product_kp<kF32First, L>(I, X32, I.y32, r0, r1, first);
+            h32_ready = true;
+        }
         if (first) {
             hs = warp_max_d(hs);
             if (lane == 0) sm.red[warp][kHinf] = hs;
         }
         team_sync();  // Y rows of every CTA written
-        if (tid < k) sm.lam[tid] = __ldcg(I.y + (size_t)tid * k + tid);
-        __syncthreads();
-        // residuals r = Y - X diag(lambda), update X' = X + r / (d_j - d_i), norms
-        double fp_dx = 0.0, fp_x = 0.0;
-        for (int rb = r0; rb < r1; rb += blockDim.x) {
-            const int i = rb + tid;
-            const bool row = i < r1;
-            const double di = row ? I.H[(size_t)i * n + i] : 0.0;
-            for (int j = 0; j < k; ++j) {
-                double rr = 0.0, xx = 0.0, xy = 0.0;
-                if (row) {
-                    const size_t e = (size_t)i * k + j;
-                    const double x = X[e];
-                    const double yv = I.y[e];
-                    const double r = yv - sm.lam[j] * x;
-                    xy = x * yv;
-                    if (i != j) {
-                        const double dx = r / (I.H[(size_t)j * n + j] - di);
-                        Xn[e] = x + dx;
-                        fp_dx += dx * dx;
-                        rr = r * r;
-                    } else {
-                        Xn[e] = 1.0;
-                    }
-                    xx = x * x;
-                    fp_x += xx;
-                }
-                rr = warp_sum_d(rr);
-                xx = warp_sum_d(xx);
-                xy = warp_sum_d(xy);
-                if (lane == 0) {
-                    sm.red[warp][j] += rr;
-                    sm.red[warp][kKMax + j] += xx;
-                    sm.red[warp][2 * kKMax + j] += xy;
-                }
+        if (tid < k) {
+            if (fp64) {
+                sm.lam[tid] = __ldcg(I.y + (size_t)tid * k + tid);
+            } else {
+                sm.lamf[tid] = __ldcg(I.y32 + (size_t)tid * k + tid);
             }
         }
-        fp_dx = warp_sum_d(fp_dx);
-        fp_x = warp_sum_d(fp_x);
-        if (lane == 0) {
-            sm.red[warp][kDx] += fp_dx;
-            sm.red[warp][kXx] += fp_x;
+        __syncthreads();
+        // residuals r = Y - X diag(lambda), update X' = X + r o G, norms
+        if (!fp64) {
+            // FP32 sweep: FP32 arithmetic, only the fixed-point residual
+            float fdx = 0.0f, fx = 0.0f;
+            for (int rb = r0; rb < r1; rb += blockDim.x) {
+                const int i = rb + tid;
+                if (i >= r1) continue;
+                for (int j = 0; j < k; ++j) {
+                    const size_t e = (size_t)i * k + j, ex = (size_t)i * KP + j;
+                    const float x = X32[ex];
+                    if (i != j) {
+                        const float r = fmaf(-sm.lamf[j], x, I.y32[e]);
+                        const float dx = r * I.g32[e];
+                        Xn32[ex] = x + dx;
+                        fdx = fmaf(dx, dx, fdx);
+                    } else {
+                        Xn32[ex] = 1.0f;
+                    }
+                    fx = fmaf(x, x, fx);
+                }
+            }
+            const double sdx = warp_sum_d((double)fdx);
+            const double sx = warp_sum_d((double)fx);
+            if (lane == 0) {
+                sm.red[warp][kDx] += sdx;
+                sm.red[warp][kXx] += sx;
+            }
+        } else {
+            for (int rb = r0; rb < r1; rb += blockDim.x) {
+                const int i = rb + tid;
+                const bool row = i < r1;
+                for (int j = 0; j < k; ++j) {
+                    double rr = 0.0, xx = 0.0, xy = 0.0;
+                    if (row) {
+                        const size_t e = (size_t)i * k + j, ex = (size_t)i * KP + j;
+                        const double x = X[ex];
+                        const double yv = I.y[e];
+                        const double r = fma(-sm.lam[j], x, yv);
+                        xy = x * yv;
+                        const double xn = i != j ? fma(r, I.g[e], x) : 1.0;
+                        Xn[ex] = xn;
+                        if (p.certify_df) {
+                            const dfloat d = df_from_double(xn);
+                            Xsn[ex] = make_float2(d.hi, d.lo);
+                        }
+                        if (i != j) rr = r * r;
+                        xx = x * x;
+                    }
+                    rr = warp_sum_d(rr);
+                    xx = warp_sum_d(xx);
+                    xy = warp_sum_d(xy);
+                    if (lane == 0) {
+                        sm.red[warp][j] += rr;
+                        sm.red[warp][kKMax + j] += xx;
+                        sm.red[warp][2 * kKMax + j] += xy;
+                    }
+                }
+            }
         }
         __syncthreads();
         const int par = it & 1;
@@ -484,27 +572,41 @@ __device__ void solve(const Params &p, int q, Shared<L> &sm, int rank, int team)
             } else if (mx <= p.tol) {
                 done = true;  // X (not Xn) is the certified block
             }
+            if (!done) {
+                double *t = X;
+                X = Xn;
+                Xn = t;
+                float2 *ts = Xs;
+                Xs = Xsn;
+                Xsn = ts;
+                if (it64 >= p.maxiter) {
+                    ++it;
+                    break;
+                }
+            }
         } else {
             const double fp = sqrt(sm.tot[kDx]) / sqrt(fmax(sm.tot[kXx], 1e-300));
-            if (!isfinite(fp)) {
-                // the low-precision sweeps diverged: certify from the unit vectors
-                for (size_t e = (size_t)r0 * k + tid; e < (size_t)r1 * k; e += blockDim.x) {
-                    const int i = (int)(e / k);
-                    Xn[e] = i == (int)(e - (size_t)i * k) ? 1.0 : 0.0;
+            const bool diverged = !isfinite(fp);
+            if (diverged || fp <= p.lowp_tol || it + 1 >= p.lowp_maxiter) {
+                // FP64-accurate sweeps from here: the FP32 iterate as the FP64
+                // block (own rows), or, if the FP32 sweeps diverged, the unit
+                // vectors
+                for (size_t e = (size_t)r0 * KP + tid; e < (size_t)r1 * KP; e += blockDim.x) {
+                    const int i = (int)(e / KP);
+                    const int j = (int)(e - (size_t)i * KP);
+                    const double x = diverged ? (i == j && j < k ? 1.0 : 0.0) : (double)Xn32[e];
+                    X[e] = x;
+                    if (p.certify_df) {
+                        const dfloat d = df_from_double(x);
+                        Xs[e] = make_float2(d.hi, d.lo);
+                    }
                 }
-                if (TEAM) team_sync();  // every CTA's rows reset before the next product
+                team_sync();  // every row before the next product stages X
                 fp64 = true;
-            } else if (fp <= p.lowp_tol || it + 1 >= p.lowp_maxiter) {
-                fp64 = true;
-            }
-        }
-        if (!done) {
-            double *t = X;
-            X = Xn;
-            Xn = t;
-            if (fp64 && it64 >= p.maxiter) {
-                ++it;
-                break;
+            } else {
+                float *t = X32;
+                X32 = Xn32;
+                Xn32 = t;
             }
         }
     }
@@ -513,7 +615,7 @@ __device__ void solve(const Params &p, int q, Shared<L> &sm, int rank, int team)
     for (size_t e = (size_t)r0 * k + tid; e < (size_t)r1 * k; e += blockDim.x) {
         const int i = (int)(e / k);
         const int j = (int)(e - (size_t)i * k);
-        I.vectors[(size_t)j * n + i] = X[e];
+        I.vectors[(size_t)j * n + i] = X[(size_t)i * KP + j];
     }
     if (rank == 0) {
         // Rayleigh quotients of the returned block (the sums hold its last sweep)
@@ -531,10 +633,10 @@ __device__ void solve(const Params &p, int q, Shared<L> &sm, int rank, int team)
 }
 
 template <int L>
-__global__ void __launch_bounds__(512)
+__global__ void __launch_bounds__(512, 1)
 batch_ipt_kernel(Params p)
 {
-    __shared__ __align__(16) Shared<L> sm;
+    Shared<L> &sm = smem<L>();
     const int tid = threadIdx.x;
     int rank = 0;
     if (p.team > 1) rank = (int)cg::this_cluster().block_rank();
@@ -550,7 +652,7 @@ batch_ipt_kernel(Params p)
             cl.sync();  // every CTA has read the index before rank 0 moves on
             if (q >= p.count) return;
             if (q < p.n_team) {
-                solve<L, true>(p, q, sm, rank, p.team);
+                solve<L, true>(p, q, rank, p.team);
                 continue;
             }
             // past the team instances: rank 0 solves this one alone, the
@@ -563,7 +665,7 @@ batch_ipt_kernel(Params p)
             q = sm.cur;
             if (q >= p.count) return;
         }
-        solve<L, false>(p, q, sm, 0, 1);
+        solve<L, false>(p, q, 0, 1);
     }
 }
 
@@ -572,6 +674,22 @@ batch_ipt_kernel(Params p)
 // ---------------------------------------------------------------------------
 // Plan: device instance table, scratch pool, autotuned launch shape, graph.
 // ---------------------------------------------------------------------------
+// Scratch of one instance, rounded so that the next instance's blocks stay
+// 16-byte aligned: doubles (two KP-padded X blocks, their double-float
+// splits, Y and G) and, for mixed plans, floats (two KP-padded X blocks, Y,
+// G and the FP32 copy of H).
+inline size_t batch_doubles(int n, int k)
+{
+    const size_t kp = (size_t)((k + 3) & ~3);
+    return 4 * (size_t)n * kp + ((2 * (size_t)n * k + 1) & ~(size_t)1);
+}
+
+inline size_t batch_floats(int n, int k)
+{
+    const size_t kp = (size_t)((k + 3) & ~3);
+    return 2 * (size_t)n * kp + (((2 * (size_t)n * k + (size_t)n * n) + 3) & ~(size_t)3);
+}
+
 struct BatchPlan {
     int count = 0;
     std::vector<batch::Inst> host_inst;
@@ -609,10 +727,10 @@ struct BatchPlan {
         IPTGB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
         if (chunk == 64) {
             IPTGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                &per_sm, batch::batch_ipt_kernel<64>, threads, 0));
+                &per_sm, batch::batch_ipt_kernel<64>, threads, sizeof(batch::Shared<64>)));
         } else {
             IPTGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                &per_sm, batch::batch_ipt_kernel<128>, threads, 0));
+                &per_sm, batch::batch_ipt_kernel<128>, threads, sizeof(batch::Shared<128>)));
         }
         const int full = std::max(1, sms * std::max(1, per_sm));
         cluster = 1;
@@ -628,6 +746,8 @@ struct BatchPlan {
             cudaLaunchConfig_t cfg = {};
             cfg.gridDim = dim3((unsigned)(full / c * c));
             cfg.blockDim = dim3((unsigned)threads);
+            cfg.dynamicSmemBytes = chunk == 64 ? sizeof(batch::Shared<64>)
+                                               : sizeof(batch::Shared<128>);
             cudaLaunchAttribute attr[1];
             attr[0].id = cudaLaunchAttributeClusterDimension;
             attr[0].val.clusterDim.x = (unsigned)c;
@@ -675,6 +795,7 @@ struct BatchPlan {
         cudaLaunchConfig_t cfg = {};
         cfg.gridDim = dim3((unsigned)ctas);
         cfg.blockDim = dim3((unsigned)threads);
+        cfg.dynamicSmemBytes = chunk == 64 ? sizeof(batch::Shared<64>) : sizeof(batch::Shared<128>);
         cfg.stream = s;
         cudaLaunchAttribute attr[1];
         attr[0].id = cudaLaunchAttributeClusterDimension;
@@ -773,9 +894,8 @@ IPT_API int ipt_block_batch_plan_create(const IPTBatchInstance *instances, int c
             x.k <= 0 || x.k > batch::kKMax || x.k > x.n) {
             return IPT_CUDA_INVALID_ARGUMENT;
         }
-        pool += 3 * (size_t)x.n * x.k;
-        // FP32 copy of H for the FP32 sweeps, 16-byte aligned per instance
-        if (mixed) pool32 += ((size_t)x.n * x.n + 3) & ~(size_t)3;
+        pool += batch_doubles(x.n, x.k);
+        if (mixed) pool32 += batch_floats(x.n, x.k);
     }
     auto *P = new BatchPlan();
     P->count = count;
@@ -809,15 +929,24 @@ IPT_API int ipt_block_batch_plan_create(const IPTBatchInstance *instances, int c
             I.values = x.values;
             I.n = x.n;
             I.k = x.k;
+            // KP-padded X blocks first: every block starts 16-byte aligned
+            const size_t nkp = (size_t)x.n * (size_t)((x.k + 3) & ~3);
             const size_t nk = (size_t)x.n * x.k;
             I.xa = P->pool + off;
-            I.xb = I.xa + nk;
-            I.y = I.xb + nk;
-            off += 3 * nk;
-            I.h32 = nullptr;
+            I.xb = I.xa + nkp;
+            I.xsa = reinterpret_cast<float2 *>(I.xb + nkp);
+            I.xsb = I.xsa + nkp;
+            I.y = reinterpret_cast<double *>(I.xsb + nkp);
+            I.g = I.y + nk;
+            off += batch_doubles(x.n, x.k);
+            I.xa32 = I.xb32 = I.y32 = I.g32 = I.h32 = nullptr;
             if (mixed) {
-                I.h32 = P->pool32 + off32;
-                off32 += ((size_t)x.n * x.n + 3) & ~(size_t)3;
+                I.xa32 = P->pool32 + off32;
+                I.xb32 = I.xa32 + nkp;
+                I.y32 = I.xb32 + nkp;
+                I.g32 = I.y32 + nk;
+                I.h32 = I.g32 + nk;
+                off32 += batch_floats(x.n, x.k);
             }
         }
         // longest (n^2 k) first

@@ -33,6 +33,7 @@
 
 #include "block_solver.h"
 #include "common.cuh"
+#include "dfloat.cuh"
 #include "fpconv.cuh"
 #include "lowp.h"
 #include "oz.cuh"
@@ -937,18 +938,6 @@ __device__ __forceinline__ float sym_entry(double h, int s2, double scale, float
         lo = __double2float_rn(h - (double)hi);
     }
     return (float)(scale * h);
-}
-
-// |h| = |hi| + sgn(hi) lo added to a double-float sum (S, C) on the FP32 pipe
-__device__ __forceinline__ void df_abs_add(float &S, float &C, float hi, float lo)
-{
-    const float a = fabsf(hi);
-    const float bl = hi < 0.0f ? -lo : lo;
-    const float t = __fadd_rn(S, a);
-    const float bp = __fsub_rn(t, S);
-    const float err = __fadd_rn(__fsub_rn(S, __fsub_rn(t, bp)), __fsub_rn(a, bp));
-    S = t;
-    C = __fadd_rn(C, __fadd_rn(err, bl));
 }
 
 // (S, C) += (So, Co) for double-float pairs

@@ -381,7 +381,7 @@ typedef struct {
     int maxiter;          /* FP64 sweeps per instance */
     int lowp_maxiter;     /* FP32 sweeps per instance */
     double lowp_tol;      /* FP32 fixed-point residual at which to switch */
-    int threads;          /* 0 = default (512) or 128 / 256 / 512 */
+    int threads;          /* 0 = default (256) or 128 / 256 / 512 */
     int chunk;            /* 0 = default (128) or 64 / 128 rows of H per stage */
     int certify_precision; /* -1 = default (IPT_BLOCK_DF64 after FP32 sweeps,
                               IPT_BLOCK_FP64 otherwise), IPT_BLOCK_FP64 or
