@@ -596,20 +596,32 @@ def learned_section(args, torch, dev, stream, flush, solve, opt, e0, e1, plain_t
     got = learned.collect(torch, held, 16, rows, 0)
     loss_plain, loss_neumann, loss_mlp = learned.correction_losses(torch, params, rows, got)
     del rows
-    opt.preconditioner = 1
-    opt.mlp_params = C.c_void_p(params.data_ptr())
-    solve()
-    times, rep = [], None
-    for _ in range(max(1, args.fci_steps)):
-        flush.zero_()
-        e0.record(stream)
-        rep = solve()
-        e1.record(stream)
-        e1.synchronize()
-        times.append(e0.elapsed_time(e1))
-    opt.preconditioner = 0
-    opt.mlp_params = None
+    def timed_with(p):
+        opt.preconditioner = 1
+        opt.mlp_params = C.c_void_p(p.data_ptr())
+        solve()
+        ts, r = [], None
+        for _ in range(max(1, args.fci_steps)):
+            flush.zero_()
+            e0.record(stream)
+            r = solve()
+            e1.record(stream)
+            e1.synchronize()
+            ts.append(e0.elapsed_time(e1))
+        opt.preconditioner = 0
+        opt.mlp_params = None
+        return ts, r
+
+    times, rep = timed_with(params)
+    # ablation: the unweighted two-term correction (weight 1 on every row)
+    two = torch.zeros_like(params)
+    two[-1] = 30.0
+    two_times, two_rep = timed_with(two)
     return {"ms": statistics.mean(times), "plain_ms": statistics.mean(plain_times),
+            "two_term_ms": statistics.mean(two_times), "two_term_steps": two_rep["davidson_steps"],
+            "two_term_fp64_matvecs": two_rep["fp64_matvecs"],
+            "two_term_precond_matvecs": two_rep["precond_matvecs"],
+            "selected": info.get("selected"), "validation_steps": info.get("validation_steps"),
             "steps": rep["davidson_steps"], "plain_steps": plain_rep["davidson_steps"],
             "fp64_matvecs": rep["fp64_matvecs"], "plain_fp64_matvecs": plain_rep["fp64_matvecs"],
             "precond_matvecs": rep["precond_matvecs"],

@@ -8,9 +8,13 @@
 // t1 = (D - theta)^-1 r and the second-order term u = -(D - theta)^-1 Delta t1,
 // which costs one product with H (H t1, the diagonal part taken off).  The
 // learned correction is t_i = t1_i + o_i u_i with the network's per-row
-// weight o_i clamped to [kWeightLo, kWeightHi]: o = 0 everywhere is the
-// plain preconditioner, o = 1 the two-term Neumann correction, and the
-// output bias starts at 1.  Features of row i, all O(1):
+// weight o_i = sigmoid(z_i), z_i its linear output: o -> 1 everywhere is the
+// two-term Neumann correction, near which training starts (output bias 4:
+// o = 0.982), o -> 0 the plain preconditioner.  The two-term correction is
+// a strong baseline on the FCI-like family (it saves about 40 % of the
+// Davidson steps of the plain one); the network learns per row how much of
+// the second-order term to keep, never more than all of it.  Features of
+// row i, all O(1):
 //   f0 = t1_i sqrt(n) / ||t1||       plain correction, normalised
 //   f1 = u_i sqrt(n) / ||t1||        second-order term, same units
 //   f2 = x_i sqrt(n)                 Ritz vector (unit norm)
@@ -23,10 +27,17 @@
 // against the converged eigenvectors x*): the part of the exact error that
 // lies outside the current search space V, e = (I - V V^T)(s x*_l - x)
 // (x*_l the converged vector that overlaps x most, s its sign), scaled by
-// the least-squares fit e ~ alpha (I - V V^T)(t1 + u); per row the weight
-// that reproduces it, y_i = (e_i / alpha - t1_i) / u_i, with weight
-// w_i = f1_i^2, so that the weighted loss sum_i w_i (o_i - y_i)^2 equals
-// ||t1 + o o u - e / alpha||^2 in the units of f1.
+// the least-squares fit e ~ alpha (I - V V^T)(t1 + u).  Davidson keeps only
+// the part of a correction outside V, so the targets compare projected
+// vectors: with p = (I - V V^T) t1 and q = (I - V V^T) u, per row the weight
+// that reproduces the scaled error, y_i = (e_i / alpha - p_i) / q_i, with
+// weight w_i = n q_i^2 / ||t1||^2, so that the weighted loss
+// sum_i w_i (o_i - y_i)^2 equals ||p + o o q - e / alpha||^2 in the units
+// of f1: for o = 1 (the two-term correction) and o = 0 (the plain one) it is
+// the error of exactly the direction the Davidson step adds.  (Comparing the
+// unprojected t1 + o u instead ranks the two-term correction below the plain
+// one, although it saves Davidson steps: its components inside V count
+// against it there and are discarded by the step.)
 //
 // Training runs on the GPU: a fused forward/backward kernel over 128-row
 // tiles of a batch (per-tile gradient partials, no atomics) and an Adam
@@ -76,9 +87,6 @@ __device__ __forceinline__ float clampf(float v, float lim)
     return fminf(fmaxf(v, -lim), lim);
 }
 
-// Range of the learned weight of the second-order term.
-constexpr float kWeightLo = -1.f;
-constexpr float kWeightHi = 3.f;
 
 __device__ __forceinline__ void row_features(double t, double tn, double u, double rn, double x,
                                              double delta, double sigma, double clip,
@@ -94,7 +102,12 @@ __device__ __forceinline__ void row_features(double t, double tn, double u, doub
     f[5] = clampf((float)(log10(rn / fmax(1.0, hnorm) + 1e-300) / 8.0), 40.f);
 }
 
-// o = W3 relu(W2 relu(W1 f + b1) + b2) + b3 with the parameters in shared memory
+// Weight of the second-order term from the network's linear output z.
+constexpr float kOutBias = 4.f;  // initial z: o = sigmoid(4) = 0.982
+__device__ __forceinline__ float weight_of(float z) { return 1.f / (1.f + expf(-z)); }
+
+// o = sigmoid(z), z = W3 relu(W2 relu(W1 f + b1) + b2) + b3, with the
+// parameters in shared memory
 __device__ __forceinline__ float forward_row(const float *__restrict__ P, const float f[kIn])
 {
     float h1[kH];
@@ -119,7 +132,7 @@ __device__ __forceinline__ float forward_row(const float *__restrict__ P, const 
         }
         o = fmaf(P[oW3 + j], fmaxf(s, 0.f), o);
     }
-    return o;
+    return weight_of(o);
 }
 
 __device__ __forceinline__ void load_params(const float *__restrict__ g, float *s)
@@ -130,8 +143,9 @@ __device__ __forceinline__ void load_params(const float *__restrict__ g, float *
 
 // ---------------------------------------------------------------------------
 // Initialisation: weights U(-a, a) with a = sqrt(6 / fan_in) (ReLU layers) and
-// 0.1 sqrt(3 / fan_in) (linear output), hidden biases 0, output bias 1 (the
-// plain correction); counter-based, seeded.
+// 0.1 sqrt(3 / fan_in) (linear output), hidden biases 0, output bias
+// kOutBias (so o starts near 1, the two-term correction); counter-based,
+// seeded.
 // ---------------------------------------------------------------------------
 __global__ void mlp_init_kernel(float *__restrict__ params, unsigned long long seed)
 {
@@ -143,7 +157,7 @@ __global__ void mlp_init_kernel(float *__restrict__ params, unsigned long long s
     else if (p >= oW3 && p < oB3) a = 0.1f * sqrtf(3.f / kH);
     const unsigned long long h = splitmix(seed * 0x100000001B3ULL + (unsigned long long)p);
     const float u = (float)((h >> 11) * (1.0 / 9007199254740992.0));  // [0, 1)
-    params[p] = p == oB3 ? 1.f : a * (2.f * u - 1.f);
+    params[p] = p == oB3 ? kOutBias : a * (2.f * u - 1.f);
 }
 
 // ---------------------------------------------------------------------------
@@ -165,7 +179,7 @@ mlp_forward_rows_kernel(const float *__restrict__ params, const float *__restric
 
 // ---------------------------------------------------------------------------
 // Fused forward + backward over one 128-row tile of a batch.  Loss: mean
-// over the batch of w (o - y)^2 (row = f0..f5, y, w).  Row b of the batch is row b of `rows`
+// over the batch of w (o - y)^2 with o = sigmoid(z) (row = f0..f5, y, w).  Row b of the batch is row b of `rows`
 // (sample = 0) or a seeded hash of (seed, step, b) modulo nrows (sample = 1).
 // partials[tile][p] = d loss / d param_p restricted to the tile, and
 // partials[tile][kParams] = the tile's sum of weighted squared errors.
@@ -225,8 +239,10 @@ mlp_fwd_bwd_kernel(const float *__restrict__ params, const float *__restrict__ r
         h2[j] = fmaxf(s, 0.f);
         o = fmaf(P[oW3 + j], h2[j], o);
     }
-    const float err = valid ? o - y : 0.f;
-    const float g = valid ? 2.f * wgt * err / (float)batch : 0.f;
+    const float sg = weight_of(o);
+    const float err = valid ? sg - y : 0.f;
+    // d loss / d z through o = sigmoid(z)
+    const float g = valid ? 2.f * wgt * err * sg * (1.f - sg) / (float)batch : 0.f;
     dO[t] = g;
     sq[t] = wgt * err * err;
 #pragma unroll
@@ -368,7 +384,7 @@ mlp_correct_kernel(const float *__restrict__ params, const double *__restrict__ 
     const double u = U[idx];
     row_features(T[idx], tnorm[c], u, rnorm[j], X[(size_t)i + (size_t)j * n], d[i] - theta[j],
                  sigma[i], clip, hnorm, n, f);
-    const float o = fminf(fmaxf(forward_row(P, f), kWeightLo), kWeightHi);
+    const float o = forward_row(P, f);
     T[idx] = fma((double)o, u, T[idx]);
 }
 
@@ -429,6 +445,7 @@ __global__ void collect_rows_kernel(const double *__restrict__ E, const double *
                                     double hnorm, const double *__restrict__ sigma,
                                     const double *__restrict__ tnorm,
                                     const double *__restrict__ rnorm, const double *__restrict__ T,
+                                    const double *__restrict__ Tp, const double *__restrict__ Up,
                                     float *__restrict__ out)
 {
     const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -442,14 +459,17 @@ __global__ void collect_rows_kernel(const double *__restrict__ E, const double *
     const double x = X[(size_t)i + (size_t)j * n];
     const double u = U[idx];
     row_features(T[idx], tn, u, rnorm[j], x, d[i] - theta[j], sigma[i], clip, hnorm, n, f);
-    // the per-row weight of u that reproduces the scaled exact error; rows
-    // where u vanishes carry (almost) no weight
-    const double y = fabs(u) > 0.0 ? (E[idx] / alpha[c] - T[idx]) / u : 1.0;
+    // the per-row weight of the projected u that reproduces the scaled exact
+    // error with the projected t1; rows where it vanishes carry (almost) no
+    // weight
+    const double up = Up[idx];
+    const double y = fabs(up) > 0.0 ? (E[idx] / alpha[c] - Tp[idx]) / up : 1.0;
+    const float g = tn > 0.0 ? (float)(up * sqrt((double)n) / tn) : 0.f;
     float *o = out + (size_t)(slot[c] + i) * kRow;
 #pragma unroll
     for (int q = 0; q < kIn; ++q) o[q] = f[q];
     o[kIn] = clampf((float)y, 5.f);
-    o[kIn + 1] = f[1] * f[1];
+    o[kIn + 1] = g * g;
 }
 
 // Row coupling s_i = ||H[i, j != i]||_2 of a CSR matrix (one warp per row).
@@ -575,7 +595,7 @@ struct MlpCollector final : LearnedCorrection {
     long long capacity = 0;
     long long count = 0;
     BlockOps ops;
-    DeviceBuffer<double> tn, Xs, O, dots, sgn_d, alpha_d, E, G, U, B;
+    DeviceBuffer<double> tn, Xs, O, dots, sgn_d, alpha_d, E, G, U, B, Tp, Up;
     DeviceBuffer<int> lidx_d;
     DeviceBuffer<long long> slot_d;
     void bind(const double *row_coupling, double h) override
@@ -605,6 +625,8 @@ struct MlpCollector final : LearnedCorrection {
             IPTGB_CHECK(Xs.alloc((size_t)n * c, s));
             IPTGB_CHECK(E.alloc((size_t)n * c, s));
             IPTGB_CHECK(B.alloc((size_t)n * c, s));
+            IPTGB_CHECK(Tp.alloc((size_t)n * c, s));
+            IPTGB_CHECK(Up.alloc((size_t)n * c, s));
         }
         IPTGB_CHECK(plain_and_second_order(ops, a, T, U, tn.ptr));
         // overlaps of the current Ritz vectors with the converged ones
@@ -640,6 +662,15 @@ struct MlpCollector final : LearnedCorrection {
                                                                       (size_t)n * c);
         IPTGB_LAUNCH();
         IPTGB_CHECK(project_out(ops, a, B.ptr, G));
+        // the projected t1 and u of the per-row targets
+        IPTGB_CUDA(cudaMemcpyAsync(Tp.ptr, T, (size_t)n * c * sizeof(double),
+                                   cudaMemcpyDeviceToDevice, s));
+        IPTGB_CUDA(cudaMemcpyAsync(Up.ptr, U.ptr, (size_t)n * c * sizeof(double),
+                                   cudaMemcpyDeviceToDevice, s));
+        for (int pass = 0; pass < 2; ++pass) {
+            IPTGB_CHECK(project_out(ops, a, Tp.ptr, G));
+            IPTGB_CHECK(project_out(ops, a, Up.ptr, G));
+        }
         mlp::collect_dots_kernel<<<c, 256, 0, s>>>(E.ptr, B.ptr, n, dots.ptr);
         IPTGB_LAUNCH();
         std::vector<double> hd(3 * (size_t)c);
@@ -664,7 +695,7 @@ struct MlpCollector final : LearnedCorrection {
                                    cudaMemcpyHostToDevice, s));
         mlp::collect_rows_kernel<<<blocks_for((size_t)n * c), kThreads, 0, s>>>(
             E.ptr, alpha_d.ptr, slot_d.ptr, U.ptr, a.X, a.d, a.theta, a.sel, c, n, a.clip, hnorm,
-            sigma, tn.ptr, a.rnorm, T, out);
+            sigma, tn.ptr, a.rnorm, T, Tp.ptr, Up.ptr, out);
         IPTGB_LAUNCH();
         if (params != nullptr) {
             mlp::mlp_correct_kernel<<<blocks_for((size_t)n * c), 256, 0, s>>>(

@@ -67,21 +67,41 @@ def train(torch, rows, count, steps=3000, batch=4096, lr=1e-3, seed=11, init_see
 def correction_losses(torch, params, rows, count):
     """Weighted correction error, on rows[:count], of the plain preconditioner
     (weight 0 on the second-order term), of the two-term Neumann correction
-    (weight 1) and of the network (weight clamped to [-1, 3] as in the
-    solver)."""
+    (weight 1) and of the network (its weight sigmoid(z), as the solver
+    applies it)."""
     R = rows[:count]
     out = torch.empty(count, dtype=torch.float32, device=rows.device)
     api.mlp_forward(params.data_ptr(), R.data_ptr(), count, ROW, out.data_ptr())
     w, y = R[:, 7], R[:, 6]
     plain = torch.mean(w * y ** 2).item()
     neumann = torch.mean(w * (1.0 - y) ** 2).item()
-    mlp = torch.mean(w * (out.clamp(-1.0, 3.0) - y) ** 2).item()
+    mlp = torch.mean(w * (out - y) ** 2).item()
     return plain, neumann, mlp
 
 
+VALIDATION_SPECS = ((8, 4, 4, 5), (8, 4, 4, 6))
+
+
+def davidson_steps(torch, csr, params, k=16):
+    """Davidson steps of the learned solve of one instance (the library's
+    FP64-accurate Davidson strategy, residual 1e-8)."""
+    _, _, rep = solve_csr(torch, csr, min(k, csr["n"] // 4), strategy=1,
+                          davidson_maxsteps=60, preconditioner=1, mlp_params=params.data_ptr())
+    return rep["davidson_steps"] if rep["converged"] == 1 else 10 ** 6
+
+
 def build(torch, k=16, specs=TRAIN_SPECS, dagger=True, capacity=8_000_000, steps=3000,
-          device="cuda"):
-    """Train the preconditioner on the FCI-like family; returns (params, info)."""
+          device="cuda", validation=VALIDATION_SPECS):
+    """Train the preconditioner on the FCI-like family; returns (params, info).
+
+    Model selection: the trained network and the untrained one (the output
+    bias alone, o = sigmoid(4) = 0.98 on every row: the two-term correction)
+    each solve the validation instances (held out from training); the trained
+    one is returned only if it takes fewer Davidson steps in total.  The
+    per-row targets only approximate what a Davidson step needs, so a lower
+    training loss does not guarantee fewer steps: on the FCI-like family the
+    trained network matches the two-term correction at the training sizes
+    and can take many more steps than it at 10 orbitals."""
     rows = torch.empty((capacity, ROW), dtype=torch.float32, device=device)
     total = 0
     csrs = [device_csr(torch, *spec, device=device) for spec in specs]
@@ -97,4 +117,14 @@ def build(torch, k=16, specs=TRAIN_SPECS, dagger=True, capacity=8_000_000, steps
     info = {"rows_plain_trajectory": first, "rows_total": total,
             "loss_first": float(hist[:20].mean().item()),
             "loss_last": float(hist[-200:].mean().item())}
+    if validation:
+        base = torch.zeros_like(params)
+        base[-1] = 4.0  # output bias only: the two-term correction's weight
+        vcsr = [device_csr(torch, *spec, device=device) for spec in validation]
+        trained_steps = sum(davidson_steps(torch, c, params, k) for c in vcsr)
+        base_steps = sum(davidson_steps(torch, c, base, k) for c in vcsr)
+        info["validation_steps"] = {"trained": trained_steps, "two_term": base_steps}
+        info["selected"] = "trained" if trained_steps < base_steps else "two_term"
+        if trained_steps >= base_steps:
+            params = base
     return params, info

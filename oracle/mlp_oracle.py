@@ -5,7 +5,9 @@ kernels; the product never imports it).
 The network has no counterpart in the reference, which uses the diagonal
 Davidson correction (IPT_C_GPU/src/ipt_cuda.cu:2449-2465).  Parameter layout
 (FP32 vector of 4673): W1[64][6], b1[64], W2[64][64], b2[64], W3[64], b3.
-Rows are [6 features | target | weight]; loss = mean of weight * (MLP(features) - target)^2.
+Rows are [6 features | target | weight]; the network's weight of the
+second-order term is o = sigmoid(z), z its linear output;
+loss = mean of weight * (o - target)^2.
 Everything here is float64; finite differences pin the backward pass.
 """
 import numpy as np
@@ -38,8 +40,8 @@ def forward(p, F):
     h1 = np.maximum(z1, 0.0)
     z2 = h1 @ w["W2"].T + w["b2"]
     h2 = np.maximum(z2, 0.0)
-    o = h2 @ w["W3"] + w["b3"][0]
-    return o, (F, z1, h1, z2, h2)
+    z = h2 @ w["W3"] + w["b3"][0]
+    return 1.0 / (1.0 + np.exp(-z)), (F, z1, h1, z2, h2)
 
 
 def loss_grad(p, rows):
@@ -51,7 +53,8 @@ def loss_grad(p, rows):
     B = len(y)
     err = o - y
     loss = float(np.mean(wt * err ** 2))
-    dO = 2.0 * wt * err / B
+    # through o = sigmoid(z): do/dz = o (1 - o)
+    dO = 2.0 * wt * err * o * (1.0 - o) / B
     g = {}
     g["W3"] = dO @ h2
     g["b3"] = np.array([dO.sum()])

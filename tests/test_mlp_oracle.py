@@ -25,7 +25,7 @@ def test_backward_matches_finite_differences():
 def test_adam_reduces_loss():
     rng = np.random.default_rng(1)
     F = rng.standard_normal((512, 6))
-    y = 1.0 + 0.5 * np.tanh(F[:, 3])
+    y = 0.5 + 0.3 * np.tanh(F[:, 3])
     rows = np.column_stack([F, y, np.ones(512)])
     p = rng.standard_normal(M.N_PARAMS) * 0.1
     _, losses = M.adam_steps(p, [rows] * 200, lr=3e-3)
