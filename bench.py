@@ -746,7 +746,10 @@ def fci_free_section(args, torch, dev, mlp_params=None):
     dv = torch.empty(k, dtype=torch.float64, device=dev)
     runs = [("fp64", {}), ("bf16", {})]
     if mlp_params is not None:
-        runs.append(("bf16_learned", {"preconditioner": 1, "mlp_params": mlp_params.data_ptr()}))
+        # the learned correction on the FP64-accurate Davidson (its second-order
+        # term from the FP32 sigma); after the BF16 phase its first steps are
+        # rejected and the solve falls back to the plain correction
+        runs.append(("fp64_learned", {"preconditioner": 1, "mlp_params": mlp_params.data_ptr()}))
     for name, extra in runs:
         prec = "bf16" if name.startswith("bf16") else "fp64"
         t0 = time.perf_counter()

@@ -789,8 +789,14 @@ IPT_API int ipt_block_solve_fci(const IPTFciSpec *spec, int k, const IPTBlockOpt
         learned.reset(make_learned_correction(opt.mlp_params, s));
         learned->bind(coupling.ptr, hnorm);
     }
+    // the learned correction's second-order term: FP32 sigma by default
+    // (BF16 with IPT_GB300_FCI_PRECOND=16, FP64-accurate with =64)
     FciFixedPrecision precond_op;
     precond_op.op = &op;
+    {
+        const int pp = env_int("IPT_GB300_FCI_PRECOND", 32);
+        precond_op.precision = pp == 16 ? kFciBF16 : pp == 64 ? kFciF64 : kFciF32;
+    }
     BlockSolveInput in;
     in.apply = &op;
     in.precond_apply = &precond_op;
