@@ -110,8 +110,9 @@ gram_partial_df_kernel(const double *__restrict__ A, long long lda, int ma,
 {
     pdl_wait();  // programmatic dependent launch: predecessor done
     pdl_trigger();
-    __shared__ float ash[kGramRows][kGramTile + 1], asl[kGramRows][kGramTile + 1];
-    __shared__ float bsh[kGramRows][kGramTile + 1], bsl[kGramRows][kGramTile + 1];
+    // (hi, lo) pairs: one 8-byte load per entry
+    __shared__ float2 as2[kGramRows][kGramTile + 1];
+    __shared__ float2 bs2[kGramRows][kGramTile + 1];
     const int tiles_i = (ma + kGramTile - 1) / kGramTile;
     const int ti = blockIdx.y % tiles_i;
     const int tj = blockIdx.y / tiles_i;
@@ -145,18 +146,17 @@ gram_partial_df_kernel(const double *__restrict__ A, long long lda, int ma,
             const int col = e / kGramRows;
             const dfloat a = df_from_double(av[q]);
             const dfloat b = df_from_double(bv[q]);
-            ash[r][col] = a.hi;
-            asl[r][col] = a.lo;
-            bsh[r][col] = b.hi;
-            bsl[r][col] = b.lo;
+            as2[r][col] = make_float2(a.hi, a.lo);
+            bs2[r][col] = make_float2(b.hi, b.lo);
         }
         __syncthreads();
 #pragma unroll 4
         for (int r = 0; r < kGramRows; ++r) {
-            const float ah = ash[r][li], al = asl[r][li];
+            const float2 a = as2[r][li];
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
-                df_acc(S[q], sl[q], ah, al, bsh[r][lj + 8 * q], bsl[r][lj + 8 * q]);
+                const float2 b = bs2[r][lj + 8 * q];
+                df_acc(S[q], sl[q], a.x, a.y, b.x, b.y);
             }
         }
     }
@@ -285,8 +285,10 @@ __global__ void __launch_bounds__(kTallThreads)
 }
 
 // tall_gemm_kernel in double-float arithmetic (BlockOps::df_products): the
-// B tile split into (hi, lo) floats in shared memory, each A entry split once
-// per row and used for TC columns.
+// B tile split into (hi, lo) floats in shared memory, interleaved so that one
+// 16-byte load brings two columns' pairs (every thread of the CTA reads the
+// same address: a broadcast), each A entry split once per row and used for TC
+// columns.
 template <int TC>
 __global__ void __launch_bounds__(kTallThreads)
     tall_gemm_df_kernel(const double *__restrict__ A, long long lda, const double *__restrict__ B,
@@ -295,7 +297,7 @@ __global__ void __launch_bounds__(kTallThreads)
 {
     pdl_wait();  // programmatic dependent launch: predecessor done
     pdl_trigger();
-    __shared__ float bsh[kTallK][TC], bsl[kTallK][TC];
+    __shared__ float4 bs4[kTallK][TC / 2];  // (hi_j, lo_j, hi_j+1, lo_j+1)
     const int row = blockIdx.x * blockDim.x + threadIdx.x;
     const int c0 = blockIdx.y * TC;
     float S[TC], sl[TC];
@@ -306,13 +308,16 @@ __global__ void __launch_bounds__(kTallThreads)
     }
     for (int l0 = 0; l0 < m; l0 += kTallK) {
         __syncthreads();
-        for (int e = threadIdx.x; e < kTallK * TC; e += blockDim.x) {
+        for (int e = threadIdx.x; e < kTallK * TC / 2; e += blockDim.x) {
             const int l = e % kTallK;
-            const int j = e / kTallK;
-            const dfloat b = df_from_double(
-                (l0 + l < m && c0 + j < p) ? B[(size_t)(l0 + l) + (size_t)(c0 + j) * ldb] : 0.0);
-            bsh[l][j] = b.hi;
-            bsl[l][j] = b.lo;
+            const int j = 2 * (e / kTallK);
+            const bool row_ok = l0 + l < m;
+            const dfloat b0 = df_from_double(
+                (row_ok && c0 + j < p) ? B[(size_t)(l0 + l) + (size_t)(c0 + j) * ldb] : 0.0);
+            const dfloat b1 = df_from_double(
+                (row_ok && c0 + j + 1 < p) ? B[(size_t)(l0 + l) + (size_t)(c0 + j + 1) * ldb]
+                                           : 0.0);
+            bs4[l][j / 2] = make_float4(b0.hi, b0.lo, b1.hi, b1.lo);
         }
         __syncthreads();
         if (row < n) {
@@ -332,8 +337,10 @@ __global__ void __launch_bounds__(kTallThreads)
                     if (g + u < lc) {
                         const dfloat a = df_from_double(av[u]);
 #pragma unroll
-                        for (int j = 0; j < TC; ++j) {
-                            df_acc(S[j], sl[j], a.hi, a.lo, bsh[g + u][j], bsl[g + u][j]);
+                        for (int q = 0; q < TC / 2; ++q) {
+                            const float4 b = bs4[g + u][q];
+                            df_acc(S[2 * q], sl[2 * q], a.hi, a.lo, b.x, b.y);
+                            df_acc(S[2 * q + 1], sl[2 * q + 1], a.hi, a.lo, b.z, b.w);
                         }
                     }
                 }
