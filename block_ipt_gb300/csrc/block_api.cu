@@ -663,7 +663,12 @@ int dense_block_device(const double *dH_in, int n, int k, const IPTBlockOptions 
         }
         IPTGB_CHECK(Xfb.alloc((size_t)n * k, s));
         bool conv = false;
+        // Anderson mixing in the low-precision iterations of the refinement
+        // (lowp.h set_mixing; tuning knob IPT_GB300_ANDERSON=0 turns it off)
+        rin.mixing = lowp != nullptr && env_int("IPT_GB300_ANDERSON", 1) != 0;
+        if (lowp) lowp->set_mixing(rin.mixing);
         IPTGB_CHECK(refine_solve(rin, xout, d_values, report, s, &conv, Xfb.ptr));
+        if (lowp) lowp->set_mixing(false);
         done = conv;
     }
     if (!done) {

@@ -101,6 +101,7 @@ struct RefineInput {
     int max_outer = 8;
     int inner_maxiter = 64;
     double inner_tol = 1e-3;
+    bool mixing = false;                // the low-precision iterations mix (lowp.h set_mixing)
     IPTBlockOptions opt{};
 };
 

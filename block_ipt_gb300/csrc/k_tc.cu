@@ -1485,6 +1485,11 @@ __device__ __forceinline__ void sum_slots4(const float *__restrict__ P, int S, i
     }
 }
 
+// Anderson mixing (lowp.h set_mixing): Xn receives the map's value f and
+// Gout (non-null) g = f - x; Xlp may be null (the mixing kernel writes the
+// operand).  mix_part: with n % 1024 == 0 and one item per thread, CTA b
+// covers the 1024-row chunk b of one column; it stores that chunk's
+// <g, g - Gprev> and ||g - Gprev||^2 in mix_part[b].  Null: not formed here.
 template <typename LP>
 __global__ void lowp_update4_kernel(const float *__restrict__ P, int S, int n, int p,
                                     float inv_scale, const float *__restrict__ inv_row,
@@ -1492,7 +1497,9 @@ __global__ void lowp_update4_kernel(const float *__restrict__ P, int S, int n, i
                                     const float *__restrict__ X, float *__restrict__ Xn,
                                     LP *__restrict__ Xlp, int ldx, int want_norms,
                                     double2 *partials, unsigned int *counter, double *norms,
-                                    double *hist, int step, double stop_tol)
+                                    double *hist, int step, double stop_tol,
+                                    const float *__restrict__ Gprev, float *__restrict__ Gout,
+                                    double2 *__restrict__ mix_part)
 {
     pdl_wait();  // P and X come from the previous grids
     pdl_trigger();
@@ -1514,6 +1521,7 @@ __global__ void lowp_update4_kernel(const float *__restrict__ P, int S, int n, i
     }
     want_norms = want_norms || hist != nullptr;
     float dsq = 0.0f, xsq = 0.0f;
+    double ma = 0.0, mb = 0.0;
     for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < total; q += stride) {
         const int col = q / nq;
         const int row0 = (q - col * nq) << 2;
@@ -1534,12 +1542,33 @@ __global__ void lowp_update4_kernel(const float *__restrict__ P, int S, int n, i
         o.w = (y.w * ir.w - x.w * ci) * g.w;
         if (col >= row0 && col < row0 + 4) f4_at(o, col - row0) = 1.0f;  // X_jj = 1
         *reinterpret_cast<float4 *>(Xn + e) = o;
-        *reinterpret_cast<LpQuad<LP> *>(Xlp + (size_t)col * ldx + row0) =
-            LpQuad<LP>{to_lp<LP>(o.x), to_lp<LP>(o.y), to_lp<LP>(o.z), to_lp<LP>(o.w)};
+        if (Xlp != nullptr) {
+            *reinterpret_cast<LpQuad<LP> *>(Xlp + (size_t)col * ldx + row0) =
+                LpQuad<LP>{to_lp<LP>(o.x), to_lp<LP>(o.y), to_lp<LP>(o.z), to_lp<LP>(o.w)};
+        }
+        if (Gout != nullptr) {
+            *reinterpret_cast<float4 *>(Gout + e) =
+                make_float4(o.x - x.x, o.y - x.y, o.z - x.z, o.w - x.w);
+        }
         if (want_norms) {
             const float d0 = o.x - x.x, d1 = o.y - x.y, d2 = o.z - x.z, d3 = o.w - x.w;
             dsq += d0 * d0 + d1 * d1 + d2 * d2 + d3 * d3;
             xsq += x.x * x.x + x.y * x.y + x.z * x.z + x.w * x.w;
+        }
+        if (mix_part != nullptr) {
+            const float4 gp = *reinterpret_cast<const float4 *>(Gprev + e);
+            const float g0 = o.x - x.x, g1 = o.y - x.y, g2 = o.z - x.z, g3 = o.w - x.w;
+            const float e0 = g0 - gp.x, e1 = g1 - gp.y, e2 = g2 - gp.z, e3 = g3 - gp.w;
+            ma += (double)g0 * e0 + (double)g1 * e1 + (double)g2 * e2 + (double)g3 * e3;
+            mb += (double)e0 * e0 + (double)e1 * e1 + (double)e2 * e2 + (double)e3 * e3;
+        }
+    }
+    if (mix_part != nullptr) {
+        const double2 t = block_sum2(ma, mb);
+        // only CTAs with items own a chunk (the grid has no others when the
+        // host fuses the inner products, but an idle CTA must not write)
+        if (threadIdx.x == 0 && (long long)blockIdx.x * blockDim.x < (long long)total) {
+            mix_part[blockIdx.x] = t;
         }
     }
     if (hist != nullptr) {
@@ -1658,7 +1687,9 @@ __global__ void refine_update4_kernel(const float *__restrict__ P, int S, int n,
                                       const float *__restrict__ dcur, float *__restrict__ dnext,
                                       LP *__restrict__ dlp, int ldx, int want_norms,
                                       double2 *partials, unsigned int *counter, double *norms,
-                                      double *hist, int step, double stop_tol)
+                                      double *hist, int step, double stop_tol,
+                                      const float *__restrict__ Gprev, float *__restrict__ Gout,
+                                      double2 *__restrict__ mix_part)
 {
     pdl_wait();  // P and X come from the previous grids
     pdl_trigger();
@@ -1682,6 +1713,7 @@ __global__ void refine_update4_kernel(const float *__restrict__ P, int S, int n,
     }
     want_norms = want_norms || hist != nullptr;
     float dsq = 0.0f, xsq = 0.0f;
+    double ma = 0.0, mb = 0.0;
     for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < total; q += stride) {
         const int col = q / nq;
         const int row0 = (q - col * nq) << 2;
@@ -1707,20 +1739,107 @@ __global__ void refine_update4_kernel(const float *__restrict__ P, int S, int n,
         o.w = r.w + (y.w - x.w * b - cur.w * cb) * g.w;
         if (col >= row0 && col < row0 + 4) f4_at(o, col - row0) = 0.0f;  // X_jj stays 1
         *reinterpret_cast<float4 *>(dnext + e) = o;
-        const float sg = sig[col];
-        *reinterpret_cast<LpQuad<LP> *>(dlp + (size_t)col * ldx + row0) =
-            LpQuad<LP>{to_lp<LP>(o.x * sg), to_lp<LP>(o.y * sg), to_lp<LP>(o.z * sg),
-                       to_lp<LP>(o.w * sg)};
+        if (dlp != nullptr) {
+            const float sg = sig[col];
+            *reinterpret_cast<LpQuad<LP> *>(dlp + (size_t)col * ldx + row0) =
+                LpQuad<LP>{to_lp<LP>(o.x * sg), to_lp<LP>(o.y * sg), to_lp<LP>(o.z * sg),
+                           to_lp<LP>(o.w * sg)};
+        }
+        if (Gout != nullptr) {
+            *reinterpret_cast<float4 *>(Gout + e) =
+                make_float4(o.x - cur.x, o.y - cur.y, o.z - cur.z, o.w - cur.w);
+        }
         if (want_norms) {
             const float d0 = o.x - cur.x, d1 = o.y - cur.y, d2 = o.z - cur.z, d3 = o.w - cur.w;
             dsq += d0 * d0 + d1 * d1 + d2 * d2 + d3 * d3;
             xsq += cur.x * cur.x + cur.y * cur.y + cur.z * cur.z + cur.w * cur.w;
+        }
+        if (mix_part != nullptr) {
+            const float4 gp = *reinterpret_cast<const float4 *>(Gprev + e);
+            const float g0 = o.x - cur.x, g1 = o.y - cur.y, g2 = o.z - cur.z, g3 = o.w - cur.w;
+            const float e0 = g0 - gp.x, e1 = g1 - gp.y, e2 = g2 - gp.z, e3 = g3 - gp.w;
+            ma += (double)g0 * e0 + (double)g1 * e1 + (double)g2 * e2 + (double)g3 * e3;
+            mb += (double)e0 * e0 + (double)e1 * e1 + (double)e2 * e2 + (double)e3 * e3;
+        }
+    }
+    if (mix_part != nullptr) {
+        const double2 t = block_sum2(ma, mb);
+        // only CTAs with items own a chunk (the grid has no others when the
+        // host fuses the inner products, but an idle CTA must not write)
+        if (threadIdx.x == 0 && (long long)blockIdx.x * blockDim.x < (long long)total) {
+            mix_part[blockIdx.x] = t;
         }
     }
     if (hist != nullptr) {
         hist_add(hist, step, block_sum2((double)dsq, (double)xsq));
     } else if (want_norms) {
         grid_finish_norms2(block_sum2((double)dsq, (double)xsq), partials, counter, norms);
+    }
+}
+
+// Anderson mixing of depth one, column by column, of an n x p block
+// (column-major, FP32).  The update kernel of a step writes the map's value
+// f and g = f - x (x the step's iterate) into two-slot history rings; with
+// theta = <g, g - g_prev> / ||g - g_prev||^2 (0 when g does not change, and
+// on the first step), the next iterate is x+ = f - theta (f - f_prev),
+// written with its low-precision operand copy (scaled by sig[col] when
+// given).  Entries the map pins (X_jj = 1, delta_jj = 0) are pinned in f and
+// f_prev alike, so they stay pinned.  The inner products come in partials per
+// (column, chunk of kMixRows rows), from the update kernel itself or from
+// anderson_dots_kernel; every CTA of a column adds its column's partials in
+// chunk order (deterministic).
+constexpr int kMixRows = 1024;
+
+__global__ void __launch_bounds__(256)
+anderson_dots_kernel(int n, const float *__restrict__ Gcur, const float *__restrict__ Gprev,
+                     double2 *__restrict__ part)
+{
+    pdl_wait();  // Gcur comes from the update kernel
+    pdl_trigger();
+    const int col = blockIdx.x;
+    const int r0 = blockIdx.y * kMixRows;
+    const int r1 = min(n, r0 + kMixRows);
+    const size_t off = (size_t)col * n;
+    double a = 0.0, b = 0.0;
+    for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
+        const float g = Gcur[off + i];
+        const float dg = g - Gprev[off + i];
+        a = fma((double)g, (double)dg, a);
+        b = fma((double)dg, (double)dg, b);
+    }
+    const double2 ab = block_sum2(a, b);
+    if (threadIdx.x == 0) part[(size_t)col * gridDim.y + blockIdx.y] = ab;
+}
+
+template <typename LP>
+__global__ void __launch_bounds__(256)
+anderson_mix_kernel(int n, const float *__restrict__ F, const float *__restrict__ Fprev,
+                    float *__restrict__ Xout, LP *__restrict__ Xlp, int ldx,
+                    const float *__restrict__ sig, const double2 *__restrict__ part, int first)
+{
+    pdl_wait();  // F and the partials come from the previous grids
+    pdl_trigger();
+    const int col = blockIdx.x;
+    const int r0 = blockIdx.y * kMixRows;
+    const int r1 = min(n, r0 + kMixRows);
+    const size_t off = (size_t)col * n;
+    float theta = 0.0f;
+    if (!first) {
+        double a = 0.0, b = 0.0;
+        for (int r = 0; r < (int)gridDim.y; ++r) {
+            const double2 t = part[(size_t)col * gridDim.y + r];
+            a += t.x;
+            b += t.y;
+        }
+        theta = b > 0.0 && isfinite(a) && isfinite(b) ? (float)(a / b) : 0.0f;
+    }
+    const float sg = sig != nullptr ? sig[col] : 1.0f;
+    for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
+        const float f = F[off + i];
+        // the first step reads no history (the ring holds no values yet)
+        const float xn = first ? f : fmaf(-theta, f - Fprev[off + i], f);
+        Xout[off + i] = xn;
+        Xlp[(size_t)col * ldx + i] = to_lp<LP>(xn * sg);
     }
 }
 
@@ -2153,6 +2272,8 @@ struct LowpDense final : LowpDenseOperator {
             X32[0].ptr, Xlp[0].ptr, n, p, ldp);
         IPTGB_LAUNCH();
         cur = 0;
+        mix_first = true;
+        kf = 0;
         return IPT_CUDA_SUCCESS;
     }
 
@@ -2200,18 +2321,82 @@ struct LowpDense final : LowpDenseOperator {
         const int grid = update_grid();
         if (want_norms && grid > ns->capacity) return IPT_CUDA_INVALID_ARGUMENT;
         const int nxt = cur ^ 1;
-        KernelTimerScope timer(kProfLowpUpdate, s);
-        IPTGB_CHECK(launch_pdl(n % 4 == 0 ? lowp_update4_kernel<LP> : lowp_update_kernel<LP>,
-                               dim3(grid), dim3(kThreads), 0, s, (const float *)P.ptr, splits, n,
-                               p, (float)(1.0 / scale), (const float *)inv_rows.ptr,
-                               (const float *)G.ptr,
-                               (const float *)X32[cur].ptr, X32[nxt].ptr, Xlp[nxt].ptr, ldp,
-                               want_norms, ns->partials, ns->counter, ns->norms, hist, hstep,
-                               ns->stop_tol));
+        const bool mixed = mixing && hist == nullptr && n % 4 == 0;
+        const bool fused = mixed && fused_dots(grid);
+        if (mixed) IPTGB_CHECK(mix_buffers());
+        {
+            KernelTimerScope timer(kProfLowpUpdate, s);
+            if (n % 4 == 0) {
+                IPTGB_CHECK(launch_pdl(lowp_update4_kernel<LP>, dim3(grid), dim3(kThreads), 0, s,
+                                       (const float *)P.ptr, splits, n, p, (float)(1.0 / scale),
+                                       (const float *)inv_rows.ptr, (const float *)G.ptr,
+                                       (const float *)X32[cur].ptr,
+                                       mixed ? Fring[kf].ptr : X32[nxt].ptr,
+                                       mixed ? (LP *)nullptr : Xlp[nxt].ptr, ldp, want_norms,
+                                       ns->partials, ns->counter, ns->norms, hist, hstep,
+                                       ns->stop_tol, (const float *)Gring[kf ^ 1].ptr,
+                                       mixed ? Gring[kf].ptr : nullptr,
+                                       fused ? mix_part.ptr : nullptr));
+            } else {
+                IPTGB_CHECK(launch_pdl(lowp_update_kernel<LP>, dim3(grid), dim3(kThreads), 0, s,
+                                       (const float *)P.ptr, splits, n, p, (float)(1.0 / scale),
+                                       (const float *)inv_rows.ptr, (const float *)G.ptr,
+                                       (const float *)X32[cur].ptr, X32[nxt].ptr, Xlp[nxt].ptr,
+                                       ldp, want_norms, ns->partials, ns->counter, ns->norms,
+                                       hist, hstep, ns->stop_tol));
+            }
+        }
+        if (mixed) IPTGB_CHECK(mix(nxt, nullptr, fused));
         if (hm) ++ns->step;
         cur = nxt;
         return IPT_CUDA_SUCCESS;
     }
+
+    // The update kernel forms the mixing's partial inner products itself when
+    // each of its threads takes one four-row item and every CTA one 1024-row
+    // chunk of a column (n % 1024 == 0), after the first mixed step.
+    bool fused_dots(int grid) const
+    {
+        return !mix_first && n % kMixRows == 0 &&
+               (size_t)grid * kThreads >= (size_t)n * p / 4 && kThreads * 4 == kMixRows;
+    }
+
+    int mix_buffers()
+    {
+        const size_t elems = (size_t)n * p;
+        const int chunks = (n + kMixRows - 1) / kMixRows;
+        for (int r = 0; r < 2; ++r) {
+            if (Fring[r].count < elems) {
+                IPTGB_CHECK(Fring[r].alloc(elems, s));
+                IPTGB_CHECK(Gring[r].alloc(elems, s));
+            }
+        }
+        if (mix_part.count < (size_t)p * chunks) IPTGB_CHECK(mix_part.alloc((size_t)p * chunks, s));
+        return IPT_CUDA_SUCCESS;
+    }
+
+    // Anderson mixing of this step's map value (in X32[nxt]) with the last
+    // one's (lowp.h set_mixing); `fused`: the update kernel formed the
+    // partial inner products
+    int mix(int nxt, const float *sig, bool fused)
+    {
+        const int chunks = (n + kMixRows - 1) / kMixRows;
+        KernelTimerScope timer(kProfLowpUpdate, s);
+        const dim3 grid(p, chunks);
+        if (!mix_first && !fused) {
+            IPTGB_CHECK(launch_pdl(anderson_dots_kernel, grid, dim3(256), 0, s, n,
+                                   (const float *)Gring[kf].ptr, (const float *)Gring[kf ^ 1].ptr,
+                                   mix_part.ptr));
+        }
+        IPTGB_CHECK(launch_pdl(anderson_mix_kernel<LP>, grid, dim3(256), 0, s, n,
+                               (const float *)Fring[kf].ptr, (const float *)Fring[kf ^ 1].ptr,
+                               X32[nxt].ptr, Xlp[nxt].ptr, ldp, sig,
+                               (const double2 *)mix_part.ptr, mix_first ? 1 : 0));
+        mix_first = false;
+        kf ^= 1;
+        return IPT_CUDA_SUCCESS;
+    }
+    void set_mixing(bool on) override { mixing = on; }
 
     int read_error(int *host_err) override
     {
@@ -2253,6 +2438,8 @@ struct LowpDense final : LowpDenseOperator {
             small.ptr, small.ptr + p, small.ptr + 2 * p);
         IPTGB_LAUNCH();
         cur = 0;
+        mix_first = true;
+        kf = 0;
         return IPT_CUDA_SUCCESS;
     }
 
@@ -2265,16 +2452,38 @@ struct LowpDense final : LowpDenseOperator {
         const int grid = update_grid();
         if (want_norms && grid > ns->capacity) return IPT_CUDA_INVALID_ARGUMENT;
         const int nxt = cur ^ 1;
-        KernelTimerScope timer(kProfLowpUpdate, s);
-        IPTGB_CHECK(launch_pdl(n % 4 == 0 ? refine_update4_kernel<LP> : refine_update_kernel<LP>,
-                               dim3(grid), dim3(kThreads), 0, s, (const float *)P.ptr, splits, n,
-                               p, (float)(1.0 / scale), (const float *)inv_rows.ptr,
-                               (const float *)(small.ptr + p),
-                               (const float *)(small.ptr + 2 * p), (const float *)G.ptr,
-                               (const float *)R32.ptr, (const float *)Xref32.ptr,
-                               (const float *)small.ptr, (const float *)X32[cur].ptr,
-                               X32[nxt].ptr, Xlp[nxt].ptr, ldp, want_norms, ns->partials,
-                               ns->counter, ns->norms, hist, hstep, ns->stop_tol));
+        const bool mixed = mixing && hist == nullptr && n % 4 == 0;
+        const bool fused = mixed && fused_dots(grid);
+        if (mixed) IPTGB_CHECK(mix_buffers());
+        {
+            KernelTimerScope timer(kProfLowpUpdate, s);
+            if (n % 4 == 0) {
+                IPTGB_CHECK(launch_pdl(refine_update4_kernel<LP>, dim3(grid), dim3(kThreads), 0, s,
+                                       (const float *)P.ptr, splits, n, p, (float)(1.0 / scale),
+                                       (const float *)inv_rows.ptr,
+                                       (const float *)(small.ptr + p),
+                                       (const float *)(small.ptr + 2 * p), (const float *)G.ptr,
+                                       (const float *)R32.ptr, (const float *)Xref32.ptr,
+                                       (const float *)small.ptr, (const float *)X32[cur].ptr,
+                                       mixed ? Fring[kf].ptr : X32[nxt].ptr,
+                                       mixed ? (LP *)nullptr : Xlp[nxt].ptr, ldp, want_norms,
+                                       ns->partials, ns->counter, ns->norms, hist, hstep,
+                                       ns->stop_tol, (const float *)Gring[kf ^ 1].ptr,
+                                       mixed ? Gring[kf].ptr : nullptr,
+                                       fused ? mix_part.ptr : nullptr));
+            } else {
+                IPTGB_CHECK(launch_pdl(refine_update_kernel<LP>, dim3(grid), dim3(kThreads), 0, s,
+                                       (const float *)P.ptr, splits, n, p, (float)(1.0 / scale),
+                                       (const float *)inv_rows.ptr,
+                                       (const float *)(small.ptr + p),
+                                       (const float *)(small.ptr + 2 * p), (const float *)G.ptr,
+                                       (const float *)R32.ptr, (const float *)Xref32.ptr,
+                                       (const float *)small.ptr, (const float *)X32[cur].ptr,
+                                       X32[nxt].ptr, Xlp[nxt].ptr, ldp, want_norms, ns->partials,
+                                       ns->counter, ns->norms, hist, hstep, ns->stop_tol));
+            }
+        }
+        if (mixed) IPTGB_CHECK(mix(nxt, small.ptr + p, fused));
         if (hm) ++ns->step;
         cur = nxt;
         return IPT_CUDA_SUCCESS;
@@ -2289,6 +2498,10 @@ struct LowpDense final : LowpDenseOperator {
     }
 
     DeviceBuffer<float> R32, Xref32, small;  // small: c32 | sigma | 1/sigma
+    DeviceBuffer<float> Fring[2], Gring[2];  // Anderson mixing history (f, g)
+    DeviceBuffer<double2> mix_part;          // its partial inner products
+    bool mixing = false, mix_first = true;
+    int kf = 0;                              // ring slot of this step
 
     int sms = 148;
     int n = 0;

@@ -40,6 +40,13 @@ struct LowpDenseOperator {
                              const float *sigma) = 0;
     virtual int refine_step(int want_norms, NormScratch *ns) = 0;
     virtual int refine_apply(double *X) = 0;  // X += delta (FP64)
+    // Anderson mixing of depth one, column by column, after every step of
+    // the IPT iteration and of the correction solve (with host-read checks):
+    // with the map's value f = F(x) and g = f - x of this step and of the
+    // previous one, x+ = f - theta (f - f_prev), theta = <g, g - g_prev> /
+    // ||g - g_prev||^2 (Walker and Ni, SIAM J. Numer. Anal. 49 (2011)).  Off
+    // by default: the reference's IPT entry points iterate the plain map.
+    virtual void set_mixing(bool on) { (void)on; }
 };
 
 // Statistics of a dense symmetric H (device, zero-initialised before use):

@@ -142,6 +142,9 @@ __global__ void defect_finish_kernel(const double *__restrict__ P, int chunks, i
 // norms (each step ~25 us at n = 8192; a host round trip ~40 us).
 constexpr int kLookahead = 2;
 
+// Largest check interval of a correction solve with Anderson mixing.
+constexpr int kMixedCheck = 4;
+
 // Per host thread: a small page-locked buffer the check norms are copied
 // into, so that the copy is asynchronous (allocated on the thread's first
 // refinement and kept for the life of the process).
@@ -311,7 +314,10 @@ int refine_solve(const RefineInput &in, double *X_out, double *values_out, IPTBl
             if (device_stop) {
                 IPTGB_CHECK(scratch.arm_history(std::max(1, in.inner_maxiter), in.inner_tol, s));
             }
-            const int check = std::max(1, in.opt.ipt_check_every);
+            // with Anderson mixing the solve converges in about half the
+            // steps, so its checks come at least every kMixedCheck steps
+            const int check = in.mixing ? std::max(1, std::min(in.opt.ipt_check_every, kMixedCheck))
+                                        : std::max(1, in.opt.ipt_check_every);
             int ran = 0;
             // A check's norms are copied to pinned memory and the next
             // kLookahead steps are launched before the host waits for them,
@@ -323,6 +329,14 @@ int refine_solve(const RefineInput &in, double *X_out, double *values_out, IPTBl
                 const int want = ((i + 1) % check == 0) || i + 1 == in.inner_maxiter;
                 IPTGB_CHECK(in.lowp->refine_step(device_stop ? 0 : want, &scratch.ns));
                 ran = i + 1;
+                if (want && pending >= 0) {
+                    // a check still in flight (check interval <= kLookahead):
+                    // judge it before its norms are overwritten
+                    IPTGB_CUDA(cudaEventSynchronize(check_ev));
+                    pending = -1;
+                    const double rel = check_norms[0] / check_norms[1];
+                    if (!(rel > in.inner_tol)) break;  // met (or non-finite): stop
+                }
                 if (want) {
                     trace_mark("refine:correction_check", s);
                     if (device_stop) {
