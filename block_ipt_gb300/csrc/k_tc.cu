@@ -1787,7 +1787,8 @@ __global__ void refine_update4_kernel(const float *__restrict__ P, int S, int n,
 // f_prev alike, so they stay pinned.  The inner products come in partials per
 // (column, chunk of kMixRows rows), from the update kernel itself or from
 // anderson_dots_kernel; every CTA of a column adds its column's partials in
-// chunk order (deterministic).
+// chunk order (deterministic).  Mixing runs only when n % 4 == 0 (four rows
+// per thread and item).
 constexpr int kMixRows = 1024;
 
 __global__ void __launch_bounds__(256)
@@ -1801,11 +1802,13 @@ anderson_dots_kernel(int n, const float *__restrict__ Gcur, const float *__restr
     const int r1 = min(n, r0 + kMixRows);
     const size_t off = (size_t)col * n;
     double a = 0.0, b = 0.0;
-    for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
-        const float g = Gcur[off + i];
-        const float dg = g - Gprev[off + i];
-        a = fma((double)g, (double)dg, a);
-        b = fma((double)dg, (double)dg, b);
+    // four consecutive rows per item (n % 4 == 0: 16-byte aligned columns)
+    for (int i = r0 + 4 * (int)threadIdx.x; i < r1; i += 4 * (int)blockDim.x) {
+        const float4 g = *reinterpret_cast<const float4 *>(Gcur + off + i);
+        const float4 gp = *reinterpret_cast<const float4 *>(Gprev + off + i);
+        const float d0 = g.x - gp.x, d1 = g.y - gp.y, d2 = g.z - gp.z, d3 = g.w - gp.w;
+        a += (double)g.x * d0 + (double)g.y * d1 + (double)g.z * d2 + (double)g.w * d3;
+        b += (double)d0 * d0 + (double)d1 * d1 + (double)d2 * d2 + (double)d3 * d3;
     }
     const double2 ab = block_sum2(a, b);
     if (threadIdx.x == 0) part[(size_t)col * gridDim.y + blockIdx.y] = ab;
@@ -1834,12 +1837,20 @@ anderson_mix_kernel(int n, const float *__restrict__ F, const float *__restrict_
         theta = b > 0.0 && isfinite(a) && isfinite(b) ? (float)(a / b) : 0.0f;
     }
     const float sg = sig != nullptr ? sig[col] : 1.0f;
-    for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
-        const float f = F[off + i];
+    // four consecutive rows per item (n % 4 == 0: 16-byte aligned columns)
+    for (int i = r0 + 4 * (int)threadIdx.x; i < r1; i += 4 * (int)blockDim.x) {
+        const float4 f = *reinterpret_cast<const float4 *>(F + off + i);
+        float4 xn = f;
         // the first step reads no history (the ring holds no values yet)
-        const float xn = first ? f : fmaf(-theta, f - Fprev[off + i], f);
-        Xout[off + i] = xn;
-        Xlp[(size_t)col * ldx + i] = to_lp<LP>(xn * sg);
+        if (!first) {
+            const float4 fp = *reinterpret_cast<const float4 *>(Fprev + off + i);
+            xn = make_float4(fmaf(-theta, f.x - fp.x, f.x), fmaf(-theta, f.y - fp.y, f.y),
+                             fmaf(-theta, f.z - fp.z, f.z), fmaf(-theta, f.w - fp.w, f.w));
+        }
+        *reinterpret_cast<float4 *>(Xout + off + i) = xn;
+        *reinterpret_cast<LpQuad<LP> *>(Xlp + (size_t)col * ldx + i) =
+            LpQuad<LP>{to_lp<LP>(xn.x * sg), to_lp<LP>(xn.y * sg), to_lp<LP>(xn.z * sg),
+                       to_lp<LP>(xn.w * sg)};
     }
 }
 
