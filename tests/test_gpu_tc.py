@@ -146,6 +146,25 @@ def check_pairs(H, X, v, k):
     assert r.max() <= 1e-8, r.max()
 
 
+@pytest.mark.parametrize("prec", ["fp16", "bf16", "tf32"])
+@pytest.mark.parametrize("n", [2048, 3000])
+def test_anderson_mixing_saves_low_precision_steps(cuda, monkeypatch, prec, n):
+    """The refinement's Anderson-mixed low-precision iterations reach the
+    plain map's eigenpairs (LAPACK's, to 1e-10 ||H||) in fewer low-precision
+    products, with no more FP64-accurate ones.  n = 3000 is not a multiple of
+    1024: its inner products come from a kernel of their own."""
+    H, _ = workloads.dense_config1(n, seed=21)
+    runs = {}
+    for mode in ("0", "1"):
+        monkeypatch.setenv("IPT_GB300_ANDERSON", mode)
+        X, v, rep = api.block_solve_dense(H, 32, prec, ipt_maxiter=60, ipt_check_every=8)
+        assert rep["converged"] == 1
+        check_pairs(H, X, v, 32)
+        runs[mode] = rep
+    assert runs["1"]["lowp_matvecs"] < runs["0"]["lowp_matvecs"], runs
+    assert runs["1"]["fp64_matvecs"] <= runs["0"]["fp64_matvecs"], runs
+
+
 @pytest.mark.parametrize("strategy", [0, 1])
 @pytest.mark.parametrize("prec", ["fp16", "bf16", "tf32"])
 def test_block_mixed_config1_shape_small(cuda, prec, strategy):
