@@ -388,7 +388,9 @@ def fci_section(args, torch, lib, stream, flush, dev):
                                        times, rep)
     achieved = (2.0 * Hs.nnz * cols * len(times)) / (cp_ms * 1e-3) / 1e12 if cp_ms else None
     cluster = cluster_part(args, torch, lib, stream, flush, dev, Hs, drp, dci, dvv, k, e0, e1)
+    cpu = None if args.no_cpu else fci_cpu_baseline(Hs, k, hn)
     return {"workload": "FCI-like CSR, 10 orbitals 5a/5b, n=%d nnz=%d, k=%d, seed 0" % (n, Hs.nnz, k),
+            "cpu_baseline": cpu,
             "ms": statistics.mean(times), "report": {kk: rep[kk] for kk in (
                 "converged", "ipt_iterations", "davidson_steps", "restarts", "basis_cols",
                 "fp64_matvecs", "total_ms")},
@@ -397,6 +399,54 @@ def fci_section(args, torch, lib, stream, flush, dev):
                             "achieved_fp64_tflops": achieved},
             "kernel_ms": {kk: round(val[0] / len(times), 4) for kk, val in prof.items() if val[1]},
             "learned": learned_part, "block_cluster": cluster}
+
+
+def fci_cpu_baseline(Hs, k, hn):
+    """The FCI-like workload on the host: ARPACK's implicitly restarted
+    Lanczos (scipy.sparse.linalg.eigsh) for the k lowest pairs of the same
+    CSR matrix, relative tolerance 1e-10 (the reference's plain CPU IPT does
+    not converge on this family: its map diverges from the first step).
+    One complete solve, timed; the scaled residual of its pairs is checked."""
+    from scipy.sparse.linalg import eigsh
+    t0 = time.perf_counter()
+    w, X = eigsh(Hs, k=k, which="SA", tol=1e-10)
+    s = time.perf_counter() - t0
+    res = float((np.linalg.norm(Hs @ X - X * w[None, :], axis=0) / max(1.0, hn)).max())
+    return {"s": s, "max_scaled_residual": res, "threads": 1,
+            "routine": "scipy.sparse.linalg.eigsh (ARPACK Lanczos), which='SA', tol 1e-10; "
+                       "the CSR products run on one thread"}
+
+
+def batch_cpu_baseline(specs, budget_s=6.0):
+    """The batched workload on the host cores, over the leading instances of
+    the batch (its order is random in n) until budget_s is spent: the
+    reference's CPU IPT (the oracle port, all cores) from the identity block
+    until every scaled residual is <= 1e-8, and LAPACK dsyevd on each of them;
+    reported as instances per second of each."""
+    from block_ipt_gb300 import workloads
+    from oracle import oracle
+    ipt_s = lap_s = 0.0
+    done = 0
+    unconverged = 0
+    for n, k, sig, seed in specs:
+        H, _ = workloads.batch_instance(n, sig, seed)
+        t0 = time.perf_counter()
+        cnt, _ = oracle.products_to_residual(H, k, 500, 1e-8)
+        ipt_s += time.perf_counter() - t0
+        if cnt <= 0:
+            unconverged += 1
+        t0 = time.perf_counter()
+        oracle.dsyevd_lowest(H, k)
+        lap_s += time.perf_counter() - t0
+        done += 1
+        if ipt_s + lap_s >= budget_s:
+            break
+    return {"instances": done, "of": len(specs),
+            "ipt_port": {"s": ipt_s, "instances_per_s": done / ipt_s if ipt_s else None,
+                         "cores": oracle.num_threads(), "unconverged": unconverged},
+            "dsyevd": {"s": lap_s, "instances_per_s": done / lap_s if lap_s else None,
+                       "threads": blas_threads()},
+            "sample": "the first %d instances of the batch, each solved completely" % done}
 
 
 def lowp_sweep_section(torch, lib, dev, k, peak):
@@ -698,6 +748,8 @@ def batch_section(args, torch, dev):
         worst = max(worst, float(np.abs(np.sort(dv.cpu().numpy()) - w).max()
                                  / np.abs(Hn).sum(axis=1).max()))
     out["check"] = {"max_abs_dlambda_over_norm_inf_sampled": worst}
+    if not args.no_cpu:
+        out["cpu_baseline"] = batch_cpu_baseline(specs)
     del bufs
     torch.cuda.empty_cache()
     return out
