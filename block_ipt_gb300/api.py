@@ -47,6 +47,12 @@ def _take_result(res, status, what):
         "davidson_residual_after": res.davidson_residual_after,
         "adaptive_added_indices": res.adaptive_added_indices.decode(),
         "adaptive_target_block": (res.adaptive_target_block_start, res.adaptive_target_block_end),
+        "rayleigh_ritz_used_qr": res.rayleigh_ritz_used_qr,
+        "basis_orthogonality": (res.basis_orthogonality_frobenius_error,
+                                res.basis_orthogonality_max_abs_error, res.basis_has_nan_or_inf),
+        "ritz_vectors_orthogonality": (res.ritz_vectors_orthogonality_frobenius_error,
+                                       res.ritz_vectors_orthogonality_max_abs_error,
+                                       res.ritz_vectors_has_nan_or_inf),
     }
     lib.ipt_cuda_free_result(C.byref(res))
     return vec, val, info

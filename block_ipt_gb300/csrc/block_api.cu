@@ -712,7 +712,7 @@ int csr_block_device(const int *row_ptr, const int *col_ind, const double *vals,
                      int k, const IPTBlockOptions *options, const double *d_diag_sorted,
                      double *d_vectors, double *d_values, IPTBlockReport *report,
                      LearnedCorrection *hook = nullptr, const double *d_initial = nullptr,
-                     int initial_cols = 0)
+                     int initial_cols = 0, OrthStats *orth = nullptr)
 {
     IPTBlockOptions opt;
     if (options != nullptr) {
@@ -846,6 +846,7 @@ int csr_block_device(const int *row_ptr, const int *col_ind, const double *vals,
         in.k = k;
         in.hnorm = hnorm;
         in.opt = opt;
+        in.orth = orth;
         if (Xfb.ptr != nullptr) {
             in.initial = Xfb.ptr;
             in.initial_cols = k;
@@ -1158,6 +1159,18 @@ int ipt_block_sparse_host_entry(const int *col_ptr, const int *row_ind, const do
                       std::max(0, env_int("IPT_DAVIDSON_EXTRA_STEPS", 0));
     opt.davidson_maxsteps = enrich ? std::max(1, steps) : 0;
     opt.residual_tol = env_double("IPT_DAVIDSON_CONVERGED_TOL", 1e-13);
+    // The reference's Rayleigh-Ritz on the cluster basis is a Gram matrix and
+    // a generalized eigensolve by default, or Householder QR and a standard
+    // eigensolve with IPT_BLOCK_CLUSTER_QR (ipt_cuda.cu:3071, 3103-3218).
+    // Both give the Ritz pairs of the same subspace; here the basis is always
+    // orthonormalised (CholQR2) before a standard eigensolve, and the knob
+    // sets rayleigh_ritz_used_qr and which basis the orthogonality figures of
+    // IPT_RR_HOST_ORTHOGONALITY_STATS (ipt_cuda.cu:3072, 3191-3268) describe:
+    // the cluster basis as built, or its orthonormalised form.
+    const int use_qr = env_flag("IPT_BLOCK_CLUSTER_QR", 0);
+    OrthStats orth;
+    orth.raw_first_basis = !use_qr;
+    OrthStats *orth_out = env_flag("IPT_RR_HOST_ORTHOGONALITY_STATS", 0) ? &orth : nullptr;
     result->vectors = (double *)calloc((size_t)n * k, sizeof(double));
     result->values = (double *)calloc((size_t)k, sizeof(double));
     if (result->vectors == nullptr || result->values == nullptr) {
@@ -1229,7 +1242,7 @@ int ipt_block_sparse_host_entry(const int *col_ptr, const int *row_ind, const do
                 }
             }
             status = csr_block_device(rp.ptr, ci.ptr, cv.ptr, n, prep.nnz, k, &opt, dd.ptr, dX.ptr,
-                                      dv.ptr, &rep, nullptr, basis.ptr, basis_cols);
+                                      dv.ptr, &rep, nullptr, basis.ptr, basis_cols, orth_out);
         }
         basis.release();
         if (status == IPT_CUDA_SUCCESS &&
@@ -1264,7 +1277,7 @@ int ipt_block_sparse_host_entry(const int *col_ptr, const int *row_ind, const do
     result->davidson_time_sec = rep.davidson_ms * 1e-3;
     result->solve_time_sec = rep.total_ms * 1e-3;
     result->oversample = opt.oversample;
-    result->rayleigh_ritz_used_qr = 0;
+    result->rayleigh_ritz_used_qr = use_qr;
     result->davidson_attempted = opt.davidson_maxsteps > 0;
     result->davidson_accepted = rep.davidson_steps > 0;
     result->davidson_residual_after = rep.max_scaled_residual;
@@ -1281,9 +1294,11 @@ int ipt_block_sparse_host_entry(const int *col_ptr, const int *row_ind, const do
     result->cluster_residual_max = NAN;
     result->pair28_best_residual = NAN;
     result->pair29_best_residual = NAN;
-    result->basis_orthogonality_frobenius_error = NAN;
-    result->basis_orthogonality_max_abs_error = NAN;
-    result->ritz_vectors_orthogonality_frobenius_error = NAN;
-    result->ritz_vectors_orthogonality_max_abs_error = NAN;
+    result->basis_orthogonality_frobenius_error = orth.basis.frobenius;
+    result->basis_orthogonality_max_abs_error = orth.basis.max_abs;
+    result->basis_has_nan_or_inf = orth.basis.invalid;
+    result->ritz_vectors_orthogonality_frobenius_error = orth.ritz.frobenius;
+    result->ritz_vectors_orthogonality_max_abs_error = orth.ritz.max_abs;
+    result->ritz_vectors_has_nan_or_inf = orth.ritz.invalid;
     return IPT_CUDA_SUCCESS;
 }

@@ -104,6 +104,41 @@ int cholqr(BlockOps &ops, const double *B, int n, int c, double *dst, double *G,
     return IPT_CUDA_SUCCESS;
 }
 
+// Orthogonality of the n x c columns C: G = C^T C with FP64 products into
+// the c x c scratch G, then the Frobenius norm and the largest entry of
+// G - I on the host.  A non-finite entry of C makes its column's diagonal
+// entry of G non-finite (an entry of magnitude above ~1e154 does too, which
+// the reference's host scan would not flag).  Reference:
+// IPT_C_GPU/src/ipt_cuda.cu:2489-2524.
+int orth_figure(BlockOps &ops, const double *C, int n, int c, double *G, cudaStream_t s,
+                OrthFigure *out)
+{
+    const bool df = ops.df_products;
+    ops.df_products = false;
+    const int st = ops.gram(C, n, c, C, n, c, n, G, c);
+    ops.df_products = df;
+    IPTGB_CHECK(st);
+    std::vector<double> h((size_t)c * c);
+    IPTGB_CUDA(cudaMemcpyAsync(h.data(), G, h.size() * sizeof(double), cudaMemcpyDeviceToHost, s));
+    IPTGB_CUDA(cudaStreamSynchronize(s));
+    double fro = 0.0, mx = 0.0;
+    int invalid = 0;
+    for (int j = 0; j < c && !invalid; ++j) {
+        invalid = !isfinite(h[(size_t)j * c + j]);
+    }
+    for (int j = 0; j < c && !invalid; ++j) {
+        for (int i = 0; i < c; ++i) {
+            const double e = h[(size_t)j * c + i] - (i == j ? 1.0 : 0.0);
+            fro += e * e;
+            mx = std::max(mx, fabs(e));
+        }
+    }
+    out->invalid = invalid;
+    out->frobenius = invalid ? NAN : sqrt(fro);
+    out->max_abs = invalid ? NAN : mx;
+    return IPT_CUDA_SUCCESS;
+}
+
 }  // namespace
 
 int block_solve(const BlockSolveInput &in, double *X_out, double *values_out,
@@ -205,6 +240,12 @@ int block_solve(const BlockSolveInput &in, double *X_out, double *values_out,
 
     // ---- 2. CholQR2 of the IPT block ---------------------------------------
     int m = p;
+    OrthFigure basis_now, ritz_now, basis_best, ritz_best;
+    bool raw_basis_pending = false;
+    if (in.orth != nullptr && in.orth->raw_first_basis) {
+        IPTGB_CHECK(orth_figure(ops, Vt.ptr, n, m, Gm, s, &basis_now));
+        raw_basis_pending = true;
+    }
     {
         int st = cholqr(ops, Vt.ptr, n, m, V.ptr, Gm, Rinv, st_dev, &h_status, s);
         if (st == IPT_CUDA_SUCCESS) {
@@ -239,6 +280,13 @@ int block_solve(const BlockSolveInput &in, double *X_out, double *values_out,
         IPTGB_CUDA(cudaMemcpyAsync(h_theta.data(), theta, (size_t)m * sizeof(double),
                                    cudaMemcpyDeviceToHost, s));
         IPTGB_CUDA(cudaStreamSynchronize(s));
+        if (in.orth != nullptr) {
+            if (!raw_basis_pending) {
+                IPTGB_CHECK(orth_figure(ops, V.ptr, n, m, Gm, s, &basis_now));
+            }
+            raw_basis_pending = false;
+            IPTGB_CHECK(orth_figure(ops, Xr.ptr, n, k, Gm, s, &ritz_now));
+        }
         return IPT_CUDA_SUCCESS;
     };
     IPTGB_CHECK(rayleigh_ritz());
@@ -262,6 +310,8 @@ int block_solve(const BlockSolveInput &in, double *X_out, double *values_out,
                                        cudaMemcpyDeviceToDevice, s));
             IPTGB_CUDA(cudaMemcpyAsync(theta_best, theta, (size_t)k * sizeof(double),
                                        cudaMemcpyDeviceToDevice, s));
+            basis_best = basis_now;
+            ritz_best = ritz_now;
         }
         return IPT_CUDA_SUCCESS;
     };
@@ -445,6 +495,10 @@ int block_solve(const BlockSolveInput &in, double *X_out, double *values_out,
     IPTGB_CUDA(cudaEventRecord(ev.e[4], s));
     IPTGB_CUDA(cudaEventSynchronize(ev.e[4]));
     ops.release();
+    if (in.orth != nullptr) {
+        in.orth->basis = basis_best;
+        in.orth->ritz = ritz_best;
+    }
     rep->davidson_steps = steps;
     rep->restarts = restarts;
     rep->basis_cols = m;

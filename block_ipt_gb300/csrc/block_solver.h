@@ -2,6 +2,7 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <math.h>
 
 #include "../../include/ipt_block.h"
 #include "block_ops.h"
@@ -71,6 +72,26 @@ int launch_dense_row_coupling(const double *H, int n, double *sigma, cudaStream_
 
 struct LowpDenseOperator;
 
+// Orthogonality of a Rayleigh-Ritz basis and of its Ritz vectors: the
+// Frobenius norm and the largest entry of C^T C - I over the columns C, and
+// whether C held a non-finite entry (both figures NaN then), as the
+// reference's IPT_RR_HOST_ORTHOGONALITY_STATS report
+// (IPT_C_GPU/src/ipt_cuda.cu:2489-2524, 3191-3268).
+struct OrthFigure {
+    double frobenius = NAN;
+    double max_abs = NAN;
+    int invalid = 0;
+};
+struct OrthStats {
+    // the first basis figure describes the start block as given, before its
+    // orthogonalisation (the reference's Gram + generalized eigensolve on the
+    // raw cluster basis); otherwise the orthonormalised basis (its
+    // IPT_BLOCK_CLUSTER_QR path)
+    bool raw_first_basis = true;
+    OrthFigure basis;
+    OrthFigure ritz;
+};
+
 struct BlockSolveInput {
     const double *initial = nullptr;  // optional start block (n x initial_cols), skips the IPT stage
     int initial_cols = 0;
@@ -85,6 +106,9 @@ struct BlockSolveInput {
     double hnorm = 1.0;         // ||H||_inf
     IPTBlockOptions opt{};
     int lowp = 0;               // 1 if the IPT stage is low precision (report only)
+    // when set, receives the orthogonality figures of the Rayleigh-Ritz step
+    // whose pairs are returned (computed in FP64 after every such step)
+    OrthStats *orth = nullptr;
 };
 
 int block_solve(const BlockSolveInput &in, double *X_out, double *values_out,

@@ -3,6 +3,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
 #include <cstring>
 #include <limits>
 #include <numeric>
@@ -15,10 +16,16 @@ namespace iptgb {
 
 double env_double(const char *name, double default_value);
 int env_int(const char *name, int default_value);
+int env_flag(const char *name, int default_value);
 int lift_degeneracies(std::vector<int> *cp, std::vector<int> *ri, std::vector<double> *va, int n,
-                      int k, double degeneracy_threshold, std::vector<double> *diag,
-                      std::vector<int> *rot_first, std::vector<int> *rot_size,
-                      std::vector<double> *rot_values);
+                      int k, double degeneracy_threshold, int sorted_changed,
+                      std::vector<double> *diag, std::vector<int> *rot_first,
+                      std::vector<int> *rot_size, std::vector<double> *rot_values);
+
+// IPT_DEBUG_PREPARATION: the reference's diagnostic lines of the degeneracy
+// detection and lifting on standard output, "[IPT preparation] ..." with the
+// same fields (IPT_C_GPU/src/ipt_preparation.cu:69-82, 601-613, 1448-1610).
+static bool prep_debug() { return env_flag("IPT_DEBUG_PREPARATION", 0) != 0; }
 
 #define IPTGB_PREP_CHECK(expr)                  \
     do {                                        \
@@ -109,8 +116,9 @@ int prepare_csc(const int *col_ptr, const int *row_ind, const double *vals, int 
                    &ri, &va);
     }
     std::vector<double> diag;
-    IPTGB_PREP_CHECK(lift_degeneracies(&cp, &ri, &va, n, lift_k, degeneracy_threshold, &diag,
-                                       &out->rot_first, &out->rot_size, &out->rot_values));
+    IPTGB_PREP_CHECK(lift_degeneracies(&cp, &ri, &va, n, lift_k, degeneracy_threshold,
+                                       out->permuted ? 1 : 0, &diag, &out->rot_first,
+                                       &out->rot_size, &out->rot_values));
     if (!out->rot_first.empty()) {
         csc_to_csr(cp.data(), ri.data(), va.data(), n, (int)ri.size(), &out->row_ptr,
                    &out->col_ind, &out->vals);
@@ -559,12 +567,28 @@ struct HostCscView final : ClusterMatrixView {
     }
 };
 
-// Calls join(row, col) for every target col < k and every other index row
-// whose gap to it is numerically zero or small against their coupling
+// A candidate pair's figures: |d_row - d_col|, the gap counted as zero, the
+// coupling, coupling / max(gap, floor) and the largest gap at which the pair
+// still joins (ipt_preparation.cu:443-478).
+struct ClosePair {
+    double gap, floor, coupling, ratio, allowed;
+};
+// Candidates seen by a scan and the one with the largest coupling/gap ratio
+// (the diagnostics of ipt_preparation.cu:519-613).
+struct CandidateScan {
+    int candidates = 0;
+    double max_ratio = 0.0;
+    int col = -1, row = -1;
+    double gap = 0.0, coupling = 0.0;
+};
+
+// Calls join(row, col, pair) for every target col < k and every other index
+// row whose gap to it is numerically zero or small against their coupling
 // (ipt_preparation.cu:383-455 and the candidate loops of :502-611, 658-757).
 template <class Join>
 void for_each_close_pair(ClusterMatrixView &view, int n, const std::vector<double> &diag, int k,
-                         const GapOptions &o, const GapScan &g, Join join)
+                         const GapOptions &o, const GapScan &g, Join join,
+                         CandidateScan *scan = nullptr)
 {
     for (int col = 0; col < std::min(k, n); ++col) {
         const double dc = diag[(size_t)col];
@@ -584,8 +608,20 @@ void for_each_close_pair(ClusterMatrixView &view, int n, const std::vector<doubl
             }
             const double gap = std::fabs(dr - dc);
             const double fl = gap_floor(dr, dc, g.tau_num, o);
-            if (gap <= fl || (coupling > 0.0 && coupling / std::max(gap, fl) >= o.ratio_tol)) {
-                join(row, col);
+            const double ratio = coupling > 0.0 ? coupling / std::max(gap, fl) : 0.0;
+            if (scan != nullptr) {
+                ++scan->candidates;
+                if (ratio > scan->max_ratio) {
+                    scan->max_ratio = ratio;
+                    scan->col = col;
+                    scan->row = row;
+                    scan->gap = gap;
+                    scan->coupling = coupling;
+                }
+            }
+            if (gap <= fl || (coupling > 0.0 && ratio >= o.ratio_tol)) {
+                join(row, col, ClosePair{gap, fl, coupling, ratio,
+                                         std::max(fl, coupling / o.ratio_tol)});
             }
         }
     }
@@ -599,7 +635,33 @@ std::vector<std::pair<int, int>> degenerate_subspaces(ClusterMatrixView &view, i
                                                       const GapOptions &o, int *too_large)
 {
     DisjointSets sets(n);
-    for_each_close_pair(view, n, diag, k, o, g, [&](int row, int col) { sets.unite(row, col); });
+    const bool debug = prep_debug();
+    CandidateScan scan;
+    int unions = 0;
+    constexpr int kUnionLines = 64;
+    for_each_close_pair(
+        view, n, diag, k, o, g,
+        [&](int row, int col, const ClosePair &c) {
+            sets.unite(row, col);
+            if (debug && unions < kUnionLines) {
+                printf("[IPT preparation] union target=%d row=%d gap=%.17g gap_floor=%.17g "
+                       "coupling=%.17g coupling_gap_ratio=%.17g ratio_tol=%.17g "
+                       "allowed_gap=%.17g\n",
+                       col, row, c.gap, c.floor, c.coupling, c.ratio, o.ratio_tol, c.allowed);
+            }
+            ++unions;
+        },
+        debug ? &scan : nullptr);
+    if (debug) {
+        printf("[IPT preparation] target_vs_all_candidates=%d unions=%d "
+               "max_coupling_gap_ratio=%.17g at target=%d row=%d gap=%.17g coupling=%.17g\n",
+               scan.candidates, unions, scan.max_ratio, scan.col, scan.row, scan.gap,
+               scan.coupling);
+        if (unions > kUnionLines) {
+            printf("[IPT preparation] union log truncated after %d pairs\n", kUnionLines);
+        }
+        fflush(stdout);
+    }
     std::vector<int> cmin((size_t)n, n), cmax((size_t)n, -1), target((size_t)n, 0);
     for (int i = 0; i < n; ++i) {
         const int r = sets.find(i);
@@ -640,16 +702,50 @@ std::vector<std::pair<int, int>> degenerate_subspaces_host(const int *col_ptr,
     return degenerate_subspaces(view, n, diag, g, k, o, too_large);
 }
 
-// Number of (target, index) pairs still close after lifting
-// (ipt_validate_target_gaps, ipt_preparation.cu:658-757).
-int target_gap_violations(const int *col_ptr, const int *row_ind, const double *vals, int n,
+// The (target, index) pairs still close after lifting: their number, the
+// first one, and the smallest gap of a target to a close index or to its
+// neighbours in diagonal order (ipt_validate_target_gaps,
+// ipt_preparation.cu:658-757).
+struct GapCheck {
+    int bad = 0;
+    double min_abs_gap = std::numeric_limits<double>::infinity();
+    int first_col = -1, first_row = -1;
+    ClosePair first{0.0, 0.0, 0.0, 0.0, 0.0};
+};
+
+GapCheck target_gap_check(const int *col_ptr, const int *row_ind, const double *vals, int n,
                           const std::vector<double> &diag, int k, const GapOptions &o)
 {
     const GapScan g = gap_scan(col_ptr, row_ind, vals, n, diag, o);
     HostCscView view(col_ptr, row_ind, vals);
-    int bad = 0;
-    for_each_close_pair(view, n, diag, k, o, g, [&](int, int) { ++bad; });
-    return bad;
+    GapCheck check;
+    std::vector<int> rank((size_t)n);
+    for (int i = 0; i < n; ++i) rank[(size_t)g.order[(size_t)i]] = i;
+    for (int col = 0; col < std::min(k, n); ++col) {
+        const int r = rank[(size_t)col];
+        const double dc = diag[(size_t)col];
+        if (r > 0) {
+            check.min_abs_gap = std::min(check.min_abs_gap, std::fabs(dc - g.sorted_diag[(size_t)r - 1]));
+        }
+        if (r + 1 < n) {
+            check.min_abs_gap = std::min(check.min_abs_gap, std::fabs(dc - g.sorted_diag[(size_t)r + 1]));
+        }
+    }
+    for_each_close_pair(view, n, diag, k, o, g, [&](int row, int col, const ClosePair &c) {
+        check.min_abs_gap = std::min(check.min_abs_gap, c.gap);
+        if (check.bad++ == 0) {
+            check.first_col = col;
+            check.first_row = row;
+            check.first = c;
+        }
+    });
+    return check;
+}
+
+int target_gap_violations(const int *col_ptr, const int *row_ind, const double *vals, int n,
+                          const std::vector<double> &diag, int k, const GapOptions &o)
+{
+    return target_gap_check(col_ptr, row_ind, vals, n, diag, k, o).bad;
 }
 
 }  // namespace
@@ -878,16 +974,40 @@ static bool csc_is_symmetric(const std::vector<int> &cp, const std::vector<int> 
     return true;
 }
 
+// the first `count` diagonal entries with their gaps to the next one
+static void print_diagonal(const char *label, const char *gap_label,
+                           const std::vector<double> &diag, int count)
+{
+    for (int i = 0; i < count; ++i) {
+        if (i + 1 < count) {
+            printf("[IPT preparation] %s[%d]=%.17g %s=%.17g\n", label, i, diag[(size_t)i], gap_label,
+                   diag[(size_t)i + 1] - diag[(size_t)i]);
+        } else {
+            printf("[IPT preparation] %s[%d]=%.17g\n", label, i, diag[(size_t)i]);
+        }
+    }
+}
+
 int lift_degeneracies(std::vector<int> *cp, std::vector<int> *ri, std::vector<double> *va, int n,
-                      int k, double degeneracy_threshold, std::vector<double> *diag,
-                      std::vector<int> *rot_first, std::vector<int> *rot_size,
-                      std::vector<double> *rot_values)
+                      int k, double degeneracy_threshold, int sorted_changed,
+                      std::vector<double> *diag, std::vector<int> *rot_first,
+                      std::vector<int> *rot_size, std::vector<double> *rot_values)
 {
     const GapOptions o = gap_options(degeneracy_threshold);
     const int mr = env_int("IPT_MAX_LIFT_ROUNDS", 3);
     const int rounds = mr > 0 ? mr : 3;
+    const bool debug = prep_debug();
     // symmetry of the matrix as it enters the rounds; only a lift needs it
-    int symmetric = -1;
+    // (and the diagnostics, which report it first)
+    int symmetric = debug ? (csc_is_symmetric(*cp, *ri, *va, n) ? 1 : 0) : -1;
+    if (debug) {
+        printf("[IPT preparation] n=%d k=%d abs_threshold=%.17g eps_multiplier=%.17g "
+               "rel_gap_tol=%.17g coupling_gap_ratio_tol=%.17g eta=%.17g max_block_size=%d "
+               "max_lift_rounds=%d sorted_changed=%d hermitian=%d\n",
+               n, k, o.absolute_gap, o.eps_multiplier, o.rel_gap_tol, o.ratio_tol, o.eta,
+               o.max_block_size, rounds, sorted_changed, symmetric);
+        fflush(stdout);
+    }
     bool clean = false;
     for (int round = 0; round < rounds; ++round) {
         csc_diagonal_sum(cp->data(), ri->data(), va->data(), n, diag);
@@ -895,7 +1015,32 @@ int lift_degeneracies(std::vector<int> *cp, std::vector<int> *ri, std::vector<do
         const auto subspaces =
             degenerate_subspaces_host(cp->data(), ri->data(), va->data(), n, *diag, k, o,
                                       &too_large);
-        if (too_large) return IPT_CUDA_INVALID_ARGUMENT;
+        if (debug) {
+            printf("[IPT preparation] round=%d target_vs_all_blocks=%zu\n", round + 1,
+                   subspaces.size());
+            print_diagonal("diag", "gap_to_next_index", *diag, std::min(n, 10));
+            for (size_t b = 0; b < subspaces.size(); ++b) {
+                const int first = subspaces[b].first, last = subspaces[b].second;
+                double max_gap = 0.0;
+                for (int i = first; i < last; ++i) {
+                    max_gap = std::max(max_gap, std::fabs((*diag)[(size_t)i + 1] - (*diag)[(size_t)i]));
+                }
+                printf("[IPT preparation] block[%zu]=%d:%d size=%d diag_first=%.17g "
+                       "diag_last=%.17g max_adjacent_index_gap=%.17g\n",
+                       b, first, last, last - first + 1, (*diag)[(size_t)first],
+                       (*diag)[(size_t)last], max_gap);
+            }
+            fflush(stdout);
+        }
+        if (too_large) {
+            if (debug) {
+                printf("[IPT preparation] near-degenerate block exceeds max_block_size=%d; "
+                       "fallback eigensolver needed\n",
+                       o.max_block_size);
+                fflush(stdout);
+            }
+            return IPT_CUDA_INVALID_ARGUMENT;
+        }
         if (subspaces.empty()) {
             clean = target_gap_violations(cp->data(), ri->data(), va->data(), n, *diag, k, o) == 0;
             break;
@@ -904,7 +1049,13 @@ int lift_degeneracies(std::vector<int> *cp, std::vector<int> *ri, std::vector<do
         // reference then calls LAPACK dgeev when it is linked in and fails
         // the preparation otherwise, which is what happens here
         if (symmetric < 0) symmetric = csc_is_symmetric(*cp, *ri, *va, n) ? 1 : 0;
-        if (symmetric == 0) return IPT_CUDA_INVALID_ARGUMENT;
+        if (symmetric == 0) {
+            if (debug) {
+                printf("[IPT preparation] lift failed status=%d\n", 1);
+                fflush(stdout);
+            }
+            return IPT_CUDA_INVALID_ARGUMENT;
+        }
         for (const auto &sub : subspaces) {
             const int first = sub.first, m = sub.second - sub.first + 1;
             std::vector<double> block((size_t)m * (size_t)m, 0.0);
@@ -922,14 +1073,38 @@ int lift_degeneracies(std::vector<int> *cp, std::vector<int> *ri, std::vector<do
             rot_values->insert(rot_values->end(), V.begin(), V.end());
         }
         csc_diagonal_sum(cp->data(), ri->data(), va->data(), n, diag);
-        if (target_gap_violations(cp->data(), ri->data(), va->data(), n, *diag, k, o) == 0) {
+        const GapCheck check = target_gap_check(cp->data(), ri->data(), va->data(), n, *diag, k, o);
+        if (debug) {
+            printf("[IPT preparation] round=%d lift succeeded total_rotations=%zu bad_gaps=%d "
+                   "min_abs_gap=%.17g\n",
+                   round + 1, rot_first->size(), check.bad, check.min_abs_gap);
+            print_diagonal("post_lift_diag", "gap_to_next", *diag, std::min(n, std::min(k, 10)));
+            if (check.bad > 0) {
+                printf("[IPT preparation] first_bad_gap col=%d row=%d gap=%.17g allowed=%.17g "
+                       "coupling=%.17g coupling_gap_ratio=%.17g\n",
+                       check.first_col, check.first_row, check.first.gap, check.first.allowed,
+                       check.first.coupling, check.first.ratio);
+            }
+            fflush(stdout);
+        }
+        if (check.bad == 0) {
             clean = true;
             break;
         }
     }
     if (!clean) {
         csc_diagonal_sum(cp->data(), ri->data(), va->data(), n, diag);
-        if (target_gap_violations(cp->data(), ri->data(), va->data(), n, *diag, k, o) > 0) {
+        const GapCheck check = target_gap_check(cp->data(), ri->data(), va->data(), n, *diag, k, o);
+        if (check.bad > 0) {
+            if (debug) {
+                printf("[IPT preparation] unresolved target gap after %d lift rounds: bad_gaps=%d "
+                       "min_abs_gap=%.17g first_col=%d first_row=%d gap=%.17g allowed=%.17g "
+                       "coupling=%.17g coupling_gap_ratio=%.17g\n",
+                       rounds, check.bad, check.min_abs_gap, check.first_col, check.first_row,
+                       check.first.gap, check.first.allowed, check.first.coupling,
+                       check.first.ratio);
+                fflush(stdout);
+            }
             return IPT_CUDA_INVALID_ARGUMENT;
         }
     }

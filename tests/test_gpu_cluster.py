@@ -163,6 +163,50 @@ def test_block_cluster_entry_degenerate(cuda, monkeypatch, adaptive, n, seed, k)
     assert info["adaptive_added_indices"] == added
 
 
+def orthogonality(B):
+    """(Frobenius norm, largest entry) of B^T B - I, the reference's
+    host statistics (ipt_cuda.cu:2489-2524)."""
+    E = B.T @ B - np.eye(B.shape[1])
+    return np.sqrt((E * E).sum()), np.abs(E).max()
+
+
+@pytest.mark.parametrize("qr", ["0", "1"])
+def test_block_cluster_orthogonality_stats(cuda, monkeypatch, qr):
+    """IPT_RR_HOST_ORTHOGONALITY_STATS and IPT_BLOCK_CLUSTER_QR on the
+    block-cluster entry: rayleigh_ritz_used_qr follows the knob; the basis
+    figures describe the cluster basis as built (against the oracle's basis)
+    or, with QR, its orthonormalised form; the Ritz vectors' figures are at
+    rounding level; with the statistics off the figures stay NaN."""
+    monkeypatch.setenv("IPT_BLOCK_CLUSTER", "1")
+    monkeypatch.setenv("IPT_BLOCK_CLUSTER_QR", qr)
+    monkeypatch.setenv("IPT_RR_HOST_ORTHOGONALITY_STATS", "1")
+    n, k = 90, 6
+    cp, ri, va, H = oracle.cluster_test_matrix(n, 5, 0.3)
+    X, v, info = api.ipt_cuda_sparse_csc_tol(cp, ri, va, n, k, 1e-12, 200)
+    assert info["rayleigh_ritz_used_qr"] == int(qr)
+    fro, mx, bad = info["basis_orthogonality"]
+    assert bad == 0 and np.isfinite(fro) and mx <= fro
+    if qr == "0":
+        ranges, _, _, _ = oracle.cluster_ranges(cp, ri, va, n, k)
+        # symmetric: the CSC arrays are also the CSR arrays
+        B, _, _, st = oracle.cluster_basis(cp, ri, va, np.diag(H).copy(), ranges, 200, 1e-12)
+        assert st == 0
+        wf, wm = orthogonality(B)
+        assert wf > 1e-6  # the cluster basis is not orthonormal
+        assert abs(fro - wf) <= 1e-8 * wf and abs(mx - wm) <= 1e-8 * wm
+    else:
+        assert fro <= 1e-12
+    rf, rm, rbad = info["ritz_vectors_orthogonality"]
+    assert rbad == 0 and rf <= 1e-12 and rm <= rf
+    wf, _ = orthogonality(X)
+    assert abs(rf - wf) <= 1e-12
+    monkeypatch.setenv("IPT_RR_HOST_ORTHOGONALITY_STATS", "0")
+    _, v2, info = api.ipt_cuda_sparse_csc_tol(cp, ri, va, n, k, 1e-12, 200)
+    assert np.isnan(info["basis_orthogonality"][0]) and np.isnan(info["ritz_vectors_orthogonality"][1])
+    assert info["rayleigh_ritz_used_qr"] == int(qr)
+    np.testing.assert_array_equal(v2, v)
+
+
 def test_block_cluster_entry_singular_block(cuda, monkeypatch):
     """A cluster whose row system turns singular makes the entry fail with
     an invalid argument, as the oracle's (and the reference's) block solve

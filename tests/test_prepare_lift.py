@@ -184,3 +184,44 @@ def test_duplicates_zeros_and_unsorted_columns_against_reference(lib):
                 assert np.array_equal(bits(got[key]), bits(ref[key])), (seed, k, key)
             ok += 1
     assert ok >= 15
+
+
+def prep_debug_lines(capfd, monkeypatch, cp, ri, va, n, k):
+    monkeypatch.setenv("IPT_DEBUG_PREPARATION", "1")
+    capfd.readouterr()
+    try:
+        api.prepare_csc(cp, ri, va, n, k)
+    except Exception:
+        pass
+    out = capfd.readouterr().out
+    return [line for line in out.splitlines() if line.startswith("[IPT preparation]")]
+
+
+def test_debug_preparation_lines_match_reference(lib, kat, capfd, monkeypatch):
+    """IPT_DEBUG_PREPARATION: the diagnostic lines of the detection and the
+    lift rounds (unions, candidate summary, rounds and blocks, post-lift
+    diagonal, the rejection of a block wider than the limit) are the
+    reference's, character for character (tests/golden/prep_debug_kat.json,
+    recorded from the reference's own preparation)."""
+    import json
+    with open(os.path.join(os.path.dirname(GOLDEN), "prep_debug_kat.json")) as f:
+        want = json.load(f)
+    for c in [str(x) for x in kat["cases"]]:
+        cp, ri, va, n, k = case_input(kat, c)
+        assert prep_debug_lines(capfd, monkeypatch, cp, ri, va, n, k) == want[c], c
+    assert any("lift succeeded" in line for lines in want.values() for line in lines)
+    assert any("unresolved target gap" in line for line in want["reject"])
+    monkeypatch.setenv("IPT_MAX_LIFT_BLOCK_SIZE", "2")
+    cp, ri, va, n, k = case_input(kat, "lift_5")
+    got = prep_debug_lines(capfd, monkeypatch, cp, ri, va, n, k)
+    assert got == want["lift_5_max_block_2"]
+    assert "exceeds max_block_size=2" in got[-1]
+
+
+def test_debug_preparation_off_prints_nothing(lib, kat, capfd, monkeypatch):
+    cp, ri, va, n, k = case_input(kat, "lift_5")
+    for value in ("0", "no", ""):
+        monkeypatch.setenv("IPT_DEBUG_PREPARATION", value)
+        capfd.readouterr()
+        api.prepare_csc(cp, ri, va, n, k)
+        assert "[IPT preparation]" not in capfd.readouterr().out
