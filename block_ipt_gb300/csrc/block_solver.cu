@@ -325,6 +325,7 @@ int block_solve(const BlockSolveInput &in, double *X_out, double *values_out,
     double plain_log_drop = 0.0;
     int plain_drops = 0;
     const double forced_accept = env_double("IPT_GB300_MLP_ACCEPT", 0.0);
+    const int restart_keep = env_int("IPT_GB300_RESTART_KEEP", 0);
     auto required_drop = [&]() -> double {
         if (forced_accept > 0.0) return forced_accept;
         const double expect =
@@ -344,8 +345,10 @@ int block_solve(const BlockSolveInput &in, double *X_out, double *values_out,
             break;
         }
         // thick restart: keep the lowest Ritz vectors so the new block fits
+        // (tuning knob IPT_GB300_RESTART_KEEP: keep at most that many)
         if (m + nsel > maxb) {
-            const int kr = std::max(k, std::min(m, maxb - nsel));
+            const int room = restart_keep > 0 ? std::min(restart_keep, maxb - nsel) : maxb - nsel;
+            const int kr = std::max(k, std::min(m, room));
             IPTGB_CHECK(ops.tall_gemm(V.ptr, n, Zm, m, Vt.ptr, n, n, m, kr));
             IPTGB_CHECK(ops.tall_gemm(AV.ptr, n, Zm, m, AVt.ptr, n, n, m, kr));
             std::swap(V.ptr, Vt.ptr);
