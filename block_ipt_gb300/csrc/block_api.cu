@@ -847,6 +847,7 @@ int csr_block_device(const int *row_ptr, const int *col_ind, const double *vals,
         in.hnorm = hnorm;
         in.opt = opt;
         in.orth = orth;
+
         if (Xfb.ptr != nullptr) {
             in.initial = Xfb.ptr;
             in.initial_cols = k;

@@ -325,7 +325,7 @@ int block_solve(const BlockSolveInput &in, double *X_out, double *values_out,
     double plain_log_drop = 0.0;
     int plain_drops = 0;
     const double forced_accept = env_double("IPT_GB300_MLP_ACCEPT", 0.0);
-    const int restart_keep = env_int("IPT_GB300_RESTART_KEEP", 0);
+    const int restart_keep = env_int("IPT_GB300_RESTART_KEEP", in.restart_keep);
     auto required_drop = [&]() -> double {
         if (forced_accept > 0.0) return forced_accept;
         const double expect =
@@ -344,8 +344,8 @@ int block_solve(const BlockSolveInput &in, double *X_out, double *values_out,
         if (nsel == 0) {
             break;
         }
-        // thick restart: keep the lowest Ritz vectors so the new block fits
-        // (tuning knob IPT_GB300_RESTART_KEEP: keep at most that many)
+        // thick restart: keep the lowest Ritz vectors so the new block fits,
+        // at most restart_keep of them when that is set
         if (m + nsel > maxb) {
             const int room = restart_keep > 0 ? std::min(restart_keep, maxb - nsel) : maxb - nsel;
             const int kr = std::max(k, std::min(m, room));

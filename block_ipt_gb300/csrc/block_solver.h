@@ -106,6 +106,14 @@ struct BlockSolveInput {
     double hnorm = 1.0;         // ||H||_inf
     IPTBlockOptions opt{};
     int lowp = 0;               // 1 if the IPT stage is low precision (report only)
+    // Ritz vectors a thick restart keeps at most (0: as many as leave room
+    // for the next block).  A restart costs two n x m x keep products; where
+    // an operator product is cheap (sparse H) a small restart can save more
+    // than the extra steps it causes (FCI-like n = 63,504, k = 16, keep 2k:
+    // 28.5 ms and 11 steps against 33.7 ms and 10), where it is dear
+    // (matrix-free sigma) the opposite.  Every entry leaves it at 0; tuning
+    // knob IPT_GB300_RESTART_KEEP sets it.
+    int restart_keep = 0;
     // when set, receives the orthogonality figures of the Rayleigh-Ritz step
     // whose pairs are returned (computed in FP64 after every such step)
     OrthStats *orth = nullptr;
