@@ -874,15 +874,300 @@ static void sorted_symmetric_eigenvectors(const std::vector<double> &block, int 
     V->swap(sorted);
 }
 
-// H <- Q^T H Q on the block [first, first + m) (Q = V, orthogonal): column
+// ---- general (non-symmetric) blocks -------------------------------------------
+// The reference lifts a degenerate group of a non-symmetric matrix with the
+// eigenvectors LAPACK dgeev returns (all eigenvalues real: |Im| <= 1e-12
+// max(1, |Re|), else the preparation fails), sorted by eigenvalue, and the
+// inverse of that eigenvector matrix as the left factor
+// (ipt_preparation.cu:979-1030, 1032-1107, 1313-1324).  This build computes
+// the eigenvectors itself: Householder reduction to Hessenberg form, Francis
+// double-shift QR to real Schur form with the transformations accumulated,
+// real 2 x 2 blocks split by a rotation, and back substitution on the
+// triangular factor (Golub & Van Loan, Matrix Computations, 4th ed.,
+// Algorithms 7.4.2 and 7.5.1-7.5.2, section 7.6.4).  The vectors agree with
+// dgeev's to rounding and up to sign; they are not its bits.
+
+namespace {
+
+struct Dense {
+    std::vector<double> a;
+    int m;
+    Dense(int m_, double fill = 0.0) : a((size_t)m_ * (size_t)m_, fill), m(m_) {}
+    double &operator()(int i, int j) { return a[(size_t)i + (size_t)j * (size_t)m]; }
+};
+
+// Reflect rows r0..r0+len-1 of H (columns c0..m-1) and columns r0.. of H
+// (rows 0..rmax) and of Z by I - beta v v^T.
+void apply_reflector(Dense &H, Dense &Z, const double *v, int len, double beta, int r0, int c0,
+                     int rmax)
+{
+    const int m = H.m;
+    for (int j = c0; j < m; ++j) {
+        double t = 0.0;
+        for (int q = 0; q < len; ++q) t += v[q] * H(r0 + q, j);
+        t *= beta;
+        for (int q = 0; q < len; ++q) H(r0 + q, j) -= t * v[q];
+    }
+    for (int i = 0; i <= rmax; ++i) {
+        double t = 0.0;
+        for (int q = 0; q < len; ++q) t += H(i, r0 + q) * v[q];
+        t *= beta;
+        for (int q = 0; q < len; ++q) H(i, r0 + q) -= t * v[q];
+    }
+    for (int i = 0; i < m; ++i) {
+        double t = 0.0;
+        for (int q = 0; q < len; ++q) t += Z(i, r0 + q) * v[q];
+        t *= beta;
+        for (int q = 0; q < len; ++q) Z(i, r0 + q) -= t * v[q];
+    }
+}
+
+// Householder vector v (v[0] = x[0] - alpha) and beta = 2 / v^T v mapping x
+// to alpha e_1; beta = 0 when x is already a multiple of e_1.
+double householder(const double *x, int len, double *v)
+{
+    double nrm = 0.0;
+    for (int q = 0; q < len; ++q) nrm += x[q] * x[q];
+    nrm = std::sqrt(nrm);
+    for (int q = 0; q < len; ++q) v[q] = x[q];
+    if (nrm == 0.0) return 0.0;
+    const double alpha = x[0] > 0.0 ? -nrm : nrm;
+    v[0] -= alpha;
+    double vv = 0.0;
+    for (int q = 0; q < len; ++q) vv += v[q] * v[q];
+    return vv > 0.0 ? 2.0 / vv : 0.0;
+}
+
+// Rotate rows and columns p, p+1 so that the real 2 x 2 diagonal block at p
+// becomes upper triangular; false when its eigenvalues are complex beyond
+// the reference's tolerance.
+bool split_block(Dense &H, Dense &Z, int p)
+{
+    const int m = H.m;
+    const double a = H(p, p), b = H(p, p + 1), c = H(p + 1, p), d = H(p + 1, p + 1);
+    const double half = 0.5 * (a - d);
+    const double disc = half * half + b * c;
+    const double mean = 0.5 * (a + d);
+    double lam;
+    if (disc < 0.0) {
+        const double im = std::sqrt(-disc);
+        if (im > 1.0e-12 * std::max(1.0, std::fabs(mean))) return false;
+        lam = mean;  // a numerically double real eigenvalue
+    } else {
+        const double r = std::sqrt(disc);
+        lam = mean + (half >= 0.0 ? r : -r);  // the root without cancellation
+    }
+    // eigenvector of the block for lam: (b, lam - a) or (lam - d, c)
+    double u0 = b, u1 = lam - a;
+    const double w0 = lam - d, w1 = c;
+    if (w0 * w0 + w1 * w1 > u0 * u0 + u1 * u1) {
+        u0 = w0;
+        u1 = w1;
+    }
+    const double nu = std::hypot(u0, u1);
+    if (nu == 0.0) return true;  // already triangular
+    const double cs = u0 / nu, sn = u1 / nu;
+    // G = [[cs, -sn], [sn, cs]]: H <- G^T H G, Z <- Z G
+    for (int j = 0; j < m; ++j) {
+        const double x = H(p, j), y = H(p + 1, j);
+        H(p, j) = cs * x + sn * y;
+        H(p + 1, j) = -sn * x + cs * y;
+    }
+    for (int i = 0; i < m; ++i) {
+        const double x = H(i, p), y = H(i, p + 1);
+        H(i, p) = cs * x + sn * y;
+        H(i, p + 1) = -sn * x + cs * y;
+        const double zx = Z(i, p), zy = Z(i, p + 1);
+        Z(i, p) = cs * zx + sn * zy;
+        Z(i, p + 1) = -sn * zx + cs * zy;
+    }
+    H(p + 1, p) = 0.0;
+    return true;
+}
+
+// Real Schur form T = Z^T A Z (upper triangular: every eigenvalue real);
+// false on complex eigenvalues or no convergence.
+bool real_schur(Dense &H, Dense &Z)
+{
+    const int m = H.m;
+    const double eps = std::numeric_limits<double>::epsilon();
+    for (int i = 0; i < m; ++i) Z(i, i) = 1.0;
+    std::vector<double> v((size_t)std::max(m, 3));
+    // Hessenberg reduction
+    for (int k = 0; k + 2 < m; ++k) {
+        std::vector<double> x((size_t)(m - k - 1));
+        for (int q = 0; q < m - k - 1; ++q) x[(size_t)q] = H(k + 1 + q, k);
+        const double beta = householder(x.data(), m - k - 1, v.data());
+        if (beta == 0.0) continue;
+        apply_reflector(H, Z, v.data(), m - k - 1, beta, k + 1, k, m - 1);
+        for (int q = 2; q < m - k; ++q) H(k + q, k) = 0.0;
+    }
+    double anorm = 0.0;
+    for (double e : H.a) anorm = std::max(anorm, std::fabs(e));
+    int hi = m - 1, iter = 0, total = 0;
+    while (hi >= 0) {
+        int l = hi;
+        while (l > 0) {
+            double sc = std::fabs(H(l - 1, l - 1)) + std::fabs(H(l, l));
+            if (sc == 0.0) sc = anorm;
+            if (std::fabs(H(l, l - 1)) <= eps * sc) {
+                H(l, l - 1) = 0.0;
+                break;
+            }
+            --l;
+        }
+        if (l == hi) {
+            --hi;
+            iter = 0;
+            continue;
+        }
+        if (l == hi - 1) {
+            if (!split_block(H, Z, hi - 1)) return false;
+            hi -= 2;
+            iter = 0;
+            continue;
+        }
+        if (++total > 60 * m) return false;
+        ++iter;
+        // shifts: the eigenvalues of the trailing 2 x 2 block, or an
+        // exceptional pair after 10 and 20 fruitless sweeps
+        double sum = H(hi - 1, hi - 1) + H(hi, hi);
+        double prod = H(hi - 1, hi - 1) * H(hi, hi) - H(hi - 1, hi) * H(hi, hi - 1);
+        if (iter == 10 || iter == 20) {
+            const double w = std::fabs(H(hi, hi - 1)) + std::fabs(H(hi - 1, hi - 2));
+            sum = 1.5 * w + H(hi, hi);
+            prod = w * w;
+        }
+        // first column of (H - s1 I)(H - s2 I) on the active window
+        double x = H(l, l) * H(l, l) + H(l, l + 1) * H(l + 1, l) - sum * H(l, l) + prod;
+        double y = H(l + 1, l) * (H(l, l) + H(l + 1, l + 1) - sum);
+        double z = H(l + 1, l) * H(l + 2, l + 1);
+        for (int k = l; k <= hi - 2; ++k) {
+            const double xv[3] = {x, y, z};
+            const double beta = householder(xv, 3, v.data());
+            if (beta != 0.0) {
+                apply_reflector(H, Z, v.data(), 3, beta, k, std::max(l, k - 1), std::min(k + 3, hi));
+            }
+            if (k > l) {
+                H(k + 1, k - 1) = 0.0;
+                H(k + 2, k - 1) = 0.0;
+            }
+            x = H(k + 1, k);
+            y = H(k + 2, k);
+            if (k + 3 <= hi) z = H(k + 3, k);
+        }
+        const double xv[2] = {x, y};
+        const double beta = householder(xv, 2, v.data());
+        if (beta != 0.0) apply_reflector(H, Z, v.data(), 2, beta, hi - 1, hi - 2, hi);
+        H(hi, hi - 2) = 0.0;
+    }
+    return true;
+}
+
+}  // namespace
+
+// Eigenvectors of a general real m x m block, unit 2-norm columns sorted by
+// ascending eigenvalue (stable); false when an eigenvalue is complex or the
+// iteration fails, as the reference's dgeev path fails.
+static bool general_real_eigenvectors(const std::vector<double> &block, int m,
+                                      std::vector<double> *V)
+{
+    Dense T(m), Z(m);
+    T.a = block;
+    if (!real_schur(T, Z)) return false;
+    double tnorm = 0.0;
+    for (double e : T.a) tnorm = std::max(tnorm, std::fabs(e));
+    const double small = std::max(std::numeric_limits<double>::epsilon() * tnorm,
+                                  std::numeric_limits<double>::min());
+    std::vector<double> lam((size_t)m), vecs((size_t)m * (size_t)m, 0.0), y((size_t)m);
+    for (int i = 0; i < m; ++i) {
+        const double li = T(i, i);
+        lam[(size_t)i] = li;
+        std::fill(y.begin(), y.end(), 0.0);
+        y[(size_t)i] = 1.0;
+        for (int j = i - 1; j >= 0; --j) {
+            double s = 0.0;
+            for (int q = j + 1; q <= i; ++q) s += T(j, q) * y[(size_t)q];
+            double den = T(j, j) - li;
+            if (std::fabs(den) < small) den = den < 0.0 ? -small : small;
+            y[(size_t)j] = -s / den;
+            if (std::fabs(y[(size_t)j]) > 1e150) {  // keep the back substitution finite
+                const double r = 1.0 / std::fabs(y[(size_t)j]);
+                for (int q = j; q <= i; ++q) y[(size_t)q] *= r;
+            }
+        }
+        double nrm = 0.0;
+        double *x = vecs.data() + (size_t)i * (size_t)m;
+        for (int r = 0; r < m; ++r) {
+            double t = 0.0;
+            for (int q = 0; q <= i; ++q) t += Z(r, q) * y[(size_t)q];
+            x[r] = t;
+            nrm += t * t;
+        }
+        nrm = std::sqrt(nrm);
+        if (!(nrm > 0.0) || !std::isfinite(nrm)) return false;
+        for (int r = 0; r < m; ++r) x[r] /= nrm;
+    }
+    std::vector<int> idx((size_t)m);
+    std::iota(idx.begin(), idx.end(), 0);
+    std::stable_sort(idx.begin(), idx.end(), [&](int a, int b) { return lam[(size_t)a] < lam[(size_t)b]; });
+    V->resize((size_t)m * (size_t)m);
+    for (int j = 0; j < m; ++j) {
+        std::copy(vecs.begin() + (size_t)idx[(size_t)j] * (size_t)m,
+                  vecs.begin() + (size_t)(idx[(size_t)j] + 1) * (size_t)m,
+                  V->begin() + (size_t)j * (size_t)m);
+    }
+    return true;
+}
+
+// Inverse of an m x m matrix by Gauss-Jordan elimination with partial
+// pivoting; false when a pivot is at most 1e-14 in magnitude, the
+// reference's rule (ipt_preparation.cu:1032-1107).  Writes W = (A^{-1})^T.
+static bool inverse_transposed(const std::vector<double> &A, int m, std::vector<double> *W)
+{
+    // rows of [A | I] as row-major strips
+    const int w = 2 * m;
+    std::vector<double> g((size_t)m * (size_t)w, 0.0);
+    for (int r = 0; r < m; ++r) {
+        for (int c = 0; c < m; ++c) g[(size_t)r * w + c] = A[(size_t)r + (size_t)c * (size_t)m];
+        g[(size_t)r * w + m + r] = 1.0;
+    }
+    for (int c = 0; c < m; ++c) {
+        int piv = c;
+        for (int r = c + 1; r < m; ++r) {
+            if (std::fabs(g[(size_t)r * w + c]) > std::fabs(g[(size_t)piv * w + c])) piv = r;
+        }
+        if (std::fabs(g[(size_t)piv * w + c]) <= 1.0e-14) return false;
+        if (piv != c) {
+            for (int j = 0; j < w; ++j) std::swap(g[(size_t)c * w + j], g[(size_t)piv * w + j]);
+        }
+        const double inv = 1.0 / g[(size_t)c * w + c];
+        for (int j = 0; j < w; ++j) g[(size_t)c * w + j] *= inv;
+        for (int r = 0; r < m; ++r) {
+            if (r == c) continue;
+            const double f = g[(size_t)r * w + c];
+            if (f == 0.0) continue;
+            for (int j = 0; j < w; ++j) g[(size_t)r * w + j] -= f * g[(size_t)c * w + j];
+        }
+    }
+    // W(r, c) = (A^{-1})(c, r)
+    W->resize((size_t)m * (size_t)m);
+    for (int r = 0; r < m; ++r) {
+        for (int c = 0; c < m; ++c) (*W)[(size_t)r + (size_t)c * (size_t)m] = g[(size_t)c * w + m + r];
+    }
+    return true;
+}
+
+// H <- W^T H V on the block [first, first + m), with W = V for an orthogonal
+// V (the symmetric lift: Q^T H Q) or W = (V^{-1})^T for a general one: column
 // lists rebuilt entry by entry, then sorted by row, duplicates summed in
 // that order and exact zeros dropped (ipt_preparation.cu:1109-1220).
 static void rotate_block_csc(std::vector<int> *col_ptr, std::vector<int> *row_ind,
                              std::vector<double> *vals, int n, int first, int m,
-                             const std::vector<double> &V)
+                             const std::vector<double> &V, const std::vector<double> &W)
 {
     std::vector<std::vector<std::pair<int, double>>> cols((size_t)n);
-    auto Q = [&](int r, int c) { return V[(size_t)r + (size_t)c * (size_t)m]; };
+    auto Q = [&](int r, int c) { return W[(size_t)r + (size_t)c * (size_t)m]; };
     for (int c = 0; c < n; ++c) {
         const int cl = c - first;
         const bool c_in = cl >= 0 && cl < m;
@@ -895,17 +1180,17 @@ static void rotate_block_csc(std::vector<int> *col_ptr, std::vector<int> *row_in
                 cols[(size_t)c].emplace_back(r, v);
             } else if (!r_in) {
                 for (int j = 0; j < m; ++j) {
-                    const double w = v * Q(cl, j);
+                    const double w = v * V[(size_t)cl + (size_t)j * (size_t)m];
                     if (w != 0.0) cols[(size_t)(first + j)].emplace_back(r, w);
                 }
             } else if (!c_in) {
                 for (int i = 0; i < m; ++i) {
-                    const double w = Q(rl, i) * v;  // (Q^T)[i, rl]
+                    const double w = Q(rl, i) * v;  // (W^T)[i, rl]
                     if (w != 0.0) cols[(size_t)c].emplace_back(first + i, w);
                 }
             } else {
                 for (int j = 0; j < m; ++j) {
-                    const double qj = Q(cl, j);
+                    const double qj = V[(size_t)cl + (size_t)j * (size_t)m];
                     if (qj == 0.0) continue;
                     for (int i = 0; i < m; ++i) {
                         const double w = Q(rl, i) * v * qj;
@@ -997,6 +1282,7 @@ int lift_degeneracies(std::vector<int> *cp, std::vector<int> *ri, std::vector<do
     const int mr = env_int("IPT_MAX_LIFT_ROUNDS", 3);
     const int rounds = mr > 0 ? mr : 3;
     const bool debug = prep_debug();
+    const bool general = env_flag("IPT_GB300_GENERAL_LIFT", 0) != 0;
     // symmetry of the matrix as it enters the rounds; only a lift needs it
     // (and the diagnostics, which report it first)
     int symmetric = debug ? (csc_is_symmetric(*cp, *ri, *va, n) ? 1 : 0) : -1;
@@ -1045,11 +1331,12 @@ int lift_degeneracies(std::vector<int> *cp, std::vector<int> *ri, std::vector<do
             clean = target_gap_violations(cp->data(), ri->data(), va->data(), n, *diag, k, o) == 0;
             break;
         }
-        // a non-symmetric block would need a general real eigensolver; the
-        // reference then calls LAPACK dgeev when it is linked in and fails
-        // the preparation otherwise, which is what happens here
+        // a non-symmetric block needs a general real eigensolver: the
+        // reference calls LAPACK dgeev when it is linked in and fails the
+        // preparation otherwise (its own test build); this build does the
+        // latter unless IPT_GB300_GENERAL_LIFT asks for its own eigensolver
         if (symmetric < 0) symmetric = csc_is_symmetric(*cp, *ri, *va, n) ? 1 : 0;
-        if (symmetric == 0) {
+        if (symmetric == 0 && !general) {
             if (debug) {
                 printf("[IPT preparation] lift failed status=%d\n", 1);
                 fflush(stdout);
@@ -1065,9 +1352,20 @@ int lift_degeneracies(std::vector<int> *cp, std::vector<int> *ri, std::vector<do
                     if (r >= 0 && r < m) block[(size_t)r + (size_t)c * (size_t)m] += (*va)[(size_t)p];
                 }
             }
-            std::vector<double> V;
-            sorted_symmetric_eigenvectors(block, m, &V);
-            rotate_block_csc(cp, ri, va, n, first, m, V);
+            std::vector<double> V, W;
+            if (symmetric) {
+                sorted_symmetric_eigenvectors(block, m, &V);
+                rotate_block_csc(cp, ri, va, n, first, m, V, V);
+            } else {
+                if (!general_real_eigenvectors(block, m, &V) || !inverse_transposed(V, m, &W)) {
+                    if (debug) {
+                        printf("[IPT preparation] lift failed status=%d\n", 1);
+                        fflush(stdout);
+                    }
+                    return IPT_CUDA_INVALID_ARGUMENT;
+                }
+                rotate_block_csc(cp, ri, va, n, first, m, V, W);
+            }
             rot_first->push_back(first);
             rot_size->push_back(m);
             rot_values->insert(rot_values->end(), V.begin(), V.end());

@@ -185,7 +185,10 @@ int ipt_block_cluster_ranges_device(const int *d_row_ptr, const int *d_col_ind,
  * IPT_CUDA_INVALID_ARGUMENT for invalid input, capacities too small, a group
  * wider than IPT_MAX_LIFT_BLOCK_SIZE, gaps still unresolved after the
  * rounds, or a group of a non-symmetric matrix (which the reference lifts only
- * when LAPACK dgeev is linked in). */
+ * when LAPACK dgeev is linked in; with IPT_GB300_GENERAL_LIFT=1 it is lifted
+ * here by a general similarity, eigenvectors from this library's real
+ * eigensolver, unless an eigenvalue is complex or the eigenvector matrix
+ * singular). */
 int ipt_block_prepare_csc(const int *col_ptr, const int *row_ind, const double *vals, int n,
                           int k, int nnz, int lift, double degeneracy_threshold, int *out_col_ptr,
                           int *out_row_ind, double *out_vals, int capacity, int *out_nnz,

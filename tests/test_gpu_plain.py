@@ -204,3 +204,30 @@ def test_sparse_lifted_degenerate_targets(cuda):
         assert oracle.max_relative_residual(H, X, v) <= 1e-8, c
         lifted += len(z[c + "_rot_first"]) > 0
     assert lifted >= 4
+
+
+def test_sparse_general_lift_nonsymmetric(cuda, monkeypatch):
+    """IPT_GB300_GENERAL_LIFT on the plain sparse path: a non-symmetric
+    matrix with a degenerate target group is lifted by a general similarity
+    (V^-1 H V on the group) and solved; the result is the oracle's IPT on
+    the prepared matrix, transformed back, and satisfies H X = X diag(v)."""
+    from scipy.sparse import csc_matrix
+    from tests.test_prepare_lift import nonsymmetric_cluster_matrix
+    monkeypatch.setenv("IPT_GB300_GENERAL_LIFT", "1")
+    lifted = 0
+    for seed, m in ((0, 2), (1, 3), (2, 5), (3, 8)):
+        n, k = 40, 6
+        cp, ri, va, H = nonsymmetric_cluster_matrix(n, m, 2, seed)
+        prep = api.prepare_csc(cp, ri, va, n, k)
+        X, v, _ = api.ipt_cuda_sparse_csc_tol(cp, ri, va, n, k, 1e-13, 200)
+        Hp = csc_matrix((prep["values"], prep["row_ind"], prep["col_ptr"]), shape=(n, n)).tocsr()
+        Hp.sort_indices()
+        Xo, vo, _, _ = oracle.ipt_csr(Hp.indptr, Hp.indices, Hp.data, prep["diag"], n, k, 200,
+                                      tol=1e-13, use_tol=True)
+        Xb = oracle.unprepare_vectors(Xo, prep["perm"], prep["rot_first"], prep["rot_size"],
+                                      prep["rot_values"])
+        assert np.abs(v - vo).max() <= 1e-10
+        assert np.abs(X - Xb).max() <= 1e-8
+        assert oracle.max_relative_residual(H, X, v) <= 1e-8
+        lifted += len(prep["rot_first"]) > 0
+    assert lifted >= 3

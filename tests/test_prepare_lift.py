@@ -225,3 +225,92 @@ def test_debug_preparation_off_prints_nothing(lib, kat, capfd, monkeypatch):
         capfd.readouterr()
         api.prepare_csc(cp, ri, va, n, k)
         assert "[IPT preparation]" not in capfd.readouterr().out
+
+
+def nonsymmetric_cluster_matrix(n, m, first, seed, spread=1e-3):
+    """A non-symmetric matrix whose diagonal is degenerate at positions
+    first..first+m-1 (shuffled), coupled there by a real-spectrum block
+    S D S^-1 (D: m distinct values within `spread`), with weak symmetric
+    couplings elsewhere."""
+    rng = np.random.default_rng(seed)
+    d = np.arange(n, dtype=float) + 0.5
+    d[first:first + m] = d[first]
+    H = np.diag(d)
+    for _ in range(3 * n):
+        i, j = rng.integers(0, n, 2)
+        if i != j and not (first <= i < first + m and first <= j < first + m):
+            v = rng.uniform(-1e-3, 1e-3)
+            H[i, j] += v
+            H[j, i] += v
+    S = rng.standard_normal((m, m)) + 3 * np.eye(m)
+    D = np.diag(np.sort(rng.uniform(-1, 1, m)) * spread)
+    H[first:first + m, first:first + m] += S @ D @ np.linalg.inv(S)
+    P = rng.permutation(n)
+    S = csc_matrix(H[np.ix_(P, P)])
+    S.sort_indices()
+    return S.indptr, S.indices, S.data, H[np.ix_(P, P)]
+
+
+def test_general_lift_of_nonsymmetric_groups(lib, monkeypatch):
+    """IPT_GB300_GENERAL_LIFT: a degenerate group of a non-symmetric matrix
+    is lifted with this build's real eigensolver, where the reference uses
+    LAPACK dgeev when linked: the block's eigenvectors agree with dgeev's
+    (scipy.linalg.eig) up to sign, the left factor is their inverse (the
+    lifted block is diagonal), the spectrum is kept, and the back-transform
+    of the prepared matrix's eigenvectors gives the input's.  Without the
+    switch the same inputs are rejected, as the reference's own build
+    without dgeev rejects them."""
+    scipy_linalg = pytest.importorskip("scipy.linalg")
+    lifted = 0
+    for seed in range(5):
+        for m in (2, 3, 5, 8):
+            n, k = 40, 6
+            cp, ri, va, H = nonsymmetric_cluster_matrix(n, m, 2, seed)
+            monkeypatch.setenv("IPT_GB300_GENERAL_LIFT", "1")
+            got = api.prepare_csc(cp, ri, va, n, k)
+            if len(got["rot_first"]) == 0:
+                continue
+            lifted += 1
+            scale = np.abs(H).sum(axis=1).max()
+            Hp = csc_matrix((got["values"], got["row_ind"], got["col_ptr"]), shape=(n, n)).toarray()
+            np.testing.assert_allclose(np.sort(np.linalg.eigvals(Hp).real),
+                                       np.sort(np.linalg.eigvals(H).real), atol=1e-11 * scale)
+            pre = api.prepare_csc(cp, ri, va, n, k, lift=False)
+            Hs = csc_matrix((pre["values"], pre["row_ind"], pre["col_ptr"]), shape=(n, n)).toarray()
+            f, b = int(got["rot_first"][0]), int(got["rot_size"][0])
+            w, Vl = scipy_linalg.eig(Hs[f:f + b, f:f + b])
+            Vl = Vl[:, np.argsort(w.real)].real
+            V = got["rot_values"][:b * b].reshape((b, b), order="F")
+            np.testing.assert_allclose(np.linalg.norm(V, axis=0), 1.0, atol=1e-13)
+            cos = np.abs((V * Vl).sum(axis=0)) / np.linalg.norm(Vl, axis=0)
+            assert cos.min() >= 1 - 1e-10, (seed, m, cos)
+            off = Hp[f:f + b, f:f + b] - np.diag(np.diag(Hp[f:f + b, f:f + b]))
+            assert np.abs(off).max() <= 1e-12 * scale
+            w, Y = np.linalg.eig(Hp)
+            X = oracle.unprepare_vectors(np.asfortranarray(Y.real), got["perm"], got["rot_first"],
+                                         got["rot_size"], got["rot_values"])
+            assert np.abs(H @ X - X * w.real).max() <= 1e-11 * scale
+            monkeypatch.setenv("IPT_GB300_GENERAL_LIFT", "0")
+            with pytest.raises(Exception):
+                api.prepare_csc(cp, ri, va, n, k)
+            if oracle.ref_available():
+                assert isinstance(oracle.ref_prepare_lifted(cp, ri, va, n, k), int)
+    assert lifted >= 15
+
+
+def test_general_lift_rejects_complex_eigenvalues(lib, monkeypatch, capfd):
+    """A degenerate group whose block has complex eigenvalues cannot be
+    lifted by a real similarity: rejected even with the general lift, with
+    the reference's diagnostic."""
+    n = 12
+    H = np.diag(np.arange(n, dtype=float))
+    H[1, 1] = H[2, 2] = 0.5
+    H[1, 2], H[2, 1] = 1e-3, -1e-3
+    S = csc_matrix(H)
+    S.sort_indices()
+    monkeypatch.setenv("IPT_GB300_GENERAL_LIFT", "1")
+    monkeypatch.setenv("IPT_DEBUG_PREPARATION", "1")
+    capfd.readouterr()
+    with pytest.raises(Exception):
+        api.prepare_csc(S.indptr, S.indices, S.data, n, 3)
+    assert "[IPT preparation] lift failed status=1" in capfd.readouterr().out
