@@ -1099,10 +1099,11 @@ int ipt_block_sparse_host_entry(const int *col_ptr, const int *row_ind, const do
     // preparation is merged already; otherwise merge the caller's arrays.
     std::vector<int> mcp, mri;
     std::vector<double> mva;
-    if (!prep.permuted) merge_csc_columns(col_ptr, row_ind, vals, n, &mcp, &mri, &mva);
-    const int *m_ptr = prep.permuted ? prep.row_ptr.data() : mcp.data();
-    const int *m_idx = prep.permuted ? prep.col_ind.data() : mri.data();
-    const double *m_val = prep.permuted ? prep.vals.data() : mva.data();
+    const bool as_given = !prep.permuted && csc_columns_merged(col_ptr, row_ind, vals, n);
+    if (!prep.permuted && !as_given) merge_csc_columns(col_ptr, row_ind, vals, n, &mcp, &mri, &mva);
+    const int *m_ptr = prep.permuted ? prep.row_ptr.data() : as_given ? col_ptr : mcp.data();
+    const int *m_idx = prep.permuted ? prep.col_ind.data() : as_given ? row_ind : mri.data();
+    const double *m_val = prep.permuted ? prep.vals.data() : as_given ? vals : mva.data();
     if (!merged_is_symmetric(m_ptr, m_idx, m_val, n)) {
         ipt_cuda_free_result(result);
         return IPT_CUDA_INVALID_ARGUMENT;

@@ -33,7 +33,8 @@ struct ClusterMatrixView {
 };
 
 // Cluster ranges of the k targets (the basis target: requested + oversample)
-// of a symmetric CSC matrix whose diagonal is ascending (prep.cpp;
+// of a symmetric CSC matrix whose diagonal is ascending and whose columns are
+// merged (sorted by row, no duplicates: merge_csc_columns) (prep.cpp;
 // ipt_preparation.cu:502-644, ipt_cuda.cu:4114-4272); the adaptive expansion
 // grows the cluster of target requested_k - 1.
 void cluster_ranges(const int *col_ptr, const int *row_ind, const double *vals, int n, int k,

@@ -7,6 +7,8 @@
 #include <cstring>
 #include <limits>
 #include <numeric>
+#include <thread>
+#include <vector>
 #include <utility>
 
 #include "../../include/ipt_cuda.h"
@@ -46,12 +48,27 @@ bool validate_csc(const int *col_ptr, const int *row_ind, int n, int nnz)
             return false;
         }
     }
-    for (int p = 0; p < nnz; ++p) {
-        if (row_ind[p] < 0 || row_ind[p] >= n) {
-            return false;
+    // row indices in range, checked in slices on host threads for large inputs
+    const int hw = std::max(1, (int)std::thread::hardware_concurrency());
+    const int parts = std::max(1, std::min({nnz >> 22, hw, 16}));
+    std::vector<char> ok((size_t)parts, 1);
+    auto check = [&](int t) {
+        const long long lo = (long long)nnz * t / parts, hi = (long long)nnz * (t + 1) / parts;
+        for (long long p = lo; p < hi; ++p) {
+            if (row_ind[p] < 0 || row_ind[p] >= n) {
+                ok[(size_t)t] = 0;
+                return;
+            }
         }
+    };
+    if (parts == 1) {
+        check(0);
+    } else {
+        std::vector<std::thread> pool;
+        for (int t = 0; t < parts; ++t) pool.emplace_back(check, t);
+        for (auto &th : pool) th.join();
     }
-    return true;
+    return std::all_of(ok.begin(), ok.end(), [](char x) { return x != 0; });
 }
 
 void csc_diagonal(const int *col_ptr, const int *row_ind, const double *vals, int n,
@@ -274,14 +291,76 @@ void unpermute_vectors(const PreparedCsr &prep, double *vectors, int k)
 // dropped: the reference's permutation step with the identity order
 // (ipt_permute_csc, ipt_preparation.cu:210-262), which its block-cluster
 // preparation always applies (ipt_cuda.cu:4568-4575).
+// Runs fn(first, last, part) over `parts` column ranges of about equal
+// nonzero counts on host threads (the scans of large matrices are
+// memory-bound passes over every nonzero); every column is visited by one
+// part, so per-column results do not depend on the split.
+template <class Fn>
+static void for_column_parts(const int *col_ptr, int n, int parts, Fn fn)
+{
+    if (parts <= 1) {
+        fn(0, n, 0);
+        return;
+    }
+    const long long nnz = col_ptr[n];
+    std::vector<int> cut((size_t)parts + 1U, n);
+    cut[0] = 0;
+    for (int t = 1; t < parts; ++t) {
+        const long long want = nnz * t / parts;
+        cut[(size_t)t] = (int)(std::lower_bound(col_ptr, col_ptr + n + 1, want) - col_ptr);
+        cut[(size_t)t] = std::max(cut[(size_t)t - 1], std::min(cut[(size_t)t], n));
+    }
+    std::vector<std::thread> pool;
+    for (int t = 0; t < parts; ++t) {
+        pool.emplace_back(fn, cut[(size_t)t], cut[(size_t)t + 1], t);
+    }
+    for (auto &th : pool) th.join();
+}
+
+// Host threads for a scan over nnz nonzeros: one per 4 M nonzeros, at most
+// the hardware threads and 16.
+static int scan_parts(long long nnz)
+{
+    const int hw = std::max(1, (int)std::thread::hardware_concurrency());
+    return (int)std::max(1LL, std::min<long long>({nnz >> 22, (long long)hw, 16LL}));
+}
+
+static bool column_merged(const int *col_ptr, const int *row_ind, const double *vals, int c)
+{
+    for (int p = col_ptr[c]; p < col_ptr[c + 1]; ++p) {
+        if (vals[p] == 0.0 || (p > col_ptr[c] && row_ind[p - 1] >= row_ind[p])) return false;
+    }
+    return true;
+}
+
+bool csc_columns_merged(const int *col_ptr, const int *row_ind, const double *vals, int n)
+{
+    const int parts = scan_parts(col_ptr[n]);
+    std::vector<char> ok((size_t)parts, 1);
+    for_column_parts(col_ptr, n, parts, [&](int c0, int c1, int t) {
+        for (int c = c0; c < c1 && ok[(size_t)t]; ++c) ok[(size_t)t] = column_merged(col_ptr, row_ind, vals, c);
+    });
+    return std::all_of(ok.begin(), ok.end(), [](char x) { return x != 0; });
+}
+
 void merge_csc_columns(const int *col_ptr, const int *row_ind, const double *vals, int n,
                        std::vector<int> *cp, std::vector<int> *ri, std::vector<double> *va)
 {
     cp->assign((size_t)n + 1U, 0);
     ri->clear();
     va->clear();
+    ri->reserve((size_t)col_ptr[n]);
+    va->reserve((size_t)col_ptr[n]);
     std::vector<std::pair<int, double>> e;
     for (int c = 0; c < n; ++c) {
+        // a column already sorted by row, without duplicates or stored
+        // zeros, is its own merged form
+        if (column_merged(col_ptr, row_ind, vals, c)) {
+            (*cp)[(size_t)c] = (int)ri->size();
+            ri->insert(ri->end(), row_ind + col_ptr[c], row_ind + col_ptr[c + 1]);
+            va->insert(va->end(), vals + col_ptr[c], vals + col_ptr[c + 1]);
+            continue;
+        }
         e.clear();
         for (int p = col_ptr[c]; p < col_ptr[c + 1]; ++p) e.emplace_back(row_ind[p], vals[p]);
         std::sort(e.begin(), e.end(), [](const std::pair<int, double> &x,
@@ -499,7 +578,10 @@ static void csc_diagonal_sum(const int *col_ptr, const int *row_ind, const doubl
                              std::vector<double> *diag)
 {
     diag->assign((size_t)n, 0.0);
-    for (int c = 0; c < n; ++c) (*diag)[(size_t)c] = csc_value_sum(col_ptr, row_ind, vals, c, c);
+    double *dg = diag->data();
+    for_column_parts(col_ptr, n, scan_parts(col_ptr[n]), [&](int c0, int c1, int) {
+        for (int c = c0; c < c1; ++c) dg[c] = csc_value_sum(col_ptr, row_ind, vals, c, c);
+    });
 }
 
 namespace {
@@ -516,17 +598,29 @@ struct GapScan {
 // strongest off-diagonal entry of each row and column (ipt_preparation.cu:353-380)
 std::vector<double> offdiag_max(const int *col_ptr, const int *row_ind, const double *vals, int n)
 {
-    std::vector<double> cs((size_t)n, 0.0), rs((size_t)n, 0.0), off((size_t)n);
-    for (int c = 0; c < n; ++c) {
-        for (int p = col_ptr[c]; p < col_ptr[c + 1]; ++p) {
-            const int r = row_ind[p];
-            if (r == c) continue;
-            const double a = std::fabs(vals[p]);
-            cs[(size_t)c] = std::max(cs[(size_t)c], a);
-            rs[(size_t)r] = std::max(rs[(size_t)r], a);
+    // column maxima per column; row maxima per part, then combined (a
+    // maximum does not depend on the order; NaN entries never win a
+    // comparison either way); parts limited so their row arrays stay small
+    int parts = scan_parts(col_ptr[n]);
+    parts = std::max(1, std::min(parts, (int)((32LL << 20) / std::max(1, n))));
+    std::vector<double> cs((size_t)n, 0.0), rs((size_t)n * (size_t)parts, 0.0), off((size_t)n);
+    for_column_parts(col_ptr, n, parts, [&](int c0, int c1, int t) {
+        double *rt = rs.data() + (size_t)t * (size_t)n;
+        for (int c = c0; c < c1; ++c) {
+            for (int p = col_ptr[c]; p < col_ptr[c + 1]; ++p) {
+                const int r = row_ind[p];
+                if (r == c) continue;
+                const double a = std::fabs(vals[p]);
+                cs[(size_t)c] = std::max(cs[(size_t)c], a);
+                rt[r] = std::max(rt[r], a);
+            }
         }
+    });
+    for (int i = 0; i < n; ++i) {
+        double m = cs[(size_t)i];
+        for (int t = 0; t < parts; ++t) m = std::max(m, rs[(size_t)t * (size_t)n + (size_t)i]);
+        off[(size_t)i] = m;
     }
-    for (int i = 0; i < n; ++i) off[(size_t)i] = std::max(cs[(size_t)i], rs[(size_t)i]);
     return off;
 }
 
@@ -553,13 +647,25 @@ GapScan gap_scan(const int *col_ptr, const int *row_ind, const double *vals, int
     return gap_scan_from(n, diag, offdiag_max(col_ptr, row_ind, vals, n), o);
 }
 
-// The view of host CSC arrays.
+// The view of host CSC arrays.  `merged`: every column sorted by row without
+// duplicates, so an entry is found by binary search; otherwise the first
+// stored entry of the row is taken, scanning the column as the reference does.
 struct HostCscView final : ClusterMatrixView {
     const int *col_ptr;
     const int *row_ind;
     const double *vals;
-    HostCscView(const int *cp, const int *ri, const double *va) : col_ptr(cp), row_ind(ri), vals(va) {}
-    double entry(int row, int col) override { return csc_entry(col_ptr, row_ind, vals, row, col); }
+    bool merged;
+    HostCscView(const int *cp, const int *ri, const double *va, bool merged_ = false)
+        : col_ptr(cp), row_ind(ri), vals(va), merged(merged_)
+    {
+    }
+    double entry(int row, int col) override
+    {
+        if (!merged) return csc_entry(col_ptr, row_ind, vals, row, col);
+        const int *lo = row_ind + col_ptr[col], *hi = row_ind + col_ptr[col + 1];
+        const int *it = std::lower_bound(lo, hi, row);
+        return it != hi && *it == row ? vals[it - row_ind] : 0.0;
+    }
     void column(int col, std::vector<std::pair<int, double>> *e) override
     {
         e->clear();
@@ -756,7 +862,7 @@ void cluster_ranges(const int *col_ptr, const int *row_ind, const double *vals, 
 {
     std::vector<double> diag;
     csc_diagonal_sum(col_ptr, row_ind, vals, n, &diag);
-    HostCscView view(col_ptr, row_ind, vals);
+    HostCscView view(col_ptr, row_ind, vals, true);
     cluster_ranges_from(view, n, diag, offdiag_max(col_ptr, row_ind, vals, n), k, requested_k,
                         degeneracy_threshold, adaptive, coupling_tau, out);
 }
@@ -1434,10 +1540,12 @@ IPT_API int ipt_block_cluster_ranges(const int *col_ptr, const int *row_ind, con
     // always does (a no-op for a prepared matrix)
     std::vector<int> mcp, mri;
     std::vector<double> mva;
-    iptgb::merge_csc_columns(col_ptr, row_ind, vals, n, &mcp, &mri, &mva);
+    const bool merged = iptgb::csc_columns_merged(col_ptr, row_ind, vals, n);
+    if (!merged) iptgb::merge_csc_columns(col_ptr, row_ind, vals, n, &mcp, &mri, &mva);
     iptgb::ClusterRanges cr;
-    iptgb::cluster_ranges(mcp.data(), mri.data(), mva.data(), n, k, requested_k,
-                          degeneracy_threshold, adaptive, coupling_tau, &cr);
+    iptgb::cluster_ranges(merged ? col_ptr : mcp.data(), merged ? row_ind : mri.data(),
+                          merged ? vals : mva.data(), n, k, requested_k, degeneracy_threshold,
+                          adaptive, coupling_tau, &cr);
     *count = (int)cr.ranges.size();
     if (limit_hit != nullptr) *limit_hit = cr.limit_hit;
     if (cr.too_large || *count > capacity || ranges == nullptr) {

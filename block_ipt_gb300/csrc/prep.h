@@ -55,6 +55,9 @@ void unpermute_vectors(const PreparedCsr &prep, double *vectors_col_major, int k
 // reference's identity permutation, ipt_preparation.cu:210-262).
 void merge_csc_columns(const int *col_ptr, const int *row_ind, const double *vals, int n,
                        std::vector<int> *cp, std::vector<int> *ri, std::vector<double> *va);
+// Whether merge_csc_columns would return the arrays unchanged (every column
+// strictly increasing in row, no stored zeros).
+bool csc_columns_merged(const int *col_ptr, const int *row_ind, const double *vals, int n);
 
 // Real-symmetry test of merged compressed arrays (sorted, no duplicates),
 // by value lookup within 1e-12 * max(1, |a|, |b|) (ipt_preparation.cu:860-883).

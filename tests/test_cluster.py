@@ -165,3 +165,35 @@ def test_ranges_with_duplicates_and_unsorted_columns_against_reference(lib, monk
                 assert got == ref[0] and lim == ref[2], (seed, k, adaptive)
                 checked += 1
     assert checked >= 40
+
+
+def test_host_ranges_large_matrix_threaded_scans(lib):
+    """A matrix of 8.8 M nonzeros, where the host entry's scans over the
+    nonzeros (validation, merged-column check, diagonal, strongest couplings)
+    run in parts on host threads: the planted degenerate pair (3, 4) forms
+    the only multi-index cluster, the other targets are singletons, the
+    same input with unsorted columns (merged first) gives the same ranges,
+    and a row index out of range near the end is rejected."""
+    from scipy.sparse import csc_matrix, diags
+    n, k = 40000, 6
+    d = np.arange(n, dtype=float)
+    d[4] = d[3]
+    rng = np.random.default_rng(7)
+    half = 110 * n
+    R = csc_matrix((np.full(half, 1e-9), (rng.integers(0, n, half), rng.integers(0, n, half))),
+                   shape=(n, n))
+    H = (R + R.T + diags(d)).tocsc()
+    H.sort_indices()
+    assert H.nnz > 8_000_000
+    ranges, _ = api.cluster_ranges(H.indptr, H.indices, H.data, n, k)
+    assert ranges == [(0, 0), (1, 1), (2, 2), (3, 4), (5, 5)]
+    ri = H.indices.copy()
+    c = n // 2
+    a, b = H.indptr[c], H.indptr[c + 1]
+    ri[a:b] = ri[a:b][::-1].copy()
+    va = H.data.copy()
+    va[a:b] = va[a:b][::-1].copy()
+    assert api.cluster_ranges(H.indptr, ri, va, n, k)[0] == ranges
+    ri[-1] = n
+    with pytest.raises(api.IPTError):
+        api.cluster_ranges(H.indptr, ri, va, n, k)
